@@ -1,0 +1,158 @@
+/*
+ * visacd_gpu.h — C ABI of the GB300 (sm_103a) visibility-edge decomposition kernels.
+ *
+ * Plain C types only: host-owned handles, raw pointers, sizes and an int status
+ * (0 = ok, otherwise a visacd_status code; visacd_last_error() returns the message
+ * of the calling thread's most recent failure). Nothing here calls exit().
+ *
+ * Threading: a visacd_ctx owns one CUDA stream and a set of grow-only device
+ * buffers. A context is not thread-safe; use one per host thread. Calls taking
+ * `device_ptrs = 0` read and write host memory and return after the result is
+ * on the host. Calls taking `device_ptrs = 1` read and write device memory and
+ * are asynchronous on the context stream unless they also return host-side
+ * counts (documented per call).
+ *
+ * Reference interfaces these entry points replace (paths inside the VisACD
+ * source tree):
+ *   classify_and_rate_planes ........ lib/cuda/plane_intersections.cu:71-133
+ *   visacd_score_planes ............. same, with FP64 scores, exact crossing
+ *                                     classification and a first-max argmax
+ *                                     (lib/src/process.cpp:123-134)
+ *   visacd_bvh_build ................ optixAccelBuild, lib/src/intersections.cpp:131-180
+ *   visacd_visibility ............... run_optix + the host scan of
+ *                                     compute_intersection_matrix,
+ *                                     lib/src/intersections.cpp:75-385 and
+ *                                     lib/ptx/ray_segments.cu:49-125
+ *   visacd_compute_intersection_matrix  compute_intersection_matrix,
+ *                                     lib/include/intersections.hpp:24
+ */
+#ifndef VISACD_GPU_H
+#define VISACD_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VISACD_ABI_VERSION 1
+
+typedef enum {
+  VISACD_OK = 0,
+  VISACD_ERR_INVALID_ARG = 1,  /* bad size, null pointer, index out of range */
+  VISACD_ERR_CUDA = 2,         /* a CUDA runtime call failed */
+  VISACD_ERR_NO_MEMORY = 3,    /* device or pinned allocation failed */
+  VISACD_ERR_CAPACITY = 4,     /* caller's output buffer is too small */
+  VISACD_ERR_DEVICE = 5        /* a kernel reported a bounded-loop overrun */
+} visacd_status;
+
+typedef struct visacd_ctx visacd_ctx;
+typedef struct visacd_bvh visacd_bvh;
+
+/* Counters of one visibility call. */
+typedef struct {
+  int64_t pairs_tested;   /* pairs whose segment was traced (mask applied) */
+  int64_t n_edges;        /* visibility edges: cage hit and no self hit */
+  int64_t self_hits;      /* pairs whose segment crosses the part itself */
+  int64_t cage_hits;      /* pairs with no self hit whose segment leaves the cage */
+  int64_t fp64_rechecks;  /* segment-triangle tests re-decided in FP64 */
+  int64_t degenerate;     /* pairs with coincident endpoints (never edges) */
+} visacd_vis_stats;
+
+/* Counters of one scoring call. */
+typedef struct {
+  int32_t quantum_exp;    /* edge lengths are summed in units of 2^quantum_exp */
+  int32_t argmax;         /* first plane with the maximum score, -1 if P == 0 */
+  int64_t band_blocks;    /* (plane, edge block) pairs re-decided in FP64 */
+  int64_t skipped_edges;  /* edges with an out-of-range index or non-finite endpoint */
+} visacd_score_stats;
+
+/* ---- errors, version ---------------------------------------------------- */
+const char* visacd_last_error(void);
+int visacd_abi_version(void);
+
+/* ---- context ------------------------------------------------------------ */
+/* cuda_stream: a cudaStream_t to run on, or NULL to create a private stream. */
+int visacd_ctx_create(int device, void* cuda_stream, visacd_ctx** out);
+int visacd_ctx_destroy(visacd_ctx* ctx);
+int visacd_ctx_synchronize(visacd_ctx* ctx);
+/* Per-kernel CUDA-event timing on the context stream (off by default). */
+int visacd_ctx_set_timing(visacd_ctx* ctx, int enable);
+int visacd_ctx_reset_times(visacd_ctx* ctx);
+/* Accumulated time and launch count per kernel name since the last reset.
+   Synchronizes the stream. names[i] stay valid for the life of the library. */
+int visacd_ctx_kernel_times(visacd_ctx* ctx, const char** names, double* total_ms,
+                            int64_t* launches, int capacity, int* n_kernels);
+/* Number of kernel launches issued on this context since creation. */
+int64_t visacd_ctx_launch_count(const visacd_ctx* ctx);
+int visacd_ctx_sm_count(const visacd_ctx* ctx);
+
+/* ---- BVH ---------------------------------------------------------------- */
+/* Linear BVH over a triangle mesh: 63-bit Morton codes of triangle centroids,
+   LSD radix sort, Karras (2012) hierarchy, bottom-up AABB fit. verts is nv x 3
+   float32, tris is nt x 3 uint32 (indices < nv, else VISACD_ERR_INVALID_ARG).
+   device_ptrs selects host or device input. The BVH keeps the vertex indices
+   of every triangle so a visibility query can skip triangles incident to the
+   segment's endpoints. Synchronizes. */
+int visacd_bvh_build(visacd_ctx* ctx, const float* verts, int32_t nv, const uint32_t* tris,
+                     int32_t nt, int device_ptrs, visacd_bvh** out);
+int visacd_bvh_destroy(visacd_bvh* bvh);
+int visacd_bvh_info(const visacd_bvh* bvh, int32_t* n_tris, int32_t* depth);
+
+/* ---- visibility --------------------------------------------------------- */
+/* For every unordered vertex pair i < j of pts (n x 3 float32) — or, when
+   is_new != NULL, every pair with at least one is_new[] != 0 endpoint — trace
+   the segment p_i -> p_j over t in [0.001 / |p_j - p_i|, 1]. The pair is a
+   visibility edge iff the segment hits cage_bvh and does not hit self_bvh,
+   where triangles of self_bvh incident to i or j are skipped (the end-vertex
+   policy). Segment-triangle tests run in FP32 with a rigorous rounding bound;
+   tests inside the bound are re-decided in FP64. Edges are kept on the device
+   in row-major (i, j) order; fetch them with visacd_visibility_edges*.
+   Returns the edge count in *n_edges. Synchronizes. */
+int visacd_visibility(visacd_ctx* ctx, const float* pts, int32_t n, const uint8_t* is_new,
+                      int device_ptrs, const visacd_bvh* self_bvh, const visacd_bvh* cage_bvh,
+                      int64_t* n_edges, visacd_vis_stats* stats);
+/* Copy the last visibility result (2 x n_edges uint32, i < j) to host memory. */
+int visacd_visibility_edges(visacd_ctx* ctx, uint32_t* edges_out, int64_t capacity_edges);
+/* Device pointer to the last visibility result (valid until the next call). */
+int visacd_visibility_edges_device(visacd_ctx* ctx, const uint32_t** d_edges, int64_t* n_edges);
+
+/* One call that builds both BVHs, runs visacd_visibility and copies the edges
+   out: the C form of compute_intersection_matrix(mesh, cage). If the edge
+   count exceeds capacity_edges, *n_edges holds the count and the call returns
+   VISACD_ERR_CAPACITY without writing edges_out. Host pointers. */
+int visacd_compute_intersection_matrix(visacd_ctx* ctx, const float* verts, int32_t nv,
+                                       const uint32_t* tris, int32_t nt, const uint8_t* is_new,
+                                       const float* cage_verts, int32_t ncv,
+                                       const uint32_t* cage_tris, int32_t nct,
+                                       uint32_t* edges_out, int64_t capacity_edges,
+                                       int64_t* n_edges, visacd_vis_stats* stats);
+
+/* ---- plane scoring ------------------------------------------------------ */
+/* score[p] = sum over edges e = (i, j) of |p_j - p_i| where the endpoints lie
+   strictly on opposite sides of plane p: side(x) = +1 if a x + b y + c z + d >
+   1e-6f, -1 if < -1e-6f, else 0 (lib/cuda/plane_intersections.cu:44-57). The
+   side test is exact with respect to FP64 evaluation of the FP32 inputs
+   (FP32 fast path, FP64 re-decision inside the rounding band). Edge lengths
+   are FP32 (IEEE ops, no contraction) quantized to 2^quantum_exp and summed in
+   integers, so scores are deterministic and independent of launch shape.
+   planes P x 4, points N x 3 float32, edges E x 2 uint32; edges with an index
+   >= N are skipped as in the reference. scores is P float64. If device_ptrs
+   is 1 the call is asynchronous unless stats != NULL. */
+int visacd_score_planes(visacd_ctx* ctx, const float* planes, int32_t P, const float* points,
+                        int32_t N, const uint32_t* edges, int64_t E, int device_ptrs,
+                        double* scores, visacd_score_stats* stats);
+
+/* Drop-in for the reference's host wrapper: same signature and meaning
+   (host pointers, synchronous, float scores), run on a process-wide default
+   context on device 0. Errors are recorded in visacd_last_error() and leave
+   scores at zero, as the reference does on a launch error. */
+void classify_and_rate_planes(const float* planes, const float* points,
+                              const unsigned int* edges, float* scores, int numPlanes,
+                              int numPoints, int numEdges);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VISACD_GPU_H */

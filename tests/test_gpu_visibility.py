@@ -1,0 +1,107 @@
+"""Visibility on the GPU (LBVH + traversal, through the C ABI) against the FP64
+oracle: identical edge sets except for pairs the oracle marks as grazing
+(within 1e-6 of a decision boundary); the grazing count is reported."""
+import numpy as np
+import pytest
+
+from visacd_gb300 import meshgen as mg
+
+pytestmark = pytest.mark.gpu
+
+
+def _compare(ctx, orc, v, t, cv, ct, is_new=None, brute=False):
+    sb = ctx.bvh(v, t)
+    cb = ctx.bvh(cv, ct)
+    e_gpu, st = ctx.visibility(v, sb, cb, is_new=is_new)
+    bits, e_orc, ost = orc.visibility(v, t, cv, ct, is_new=is_new, use_bvh=not brute)
+    n = len(v)
+    assert np.all(e_gpu[:, 0] < e_gpu[:, 1]) if len(e_gpu) else True
+    k_gpu = orc.linear_from_pairs(e_gpu, n) if len(e_gpu) else np.zeros(0, np.int64)
+    assert np.all(np.diff(k_gpu) > 0), "edges must be in row-major order"
+    gpu_bits = np.zeros(n * (n - 1) // 2, dtype=bool)
+    gpu_bits[k_gpu] = True
+    orc_edge = (bits & 1).astype(bool)
+    grazing = (bits & 2).astype(bool)
+    diff = gpu_bits != orc_edge
+    assert not np.any(diff & ~grazing), f"{int(np.sum(diff & ~grazing))} non-grazing pairs differ"
+    assert st["pairs_tested"] == ost["pairs"]
+    return e_gpu, st, ost, int(np.sum(diff))
+
+
+def test_blob_level2_bruteforce(ctx, orc):
+    v, t = mg.displaced_blob(2, seed=3)
+    cv, ct = mg.offset_cage(v, t, 0.03)
+    e, st, ost, nd = _compare(ctx, orc, v, t, cv, ct, brute=True)
+    assert len(e) > 10
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_blob_level3(ctx, orc, seed):
+    v, t = mg.displaced_blob(3, seed=seed)
+    cv, ct = mg.offset_cage(v, t, 0.03)
+    _compare(ctx, orc, v, t, cv, ct)
+
+
+def test_torus_small(ctx, orc):
+    v, t = mg.torus(nu=32, nv=16, seed=42)
+    cv, ct = mg.offset_cage(v, t, 0.03)
+    e, st, ost, nd = _compare(ctx, orc, v, t, cv, ct)
+    assert len(e) > 100
+
+
+def test_masked_pairs(ctx, orc):
+    v, t = mg.displaced_blob(3, seed=7)
+    cv, ct = mg.offset_cage(v, t, 0.03)
+    rng = np.random.default_rng(0)
+    m = (rng.random(len(v)) < 0.1).astype(np.uint8)
+    e, st, ost, nd = _compare(ctx, orc, v, t, cv, ct, is_new=m)
+    assert np.all(m[e[:, 0]] | m[e[:, 1]])
+
+
+def test_mask_all_and_none(ctx, orc):
+    v, t = mg.displaced_blob(2, seed=5)
+    cv, ct = mg.offset_cage(v, t, 0.03)
+    e_all, _, _, _ = _compare(ctx, orc, v, t, cv, ct, is_new=np.ones(len(v), np.uint8))
+    e_ref, _, _, _ = _compare(ctx, orc, v, t, cv, ct)
+    np.testing.assert_array_equal(e_all, e_ref)
+    e_none, st, _, _ = _compare(ctx, orc, v, t, cv, ct, is_new=np.zeros(len(v), np.uint8))
+    assert len(e_none) == 0 and st["pairs_tested"] == 0
+
+
+def test_tiny_inputs(ctx, orc):
+    # two points, one triangle part, tetrahedral cage
+    v = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float64)
+    t = np.array([[0, 1, 2]], np.int32)
+    cv = np.array([[-5, -5, -5], [5, -5, -5], [0, 5, -5], [0, 0, 5]], np.float64)
+    ct = np.array([[0, 2, 1], [0, 1, 3], [1, 2, 3], [2, 0, 3]], np.int32)
+    _compare(ctx, orc, v, t, cv, ct, brute=True)
+    # empty cage: nothing can hit it -> no edges
+    sb, cb = ctx.bvh(v, t), ctx.bvh(np.zeros((0, 3)), np.zeros((0, 3), np.int32))
+    e, st = ctx.visibility(v, sb, cb)
+    assert len(e) == 0
+    # single point
+    sb1 = ctx.bvh(v[:1], np.zeros((0, 3), np.int32))
+    e, st = ctx.visibility(v[:1], sb1, cb)
+    assert len(e) == 0
+
+
+def test_duplicate_vertices_are_not_edges(ctx, orc):
+    v, t = mg.displaced_blob(2, seed=9)
+    v = np.concatenate([v, v[:5]])  # 5 coincident copies (unreferenced)
+    cv, ct = mg.offset_cage(*mg.displaced_blob(2, seed=9), 0.03)
+    e, st, ost, nd = _compare(ctx, orc, v, t, cv, ct)
+    assert st["degenerate"] >= 5
+
+
+def test_bad_triangle_index_rejected(ctx, native):
+    v = np.zeros((3, 3))
+    with pytest.raises(native.VisacdError):
+        ctx.bvh(v, np.array([[0, 1, 7]], np.int32))
+
+
+def test_compute_intersection_matrix_one_call(ctx, orc):
+    v, t = mg.displaced_blob(2, seed=4)
+    cv, ct = mg.offset_cage(v, t, 0.03)
+    e1, st1 = ctx.compute_intersection_matrix(v, t, cv, ct)
+    e2, st2, _, _ = _compare(ctx, orc, v, t, cv, ct)
+    np.testing.assert_array_equal(e1, e2)

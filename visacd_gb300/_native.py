@@ -1,0 +1,254 @@
+"""ctypes binding of the C ABI in include/visacd_gpu.h (libvisacd_gpu.so).
+
+This is how Python callers (tests, benchmarks, the host driver's debugging
+tools) reach the sm_103a kernels without torch types. The library must exist:
+a missing or unloadable library raises ImportError — there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+_LIB_PATH = Path(__file__).resolve().parent / "libvisacd_gpu.so"
+
+EXPORTED = [
+    "visacd_last_error", "visacd_abi_version",
+    "visacd_ctx_create", "visacd_ctx_destroy", "visacd_ctx_synchronize",
+    "visacd_ctx_set_timing", "visacd_ctx_reset_times", "visacd_ctx_kernel_times",
+    "visacd_ctx_launch_count", "visacd_ctx_sm_count",
+    "visacd_bvh_build", "visacd_bvh_destroy", "visacd_bvh_info",
+    "visacd_visibility", "visacd_visibility_edges", "visacd_visibility_edges_device",
+    "visacd_compute_intersection_matrix",
+    "visacd_score_planes", "classify_and_rate_planes",
+]
+
+
+class VisStats(C.Structure):
+    _fields_ = [("pairs_tested", C.c_int64), ("n_edges", C.c_int64), ("self_hits", C.c_int64),
+                ("cage_hits", C.c_int64), ("fp64_rechecks", C.c_int64), ("degenerate", C.c_int64)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class ScoreStats(C.Structure):
+    _fields_ = [("quantum_exp", C.c_int32), ("argmax", C.c_int32), ("band_blocks", C.c_int64),
+                ("skipped_edges", C.c_int64)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+def load() -> C.CDLL:
+    if not _LIB_PATH.exists():
+        raise ImportError(f"{_LIB_PATH} is missing: build it with visacd_gb300.build.build_gpu()")
+    lib = C.CDLL(str(_LIB_PATH))
+    P = C.c_void_p
+    i32, i64 = C.c_int32, C.c_int64
+    lib.visacd_last_error.restype = C.c_char_p
+    lib.visacd_abi_version.restype = C.c_int
+    lib.visacd_ctx_create.argtypes = [C.c_int, P, C.POINTER(P)]
+    lib.visacd_ctx_destroy.argtypes = [P]
+    lib.visacd_ctx_synchronize.argtypes = [P]
+    lib.visacd_ctx_set_timing.argtypes = [P, C.c_int]
+    lib.visacd_ctx_reset_times.argtypes = [P]
+    lib.visacd_ctx_kernel_times.argtypes = [P, C.POINTER(C.c_char_p), C.POINTER(C.c_double),
+                                            C.POINTER(i64), C.c_int, C.POINTER(C.c_int)]
+    lib.visacd_ctx_launch_count.argtypes = [P]
+    lib.visacd_ctx_launch_count.restype = i64
+    lib.visacd_ctx_sm_count.argtypes = [P]
+    lib.visacd_bvh_build.argtypes = [P, P, i32, P, i32, C.c_int, C.POINTER(P)]
+    lib.visacd_bvh_destroy.argtypes = [P]
+    lib.visacd_bvh_info.argtypes = [P, C.POINTER(i32), C.POINTER(i32)]
+    lib.visacd_visibility.argtypes = [P, P, i32, P, C.c_int, P, P, C.POINTER(i64),
+                                      C.POINTER(VisStats)]
+    lib.visacd_visibility_edges.argtypes = [P, P, i64]
+    lib.visacd_visibility_edges_device.argtypes = [P, C.POINTER(P), C.POINTER(i64)]
+    lib.visacd_compute_intersection_matrix.argtypes = [P, P, i32, P, i32, P, P, i32, P, i32, P,
+                                                       i64, C.POINTER(i64), C.POINTER(VisStats)]
+    lib.visacd_score_planes.argtypes = [P, P, i32, P, i32, P, i64, C.c_int, P,
+                                        C.POINTER(ScoreStats)]
+    lib.classify_and_rate_planes.argtypes = [P, P, P, P, C.c_int, C.c_int, C.c_int]
+    lib.classify_and_rate_planes.restype = None
+    return lib
+
+
+_lib: C.CDLL | None = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        _lib = load()
+    return _lib
+
+
+class VisacdError(RuntimeError):
+    pass
+
+
+def _check(rc: int, what: str) -> None:
+    if rc != 0:
+        msg = lib().visacd_last_error()
+        raise VisacdError(f"{what} failed (status {rc}): {msg.decode() if msg else ''}")
+
+
+def _ptr(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _f32(a, cols: int) -> np.ndarray:
+    a = np.ascontiguousarray(np.asarray(a, dtype=np.float32))
+    return a.reshape(-1, cols)
+
+
+def _u32(a, cols: int) -> np.ndarray:
+    a = np.ascontiguousarray(np.asarray(a, dtype=np.uint32))
+    return a.reshape(-1, cols)
+
+
+class Context:
+    """Owns a visacd_ctx (one CUDA stream + pooled device buffers)."""
+
+    def __init__(self, device: int = 0, stream: int | None = None):
+        self._h = C.c_void_p()
+        _check(lib().visacd_ctx_create(device, stream, C.byref(self._h)), "visacd_ctx_create")
+
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._h
+
+    def close(self) -> None:
+        if self._h:
+            lib().visacd_ctx_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):  # pragma: no cover - interpreter shutdown order
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def synchronize(self) -> None:
+        _check(lib().visacd_ctx_synchronize(self._h), "synchronize")
+
+    def set_timing(self, on: bool) -> None:
+        _check(lib().visacd_ctx_set_timing(self._h, int(on)), "set_timing")
+
+    def reset_times(self) -> None:
+        _check(lib().visacd_ctx_reset_times(self._h), "reset_times")
+
+    def kernel_times(self) -> dict[str, tuple[float, int]]:
+        cap = 64
+        names = (C.c_char_p * cap)()
+        ms = (C.c_double * cap)()
+        n_l = (C.c_int64 * cap)()
+        n = C.c_int()
+        _check(lib().visacd_ctx_kernel_times(self._h, names, ms, n_l, cap, C.byref(n)), "kernel_times")
+        return {names[i].decode(): (ms[i], n_l[i]) for i in range(min(n.value, cap))}
+
+    @property
+    def launches(self) -> int:
+        return int(lib().visacd_ctx_launch_count(self._h))
+
+    @property
+    def sm_count(self) -> int:
+        return int(lib().visacd_ctx_sm_count(self._h))
+
+    # ---- BVH / visibility ------------------------------------------------
+    def bvh(self, verts, tris) -> "Bvh":
+        return Bvh(self, verts, tris)
+
+    def visibility(self, pts, self_bvh: "Bvh", cage_bvh: "Bvh", is_new=None):
+        """Edges (E, 2) uint32 in row-major order, plus the counters."""
+        p = _f32(pts, 3)
+        m = None if is_new is None else np.ascontiguousarray(np.asarray(is_new, dtype=np.uint8))
+        ne = C.c_int64()
+        st = VisStats()
+        _check(lib().visacd_visibility(self._h, _ptr(p), len(p), _ptr(m), 0, self_bvh.handle,
+                                       cage_bvh.handle, C.byref(ne), C.byref(st)), "visacd_visibility")
+        out = np.empty((ne.value, 2), dtype=np.uint32)
+        _check(lib().visacd_visibility_edges(self._h, _ptr(out), ne.value), "visibility_edges")
+        return out, st.as_dict()
+
+    def compute_intersection_matrix(self, verts, tris, cage_verts, cage_tris, is_new=None,
+                                    capacity: int | None = None):
+        v = _f32(verts, 3)
+        t = _u32(tris, 3)
+        cv = _f32(cage_verts, 3)
+        ct = _u32(cage_tris, 3)
+        m = None if is_new is None else np.ascontiguousarray(np.asarray(is_new, dtype=np.uint8))
+        n = len(v)
+        cap = capacity if capacity is not None else max(1, n * (n - 1) // 2)
+        out = np.empty((cap, 2), dtype=np.uint32)
+        ne = C.c_int64()
+        st = VisStats()
+        _check(lib().visacd_compute_intersection_matrix(
+            self._h, _ptr(v), n, _ptr(t), len(t), _ptr(m), _ptr(cv), len(cv), _ptr(ct), len(ct),
+            _ptr(out), cap, C.byref(ne), C.byref(st)), "compute_intersection_matrix")
+        return out[: ne.value].copy(), st.as_dict()
+
+    # ---- scoring -----------------------------------------------------------
+    def score_planes(self, planes, points, edges):
+        pl = _f32(planes, 4)
+        pt = _f32(points, 3)
+        ed = _u32(edges, 2)
+        scores = np.zeros(len(pl), dtype=np.float64)
+        st = ScoreStats()
+        _check(lib().visacd_score_planes(self._h, _ptr(pl), len(pl), _ptr(pt), len(pt), _ptr(ed),
+                                         len(ed), 0, _ptr(scores), C.byref(st)), "visacd_score_planes")
+        return scores, st.as_dict()
+
+    def score_planes_device(self, d_planes: int, P: int, d_points: int, N: int, d_edges: int,
+                            E: int, d_scores: int, stats: bool = False):
+        st = ScoreStats()
+        _check(lib().visacd_score_planes(self._h, C.c_void_p(d_planes), P, C.c_void_p(d_points), N,
+                                         C.c_void_p(d_edges), E, 1, C.c_void_p(d_scores),
+                                         C.byref(st) if stats else None), "visacd_score_planes")
+        return st.as_dict() if stats else None
+
+
+class Bvh:
+    def __init__(self, ctx: Context, verts, tris, device_ptrs: bool = False, nv: int = 0, nt: int = 0):
+        self._h = C.c_void_p()
+        self._ctx = ctx
+        if device_ptrs:
+            _check(lib().visacd_bvh_build(ctx.handle, C.c_void_p(verts), nv, C.c_void_p(tris), nt, 1,
+                                          C.byref(self._h)), "visacd_bvh_build")
+        else:
+            v = _f32(verts, 3)
+            t = _u32(tris, 3)
+            _check(lib().visacd_bvh_build(ctx.handle, _ptr(v), len(v), _ptr(t), len(t), 0,
+                                          C.byref(self._h)), "visacd_bvh_build")
+
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._h
+
+    def info(self) -> tuple[int, int]:
+        nt, depth = C.c_int32(), C.c_int32()
+        _check(lib().visacd_bvh_info(self._h, C.byref(nt), C.byref(depth)), "bvh_info")
+        return nt.value, depth.value
+
+    def close(self) -> None:
+        if self._h:
+            lib().visacd_bvh_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):  # pragma: no cover
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def classify_and_rate_planes(planes, points, edges) -> np.ndarray:
+    """The reference-signature entry point (float scores, default context)."""
+    pl = _f32(planes, 4)
+    pt = _f32(points, 3)
+    ed = _u32(edges, 2)
+    out = np.zeros(len(pl), dtype=np.float32)
+    lib().classify_and_rate_planes(_ptr(pl), _ptr(pt), _ptr(ed), _ptr(out), len(pl), len(pt), len(ed))
+    return out

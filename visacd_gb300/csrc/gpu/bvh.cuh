@@ -1,0 +1,35 @@
+// Device-resident linear BVH shared by the builder and the visibility kernel.
+#pragma once
+
+#include <string.h>
+
+#include "common.cuh"
+
+// Node record (64 bytes, 4 x float4):
+//   [0] lmin.x lmin.y lmin.z lmax.x
+//   [1] lmax.y lmax.z rmin.x rmin.y
+//   [2] rmin.z rmax.x rmax.y rmax.z
+//   [3] left  right  (int bits; >= 0 internal node, < 0 leaf ~sorted_triangle)
+// Leaf triangle record (48 bytes, 3 x float4): vertex xyz + vertex index bits.
+struct visacd_bvh {
+  int device = 0;
+  int32_t nt = 0;
+  int32_t nv = 0;
+  int32_t depth = 0;
+  float amax = 0.f;  // largest |vertex coordinate|
+  float4* nodes = nullptr;
+  float4* tris = nullptr;
+};
+
+namespace vgpu {
+
+inline float __uint_as_float_host(unsigned u) {
+  float f;
+  memcpy(&f, &u, 4);
+  return f;
+}
+
+int bvh_build(visacd_ctx* ctx, const float* verts, int32_t nv, const uint32_t* tris, int32_t nt,
+              int device_ptrs, visacd_bvh** out);
+
+}  // namespace vgpu

@@ -1,0 +1,198 @@
+// Shared plumbing of the sm_103a library: error reporting, the context object,
+// grow-only device buffers and per-kernel CUDA-event timing.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "visacd_gpu.h"
+
+namespace vgpu {
+
+void set_error(const char* fmt, ...);
+
+#define VCUDA(call)                                                                     \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess) {                                                            \
+      vgpu::set_error("%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                      __LINE__);                                                        \
+      return e_ == cudaErrorMemoryAllocation ? VISACD_ERR_NO_MEMORY : VISACD_ERR_CUDA;  \
+    }                                                                                   \
+  } while (0)
+
+#define VCHECK(cond, code, ...)   \
+  do {                            \
+    if (!(cond)) {                \
+      vgpu::set_error(__VA_ARGS__); \
+      return (code);              \
+    }                             \
+  } while (0)
+
+#define VTRY(expr)          \
+  do {                      \
+    int rc_ = (expr);       \
+    if (rc_ != VISACD_OK) { \
+      return rc_;           \
+    }                       \
+  } while (0)
+
+// Device status word bits, set by kernels whose bounded loops ran out.
+enum : uint32_t {
+  kStatusTraversalOverrun = 1u << 0,
+  kStatusStackOverflow = 1u << 1,
+  kStatusRecheckOverflow = 1u << 2,
+  kStatusMbarrierTimeout = 1u << 3,
+  kStatusWorkOverrun = 1u << 4,
+};
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+};
+
+// Grow-only device buffer: reallocates (without preserving contents) only when
+// the request exceeds the current capacity; capacities round up to 1.25x.
+int ensure(DevBuf& b, size_t bytes);
+void release(DevBuf& b);
+
+struct KernelTime {
+  const char* name;
+  double ms = 0.0;
+  int64_t launches = 0;
+};
+
+}  // namespace vgpu
+
+// Named buffer slots owned by a context.
+enum CtxSlot {
+  kSlotPoints = 0,
+  kSlotMask,
+  kSlotPlanes,
+  kSlotEdgesIn,
+  kSlotEdgePack,
+  kSlotScoreQ,
+  kSlotScores,
+  kSlotRecheck,
+  kSlotPointStats,
+  kSlotVisKeys,
+  kSlotVisKeysAlt,
+  kSlotVisPerm,
+  kSlotVisPermAlt,
+  kSlotVisRank,
+  kSlotBitset,
+  kSlotWordCounts,
+  kSlotWordOffsets,
+  kSlotEdgesOut,
+  kSlotScanScratch,
+  kSlotSortHist,
+  kSlotCounters,
+  kSlotBuildVerts,
+  kSlotBuildTris,
+  kSlotTmpVerts,
+  kSlotTmpTris,
+  kSlotCount
+};
+
+struct visacd_ctx {
+  int device = 0;
+  int sm_count = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  vgpu::DevBuf buf[kSlotCount];
+  uint32_t* d_status = nullptr;      // device status word
+  void* h_pinned = nullptr;          // small pinned staging area
+  size_t h_pinned_cap = 0;
+  int64_t launches = 0;
+  int64_t last_n_edges = 0;
+  bool timing = false;
+  // Per-kernel timing: events recorded around each launch when timing is on.
+  struct Pending {
+    int kernel;
+    cudaEvent_t a, b;
+  };
+  std::vector<Pending> pending;
+  std::vector<cudaEvent_t> event_pool;
+  std::vector<vgpu::KernelTime> times;
+};
+
+namespace vgpu {
+
+// Kernel ids for timing (index into a static name table).
+enum KernelId {
+  kKPointStats = 0,
+  kKPackEdges,
+  kKScore,
+  kKScoreRecheck,
+  kKScoreFinish,
+  kKTriPrep,
+  kKMorton,
+  kKSortHist,
+  kKSortScan,
+  kKSortScatter,
+  kKKarras,
+  kKFit,
+  kKNodeLayout,
+  kKVisPrep,
+  kKVisibility,
+  kKBitPopc,
+  kKScanBlocks,
+  kKScanTop,
+  kKScanAdd,
+  kKBitEmit,
+  kKMisc,
+  kKCount
+};
+const char* kernel_name(int id);
+
+// Launch bookkeeping: call before and after each launch on ctx->stream.
+void timing_begin(visacd_ctx* ctx, int kernel, cudaEvent_t* a);
+int timing_end(visacd_ctx* ctx, int kernel, cudaEvent_t a);
+
+// Check cudaGetLastError after a launch and update the launch counter.
+int after_launch(visacd_ctx* ctx, const char* what);
+
+// Read back and clear the device status word; returns VISACD_ERR_DEVICE with a
+// message when any bit is set. Synchronizes the context stream.
+int check_status(visacd_ctx* ctx, const char* what);
+
+// Pinned host staging of at least `bytes`.
+int pinned(visacd_ctx* ctx, size_t bytes, void** out);
+
+template <class T>
+inline T* slot(visacd_ctx* ctx, int s) {
+  return reinterpret_cast<T*>(ctx->buf[s].p);
+}
+inline int ensure_slot(visacd_ctx* ctx, int s, size_t bytes) { return ensure(ctx->buf[s], bytes); }
+
+inline unsigned grid_for(int64_t n, int block, int64_t cap) {
+  int64_t g = (n + block - 1) / block;
+  if (g < 1) g = 1;
+  if (g > cap) g = cap;
+  return (unsigned)g;
+}
+
+// Exclusive scan of n uint32 counts into uint64 offsets (device), total also
+// written to offsets[n]. Uses ctx scan scratch.
+int exclusive_scan_u32_to_u64(visacd_ctx* ctx, const uint32_t* in, uint64_t* out, int64_t n);
+
+// Stable LSD radix sort of (key, value) pairs on the device. key_bits selects
+// how many low bits of the key take part (multiple of 8). Results land in
+// keys/vals (the alt buffers are scratch of the same size).
+int radix_sort_u64(visacd_ctx* ctx, uint64_t* keys, uint32_t* vals, uint64_t* keys_alt,
+                   uint32_t* vals_alt, int32_t n, int key_bits);
+
+}  // namespace vgpu
+
+// Launch helper: times the launch when ctx timing is on, checks the launch.
+#define VLAUNCH(ctx, kid, grid, block, smem, kernel, ...)                 \
+  do {                                                                    \
+    cudaEvent_t ev_a_ = nullptr;                                          \
+    vgpu::timing_begin((ctx), (kid), &ev_a_);                             \
+    kernel<<<(grid), (block), (smem), (ctx)->stream>>>(__VA_ARGS__);      \
+    VTRY(vgpu::after_launch((ctx), #kernel));                             \
+    VTRY(vgpu::timing_end((ctx), (kid), ev_a_));                          \
+  } while (0)

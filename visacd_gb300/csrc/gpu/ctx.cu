@@ -1,0 +1,461 @@
+// Context lifetime, error strings, grow-only buffers, launch timing, and the two
+// generic device primitives the kernels share: an exclusive scan and a stable
+// LSD radix sort (own kernels; no CUB/Thrust on the product path).
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include "common.cuh"
+
+namespace vgpu {
+
+static thread_local char g_err[1024] = "";
+
+void set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+int ensure(DevBuf& b, size_t bytes) {
+  if (bytes <= b.cap && b.p) return VISACD_OK;
+  if (b.p) {
+    cudaFree(b.p);
+    b.p = nullptr;
+    b.cap = 0;
+  }
+  size_t want = bytes + bytes / 4;
+  if (want < 256) want = 256;
+  want = (want + 255) & ~size_t(255);
+  cudaError_t e = cudaMalloc(&b.p, want);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    b.p = nullptr;
+    set_error("cudaMalloc(%zu) failed: %s", want, cudaGetErrorString(e));
+    return VISACD_ERR_NO_MEMORY;
+  }
+  b.cap = want;
+  return VISACD_OK;
+}
+
+void release(DevBuf& b) {
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.cap = 0;
+}
+
+static const char* kNames[kKCount] = {
+    "point_stats",   "pack_edges",     "score_planes", "score_recheck_fp64",
+    "score_finish",  "tri_prep",       "morton",       "radix_hist",
+    "radix_scan",    "radix_scatter",  "karras_build", "aabb_fit",
+    "node_layout",   "vis_prep",       "visibility",   "bitset_popc",
+    "scan_blocks",   "scan_top",       "scan_add",     "bitset_emit",
+    "misc"};
+
+const char* kernel_name(int id) { return (id >= 0 && id < kKCount) ? kNames[id] : "?"; }
+
+static cudaEvent_t take_event(visacd_ctx* ctx) {
+  if (!ctx->event_pool.empty()) {
+    cudaEvent_t e = ctx->event_pool.back();
+    ctx->event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  if (cudaEventCreate(&e) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return e;
+}
+
+void timing_begin(visacd_ctx* ctx, int kernel, cudaEvent_t* a) {
+  (void)kernel;
+  *a = nullptr;
+  if (!ctx->timing) return;
+  *a = take_event(ctx);
+  if (*a) cudaEventRecord(*a, ctx->stream);
+}
+
+int timing_end(visacd_ctx* ctx, int kernel, cudaEvent_t a) {
+  if (!ctx->timing || !a) return VISACD_OK;
+  cudaEvent_t b = take_event(ctx);
+  if (!b) return VISACD_OK;
+  VCUDA(cudaEventRecord(b, ctx->stream));
+  ctx->pending.push_back({kernel, a, b});
+  return VISACD_OK;
+}
+
+int after_launch(visacd_ctx* ctx, const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error("launch of %s failed: %s", what, cudaGetErrorString(e));
+    return VISACD_ERR_CUDA;
+  }
+  ctx->launches++;
+  return VISACD_OK;
+}
+
+int pinned(visacd_ctx* ctx, size_t bytes, void** out) {
+  if (bytes > ctx->h_pinned_cap) {
+    if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
+    ctx->h_pinned = nullptr;
+    ctx->h_pinned_cap = 0;
+    size_t want = bytes < 4096 ? 4096 : bytes + bytes / 4;
+    cudaError_t e = cudaMallocHost(&ctx->h_pinned, want);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      set_error("cudaMallocHost(%zu) failed: %s", want, cudaGetErrorString(e));
+      return VISACD_ERR_NO_MEMORY;
+    }
+    ctx->h_pinned_cap = want;
+  }
+  *out = ctx->h_pinned;
+  return VISACD_OK;
+}
+
+int check_status(visacd_ctx* ctx, const char* what) {
+  uint32_t* h = nullptr;
+  VTRY(pinned(ctx, 64, (void**)&h));
+  VCUDA(cudaMemcpyAsync(h, ctx->d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+  VCUDA(cudaStreamSynchronize(ctx->stream));
+  uint32_t s = h[0];
+  if (s) {
+    VCUDA(cudaMemsetAsync(ctx->d_status, 0, sizeof(uint32_t), ctx->stream));
+    set_error("%s: device status 0x%x (traversal overrun=%d, stack overflow=%d, recheck "
+              "overflow=%d, mbarrier timeout=%d, work overrun=%d)",
+              what, s, !!(s & kStatusTraversalOverrun), !!(s & kStatusStackOverflow),
+              !!(s & kStatusRecheckOverflow), !!(s & kStatusMbarrierTimeout),
+              !!(s & kStatusWorkOverrun));
+    return VISACD_ERR_DEVICE;
+  }
+  return VISACD_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Exclusive scan u32 -> u64 (three phases: block sums, top scan, add).
+// ---------------------------------------------------------------------------
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+__device__ __forceinline__ uint64_t block_exclusive_scan_u64(uint64_t v, uint64_t* total) {
+  __shared__ uint64_t warp_sums[kScanThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint64_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint64_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_sums[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint64_t w = lane < kScanThreads / 32 ? warp_sums[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint64_t y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    if (lane < kScanThreads / 32) warp_sums[lane] = w;
+  }
+  __syncthreads();
+  uint64_t before = warp ? warp_sums[warp - 1] : 0;
+  *total = warp_sums[kScanThreads / 32 - 1];
+  __syncthreads();
+  return before + x - v;
+}
+
+__global__ void scan_blocks_kernel(const uint32_t* __restrict__ in, int64_t n,
+                                   uint64_t* __restrict__ block_sums) {
+  int64_t base = (int64_t)blockIdx.x * kScanTile;
+  uint64_t s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    int64_t i = base + (int64_t)k * kScanThreads + threadIdx.x;
+    if (i < n) s += in[i];
+  }
+  uint64_t total;
+  block_exclusive_scan_u64(s, &total);
+  if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
+}
+
+__global__ void scan_top_kernel(uint64_t* __restrict__ block_sums, int64_t nb) {
+  uint64_t carry = 0;
+  for (int64_t start = 0; start < nb; start += kScanThreads) {
+    int64_t i = start + threadIdx.x;
+    uint64_t v = i < nb ? block_sums[i] : 0;
+    uint64_t total;
+    uint64_t ex = block_exclusive_scan_u64(v, &total);
+    if (i < nb) block_sums[i] = carry + ex;
+    carry += total;
+  }
+  if (threadIdx.x == 0) block_sums[nb] = carry;
+}
+
+__global__ void scan_add_kernel(const uint32_t* __restrict__ in, int64_t n,
+                                const uint64_t* __restrict__ block_sums,
+                                uint64_t* __restrict__ out, int64_t nb) {
+  // Each thread owns kScanItems consecutive elements.
+  int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+  uint32_t v[kScanItems];
+  uint64_t s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    int64_t i = base + k;
+    v[k] = i < n ? in[i] : 0u;
+    s += v[k];
+  }
+  uint64_t total;
+  uint64_t ex = block_exclusive_scan_u64(s, &total) + block_sums[blockIdx.x];
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    int64_t i = base + k;
+    if (i < n) out[i] = ex;
+    ex += v[k];
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) out[n] = block_sums[nb];
+}
+
+int exclusive_scan_u32_to_u64(visacd_ctx* ctx, const uint32_t* in, uint64_t* out, int64_t n) {
+  int64_t nb = (n + kScanTile - 1) / kScanTile;
+  if (nb < 1) nb = 1;
+  VCHECK(nb < (1ll << 31), VISACD_ERR_INVALID_ARG, "scan too large: %lld", (long long)n);
+  VTRY(ensure_slot(ctx, kSlotScanScratch, (size_t)(nb + 1) * sizeof(uint64_t)));
+  uint64_t* bs = slot<uint64_t>(ctx, kSlotScanScratch);
+  VLAUNCH(ctx, kKScanBlocks, (unsigned)nb, kScanThreads, 0, scan_blocks_kernel, in, n, bs);
+  VLAUNCH(ctx, kKScanTop, 1, kScanThreads, 0, scan_top_kernel, bs, nb);
+  VLAUNCH(ctx, kKScanAdd, (unsigned)nb, kScanThreads, 0, scan_add_kernel, in, n, bs, out, nb);
+  return VISACD_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Stable LSD radix sort, 8-bit digits.
+// ---------------------------------------------------------------------------
+constexpr int kSortThreads = 256;
+constexpr int kSortRounds = 8;
+constexpr int kSortTile = kSortThreads * kSortRounds;
+
+__global__ void radix_hist_kernel(const uint64_t* __restrict__ keys, int32_t n, int shift,
+                                  uint32_t* __restrict__ hist, int nblocks) {
+  __shared__ uint32_t h[256];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  int64_t base = (int64_t)blockIdx.x * kSortTile;
+  for (int r = 0; r < kSortRounds; ++r) {
+    int64_t i = base + (int64_t)r * kSortThreads + threadIdx.x;
+    if (i < n) atomicAdd(&h[(keys[i] >> shift) & 0xffu], 1u);
+  }
+  __syncthreads();
+  hist[(int64_t)threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
+}
+
+__global__ void radix_scatter_kernel(const uint64_t* __restrict__ keys,
+                                     const uint32_t* __restrict__ vals, int32_t n, int shift,
+                                     const uint64_t* __restrict__ offsets, int nblocks,
+                                     uint64_t* __restrict__ keys_out,
+                                     uint32_t* __restrict__ vals_out) {
+  __shared__ uint32_t cnt[kSortThreads / 32][256];
+  __shared__ uint64_t base_off[256];
+  __shared__ uint32_t round_total[256];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  base_off[threadIdx.x] = offsets[(int64_t)threadIdx.x * nblocks + blockIdx.x];
+  int64_t tile = (int64_t)blockIdx.x * kSortTile;
+  for (int r = 0; r < kSortRounds; ++r) {
+#pragma unroll
+    for (int w = 0; w < kSortThreads / 32; ++w) cnt[w][threadIdx.x] = 0;
+    __syncthreads();
+    int64_t i = tile + (int64_t)r * kSortThreads + threadIdx.x;
+    bool valid = i < n;
+    uint64_t k = valid ? keys[i] : 0;
+    uint32_t v = valid ? vals[i] : 0;
+    uint32_t digit = (uint32_t)(k >> shift) & 0xffu;
+    unsigned active = __ballot_sync(0xffffffffu, valid);
+    unsigned rank = 0;
+    if (valid) {
+      unsigned peers = __match_any_sync(active, digit);
+      unsigned lower = peers & ((1u << lane) - 1u);
+      rank = __popc(lower);
+      if (lower == 0) cnt[warp][digit] = __popc(peers);
+    }
+    __syncthreads();
+    {
+      uint32_t run = 0;
+#pragma unroll
+      for (int w = 0; w < kSortThreads / 32; ++w) {
+        uint32_t c = cnt[w][threadIdx.x];
+        cnt[w][threadIdx.x] = run;
+        run += c;
+      }
+      round_total[threadIdx.x] = run;
+    }
+    __syncthreads();
+    if (valid) {
+      uint64_t pos = base_off[digit] + cnt[warp][digit] + rank;
+      keys_out[pos] = k;
+      vals_out[pos] = v;
+    }
+    __syncthreads();
+    base_off[threadIdx.x] += round_total[threadIdx.x];
+    __syncthreads();
+  }
+}
+
+int radix_sort_u64(visacd_ctx* ctx, uint64_t* keys, uint32_t* vals, uint64_t* keys_alt,
+                   uint32_t* vals_alt, int32_t n, int key_bits) {
+  if (n <= 1) return VISACD_OK;
+  int nblocks = (int)((n + kSortTile - 1) / kSortTile);
+  size_t hist_n = (size_t)256 * nblocks;
+  VTRY(ensure_slot(ctx, kSlotSortHist, hist_n * sizeof(uint32_t) + (hist_n + 1) * sizeof(uint64_t) + 16));
+  uint32_t* hist = slot<uint32_t>(ctx, kSlotSortHist);
+  uint64_t* offs = reinterpret_cast<uint64_t*>(
+      (reinterpret_cast<uintptr_t>(hist + hist_n) + 15) & ~uintptr_t(15));
+  uint64_t *ksrc = keys, *kdst = keys_alt;
+  uint32_t *vsrc = vals, *vdst = vals_alt;
+  int passes = (key_bits + 7) / 8;
+  for (int p = 0; p < passes; ++p) {
+    int shift = 8 * p;
+    VLAUNCH(ctx, kKSortHist, nblocks, kSortThreads, 0, radix_hist_kernel, ksrc, n, shift, hist,
+            nblocks);
+    VTRY(exclusive_scan_u32_to_u64(ctx, hist, offs, (int64_t)hist_n));
+    VLAUNCH(ctx, kKSortScatter, nblocks, kSortThreads, 0, radix_scatter_kernel, ksrc, vsrc, n,
+            shift, offs, nblocks, kdst, vdst);
+    uint64_t* kt = ksrc; ksrc = kdst; kdst = kt;
+    uint32_t* vt = vsrc; vsrc = vdst; vdst = vt;
+  }
+  if (ksrc != keys) {
+    VCUDA(cudaMemcpyAsync(keys, ksrc, (size_t)n * sizeof(uint64_t), cudaMemcpyDeviceToDevice,
+                          ctx->stream));
+    VCUDA(cudaMemcpyAsync(vals, vsrc, (size_t)n * sizeof(uint32_t), cudaMemcpyDeviceToDevice,
+                          ctx->stream));
+  }
+  return VISACD_OK;
+}
+
+}  // namespace vgpu
+
+// ---------------------------------------------------------------------------
+// C ABI: errors and context.
+// ---------------------------------------------------------------------------
+using namespace vgpu;
+
+extern "C" const char* visacd_last_error(void) { return g_err; }
+extern "C" int visacd_abi_version(void) { return VISACD_ABI_VERSION; }
+
+extern "C" int visacd_ctx_create(int device, void* cuda_stream, visacd_ctx** out) {
+  VCHECK(out != nullptr, VISACD_ERR_INVALID_ARG, "visacd_ctx_create: out is NULL");
+  *out = nullptr;
+  int ndev = 0;
+  VCUDA(cudaGetDeviceCount(&ndev));
+  VCHECK(device >= 0 && device < ndev, VISACD_ERR_INVALID_ARG,
+         "visacd_ctx_create: device %d out of range (%d devices)", device, ndev);
+  VCUDA(cudaSetDevice(device));
+  visacd_ctx* ctx = new visacd_ctx();
+  ctx->device = device;
+  cudaDeviceProp prop;
+  cudaError_t e = cudaGetDeviceProperties(&prop, device);
+  if (e != cudaSuccess) {
+    delete ctx;
+    set_error("cudaGetDeviceProperties: %s", cudaGetErrorString(e));
+    return VISACD_ERR_CUDA;
+  }
+  ctx->sm_count = prop.multiProcessorCount;
+  if (cuda_stream) {
+    ctx->stream = (cudaStream_t)cuda_stream;
+  } else {
+    e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+      delete ctx;
+      set_error("cudaStreamCreate: %s", cudaGetErrorString(e));
+      return VISACD_ERR_CUDA;
+    }
+    ctx->own_stream = true;
+  }
+  e = cudaMalloc(&ctx->d_status, 256);
+  if (e == cudaSuccess) e = cudaMemset(ctx->d_status, 0, 256);
+  if (e != cudaSuccess) {
+    if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    set_error("status word allocation: %s", cudaGetErrorString(e));
+    return VISACD_ERR_NO_MEMORY;
+  }
+  ctx->times.resize(kKCount);
+  for (int i = 0; i < kKCount; ++i) ctx->times[i].name = kernel_name(i);
+  *out = ctx;
+  return VISACD_OK;
+}
+
+extern "C" int visacd_ctx_destroy(visacd_ctx* ctx) {
+  if (!ctx) return VISACD_OK;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  for (int i = 0; i < kSlotCount; ++i) release(ctx->buf[i]);
+  if (ctx->d_status) cudaFree(ctx->d_status);
+  if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
+  for (auto& p : ctx->pending) {
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.b);
+  }
+  for (auto e : ctx->event_pool) cudaEventDestroy(e);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return VISACD_OK;
+}
+
+extern "C" int visacd_ctx_synchronize(visacd_ctx* ctx) {
+  VCHECK(ctx, VISACD_ERR_INVALID_ARG, "null context");
+  VCUDA(cudaStreamSynchronize(ctx->stream));
+  return VISACD_OK;
+}
+
+extern "C" int visacd_ctx_set_timing(visacd_ctx* ctx, int enable) {
+  VCHECK(ctx, VISACD_ERR_INVALID_ARG, "null context");
+  ctx->timing = enable != 0;
+  return VISACD_OK;
+}
+
+static int drain_pending(visacd_ctx* ctx) {
+  if (ctx->pending.empty()) return VISACD_OK;
+  VCUDA(cudaStreamSynchronize(ctx->stream));
+  for (auto& p : ctx->pending) {
+    float ms = 0.f;
+    VCUDA(cudaEventElapsedTime(&ms, p.a, p.b));
+    ctx->times[p.kernel].ms += ms;
+    ctx->times[p.kernel].launches += 1;
+    ctx->event_pool.push_back(p.a);
+    ctx->event_pool.push_back(p.b);
+  }
+  ctx->pending.clear();
+  return VISACD_OK;
+}
+
+extern "C" int visacd_ctx_reset_times(visacd_ctx* ctx) {
+  VCHECK(ctx, VISACD_ERR_INVALID_ARG, "null context");
+  VTRY(drain_pending(ctx));
+  for (auto& t : ctx->times) {
+    t.ms = 0.0;
+    t.launches = 0;
+  }
+  return VISACD_OK;
+}
+
+extern "C" int visacd_ctx_kernel_times(visacd_ctx* ctx, const char** names, double* total_ms,
+                                       int64_t* launches, int capacity, int* n_kernels) {
+  VCHECK(ctx, VISACD_ERR_INVALID_ARG, "null context");
+  VTRY(drain_pending(ctx));
+  int n = 0;
+  for (auto& t : ctx->times) {
+    if (t.launches == 0) continue;
+    if (n < capacity) {
+      if (names) names[n] = t.name;
+      if (total_ms) total_ms[n] = t.ms;
+      if (launches) launches[n] = t.launches;
+    }
+    ++n;
+  }
+  if (n_kernels) *n_kernels = n;
+  return VISACD_OK;
+}
+
+extern "C" int64_t visacd_ctx_launch_count(const visacd_ctx* ctx) { return ctx ? ctx->launches : 0; }
+extern "C" int visacd_ctx_sm_count(const visacd_ctx* ctx) { return ctx ? ctx->sm_count : 0; }

@@ -1,0 +1,596 @@
+// Plane scoring: score[p] = sum of |e| over visibility edges e that plane p cuts
+// strictly (both endpoints farther than eps = 1e-6f on opposite sides).
+//
+// Reference semantics: lib/cuda/plane_intersections.cu:7-67 (one thread per
+// (plane, edge), FP32 side test with eps, float atomicAdd of the FP32 length).
+//
+// GB300 design:
+//  * pack_edges gathers each edge's two endpoints once into a 32-byte record
+//    {x1,x2,y1,y2 | z1,z2,q,0} so the hot loop reads coalesced, pre-paired
+//    operands for packed FP32x2 FMAs. q is the FP32 edge length (IEEE ops, no
+//    contraction) quantized to 2^qexp, qexp chosen from the largest |coordinate|
+//    so that q < 2^24 and a 256-edge block sums in 32 bits.
+//  * score_planes keeps 1..8 planes per thread in registers (coefficients
+//    duplicated into f32x2 pairs) and streams 512-edge blocks into shared memory
+//    with cp.async.bulk (TMA bulk copy) + mbarrier, double-buffered (256-edge blocks). Every
+//    thread of the CTA reads the same edge (shared-memory broadcast).
+//  * The FP32 plane value carries an a-priori rounding bound B_p (Higham,
+//    3 nested FMAs: |err| <= 3u * (|a|X + |b|Y + |c|Z + |d|)). Per (plane, edge
+//    block) the kernel accumulates the certain crossings (beyond eps + B) and the
+//    possible ones (beyond eps - B); if they differ the block is queued and
+//    score_recheck re-decides only its band pairs in FP64 — the same FP64
+//    evaluation the oracle uses — so classification equals the FP64 oracle's.
+//  * Sums are integers (order independent), so scores are deterministic.
+#include "common.cuh"
+
+namespace vgpu {
+
+constexpr int kScoreThreads = 256;
+constexpr int kEdgeBlock = 256;  // edges per shared-memory block; 256 * (2^24 - 1) < 2^32
+constexpr float kSideEps = 1e-6f;
+// 3.0001u would do for the FMA chain; the extra covers the FP32 evaluation of
+// S itself and the FP64 re-decision's own rounding.
+constexpr float kBandFactor = 3.0e-7f;
+
+struct __align__(16) EdgeRec {
+  float x1, x2, y1, y2;
+  float z1, z2;
+  uint32_t q;
+  uint32_t pad;
+};
+static_assert(sizeof(EdgeRec) == 32, "edge record must be 32 bytes");
+
+__device__ __forceinline__ unsigned long long pack2(float a, float b) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ void unpack2(unsigned long long v, float& a, float& b) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ unsigned long long ffma2(unsigned long long a, unsigned long long b,
+                                                    unsigned long long c) {
+  unsigned long long d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+
+// Largest |coordinate| over finite points, as float bits (non-negative floats
+// order like unsigned ints).
+__global__ void point_stats_kernel(const float* __restrict__ pts, int32_t n,
+                                   unsigned* __restrict__ stats) {
+  float mx = 0.f, my = 0.f, mz = 0.f;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    float x = pts[3 * i], y = pts[3 * i + 1], z = pts[3 * i + 2];
+    if (isfinite(x) && isfinite(y) && isfinite(z)) {
+      mx = fmaxf(mx, fabsf(x));
+      my = fmaxf(my, fabsf(y));
+      mz = fmaxf(mz, fabsf(z));
+    }
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    my = fmaxf(my, __shfl_xor_sync(0xffffffffu, my, o));
+    mz = fmaxf(mz, __shfl_xor_sync(0xffffffffu, mz, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(&stats[0], __float_as_uint(mx));
+    atomicMax(&stats[1], __float_as_uint(my));
+    atomicMax(&stats[2], __float_as_uint(mz));
+  }
+}
+
+// Exponent e with max|coord| < 2^e; edge lengths are below 2^(e+2), so with
+// the quantum 2^(e - 22) every quantized length is below 2^24.
+__device__ __host__ __forceinline__ int quantum_exp_from_cmax_bits(unsigned cbits) {
+  int eb = (int)((cbits >> 23) & 0xffu);
+  int e = eb >= 1 ? eb - 126 : -126;
+  return e - 22;
+}
+
+__device__ __forceinline__ float edge_len32(float dx, float dy, float dz) {
+  // IEEE single ops in a fixed order, no contraction: reproducible on the host.
+  float s = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+  return __fsqrt_rn(s);
+}
+
+__global__ void pack_edges_kernel(const float* __restrict__ pts, int32_t n,
+                                  const uint32_t* __restrict__ edges, int64_t E,
+                                  const unsigned* __restrict__ stats, EdgeRec* __restrict__ out,
+                                  unsigned long long* __restrict__ skipped) {
+  unsigned cmax = max(stats[0], max(stats[1], stats[2]));
+  int qexp = quantum_exp_from_cmax_bits(cmax);
+  unsigned long long nskip = 0;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < E;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    uint2 ij = reinterpret_cast<const uint2*>(edges)[e];
+    EdgeRec r;
+    r.pad = 0;
+    bool ok = ij.x < (uint32_t)n && ij.y < (uint32_t)n;
+    float x1 = 0, y1 = 0, z1 = 0, x2 = 0, y2 = 0, z2 = 0;
+    if (ok) {
+      x1 = pts[3 * (int64_t)ij.x];
+      y1 = pts[3 * (int64_t)ij.x + 1];
+      z1 = pts[3 * (int64_t)ij.x + 2];
+      x2 = pts[3 * (int64_t)ij.y];
+      y2 = pts[3 * (int64_t)ij.y + 1];
+      z2 = pts[3 * (int64_t)ij.y + 2];
+      ok = isfinite(x1) && isfinite(y1) && isfinite(z1) && isfinite(x2) && isfinite(y2) &&
+           isfinite(z2);
+    }
+    if (ok) {
+      float len = edge_len32(__fsub_rn(x2, x1), __fsub_rn(y2, y1), __fsub_rn(z2, z1));
+      r.x1 = x1; r.x2 = x2; r.y1 = y1; r.y2 = y2; r.z1 = z1; r.z2 = z2;
+      r.q = __float2uint_rn(ldexpf(len, -qexp));
+    } else {
+      r.x1 = r.x2 = r.y1 = r.y2 = r.z1 = r.z2 = 0.f;
+      r.q = 0;
+      ++nskip;
+    }
+    out[e] = r;
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) nskip += __shfl_xor_sync(0xffffffffu, nskip, o);
+  if ((threadIdx.x & 31) == 0 && nskip) atomicAdd(skipped, nskip);
+}
+
+// Negated thresholds: crossing is certain when s < nhi, possible when s < nlo,
+// with s = max(min(v1, v2), -max(v1, v2)) (negative iff signs differ; then
+// -s = min(|v1|, |v2|)).
+__device__ __forceinline__ void plane_thresholds(float4 pl, const unsigned* stats, float& nlo,
+                                                 float& nhi) {
+  float X = __uint_as_float(stats[0]), Y = __uint_as_float(stats[1]),
+        Z = __uint_as_float(stats[2]);
+  float S = fabsf(pl.x) * X + fabsf(pl.y) * Y + fabsf(pl.z) * Z + fabsf(pl.w);
+  float B = S * kBandFactor;
+  nhi = -(kSideEps + B);
+  nlo = -(kSideEps - B);
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes,
+                                          uint64_t* bar) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+  asm volatile(
+      "cp.async.bulk.shared::cta.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Bounded wait on an mbarrier phase; returns false if the phase never completed.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+  for (int it = 0; it < (1 << 22); ++it) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 "
+        "%0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+template <int K>
+__global__ void __launch_bounds__(kScoreThreads, (K <= 4 ? 2 : 1))
+    score_planes_kernel(const float4* __restrict__ planes, int32_t P,
+                        const EdgeRec* __restrict__ recs, int64_t E, int64_t blocks_per_cta,
+                        const unsigned* __restrict__ stats,
+                        unsigned long long* __restrict__ score_q, uint2* __restrict__ recheck,
+                        unsigned* __restrict__ recheck_count, unsigned recheck_cap,
+                        unsigned* __restrict__ status) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  EdgeRec* buf = reinterpret_cast<EdgeRec*>(smem_raw);  // 2 x kEdgeBlock records
+  unsigned long long* tot =
+      reinterpret_cast<unsigned long long*>(smem_raw + 2 * kEdgeBlock * sizeof(EdgeRec));
+  __shared__ __align__(8) uint64_t bars[2];
+
+  const int tid = threadIdx.x;
+  const int64_t n_blocks_total = (E + kEdgeBlock - 1) / kEdgeBlock;
+  const int64_t b_begin = (int64_t)blockIdx.x * blocks_per_cta;
+  int64_t b_end = b_begin + blocks_per_cta;
+  if (b_end > n_blocks_total) b_end = n_blocks_total;
+  const int nb = (int)(b_end > b_begin ? b_end - b_begin : 0);
+  const int plane_base = blockIdx.y * (kScoreThreads * K);
+
+  unsigned long long a2[K], b2[K], c2[K], d2[K];
+  float nlo[K], nhi[K];
+  uint32_t acc_lo[K], acc_hi[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    int p = plane_base + k * kScoreThreads + tid;
+    float4 pl = p < P ? planes[p] : make_float4(__int_as_float(0x7fc00000), 0.f, 0.f, 0.f);
+    if (p >= P) pl = make_float4(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000),
+                                 __int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
+    a2[k] = pack2(pl.x, pl.x);
+    b2[k] = pack2(pl.y, pl.y);
+    c2[k] = pack2(pl.z, pl.z);
+    d2[k] = pack2(pl.w, pl.w);
+    plane_thresholds(pl, stats, nlo[k], nhi[k]);
+    acc_lo[k] = acc_hi[k] = 0u;
+    tot[k * kScoreThreads + tid] = 0ull;
+  }
+  if (nb == 0) return;
+
+  if (tid == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (tid == 0) {
+    int64_t e0 = b_begin * kEdgeBlock;
+    int64_t cnt = E - e0 < kEdgeBlock ? E - e0 : kEdgeBlock;
+    bulk_load(buf, recs + e0, (unsigned)(cnt * sizeof(EdgeRec)), &bars[0]);
+  }
+
+  bool failed = false;
+  for (int it = 0; it < nb; ++it) {
+    const int cur = it & 1;
+    if (tid == 0 && it + 1 < nb) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      int64_t e0 = (b_begin + it + 1) * kEdgeBlock;
+      int64_t cnt = E - e0 < kEdgeBlock ? E - e0 : kEdgeBlock;
+      bulk_load(buf + (cur ^ 1) * kEdgeBlock, recs + e0, (unsigned)(cnt * sizeof(EdgeRec)),
+                &bars[cur ^ 1]);
+    }
+    bool ok = mbar_wait(&bars[cur], (unsigned)((it >> 1) & 1));
+    if (__syncthreads_or(!ok)) {
+      failed = true;
+      break;
+    }
+    const int64_t e0 = (b_begin + it) * kEdgeBlock;
+    const int cnt = (int)(E - e0 < kEdgeBlock ? E - e0 : kEdgeBlock);
+    const ulonglong2* s = reinterpret_cast<const ulonglong2*>(buf + cur * kEdgeBlock);
+#pragma unroll 2
+    for (int e = 0; e < cnt; ++e) {
+      ulonglong2 r0 = s[2 * e];      // (x1,x2), (y1,y2)
+      ulonglong2 r1 = s[2 * e + 1];  // (z1,z2), (q,pad)
+      uint32_t q = (uint32_t)(r1.y & 0xffffffffull);
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        unsigned long long v = ffma2(c2[k], r1.x, d2[k]);
+        v = ffma2(b2[k], r0.y, v);
+        v = ffma2(a2[k], r0.x, v);
+        float v1, v2;
+        unpack2(v, v1, v2);
+        float sv = fmaxf(fminf(v1, v2), -fmaxf(v1, v2));
+        acc_hi[k] += sv < nhi[k] ? q : 0u;
+        acc_lo[k] += sv < nlo[k] ? q : 0u;
+      }
+    }
+    // Close the block: certain sums go to the total; blocks with band pairs
+    // are queued for the FP64 re-decision and contribute nothing here.
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      if (acc_lo[k] == acc_hi[k]) {
+        tot[k * kScoreThreads + tid] += acc_hi[k];
+      } else {
+        int p = plane_base + k * kScoreThreads + tid;
+        unsigned idx = atomicAdd(recheck_count, 1u);
+        if (idx < recheck_cap) {
+          recheck[idx] = make_uint2((unsigned)p, (unsigned)(b_begin + it));
+        } else {
+          atomicOr(status, kStatusRecheckOverflow);
+        }
+      }
+      acc_lo[k] = acc_hi[k] = 0u;
+    }
+    __syncthreads();
+  }
+  if (failed) {
+    if (tid == 0) atomicOr(status, kStatusMbarrierTimeout);
+    return;
+  }
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    int p = plane_base + k * kScoreThreads + tid;
+    unsigned long long t = tot[k * kScoreThreads + tid];
+    if (p < P && t) atomicAdd(&score_q[p], t);
+  }
+}
+
+// FP64 side value of a point, in the fixed order the oracle uses. Products of
+// two floats are exact in double, so contraction would not change them; the
+// explicit intrinsics pin the order of the three additions.
+__device__ __forceinline__ double side_value64(float4 pl, float x, float y, float z) {
+  double ax = __dmul_rn((double)pl.x, (double)x);
+  double by = __dmul_rn((double)pl.y, (double)y);
+  double cz = __dmul_rn((double)pl.z, (double)z);
+  return __dadd_rn(__dadd_rn(__dadd_rn(ax, by), cz), (double)pl.w);
+}
+
+// One warp per queued (plane, edge block): certain pairs are taken from the
+// same FP32 evaluation as the main kernel, band pairs are decided in FP64.
+__global__ void score_recheck_kernel(const float4* __restrict__ planes,
+                                     const EdgeRec* __restrict__ recs, int64_t E,
+                                     const unsigned* __restrict__ stats,
+                                     const uint2* __restrict__ recheck,
+                                     const unsigned* __restrict__ recheck_count,
+                                     unsigned recheck_cap,
+                                     unsigned long long* __restrict__ score_q) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  unsigned n = *recheck_count;
+  if (n > recheck_cap) n = recheck_cap;
+  const double eps = (double)kSideEps;
+  for (int64_t r = warp; r < n; r += nwarps) {
+    uint2 rec = recheck[r];
+    float4 pl = planes[rec.x];
+    float nlo, nhi;
+    plane_thresholds(pl, stats, nlo, nhi);
+    int64_t e0 = (int64_t)rec.y * kEdgeBlock;
+    int64_t e1 = e0 + kEdgeBlock < E ? e0 + kEdgeBlock : E;
+    unsigned long long sum = 0;
+    for (int64_t e = e0 + lane; e < e1; e += 32) {
+      EdgeRec er = recs[e];
+      float v1 = fmaf(pl.x, er.x1, fmaf(pl.y, er.y1, fmaf(pl.z, er.z1, pl.w)));
+      float v2 = fmaf(pl.x, er.x2, fmaf(pl.y, er.y2, fmaf(pl.z, er.z2, pl.w)));
+      float sv = fmaxf(fminf(v1, v2), -fmaxf(v1, v2));
+      if (sv < nhi) {
+        sum += er.q;
+      } else if (sv < nlo) {
+        double w1 = side_value64(pl, er.x1, er.y1, er.z1);
+        double w2 = side_value64(pl, er.x2, er.y2, er.z2);
+        bool cross = (w1 > eps && w2 < -eps) || (w1 < -eps && w2 > eps);
+        if (cross) sum += er.q;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    if (lane == 0 && sum) atomicAdd(&score_q[rec.x], sum);
+  }
+}
+
+// Scores in float64 (exact: integer sum times a power of two) and the first
+// index of the maximum.
+__global__ void score_finish_kernel(const unsigned long long* __restrict__ score_q, int32_t P,
+                                    const unsigned* __restrict__ stats, double* __restrict__ out,
+                                    float* __restrict__ out_f32, int* __restrict__ argmax) {
+  unsigned cmax = max(stats[0], max(stats[1], stats[2]));
+  int qexp = quantum_exp_from_cmax_bits(cmax);
+  unsigned long long best = 0;
+  int best_i = P > 0 ? 0 : -1;
+  for (int p = threadIdx.x; p < P; p += blockDim.x) {
+    unsigned long long v = score_q[p];
+    double s = ldexp((double)v, qexp);
+    if (out) out[p] = s;
+    if (out_f32) out_f32[p] = (float)s;
+    if (v > best || (v == best && p < best_i)) {
+      best = v;
+      best_i = p;
+    }
+  }
+  __shared__ unsigned long long sv[1024];
+  __shared__ int si[1024];
+  sv[threadIdx.x] = best;
+  si[threadIdx.x] = best_i;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o; o >>= 1) {
+    if ((int)threadIdx.x < o) {
+      unsigned long long v2 = sv[threadIdx.x + o];
+      int i2 = si[threadIdx.x + o];
+      if (v2 > sv[threadIdx.x] || (v2 == sv[threadIdx.x] && i2 >= 0 && i2 < si[threadIdx.x])) {
+        sv[threadIdx.x] = v2;
+        si[threadIdx.x] = i2;
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    argmax[0] = si[0];
+    argmax[1] = qexp;
+  }
+}
+
+// Device-side workspace layout inside kSlotCounters.
+struct ScoreCounters {
+  unsigned stats[4];                 // max |x|, |y|, |z| (float bits)
+  unsigned recheck_count;
+  unsigned pad0[3];
+  unsigned long long skipped;
+  int argmax[2];                     // argmax, qexp
+};
+
+static int planes_per_thread(int32_t P) {
+  if (P > 4 * kScoreThreads * 152 / 2) return 8;
+  if (P > 2 * kScoreThreads * 4) return 4;
+  if (P > kScoreThreads * 2) return 2;
+  return 1;
+}
+
+template <int K>
+static int launch_score(visacd_ctx* ctx, const float4* planes, int32_t P, const EdgeRec* recs,
+                        int64_t E, const unsigned* stats, unsigned long long* sq, uint2* rq,
+                        unsigned* rcount, unsigned rcap) {
+  const int per_cta = kScoreThreads * K;
+  const int groups = (P + per_cta - 1) / per_cta;
+  const int64_t nblocks = (E + kEdgeBlock - 1) / kEdgeBlock;
+  // Aim for ~2 CTAs per SM in total; each CTA streams a contiguous run of blocks.
+  int64_t target_ctas = 2LL * ctx->sm_count;
+  int64_t slices = (target_ctas + groups - 1) / groups;
+  if (slices > nblocks) slices = nblocks;
+  if (slices < 1) slices = 1;
+  int64_t per = (nblocks + slices - 1) / slices;
+  slices = (nblocks + per - 1) / per;
+  size_t smem = 2 * kEdgeBlock * sizeof(EdgeRec) + (size_t)K * kScoreThreads * 8;
+  static bool configured[9] = {false};
+  if (!configured[K]) {
+    VCUDA(cudaFuncSetAttribute(score_planes_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem));
+    configured[K] = true;
+  }
+  dim3 grid((unsigned)slices, (unsigned)groups);
+  VLAUNCH(ctx, kKScore, grid, kScoreThreads, smem, score_planes_kernel<K>, planes, P, recs, E, per,
+          stats, sq, rq, rcount, rcap, ctx->d_status);
+  return VISACD_OK;
+}
+
+// Core of every scoring entry point. All pointers are device pointers.
+static int score_device(visacd_ctx* ctx, const float* d_planes, int32_t P, const float* d_pts,
+                        int32_t N, const uint32_t* d_edges, int64_t E, double* d_scores,
+                        float* d_scores_f32, ScoreCounters** d_counters_out, unsigned rcap) {
+  VTRY(ensure_slot(ctx, kSlotCounters, sizeof(ScoreCounters)));
+  ScoreCounters* cnt = slot<ScoreCounters>(ctx, kSlotCounters);
+  *d_counters_out = cnt;
+  VCUDA(cudaMemsetAsync(cnt, 0, sizeof(ScoreCounters), ctx->stream));
+  VTRY(ensure_slot(ctx, kSlotScoreQ, (size_t)(P > 0 ? P : 1) * sizeof(unsigned long long)));
+  unsigned long long* sq = slot<unsigned long long>(ctx, kSlotScoreQ);
+  if (P > 0) VCUDA(cudaMemsetAsync(sq, 0, (size_t)P * sizeof(unsigned long long), ctx->stream));
+  if (N > 0) {
+    VLAUNCH(ctx, kKPointStats, grid_for(N, 256, 4LL * ctx->sm_count), 256, 0, point_stats_kernel,
+            d_pts, N, cnt->stats);
+  }
+  if (E > 0 && P > 0) {
+    VTRY(ensure_slot(ctx, kSlotEdgePack, (size_t)E * sizeof(EdgeRec)));
+    EdgeRec* recs = slot<EdgeRec>(ctx, kSlotEdgePack);
+    VLAUNCH(ctx, kKPackEdges, grid_for(E, 256, 8LL * ctx->sm_count), 256, 0, pack_edges_kernel,
+            d_pts, N, d_edges, E, cnt->stats, recs, &cnt->skipped);
+    VTRY(ensure_slot(ctx, kSlotRecheck, (size_t)rcap * sizeof(uint2)));
+    uint2* rq = slot<uint2>(ctx, kSlotRecheck);
+    const float4* pl = reinterpret_cast<const float4*>(d_planes);
+    int K = planes_per_thread(P);
+    switch (K) {
+      case 8: VTRY(launch_score<8>(ctx, pl, P, recs, E, cnt->stats, sq, rq, &cnt->recheck_count, rcap)); break;
+      case 4: VTRY(launch_score<4>(ctx, pl, P, recs, E, cnt->stats, sq, rq, &cnt->recheck_count, rcap)); break;
+      case 2: VTRY(launch_score<2>(ctx, pl, P, recs, E, cnt->stats, sq, rq, &cnt->recheck_count, rcap)); break;
+      default: VTRY(launch_score<1>(ctx, pl, P, recs, E, cnt->stats, sq, rq, &cnt->recheck_count, rcap)); break;
+    }
+    VLAUNCH(ctx, kKScoreRecheck, 2 * ctx->sm_count, 256, 0, score_recheck_kernel, pl, recs, E,
+            cnt->stats, rq, &cnt->recheck_count, rcap, sq);
+  }
+  VLAUNCH(ctx, kKScoreFinish, 1, 1024, 0, score_finish_kernel, sq, P, cnt->stats, d_scores,
+          d_scores_f32, cnt->argmax);
+  return VISACD_OK;
+}
+
+static unsigned recheck_capacity(int32_t P, int64_t E) {
+  int64_t nblocks = (E + kEdgeBlock - 1) / kEdgeBlock;
+  int64_t all = (int64_t)P * nblocks;
+  int64_t cap = all / 128;
+  if (cap < (1 << 20)) cap = 1 << 20;
+  if (cap > all) cap = all;
+  if (cap < 1) cap = 1;
+  if (cap > (1LL << 30)) cap = 1LL << 30;
+  return (unsigned)cap;
+}
+
+int score_planes_impl(visacd_ctx* ctx, const float* planes, int32_t P, const float* points,
+                      int32_t N, const uint32_t* edges, int64_t E, int device_ptrs,
+                      double* scores, float* scores_f32, visacd_score_stats* stats) {
+  VCHECK(ctx, VISACD_ERR_INVALID_ARG, "score_planes: null context");
+  VCHECK(P >= 0 && N >= 0 && E >= 0, VISACD_ERR_INVALID_ARG, "score_planes: negative size");
+  VCHECK(P == 0 || planes, VISACD_ERR_INVALID_ARG, "score_planes: planes is NULL");
+  VCHECK(N == 0 || points, VISACD_ERR_INVALID_ARG, "score_planes: points is NULL");
+  VCHECK(E == 0 || edges, VISACD_ERR_INVALID_ARG, "score_planes: edges is NULL");
+  VCHECK(E < (1LL << 40), VISACD_ERR_INVALID_ARG, "score_planes: too many edges");
+  VCUDA(cudaSetDevice(ctx->device));
+  const float *d_planes = planes, *d_pts = points;
+  const uint32_t* d_edges = edges;
+  double* d_scores = scores;
+  float* d_scores_f32 = scores_f32;
+  if (!device_ptrs) {
+    VTRY(ensure_slot(ctx, kSlotPlanes, (size_t)(P > 0 ? P : 1) * 16));
+    VTRY(ensure_slot(ctx, kSlotPoints, (size_t)(N > 0 ? N : 1) * 12));
+    VTRY(ensure_slot(ctx, kSlotEdgesIn, (size_t)(E > 0 ? E : 1) * 8));
+    VTRY(ensure_slot(ctx, kSlotScores, (size_t)(P > 0 ? P : 1) * 8));
+    if (P) VCUDA(cudaMemcpyAsync(ctx->buf[kSlotPlanes].p, planes, (size_t)P * 16, cudaMemcpyHostToDevice, ctx->stream));
+    if (N) VCUDA(cudaMemcpyAsync(ctx->buf[kSlotPoints].p, points, (size_t)N * 12, cudaMemcpyHostToDevice, ctx->stream));
+    if (E) VCUDA(cudaMemcpyAsync(ctx->buf[kSlotEdgesIn].p, edges, (size_t)E * 8, cudaMemcpyHostToDevice, ctx->stream));
+    d_planes = slot<float>(ctx, kSlotPlanes);
+    d_pts = slot<float>(ctx, kSlotPoints);
+    d_edges = slot<uint32_t>(ctx, kSlotEdgesIn);
+    d_scores = slot<double>(ctx, kSlotScores);
+    d_scores_f32 = nullptr;
+  }
+  unsigned rcap = recheck_capacity(P, E);
+  ScoreCounters* cnt = nullptr;
+  VTRY(score_device(ctx, d_planes, P, d_pts, N, d_edges, E, d_scores, d_scores_f32, &cnt, rcap));
+  if (!device_ptrs || stats) {
+    ScoreCounters* h = nullptr;
+    VTRY(pinned(ctx, sizeof(ScoreCounters), (void**)&h));
+    VCUDA(cudaMemcpyAsync(h, cnt, sizeof(ScoreCounters), cudaMemcpyDeviceToHost, ctx->stream));
+    VCUDA(cudaStreamSynchronize(ctx->stream));
+    ScoreCounters hc = *h;
+    if (hc.recheck_count > rcap) {
+      // The FP64 queue overflowed: rerun with room for every queued block.
+      VCUDA(cudaMemsetAsync(ctx->d_status, 0, 4, ctx->stream));
+      rcap = hc.recheck_count;
+      VTRY(score_device(ctx, d_planes, P, d_pts, N, d_edges, E, d_scores, d_scores_f32, &cnt, rcap));
+      VCUDA(cudaMemcpyAsync(h, cnt, sizeof(ScoreCounters), cudaMemcpyDeviceToHost, ctx->stream));
+      VCUDA(cudaStreamSynchronize(ctx->stream));
+      hc = *h;
+    }
+    VTRY(check_status(ctx, "score_planes"));
+    if (!device_ptrs && P) {
+      VCUDA(cudaMemcpyAsync(scores, d_scores, (size_t)P * 8, cudaMemcpyDeviceToHost, ctx->stream));
+      VCUDA(cudaStreamSynchronize(ctx->stream));
+    }
+    if (stats) {
+      stats->quantum_exp = hc.argmax[1];
+      stats->argmax = hc.argmax[0];
+      stats->band_blocks = hc.recheck_count;
+      stats->skipped_edges = (int64_t)hc.skipped;
+    }
+  }
+  return VISACD_OK;
+}
+
+}  // namespace vgpu
+
+using namespace vgpu;
+
+extern "C" int visacd_score_planes(visacd_ctx* ctx, const float* planes, int32_t P,
+                                   const float* points, int32_t N, const uint32_t* edges,
+                                   int64_t E, int device_ptrs, double* scores,
+                                   visacd_score_stats* stats) {
+  return score_planes_impl(ctx, planes, P, points, N, edges, E, device_ptrs, scores, nullptr,
+                           stats);
+}
+
+// ---------------------------------------------------------------------------
+// Drop-in replacement of the reference host wrapper
+// (lib/cuda/plane_intersections.cu:71-133): host pointers, synchronous, float
+// scores, no status return. Runs on a process-wide context on device 0.
+// ---------------------------------------------------------------------------
+#include <mutex>
+#include <vector>
+
+namespace vgpu {
+visacd_ctx* default_ctx() {
+  static std::once_flag once;
+  static visacd_ctx* ctx = nullptr;
+  std::call_once(once, [] {
+    if (visacd_ctx_create(0, nullptr, &ctx) != VISACD_OK) ctx = nullptr;
+  });
+  return ctx;
+}
+}  // namespace vgpu
+
+extern "C" void classify_and_rate_planes(const float* planes, const float* points,
+                                         const unsigned int* edges, float* scores,
+                                         int numPlanes, int numPoints, int numEdges) {
+  if (numPlanes <= 0) return;
+  for (int p = 0; p < numPlanes; ++p) scores[p] = 0.f;
+  visacd_ctx* ctx = vgpu::default_ctx();
+  if (!ctx) return;
+  std::vector<double> s((size_t)numPlanes, 0.0);
+  int rc = score_planes_impl(ctx, planes, numPlanes, points, numPoints < 0 ? 0 : numPoints,
+                             edges, numEdges < 0 ? 0 : numEdges, 0, s.data(), nullptr, nullptr);
+  if (rc != VISACD_OK) return;
+  for (int p = 0; p < numPlanes; ++p) scores[p] = (float)s[p];
+}

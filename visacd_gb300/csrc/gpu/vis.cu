@@ -1,0 +1,696 @@
+// Visibility edges: for each vertex pair (i < j), trace the segment p_i -> p_j
+// against the part itself and against its cage; the pair is an edge iff the
+// segment leaves the cage and does not cross the part.
+//
+// Reference: lib/ptx/ray_segments.cu:49-125 (one OptiX ray per pair, origin
+// p_i, tmin 0.001, tmax |p_j - p_i|, any-hit), lib/src/intersections.cpp:327-385
+// (edge iff hits cage && !hits self; pairs whose endpoints are both old are
+// skipped when is_new is given; edges in row-major (i, j) order).
+//
+// GB300 design:
+//  * Vertices are Morton-sorted; a persistent warp takes an 8 x 4 tile of
+//    (origin, target) positions from a global counter, so the 32 segments of a
+//    warp start and end close together (coherent traversal, dynamic balance).
+//  * Short-stack any-hit traversal of a 64-byte-node LBVH (both child boxes per
+//    node) with a per-thread stack in shared memory; the self test runs first
+//    and the cage test only when the part is not crossed.
+//  * Segment-triangle test: edge functions W = D.(B x C), ... relative to the
+//    origin in FP32 with an a-priori rounding bound (8 roundings per term,
+//    bounded by 17u |D|_1 L^2). Only tests whose signs fall inside the bound
+//    are re-decided in FP64 (the same formula as the oracle).
+//  * Self-test end-vertex policy: triangles incident to i or j are skipped.
+//  * Results land in a bitset over the reference's linear pair index; a
+//    popcount / scan / emit pass compacts it into the row-major edge list.
+#include <math.h>
+
+#include "bvh.cuh"
+
+namespace vgpu {
+
+constexpr int kVisThreads = 128;
+constexpr int kStack = 64;
+constexpr float kU = 5.9604645e-8f;  // 2^-24
+constexpr float kTmin = 0.001f;      // reference tmin (ray_segments.cu:99)
+
+struct VisCounters {
+  unsigned long long work;
+  unsigned long long pairs, edges, self_hits, cage_hits, rechecks, degenerate;
+  unsigned pmin[3], pmax[3];  // orderable point bounds
+  unsigned long long n_rows;  // rows of the tile space (masked mode)
+};
+
+struct Seg {
+  float ox, oy, oz;
+  float dx, dy, dz;
+  float ix, iy, iz;
+  float kw;   // Ew = kw * L^2
+  float len;  // FP32 |D|
+  float qx, qy, qz;
+  int vi, vj;
+};
+
+__device__ __forceinline__ unsigned f2o_v(float f) {
+  unsigned b = __float_as_uint(f);
+  return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float o2f_v(unsigned o) {
+  unsigned b = (o & 0x80000000u) ? (o & 0x7fffffffu) : ~o;
+  return __uint_as_float(b);
+}
+
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+  float r;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+  float r;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+
+__device__ __forceinline__ float inv_guard(float d) {
+  float ad = fabsf(d);
+  float g = ad < 1e-30f ? copysignf(1e-30f, d) : d;
+  return __frcp_rn(g);
+}
+
+__device__ __forceinline__ void make_seg(Seg& s, float3 p, float3 q, int vi, int vj) {
+  s.ox = p.x; s.oy = p.y; s.oz = p.z;
+  s.qx = q.x; s.qy = q.y; s.qz = q.z;
+  s.dx = __fsub_rn(q.x, p.x);
+  s.dy = __fsub_rn(q.y, p.y);
+  s.dz = __fsub_rn(q.z, p.z);
+  s.ix = inv_guard(s.dx);
+  s.iy = inv_guard(s.dy);
+  s.iz = inv_guard(s.dz);
+  float d1 = fabsf(s.dx) + fabsf(s.dy) + fabsf(s.dz);
+  s.kw = 17.0f * kU * d1 * (1.0f + 4.0f * kU);
+  s.len = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(s.dx, s.dx), __fmul_rn(s.dy, s.dy)),
+                               __fmul_rn(s.dz, s.dz)));
+  s.vi = vi;
+  s.vj = vj;
+}
+
+// Conservative slab test of the segment (t in [0, 1]) against a box.
+__device__ __forceinline__ bool box_hit(const Seg& s, float lx, float ly, float lz, float hx,
+                                        float hy, float hz) {
+  float t0x = __fmul_rn(__fsub_rn(lx, s.ox), s.ix), t1x = __fmul_rn(__fsub_rn(hx, s.ox), s.ix);
+  float t0y = __fmul_rn(__fsub_rn(ly, s.oy), s.iy), t1y = __fmul_rn(__fsub_rn(hy, s.oy), s.iy);
+  float t0z = __fmul_rn(__fsub_rn(lz, s.oz), s.iz), t1z = __fmul_rn(__fsub_rn(hz, s.oz), s.iz);
+  float tn = max3f(fminf(t0x, t1x), fminf(t0y, t1y), fmaxf(fminf(t0z, t1z), 0.f));
+  float tf = min3f(fmaxf(t0x, t1x), fmaxf(t0y, t1y), fminf(fmaxf(t0z, t1z), 1.f));
+  tf = fmaf(fabsf(tf), 4e-6f, tf);
+  return tn <= tf;
+}
+
+// FP64 segment-triangle decision from the FP32 inputs; identical formula to the
+// oracle. Explicit round-to-nearest intrinsics keep contraction out.
+__device__ __noinline__ bool tri_test64(float ox, float oy, float oz, float qx, float qy, float qz,
+                                        float4 a, float4 b, float4 c) {
+  double Ax = __dsub_rn(a.x, ox), Ay = __dsub_rn(a.y, oy), Az = __dsub_rn(a.z, oz);
+  double Bx = __dsub_rn(b.x, ox), By = __dsub_rn(b.y, oy), Bz = __dsub_rn(b.z, oz);
+  double Cx = __dsub_rn(c.x, ox), Cy = __dsub_rn(c.y, oy), Cz = __dsub_rn(c.z, oz);
+  double Dx = __dsub_rn(qx, ox), Dy = __dsub_rn(qy, oy), Dz = __dsub_rn(qz, oz);
+  double BCx = __dsub_rn(__dmul_rn(By, Cz), __dmul_rn(Bz, Cy));
+  double BCy = __dsub_rn(__dmul_rn(Bz, Cx), __dmul_rn(Bx, Cz));
+  double BCz = __dsub_rn(__dmul_rn(Bx, Cy), __dmul_rn(By, Cx));
+  double CAx = __dsub_rn(__dmul_rn(Cy, Az), __dmul_rn(Cz, Ay));
+  double CAy = __dsub_rn(__dmul_rn(Cz, Ax), __dmul_rn(Cx, Az));
+  double CAz = __dsub_rn(__dmul_rn(Cx, Ay), __dmul_rn(Cy, Ax));
+  double ABx = __dsub_rn(__dmul_rn(Ay, Bz), __dmul_rn(Az, By));
+  double ABy = __dsub_rn(__dmul_rn(Az, Bx), __dmul_rn(Ax, Bz));
+  double ABz = __dsub_rn(__dmul_rn(Ax, By), __dmul_rn(Ay, Bx));
+  double Wa = __dadd_rn(__dadd_rn(__dmul_rn(Dx, BCx), __dmul_rn(Dy, BCy)), __dmul_rn(Dz, BCz));
+  double Wb = __dadd_rn(__dadd_rn(__dmul_rn(Dx, CAx), __dmul_rn(Dy, CAy)), __dmul_rn(Dz, CAz));
+  double Wc = __dadd_rn(__dadd_rn(__dmul_rn(Dx, ABx), __dmul_rn(Dy, ABy)), __dmul_rn(Dz, ABz));
+  double det = __dadd_rn(__dadd_rn(Wa, Wb), Wc);
+  if (!(det != 0.0)) return false;
+  bool inside = (Wa >= 0.0 && Wb >= 0.0 && Wc >= 0.0) || (Wa <= 0.0 && Wb <= 0.0 && Wc <= 0.0);
+  if (!inside) return false;
+  double vol = __dadd_rn(__dadd_rn(__dmul_rn(Ax, BCx), __dmul_rn(Ay, BCy)), __dmul_rn(Az, BCz));
+  double len = __dsqrt_rn(
+      __dadd_rn(__dadd_rn(__dmul_rn(Dx, Dx), __dmul_rn(Dy, Dy)), __dmul_rn(Dz, Dz)));
+  double tmin = (double)kTmin;
+  double lhs = __dmul_rn(vol, len), rhs = __dmul_rn(tmin, det);
+  if (det > 0.0) return lhs >= rhs && vol <= det;
+  return lhs <= rhs && vol >= det;
+}
+
+// FP32 filter: 1 certain hit, 0 certain miss, 2 undecided (needs FP64).
+__device__ __forceinline__ int tri_test32(const Seg& s, float4 a, float4 b, float4 c) {
+  float Ax = __fsub_rn(a.x, s.ox), Ay = __fsub_rn(a.y, s.oy), Az = __fsub_rn(a.z, s.oz);
+  float Bx = __fsub_rn(b.x, s.ox), By = __fsub_rn(b.y, s.oy), Bz = __fsub_rn(b.z, s.oz);
+  float Cx = __fsub_rn(c.x, s.ox), Cy = __fsub_rn(c.y, s.oy), Cz = __fsub_rn(c.z, s.oz);
+  float L = max3f(max3f(fabsf(Ax), fabsf(Ay), fabsf(Az)), max3f(fabsf(Bx), fabsf(By), fabsf(Bz)),
+                  max3f(fabsf(Cx), fabsf(Cy), fabsf(Cz)));
+  float BCx = By * Cz - Bz * Cy, BCy = Bz * Cx - Bx * Cz, BCz = Bx * Cy - By * Cx;
+  float CAx = Cy * Az - Cz * Ay, CAy = Cz * Ax - Cx * Az, CAz = Cx * Ay - Cy * Ax;
+  float ABx = Ay * Bz - Az * By, ABy = Az * Bx - Ax * Bz, ABz = Ax * By - Ay * Bx;
+  float Wa = s.dx * BCx + s.dy * BCy + s.dz * BCz;
+  float Wb = s.dx * CAx + s.dy * CAy + s.dz * CAz;
+  float Wc = s.dx * ABx + s.dy * ABy + s.dz * ABz;
+  float L2 = L * L;
+  float Ew = s.kw * L2;
+  float mx = max3f(Wa, Wb, Wc), mn = min3f(Wa, Wb, Wc);
+  if (mx > Ew && mn < -Ew) return 0;  // edge functions of strictly opposite sign
+  bool allpos = mn > Ew, allneg = mx < -Ew;
+  if (!(allpos || allneg)) return 2;
+  float sg = allpos ? 1.f : -1.f;
+  float det_s = sg * ((Wa + Wb) + Wc);
+  float vol_s = sg * (Ax * BCx + Ay * BCy + Az * BCz);
+  float Ev = 49.0f * kU * L2 * L;
+  float Edet = 3.0f * Ew + 2.02f * kU * det_s;
+  float g1 = det_s - vol_s;
+  float e1 = Edet + Ev + 2.0f * kU * fabsf(g1);
+  float g2 = vol_s * s.len - kTmin * det_s;
+  float e2 = (Ev + 6.0f * kU * fabsf(vol_s)) * s.len + kTmin * (Edet + 2.0f * kU * det_s) +
+             2.0f * kU * fabsf(g2);
+  if (g1 < -e1 || g2 < -e2) return 0;
+  if (g1 > e1 && g2 > e2) return 1;
+  return 2;
+}
+
+__device__ __forceinline__ bool leaf_hit(const float4* __restrict__ tris, int leaf, const Seg& s,
+                                         unsigned& rechecks) {
+  float4 a = __ldg(&tris[3 * leaf]), b = __ldg(&tris[3 * leaf + 1]), c = __ldg(&tris[3 * leaf + 2]);
+  int ia = __float_as_int(a.w), ib = __float_as_int(b.w), ic = __float_as_int(c.w);
+  if (ia == s.vi || ia == s.vj || ib == s.vi || ib == s.vj || ic == s.vi || ic == s.vj)
+    return false;
+  int r = tri_test32(s, a, b, c);
+  if (r == 2) {
+    ++rechecks;
+    return tri_test64(s.ox, s.oy, s.oz, s.qx, s.qy, s.qz, a, b, c);
+  }
+  return r == 1;
+}
+
+// Any-hit traversal. Returns true on the first hit. `status_bits` collects
+// stack-overflow / iteration-overrun conditions (the pair is then reported as
+// hit and the call fails on the host).
+__device__ bool any_hit(const float4* __restrict__ nodes, const float4* __restrict__ tris,
+                        int nt, const Seg& s, int* __restrict__ stk, int stride,
+                        unsigned& rechecks, unsigned& status_bits) {
+  if (nt <= 0) return false;
+  int node = 0, sp = 0;
+  const int max_iter = 4 * nt + 64;
+  for (int it = 0; it < max_iter; ++it) {
+    float4 n0 = __ldg(&nodes[4 * node]), n1 = __ldg(&nodes[4 * node + 1]);
+    float4 n2 = __ldg(&nodes[4 * node + 2]), n3 = __ldg(&nodes[4 * node + 3]);
+    int l = __float_as_int(n3.x), r = __float_as_int(n3.y);
+    bool hl = box_hit(s, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y);
+    bool hr = box_hit(s, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w);
+    int next = -1;
+    if (hl) {
+      if (l < 0) {
+        if (leaf_hit(tris, ~l, s, rechecks)) return true;
+      } else {
+        next = l;
+      }
+    }
+    if (hr) {
+      if (r < 0) {
+        if (leaf_hit(tris, ~r, s, rechecks)) return true;
+      } else if (next < 0) {
+        next = r;
+      } else {
+        if (sp >= kStack) {
+          status_bits |= kStatusStackOverflow;
+          return true;
+        }
+        stk[sp * stride] = r;
+        ++sp;
+      }
+    }
+    if (next < 0) {
+      if (sp == 0) return false;
+      --sp;
+      next = stk[sp * stride];
+    }
+    node = next;
+  }
+  status_bits |= kStatusTraversalOverrun;
+  return true;
+}
+
+__device__ __forceinline__ int64_t row_start(int64_t i, int64_t n) {
+  return i * (2 * n - i - 1) / 2;
+}
+
+struct VisParams {
+  const float* pts;
+  int32_t n;
+  const uint32_t* rows;    // sorted positions -> original ids (rows of the tile space)
+  const uint32_t* cols;    // same for columns
+  int32_t nr, nc;
+  int triangular;          // 1: rows == cols and pairs with row < col
+  const uint8_t* is_new;   // masked mode
+  const int32_t* newrank;  // masked mode: position of a new vertex in rows, else INT_MAX
+  const float4* self_nodes;
+  const float4* self_tris;
+  int32_t self_nt;
+  const float4* cage_nodes;
+  const float4* cage_tris;
+  int32_t cage_nt;
+  uint32_t* bitset;
+  VisCounters* cnt;
+  unsigned* status;
+  unsigned long long total_tiles;
+  int64_t ntc;  // tile columns
+};
+
+__device__ __forceinline__ void tile_of(const VisParams& P, unsigned long long w, int64_t& tr,
+                                        int64_t& tc) {
+  if (!P.triangular) {
+    tr = (int64_t)(w / (unsigned long long)P.ntc);
+    tc = (int64_t)(w % (unsigned long long)P.ntc);
+    return;
+  }
+  // Row tr holds ntc - 2 tr tiles; start(tr) = tr * (ntc + 1 - tr).
+  const double m = (double)(P.ntc + 1);
+  double disc = m * m - 4.0 * (double)w;
+  int64_t r = (int64_t)((m - sqrt(disc > 0 ? disc : 0.0)) * 0.5);
+  if (r < 0) r = 0;
+  while (r > 0 && (unsigned long long)(r * (P.ntc + 1 - r)) > w) --r;
+  while ((unsigned long long)((r + 1) * (P.ntc + 1 - (r + 1))) <= w && P.ntc - 2 * (r + 1) > 0) ++r;
+  tr = r;
+  tc = 2 * r + (int64_t)(w - (unsigned long long)(r * (P.ntc + 1 - r)));
+}
+
+__global__ void __launch_bounds__(kVisThreads, 4) visibility_kernel(VisParams P) {
+  __shared__ int stk_all[kStack * kVisThreads];
+  int* stk = stk_all + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  unsigned long long c_pairs = 0, c_edges = 0, c_self = 0, c_cage = 0, c_deg = 0;
+  unsigned rechecks = 0, status_bits = 0;
+  const int64_t n = P.n;
+  for (int guard = 0; guard < (1 << 30); ++guard) {
+    unsigned long long w = 0;
+    if (lane == 0) w = atomicAdd(&P.cnt->work, 1ull);
+    w = __shfl_sync(0xffffffffu, w, 0);
+    if (w >= P.total_tiles) break;
+    int64_t tr, tc;
+    tile_of(P, w, tr, tc);
+    const int64_t a = tr * 8 + (lane >> 2);
+    const int64_t b = tc * 4 + (lane & 3);
+    bool valid;
+    uint32_t oi = 0, oj = 0;
+    if (P.triangular) {
+      valid = a < b && b < P.nc;
+      if (valid) {
+        oi = P.rows[a];
+        oj = P.cols[b];
+      }
+    } else {
+      valid = a < P.nr && b < P.nc;
+      if (valid) {
+        oi = P.rows[a];
+        oj = P.cols[b];
+        valid = oi != oj && (!P.is_new[oj] || P.newrank[oj] > a);
+      }
+    }
+    if (!valid) continue;
+    const uint32_t i = min(oi, oj), j = max(oi, oj);
+    ++c_pairs;
+    float3 p = make_float3(P.pts[3 * (int64_t)i], P.pts[3 * (int64_t)i + 1], P.pts[3 * (int64_t)i + 2]);
+    float3 q = make_float3(P.pts[3 * (int64_t)j], P.pts[3 * (int64_t)j + 1], P.pts[3 * (int64_t)j + 2]);
+    Seg s;
+    make_seg(s, p, q, (int)i, (int)j);
+    if (!(s.len > 0.f)) {  // coincident endpoints (or NaN): never an edge
+      ++c_deg;
+      continue;
+    }
+    if (any_hit(P.self_nodes, P.self_tris, P.self_nt, s, stk, kVisThreads, rechecks, status_bits)) {
+      ++c_self;
+      continue;
+    }
+    s.vi = -1;
+    s.vj = -1;
+    if (any_hit(P.cage_nodes, P.cage_tris, P.cage_nt, s, stk, kVisThreads, rechecks, status_bits)) {
+      ++c_cage;
+      ++c_edges;
+      const int64_t k = row_start(i, n) + (int64_t)(j - i - 1);
+      atomicOr(&P.bitset[k >> 5], 1u << (k & 31));
+    }
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    c_pairs += __shfl_xor_sync(0xffffffffu, c_pairs, o);
+    c_edges += __shfl_xor_sync(0xffffffffu, c_edges, o);
+    c_self += __shfl_xor_sync(0xffffffffu, c_self, o);
+    c_cage += __shfl_xor_sync(0xffffffffu, c_cage, o);
+    c_deg += __shfl_xor_sync(0xffffffffu, c_deg, o);
+    rechecks += __shfl_xor_sync(0xffffffffu, rechecks, o);
+    status_bits |= __shfl_xor_sync(0xffffffffu, status_bits, o);
+  }
+  if (lane == 0) {
+    atomicAdd(&P.cnt->pairs, c_pairs);
+    atomicAdd(&P.cnt->edges, c_edges);
+    atomicAdd(&P.cnt->self_hits, c_self);
+    atomicAdd(&P.cnt->cage_hits, c_cage);
+    atomicAdd(&P.cnt->degenerate, c_deg);
+    atomicAdd(&P.cnt->rechecks, (unsigned long long)rechecks);
+    if (status_bits) atomicOr(P.status, status_bits);
+  }
+}
+
+// ---- vertex ordering ------------------------------------------------------
+__global__ void point_bounds_kernel(const float* __restrict__ pts, int32_t n,
+                                    VisCounters* __restrict__ c) {
+  float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      float x = pts[3 * i + a];
+      if (fabsf(x) < INFINITY) {
+        lo[a] = fminf(lo[a], x);
+        hi[a] = fmaxf(hi[a], x);
+      }
+    }
+  }
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      lo[a] = fminf(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
+      hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
+    }
+  }
+  if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      if (lo[a] <= hi[a]) {
+        atomicMin(&c->pmin[a], f2o_v(lo[a]));
+        atomicMax(&c->pmax[a], f2o_v(hi[a]));
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ uint64_t spread21_v(uint64_t x) {
+  x &= 0x1fffffull;
+  x = (x | (x << 32)) & 0x1f00000000ffffull;
+  x = (x | (x << 16)) & 0x1f0000ff0000ffull;
+  x = (x | (x << 8)) & 0x100f00f00f00f00full;
+  x = (x | (x << 4)) & 0x10c30c30c30c30c3ull;
+  x = (x | (x << 2)) & 0x1249249249249249ull;
+  return x;
+}
+
+__global__ void point_morton_kernel(const float* __restrict__ pts, int32_t n,
+                                    const VisCounters* __restrict__ c, uint64_t* __restrict__ keys,
+                                    uint32_t* __restrict__ vals) {
+  float lo[3], sc[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    lo[a] = o2f_v(c->pmin[a]);
+    float ext = o2f_v(c->pmax[a]) - lo[a];
+    sc[a] = ext > 0.f ? 2097151.0f / ext : 0.f;
+  }
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    uint64_t q[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      float x = (pts[3 * i + a] - lo[a]) * sc[a];
+      x = fminf(fmaxf(x, 0.f), 2097151.0f);
+      q[a] = (uint64_t)x;
+    }
+    keys[i] = (spread21_v(q[0]) << 2) | (spread21_v(q[1]) << 1) | spread21_v(q[2]);
+    vals[i] = (uint32_t)i;
+  }
+}
+
+__global__ void new_flags_kernel(const uint32_t* __restrict__ perm, const uint8_t* __restrict__ is_new,
+                                 int32_t n, uint32_t* __restrict__ flags) {
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n;
+       s += (int64_t)gridDim.x * blockDim.x)
+    flags[s] = is_new[perm[s]] ? 1u : 0u;
+}
+
+__global__ void new_rows_kernel(const uint32_t* __restrict__ perm, const uint32_t* __restrict__ flags,
+                                const uint64_t* __restrict__ off, int32_t n,
+                                uint32_t* __restrict__ rows, int32_t* __restrict__ newrank) {
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n;
+       s += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t v = perm[s];
+    if (flags[s]) {
+      rows[off[s]] = v;
+      newrank[v] = (int32_t)off[s];
+    } else {
+      newrank[v] = 0x7fffffff;
+    }
+  }
+}
+
+// ---- bitset compaction ----------------------------------------------------
+__global__ void bit_popc_kernel(const uint32_t* __restrict__ bits, int64_t nw,
+                                uint32_t* __restrict__ counts) {
+  for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < nw;
+       w += (int64_t)gridDim.x * blockDim.x)
+    counts[w] = __popc(bits[w]);
+}
+
+__global__ void bit_emit_kernel(const uint32_t* __restrict__ bits, int64_t nw,
+                                const uint64_t* __restrict__ off, int64_t n,
+                                uint32_t* __restrict__ edges) {
+  for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < nw;
+       w += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t m = bits[w];
+    if (!m) continue;
+    uint64_t o = off[w];
+    const int64_t k0 = w * 32;
+    // Row of k0: largest i with row_start(i) <= k0.
+    double b2 = (double)(2 * n - 1);
+    double disc = b2 * b2 - 8.0 * (double)k0;
+    int64_t i = (int64_t)((b2 - sqrt(disc > 0 ? disc : 0.0)) * 0.5);
+    if (i < 0) i = 0;
+    if (i > n - 2) i = n - 2;
+    while (i > 0 && row_start(i, n) > k0) --i;
+    while (i + 1 <= n - 2 && row_start(i + 1, n) <= k0) ++i;
+    while (m) {
+      int bpos = __ffs(m) - 1;
+      m &= m - 1;
+      int64_t k = k0 + bpos;
+      while (i + 1 <= n - 2 && row_start(i + 1, n) <= k) ++i;
+      int64_t j = k - row_start(i, n) + i + 1;
+      edges[2 * o] = (uint32_t)i;
+      edges[2 * o + 1] = (uint32_t)j;
+      ++o;
+    }
+  }
+}
+
+static int vis_device(visacd_ctx* ctx, const float* d_pts, int32_t n, const uint8_t* d_new,
+                      const visacd_bvh* self_bvh, const visacd_bvh* cage_bvh, int64_t* n_edges,
+                      visacd_vis_stats* stats) {
+  VTRY(ensure_slot(ctx, kSlotCounters, sizeof(VisCounters)));
+  VisCounters* cnt = slot<VisCounters>(ctx, kSlotCounters);
+  VisCounters init;
+  memset(&init, 0, sizeof(init));
+  for (int a = 0; a < 3; ++a) {
+    init.pmin[a] = 0xffffffffu;
+    init.pmax[a] = 0u;
+  }
+  VisCounters* h = nullptr;
+  VTRY(pinned(ctx, sizeof(VisCounters), (void**)&h));
+  *h = init;
+  VCUDA(cudaMemcpyAsync(cnt, h, sizeof(VisCounters), cudaMemcpyHostToDevice, ctx->stream));
+  ctx->last_n_edges = 0;
+
+  const int64_t np = (int64_t)n * (n - 1) / 2;
+  const int64_t nw = (np + 31) / 32;
+  if (n < 2) {
+    if (n_edges) *n_edges = 0;
+    if (stats) memset(stats, 0, sizeof(*stats));
+    return VISACD_OK;
+  }
+  // Morton order of the points.
+  VTRY(ensure_slot(ctx, kSlotVisKeys, (size_t)n * 8));
+  VTRY(ensure_slot(ctx, kSlotVisKeysAlt, (size_t)n * 8));
+  VTRY(ensure_slot(ctx, kSlotVisPerm, (size_t)n * 4));
+  VTRY(ensure_slot(ctx, kSlotVisPermAlt, (size_t)n * 4));
+  uint64_t* keys = slot<uint64_t>(ctx, kSlotVisKeys);
+  uint32_t* perm = slot<uint32_t>(ctx, kSlotVisPerm);
+  const unsigned gp = grid_for(n, 256, 4LL * ctx->sm_count);
+  VLAUNCH(ctx, kKVisPrep, gp, 256, 0, point_bounds_kernel, d_pts, n, cnt);
+  VLAUNCH(ctx, kKVisPrep, gp, 256, 0, point_morton_kernel, d_pts, n, cnt, keys, perm);
+  VTRY(radix_sort_u64(ctx, keys, perm, slot<uint64_t>(ctx, kSlotVisKeysAlt),
+                      slot<uint32_t>(ctx, kSlotVisPermAlt), n, 64));
+
+  VisParams P;
+  memset(&P, 0, sizeof(P));
+  P.pts = d_pts;
+  P.n = n;
+  P.cols = perm;
+  P.nc = n;
+  if (d_new) {
+    // Rows: new vertices in Morton order (compaction by scan).
+    VTRY(ensure_slot(ctx, kSlotWordCounts, (size_t)n * 4));
+    VTRY(ensure_slot(ctx, kSlotWordOffsets, (size_t)(n + 1) * 8));
+    VTRY(ensure_slot(ctx, kSlotVisRank, (size_t)n * 4 + (size_t)n * 4 + 256));
+    uint32_t* flags = slot<uint32_t>(ctx, kSlotWordCounts);
+    uint64_t* off = slot<uint64_t>(ctx, kSlotWordOffsets);
+    uint32_t* rows = slot<uint32_t>(ctx, kSlotVisRank);
+    int32_t* newrank = reinterpret_cast<int32_t*>(rows + ((n + 63) & ~63));
+    VLAUNCH(ctx, kKVisPrep, gp, 256, 0, new_flags_kernel, perm, d_new, n, flags);
+    VTRY(exclusive_scan_u32_to_u64(ctx, flags, off, n));
+    VLAUNCH(ctx, kKVisPrep, gp, 256, 0, new_rows_kernel, perm, flags, off, n, rows, newrank);
+    uint64_t* hn = nullptr;
+    VTRY(pinned(ctx, 8, (void**)&hn));
+    VCUDA(cudaMemcpyAsync(hn, off + n, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    VCUDA(cudaStreamSynchronize(ctx->stream));
+    P.rows = rows;
+    P.nr = (int32_t)*hn;
+    P.triangular = 0;
+    P.is_new = d_new;
+    P.newrank = newrank;
+    P.ntc = (n + 3) / 4;
+    P.total_tiles = (unsigned long long)((P.nr + 7) / 8) * (unsigned long long)P.ntc;
+  } else {
+    P.rows = perm;
+    P.nr = n;
+    P.triangular = 1;
+    P.ntc = (n + 3) / 4;
+    int64_t ntr = (n + 7) / 8;
+    int64_t rmax = (P.ntc + 1) / 2;  // rows with ntc - 2 tr > 0
+    if (rmax > ntr) rmax = ntr;
+    P.total_tiles = (unsigned long long)(rmax * (P.ntc + 1 - rmax));
+  }
+  P.self_nodes = self_bvh->nodes;
+  P.self_tris = self_bvh->tris;
+  P.self_nt = self_bvh->nt;
+  P.cage_nodes = cage_bvh->nodes;
+  P.cage_tris = cage_bvh->tris;
+  P.cage_nt = cage_bvh->nt;
+  VTRY(ensure_slot(ctx, kSlotBitset, (size_t)nw * 4));
+  P.bitset = slot<uint32_t>(ctx, kSlotBitset);
+  VCUDA(cudaMemsetAsync(P.bitset, 0, (size_t)nw * 4, ctx->stream));
+  P.cnt = cnt;
+  P.status = ctx->d_status;
+  if (P.total_tiles > 0) {
+    unsigned grid = (unsigned)(ctx->sm_count * 4);
+    VLAUNCH(ctx, kKVisibility, grid, kVisThreads, 0, visibility_kernel, P);
+  }
+  // Compaction: popcount, scan, emit in linear-pair order.
+  VTRY(ensure_slot(ctx, kSlotWordCounts, (size_t)nw * 4));
+  VTRY(ensure_slot(ctx, kSlotWordOffsets, (size_t)(nw + 1) * 8));
+  uint32_t* wc = slot<uint32_t>(ctx, kSlotWordCounts);
+  uint64_t* wo = slot<uint64_t>(ctx, kSlotWordOffsets);
+  const unsigned gw = grid_for(nw, 256, 16LL * ctx->sm_count);
+  VLAUNCH(ctx, kKBitPopc, gw, 256, 0, bit_popc_kernel, P.bitset, nw, wc);
+  VTRY(exclusive_scan_u32_to_u64(ctx, wc, wo, nw));
+  VCUDA(cudaMemcpyAsync(h, cnt, sizeof(VisCounters), cudaMemcpyDeviceToHost, ctx->stream));
+  VCUDA(cudaStreamSynchronize(ctx->stream));
+  VTRY(check_status(ctx, "visibility"));
+  const int64_t ne = (int64_t)h->edges;
+  VTRY(ensure_slot(ctx, kSlotEdgesOut, (size_t)(ne > 0 ? ne : 1) * 8));
+  if (ne > 0) {
+    VLAUNCH(ctx, kKBitEmit, gw, 256, 0, bit_emit_kernel, P.bitset, nw, wo, (int64_t)n,
+            slot<uint32_t>(ctx, kSlotEdgesOut));
+  }
+  ctx->last_n_edges = ne;
+  if (n_edges) *n_edges = ne;
+  if (stats) {
+    stats->pairs_tested = (int64_t)h->pairs;
+    stats->n_edges = ne;
+    stats->self_hits = (int64_t)h->self_hits;
+    stats->cage_hits = (int64_t)h->cage_hits;
+    stats->fp64_rechecks = (int64_t)h->rechecks;
+    stats->degenerate = (int64_t)h->degenerate;
+  }
+  return VISACD_OK;
+}
+
+int visibility_impl(visacd_ctx* ctx, const float* pts, int32_t n, const uint8_t* is_new,
+                    int device_ptrs, const visacd_bvh* self_bvh, const visacd_bvh* cage_bvh,
+                    int64_t* n_edges, visacd_vis_stats* stats) {
+  VCHECK(ctx && self_bvh && cage_bvh, VISACD_ERR_INVALID_ARG, "visibility: null argument");
+  VCHECK(n >= 0 && (n == 0 || pts), VISACD_ERR_INVALID_ARG, "visibility: bad points");
+  VCHECK(n <= (1 << 24), VISACD_ERR_INVALID_ARG, "visibility: n = %d above the 2^24 limit", n);
+  VCHECK(self_bvh->device == ctx->device && cage_bvh->device == ctx->device,
+         VISACD_ERR_INVALID_ARG, "visibility: BVH built on another device");
+  VCHECK(self_bvh->depth <= kStack && cage_bvh->depth <= kStack, VISACD_ERR_INVALID_ARG,
+         "visibility: BVH depth %d/%d exceeds the traversal stack (%d)", self_bvh->depth,
+         cage_bvh->depth, kStack);
+  VCHECK(self_bvh->nt == 0 || self_bvh->nv == n, VISACD_ERR_INVALID_ARG,
+         "visibility: self BVH has %d vertices, points have %d", self_bvh->nv, n);
+  VCUDA(cudaSetDevice(ctx->device));
+  const float* d_pts = pts;
+  const uint8_t* d_new = is_new;
+  if (!device_ptrs && n > 0) {
+    VTRY(ensure_slot(ctx, kSlotPoints, (size_t)n * 12));
+    VCUDA(cudaMemcpyAsync(ctx->buf[kSlotPoints].p, pts, (size_t)n * 12, cudaMemcpyHostToDevice,
+                          ctx->stream));
+    d_pts = slot<float>(ctx, kSlotPoints);
+    if (is_new) {
+      VTRY(ensure_slot(ctx, kSlotMask, (size_t)n));
+      VCUDA(cudaMemcpyAsync(ctx->buf[kSlotMask].p, is_new, (size_t)n, cudaMemcpyHostToDevice,
+                            ctx->stream));
+      d_new = slot<uint8_t>(ctx, kSlotMask);
+    }
+  }
+  return vis_device(ctx, d_pts, n, d_new, self_bvh, cage_bvh, n_edges, stats);
+}
+
+}  // namespace vgpu
+
+using namespace vgpu;
+
+extern "C" int visacd_visibility(visacd_ctx* ctx, const float* pts, int32_t n,
+                                 const uint8_t* is_new, int device_ptrs,
+                                 const visacd_bvh* self_bvh, const visacd_bvh* cage_bvh,
+                                 int64_t* n_edges, visacd_vis_stats* stats) {
+  return visibility_impl(ctx, pts, n, is_new, device_ptrs, self_bvh, cage_bvh, n_edges, stats);
+}
+
+extern "C" int visacd_visibility_edges(visacd_ctx* ctx, uint32_t* edges_out,
+                                       int64_t capacity_edges) {
+  VCHECK(ctx, VISACD_ERR_INVALID_ARG, "visibility_edges: null context");
+  VCHECK(capacity_edges >= ctx->last_n_edges, VISACD_ERR_CAPACITY,
+         "visibility_edges: capacity %lld < %lld edges", (long long)capacity_edges,
+         (long long)ctx->last_n_edges);
+  if (ctx->last_n_edges == 0) return VISACD_OK;
+  VCHECK(edges_out, VISACD_ERR_INVALID_ARG, "visibility_edges: edges_out is NULL");
+  VCUDA(cudaMemcpyAsync(edges_out, ctx->buf[kSlotEdgesOut].p, (size_t)ctx->last_n_edges * 8,
+                        cudaMemcpyDeviceToHost, ctx->stream));
+  VCUDA(cudaStreamSynchronize(ctx->stream));
+  return VISACD_OK;
+}
+
+extern "C" int visacd_visibility_edges_device(visacd_ctx* ctx, const uint32_t** d_edges,
+                                              int64_t* n_edges) {
+  VCHECK(ctx && d_edges && n_edges, VISACD_ERR_INVALID_ARG, "visibility_edges_device: null");
+  *d_edges = slot<uint32_t>(ctx, kSlotEdgesOut);
+  *n_edges = ctx->last_n_edges;
+  return VISACD_OK;
+}
+
+extern "C" int visacd_compute_intersection_matrix(
+    visacd_ctx* ctx, const float* verts, int32_t nv, const uint32_t* tris, int32_t nt,
+    const uint8_t* is_new, const float* cage_verts, int32_t ncv, const uint32_t* cage_tris,
+    int32_t nct, uint32_t* edges_out, int64_t capacity_edges, int64_t* n_edges,
+    visacd_vis_stats* stats) {
+  VCHECK(ctx && n_edges, VISACD_ERR_INVALID_ARG, "compute_intersection_matrix: null argument");
+  visacd_bvh *sb = nullptr, *cb = nullptr;
+  int rc = bvh_build(ctx, verts, nv, tris, nt, 0, &sb);
+  if (rc == VISACD_OK) rc = bvh_build(ctx, cage_verts, ncv, cage_tris, nct, 0, &cb);
+  if (rc == VISACD_OK) {
+    // A BVH over a mesh with no triangles still needs the vertex count check.
+    if (sb->nt == 0) sb->nv = nv;
+    rc = visibility_impl(ctx, verts, nv, is_new, 0, sb, cb, n_edges, stats);
+  }
+  if (rc == VISACD_OK) {
+    if (*n_edges > capacity_edges) {
+      set_error("compute_intersection_matrix: %lld edges exceed capacity %lld",
+                (long long)*n_edges, (long long)capacity_edges);
+      rc = VISACD_ERR_CAPACITY;
+    } else {
+      rc = visacd_visibility_edges(ctx, edges_out, capacity_edges);
+    }
+  }
+  visacd_bvh_destroy(sb);
+  visacd_bvh_destroy(cb);
+  return rc;
+}
