@@ -1,0 +1,350 @@
+"""Benchmark of the visibility-edge hot path on one GB300.
+
+Workload (the large concave blob): icosphere subdivision 5 (10242 vertices,
+20480 triangles) displaced by 8 seeded Gaussian bumps, all 52,444,161 vertex
+pairs segment-tested against the part and a 0.03 offset cage, then 2500
+candidate planes scored against the resulting visibility edges.
+
+One step = BVH builds (part + cage) + visibility over every pair + edge
+compaction + scoring of the candidate planes + argmax — the GPU hot path of one
+decomposition split (reference: compute_intersection_matrix,
+lib/src/intersections.cpp:327; classify_and_rate_planes,
+lib/cuda/plane_intersections.cu:71).
+
+value: pairs/s with inputs resident in device memory.
+e2e:   the same through the C ABI with host buffers (copies inside the timing).
+Prints one JSON line (rank 0). --impl reference times the CPU restatement of
+the same path (FP64, OpenMP, all host threads) on a bounded sample of rows.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "decomps/sec batched+learned vs plain on 1 GB300 at <=1% concavity gap; pairs/s"
+UNIT = "pairs/s"
+N_PLANES = 2500
+L2_BYTES = 129 * 1024 * 1024
+
+
+def workload(seed: int = 2026):
+    from visacd_gb300 import meshgen
+
+    v, t = meshgen.displaced_blob(5, seed=seed)
+    cv, ct = meshgen.offset_cage(v, t, 0.03)
+    return v, t, cv, ct
+
+
+def bisector_planes(v: np.ndarray, edges: np.ndarray, n: int, seed: int) -> np.ndarray:
+    """Perpendicular-bisector planes of randomly drawn edges (setup only)."""
+    rng = np.random.default_rng(seed)
+    idx = rng.integers(0, len(edges), size=n)
+    p1, p2 = v[edges[idx, 0]], v[edges[idx, 1]]
+    nrm = p2 - p1
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    d = -(nrm * (p1 + p2) * 0.5).sum(1)
+    return np.concatenate([nrm, d[:, None]], 1).astype(np.float32)
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    def __init__(self, index: int = 0):
+        self.index = index
+        self.rows: list[list[str]] = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True,
+                                     text=True, timeout=5).stdout.strip()
+                if out:
+                    self.rows.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self) -> dict:
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4)
+                          if len(r) > 3 + k and r[3 + k].lower().startswith("active")})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(self.rows)}
+
+
+def dist_setup():
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_ours(args) -> dict:
+    import torch
+
+    from visacd_gb300 import _native, build
+
+    world, rank, local = dist_setup()
+    build.build_gpu()
+    stream = torch.cuda.current_stream()
+    ctx = _native.Context(local, stream.cuda_stream)
+    v, t, cv, ct = workload()
+    n = len(v)
+    n_pairs = n * (n - 1) // 2
+    dev = torch.device("cuda", local)
+    d_v = torch.from_numpy(v.astype(np.float32)).to(dev)
+    d_t = torch.from_numpy(t.astype(np.int32)).to(dev)
+    d_cv = torch.from_numpy(cv.astype(np.float32)).to(dev)
+    d_ct = torch.from_numpy(ct.astype(np.int32)).to(dev)
+    lib = _native.lib()
+    import ctypes as C
+
+    # Setup: one pass to get edges for the candidate planes.
+    sb, cb = ctx.bvh(v, t), ctx.bvh(cv, ct)
+    edges0, st0 = ctx.visibility(v, sb, cb)
+    sb.close()
+    cb.close()
+    planes = bisector_planes(v, edges0, N_PLANES, seed=1)
+    d_planes = torch.from_numpy(planes).to(dev)
+    d_scores = torch.empty(N_PLANES, dtype=torch.float64, device=dev)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
+
+    def step_device():
+        h_s, h_c = C.c_void_p(), C.c_void_p()
+        _native._check(lib.visacd_bvh_build(ctx.handle, C.c_void_p(d_v.data_ptr()), n,
+                                            C.c_void_p(d_t.data_ptr()), len(t), 1, C.byref(h_s)), "bvh")
+        _native._check(lib.visacd_bvh_build(ctx.handle, C.c_void_p(d_cv.data_ptr()), len(cv),
+                                            C.c_void_p(d_ct.data_ptr()), len(ct), 1, C.byref(h_c)), "bvh")
+        ne = C.c_int64()
+        _native._check(lib.visacd_visibility(ctx.handle, C.c_void_p(d_v.data_ptr()), n, None, 1, h_s,
+                                             h_c, C.byref(ne), None), "visibility")
+        d_e, ne2 = C.c_void_p(), C.c_int64()
+        lib.visacd_visibility_edges_device(ctx.handle, C.byref(d_e), C.byref(ne2))
+        _native._check(lib.visacd_score_planes(ctx.handle, C.c_void_p(d_planes.data_ptr()), N_PLANES,
+                                               C.c_void_p(d_v.data_ptr()), n, d_e, ne2.value, 1,
+                                               C.c_void_p(d_scores.data_ptr()), None), "score")
+        lib.visacd_bvh_destroy(h_s)
+        lib.visacd_bvh_destroy(h_c)
+        return ne.value
+
+    # e2e: the C ABI with host buffers (pinned inputs copied in, edges + scores out).
+    h_v = torch.from_numpy(v.astype(np.float32)).pin_memory().numpy()
+    h_t = torch.from_numpy(t.astype(np.int32)).pin_memory().numpy().view(np.uint32)
+    h_cv = torch.from_numpy(cv.astype(np.float32)).pin_memory().numpy()
+    h_ct = torch.from_numpy(ct.astype(np.int32)).pin_memory().numpy().view(np.uint32)
+    h_planes = torch.from_numpy(planes).pin_memory().numpy()
+    cap = len(edges0) + 1024
+    h_edges = torch.empty((cap, 2), dtype=torch.int32).pin_memory().numpy().view(np.uint32)
+    h_scores = torch.empty(N_PLANES, dtype=torch.float64).pin_memory().numpy()
+    bytes_in = h_v.nbytes + h_t.nbytes + h_cv.nbytes + h_ct.nbytes + h_planes.nbytes + h_v.nbytes
+
+    def step_e2e():
+        ne = C.c_int64()
+        _native._check(lib.visacd_compute_intersection_matrix(
+            ctx.handle, h_v.ctypes.data, n, h_t.ctypes.data, len(t), None, h_cv.ctypes.data, len(cv),
+            h_ct.ctypes.data, len(ct), h_edges.ctypes.data, cap, C.byref(ne), None), "cim")
+        _native._check(lib.visacd_score_planes(ctx.handle, h_planes.ctypes.data, N_PLANES,
+                                               h_v.ctypes.data, n, h_edges.ctypes.data, ne.value, 0,
+                                               h_scores.ctypes.data, None), "score")
+        return ne.value
+
+    for _ in range(args.warmup):
+        step_device()
+        step_e2e()
+    torch.cuda.synchronize()
+
+    # value: device-resident, CUDA events per step on the launching stream,
+    # L2 flushed (untimed) before each step.
+    ctx.set_timing(True)
+    ctx.reset_times()
+    launches0 = ctx.launches
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            flush.zero_()
+            ev[k][0].record(stream)
+            ne = step_device()
+            ev[k][1].record(stream)
+        torch.cuda.synchronize()
+    barrier(world)
+    ms = sum(a.elapsed_time(b) for a, b in ev)
+    launches = ctx.launches - launches0
+    ktimes = ctx.kernel_times()
+    ctx.set_timing(False)
+    ms = max_over_ranks(ms, world)
+    ms_step = ms / args.steps
+    value = world * n_pairs / (ms_step / 1e3)
+
+    # e2e (host buffers, copies inside the timing).
+    torch.cuda.synchronize()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ne_e = step_e2e()
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps, world)
+    e2e = {"value": world * n_pairs / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(bytes_in + ne_e * 8),
+           "d2h_bytes_per_step": int(ne_e * 8 + N_PLANES * 8), "ms_per_step": e2e_s * 1e3}
+
+    # Roofline of the dominant kernel (visibility traversal): per-launch time from
+    # the CUDA events the library records around each launch.
+    vis_ms, vis_n = ktimes.get("visibility", (0.0, 0))
+    sc_ms, sc_n = ktimes.get("score_planes", (0.0, 0))
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64recheck", "data": "synthetic (seeded)",
+        "config": {"workload": "displaced icosphere s5 blob: 10242 verts, 20480 tris, all 52,444,161 "
+                               "pairs vs part + 0.03 offset cage, then 2500 candidate planes scored",
+                   "pairs": n_pairs, "edges": int(ne), "planes": N_PLANES,
+                   "l2": "flushed before each timed step (256 MB write)",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": e2e,
+        "gpu_launches": int(launches),
+        "kernels_ms_per_step": {k: v[0] / args.steps for k, v in sorted(ktimes.items(), key=lambda kv: -kv[1][0])},
+        "kernel_launches": {k: v[1] for k, v in ktimes.items()},
+        "roofline_visibility": {"kernel": "visibility", "ms_per_launch": vis_ms / max(vis_n, 1),
+                                "pairs_per_s": n_pairs / (vis_ms / max(vis_n, 1) / 1e3) if vis_ms else None},
+        "roofline_scoring": {"kernel": "score_planes", "ms_per_launch": sc_ms / max(sc_n, 1),
+                             "plane_edge_pairs_per_s": N_PLANES * ne / (sc_ms / max(sc_n, 1) / 1e3) if sc_ms else None},
+        "clocks": clk.summary(),
+        "peaks_source": "MEASURED_PEAKS.json" if peaks else "fallback",
+    }
+    return out, rank
+
+
+def run_reference(args) -> dict:
+    """CPU restatement (oracle, FP64, OpenMP) on a bounded sample of pair rows."""
+    import oracle
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return None, rank
+    v, t, cv, ct = workload()
+    n = len(v)
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    rng = np.random.default_rng(0)
+    rows_per_step = 48
+    times, pairs = [], []
+    for k in range(args.warmup + args.steps):
+        r0 = int(rng.integers(0, n - rows_per_step))
+        t0 = time.perf_counter()
+        _, _, st = oracle.visibility(v, t, cv, ct, use_bvh=True, rows=(r0, r0 + rows_per_step))
+        dt = time.perf_counter() - t0
+        if k >= args.warmup:
+            times.append(dt)
+            pairs.append(st["pairs"])
+    value = sum(pairs) / sum(times)
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (seeded)", "impl": "reference",
+           "config": {"workload": "displaced icosphere s5 blob: visibility pairs vs part + 0.03 offset cage",
+                      "sample": f"{rows_per_step} pair rows per step (random start)"},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                            "sample": f"{rows_per_step} consecutive pair rows of the 10242-vertex blob per step"},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    return out, rank
+
+
+def cpu_baseline_sample() -> dict:
+    import oracle
+
+    v, t, cv, ct = workload()
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    n = len(v)
+    t0 = time.perf_counter()
+    total = 0
+    r0 = 0
+    while time.perf_counter() - t0 < 12.0 and r0 < n:
+        _, _, st = oracle.visibility(v, t, cv, ct, use_bvh=True, rows=(r0, r0 + 32))
+        total += st["pairs"]
+        r0 += 331
+    dt = time.perf_counter() - t0
+    return {"value": total / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{total} pairs (rows of 32, stride 331) of the 10242-vertex blob, FP64 BVH oracle"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        out, rank = run_reference(args)
+    else:
+        out, rank = run_ours(args)
+        if rank == 0 and out is not None and not args.no_cpu_baseline and out["n_gpus"] >= 1:
+            out["cpu_baseline"] = cpu_baseline_sample()
+    if rank == 0 and out is not None:
+        print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()
