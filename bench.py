@@ -38,10 +38,13 @@ N_PLANES = 2500
 L2_BYTES = 129 * 1024 * 1024
 
 
-def workload(seed: int = 2026):
+WORKLOADS = {"blob_s5": 5, "blob_s4": 4, "blob_s3": 3}
+
+
+def workload(seed: int = 2026, name: str = "blob_s5"):
     from visacd_gb300 import meshgen
 
-    v, t = meshgen.displaced_blob(5, seed=seed)
+    v, t = meshgen.displaced_blob(WORKLOADS[name], seed=seed)
     cv, ct = meshgen.offset_cage(v, t, 0.03)
     return v, t, cv, ct
 
@@ -144,7 +147,7 @@ def run_ours(args) -> dict:
     build.build_gpu()
     stream = torch.cuda.current_stream()
     ctx = _native.Context(local, stream.cuda_stream)
-    v, t, cv, ct = workload()
+    v, t, cv, ct = workload(name=args.workload)
     n = len(v)
     n_pairs = n * (n - 1) // 2
     dev = torch.device("cuda", local)
@@ -158,6 +161,9 @@ def run_ours(args) -> dict:
     # Setup: one pass to get edges for the candidate planes.
     sb, cb = ctx.bvh(v, t), ctx.bvh(cv, ct)
     edges0, st0 = ctx.visibility(v, sb, cb)
+    bvh_depth = (sb.info()[1], cb.info()[1])
+    # Autotune the visibility launch shape for this shape class (setup, untimed).
+    tuned_variant, tuned_ms = ctx.autotune_visibility(v, sb, cb)
     sb.close()
     cb.close()
     planes = bisector_planes(v, edges0, N_PLANES, seed=1)
@@ -257,6 +263,9 @@ def run_ours(args) -> dict:
         "config": {"workload": "displaced icosphere s5 blob: 10242 verts, 20480 tris, all 52,444,161 "
                                "pairs vs part + 0.03 offset cage, then 2500 candidate planes scored",
                    "pairs": n_pairs, "edges": int(ne), "planes": N_PLANES,
+                   "name": args.workload, "bvh_depth": bvh_depth,
+                   "visibility_counters": st0,
+                   "vis_variant": tuned_variant, "vis_variant_ms": [round(x, 3) for x in tuned_ms],
                    "l2": "flushed before each timed step (256 MB write)",
                    "parallelism": f"replicas x{world}"},
         "e2e": e2e,
@@ -335,6 +344,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="blob_s5", choices=sorted(WORKLOADS))
     args = ap.parse_args()
     if args.impl == "reference":
         out, rank = run_reference(args)

@@ -58,6 +58,8 @@ typedef struct {
   int64_t cage_hits;      /* pairs with no self hit whose segment leaves the cage */
   int64_t fp64_rechecks;  /* segment-triangle tests re-decided in FP64 */
   int64_t degenerate;     /* pairs with coincident endpoints (never edges) */
+  int64_t node_visits;    /* BVH node records fetched (per warp packet) */
+  int64_t tri_tests;      /* segment-triangle tests started (per segment) */
 } visacd_vis_stats;
 
 /* Counters of one scoring call. */
@@ -117,6 +119,21 @@ int visacd_visibility(visacd_ctx* ctx, const float* pts, int32_t n, const uint8_
 int visacd_visibility_edges(visacd_ctx* ctx, uint32_t* edges_out, int64_t capacity_edges);
 /* Device pointer to the last visibility result (valid until the next call). */
 int visacd_visibility_edges_device(visacd_ctx* ctx, const uint32_t** d_edges, int64_t* n_edges);
+
+/* Launch shapes of the visibility kernel (tile rows x columns per warp and the
+   resident-CTA target). variant -1 restores automatic choice: the autotuned
+   shape for the call's shape class if one was measured, else variant 0. */
+int visacd_vis_variant_count(void);
+int visacd_ctx_set_vis_variant(visacd_ctx* ctx, int variant);
+/* Autotuner: times every launch shape on this exact call (twice each, CUDA
+   events on the context stream), caches the fastest for the call's shape class
+   (log2 buckets of n and of both triangle counts, masked or not) in the
+   context, and reports it. ms_per_variant (optional) gets
+   visacd_vis_variant_count() entries. Resets the context's kernel timers. */
+int visacd_autotune_visibility(visacd_ctx* ctx, const float* pts, int32_t n, const uint8_t* is_new,
+                               int device_ptrs, const visacd_bvh* self_bvh,
+                               const visacd_bvh* cage_bvh, int* best_variant,
+                               double* ms_per_variant);
 
 /* One call that builds both BVHs, runs visacd_visibility and copies the edges
    out: the C form of compute_intersection_matrix(mesh, cage). If the edge

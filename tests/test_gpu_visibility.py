@@ -105,3 +105,23 @@ def test_compute_intersection_matrix_one_call(ctx, orc):
     e1, st1 = ctx.compute_intersection_matrix(v, t, cv, ct)
     e2, st2, _, _ = _compare(ctx, orc, v, t, cv, ct)
     np.testing.assert_array_equal(e1, e2)
+
+
+def test_every_launch_shape_gives_the_same_edges(ctx, native, orc):
+    v, t = mg.displaced_blob(3, seed=21)
+    cv, ct = mg.offset_cage(v, t, 0.03)
+    sb, cb = ctx.bvh(v, t), ctx.bvh(cv, ct)
+    ref, _ = ctx.visibility(v, sb, cb)
+    m = (np.arange(len(v)) % 5 == 0).astype(np.uint8)
+    ref_m, _ = ctx.visibility(v, sb, cb, is_new=m)
+    for var in range(native.lib().visacd_vis_variant_count()):
+        ctx.set_vis_variant(var)
+        e, _ = ctx.visibility(v, sb, cb)
+        np.testing.assert_array_equal(e, ref)
+        e, _ = ctx.visibility(v, sb, cb, is_new=m)
+        np.testing.assert_array_equal(e, ref_m)
+    ctx.set_vis_variant(-1)
+    best, ms = ctx.autotune_visibility(v, sb, cb)
+    assert 0 <= best < len(ms) and all(x > 0 for x in ms)
+    e, _ = ctx.visibility(v, sb, cb)
+    np.testing.assert_array_equal(e, ref)

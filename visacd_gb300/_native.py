@@ -21,13 +21,15 @@ EXPORTED = [
     "visacd_bvh_build", "visacd_bvh_destroy", "visacd_bvh_info",
     "visacd_visibility", "visacd_visibility_edges", "visacd_visibility_edges_device",
     "visacd_compute_intersection_matrix",
+    "visacd_vis_variant_count", "visacd_ctx_set_vis_variant", "visacd_autotune_visibility",
     "visacd_score_planes", "classify_and_rate_planes",
 ]
 
 
 class VisStats(C.Structure):
     _fields_ = [("pairs_tested", C.c_int64), ("n_edges", C.c_int64), ("self_hits", C.c_int64),
-                ("cage_hits", C.c_int64), ("fp64_rechecks", C.c_int64), ("degenerate", C.c_int64)]
+                ("cage_hits", C.c_int64), ("fp64_rechecks", C.c_int64), ("degenerate", C.c_int64),
+                ("node_visits", C.c_int64), ("tri_tests", C.c_int64)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -68,6 +70,10 @@ def load() -> C.CDLL:
     lib.visacd_visibility_edges_device.argtypes = [P, C.POINTER(P), C.POINTER(i64)]
     lib.visacd_compute_intersection_matrix.argtypes = [P, P, i32, P, i32, P, P, i32, P, i32, P,
                                                        i64, C.POINTER(i64), C.POINTER(VisStats)]
+    lib.visacd_vis_variant_count.restype = C.c_int
+    lib.visacd_ctx_set_vis_variant.argtypes = [P, C.c_int]
+    lib.visacd_autotune_visibility.argtypes = [P, P, i32, P, C.c_int, P, P, C.POINTER(C.c_int),
+                                               C.POINTER(C.c_double)]
     lib.visacd_score_planes.argtypes = [P, P, i32, P, i32, P, i64, C.c_int, P,
                                         C.POINTER(ScoreStats)]
     lib.classify_and_rate_planes.argtypes = [P, P, P, P, C.c_int, C.c_int, C.c_int]
@@ -172,6 +178,19 @@ class Context:
         out = np.empty((ne.value, 2), dtype=np.uint32)
         _check(lib().visacd_visibility_edges(self._h, _ptr(out), ne.value), "visibility_edges")
         return out, st.as_dict()
+
+    def set_vis_variant(self, v: int) -> None:
+        _check(lib().visacd_ctx_set_vis_variant(self._h, v), "set_vis_variant")
+
+    def autotune_visibility(self, pts, self_bvh: "Bvh", cage_bvh: "Bvh", is_new=None):
+        p = _f32(pts, 3)
+        m = None if is_new is None else np.ascontiguousarray(np.asarray(is_new, dtype=np.uint8))
+        nv = lib().visacd_vis_variant_count()
+        ms = (C.c_double * nv)()
+        best = C.c_int()
+        _check(lib().visacd_autotune_visibility(self._h, _ptr(p), len(p), _ptr(m), 0, self_bvh.handle,
+                                                cage_bvh.handle, C.byref(best), ms), "autotune")
+        return best.value, list(ms)
 
     def compute_intersection_matrix(self, verts, tris, cage_verts, cage_tris, is_new=None,
                                     capacity: int | None = None):

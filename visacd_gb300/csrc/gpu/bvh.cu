@@ -8,7 +8,8 @@
 //     BVHs, octrees and k-d trees" — each internal node finds its key range and
 //     split from common-prefix lengths (ties broken by sorted position).
 //  5. aabb_fit: bottom-up union with one atomic arrival counter per node.
-//  6. node_layout: traversal records of 64 bytes (both child boxes + child ids)
+//  6. node_layout: traversal records of 64 bytes (both child boxes with each
+//     axis stored as a (lo, hi) pair for packed f32x2 slab tests, + child ids)
 //     and leaf triangles of 48 bytes (3 vertices, vertex ids in .w).
 #include "bvh.cuh"
 
@@ -242,9 +243,10 @@ __global__ void node_layout_kernel(const int2* __restrict__ child,
     int2 ch = child[i];
     const float* lb = ch.x < 0 ? &leafbox[6 * (int64_t)(~ch.x)] : &nodebox[6 * (int64_t)ch.x];
     const float* rb = ch.y < 0 ? &leafbox[6 * (int64_t)(~ch.y)] : &nodebox[6 * (int64_t)ch.y];
-    nodes[4 * (int64_t)i + 0] = make_float4(lb[0], lb[1], lb[2], lb[3]);
-    nodes[4 * (int64_t)i + 1] = make_float4(lb[4], lb[5], rb[0], rb[1]);
-    nodes[4 * (int64_t)i + 2] = make_float4(rb[2], rb[3], rb[4], rb[5]);
+    // (lo, hi) per axis side by side: the traversal reads them as f32x2 pairs.
+    nodes[4 * (int64_t)i + 0] = make_float4(lb[0], lb[3], lb[1], lb[4]);
+    nodes[4 * (int64_t)i + 1] = make_float4(lb[2], lb[5], rb[0], rb[3]);
+    nodes[4 * (int64_t)i + 2] = make_float4(rb[1], rb[4], rb[2], rb[5]);
     nodes[4 * (int64_t)i + 3] = make_float4(__int_as_float(ch.x), __int_as_float(ch.y), 0.f, 0.f);
   }
 }
@@ -253,9 +255,9 @@ __global__ void node_layout_kernel(const int2* __restrict__ child,
 // (the duplicate test is harmless and keeps the traversal branch-free).
 __global__ void single_node_kernel(const float* __restrict__ leafbox, float4* __restrict__ nodes) {
   const float* lb = leafbox;
-  nodes[0] = make_float4(lb[0], lb[1], lb[2], lb[3]);
-  nodes[1] = make_float4(lb[4], lb[5], lb[0], lb[1]);
-  nodes[2] = make_float4(lb[2], lb[3], lb[4], lb[5]);
+  nodes[0] = make_float4(lb[0], lb[3], lb[1], lb[4]);
+  nodes[1] = make_float4(lb[2], lb[5], lb[0], lb[3]);
+  nodes[2] = make_float4(lb[1], lb[4], lb[2], lb[5]);
   nodes[3] = make_float4(__int_as_float(~0), __int_as_float(~0), 0.f, 0.f);
 }
 

@@ -5,10 +5,10 @@
 
 #include "common.cuh"
 
-// Node record (64 bytes, 4 x float4):
-//   [0] lmin.x lmin.y lmin.z lmax.x
-//   [1] lmax.y lmax.z rmin.x rmin.y
-//   [2] rmin.z rmax.x rmax.y rmax.z
+// Node record (64 bytes, 4 x float4), each axis a (lo, hi) pair:
+//   [0] L.lo.x L.hi.x L.lo.y L.hi.y
+//   [1] L.lo.z L.hi.z R.lo.x R.hi.x
+//   [2] R.lo.y R.hi.y R.lo.z R.hi.z
 //   [3] left  right  (int bits; >= 0 internal node, < 0 leaf ~sorted_triangle)
 // Leaf triangle record (48 bytes, 3 x float4): vertex xyz + vertex index bits.
 struct visacd_bvh {

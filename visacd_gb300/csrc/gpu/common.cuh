@@ -6,6 +6,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "visacd_gpu.h"
@@ -94,6 +95,7 @@ enum CtxSlot {
   kSlotBuildTris,
   kSlotTmpVerts,
   kSlotTmpTris,
+  kSlotVisRowTiles,
   kSlotCount
 };
 
@@ -109,6 +111,8 @@ struct visacd_ctx {
   int64_t launches = 0;
   int64_t last_n_edges = 0;
   bool timing = false;
+  int vis_variant_override = -1;                  // forced launch shape, -1 = tuned/default
+  std::unordered_map<uint32_t, int> vis_tuned;    // shape class -> autotuned variant
   // Per-kernel timing: events recorded around each launch when timing is on.
   struct Pending {
     int kernel;

@@ -11,9 +11,11 @@
 //  * Vertices are Morton-sorted; a persistent warp takes an 8 x 4 tile of
 //    (origin, target) positions from a global counter, so the 32 segments of a
 //    warp start and end close together (coherent traversal, dynamic balance).
-//  * Short-stack any-hit traversal of a 64-byte-node LBVH (both child boxes per
-//    node) with a per-thread stack in shared memory; the self test runs first
-//    and the cage test only when the part is not crossed.
+//  * Warp-packet any-hit traversal of a 64-byte-node LBVH (both child boxes per
+//    node): the warp follows one path (ballot of per-lane box tests), node
+//    records are broadcast loads, a per-warp stack lives in shared memory; the
+//    self test runs first and the cage test only for lanes whose segment does
+//    not cross the part.
 //  * Segment-triangle test: edge functions W = D.(B x C), ... relative to the
 //    origin in FP32 with an a-priori rounding bound (8 roundings per term,
 //    bounded by 17u |D|_1 L^2). Only tests whose signs fall inside the bound
@@ -35,18 +37,18 @@ constexpr float kTmin = 0.001f;      // reference tmin (ray_segments.cu:99)
 struct VisCounters {
   unsigned long long work;
   unsigned long long pairs, edges, self_hits, cage_hits, rechecks, degenerate;
+  unsigned long long node_visits, tri_tests;  // per-warp node fetches, per-lane triangle tests
   unsigned pmin[3], pmax[3];  // orderable point bounds
   unsigned long long n_rows;  // rows of the tile space (masked mode)
 };
 
 struct Seg {
-  float ox, oy, oz;
+  unsigned long long ox2, oy2, oz2;  // (o, o) pairs for packed slab tests
+  unsigned long long ix2, iy2, iz2;  // (1/d, 1/d) pairs
   float dx, dy, dz;
-  float ix, iy, iz;
-  float kw;   // Ew = kw * L^2
-  float len;  // FP32 |D|
-  float qx, qy, qz;
-  int vi, vj;
+  float kw;      // Ew = kw * L^2
+  int vi, vj;    // endpoint vertex ids (q = pts[vj])
+  bool exclude;  // skip triangles incident to vi or vj (self test)
 };
 
 __device__ __forceinline__ unsigned f2o_v(float f) {
@@ -69,6 +71,30 @@ __device__ __forceinline__ float min3f(float a, float b, float c) {
   return r;
 }
 
+__device__ __forceinline__ unsigned long long pk2(float a, float b) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ float lo2(unsigned long long v) {
+  float a, b;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+  return a;
+}
+__device__ __forceinline__ void up2(unsigned long long v, float& a, float& b) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ unsigned long long sub2(unsigned long long a, unsigned long long b) {
+  unsigned long long r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ unsigned long long mul2(unsigned long long a, unsigned long long b) {
+  unsigned long long r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+
 __device__ __forceinline__ float inv_guard(float d) {
   float ad = fabsf(d);
   float g = ad < 1e-30f ? copysignf(1e-30f, d) : d;
@@ -76,28 +102,36 @@ __device__ __forceinline__ float inv_guard(float d) {
 }
 
 __device__ __forceinline__ void make_seg(Seg& s, float3 p, float3 q, int vi, int vj) {
-  s.ox = p.x; s.oy = p.y; s.oz = p.z;
-  s.qx = q.x; s.qy = q.y; s.qz = q.z;
+  s.ox2 = pk2(p.x, p.x);
+  s.oy2 = pk2(p.y, p.y);
+  s.oz2 = pk2(p.z, p.z);
   s.dx = __fsub_rn(q.x, p.x);
   s.dy = __fsub_rn(q.y, p.y);
   s.dz = __fsub_rn(q.z, p.z);
-  s.ix = inv_guard(s.dx);
-  s.iy = inv_guard(s.dy);
-  s.iz = inv_guard(s.dz);
+  float ix = inv_guard(s.dx), iy = inv_guard(s.dy), iz = inv_guard(s.dz);
+  s.ix2 = pk2(ix, ix);
+  s.iy2 = pk2(iy, iy);
+  s.iz2 = pk2(iz, iz);
   float d1 = fabsf(s.dx) + fabsf(s.dy) + fabsf(s.dz);
   s.kw = 17.0f * kU * d1 * (1.0f + 4.0f * kU);
-  s.len = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(s.dx, s.dx), __fmul_rn(s.dy, s.dy)),
-                               __fmul_rn(s.dz, s.dz)));
   s.vi = vi;
   s.vj = vj;
+  s.exclude = true;
 }
 
-// Conservative slab test of the segment (t in [0, 1]) against a box.
-__device__ __forceinline__ bool box_hit(const Seg& s, float lx, float ly, float lz, float hx,
-                                        float hy, float hz) {
-  float t0x = __fmul_rn(__fsub_rn(lx, s.ox), s.ix), t1x = __fmul_rn(__fsub_rn(hx, s.ox), s.ix);
-  float t0y = __fmul_rn(__fsub_rn(ly, s.oy), s.iy), t1y = __fmul_rn(__fsub_rn(hy, s.oy), s.iy);
-  float t0z = __fmul_rn(__fsub_rn(lz, s.oz), s.iz), t1z = __fmul_rn(__fsub_rn(hz, s.oz), s.iz);
+__device__ __forceinline__ float seg_len(const Seg& s) {
+  return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(s.dx, s.dx), __fmul_rn(s.dy, s.dy)),
+                              __fmul_rn(s.dz, s.dz)));
+}
+
+// Conservative slab test of the segment (t in [0, 1]) against a box given as
+// (lo, hi) pairs per axis; one packed sub + mul per axis.
+__device__ __forceinline__ bool box_hit(const Seg& s, unsigned long long bx, unsigned long long by,
+                                        unsigned long long bz) {
+  float t0x, t1x, t0y, t1y, t0z, t1z;
+  up2(mul2(sub2(bx, s.ox2), s.ix2), t0x, t1x);
+  up2(mul2(sub2(by, s.oy2), s.iy2), t0y, t1y);
+  up2(mul2(sub2(bz, s.oz2), s.iz2), t0z, t1z);
   float tn = max3f(fminf(t0x, t1x), fminf(t0y, t1y), fmaxf(fminf(t0z, t1z), 0.f));
   float tf = min3f(fmaxf(t0x, t1x), fmaxf(t0y, t1y), fminf(fmaxf(t0z, t1z), 1.f));
   tf = fmaf(fabsf(tf), 4e-6f, tf);
@@ -139,9 +173,10 @@ __device__ __noinline__ bool tri_test64(float ox, float oy, float oz, float qx, 
 
 // FP32 filter: 1 certain hit, 0 certain miss, 2 undecided (needs FP64).
 __device__ __forceinline__ int tri_test32(const Seg& s, float4 a, float4 b, float4 c) {
-  float Ax = __fsub_rn(a.x, s.ox), Ay = __fsub_rn(a.y, s.oy), Az = __fsub_rn(a.z, s.oz);
-  float Bx = __fsub_rn(b.x, s.ox), By = __fsub_rn(b.y, s.oy), Bz = __fsub_rn(b.z, s.oz);
-  float Cx = __fsub_rn(c.x, s.ox), Cy = __fsub_rn(c.y, s.oy), Cz = __fsub_rn(c.z, s.oz);
+  const float ox = lo2(s.ox2), oy = lo2(s.oy2), oz = lo2(s.oz2);
+  float Ax = __fsub_rn(a.x, ox), Ay = __fsub_rn(a.y, oy), Az = __fsub_rn(a.z, oz);
+  float Bx = __fsub_rn(b.x, ox), By = __fsub_rn(b.y, oy), Bz = __fsub_rn(b.z, oz);
+  float Cx = __fsub_rn(c.x, ox), Cy = __fsub_rn(c.y, oy), Cz = __fsub_rn(c.z, oz);
   float L = max3f(max3f(fabsf(Ax), fabsf(Ay), fabsf(Az)), max3f(fabsf(Bx), fabsf(By), fabsf(Bz)),
                   max3f(fabsf(Cx), fabsf(Cy), fabsf(Cz)));
   float BCx = By * Cz - Bz * Cy, BCy = Bz * Cx - Bx * Cz, BCz = Bx * Cy - By * Cx;
@@ -163,8 +198,9 @@ __device__ __forceinline__ int tri_test32(const Seg& s, float4 a, float4 b, floa
   float Edet = 3.0f * Ew + 2.02f * kU * det_s;
   float g1 = det_s - vol_s;
   float e1 = Edet + Ev + 2.0f * kU * fabsf(g1);
-  float g2 = vol_s * s.len - kTmin * det_s;
-  float e2 = (Ev + 6.0f * kU * fabsf(vol_s)) * s.len + kTmin * (Edet + 2.0f * kU * det_s) +
+  const float len = seg_len(s);
+  float g2 = vol_s * len - kTmin * det_s;
+  float e2 = (Ev + 6.0f * kU * fabsf(vol_s)) * len + kTmin * (Edet + 2.0f * kU * det_s) +
              2.0f * kU * fabsf(g2);
   if (g1 < -e1 || g2 < -e2) return 0;
   if (g1 > e1 && g2 > e2) return 1;
@@ -172,45 +208,75 @@ __device__ __forceinline__ int tri_test32(const Seg& s, float4 a, float4 b, floa
 }
 
 __device__ __forceinline__ bool leaf_hit(const float4* __restrict__ tris, int leaf, const Seg& s,
-                                         unsigned& rechecks) {
+                                         const float* __restrict__ pts, unsigned& rechecks) {
   float4 a = __ldg(&tris[3 * leaf]), b = __ldg(&tris[3 * leaf + 1]), c = __ldg(&tris[3 * leaf + 2]);
-  int ia = __float_as_int(a.w), ib = __float_as_int(b.w), ic = __float_as_int(c.w);
-  if (ia == s.vi || ia == s.vj || ib == s.vi || ib == s.vj || ic == s.vi || ic == s.vj)
-    return false;
+  if (s.exclude) {
+    int ia = __float_as_int(a.w), ib = __float_as_int(b.w), ic = __float_as_int(c.w);
+    if (ia == s.vi || ia == s.vj || ib == s.vi || ib == s.vj || ic == s.vi || ic == s.vj)
+      return false;
+  }
   int r = tri_test32(s, a, b, c);
   if (r == 2) {
     ++rechecks;
-    return tri_test64(s.ox, s.oy, s.oz, s.qx, s.qy, s.qz, a, b, c);
+    const float* q = pts + 3 * (int64_t)s.vj;
+    return tri_test64(lo2(s.ox2), lo2(s.oy2), lo2(s.oz2), q[0], q[1], q[2], a, b, c);
   }
   return r == 1;
 }
 
-// Any-hit traversal. Returns true on the first hit. `status_bits` collects
-// stack-overflow / iteration-overrun conditions (the pair is then reported as
-// hit and the call fails on the host).
-__device__ bool any_hit(const float4* __restrict__ nodes, const float4* __restrict__ tris,
-                        int nt, const Seg& s, int* __restrict__ stk, int stride,
-                        unsigned& rechecks, unsigned& status_bits) {
+// Warp-packet any-hit traversal. Every lane carries its own segment; the warp
+// walks one path through the BVH: a child is visited when any still-active
+// lane's segment overlaps its box (ballot), node records are fetched at a
+// warp-uniform address (one broadcast transaction), and a lane retires at its
+// first hit. The stack is per warp (shared memory, kStack entries).
+// Returns this lane's hit flag. `status_bits` collects stack-overflow /
+// iteration-overrun conditions (the lane is then reported as hit and the call
+// fails on the host).
+__device__ bool packet_any_hit(const float4* __restrict__ nodes, const float4* __restrict__ tris,
+                               int nt, const Seg& s, const float* __restrict__ pts, bool active,
+                               int* __restrict__ wstk,
+                               unsigned& rechecks, unsigned& status_bits, unsigned& visits,
+                               unsigned& tri_tests) {
+  bool hit = false;
   if (nt <= 0) return false;
+  unsigned live = __ballot_sync(0xffffffffu, active);
+  if (!live) return false;
+  const int lane = threadIdx.x & 31;
   int node = 0, sp = 0;
   const int max_iter = 4 * nt + 64;
   for (int it = 0; it < max_iter; ++it) {
-    float4 n0 = __ldg(&nodes[4 * node]), n1 = __ldg(&nodes[4 * node + 1]);
-    float4 n2 = __ldg(&nodes[4 * node + 2]), n3 = __ldg(&nodes[4 * node + 3]);
-    int l = __float_as_int(n3.x), r = __float_as_int(n3.y);
-    bool hl = box_hit(s, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y);
-    bool hr = box_hit(s, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w);
+    ++visits;
+    const ulonglong2* nd = reinterpret_cast<const ulonglong2*>(nodes) + 4 * node;
+    const ulonglong2 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2);
+    const int2 lr = __ldg(reinterpret_cast<const int2*>(nd + 3));
+    const int l = lr.x, r = lr.y;
+    const bool hl = active && box_hit(s, n0.x, n0.y, n1.x);
+    const bool hr = active && box_hit(s, n1.y, n2.x, n2.y);
+    const unsigned bl = __ballot_sync(0xffffffffu, hl);
+    const unsigned br = __ballot_sync(0xffffffffu, hr);
     int next = -1;
-    if (hl) {
+    if (bl) {
       if (l < 0) {
-        if (leaf_hit(tris, ~l, s, rechecks)) return true;
+        if (hl) {
+          ++tri_tests;
+          if (leaf_hit(tris, ~l, s, pts, rechecks)) {
+            hit = true;
+            active = false;
+          }
+        }
       } else {
         next = l;
       }
     }
-    if (hr) {
+    if (br) {
       if (r < 0) {
-        if (leaf_hit(tris, ~r, s, rechecks)) return true;
+        if (hr && active) {
+          ++tri_tests;
+          if (leaf_hit(tris, ~r, s, pts, rechecks)) {
+            hit = true;
+            active = false;
+          }
+        }
       } else if (next < 0) {
         next = r;
       } else {
@@ -218,15 +284,19 @@ __device__ bool any_hit(const float4* __restrict__ nodes, const float4* __restri
           status_bits |= kStatusStackOverflow;
           return true;
         }
-        stk[sp * stride] = r;
+        if (lane == 0) wstk[sp] = r;
         ++sp;
       }
     }
+    live = __ballot_sync(0xffffffffu, active);
+    if (!live) return hit;
     if (next < 0) {
-      if (sp == 0) return false;
+      if (sp == 0) return hit;
       --sp;
-      next = stk[sp * stride];
+      __syncwarp();
+      next = wstk[sp];
     }
+    __syncwarp();
     node = next;
   }
   status_bits |= kStatusTraversalOverrun;
@@ -256,33 +326,47 @@ struct VisParams {
   VisCounters* cnt;
   unsigned* status;
   unsigned long long total_tiles;
-  int64_t ntc;  // tile columns
+  int64_t ntc;                          // tile columns
+  int64_t ntr;                          // tile rows
+  const unsigned long long* row_start;  // triangular mode: first tile of each tile row
 };
 
+// Work item w -> tile (tr, tc). Rectangle mode: row-major. Triangular mode:
+// tile row tr holds tile columns [floor(TR tr / TC), ntc); row_start is the
+// exclusive prefix of those counts (binary search).
 __device__ __forceinline__ void tile_of(const VisParams& P, unsigned long long w, int64_t& tr,
-                                        int64_t& tc) {
+                                        int64_t& tc, int TR, int TC) {
   if (!P.triangular) {
     tr = (int64_t)(w / (unsigned long long)P.ntc);
     tc = (int64_t)(w % (unsigned long long)P.ntc);
     return;
   }
-  // Row tr holds ntc - 2 tr tiles; start(tr) = tr * (ntc + 1 - tr).
-  const double m = (double)(P.ntc + 1);
-  double disc = m * m - 4.0 * (double)w;
-  int64_t r = (int64_t)((m - sqrt(disc > 0 ? disc : 0.0)) * 0.5);
-  if (r < 0) r = 0;
-  while (r > 0 && (unsigned long long)(r * (P.ntc + 1 - r)) > w) --r;
-  while ((unsigned long long)((r + 1) * (P.ntc + 1 - (r + 1))) <= w && P.ntc - 2 * (r + 1) > 0) ++r;
-  tr = r;
-  tc = 2 * r + (int64_t)(w - (unsigned long long)(r * (P.ntc + 1 - r)));
+  int64_t lo = 0, hi = P.ntr - 1;
+  while (lo < hi) {
+    int64_t mid = (lo + hi + 1) >> 1;
+    if (P.row_start[mid] <= w) lo = mid; else hi = mid - 1;
+  }
+  tr = lo;
+  tc = (tr * TR) / TC + (int64_t)(w - P.row_start[tr]);
 }
 
-__global__ void __launch_bounds__(kVisThreads, 4) visibility_kernel(VisParams P) {
-  __shared__ int stk_all[kStack * kVisThreads];
-  int* stk = stk_all + threadIdx.x;
+__global__ void tile_row_counts_kernel(int64_t ntr, int64_t ntc, int TR, int TC,
+                                       uint32_t* __restrict__ counts) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < ntr;
+       r += (int64_t)gridDim.x * blockDim.x) {
+    int64_t c = ntc - (r * TR) / TC;
+    counts[r] = (uint32_t)(c > 0 ? c : 0);
+  }
+}
+
+template <int TR, int MINB>
+__global__ void __launch_bounds__(kVisThreads, MINB) visibility_kernel(VisParams P) {
+  constexpr int TC = 32 / TR;
+  __shared__ int stk_all[kStack * (kVisThreads / 32)];
   const int lane = threadIdx.x & 31;
+  int* wstk = stk_all + (threadIdx.x >> 5) * kStack;
   unsigned long long c_pairs = 0, c_edges = 0, c_self = 0, c_cage = 0, c_deg = 0;
-  unsigned rechecks = 0, status_bits = 0;
+  unsigned rechecks = 0, status_bits = 0, visits = 0, tri_tests = 0;
   const int64_t n = P.n;
   for (int guard = 0; guard < (1 << 30); ++guard) {
     unsigned long long w = 0;
@@ -290,9 +374,9 @@ __global__ void __launch_bounds__(kVisThreads, 4) visibility_kernel(VisParams P)
     w = __shfl_sync(0xffffffffu, w, 0);
     if (w >= P.total_tiles) break;
     int64_t tr, tc;
-    tile_of(P, w, tr, tc);
-    const int64_t a = tr * 8 + (lane >> 2);
-    const int64_t b = tc * 4 + (lane & 3);
+    tile_of(P, w, tr, tc, TR, TC);
+    const int64_t a = tr * TR + lane / TC;
+    const int64_t b = tc * TC + lane % TC;
     bool valid;
     uint32_t oi = 0, oj = 0;
     if (P.triangular) {
@@ -309,24 +393,29 @@ __global__ void __launch_bounds__(kVisThreads, 4) visibility_kernel(VisParams P)
         valid = oi != oj && (!P.is_new[oj] || P.newrank[oj] > a);
       }
     }
-    if (!valid) continue;
     const uint32_t i = min(oi, oj), j = max(oi, oj);
-    ++c_pairs;
-    float3 p = make_float3(P.pts[3 * (int64_t)i], P.pts[3 * (int64_t)i + 1], P.pts[3 * (int64_t)i + 2]);
-    float3 q = make_float3(P.pts[3 * (int64_t)j], P.pts[3 * (int64_t)j + 1], P.pts[3 * (int64_t)j + 2]);
     Seg s;
+    float3 p = make_float3(0.f, 0.f, 0.f), q = make_float3(0.f, 0.f, 0.f);
+    if (valid) {
+      ++c_pairs;
+      p = make_float3(P.pts[3 * (int64_t)i], P.pts[3 * (int64_t)i + 1], P.pts[3 * (int64_t)i + 2]);
+      q = make_float3(P.pts[3 * (int64_t)j], P.pts[3 * (int64_t)j + 1], P.pts[3 * (int64_t)j + 2]);
+    }
     make_seg(s, p, q, (int)i, (int)j);
-    if (!(s.len > 0.f)) {  // coincident endpoints (or NaN): never an edge
+    bool active = valid;
+    if (valid && !(seg_len(s) > 0.f)) {  // coincident endpoints (or NaN): never an edge
       ++c_deg;
-      continue;
+      active = false;
     }
-    if (any_hit(P.self_nodes, P.self_tris, P.self_nt, s, stk, kVisThreads, rechecks, status_bits)) {
-      ++c_self;
-      continue;
-    }
-    s.vi = -1;
-    s.vj = -1;
-    if (any_hit(P.cage_nodes, P.cage_tris, P.cage_nt, s, stk, kVisThreads, rechecks, status_bits)) {
+    if (!__ballot_sync(0xffffffffu, active)) continue;
+    const bool self_hit = packet_any_hit(P.self_nodes, P.self_tris, P.self_nt, s, P.pts, active, wstk,
+                                         rechecks, status_bits, visits, tri_tests);
+    if (active && self_hit) ++c_self;
+    active = active && !self_hit;
+    s.exclude = false;
+    const bool cage_hit = packet_any_hit(P.cage_nodes, P.cage_tris, P.cage_nt, s, P.pts, active, wstk,
+                                         rechecks, status_bits, visits, tri_tests);
+    if (active && cage_hit) {
       ++c_cage;
       ++c_edges;
       const int64_t k = row_start(i, n) + (int64_t)(j - i - 1);
@@ -341,6 +430,7 @@ __global__ void __launch_bounds__(kVisThreads, 4) visibility_kernel(VisParams P)
     c_cage += __shfl_xor_sync(0xffffffffu, c_cage, o);
     c_deg += __shfl_xor_sync(0xffffffffu, c_deg, o);
     rechecks += __shfl_xor_sync(0xffffffffu, rechecks, o);
+    tri_tests += __shfl_xor_sync(0xffffffffu, tri_tests, o);
     status_bits |= __shfl_xor_sync(0xffffffffu, status_bits, o);
   }
   if (lane == 0) {
@@ -350,6 +440,8 @@ __global__ void __launch_bounds__(kVisThreads, 4) visibility_kernel(VisParams P)
     atomicAdd(&P.cnt->cage_hits, c_cage);
     atomicAdd(&P.cnt->degenerate, c_deg);
     atomicAdd(&P.cnt->rechecks, (unsigned long long)rechecks);
+    atomicAdd(&P.cnt->node_visits, (unsigned long long)visits);
+    atomicAdd(&P.cnt->tri_tests, (unsigned long long)tri_tests);
     if (status_bits) atomicOr(P.status, status_bits);
   }
 }
@@ -482,6 +574,46 @@ __global__ void bit_emit_kernel(const uint32_t* __restrict__ bits, int64_t nw,
   }
 }
 
+// Launch shapes the autotuner chooses from: tile rows (tile = TR x 32/TR pairs
+// per warp) and the minimum resident CTAs per SM (register budget).
+struct VisVariant {
+  int tr;
+  int minb;
+};
+static const VisVariant kVisVariants[] = {{8, 6}, {8, 8}, {4, 6}, {16, 6}, {2, 6}, {1, 6}, {32, 6}};
+constexpr int kNumVisVariants = sizeof(kVisVariants) / sizeof(kVisVariants[0]);
+
+static int launch_vis_variant(visacd_ctx* ctx, int v, const VisParams& P) {
+  const unsigned grid = (unsigned)(ctx->sm_count * kVisVariants[v].minb);
+  switch (v) {
+    case 0: VLAUNCH(ctx, kKVisibility, grid, kVisThreads, 0, (visibility_kernel<8, 6>), P); break;
+    case 1: VLAUNCH(ctx, kKVisibility, grid, kVisThreads, 0, (visibility_kernel<8, 8>), P); break;
+    case 2: VLAUNCH(ctx, kKVisibility, grid, kVisThreads, 0, (visibility_kernel<4, 6>), P); break;
+    case 3: VLAUNCH(ctx, kKVisibility, grid, kVisThreads, 0, (visibility_kernel<16, 6>), P); break;
+    case 4: VLAUNCH(ctx, kKVisibility, grid, kVisThreads, 0, (visibility_kernel<2, 6>), P); break;
+    case 5: VLAUNCH(ctx, kKVisibility, grid, kVisThreads, 0, (visibility_kernel<1, 6>), P); break;
+    default: VLAUNCH(ctx, kKVisibility, grid, kVisThreads, 0, (visibility_kernel<32, 6>), P); break;
+  }
+  return VISACD_OK;
+}
+
+// Shape class of a visibility call: log2 buckets of n and triangle counts, and
+// the masked flag. The autotuner caches its pick per class in the context.
+static uint32_t vis_shape_class(int32_t n, bool masked, const visacd_bvh* a, const visacd_bvh* b) {
+  auto lg = [](int64_t x) { int r = 0; while (x > 1) { x >>= 1; ++r; } return r; };
+  return (uint32_t)lg(n) | ((uint32_t)lg(a->nt + 1) << 6) | ((uint32_t)lg(b->nt + 1) << 12) |
+         ((uint32_t)masked << 18);
+}
+
+static int choose_vis_variant(visacd_ctx* ctx, int32_t n, bool masked, const visacd_bvh* a,
+                              const visacd_bvh* b) {
+  if (ctx->vis_variant_override >= 0 && ctx->vis_variant_override < kNumVisVariants)
+    return ctx->vis_variant_override;
+  auto it = ctx->vis_tuned.find(vis_shape_class(n, masked, a, b));
+  if (it != ctx->vis_tuned.end()) return it->second;
+  return 0;
+}
+
 static int vis_device(visacd_ctx* ctx, const float* d_pts, int32_t n, const uint8_t* d_new,
                       const visacd_bvh* self_bvh, const visacd_bvh* cage_bvh, int64_t* n_edges,
                       visacd_vis_stats* stats) {
@@ -519,12 +651,15 @@ static int vis_device(visacd_ctx* ctx, const float* d_pts, int32_t n, const uint
   VTRY(radix_sort_u64(ctx, keys, perm, slot<uint64_t>(ctx, kSlotVisKeysAlt),
                       slot<uint32_t>(ctx, kSlotVisPermAlt), n, 64));
 
+  const int variant = choose_vis_variant(ctx, n, d_new != nullptr, self_bvh, cage_bvh);
+  const int TR = kVisVariants[variant].tr, TC = 32 / TR;
   VisParams P;
   memset(&P, 0, sizeof(P));
   P.pts = d_pts;
   P.n = n;
   P.cols = perm;
   P.nc = n;
+  P.ntc = (n + TC - 1) / TC;
   if (d_new) {
     // Rows: new vertices in Morton order (compaction by scan).
     VTRY(ensure_slot(ctx, kSlotWordCounts, (size_t)n * 4));
@@ -546,17 +681,25 @@ static int vis_device(visacd_ctx* ctx, const float* d_pts, int32_t n, const uint
     P.triangular = 0;
     P.is_new = d_new;
     P.newrank = newrank;
-    P.ntc = (n + 3) / 4;
-    P.total_tiles = (unsigned long long)((P.nr + 7) / 8) * (unsigned long long)P.ntc;
+    P.ntr = (P.nr + TR - 1) / TR;
+    P.total_tiles = (unsigned long long)P.ntr * (unsigned long long)P.ntc;
   } else {
     P.rows = perm;
     P.nr = n;
     P.triangular = 1;
-    P.ntc = (n + 3) / 4;
-    int64_t ntr = (n + 7) / 8;
-    int64_t rmax = (P.ntc + 1) / 2;  // rows with ntc - 2 tr > 0
-    if (rmax > ntr) rmax = ntr;
-    P.total_tiles = (unsigned long long)(rmax * (P.ntc + 1 - rmax));
+    P.ntr = (n + TR - 1) / TR;
+    VTRY(ensure_slot(ctx, kSlotVisRowTiles, (size_t)P.ntr * 4 + (size_t)(P.ntr + 1) * 8 + 256));
+    uint32_t* rc = slot<uint32_t>(ctx, kSlotVisRowTiles);
+    uint64_t* rs = reinterpret_cast<uint64_t*>(rc + ((P.ntr + 63) & ~63LL));
+    VLAUNCH(ctx, kKVisPrep, grid_for(P.ntr, 256, 4LL * ctx->sm_count), 256, 0,
+            tile_row_counts_kernel, P.ntr, P.ntc, TR, TC, rc);
+    VTRY(exclusive_scan_u32_to_u64(ctx, rc, rs, P.ntr));
+    uint64_t* ht = nullptr;
+    VTRY(pinned(ctx, 8, (void**)&ht));
+    VCUDA(cudaMemcpyAsync(ht, rs + P.ntr, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    VCUDA(cudaStreamSynchronize(ctx->stream));
+    P.row_start = reinterpret_cast<const unsigned long long*>(rs);
+    P.total_tiles = (unsigned long long)*ht;
   }
   P.self_nodes = self_bvh->nodes;
   P.self_tris = self_bvh->tris;
@@ -569,10 +712,7 @@ static int vis_device(visacd_ctx* ctx, const float* d_pts, int32_t n, const uint
   VCUDA(cudaMemsetAsync(P.bitset, 0, (size_t)nw * 4, ctx->stream));
   P.cnt = cnt;
   P.status = ctx->d_status;
-  if (P.total_tiles > 0) {
-    unsigned grid = (unsigned)(ctx->sm_count * 4);
-    VLAUNCH(ctx, kKVisibility, grid, kVisThreads, 0, visibility_kernel, P);
-  }
+  if (P.total_tiles > 0) VTRY(launch_vis_variant(ctx, variant, P));
   // Compaction: popcount, scan, emit in linear-pair order.
   VTRY(ensure_slot(ctx, kSlotWordCounts, (size_t)nw * 4));
   VTRY(ensure_slot(ctx, kSlotWordOffsets, (size_t)(nw + 1) * 8));
@@ -599,6 +739,8 @@ static int vis_device(visacd_ctx* ctx, const float* d_pts, int32_t n, const uint
     stats->cage_hits = (int64_t)h->cage_hits;
     stats->fp64_rechecks = (int64_t)h->rechecks;
     stats->degenerate = (int64_t)h->degenerate;
+    stats->node_visits = (int64_t)h->node_visits;
+    stats->tri_tests = (int64_t)h->tri_tests;
   }
   return VISACD_OK;
 }
@@ -693,4 +835,59 @@ extern "C" int visacd_compute_intersection_matrix(
   visacd_bvh_destroy(sb);
   visacd_bvh_destroy(cb);
   return rc;
+}
+
+// ---------------------------------------------------------------------------
+// Launch-shape control and the visibility autotuner.
+// ---------------------------------------------------------------------------
+extern "C" int visacd_vis_variant_count(void) { return kNumVisVariants; }
+
+extern "C" int visacd_ctx_set_vis_variant(visacd_ctx* ctx, int variant) {
+  VCHECK(ctx, VISACD_ERR_INVALID_ARG, "set_vis_variant: null context");
+  VCHECK(variant >= -1 && variant < kNumVisVariants, VISACD_ERR_INVALID_ARG,
+         "set_vis_variant: variant %d out of range", variant);
+  ctx->vis_variant_override = variant;
+  return VISACD_OK;
+}
+
+extern "C" int visacd_autotune_visibility(visacd_ctx* ctx, const float* pts, int32_t n,
+                                          const uint8_t* is_new, int device_ptrs,
+                                          const visacd_bvh* self_bvh, const visacd_bvh* cage_bvh,
+                                          int* best_variant, double* ms_per_variant) {
+  VCHECK(ctx && self_bvh && cage_bvh, VISACD_ERR_INVALID_ARG, "autotune: null argument");
+  const int saved_override = ctx->vis_variant_override;
+  const bool saved_timing = ctx->timing;
+  int best = 0;
+  double best_ms = 1e300;
+  int rc = VISACD_OK;
+  for (int v = 0; v < kNumVisVariants && rc == VISACD_OK; ++v) {
+    ctx->vis_variant_override = v;
+    double ms = 0.0;
+    for (int rep = 0; rep < 2 && rc == VISACD_OK; ++rep) {
+      ctx->timing = true;
+      rc = visacd_ctx_reset_times(ctx);
+      if (rc == VISACD_OK)
+        rc = visibility_impl(ctx, pts, n, is_new, device_ptrs, self_bvh, cage_bvh, nullptr, nullptr);
+      const char* names[64];
+      double t[64];
+      int64_t cnt[64];
+      int nk = 0;
+      if (rc == VISACD_OK) rc = visacd_ctx_kernel_times(ctx, names, t, cnt, 64, &nk);
+      ms = 0.0;
+      for (int k = 0; k < nk && k < 64; ++k)
+        if (strcmp(names[k], kernel_name(kKVisibility)) == 0) ms = t[k];
+    }
+    if (ms_per_variant) ms_per_variant[v] = ms;
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = v;
+    }
+  }
+  ctx->vis_variant_override = saved_override;
+  ctx->timing = saved_timing;
+  visacd_ctx_reset_times(ctx);
+  if (rc != VISACD_OK) return rc;
+  ctx->vis_tuned[vis_shape_class(n, is_new != nullptr, self_bvh, cage_bvh)] = best;
+  if (best_variant) *best_variant = best;
+  return VISACD_OK;
 }
