@@ -161,6 +161,23 @@ int visacd_score_planes(visacd_ctx* ctx, const float* planes, int32_t P, const f
                         int32_t N, const uint32_t* edges, int64_t E, int device_ptrs,
                         double* scores, visacd_score_stats* stats);
 
+/* Allocation-free variant of visacd_score_planes. No counterpart in the
+   reference: it exists for callers that cannot allocate — code running under a
+   fixed, pre-reserved memory budget, or a latency-bound loop where cudaMalloc's
+   implicit synchronisation is not acceptable. It calls no cudaMalloc/cudaFree
+   or other allocating routine: all scratch lives in one static device array
+   of 10,518,784 bytes that every GPU loading the library reserves until exit.
+   Inputs (planes P x 4, points N x 3, edges E x 2) and outputs (scores P
+   float64, argmax one int32 or NULL) are device pointers; the call is
+   asynchronous on cuda_stream (NULL = the legacy default stream). Limits:
+   P <= 4096 and E <= 65536, larger sizes return VISACD_ERR_CAPACITY. The first
+   call on a device looks up the array's device address (do it before any
+   stream capture). Calls share the array: calls that overlap on the GPU race,
+   so serialise them. Results equal visacd_score_planes bit for bit. */
+int visacd_score_planes_noalloc(const float* planes, int32_t P, const float* points, int32_t N,
+                                const uint32_t* edges, int64_t E, double* scores,
+                                int32_t* argmax, void* cuda_stream);
+
 /* Drop-in for the reference's host wrapper: same signature and meaning
    (host pointers, synchronous, float scores), run on a process-wide default
    context on device 0. Errors are recorded in visacd_last_error() and leave

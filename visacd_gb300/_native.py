@@ -22,7 +22,7 @@ EXPORTED = [
     "visacd_visibility", "visacd_visibility_edges", "visacd_visibility_edges_device",
     "visacd_compute_intersection_matrix",
     "visacd_vis_variant_count", "visacd_ctx_set_vis_variant", "visacd_autotune_visibility",
-    "visacd_score_planes", "classify_and_rate_planes",
+    "visacd_score_planes", "visacd_score_planes_noalloc", "classify_and_rate_planes",
 ]
 
 
@@ -76,6 +76,7 @@ def load() -> C.CDLL:
                                                C.POINTER(C.c_double)]
     lib.visacd_score_planes.argtypes = [P, P, i32, P, i32, P, i64, C.c_int, P,
                                         C.POINTER(ScoreStats)]
+    lib.visacd_score_planes_noalloc.argtypes = [P, i32, P, i32, P, i64, P, P, P]
     lib.classify_and_rate_planes.argtypes = [P, P, P, P, C.c_int, C.c_int, C.c_int]
     lib.classify_and_rate_planes.restype = None
     return lib

@@ -594,3 +594,153 @@ extern "C" void classify_and_rate_planes(const float* planes, const float* point
   if (rc != VISACD_OK) return;
   for (int p = 0; p < numPlanes; ++p) scores[p] = (float)s[p];
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free plane scoring.
+//
+// For callers that must not allocate device or host memory from inside this
+// library: code that runs under a caller-owned memory budget (a fixed arena
+// reserved at start-up, a real-time loop where cudaMalloc's implicit device
+// synchronisation and unbounded latency are not allowed), or code that is not
+// allowed to touch the allocator at all while other work owns the device.
+// Inputs and outputs are the caller's device buffers; every byte of scratch
+// (packed edge records, integer score accumulators, the FP64 re-decision
+// queue, counters) lives in one file-scope device array that the library image
+// reserves on every GPU that loads it, until the process exits.
+//
+// Limits: E <= 65536 edges and P <= 4096 planes (10,518,784 bytes of scratch).
+// The queue holds every (plane, edge block) pair, so it cannot overflow.
+// All calls share the array and it keeps the previous call's contents: the
+// accumulators and counters are cleared on the stream at the start of each
+// call, and calls whose work overlaps on the GPU (different streams, or
+// different host threads) race on it — serialise them.
+// ---------------------------------------------------------------------------
+namespace vgpu {
+
+constexpr int64_t kNoAllocMaxEdges = 65536;
+constexpr int32_t kNoAllocMaxPlanes = 4096;
+constexpr int64_t kNoAllocMaxBlocks = kNoAllocMaxEdges / kEdgeBlock;
+constexpr size_t kNoAllocCountersBytes = 256;
+constexpr size_t kNoAllocScoreQBytes = (size_t)kNoAllocMaxPlanes * 8;
+constexpr size_t kNoAllocPackBytes = (size_t)kNoAllocMaxEdges * sizeof(EdgeRec);
+constexpr size_t kNoAllocQueueBytes = (size_t)kNoAllocMaxPlanes * kNoAllocMaxBlocks * sizeof(uint2);
+constexpr size_t kNoAllocBytes =
+    kNoAllocCountersBytes + kNoAllocScoreQBytes + kNoAllocPackBytes + kNoAllocQueueBytes;
+static_assert(sizeof(ScoreCounters) <= kNoAllocCountersBytes, "counters must fit");
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+// Device address of the scratch array, looked up once per device with that
+// device current (in host code the symbol is only a host-side stand-in).
+static unsigned char* noalloc_scratch_ptr(int device, int* rc) {
+  static std::mutex mu;
+  static unsigned char* ptrs[64] = {nullptr};
+  static int sms[64] = {0};
+  std::lock_guard<std::mutex> lock(mu);
+  if (device < 0 || device >= 64) {
+    set_error("score_planes_noalloc: device %d out of range", device);
+    *rc = VISACD_ERR_INVALID_ARG;
+    return nullptr;
+  }
+  if (!ptrs[device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) {
+      set_error("score_planes_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+      *rc = VISACD_ERR_CUDA;
+      return nullptr;
+    }
+    ptrs[device] = static_cast<unsigned char*>(p);
+  }
+  *rc = VISACD_OK;
+  return ptrs[device];
+}
+
+static int noalloc_sm_count(int device) {
+  int sm = 0;
+  if (cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) sm = 0;
+  return sm > 0 ? sm : 1;
+}
+
+template <int K>
+static int noalloc_launch_score(cudaStream_t st, int sm_count, const float4* planes, int32_t P,
+                                const EdgeRec* recs, int64_t E, const unsigned* stats,
+                                unsigned long long* sq, uint2* rq, unsigned* rcount, unsigned rcap,
+                                unsigned* status) {
+  const int per_cta = kScoreThreads * K;
+  const int groups = (P + per_cta - 1) / per_cta;
+  const int64_t nblocks = (E + kEdgeBlock - 1) / kEdgeBlock;
+  int64_t slices = (2LL * sm_count + groups - 1) / groups;
+  if (slices > nblocks) slices = nblocks;
+  if (slices < 1) slices = 1;
+  int64_t per = (nblocks + slices - 1) / slices;
+  slices = (nblocks + per - 1) / per;
+  size_t smem = 2 * kEdgeBlock * sizeof(EdgeRec) + (size_t)K * kScoreThreads * 8;
+  VCUDA(cudaFuncSetAttribute(score_planes_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem));
+  score_planes_kernel<K><<<dim3((unsigned)slices, (unsigned)groups), kScoreThreads, smem, st>>>(
+      planes, P, recs, E, per, stats, sq, rq, rcount, rcap, status);
+  VCUDA(cudaGetLastError());
+  return VISACD_OK;
+}
+
+}  // namespace vgpu
+
+extern "C" int visacd_score_planes_noalloc(const float* d_planes, int32_t P, const float* d_points,
+                                           int32_t N, const uint32_t* d_edges, int64_t E,
+                                           double* d_scores, int32_t* d_argmax,
+                                           void* cuda_stream) {
+  using namespace vgpu;
+  VCHECK(P >= 0 && N >= 0 && E >= 0, VISACD_ERR_INVALID_ARG, "score_planes_noalloc: negative size");
+  VCHECK(P <= kNoAllocMaxPlanes, VISACD_ERR_CAPACITY,
+         "score_planes_noalloc: P = %d planes exceeds the allocation-free limit of %d", P,
+         kNoAllocMaxPlanes);
+  VCHECK(E <= kNoAllocMaxEdges, VISACD_ERR_CAPACITY,
+         "score_planes_noalloc: E = %lld edges exceeds the allocation-free limit of %lld",
+         (long long)E, (long long)kNoAllocMaxEdges);
+  VCHECK(P == 0 || (d_planes && d_scores), VISACD_ERR_INVALID_ARG,
+         "score_planes_noalloc: planes or scores is NULL");
+  VCHECK(N == 0 || d_points, VISACD_ERR_INVALID_ARG, "score_planes_noalloc: points is NULL");
+  VCHECK(E == 0 || d_edges, VISACD_ERR_INVALID_ARG, "score_planes_noalloc: edges is NULL");
+  int device = 0;
+  VCUDA(cudaGetDevice(&device));
+  int rc = VISACD_OK;
+  unsigned char* base = noalloc_scratch_ptr(device, &rc);
+  if (!base) return rc;
+  cudaStream_t st = (cudaStream_t)cuda_stream;
+  ScoreCounters* cnt = reinterpret_cast<ScoreCounters*>(base);
+  unsigned long long* sq = reinterpret_cast<unsigned long long*>(base + kNoAllocCountersBytes);
+  EdgeRec* recs = reinterpret_cast<EdgeRec*>(base + kNoAllocCountersBytes + kNoAllocScoreQBytes);
+  uint2* rq = reinterpret_cast<uint2*>(base + kNoAllocCountersBytes + kNoAllocScoreQBytes +
+                                       kNoAllocPackBytes);
+  // The status word shares the counters block (its spare tail).
+  unsigned* status = reinterpret_cast<unsigned*>(base + kNoAllocCountersBytes - 16);
+  VCUDA(cudaMemsetAsync(base, 0, kNoAllocCountersBytes + (size_t)(P > 0 ? P : 1) * 8, st));
+  const int sm = noalloc_sm_count(device);
+  if (N > 0) {
+    point_stats_kernel<<<grid_for(N, 256, 4LL * sm), 256, 0, st>>>(d_points, N, cnt->stats);
+    VCUDA(cudaGetLastError());
+  }
+  if (E > 0 && P > 0) {
+    pack_edges_kernel<<<grid_for(E, 256, 8LL * sm), 256, 0, st>>>(d_points, N, d_edges, E,
+                                                                   cnt->stats, recs, &cnt->skipped);
+    VCUDA(cudaGetLastError());
+    const unsigned rcap = (unsigned)((int64_t)P * ((E + kEdgeBlock - 1) / kEdgeBlock));
+    const float4* pl = reinterpret_cast<const float4*>(d_planes);
+    switch (planes_per_thread(P)) {
+      case 8: VTRY(noalloc_launch_score<8>(st, sm, pl, P, recs, E, cnt->stats, sq, rq, &cnt->recheck_count, rcap, status)); break;
+      case 4: VTRY(noalloc_launch_score<4>(st, sm, pl, P, recs, E, cnt->stats, sq, rq, &cnt->recheck_count, rcap, status)); break;
+      case 2: VTRY(noalloc_launch_score<2>(st, sm, pl, P, recs, E, cnt->stats, sq, rq, &cnt->recheck_count, rcap, status)); break;
+      default: VTRY(noalloc_launch_score<1>(st, sm, pl, P, recs, E, cnt->stats, sq, rq, &cnt->recheck_count, rcap, status)); break;
+    }
+    score_recheck_kernel<<<2 * sm, 256, 0, st>>>(pl, recs, E, cnt->stats, rq, &cnt->recheck_count,
+                                                 rcap, sq);
+    VCUDA(cudaGetLastError());
+  }
+  score_finish_kernel<<<1, 1024, 0, st>>>(sq, P, cnt->stats, d_scores, nullptr, cnt->argmax);
+  VCUDA(cudaGetLastError());
+  if (d_argmax) {
+    VCUDA(cudaMemcpyAsync(d_argmax, cnt->argmax, sizeof(int32_t), cudaMemcpyDeviceToDevice, st));
+  }
+  return VISACD_OK;
+}
