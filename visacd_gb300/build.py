@@ -59,8 +59,55 @@ def build_gpu(force: bool = False) -> Path:
     return GPU_LIB
 
 
+HOST_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-fvisibility=hidden"]
+
+
+def _pybind_include() -> str:
+    """pybind11 headers: the copy shipped with torch (present on every box) or
+    the pybind11 package."""
+    import importlib.util
+
+    spec = importlib.util.find_spec("torch")
+    if spec and spec.submodule_search_locations:
+        inc = Path(list(spec.submodule_search_locations)[0]) / "include"
+        if (inc / "pybind11" / "pybind11.h").exists():
+            return str(inc)
+    import pybind11  # noqa: WPS433
+
+    return pybind11.get_include()
+
+
+def host_module_path() -> Path:
+    return PKG / ("visacd" + sysconfig.get_config_var("EXT_SUFFIX"))
+
+
+def build_host(force: bool = False) -> Path:
+    """Compile csrc/host/*.cpp into the pybind11 module `visacd` (linked to the
+    kernel library through the C ABI)."""
+    build_gpu(force)
+    BUILD.mkdir(exist_ok=True)
+    inc = ["-I" + str(INCLUDE), "-I" + sysconfig.get_paths()["include"], "-I" + _pybind_include()]
+    sources = sorted(HOST_SRC.glob("*.cpp"))
+    headers = sorted(HOST_SRC.glob("*.hpp")) + [INCLUDE / "visacd_gpu.h"]
+    objs, jobs = [], []
+    for s in sources:
+        o = BUILD / ("host_" + s.stem + ".o")
+        objs.append(o)
+        if force or _stale(o, [s] + headers):
+            jobs.append(["g++", *HOST_FLAGS, *inc, "-c", str(s), "-o", str(o)])
+    if jobs:
+        with cf.ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:
+            list(ex.map(_run, jobs))
+    out = host_module_path()
+    if force or jobs or _stale(out, objs + [GPU_LIB]):
+        _run(["g++", "-shared", "-fopenmp", "-o", str(out), *map(str, objs), f"-L{PKG}",
+              "-lvisacd_gpu", "-Wl,-rpath,$ORIGIN"])
+    return out
+
+
 def build_all(force: bool = False) -> None:
     build_gpu(force)
+    build_host(force)
 
 
 if __name__ == "__main__":

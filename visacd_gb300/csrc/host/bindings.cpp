@@ -1,0 +1,198 @@
+// pybind11 module `visacd`: the reference's Python surface (lib/bindings.cpp:14-70)
+// — Mesh, VecArray3d, VecArray3i, MeshList, Config, make_vecarray3i, set_seed,
+// config (a reference to the process-wide configuration), ProcessResult,
+// process — plus underscore-prefixed helpers used by this project's tests and
+// benchmarks.
+#include <pybind11/numpy.h>
+#include <pybind11/pybind11.h>
+#include <pybind11/stl.h>
+#include <pybind11/stl_bind.h>
+
+#include "geometry.hpp"
+#include "gpu_bridge.hpp"
+#include "process.hpp"
+
+namespace py = pybind11;
+using namespace visacd;
+
+PYBIND11_MAKE_OPAQUE(std::vector<std::array<double, 3>>);
+PYBIND11_MAKE_OPAQUE(std::vector<std::array<int, 3>>);
+PYBIND11_MAKE_OPAQUE(visacd::MeshList);
+
+namespace {
+
+py::array_t<double> verts_to_np(const std::vector<Vec3>& v) {
+  py::array_t<double> a({(py::ssize_t)v.size(), (py::ssize_t)3});
+  auto r = a.mutable_unchecked<2>();
+  for (size_t i = 0; i < v.size(); ++i)
+    for (int k = 0; k < 3; ++k) r(i, k) = v[i][k];
+  return a;
+}
+
+py::array_t<int> tris_to_np(const std::vector<Tri>& t) {
+  py::array_t<int> a({(py::ssize_t)t.size(), (py::ssize_t)3});
+  auto r = a.mutable_unchecked<2>();
+  for (size_t i = 0; i < t.size(); ++i)
+    for (int k = 0; k < 3; ++k) r(i, k) = t[i][k];
+  return a;
+}
+
+Mesh np_to_mesh(py::array_t<double, py::array::c_style | py::array::forcecast> v,
+                py::array_t<int, py::array::c_style | py::array::forcecast> t) {
+  Mesh m;
+  auto rv = v.unchecked<2>();
+  auto rt = t.unchecked<2>();
+  m.vertices.resize(rv.shape(0));
+  for (py::ssize_t i = 0; i < rv.shape(0); ++i) m.vertices[i] = {rv(i, 0), rv(i, 1), rv(i, 2)};
+  m.triangles.resize(rt.shape(0));
+  for (py::ssize_t i = 0; i < rt.shape(0); ++i) m.triangles[i] = {rt(i, 0), rt(i, 1), rt(i, 2)};
+  return m;
+}
+
+py::dict mesh_dict(const Mesh& m) {
+  py::dict d;
+  d["vertices"] = verts_to_np(m.vertices);
+  d["triangles"] = tris_to_np(m.triangles);
+  py::array_t<uint8_t> nw((py::ssize_t)m.is_new.size());
+  for (size_t i = 0; i < m.is_new.size(); ++i) nw.mutable_at(i) = m.is_new[i] ? 1 : 0;
+  d["is_new"] = nw;
+  py::array_t<uint32_t> e({(py::ssize_t)m.intersecting_edges.size(), (py::ssize_t)2});
+  for (size_t i = 0; i < m.intersecting_edges.size(); ++i) {
+    e.mutable_at(i, 0) = m.intersecting_edges[i].first;
+    e.mutable_at(i, 1) = m.intersecting_edges[i].second;
+  }
+  d["edges"] = e;
+  return d;
+}
+
+}  // namespace
+
+PYBIND11_MODULE(visacd, m) {
+  py::bind_vector<std::vector<std::array<double, 3>>>(m, "VecArray3d");
+  py::bind_vector<std::vector<std::array<int, 3>>>(m, "VecArray3i");
+
+  py::class_<Mesh>(m, "Mesh")
+      .def(py::init<>())
+      .def_readwrite("vertices", &Mesh::vertices)
+      .def_readwrite("triangles", &Mesh::triangles);
+
+  py::bind_vector<MeshList>(m, "MeshList");
+
+  py::class_<Config>(m, "Config")
+      .def(py::init<>())
+      .def_readwrite("return_parts", &Config::return_parts)
+      .def_readwrite("score_mode", &Config::score_mode)
+      .def_readwrite("flat_surface_min_area", &Config::flat_surface_min_area)
+      .def_readwrite("use_flat_surfaces", &Config::use_flat_surfaces)
+      .def_readwrite("flat_surface_k", &Config::flat_surface_k)
+      .def_readwrite("use_merging", &Config::use_merging)
+      .def_readwrite("verbose", &Config::verbose);
+
+  m.def("make_vecarray3i", [](py::array_t<int, py::array::c_style | py::array::forcecast> a) {
+    auto buf = a.request();
+    std::vector<std::array<int, 3>> out;
+    const int* p = static_cast<const int*>(buf.ptr);
+    const py::ssize_t rows = buf.ndim >= 1 ? buf.shape[0] : 0;
+    out.reserve(rows);
+    for (py::ssize_t i = 0; i < rows; ++i) out.push_back({p[3 * i], p[3 * i + 1], p[3 * i + 2]});
+    return out;
+  });
+
+  m.def("set_seed", &set_seed, py::arg("seed"));
+  m.attr("config") = py::cast(&config(), py::return_value_policy::reference);
+
+  py::class_<ProcessResult>(m, "ProcessResult")
+      .def_readwrite("parts", &ProcessResult::parts)
+      .def_readwrite("concavity", &ProcessResult::concavity)
+      .def_readwrite("num_parts", &ProcessResult::num_parts);
+
+  m.def("process", &process, py::arg("mesh"), py::arg("concavity"), py::arg("num_parts"),
+        py::call_guard<py::gil_scoped_release>());
+
+  // ---- helpers for tests and benchmarks (not part of the reference surface) --
+  m.def("_stage_times", []() {
+    const auto& t = last_stage_times();
+    py::dict d;
+    d["preprocess_ms"] = t.preprocess;
+    d["visibility_ms"] = t.visibility;
+    d["scoring_ms"] = t.scoring;
+    d["clip_ms"] = t.clip;
+    d["concavity_ms"] = t.concavity;
+    d["cages_ms"] = t.cages;
+    d["hulls_ms"] = t.hulls;
+    d["total_ms"] = t.total;
+    d["iterations"] = t.iterations;
+    const auto& c = gpu::counters();
+    d["vis_calls"] = c.vis_calls;
+    d["vis_pairs"] = c.vis_pairs;
+    d["vis_edges"] = c.vis_edges;
+    d["score_calls"] = c.score_calls;
+    d["plane_edge_pairs"] = c.plane_edge_pairs;
+    return d;
+  });
+  m.def("_manifold_preprocess", [](py::array_t<double> v, py::array_t<int> t, double scale, double level) {
+    Mesh mm = np_to_mesh(v, t);
+    manifold_preprocess(mm, scale, level);
+    return mesh_dict(mm);
+  });
+  m.def("_convex_hull", [](py::array_t<double> v) {
+    Mesh tmp = np_to_mesh(v, py::array_t<int>(std::vector<py::ssize_t>{0, 3}));
+    return mesh_dict(convex_hull(tmp.vertices, true));
+  });
+  m.def("_clip", [](py::array_t<double> v, py::array_t<int> t, std::array<double, 4> pl) {
+    Mesh mm = np_to_mesh(v, t);
+    std::vector<int> m1, m2;
+    MeshList out = clip(mm, Plane(pl[0], pl[1], pl[2], pl[3]), m1, m2);
+    py::list parts;
+    for (const auto& p : out) parts.append(mesh_dict(p));
+    return py::make_tuple(parts, m1, m2);
+  });
+  m.def("_candidate_planes", [](py::array_t<double> v, py::array_t<uint32_t> e, int num) {
+    Mesh mm = np_to_mesh(v, py::array_t<int>(std::vector<py::ssize_t>{0, 3}));
+    auto re = e.unchecked<2>();
+    std::vector<Edge> edges(re.shape(0));
+    for (py::ssize_t i = 0; i < re.shape(0); ++i) edges[i] = {re(i, 0), re(i, 1)};
+    auto planes = get_candidate_planes(mm.vertices, edges, num);
+    py::array_t<double> out({(py::ssize_t)planes.size(), (py::ssize_t)4});
+    for (size_t i = 0; i < planes.size(); ++i) {
+      out.mutable_at(i, 0) = planes[i].a;
+      out.mutable_at(i, 1) = planes[i].b;
+      out.mutable_at(i, 2) = planes[i].c;
+      out.mutable_at(i, 3) = planes[i].d;
+    }
+    return out;
+  });
+  m.def("_extract_surfaces", [](py::array_t<double> v, py::array_t<int> t, double min_area) {
+    Mesh mm = np_to_mesh(v, t);
+    auto s = extract_surfaces(mm, min_area);
+    py::list out;
+    for (const auto& x : s) out.append(py::make_tuple(x.area, std::array<double, 4>{x.plane.a, x.plane.b, x.plane.c, x.plane.d}, x.triangle_ids));
+    return out;
+  });
+  m.def("_compute_h", [](py::array_t<double> v, py::array_t<int> t, double k, unsigned res) {
+    Mesh mm = np_to_mesh(v, t);
+    Mesh h = convex_hull(mm.vertices, true);
+    return compute_h(mm, h, k, res);
+  });
+  m.def("_compute_hb", [](py::array_t<double> v, py::array_t<int> t, py::array_t<double> hv, py::array_t<int> ht, unsigned res) {
+    return compute_hb(np_to_mesh(v, t), np_to_mesh(hv, ht), res);
+  });
+  m.def("_mesh_volume", [](py::array_t<double> v, py::array_t<int> t) { return mesh_volume(np_to_mesh(v, t)); });
+  m.def("_separate_disjoint", [](py::array_t<double> v, py::array_t<int> t) {
+    MeshList parts{np_to_mesh(v, t)};
+    separate_disjoint(parts);
+    py::list out;
+    for (const auto& p : parts) out.append(mesh_dict(p));
+    return out;
+  });
+  m.def("_visibility", [](py::array_t<double> v, py::array_t<int> t, py::array_t<double> cv, py::array_t<int> ct) {
+    Mesh mm = np_to_mesh(v, t), cage = np_to_mesh(cv, ct);
+    auto e = gpu::visibility_edges(mm, cage);
+    py::array_t<uint32_t> out({(py::ssize_t)e.size(), (py::ssize_t)2});
+    for (size_t i = 0; i < e.size(); ++i) {
+      out.mutable_at(i, 0) = e[i].first;
+      out.mutable_at(i, 1) = e[i].second;
+    }
+    return out;
+  });
+}

@@ -1,0 +1,110 @@
+// Host data model of the decomposition driver.
+//
+// Mirrors the reference's data types (lib/include/core.hpp:18-64,
+// lib/include/config.hpp:7-30): a triangle mesh with float64 vertices and
+// int32 triangles, per-vertex "new" flags set by clipping, and the part's
+// visibility edges (i < j); planes a x + b y + c z + d = 0 with the 1e-6 side
+// test; a process-wide configuration and random engine.
+#pragma once
+
+#include <array>
+#include <cmath>
+#include <cstdint>
+#include <limits>
+#include <random>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+namespace visacd {
+
+using Vec3 = std::array<double, 3>;
+using Tri = std::array<int, 3>;
+using Edge = std::pair<unsigned int, unsigned int>;
+
+constexpr double kInf = std::numeric_limits<double>::max();
+
+inline Vec3 operator+(const Vec3& a, const Vec3& b) { return {a[0] + b[0], a[1] + b[1], a[2] + b[2]}; }
+inline Vec3 operator-(const Vec3& a, const Vec3& b) { return {a[0] - b[0], a[1] - b[1], a[2] - b[2]}; }
+inline Vec3 operator*(const Vec3& a, double s) { return {a[0] * s, a[1] * s, a[2] * s}; }
+inline Vec3 operator/(const Vec3& a, double s) {
+  if (s == 0) throw std::runtime_error("division of a vector by zero");
+  return {a[0] / s, a[1] / s, a[2] / s};
+}
+inline double dot(const Vec3& a, const Vec3& b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+inline Vec3 cross(const Vec3& a, const Vec3& b) {
+  return {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+}
+inline double norm(const Vec3& a) { return std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]); }
+inline Vec3 normalized(const Vec3& a) {
+  double l = norm(a);
+  if (l == 0) throw std::runtime_error("cannot normalise a zero-length vector");
+  return {a[0] / l, a[1] / l, a[2] / l};
+}
+
+// Unit normal of a triangle (lib/include/core.hpp:148-167 formula order).
+Vec3 face_normal(const Vec3& p1, const Vec3& p2, const Vec3& p3);
+// Triangle area (lib/include/core.hpp:124-137 formula order).
+double triangle_area(const Vec3& p0, const Vec3& p1, const Vec3& p2);
+
+struct Plane {
+  double a = 0, b = 0, c = 0, d = 0;
+  Plane() = default;
+  Plane(double a_, double b_, double c_, double d_) : a(a_), b(b_), c(c_), d(d_) {}
+  double eval(const Vec3& p) const { return p[0] * a + p[1] * b + p[2] * c + d; }
+  // +1 / -1 beyond eps, else 0 (lib/include/core.hpp:178-185).
+  int side(const Vec3& p, double eps = 1e-6) const {
+    double r = eval(p);
+    if (r > eps) return 1;
+    if (r < -eps) return -1;
+    return 0;
+  }
+};
+
+struct Mesh {
+  std::vector<Vec3> vertices;
+  std::vector<Tri> triangles;
+  std::vector<bool> is_new;
+  std::vector<Edge> intersecting_edges;
+
+  void clear() {
+    vertices.clear();
+    triangles.clear();
+  }
+  // Geometry only (lib/src/core.cpp:247-254 copies vertices and triangles).
+  Mesh copy_geometry() const {
+    Mesh m;
+    m.vertices = vertices;
+    m.triangles = triangles;
+    return m;
+  }
+};
+using MeshList = std::vector<Mesh>;
+
+struct Config {
+  bool return_parts = false;
+  std::string score_mode = "concavity";  // or "edge"
+  double flat_surface_min_area = 0.1;
+  bool use_flat_surfaces = true;
+  double flat_surface_k = 2.0;
+  bool use_merging = false;
+  // Additions of this implementation (not in the reference's Config).
+  bool verbose = true;  // the "[visacd] ..." progress lines
+};
+
+Config& config();
+std::mt19937& random_engine();
+void set_seed(unsigned int seed);
+
+// Bounding box (xmin, xmax, ymin, ymax, zmin, zmax).
+std::array<double, 6> bbox(const Mesh& m);
+// Map to [-1, 1] along the longest axis; returns the original bbox
+// (lib/src/core.cpp:262-291).
+std::array<double, 6> normalize(Mesh& m);
+void unnormalize(Mesh& m, const std::array<double, 6>& box);  // core.cpp:293-307
+
+// Signed volume (lib/src/cost.cpp:24-43 term order).
+double mesh_volume(const Mesh& m);
+
+}  // namespace visacd

@@ -1,0 +1,234 @@
+// Concavity metric: h = max(k * rv, hb) with rv the radius of the sphere whose
+// volume is the part/hull volume difference and hb a sampled symmetric
+// Hausdorff distance between the two surfaces.
+//
+// Semantics of lib/src/cost.cpp:45-123 and lib/include/hausdorff.hpp:214-298,
+// sampling of lib/src/core.cpp:144-232 (area-weighted triangle choice by
+// std::discrete_distribution, two std::uniform_real_distribution draws per
+// sample, one extra sample per untouched triangle, all from the process-wide
+// std::mt19937 in the reference's order). The nearest-sample search is this
+// project's kd-tree (the reference uses nanoflann); distances to the sampled
+// triangles use the exact closest-point test.
+#include <algorithm>
+#include <cmath>
+#include <queue>
+#include <unordered_set>
+#include <vector>
+
+#include "geometry.hpp"
+
+namespace visacd {
+
+constexpr double kPi = 3.14159265;  // the reference's constant (lib/include/cost.hpp:6)
+
+void extract_point_set(const Mesh& m, std::vector<Vec3>& samples, std::vector<int>& tri_ids,
+                       size_t resolution, double base, bool one_per_tri) {
+  if (m.triangles.empty() || m.vertices.empty()) return;
+  std::vector<double> areas(m.triangles.size());
+  double total = 0;
+  for (size_t i = 0; i < m.triangles.size(); ++i) {
+    const auto& t = m.triangles[i];
+    areas[i] = triangle_area(m.vertices[t[0]], m.vertices[t[1]], m.vertices[t[2]]);
+    total += areas[i];
+  }
+  if (base != 0) resolution = size_t(std::max(1000, int(resolution * (total / base))));
+  std::discrete_distribution<size_t> pick(areas.begin(), areas.end());
+  std::uniform_real_distribution<double> uni(0.0, 1.0);
+  std::mt19937& eng = random_engine();
+  std::unordered_set<size_t> touched;
+  auto sample = [&](size_t ti) {
+    const auto& t = m.triangles[ti];
+    double a = uni(eng);
+    double b = uni(eng);
+    const Vec3 &v0 = m.vertices[t[0]], &v1 = m.vertices[t[1]], &v2 = m.vertices[t[2]];
+    Vec3 v;
+    for (int k = 0; k < 3; ++k)
+      v[k] = (1 - std::sqrt(a)) * v0[k] + (std::sqrt(a) * (1 - b)) * v1[k] + b * std::sqrt(a) * v2[k];
+    samples.push_back(v);
+    tri_ids.push_back((int)ti);
+  };
+  for (size_t done = 0; done < resolution; ++done) {
+    size_t ti = pick(eng);
+    sample(ti);
+    touched.insert(ti);
+  }
+  if (one_per_tri)
+    for (size_t i = 0; i < m.triangles.size(); ++i)
+      if (touched.find(i) == touched.end()) sample(i);
+}
+
+namespace {
+
+// Static 3D kd-tree over a point set for k-nearest queries.
+class KdTree {
+ public:
+  explicit KdTree(const std::vector<Vec3>& pts) : P(pts) {
+    idx.resize(pts.size());
+    for (size_t i = 0; i < idx.size(); ++i) idx[i] = (int)i;
+    if (!idx.empty()) build(0, (int)idx.size(), 0);
+  }
+  // k nearest (ascending squared distance).
+  void knn(const Vec3& q, int k, std::vector<std::pair<double, int>>& out) const {
+    out.clear();
+    if (idx.empty()) return;
+    std::priority_queue<std::pair<double, int>> heap;
+    search(0, q, k, heap);
+    out.resize(heap.size());
+    for (int i = (int)heap.size() - 1; i >= 0; --i) {
+      out[i] = heap.top();
+      heap.pop();
+    }
+  }
+
+ private:
+  struct Node {
+    int lo, hi, left, right, axis;
+    double split;
+  };
+  const std::vector<Vec3>& P;
+  std::vector<int> idx;
+  std::vector<Node> nodes;
+
+  int build(int lo, int hi, int depth) {
+    int id = (int)nodes.size();
+    nodes.push_back({lo, hi, -1, -1, 0, 0.0});
+    if (hi - lo <= 10) return id;
+    double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300};
+    for (int i = lo; i < hi; ++i)
+      for (int a = 0; a < 3; ++a) {
+        mn[a] = std::min(mn[a], P[idx[i]][a]);
+        mx[a] = std::max(mx[a], P[idx[i]][a]);
+      }
+    int ax = 0;
+    for (int a = 1; a < 3; ++a)
+      if (mx[a] - mn[a] > mx[ax] - mn[ax]) ax = a;
+    int mid = (lo + hi) / 2;
+    std::nth_element(idx.begin() + lo, idx.begin() + mid, idx.begin() + hi,
+                     [&](int x, int y) { return P[x][ax] < P[y][ax]; });
+    nodes[id].axis = ax;
+    nodes[id].split = P[idx[mid]][ax];
+    int l = build(lo, mid, depth + 1);
+    int r = build(mid, hi, depth + 1);
+    nodes[id].left = l;
+    nodes[id].right = r;
+    return id;
+  }
+
+  void search(int n, const Vec3& q, int k, std::priority_queue<std::pair<double, int>>& heap) const {
+    const Node& nd = nodes[n];
+    if (nd.left < 0) {
+      for (int i = nd.lo; i < nd.hi; ++i) {
+        const Vec3& p = P[idx[i]];
+        double d = (p[0] - q[0]) * (p[0] - q[0]) + (p[1] - q[1]) * (p[1] - q[1]) + (p[2] - q[2]) * (p[2] - q[2]);
+        if ((int)heap.size() < k) heap.push({d, idx[i]});
+        else if (d < heap.top().first) {
+          heap.pop();
+          heap.push({d, idx[i]});
+        }
+      }
+      return;
+    }
+    double diff = q[nd.axis] - nd.split;
+    int first = diff < 0 ? nd.left : nd.right, second = diff < 0 ? nd.right : nd.left;
+    search(first, q, k, heap);
+    if ((int)heap.size() < k || diff * diff < heap.top().first) search(second, q, k, heap);
+  }
+};
+
+// One direction of the face Hausdorff distance: for each query sample, the
+// smallest distance to the triangles of its 10 nearest samples on the other
+// side (lib/include/hausdorff.hpp:236-263).
+double directed(const std::vector<Vec3>& Q, const KdTree& tree, const Mesh& other,
+                const std::vector<int>& other_ids) {
+  double cmax = 0;
+#pragma omp parallel
+  {
+    std::vector<std::pair<double, int>> nn;
+    double local = 0;
+#pragma omp for schedule(static)
+    for (int64_t i = 0; i < (int64_t)Q.size(); ++i) {
+      tree.knn(Q[i], 10, nn);
+      double cmin = kInf;
+      for (const auto& r : nn) {
+        const auto& t = other.triangles[other_ids[r.second]];
+        double d = point_triangle_distance(Q[i], other.vertices[t[0]], other.vertices[t[1]],
+                                           other.vertices[t[2]]);
+        if (d < cmin) {
+          cmin = d;
+          if (cmin < 1e-14) break;
+        }
+      }
+      if (cmin > 10 && !nn.empty()) cmin = std::sqrt(nn[0].first);
+      if (cmin > local && kInf > cmin) local = cmin;
+    }
+#pragma omp critical
+    cmax = std::max(cmax, local);
+  }
+  return cmax;
+}
+
+double face_hausdorff(const Mesh& A, const std::vector<Vec3>& XA, const std::vector<int>& idA,
+                      const Mesh& B, const std::vector<Vec3>& XB, const std::vector<int>& idB) {
+  KdTree ta(XA), tb(XB);
+  return std::max(directed(XB, ta, A, idA), directed(XA, tb, B, idB));
+}
+
+}  // namespace
+
+double compute_rv(const Mesh& a, const Mesh& b) {
+  double v1 = mesh_volume(a), v2 = mesh_volume(b);
+  return std::pow(3 * std::fabs(v1 - v2) / (4 * kPi), 1.0 / 3);
+}
+
+double compute_rv3(const Mesh& c1, const Mesh& c2, const Mesh& ch) {
+  double v1 = mesh_volume(c1), v2 = mesh_volume(c2), v3 = mesh_volume(ch);
+  return std::pow(3 * std::fabs(v1 + v2 - v3) / (4 * kPi), 1.0 / 3);
+}
+
+double compute_hb(const Mesh& a, const Mesh& b, unsigned int resolution) {
+  std::vector<Vec3> s1, s2;
+  std::vector<int> i1, i2;
+  extract_point_set(a, s1, i1, resolution, 1, true);
+  extract_point_set(b, s2, i2, resolution, 1, true);
+  if (s1.empty() || s2.empty()) return kInf;
+  return face_hausdorff(a, s1, i1, b, s2, i2);
+}
+
+// Merge cost between two hulls and their joint hull (lib/src/cost.cpp:87-105).
+// The reference's hulls keep every input point as a vertex, so the joint hull
+// always has as many vertices as the two inputs together and the sampled term
+// is zero; the same holds here because convex_hull keeps all input points.
+double compute_hb3(const Mesh& c1, const Mesh& c2, const Mesh& ch, unsigned int resolution) {
+  if (c1.vertices.size() + c2.vertices.size() == ch.vertices.size()) return 0.0;
+  Mesh both = c1;
+  const int off = (int)c1.vertices.size();
+  both.vertices.insert(both.vertices.end(), c2.vertices.begin(), c2.vertices.end());
+  for (auto t : c2.triangles) both.triangles.push_back({t[0] + off, t[1] + off, t[2] + off});
+  return compute_hb(both, ch, resolution);
+}
+
+double compute_h(const Mesh& a, const Mesh& b, double k, unsigned int resolution) {
+  double h1 = compute_rv(a, b);
+  double h2 = compute_hb(a, b, resolution);
+  return std::max(h1 * k, h2);
+}
+
+double compute_h3(const Mesh& c1, const Mesh& c2, const Mesh& ch, double k, unsigned int resolution) {
+  double h1 = compute_rv3(c1, c2, ch);
+  double h2 = compute_hb3(c1, c2, ch, resolution + 2000);
+  return std::max(h1 * k, h2);
+}
+
+double mesh_dist(const Mesh& a, const Mesh& b) {
+  if (a.vertices.empty() || b.vertices.empty()) return kInf;
+  KdTree tb(b.vertices);
+  double best = kInf;
+  std::vector<std::pair<double, int>> nn;
+  for (const auto& v : a.vertices) {
+    tb.knn(v, 1, nn);
+    best = std::min(best, std::sqrt(nn[0].first));
+  }
+  return best;
+}
+
+}  // namespace visacd

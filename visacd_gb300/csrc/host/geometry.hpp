@@ -1,0 +1,52 @@
+// Host geometry of the decomposition driver (CPU, C++): the parts of VisACD's
+// pipeline around the GPU hot path.
+#pragma once
+
+#include <vector>
+
+#include "core.hpp"
+
+namespace visacd {
+
+// ---- remesh.cpp: SDF remeshing (replaces lib/src/preprocess.cpp:18-67) ----
+void manifold_preprocess(Mesh& m, double scale, double level);
+Vec3 closest_point_on_triangle(const Vec3& p, const Vec3& a, const Vec3& b, const Vec3& c);
+double point_triangle_distance(const Vec3& p, const Vec3& a, const Vec3& b, const Vec3& c);
+
+// ---- hull.cpp: convex hull (replaces qhull "Qt Pp", lib/src/core.cpp:59-111).
+// As with qhull, the hull mesh keeps every input point as a vertex (interior
+// ones unreferenced) and triangulates the hull facets. fix_normals orients
+// every facet away from the vertex centroid (lib/src/core.cpp:33-57).
+Mesh convex_hull(const std::vector<Vec3>& pts, bool fix_normals = true);
+
+// ---- clip.cpp: split a mesh by a plane (lib/src/clip.cpp:190-741).
+// Returns {pos, neg} (or {mesh} when a side is empty); pos_map/neg_map give,
+// for every input vertex, its 1-based index in pos/neg (0 = absent). Border
+// vertices are appended to both parts and flagged is_new.
+MeshList clip(const Mesh& mesh, const Plane& plane, std::vector<int>& pos_map,
+              std::vector<int>& neg_map);
+
+// ---- cost.cpp: concavity metric (lib/src/cost.cpp, lib/include/hausdorff.hpp).
+void extract_point_set(const Mesh& m, std::vector<Vec3>& samples, std::vector<int>& tri_ids,
+                       size_t resolution, double base, bool one_per_tri);
+double compute_rv(const Mesh& a, const Mesh& b);
+double compute_rv3(const Mesh& c1, const Mesh& c2, const Mesh& ch);
+double compute_hb(const Mesh& a, const Mesh& b, unsigned int resolution);
+double compute_hb3(const Mesh& c1, const Mesh& c2, const Mesh& ch, unsigned int resolution);
+double compute_h(const Mesh& a, const Mesh& b, double k, unsigned int resolution);
+double compute_h3(const Mesh& c1, const Mesh& c2, const Mesh& ch, double k, unsigned int resolution);
+double mesh_dist(const Mesh& a, const Mesh& b);
+
+// ---- surfaces.cpp: flat-surface planes (lib/src/support_surface.cpp:14-183).
+struct Surface {
+  std::vector<int> triangle_ids;
+  double area = 0.0;
+  Plane plane;
+};
+std::vector<Surface> extract_surfaces(const Mesh& mesh, double min_area);
+
+// ---- postprocess.cpp (lib/src/postprocess.cpp) ----
+void separate_disjoint(MeshList& parts);
+void multimerge_ch(MeshList& meshes, MeshList& hulls, double current_concavity, double threshold);
+
+}  // namespace visacd

@@ -1,0 +1,126 @@
+#include "gpu_bridge.hpp"
+
+#include <chrono>
+#include <cstdlib>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+
+#include "visacd_gpu.h"
+
+namespace visacd {
+namespace gpu {
+
+namespace {
+void check(int rc, const char* what) {
+  if (rc != VISACD_OK)
+    throw std::runtime_error(std::string(what) + " failed: " + visacd_last_error());
+}
+struct BvhHandle {
+  visacd_bvh* h = nullptr;
+  ~BvhHandle() {
+    if (h) visacd_bvh_destroy(h);
+  }
+};
+double now_ms() {
+  return std::chrono::duration<double, std::milli>(
+             std::chrono::steady_clock::now().time_since_epoch())
+      .count();
+}
+}  // namespace
+
+Counters& counters() {
+  static Counters c;
+  return c;
+}
+
+visacd_ctx* context() {
+  static std::once_flag once;
+  static visacd_ctx* ctx = nullptr;
+  static std::string err;
+  std::call_once(once, [] {
+    const char* dev = std::getenv("VISACD_DEVICE");
+    int d = dev ? std::atoi(dev) : 0;
+    if (visacd_ctx_create(d, nullptr, &ctx) != VISACD_OK) {
+      err = visacd_last_error();
+      ctx = nullptr;
+    }
+  });
+  if (!ctx) throw std::runtime_error("cannot create the GPU context: " + err);
+  return ctx;
+}
+
+static void to_f32(const std::vector<Vec3>& v, std::vector<float>& out) {
+  out.resize(3 * v.size());
+  for (size_t i = 0; i < v.size(); ++i)
+    for (int k = 0; k < 3; ++k) out[3 * i + k] = (float)v[i][k];
+}
+
+std::vector<Edge> visibility_edges(const Mesh& mesh, const Mesh& cage) {
+  double t0 = now_ms();
+  visacd_ctx* ctx = context();
+  std::vector<float> v, cv;
+  to_f32(mesh.vertices, v);
+  to_f32(cage.vertices, cv);
+  static_assert(sizeof(Tri) == 12, "triangles must be 3 packed ints");
+  BvhHandle sb, cb;
+  check(visacd_bvh_build(ctx, v.data(), (int32_t)mesh.vertices.size(),
+                         reinterpret_cast<const uint32_t*>(mesh.triangles.data()),
+                         (int32_t)mesh.triangles.size(), 0, &sb.h),
+        "visacd_bvh_build(part)");
+  check(visacd_bvh_build(ctx, cv.data(), (int32_t)cage.vertices.size(),
+                         reinterpret_cast<const uint32_t*>(cage.triangles.data()),
+                         (int32_t)cage.triangles.size(), 0, &cb.h),
+        "visacd_bvh_build(cage)");
+  std::vector<uint8_t> mask;
+  if (!mesh.is_new.empty()) {
+    mask.resize(mesh.vertices.size(), 0);
+    for (size_t i = 0; i < mesh.is_new.size() && i < mask.size(); ++i) mask[i] = mesh.is_new[i] ? 1 : 0;
+  }
+  int64_t ne = 0;
+  visacd_vis_stats st;
+  check(visacd_visibility(ctx, v.data(), (int32_t)mesh.vertices.size(),
+                          mask.empty() ? nullptr : mask.data(), 0, sb.h, cb.h, &ne, &st),
+        "visacd_visibility");
+  std::vector<uint32_t> flat(2 * (size_t)ne);
+  check(visacd_visibility_edges(ctx, flat.data(), ne), "visacd_visibility_edges");
+  std::vector<Edge> out((size_t)ne);
+  for (int64_t k = 0; k < ne; ++k) out[k] = {flat[2 * k], flat[2 * k + 1]};
+  auto& c = counters();
+  c.vis_calls++;
+  c.vis_pairs += st.pairs_tested;
+  c.vis_edges += ne;
+  c.vis_ms += now_ms() - t0;
+  return out;
+}
+
+std::vector<double> score_planes(const std::vector<Plane>& planes, const std::vector<Vec3>& pts,
+                                 const std::vector<Edge>& edges) {
+  double t0 = now_ms();
+  visacd_ctx* ctx = context();
+  std::vector<float> pl(4 * planes.size()), p;
+  for (size_t i = 0; i < planes.size(); ++i) {
+    pl[4 * i] = (float)planes[i].a;
+    pl[4 * i + 1] = (float)planes[i].b;
+    pl[4 * i + 2] = (float)planes[i].c;
+    pl[4 * i + 3] = (float)planes[i].d;
+  }
+  to_f32(pts, p);
+  std::vector<uint32_t> e(2 * edges.size());
+  for (size_t k = 0; k < edges.size(); ++k) {
+    e[2 * k] = edges[k].first;
+    e[2 * k + 1] = edges[k].second;
+  }
+  std::vector<double> scores(planes.size(), 0.0);
+  check(visacd_score_planes(ctx, pl.data(), (int32_t)planes.size(), p.data(), (int32_t)pts.size(),
+                            e.data(), (int64_t)edges.size(), 0, scores.data(), nullptr),
+        "visacd_score_planes");
+  auto& c = counters();
+  c.score_calls++;
+  c.plane_edge_pairs += (long long)planes.size() * (long long)edges.size();
+  c.score_ms += now_ms() - t0;
+  return scores;
+}
+
+}  // namespace gpu
+}  // namespace visacd

@@ -1,0 +1,207 @@
+// Connected components of parts and greedy hull merging.
+//
+// separate_disjoint: lib/src/postprocess.cpp:202-326 — split each part into
+// edge-connected triangle components (numbered by their lowest triangle),
+// vertices renumbered in first-use order, is_new carried over, each visibility
+// edge given to the first component holding both endpoints; components with
+// |volume| < 1e-6 are dropped.
+// multimerge_ch: lib/src/postprocess.cpp:64-200 — the reference's packed
+// lower-triangular cost matrix, its update order and its indexing are kept
+// as they are (they decide which hulls merge).
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <numeric>
+#include <unordered_map>
+#include <vector>
+
+#include "geometry.hpp"
+
+namespace visacd {
+
+namespace {
+
+int find_root(std::vector<int>& p, int x) {
+  while (p[x] != x) {
+    p[x] = p[p[x]];
+    x = p[x];
+  }
+  return x;
+}
+
+MeshList separate_step(const Mesh& part) {
+  const int T = (int)part.triangles.size();
+  if (T == 0) return {};
+  std::vector<int> uf(T);
+  std::iota(uf.begin(), uf.end(), 0);
+  std::map<std::pair<int, int>, int> first_tri;
+  for (int i = 0; i < T; ++i) {
+    const auto& t = part.triangles[i];
+    const std::pair<int, int> e[3] = {std::minmax(t[0], t[1]), std::minmax(t[1], t[2]),
+                                      std::minmax(t[0], t[2])};
+    for (const auto& k : e) {
+      auto it = first_tri.find(k);
+      if (it == first_tri.end()) {
+        first_tri[k] = i;
+      } else {
+        int a = find_root(uf, it->second), b = find_root(uf, i);
+        if (a != b) uf[std::max(a, b)] = std::min(a, b);
+      }
+    }
+  }
+  // Component ids in order of their lowest triangle.
+  std::vector<int> comp(T), comp_of_root(T, -1);
+  int nparts = 0;
+  for (int i = 0; i < T; ++i) {
+    int r = find_root(uf, i);
+    if (comp_of_root[r] < 0) comp_of_root[r] = nparts++;
+    comp[i] = comp_of_root[r];
+  }
+  MeshList out(nparts);
+  std::vector<std::unordered_map<int, int>> remap(nparts);
+  const bool has_new = !part.is_new.empty();
+  for (int i = 0; i < T; ++i) {
+    Mesh& m = out[comp[i]];
+    auto& rm = remap[comp[i]];
+    Tri nt;
+    for (int k = 0; k < 3; ++k) {
+      int g = part.triangles[i][k];
+      auto it = rm.find(g);
+      if (it == rm.end()) {
+        int id = (int)m.vertices.size();
+        rm[g] = id;
+        m.vertices.push_back(part.vertices[g]);
+        if (has_new) m.is_new.push_back(part.is_new[g]);
+        nt[k] = id;
+      } else {
+        nt[k] = it->second;
+      }
+    }
+    m.triangles.push_back(nt);
+  }
+  for (const auto& e : part.intersecting_edges) {
+    for (int p = 0; p < nparts; ++p) {
+      auto a = remap[p].find((int)e.first), b = remap[p].find((int)e.second);
+      if (a != remap[p].end() && b != remap[p].end()) {
+        out[p].intersecting_edges.push_back({(unsigned)a->second, (unsigned)b->second});
+        break;
+      }
+    }
+  }
+  return out;
+}
+
+Mesh merged_hull(const Mesh& a, const Mesh& b) {
+  std::vector<Vec3> pts = a.vertices;
+  pts.insert(pts.end(), b.vertices.begin(), b.vertices.end());
+  return convex_hull(pts, true);
+}
+
+}  // namespace
+
+void separate_disjoint(MeshList& parts) {
+  MeshList out;
+  for (const auto& p : parts)
+    for (auto& c : separate_step(p))
+      if (std::fabs(mesh_volume(c)) >= 1e-6) out.push_back(std::move(c));
+  parts.swap(out);
+}
+
+void multimerge_ch(MeshList& meshes, MeshList& cvxs, double current_concavity, double threshold) {
+  const size_t n = cvxs.size();
+  if (n <= 1) return;
+  const size_t bound = ((n - 1) * n) >> 1;
+  std::vector<double> cost(bound), precost(bound);
+  for (size_t idx = 0; idx < bound; ++idx) {
+    size_t p1 = (size_t)(std::sqrt(8.0 * idx + 1) - 1) >> 1;
+    size_t sum = (p1 * (p1 + 1)) >> 1;
+    size_t p2 = idx - sum;
+    ++p1;
+    double dist = mesh_dist(cvxs[p1], cvxs[p2]);
+    if (dist < threshold) {
+      Mesh ch = merged_hull(cvxs[p1], cvxs[p2]);
+      cost[idx] = compute_h3(cvxs[p1], cvxs[p2], ch, 0.3, 10000);
+      precost[idx] = std::max(compute_h(meshes[p1], cvxs[p1], 0.3, 10000),
+                              compute_h(meshes[p2], cvxs[p2], 0.3, 10000));
+    } else {
+      cost[idx] = kInf;
+    }
+  }
+  // precost is indexed the way the reference indexes it; reads past its end
+  // (possible for tiny matrices) count as 0.
+  auto pre = [&](size_t i) { return i < precost.size() ? precost[i] : 0.0; };
+  size_t cost_size = n;
+  for (size_t guard = 0; guard < 4 * bound + 16; ++guard) {
+    // First minimum of the packed matrix.
+    int addr = -1;
+    double best = kInf;
+    for (size_t i = 0; i < cost.size(); ++i)
+      if (cost[i] < best) {
+        best = cost[i];
+        addr = (int)i;
+      }
+    if (addr < 0) break;
+    if (best > threshold) break;
+    if (best + pre((size_t)addr) > current_concavity) {
+      cost[addr] = kInf;
+      continue;
+    }
+    const size_t addrI = ((size_t)(int)std::sqrt(1 + (8.0 * addr)) - 1) >> 1;
+    const size_t p1 = addrI + 1;
+    const size_t p2 = addr - ((addrI * (addrI + 1)) >> 1);
+    Mesh cch = merged_hull(cvxs[p1], cvxs[p2]);
+    cvxs[p2] = cch;
+    std::swap(cvxs[p1], cvxs[cvxs.size() - 1]);
+    cvxs.pop_back();
+    cost_size -= 1;
+    // Costs against the merged hull (row p2, then column p2).
+    size_t row = ((p2 - 1) * p2) >> 1;
+    for (size_t i = 0; i < p2; ++i) {
+      double dist = mesh_dist(cvxs[p2], cvxs[i]);
+      if (dist < threshold) {
+        Mesh ch = merged_hull(cvxs[p2], cvxs[i]);
+        cost[row] = compute_h3(cvxs[p2], cvxs[i], ch, 0.3, 10000);
+        precost[row++] = std::max(pre(p2) + best, pre(i));
+      } else {
+        cost[row++] = kInf;
+      }
+    }
+    row += p2;
+    for (size_t i = p2 + 1; i < cost_size; ++i) {
+      double dist = mesh_dist(cvxs[p2], cvxs[i]);
+      if (dist < threshold) {
+        Mesh ch = merged_hull(cvxs[p2], cvxs[i]);
+        cost[row] = compute_h3(cvxs[p2], cvxs[i], ch, 0.3, 10000);
+        precost[row] = std::max(pre(p2) + best, pre(i));
+      } else {
+        cost[row] = kInf;
+      }
+      row += i;
+    }
+    // Move the last row/column into p1's place.
+    const size_t erase_idx = ((cost_size - 1) * cost_size) >> 1;
+    if (p1 < cost_size) {
+      row = (addrI * p1) >> 1;
+      size_t top = erase_idx;
+      for (size_t i = 0; i < p1; ++i) {
+        if (i != p2) {
+          cost[row] = cost[top];
+          precost[row] = precost[top];
+        }
+        ++row;
+        ++top;
+      }
+      ++top;
+      row += p1;
+      for (size_t i = p1 + 1; i < cost_size; ++i) {
+        cost[row] = cost[top];
+        precost[row] = precost[top++];
+        row += i;
+      }
+    }
+    cost.resize(erase_idx);
+    precost.resize(erase_idx);
+  }
+}
+
+}  // namespace visacd

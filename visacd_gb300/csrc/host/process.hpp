@@ -1,0 +1,42 @@
+// Decomposition driver: visacd.process(mesh, concavity, num_parts).
+#pragma once
+
+#include <vector>
+
+#include "core.hpp"
+#include "geometry.hpp"
+
+namespace visacd {
+
+struct ProcessResult {
+  MeshList parts;
+  double concavity = 0;
+  int num_parts = 0;
+};
+
+// lib/src/process.cpp:28-72.
+std::vector<Plane> get_candidate_planes(const std::vector<Vec3>& vertices,
+                                        const std::vector<Edge>& edges, int num_planes);
+
+// lib/src/process.cpp:82-181: one split of `mesh`; returns true when there is
+// nothing left to cut (no candidate planes or no visibility edges).
+bool decompose_iteration(Mesh& mesh, MeshList& parts, Mesh& cage,
+                         const std::vector<Plane>& flat_planes);
+
+double compute_part_score(const Mesh& part);
+int get_part_with_highest_score(const MeshList& parts);
+int get_part_with_highest_concavity(const MeshList& parts, double& max_concavity);
+double compute_final_concavity(const MeshList& parts, const MeshList& hulls);
+
+// lib/src/process.cpp:238-347.
+ProcessResult process(Mesh mesh, double concavity, int num_parts);
+
+// Per-stage wall time of the last process() call (ms), for benchmarks.
+struct StageTimes {
+  double preprocess = 0, visibility = 0, scoring = 0, clip = 0, concavity = 0, cages = 0,
+         hulls = 0, total = 0;
+  int iterations = 0;
+};
+const StageTimes& last_stage_times();
+
+}  // namespace visacd

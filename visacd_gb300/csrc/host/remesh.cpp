@@ -1,0 +1,244 @@
+// SDF remeshing: replace a mesh by its iso-surface at distance `level` outside
+// the surface, on a grid of voxel size 1/scale.
+//
+// Replaces lib/src/preprocess.cpp:18-67 (OpenVDB meshToSignedDistanceField +
+// volumeToMesh; OpenVDB is not available here). Steps:
+//  1. Unsigned distance (exact point-triangle distance) on every voxel centre
+//     within a narrow band of the scaled triangles; OpenMP over z-slabs.
+//  2. Inside/outside by crossing parity along rays through the voxel centres,
+//     majority of the x, y and z directions (rays offset by tiny irrational
+//     amounts so they avoid vertices and edges; a ray threading a small gap
+//     in the input flips only its own direction's vote).
+//  3. Dual contouring of the iso-level (surface-nets placement: one vertex per
+//     sign-changing cell at the mean of its edge crossings; one quad per
+//     sign-changing grid edge), quads split into two triangles, outward normals.
+// The result is watertight for closed input; like the reference's OpenVDB
+// output it can contain non-manifold edges in rare ambiguous cells.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "geometry.hpp"
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace visacd {
+
+// Closest point on triangle abc to p (Ericson, "Real-Time Collision
+// Detection", 5.1.5 — Voronoi-region classification).
+Vec3 closest_point_on_triangle(const Vec3& p, const Vec3& a, const Vec3& b, const Vec3& c) {
+  Vec3 ab = b - a, ac = c - a, ap = p - a;
+  double d1 = dot(ab, ap), d2 = dot(ac, ap);
+  if (d1 <= 0 && d2 <= 0) return a;
+  Vec3 bp = p - b;
+  double d3 = dot(ab, bp), d4 = dot(ac, bp);
+  if (d3 >= 0 && d4 <= d3) return b;
+  double vc = d1 * d4 - d3 * d2;
+  if (vc <= 0 && d1 >= 0 && d3 <= 0) {
+    double v = d1 / (d1 - d3);
+    return a + ab * v;
+  }
+  Vec3 cp = p - c;
+  double d5 = dot(ab, cp), d6 = dot(ac, cp);
+  if (d6 >= 0 && d5 <= d6) return c;
+  double vb = d5 * d2 - d1 * d6;
+  if (vb <= 0 && d2 >= 0 && d6 <= 0) {
+    double w = d2 / (d2 - d6);
+    return a + ac * w;
+  }
+  double va = d3 * d6 - d5 * d4;
+  if (va <= 0 && (d4 - d3) >= 0 && (d5 - d6) >= 0) {
+    double w = (d4 - d3) / ((d4 - d3) + (d5 - d6));
+    return b + (c - b) * w;
+  }
+  double denom = 1.0 / (va + vb + vc);
+  double v = vb * denom, w = vc * denom;
+  return a + ab * v + ac * w;
+}
+
+double point_triangle_distance(const Vec3& p, const Vec3& a, const Vec3& b, const Vec3& c) {
+  return norm(p - closest_point_on_triangle(p, a, b, c));
+}
+
+void manifold_preprocess(Mesh& m, double scale, double level) {
+  const int nt = (int)m.triangles.size();
+  if (nt == 0 || m.vertices.empty()) {
+    m.clear();
+    return;
+  }
+  std::vector<Vec3> P(m.vertices.size());
+  for (size_t i = 0; i < P.size(); ++i) P[i] = m.vertices[i] * scale;
+  const double iso = level * scale;
+  const double band = std::max(iso, 0.0) + 2.0;
+  double lo[3] = {kInf, kInf, kInf}, hi[3] = {-kInf, -kInf, -kInf};
+  for (const auto& p : P)
+    for (int a = 0; a < 3; ++a) {
+      lo[a] = std::min(lo[a], p[a]);
+      hi[a] = std::max(hi[a], p[a]);
+    }
+  int org[3], dim[3];
+  for (int a = 0; a < 3; ++a) {
+    org[a] = (int)std::floor(lo[a] - band - 2.0);
+    dim[a] = (int)std::ceil(hi[a] + band + 2.0) - org[a] + 1;
+  }
+  const int nx = dim[0], ny = dim[1], nz = dim[2];
+  const size_t nvox = (size_t)nx * ny * nz;
+  auto vid = [&](int i, int j, int k) { return ((size_t)k * ny + j) * nx + i; };
+  std::vector<float> dist(nvox, (float)band);
+
+  // 1. Unsigned distance in the band; each thread owns a z-slab.
+  struct TriBox { int lo[3], hi[3]; };
+  std::vector<TriBox> boxes(nt);
+  for (int t = 0; t < nt; ++t) {
+    const auto& tr = m.triangles[t];
+    for (int a = 0; a < 3; ++a) {
+      double mn = std::min({P[tr[0]][a], P[tr[1]][a], P[tr[2]][a]});
+      double mx = std::max({P[tr[0]][a], P[tr[1]][a], P[tr[2]][a]});
+      boxes[t].lo[a] = std::max(0, (int)std::floor(mn - band) - org[a]);
+      boxes[t].hi[a] = std::min(dim[a] - 1, (int)std::ceil(mx + band) - org[a]);
+    }
+  }
+#pragma omp parallel
+  {
+    int nth = 1, me = 0;
+#ifdef _OPENMP
+    nth = omp_get_num_threads();
+    me = omp_get_thread_num();
+#endif
+    const int k0 = (int)((int64_t)nz * me / nth), k1 = (int)((int64_t)nz * (me + 1) / nth);
+    for (int t = 0; t < nt; ++t) {
+      const TriBox& b = boxes[t];
+      int ka = std::max(b.lo[2], k0), kb = std::min(b.hi[2], k1 - 1);
+      if (ka > kb) continue;
+      const auto& tr = m.triangles[t];
+      const Vec3 &A = P[tr[0]], &B = P[tr[1]], &C = P[tr[2]];
+      for (int k = ka; k <= kb; ++k)
+        for (int j = b.lo[1]; j <= b.hi[1]; ++j)
+          for (int i = b.lo[0]; i <= b.hi[0]; ++i) {
+            Vec3 q = {(double)(org[0] + i), (double)(org[1] + j), (double)(org[2] + k)};
+            float d = (float)point_triangle_distance(q, A, B, C);
+            float& slot = dist[vid(i, j, k)];
+            if (d < slot) slot = d;
+          }
+    }
+  }
+
+  // 2. Inside/outside: crossing parity along x-, y- and z-rays through the
+  // voxel centres, majority of the three (a ray threading a small gap in the
+  // input flips only its own axis's vote).
+  std::vector<uint8_t> votes(nvox, 0);
+  for (int ax = 0; ax < 3; ++ax) {
+    const int u = (ax + 1) % 3, w = (ax + 2) % 3;  // the ray runs along ax
+    const double ou = 1.2345679e-6, ow = 2.3456789e-6;  // ray offsets, in voxels
+    std::vector<std::vector<double>> hits((size_t)dim[u] * dim[w]);
+    for (int t = 0; t < nt; ++t) {
+      const auto& tr = m.triangles[t];
+      const Vec3 &A = P[tr[0]], &B = P[tr[1]], &C = P[tr[2]];
+      int u0 = std::max(0, (int)std::floor(std::min({A[u], B[u], C[u]}) - org[u]));
+      int u1 = std::min(dim[u] - 1, (int)std::ceil(std::max({A[u], B[u], C[u]}) - org[u]));
+      int w0 = std::max(0, (int)std::floor(std::min({A[w], B[w], C[w]}) - org[w]));
+      int w1 = std::min(dim[w] - 1, (int)std::ceil(std::max({A[w], B[w], C[w]}) - org[w]));
+      for (int kw = w0; kw <= w1; ++kw)
+        for (int ku = u0; ku <= u1; ++ku) {
+          double y = org[u] + ku + ou, z = org[w] + kw + ow;
+          double e0 = (B[u] - A[u]) * (z - A[w]) - (B[w] - A[w]) * (y - A[u]);
+          double e1 = (C[u] - B[u]) * (z - B[w]) - (C[w] - B[w]) * (y - B[u]);
+          double e2 = (A[u] - C[u]) * (z - C[w]) - (A[w] - C[w]) * (y - C[u]);
+          bool in = (e0 > 0 && e1 > 0 && e2 > 0) || (e0 < 0 && e1 < 0 && e2 < 0);
+          if (!in) continue;
+          double sw = e0 + e1 + e2;
+          // Barycentric weights: e1 -> A, e2 -> B, e0 -> C.
+          hits[(size_t)kw * dim[u] + ku].push_back((e1 * A[ax] + e2 * B[ax] + e0 * C[ax]) / sw);
+        }
+    }
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t col = 0; col < (int64_t)dim[u] * dim[w]; ++col) {
+      auto& xs = hits[col];
+      if (xs.empty()) continue;
+      std::sort(xs.begin(), xs.end());
+      const int ku = (int)(col % dim[u]), kw = (int)(col / dim[u]);
+      size_t c = 0;
+      for (int i = 0; i < dim[ax]; ++i) {
+        double x = org[ax] + i;
+        while (c < xs.size() && xs[c] < x) ++c;
+        if (c & 1) {
+          int g[3];
+          g[ax] = i;
+          g[u] = ku;
+          g[w] = kw;
+          votes[vid(g[0], g[1], g[2])] += 1;
+        }
+      }
+    }
+  }
+  std::vector<float> f(nvox);
+  for (size_t v = 0; v < nvox; ++v) f[v] = votes[v] >= 2 ? -dist[v] : dist[v];
+
+  // 3. Dual contouring of f = iso.
+  const float fiso = (float)iso;
+  const int cx = nx - 1, cy = ny - 1, cz = nz - 1;
+  auto cid = [&](int i, int j, int k) { return ((size_t)k * cy + j) * cx + i; };
+  std::vector<int> cell_vertex((size_t)cx * cy * cz, -1);
+  std::vector<Vec3> out_v;
+  static const int corner[8][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {1, 1, 0},
+                                   {0, 0, 1}, {1, 0, 1}, {0, 1, 1}, {1, 1, 1}};
+  static const int cedge[12][2] = {{0, 1}, {2, 3}, {4, 5}, {6, 7}, {0, 2}, {1, 3},
+                                   {4, 6}, {5, 7}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
+  for (int k = 0; k < cz; ++k)
+    for (int j = 0; j < cy; ++j)
+      for (int i = 0; i < cx; ++i) {
+        float cv[8];
+        int nin = 0;
+        for (int c = 0; c < 8; ++c) {
+          cv[c] = f[vid(i + corner[c][0], j + corner[c][1], k + corner[c][2])];
+          nin += cv[c] < fiso;
+        }
+        if (nin == 0 || nin == 8) continue;
+        Vec3 acc = {0, 0, 0};
+        int ncross = 0;
+        for (int e = 0; e < 12; ++e) {
+          int c0 = cedge[e][0], c1 = cedge[e][1];
+          if ((cv[c0] < fiso) == (cv[c1] < fiso)) continue;
+          double t = (double)(fiso - cv[c0]) / (double)(cv[c1] - cv[c0]);
+          for (int a = 0; a < 3; ++a) acc[a] += corner[c0][a] + t * (corner[c1][a] - corner[c0][a]);
+          ++ncross;
+        }
+        acc = acc / (double)ncross;
+        cell_vertex[cid(i, j, k)] = (int)out_v.size();
+        out_v.push_back({(org[0] + i + acc[0]) / scale, (org[1] + j + acc[1]) / scale,
+                         (org[2] + k + acc[2]) / scale});
+      }
+  std::vector<Tri> out_t;
+  auto emit = [&](int q0, int q1, int q2, int q3, bool flip) {
+    if (q0 < 0 || q1 < 0 || q2 < 0 || q3 < 0) return;
+    if (flip) std::swap(q1, q3);
+    out_t.push_back({q0, q1, q2});
+    out_t.push_back({q0, q2, q3});
+  };
+  for (int k = 1; k < nz - 1; ++k)
+    for (int j = 1; j < ny - 1; ++j)
+      for (int i = 1; i < nx - 1; ++i) {
+        const bool in0 = f[vid(i, j, k)] < fiso;
+        // +x edge: cells (i, j-1..j, k-1..k), order in (y, z).
+        if (i + 1 < nx && in0 != (f[vid(i + 1, j, k)] < fiso))
+          emit(cell_vertex[cid(i, j - 1, k - 1)], cell_vertex[cid(i, j, k - 1)],
+               cell_vertex[cid(i, j, k)], cell_vertex[cid(i, j - 1, k)], !in0);
+        // +y edge: cells (i-1..i, j, k-1..k), order in (z, x).
+        if (j + 1 < ny && in0 != (f[vid(i, j + 1, k)] < fiso))
+          emit(cell_vertex[cid(i - 1, j, k - 1)], cell_vertex[cid(i - 1, j, k)],
+               cell_vertex[cid(i, j, k)], cell_vertex[cid(i, j, k - 1)], !in0);
+        // +z edge: cells (i-1..i, j-1..j, k), order in (x, y).
+        if (k + 1 < nz && in0 != (f[vid(i, j, k + 1)] < fiso))
+          emit(cell_vertex[cid(i - 1, j - 1, k)], cell_vertex[cid(i, j - 1, k)],
+               cell_vertex[cid(i, j, k)], cell_vertex[cid(i - 1, j, k)], !in0);
+      }
+  m.clear();
+  m.is_new.clear();
+  m.intersecting_edges.clear();
+  m.vertices = std::move(out_v);
+  m.triangles = std::move(out_t);
+}
+
+}  // namespace visacd
