@@ -1,0 +1,113 @@
+"""Host functions against the reference's own code (CPU). oracle/_ref compiles
+the VisACD host sources in place; these tests need the reference tree and are
+skipped where it is absent (the GPU machine uses the committed fixtures)."""
+import numpy as np
+import pytest
+
+import oracle
+from visacd_gb300 import build, meshgen as mg
+
+R = pytest.importorskip("oracle.ref")
+if not R.available():
+    pytest.skip("reference tree not available", allow_module_level=True)
+
+
+@pytest.fixture(scope="module")
+def V():
+    build.build_host()
+    from visacd_gb300 import visacd
+    return visacd
+
+
+def test_clip_bit_exact_with_reference(V):
+    rng = np.random.default_rng(0)
+    for trial in range(16):
+        v, t = mg.displaced_blob(3, seed=trial)
+        n = rng.normal(size=3)
+        n /= np.linalg.norm(n)
+        pl = [*n, rng.uniform(-0.4, 0.4)]
+        rp, r1, r2 = R.clip(v, t, pl)
+        pp, p1, p2 = V._clip(v, t, pl)
+        assert len(rp) == len(pp)
+        np.testing.assert_array_equal(r1, p1)
+        np.testing.assert_array_equal(r2, p2)
+        for a, b in zip(rp, pp):
+            np.testing.assert_array_equal(a["vertices"], b["vertices"])
+            np.testing.assert_array_equal(a["triangles"], b["triangles"])
+            np.testing.assert_array_equal(a["is_new"].astype(bool)[: len(b["is_new"])], b["is_new"].astype(bool))
+
+
+def test_clip_through_vertices_bit_exact(V):
+    # planes through mesh vertices exercise the on-plane cases
+    v, t = mg.icosphere(2)
+    for pl in ([0, 0, 1, 0.0], [1, 0, 0, 0.0], [0.0, 0.5257311121191336, 0.85065080835204, 0.0]):
+        rp, r1, r2 = R.clip(v, t, pl)
+        pp, p1, p2 = V._clip(v, t, pl)
+        assert len(rp) == len(pp)
+        np.testing.assert_array_equal(r1, p1)
+        for a, b in zip(rp, pp):
+            np.testing.assert_array_equal(a["triangles"], b["triangles"])
+            np.testing.assert_array_equal(a["vertices"], b["vertices"])
+
+
+def test_candidate_planes_bit_exact_with_reference(V):
+    v, t = mg.displaced_blob(3, seed=2)
+    _, e, _ = oracle.visibility(v, t, *mg.offset_cage(v, t, 0.03))
+    for seed in (0, 42):
+        R.set_seed(seed)
+        a = R.candidate_planes(v, e, 2500)
+        V.set_seed(seed)
+        b = V._candidate_planes(v, e, 2500)
+        np.testing.assert_array_equal(a, b)
+
+
+def test_flat_surfaces_match_reference(V):
+    g = np.linspace(-0.5, 0.5, 4)
+    xx, yy = np.meshgrid(g, g)
+    verts = np.stack([xx.ravel(), yy.ravel(), np.zeros(16)], 1)
+    tris = []
+    for i in range(3):
+        for j in range(3):
+            q = i * 4 + j
+            tris += [[q, q + 4, q + 5], [q, q + 5, q + 1]]
+    # a slab: top and bottom faces
+    v = np.concatenate([verts, verts + [0, 0, 0.3]])
+    t = np.concatenate([np.array(tris)[:, ::-1], np.array(tris) + 16])
+    pr, ar = R.extract_surfaces(v, t, 0.1)
+    pp = V._extract_surfaces(v, t, 0.1)
+    assert len(pr) == len(pp) == 2
+    for (area, plane, _), a2, p2 in zip(pp, ar, pr):
+        assert area == a2
+        np.testing.assert_array_equal(plane, p2)
+
+
+def test_separate_disjoint_matches_reference(V):
+    v1, t1 = mg.displaced_blob(2, seed=1)
+    v2, t2 = mg.displaced_blob(2, seed=2)
+    v = np.concatenate([v1, v2 + 3.0, v1 * 1e-3 + 9.0])  # the tiny third part is dropped
+    t = np.concatenate([t1, t2 + len(v1), t1 + len(v1) + len(v2)])
+    a = R.separate_disjoint(v, t)
+    b = V._separate_disjoint(v, t)
+    assert len(a) == len(b) == 2
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x["vertices"], y["vertices"])
+        np.testing.assert_array_equal(x["triangles"], y["triangles"])
+
+
+def test_concavity_metric_matches_reference(V):
+    for seed in (3, 4):
+        v, t = mg.displaced_blob(3, seed=seed)
+        R.set_seed(11)
+        a = R.compute_h(v, t, 0.3, 3000)
+        V.set_seed(11)
+        b = V._compute_h(v, t, 0.3, 3000)
+        assert abs(a - b) <= 1e-12 * max(1.0, abs(a))
+
+
+def test_hull_matches_reference(V):
+    rng = np.random.default_rng(3)
+    p = rng.normal(size=(500, 3))
+    vol, nt = R.hull_volume(p)
+    h = V._convex_hull(p)
+    assert len(h["triangles"]) == nt
+    assert abs(V._mesh_volume(h["vertices"], h["triangles"]) - vol) < 1e-12

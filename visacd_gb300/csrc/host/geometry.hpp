@@ -26,6 +26,12 @@ Mesh convex_hull(const std::vector<Vec3>& pts, bool fix_normals = true);
 MeshList clip(const Mesh& mesh, const Plane& plane, std::vector<int>& pos_map,
               std::vector<int>& neg_map);
 
+// ---- cap2d.cpp: triangulation of the region a planar border graph encloses
+// (stand-in for CDT's insertVertices/insertEdges/eraseOuterTrianglesAndHoles).
+// xy: 2 doubles per point; edges 0-based; triangles CCW. False if nothing closed.
+bool triangulate_border_2d(const std::vector<double>& xy, const std::vector<std::pair<int, int>>& edges,
+                           std::vector<Tri>& tris);
+
 // ---- cost.cpp: concavity metric (lib/src/cost.cpp, lib/include/hausdorff.hpp).
 void extract_point_set(const Mesh& m, std::vector<Vec3>& samples, std::vector<int>& tri_ids,
                        size_t resolution, double base, bool one_per_tri);
