@@ -62,6 +62,15 @@ typedef struct {
   int64_t tri_tests;      /* segment-triangle tests started (per segment) */
 } visacd_vis_stats;
 
+/* Sizes of one clip result (the cap is triangulated by the caller). */
+typedef struct {
+  int32_t n_pos, n_neg;        /* triangles of the positive / negative part, without the cap */
+  int32_t nv_pos, nv_neg;      /* original vertices kept by each part */
+  int32_t n_border;            /* border points (appended after the kept vertices of both parts) */
+  int32_t n_border_edges;      /* unique border edges, 1-based border point pairs */
+  int32_t n_touching;          /* triangles touching the plane (resolved in order) */
+} visacd_clip_result;
+
 /* Counters of one scoring call. */
 typedef struct {
   int32_t quantum_exp;    /* edge lengths are summed in units of 2^quantum_exp */
@@ -160,6 +169,24 @@ int visacd_compute_intersection_matrix(visacd_ctx* ctx, const float* verts, int3
 int visacd_score_planes(visacd_ctx* ctx, const float* planes, int32_t P, const float* points,
                         int32_t N, const uint32_t* edges, int64_t E, int device_ptrs,
                         double* scores, visacd_score_stats* stats);
+
+/* ---- per-part clipping --------------------------------------------------- */
+/* Split a mesh (float64 vertices nv x 3, int32 triangles nt x 3) by the plane
+   a x + b y + c z + d = 0 (plane = {a, b, c, d}), as lib/src/clip.cpp:190-741
+   does before its cap triangulation: 1e-6 side test, triangles wholly on one
+   side kept, touching triangles split at the plane, border points deduplicated
+   by vertex key, edge key and position (1e-4, first match). Output triangles
+   index part-local vertices: the kept original vertices in input order, then
+   the border points. Host pointers; results stay on the device until
+   visacd_clip_fetch. The caller triangulates the cap from the border points
+   and edges. Synchronizes. */
+int visacd_clip(visacd_ctx* ctx, const double* verts, int32_t nv, const int32_t* tris, int32_t nt,
+                const double* plane, visacd_clip_result* res);
+/* Copy the last clip result to host memory (any pointer may be NULL):
+   triangles 3 x n_pos / 3 x n_neg, 1-based vertex maps nv each (0 = absent),
+   border points 3 x n_border, border edges 2 x n_border_edges. */
+int visacd_clip_fetch(visacd_ctx* ctx, int32_t* pos_tris, int32_t* neg_tris, int32_t* pos_map,
+                      int32_t* neg_map, double* border, int32_t* border_edges);
 
 /* Allocation-free variant of visacd_score_planes. No counterpart in the
    reference: it exists for callers that cannot allocate — code running under a

@@ -23,7 +23,14 @@ EXPORTED = [
     "visacd_compute_intersection_matrix",
     "visacd_vis_variant_count", "visacd_ctx_set_vis_variant", "visacd_autotune_visibility",
     "visacd_score_planes", "visacd_score_planes_noalloc", "classify_and_rate_planes",
+    "visacd_clip", "visacd_clip_fetch",
 ]
+
+
+class ClipResult(C.Structure):
+    _fields_ = [("n_pos", C.c_int32), ("n_neg", C.c_int32), ("nv_pos", C.c_int32),
+                ("nv_neg", C.c_int32), ("n_border", C.c_int32), ("n_border_edges", C.c_int32),
+                ("n_touching", C.c_int32)]
 
 
 class VisStats(C.Structure):
@@ -77,6 +84,8 @@ def load() -> C.CDLL:
     lib.visacd_score_planes.argtypes = [P, P, i32, P, i32, P, i64, C.c_int, P,
                                         C.POINTER(ScoreStats)]
     lib.visacd_score_planes_noalloc.argtypes = [P, i32, P, i32, P, i64, P, P, P]
+    lib.visacd_clip.argtypes = [P, P, i32, P, i32, P, C.POINTER(ClipResult)]
+    lib.visacd_clip_fetch.argtypes = [P, P, P, P, P, P, P]
     lib.classify_and_rate_planes.argtypes = [P, P, P, P, C.c_int, C.c_int, C.c_int]
     lib.classify_and_rate_planes.restype = None
     return lib
@@ -209,6 +218,28 @@ class Context:
             self._h, _ptr(v), n, _ptr(t), len(t), _ptr(m), _ptr(cv), len(cv), _ptr(ct), len(ct),
             _ptr(out), cap, C.byref(ne), C.byref(st)), "compute_intersection_matrix")
         return out[: ne.value].copy(), st.as_dict()
+
+    # ---- clipping ----------------------------------------------------------
+    def clip(self, verts, tris, plane):
+        """GPU clip without the cap: dict with pos/neg triangles (part-local),
+        1-based maps, border points and border edges."""
+        v = np.ascontiguousarray(np.asarray(verts, dtype=np.float64)).reshape(-1, 3)
+        t = np.ascontiguousarray(np.asarray(tris, dtype=np.int32)).reshape(-1, 3)
+        pl = np.ascontiguousarray(np.asarray(plane, dtype=np.float64)).reshape(4)
+        r = ClipResult()
+        _check(lib().visacd_clip(self._h, _ptr(v), len(v), _ptr(t), len(t), _ptr(pl), C.byref(r)),
+               "visacd_clip")
+        out = {f: getattr(r, f) for f, _ in ClipResult._fields_}
+        pt = np.zeros((r.n_pos, 3), np.int32)
+        nt_ = np.zeros((r.n_neg, 3), np.int32)
+        m1 = np.zeros(len(v), np.int32)
+        m2 = np.zeros(len(v), np.int32)
+        b = np.zeros((r.n_border, 3))
+        be = np.zeros((r.n_border_edges, 2), np.int32)
+        _check(lib().visacd_clip_fetch(self._h, _ptr(pt), _ptr(nt_), _ptr(m1), _ptr(m2), _ptr(b), _ptr(be)),
+               "visacd_clip_fetch")
+        out.update(pos_tris=pt, neg_tris=nt_, pos_map=m1, neg_map=m2, border=b, border_edges=be)
+        return out
 
     # ---- scoring -----------------------------------------------------------
     def score_planes(self, planes, points, edges):

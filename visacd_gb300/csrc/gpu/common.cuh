@@ -96,6 +96,7 @@ enum CtxSlot {
   kSlotTmpVerts,
   kSlotTmpTris,
   kSlotVisRowTiles,
+  kSlotClip,
   kSlotCount
 };
 
@@ -113,6 +114,9 @@ struct visacd_ctx {
   bool timing = false;
   int vis_variant_override = -1;                  // forced launch shape, -1 = tuned/default
   std::unordered_map<uint32_t, int> vis_tuned;    // shape class -> autotuned variant
+  visacd_clip_result clip_out{};                  // last clip result (device-resident)
+  int clip_nv = 0;
+  void* clip_ptrs[7] = {nullptr};
   // Per-kernel timing: events recorded around each launch when timing is on.
   struct Pending {
     int kernel;
@@ -147,6 +151,8 @@ enum KernelId {
   kKScanTop,
   kKScanAdd,
   kKBitEmit,
+  kKClip,
+  kKClipResolve,
   kKMisc,
   kKCount
 };

@@ -86,7 +86,8 @@ PYBIND11_MODULE(visacd, m) {
       .def_readwrite("use_flat_surfaces", &Config::use_flat_surfaces)
       .def_readwrite("flat_surface_k", &Config::flat_surface_k)
       .def_readwrite("use_merging", &Config::use_merging)
-      .def_readwrite("verbose", &Config::verbose);
+      .def_readwrite("verbose", &Config::verbose)
+      .def_readwrite("gpu_clip", &Config::gpu_clip);
 
   m.def("make_vecarray3i", [](py::array_t<int, py::array::c_style | py::array::forcecast> a) {
     auto buf = a.request();
@@ -143,6 +144,14 @@ PYBIND11_MODULE(visacd, m) {
     Mesh mm = np_to_mesh(v, t);
     std::vector<int> m1, m2;
     MeshList out = clip(mm, Plane(pl[0], pl[1], pl[2], pl[3]), m1, m2);
+    py::list parts;
+    for (const auto& p : out) parts.append(mesh_dict(p));
+    return py::make_tuple(parts, m1, m2);
+  });
+  m.def("_clip_gpu", [](py::array_t<double> v, py::array_t<int> t, std::array<double, 4> pl) {
+    Mesh mm = np_to_mesh(v, t);
+    std::vector<int> m1, m2;
+    MeshList out = gpu::clip(mm, Plane(pl[0], pl[1], pl[2], pl[3]), m1, m2);
     py::list parts;
     for (const auto& p : out) parts.append(mesh_dict(p));
     return py::make_tuple(parts, m1, m2);

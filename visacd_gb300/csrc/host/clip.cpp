@@ -152,6 +152,46 @@ bool triangulate_cap(const std::vector<Vec3>& border, const std::vector<std::pai
 
 }  // namespace
 
+// Parts from the GPU clip outputs: kept vertices in input order, border
+// points appended to both, cap triangulated here (same tail as clip()).
+MeshList assemble_clip(const Mesh& mesh, const Plane& plane, const std::vector<Tri>& pos_tris,
+                       const std::vector<Tri>& neg_tris, const std::vector<int>& pos_map,
+                       const std::vector<int>& neg_map, const std::vector<Vec3>& border,
+                       const std::vector<std::pair<int, int>>& bedges) {
+  const int N = (int)mesh.vertices.size();
+  Mesh pos, neg;
+  int np = 0, nn = 0;
+  for (int i = 0; i < N; ++i) {
+    if (pos_map[i]) {
+      pos.vertices.push_back(mesh.vertices[i]);
+      ++np;
+    }
+    if (neg_map[i]) {
+      neg.vertices.push_back(mesh.vertices[i]);
+      ++nn;
+    }
+  }
+  if (np == 0 || nn == 0) return MeshList{mesh};
+  std::vector<Tri> cap;
+  if (border.size() > 2) triangulate_cap(border, bedges, plane, cap);
+  const int nbp = (int)border.size();
+  pos.is_new.assign(np + nbp, false);
+  neg.is_new.assign(nn + nbp, false);
+  for (int i = 0; i < nbp; ++i) {
+    pos.vertices.push_back(border[i]);
+    neg.vertices.push_back(border[i]);
+    pos.is_new[np + i] = true;
+    neg.is_new[nn + i] = true;
+  }
+  pos.triangles = pos_tris;
+  neg.triangles = neg_tris;
+  for (const auto& t : cap) {
+    pos.triangles.push_back({np + t[0], np + t[1], np + t[2]});
+    neg.triangles.push_back({nn + t[2], nn + t[1], nn + t[0]});
+  }
+  return MeshList{pos, neg};
+}
+
 MeshList clip(const Mesh& mesh, const Plane& plane, std::vector<int>& pos_map,
               std::vector<int>& neg_map) {
   const int N = (int)mesh.vertices.size();

@@ -90,7 +90,8 @@ struct Config {
   double flat_surface_k = 2.0;
   bool use_merging = false;
   // Additions of this implementation (not in the reference's Config).
-  bool verbose = true;  // the "[visacd] ..." progress lines
+  bool verbose = true;   // the "[visacd] ..." progress lines
+  bool gpu_clip = true;  // split parts with the GPU clip kernels (else the host clip)
 };
 
 Config& config();

@@ -26,6 +26,14 @@ Mesh convex_hull(const std::vector<Vec3>& pts, bool fix_normals = true);
 MeshList clip(const Mesh& mesh, const Plane& plane, std::vector<int>& pos_map,
               std::vector<int>& neg_map);
 
+// Same parts from the GPU clip's outputs (part-local triangles without the
+// cap, 1-based maps, border points, 1-based border edges); the cap is
+// triangulated here.
+MeshList assemble_clip(const Mesh& mesh, const Plane& plane, const std::vector<Tri>& pos_tris,
+                       const std::vector<Tri>& neg_tris, const std::vector<int>& pos_map,
+                       const std::vector<int>& neg_map, const std::vector<Vec3>& border,
+                       const std::vector<std::pair<int, int>>& bedges);
+
 // ---- cap2d.cpp: triangulation of the region a planar border graph encloses
 // (stand-in for CDT's insertVertices/insertEdges/eraseOuterTrianglesAndHoles).
 // xy: 2 doubles per point; edges 0-based; triangles CCW. False if nothing closed.

@@ -6,6 +6,7 @@
 #include <stdexcept>
 #include <string>
 
+#include "geometry.hpp"
 #include "visacd_gpu.h"
 
 namespace visacd {
@@ -120,6 +121,29 @@ std::vector<double> score_planes(const std::vector<Plane>& planes, const std::ve
   c.plane_edge_pairs += (long long)planes.size() * (long long)edges.size();
   c.score_ms += now_ms() - t0;
   return scores;
+}
+
+MeshList clip(const Mesh& mesh, const Plane& plane, std::vector<int>& pos_map,
+              std::vector<int>& neg_map) {
+  visacd_ctx* ctx = context();
+  const int nv = (int)mesh.vertices.size(), nt = (int)mesh.triangles.size();
+  const double pl[4] = {plane.a, plane.b, plane.c, plane.d};
+  visacd_clip_result r;
+  check(visacd_clip(ctx, reinterpret_cast<const double*>(mesh.vertices.data()), nv,
+                    reinterpret_cast<const int32_t*>(mesh.triangles.data()), nt, pl, &r),
+        "visacd_clip");
+  std::vector<Tri> pt(r.n_pos), ng(r.n_neg);
+  pos_map.assign(nv, 0);
+  neg_map.assign(nv, 0);
+  std::vector<Vec3> border(r.n_border);
+  std::vector<int32_t> be(2 * (size_t)r.n_border_edges);
+  check(visacd_clip_fetch(ctx, reinterpret_cast<int32_t*>(pt.data()),
+                          reinterpret_cast<int32_t*>(ng.data()), pos_map.data(), neg_map.data(),
+                          reinterpret_cast<double*>(border.data()), be.data()),
+        "visacd_clip_fetch");
+  std::vector<std::pair<int, int>> bedges(r.n_border_edges);
+  for (int k = 0; k < r.n_border_edges; ++k) bedges[k] = {be[2 * k], be[2 * k + 1]};
+  return assemble_clip(mesh, plane, pt, ng, pos_map, neg_map, border, bedges);
 }
 
 }  // namespace gpu

@@ -22,6 +22,11 @@ std::vector<Edge> visibility_edges(const Mesh& mesh, const Mesh& cage);
 std::vector<double> score_planes(const std::vector<Plane>& planes, const std::vector<Vec3>& pts,
                                  const std::vector<Edge>& edges);
 
+// Per-part clipping on the GPU (visacd_clip) + host cap: same parts and maps
+// as clip() in clip.cpp.
+MeshList clip(const Mesh& mesh, const Plane& plane, std::vector<int>& pos_map,
+              std::vector<int>& neg_map);
+
 struct Counters {
   long long vis_calls = 0, vis_pairs = 0, vis_edges = 0, score_calls = 0, plane_edge_pairs = 0;
   double vis_ms = 0, score_ms = 0;
