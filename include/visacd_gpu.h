@@ -99,6 +99,10 @@ int visacd_ctx_kernel_times(visacd_ctx* ctx, const char** names, double* total_m
 int64_t visacd_ctx_launch_count(const visacd_ctx* ctx);
 int visacd_ctx_sm_count(const visacd_ctx* ctx);
 
+/* FP32 FMA throughput of this GPU in TFLOP/s (packed f32x2 FMA loop, best of
+   3 timed launches): the denominator of the FP32-bound rooflines. */
+int visacd_measure_fp32_peak(visacd_ctx* ctx, double* tflops);
+
 /* ---- BVH ---------------------------------------------------------------- */
 /* Linear BVH over a triangle mesh: 63-bit Morton codes of triangle centroids,
    LSD radix sort, Karras (2012) hierarchy, bottom-up AABB fit. verts is nv x 3

@@ -76,5 +76,23 @@ def build(force: bool = False) -> Path | None:
     return LIB
 
 
+CUBIN = OUT / "ref_plane_intersections.cubin"
+
+
+def build_cubin(force: bool = False) -> Path | None:
+    """The reference's scoring kernel (lib/cuda/plane_intersections.cu), device
+    code only, compiled unchanged for sm_103a so the benchmark can time it on the
+    same GPU with the same planes and edges."""
+    src = REF / "lib" / "cuda" / "plane_intersections.cu"
+    if not src.exists():
+        return None
+    OUT.mkdir(exist_ok=True)
+    if force or not CUBIN.exists() or src.stat().st_mtime > CUBIN.stat().st_mtime:
+        _run(["/usr/local/cuda/bin/nvcc", "-cubin", "-O3", "-gencode", "arch=compute_103a,code=sm_103a",
+              "-o", str(CUBIN), str(src)])
+    return CUBIN
+
+
 if __name__ == "__main__":
     print(build(force=True))
+    print(build_cubin(force=True))

@@ -23,7 +23,7 @@ EXPORTED = [
     "visacd_compute_intersection_matrix",
     "visacd_vis_variant_count", "visacd_ctx_set_vis_variant", "visacd_autotune_visibility",
     "visacd_score_planes", "visacd_score_planes_noalloc", "classify_and_rate_planes",
-    "visacd_clip", "visacd_clip_fetch",
+    "visacd_clip", "visacd_clip_fetch", "visacd_measure_fp32_peak",
 ]
 
 
@@ -85,6 +85,7 @@ def load() -> C.CDLL:
                                         C.POINTER(ScoreStats)]
     lib.visacd_score_planes_noalloc.argtypes = [P, i32, P, i32, P, i64, P, P, P]
     lib.visacd_clip.argtypes = [P, P, i32, P, i32, P, C.POINTER(ClipResult)]
+    lib.visacd_measure_fp32_peak.argtypes = [P, C.POINTER(C.c_double)]
     lib.visacd_clip_fetch.argtypes = [P, P, P, P, P, P, P]
     lib.classify_and_rate_planes.argtypes = [P, P, P, P, C.c_int, C.c_int, C.c_int]
     lib.classify_and_rate_planes.restype = None
@@ -218,6 +219,11 @@ class Context:
             self._h, _ptr(v), n, _ptr(t), len(t), _ptr(m), _ptr(cv), len(cv), _ptr(ct), len(ct),
             _ptr(out), cap, C.byref(ne), C.byref(st)), "compute_intersection_matrix")
         return out[: ne.value].copy(), st.as_dict()
+
+    def fp32_peak_tflops(self) -> float:
+        t = C.c_double()
+        _check(lib().visacd_measure_fp32_peak(self._h, C.byref(t)), "measure_fp32_peak")
+        return t.value
 
     # ---- clipping ----------------------------------------------------------
     def clip(self, verts, tris, plane):
