@@ -192,6 +192,19 @@ int visacd_clip(visacd_ctx* ctx, const double* verts, int32_t nv, const int32_t*
 int visacd_clip_fetch(visacd_ctx* ctx, int32_t* pos_tris, int32_t* neg_tris, int32_t* pos_map,
                       int32_t* neg_map, double* border, int32_t* border_edges);
 
+/* ---- concavity metric ---------------------------------------------------- */
+/* Sampled symmetric face Hausdorff distance between surfaces A and B
+   (lib/include/hausdorff.hpp:214-298): for every sample of one surface, the
+   smallest FP64 distance to the triangles its 10 nearest samples on the other
+   surface were drawn from (the nearest-sample distance if that exceeds 10);
+   *out = the largest over both directions. Meshes: float64 vertices, int32
+   triangles; samples: float64 xyz with the id of the triangle each was drawn
+   from. Host pointers; synchronizes. */
+int visacd_face_hausdorff(visacd_ctx* ctx, const double* va, int32_t nva, const int32_t* ta,
+                          int32_t nta, const double* xa, const int32_t* ida, int32_t na,
+                          const double* vb, int32_t nvb, const int32_t* tb, int32_t ntb,
+                          const double* xb, const int32_t* idb, int32_t nb, double* out);
+
 /* Allocation-free variant of visacd_score_planes. No counterpart in the
    reference: it exists for callers that cannot allocate — code running under a
    fixed, pre-reserved memory budget, or a latency-bound loop where cudaMalloc's

@@ -62,3 +62,24 @@ def test_process_edge_mode_and_parts(visacd):
     assert 1 <= r.num_parts <= 5
     for p in r.parts:
         assert len(p.triangles) > 0
+
+
+def test_gpu_concavity_metric_equals_host(visacd):
+    from visacd_gb300 import visacd as V
+    for seed, level in [(3, 3), (4, 4), (5, 2)]:
+        v, t = mg.displaced_blob(level, seed=seed)
+        V.config.gpu_concavity = False
+        V.set_seed(11)
+        a = V._compute_h(v, t, 0.3, 3000)
+        V.config.gpu_concavity = True
+        V.set_seed(11)
+        b = V._compute_h(v, t, 0.3, 3000)
+        assert a == b
+        hv = V._convex_hull(v)
+        V.config.gpu_concavity = False
+        V.set_seed(5)
+        a = V._compute_hb(v, t, hv["vertices"], hv["triangles"], 10000)
+        V.config.gpu_concavity = True
+        V.set_seed(5)
+        b = V._compute_hb(v, t, hv["vertices"], hv["triangles"], 10000)
+        assert a == b

@@ -14,6 +14,7 @@ from visacd_gb300 import build, meshgen as mg
 def V():
     build.build_host()
     from visacd_gb300 import visacd
+    visacd.config.gpu_concavity = False  # host Hausdorff: these tests run without a GPU
     return visacd
 
 

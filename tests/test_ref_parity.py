@@ -16,6 +16,7 @@ if not R.available():
 def V():
     build.build_host()
     from visacd_gb300 import visacd
+    visacd.config.gpu_concavity = False  # host Hausdorff: these tests run without a GPU
     return visacd
 
 

@@ -23,7 +23,7 @@ EXPORTED = [
     "visacd_compute_intersection_matrix",
     "visacd_vis_variant_count", "visacd_ctx_set_vis_variant", "visacd_autotune_visibility",
     "visacd_score_planes", "visacd_score_planes_noalloc", "classify_and_rate_planes",
-    "visacd_clip", "visacd_clip_fetch", "visacd_measure_fp32_peak",
+    "visacd_clip", "visacd_clip_fetch", "visacd_measure_fp32_peak", "visacd_face_hausdorff",
 ]
 
 
@@ -86,6 +86,8 @@ def load() -> C.CDLL:
     lib.visacd_score_planes_noalloc.argtypes = [P, i32, P, i32, P, i64, P, P, P]
     lib.visacd_clip.argtypes = [P, P, i32, P, i32, P, C.POINTER(ClipResult)]
     lib.visacd_measure_fp32_peak.argtypes = [P, C.POINTER(C.c_double)]
+    lib.visacd_face_hausdorff.argtypes = [P, P, i32, P, i32, P, P, i32, P, i32, P, i32, P, P, i32,
+                                          C.POINTER(C.c_double)]
     lib.visacd_clip_fetch.argtypes = [P, P, P, P, P, P, P]
     lib.classify_and_rate_planes.argtypes = [P, P, P, P, C.c_int, C.c_int, C.c_int]
     lib.classify_and_rate_planes.restype = None

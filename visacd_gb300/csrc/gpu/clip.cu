@@ -8,11 +8,11 @@
 //     (|sum of sides| = 3, including the all-on-plane case oriented by the face
 //     normal) are "simple": they keep their vertices and emit themselves. All
 //     others touch the plane and are compacted, in order, into a short list.
-//  3. clip_resolve: one CTA walks that list in triangle order — the only
+//  3. clip_resolve: one warp walks that list in triangle order — the only
 //     order-dependent part: border points are deduplicated by vertex key, by
 //     directed-edge key (with the reference's key overwrites) and by position
 //     (1e-4 per coordinate, first match wins; the position scan runs across the
-//     CTA). Emits each touching triangle's pieces, border edges (unique
+//     32 lanes). Emits each touching triangle's pieces, border edges (unique
 //     unordered pairs, first occurrence) and the kept-vertex flags.
 //  4. Order-preserving scans over per-triangle output counts and per-vertex
 //     kept flags, then scatter + remap into part-local indices.
@@ -20,7 +20,7 @@
 
 namespace vgpu {
 
-constexpr int kClipResolveThreads = 256;
+constexpr int kClipResolveThreads = 32;
 
 struct ClipCounters {
   unsigned n_touch;     // touching triangles
@@ -145,23 +145,20 @@ struct Resolver {
   ClipCounters* cnt;
 };
 
-// Thread 0 owns all table updates; the position scan is CTA-parallel.
-__device__ int find_near(Resolver& R, const double* p, int n, int* red) {
+// One warp resolves the touching triangles in order. Lane 0 owns every table
+// update; the position scan runs across the 32 lanes (first match = smallest
+// index with all three coordinates within 1e-4).
+__device__ int find_near(Resolver& R, const double* p, int n) {
   int best = 0x7fffffff;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+  for (int i = (int)(threadIdx.x & 31); i < n; i += 32) {
     const double* q = R.border + 3 * (int64_t)i;
     if (fabs(ds(q[0], p[0])) < 1e-4 && fabs(ds(q[1], p[1])) < 1e-4 && fabs(ds(q[2], p[2])) < 1e-4) {
       best = i;
       break;
     }
   }
-  for (int o = 16; o; o >>= 1) best = min(best, __shfl_xor_sync(0xffffffffu, best, o));
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = best;
-  __syncthreads();
-  int r = 0x7fffffff;
-  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = min(r, red[w]);
-  __syncthreads();
-  return r == 0x7fffffff ? -1 : r;
+  best = __reduce_min_sync(0xffffffffu, best);
+  return best == 0x7fffffff ? -1 : best;
 }
 
 __device__ __forceinline__ unsigned hash2(int a, int b) {
@@ -191,72 +188,56 @@ __device__ void edge_set(Resolver& R, int a, int b, int val) {
   R.cnt->overflow = 1;
 }
 
-// Border point of a mesh vertex (whole CTA calls; result broadcast).
-__device__ int vertex_point(Resolver& R, int id, int* sh, int* red) {
-  if (threadIdx.x == 0) sh[0] = R.vmap[id];
-  __syncthreads();
-  int have = sh[0];
-  __syncthreads();
-  if (have >= 0) return have;
-  const double* p = R.v + 3 * (int64_t)id;
-  int n = (int)R.cnt->n_border;
-  int f = find_near(R, p, n, red);
-  if (threadIdx.x == 0) {
-    if (f < 0) {
-      if (n < R.max_border) {
-        f = n;
-        R.border[3 * n] = p[0];
-        R.border[3 * n + 1] = p[1];
-        R.border[3 * n + 2] = p[2];
-        R.cnt->n_border = n + 1;
-      } else {
-        R.cnt->overflow = 1;
-        f = 0;
-      }
-    }
-    R.vmap[id] = f;
-    sh[0] = f;
+__device__ __forceinline__ bool lane0() { return (threadIdx.x & 31) == 0; }
+
+// Append a new border point (lane 0) or report overflow.
+__device__ int append_border(Resolver& R, const double* p, int n) {
+  if (n < R.max_border) {
+    R.border[3 * n] = p[0];
+    R.border[3 * n + 1] = p[1];
+    R.border[3 * n + 2] = p[2];
+    R.cnt->n_border = n + 1;
+    return n;
   }
-  __syncthreads();
-  int r = sh[0];
-  __syncthreads();
-  return r;
+  R.cnt->overflow = 1;
+  return 0;
 }
 
-// Border point where edge (a, b) crosses the plane (whole CTA).
-__device__ int edge_point(Resolver& R, int a, int b, const double* p, int* sh, int* red) {
-  if (threadIdx.x == 0) {
-    int x = edge_get(R, a, b);
-    if (x < 0) x = edge_get(R, b, a);
-    sh[0] = x;
-  }
-  __syncthreads();
-  int have = sh[0];
-  __syncthreads();
+// Border point of a mesh vertex (whole warp calls; result broadcast).
+__device__ int vertex_point(Resolver& R, int id) {
+  int have = lane0() ? R.vmap[id] : 0;
+  have = __shfl_sync(0xffffffffu, have, 0);
   if (have >= 0) return have;
-  int n = (int)R.cnt->n_border;
-  int f = find_near(R, p, n, red);
-  if (threadIdx.x == 0) {
-    if (f < 0) {
-      if (n < R.max_border) {
-        f = n;
-        R.border[3 * n] = p[0];
-        R.border[3 * n + 1] = p[1];
-        R.border[3 * n + 2] = p[2];
-        R.cnt->n_border = n + 1;
-      } else {
-        R.cnt->overflow = 1;
-        f = 0;
-      }
-    }
+  const int n = (int)R.cnt->n_border;
+  int f = find_near(R, R.v + 3 * (int64_t)id, n);
+  if (lane0()) {
+    if (f < 0) f = append_border(R, R.v + 3 * (int64_t)id, n);
+    R.vmap[id] = f;
+  }
+  f = __shfl_sync(0xffffffffu, f, 0);
+  __syncwarp();
+  return f;
+}
+
+// Border point where edge (a, b) crosses the plane (whole warp).
+__device__ int edge_point(Resolver& R, int a, int b, const double* p) {
+  int have = 0;
+  if (lane0()) {
+    have = edge_get(R, a, b);
+    if (have < 0) have = edge_get(R, b, a);
+  }
+  have = __shfl_sync(0xffffffffu, have, 0);
+  if (have >= 0) return have;
+  const int n = (int)R.cnt->n_border;
+  int f = find_near(R, p, n);
+  if (lane0()) {
+    if (f < 0) f = append_border(R, p, n);
     edge_set(R, a, b, f);
     edge_set(R, b, a, f);
-    sh[0] = f;
   }
-  __syncthreads();
-  int r = sh[0];
-  __syncthreads();
-  return r;
+  f = __shfl_sync(0xffffffffu, f, 0);
+  __syncwarp();
+  return f;
 }
 
 // Unique unordered border edge, in first-occurrence order (thread 0 only).
@@ -285,8 +266,6 @@ __global__ void __launch_bounds__(kClipResolveThreads) clip_resolve_kernel(
     const signed char* __restrict__ side, const int* __restrict__ list, Resolver R,
     PieceSlot* __restrict__ slots, unsigned char* __restrict__ keep_pos,
     unsigned char* __restrict__ keep_neg) {
-  __shared__ int sh[4];
-  __shared__ int red[kClipResolveThreads / 32];
   double pl[4] = {plp[0], plp[1], plp[2], plp[3]};
   const int ntouch = (int)R.cnt->n_touch;
   for (int li = 0; li < ntouch; ++li) {
@@ -307,7 +286,7 @@ __global__ void __launch_bounds__(kClipResolveThreads) clip_resolve_kernel(
       }
     };
     auto keep = [&](bool pos, int vid) {
-      if (threadIdx.x == 0) (pos ? keep_pos : keep_neg)[vid] = 1;
+      if (lane0()) (pos ? keep_pos : keep_neg)[vid] = 1;
     };
     const bool one_pos = sum == 2 || (sum == 1 && nzero == 2);
     const bool one_neg = sum == -2 || (sum == -1 && nzero == 2);
@@ -318,14 +297,14 @@ __global__ void __launch_bounds__(kClipResolveThreads) clip_resolve_kernel(
         int k1 = (k + 1) % 3, k2 = (k + 2) % 3;
         int b1, b2;
         if (sg > 0) {
-          b1 = vertex_point(R, id[k1], sh, red);
-          b2 = vertex_point(R, id[k2], sh, red);
+          b1 = vertex_point(R, id[k1]);
+          b2 = vertex_point(R, id[k2]);
         } else {
-          b2 = vertex_point(R, id[k2], sh, red);
-          b1 = vertex_point(R, id[k1], sh, red);
+          b2 = vertex_point(R, id[k2]);
+          b1 = vertex_point(R, id[k1]);
         }
         if (b1 != b2) {
-          if (threadIdx.x == 0) {
+          if (lane0()) {
             if (sg > 0) add_bedge(R, b1 + 1, b2 + 1);
             else add_bedge(R, b2 + 1, b1 + 1);
           }
@@ -334,7 +313,7 @@ __global__ void __launch_bounds__(kClipResolveThreads) clip_resolve_kernel(
         }
       } else {
         int z = s[0] == 0 ? 0 : (s[1] == 0 ? 1 : 2);
-        int bz = vertex_point(R, id[z], sh, red);
+        int bz = vertex_point(R, id[z]);
         if (z == 2) emit(sg > 0, id[0], id[1], bref(bz));
         else if (z == 0) emit(sg > 0, id[1], id[2], bref(bz));
         else emit(sg > 0, id[0], bref(bz), id[2]);
@@ -351,18 +330,18 @@ __global__ void __launch_bounds__(kClipResolveThreads) clip_resolve_kernel(
       else if (f[2] && f[0] && !f[1]) e = 2;
       if (e >= 0) {
         const int a = e, vv = (e + 1) % 3, c = (e + 2) % 3;
-        edge_point(R, id[a], id[vv], pi[a], sh, red);
-        edge_point(R, id[vv], id[c], pi[vv], sh, red);
-        if (threadIdx.x == 0) {
-          sh[1] = edge_get(R, id[a], id[vv]);
-          sh[2] = edge_get(R, id[vv], id[c]);
+        edge_point(R, id[a], id[vv], pi[a]);
+        edge_point(R, id[vv], id[c], pi[vv]);
+        int fa = 0, fv = 0;
+        if (lane0()) {
+          fa = edge_get(R, id[a], id[vv]);
+          fv = edge_get(R, id[vv], id[c]);
         }
-        __syncthreads();
-        const int fa = sh[1], fv = sh[2];
-        __syncthreads();
+        fa = __shfl_sync(0xffffffffu, fa, 0);
+        fv = __shfl_sync(0xffffffffu, fv, 0);
         const bool apex_pos = s[vv] == 1;
         if (fv != fa) {
-          if (threadIdx.x == 0) {
+          if (lane0()) {
             if (apex_pos) add_bedge(R, fv + 1, fa + 1);
             else add_bedge(R, fa + 1, fv + 1);
           }
@@ -394,26 +373,24 @@ __global__ void __launch_bounds__(kClipResolveThreads) clip_resolve_kernel(
         else if (s[2] == 0 || (all_nz && same(pi[1], pi[2]))) k = 2;
         if (k >= 0) {
           const int k1 = (k + 1) % 3, k2 = (k + 2) % 3;
-          const int bk = vertex_point(R, id[k], sh, red);
-          if (threadIdx.x == 0) {
+          const int bk = vertex_point(R, id[k]);
+          if (lane0()) {
             edge_set(R, id[k], id[k1], bk);
             edge_set(R, id[k1], id[k], bk);
             edge_set(R, id[k2], id[k], bk);
             edge_set(R, id[k], id[k2], bk);
           }
-          __syncthreads();
-          edge_point(R, id[k1], id[k2], pi[k1], sh, red);
-          if (threadIdx.x == 0) sh[3] = edge_get(R, id[k1], id[k2]);
-          __syncthreads();
-          const int fo = sh[3];
-          __syncthreads();
+          __syncwarp();
+          edge_point(R, id[k1], id[k2], pi[k1]);
+          int fo = lane0() ? edge_get(R, id[k1], id[k2]) : 0;
+          fo = __shfl_sync(0xffffffffu, fo, 0);
           const int test = (k == 0) ? s[1] : s[0];
           const int u = (k == 1) ? k2 : k1;
           const int other = (k == 1) ? k1 : k2;
           int A, Bp;
           if (k == 1) { A = bk; Bp = fo; } else { A = fo; Bp = bk; }
           if (A != Bp) {
-            if (threadIdx.x == 0) {
+            if (lane0()) {
               if (test == 1) add_bedge(R, A + 1, Bp + 1);
               else add_bedge(R, Bp + 1, A + 1);
             }
@@ -425,8 +402,8 @@ __global__ void __launch_bounds__(kClipResolveThreads) clip_resolve_kernel(
         }
       }
     }
-    if (threadIdx.x == 0) slots[li] = out;
-    __syncthreads();
+    if (lane0()) slots[li] = out;
+    __syncwarp();
   }
 }
 

@@ -6,6 +6,9 @@
 #include <stdint.h>
 
 #include <string>
+#include <algorithm>
+#include <cmath>
+#include <cstring>
 #include <unordered_map>
 #include <vector>
 
@@ -97,6 +100,7 @@ enum CtxSlot {
   kSlotTmpTris,
   kSlotVisRowTiles,
   kSlotClip,
+  kSlotHausdorff,
   kSlotCount
 };
 
@@ -153,6 +157,7 @@ enum KernelId {
   kKBitEmit,
   kKClip,
   kKClipResolve,
+  kKHausdorff,
   kKMisc,
   kKCount
 };

@@ -1,0 +1,322 @@
+// Sampled face Hausdorff distance on the GPU (the hb term of the concavity
+// metric, lib/include/hausdorff.hpp:214-298 / lib/src/cost.cpp:69-85).
+//
+// For every sample q of one surface: its 10 nearest samples on the other
+// surface (exact k-NN, FP64 squared distances), then the smallest distance
+// from q to the triangles those samples were drawn from; a lane whose minimum
+// exceeds 10 falls back to the nearest-sample distance; the result is the
+// largest minimum over both directions.
+//  * Samples are bucketed in a uniform grid (counting sort: atomic counts,
+//    exclusive scan, scatter); a query walks Chebyshev rings of cells until it
+//    holds 10 candidates no farther than the ring radius.
+//  * Point-triangle distance: closest point by Voronoi region (Ericson,
+//    Real-Time Collision Detection 5.1.5) in FP64 with explicit round-to-
+//    nearest intrinsics in the host's operation order, so values equal the
+//    host implementation's.
+#include <float.h>
+
+#include "common.cuh"
+
+namespace vgpu {
+
+constexpr int kKnn = 10;
+
+struct HGrid {
+  double lo[3];
+  double h;
+  int dim[3];
+  const int* start;   // cell -> first sorted point (size cells + 1)
+  const int* order;   // sorted point ids
+  const double* pts;  // 3 doubles per point
+  int n;
+};
+
+struct HCounters {
+  unsigned long long max_bits;  // FP64 bits of the running maximum
+  double bbox[2][6];            // per grid: lo xyz, hi xyz (ordered bits)
+  unsigned long long lo_bits[2][3], hi_bits[2][3];
+};
+
+__device__ __forceinline__ unsigned long long d2o(double d) {
+  unsigned long long b = __double_as_longlong(d);
+  return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double o2d(unsigned long long o) {
+  unsigned long long b = (o & 0x8000000000000000ull) ? (o & 0x7fffffffffffffffull) : ~o;
+  return __longlong_as_double(b);
+}
+
+__global__ void hbbox_kernel(const double* __restrict__ p, int n, unsigned long long* lo,
+                             unsigned long long* hi) {
+  double l[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, u[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    for (int a = 0; a < 3; ++a) {
+      l[a] = fmin(l[a], p[3 * (int64_t)i + a]);
+      u[a] = fmax(u[a], p[3 * (int64_t)i + a]);
+    }
+  for (int a = 0; a < 3; ++a) {
+    for (int o = 16; o; o >>= 1) {
+      l[a] = fmin(l[a], __shfl_xor_sync(0xffffffffu, l[a], o));
+      u[a] = fmax(u[a], __shfl_xor_sync(0xffffffffu, u[a], o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+      atomicMin(&lo[a], d2o(l[a]));
+      atomicMax(&hi[a], d2o(u[a]));
+    }
+  }
+}
+
+__device__ __forceinline__ int cell_coord(double x, double lo, double h, int dim) {
+  int c = (int)floor((x - lo) / h);
+  return c < 0 ? 0 : (c >= dim ? dim - 1 : c);
+}
+
+__global__ void hcount_kernel(HGrid g, int* __restrict__ counts, int* __restrict__ cell_of) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += gridDim.x * blockDim.x) {
+    const double* p = g.pts + 3 * (int64_t)i;
+    int cx = cell_coord(p[0], g.lo[0], g.h, g.dim[0]);
+    int cy = cell_coord(p[1], g.lo[1], g.h, g.dim[1]);
+    int cz = cell_coord(p[2], g.lo[2], g.h, g.dim[2]);
+    int c = (cz * g.dim[1] + cy) * g.dim[0] + cx;
+    cell_of[i] = c;
+    atomicAdd(&counts[c], 1);
+  }
+}
+
+__global__ void hscatter_kernel(int n, const int* __restrict__ cell_of, const unsigned long long* __restrict__ off,
+                                int* __restrict__ fill, int* __restrict__ order) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    int c = cell_of[i];
+    int k = atomicAdd(&fill[c], 1);
+    order[off[c] + k] = i;
+  }
+}
+
+__global__ void hstart_kernel(const unsigned long long* __restrict__ off, int cells, int* __restrict__ start) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= cells; i += gridDim.x * blockDim.x)
+    start[i] = (int)off[i];
+}
+
+__device__ __forceinline__ double dm(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double da(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double ds(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double dot3(const double* a, const double* b) {
+  return da(da(dm(a[0], b[0]), dm(a[1], b[1])), dm(a[2], b[2]));
+}
+
+// Closest point on triangle abc to p (host order of operations).
+__device__ double point_tri_dist(const double* p, const double* a, const double* b, const double* c) {
+  double ab[3] = {ds(b[0], a[0]), ds(b[1], a[1]), ds(b[2], a[2])};
+  double ac[3] = {ds(c[0], a[0]), ds(c[1], a[1]), ds(c[2], a[2])};
+  double ap[3] = {ds(p[0], a[0]), ds(p[1], a[1]), ds(p[2], a[2])};
+  double cp[3];
+  double d1 = dot3(ab, ap), d2 = dot3(ac, ap);
+  if (d1 <= 0 && d2 <= 0) {
+    cp[0] = a[0]; cp[1] = a[1]; cp[2] = a[2];
+  } else {
+    double bp[3] = {ds(p[0], b[0]), ds(p[1], b[1]), ds(p[2], b[2])};
+    double d3 = dot3(ab, bp), d4 = dot3(ac, bp);
+    double vc = ds(dm(d1, d4), dm(d3, d2));
+    double cpv[3] = {ds(p[0], c[0]), ds(p[1], c[1]), ds(p[2], c[2])};
+    double d5 = dot3(ab, cpv), d6 = dot3(ac, cpv);
+    double vb = ds(dm(d5, d2), dm(d1, d6));
+    double va = ds(dm(d3, d6), dm(d5, d4));
+    if (d3 >= 0 && d4 <= d3) {
+      cp[0] = b[0]; cp[1] = b[1]; cp[2] = b[2];
+    } else if (vc <= 0 && d1 >= 0 && d3 <= 0) {
+      double v = __ddiv_rn(d1, ds(d1, d3));
+      for (int k = 0; k < 3; ++k) cp[k] = da(a[k], dm(ab[k], v));
+    } else if (d6 >= 0 && d5 <= d6) {
+      cp[0] = c[0]; cp[1] = c[1]; cp[2] = c[2];
+    } else if (vb <= 0 && d2 >= 0 && d6 <= 0) {
+      double w = __ddiv_rn(d2, ds(d2, d6));
+      for (int k = 0; k < 3; ++k) cp[k] = da(a[k], dm(ac[k], w));
+    } else if (va <= 0 && ds(d4, d3) >= 0 && ds(d5, d6) >= 0) {
+      double w = __ddiv_rn(ds(d4, d3), da(ds(d4, d3), ds(d5, d6)));
+      for (int k = 0; k < 3; ++k) cp[k] = da(b[k], dm(ds(c[k], b[k]), w));
+    } else {
+      double denom = __ddiv_rn(1.0, da(da(va, vb), vc));
+      double v = dm(vb, denom), w = dm(vc, denom);
+      for (int k = 0; k < 3; ++k) cp[k] = da(da(a[k], dm(ab[k], v)), dm(ac[k], w));
+    }
+  }
+  double dx = ds(p[0], cp[0]), dy = ds(p[1], cp[1]), dz = ds(p[2], cp[2]);
+  return __dsqrt_rn(da(da(dm(dx, dx), dm(dy, dy)), dm(dz, dz)));
+}
+
+// One direction: queries Q against the other surface (grid G over its samples,
+// sample triangle ids, mesh verts/tris).
+__global__ void __launch_bounds__(128) hquery_kernel(const double* __restrict__ Q, int nq, HGrid G,
+                                                     const int* __restrict__ ids,
+                                                     const double* __restrict__ mv,
+                                                     const int* __restrict__ mt,
+                                                     unsigned long long* __restrict__ out_max) {
+  double local = 0.0;
+  for (int qi = blockIdx.x * blockDim.x + threadIdx.x; qi < nq; qi += gridDim.x * blockDim.x) {
+    const double q[3] = {Q[3 * (int64_t)qi], Q[3 * (int64_t)qi + 1], Q[3 * (int64_t)qi + 2]};
+    double bd[kKnn];
+    int bi[kKnn];
+    int cnt = 0;
+    const int cx = cell_coord(q[0], G.lo[0], G.h, G.dim[0]);
+    const int cy = cell_coord(q[1], G.lo[1], G.h, G.dim[1]);
+    const int cz = cell_coord(q[2], G.lo[2], G.h, G.dim[2]);
+    const int rmax = max(G.dim[0], max(G.dim[1], G.dim[2]));
+    for (int r = 0; r <= rmax; ++r) {
+      for (int dz = -r; dz <= r; ++dz) {
+        const int z = cz + dz;
+        if (z < 0 || z >= G.dim[2]) continue;
+        for (int dy = -r; dy <= r; ++dy) {
+          const int y = cy + dy;
+          if (y < 0 || y >= G.dim[1]) continue;
+          const bool face = abs(dz) == r || abs(dy) == r;
+          for (int dx = -r; dx <= r; dx += (face ? 1 : 2 * r > 0 ? 2 * r : 1)) {
+            const int x = cx + dx;
+            if (x >= 0 && x < G.dim[0]) {
+              const int c = (z * G.dim[1] + y) * G.dim[0] + x;
+              for (int k = G.start[c]; k < G.start[c + 1]; ++k) {
+                const int pi = G.order[k];
+                const double* pp = G.pts + 3 * (int64_t)pi;
+                const double ex = ds(pp[0], q[0]), ey = ds(pp[1], q[1]), ez = ds(pp[2], q[2]);
+                const double d2 = da(da(dm(ex, ex), dm(ey, ey)), dm(ez, ez));
+                if (cnt < kKnn || d2 < bd[cnt - 1]) {
+                  int j = cnt < kKnn ? cnt++ : kKnn - 1;
+                  while (j > 0 && bd[j - 1] > d2) {
+                    bd[j] = bd[j - 1];
+                    bi[j] = bi[j - 1];
+                    --j;
+                  }
+                  bd[j] = d2;
+                  bi[j] = pi;
+                }
+              }
+            }
+            if (dx == r) break;
+          }
+        }
+      }
+      const double rad = (double)r * G.h;
+      if (cnt == kKnn && bd[kKnn - 1] <= rad * rad) break;
+      if (cnt == G.n && r >= rmax) break;
+    }
+    double cmin = DBL_MAX;
+    for (int j = 0; j < cnt; ++j) {
+      const int tri = ids[bi[j]];
+      const int* t = mt + 3 * (int64_t)tri;
+      const double d = point_tri_dist(q, mv + 3 * (int64_t)t[0], mv + 3 * (int64_t)t[1], mv + 3 * (int64_t)t[2]);
+      if (d < cmin) {
+        cmin = d;
+        if (cmin < 1e-14) break;
+      }
+    }
+    if (cmin > 10 && cnt > 0) cmin = __dsqrt_rn(bd[0]);
+    if (cmin > local && DBL_MAX > cmin) local = cmin;
+  }
+  for (int o = 16; o; o >>= 1) local = fmax(local, __shfl_xor_sync(0xffffffffu, local, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out_max, (unsigned long long)__double_as_longlong(local));
+}
+
+}  // namespace vgpu
+
+using namespace vgpu;
+
+namespace {
+size_t al(size_t x) { return (x + 255) & ~size_t(255); }
+}
+
+extern "C" int visacd_face_hausdorff(visacd_ctx* ctx, const double* va, int32_t nva, const int32_t* ta,
+                                     int32_t nta, const double* xa, const int32_t* ida, int32_t na,
+                                     const double* vb, int32_t nvb, const int32_t* tb, int32_t ntb,
+                                     const double* xb, const int32_t* idb, int32_t nb, double* out) {
+  VCHECK(ctx && out, VISACD_ERR_INVALID_ARG, "face_hausdorff: null argument");
+  VCHECK(na > 0 && nb > 0 && nva > 0 && nvb > 0 && nta > 0 && ntb > 0, VISACD_ERR_INVALID_ARG,
+         "face_hausdorff: empty input");
+  VCUDA(cudaSetDevice(ctx->device));
+  // Grid shape from the sample counts: about 2 samples per occupied cell on a
+  // surface; at most 160 cells per axis.
+  auto grid_for_points = [](const double* x, int n, HGrid& g) {
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int i = 0; i < n; ++i)
+      for (int a = 0; a < 3; ++a) {
+        lo[a] = std::min(lo[a], x[3 * (int64_t)i + a]);
+        hi[a] = std::max(hi[a], x[3 * (int64_t)i + a]);
+      }
+    double ext = std::max(hi[0] - lo[0], std::max(hi[1] - lo[1], hi[2] - lo[2]));
+    double area_like = 0;
+    for (int a = 0; a < 3; ++a) area_like += (hi[a] - lo[a]) * (hi[(a + 1) % 3] - lo[(a + 1) % 3]);
+    double h = std::sqrt(std::max(area_like, 1e-30) * 2.0 / std::max(n, 1));
+    h = std::max(h, ext / 160.0);
+    if (!(h > 0)) h = 1.0;
+    for (int a = 0; a < 3; ++a) {
+      g.lo[a] = lo[a];
+      g.dim[a] = std::max(1, (int)std::ceil((hi[a] - lo[a]) / h) + 1);
+    }
+    g.h = h;
+    g.n = n;
+  };
+  HGrid ga, gb;
+  grid_for_points(xa, na, ga);
+  grid_for_points(xb, nb, gb);
+  const int cells_a = ga.dim[0] * ga.dim[1] * ga.dim[2], cells_b = gb.dim[0] * gb.dim[1] * gb.dim[2];
+  size_t off = 0;
+  auto carve = [&](size_t b) { size_t o = off; off += al(b); return o; };
+  const size_t o_va = carve((size_t)nva * 24), o_ta = carve((size_t)nta * 12), o_xa = carve((size_t)na * 24),
+               o_ia = carve((size_t)na * 4), o_vb = carve((size_t)nvb * 24), o_tb = carve((size_t)ntb * 12),
+               o_xb = carve((size_t)nb * 24), o_ib = carve((size_t)nb * 4),
+               o_ca = carve((size_t)(cells_a + 1) * 4), o_cb = carve((size_t)(cells_b + 1) * 4),
+               o_fa = carve((size_t)cells_a * 4), o_fb = carve((size_t)cells_b * 4),
+               o_oa = carve((size_t)(cells_a + 1) * 8), o_ob = carve((size_t)(cells_b + 1) * 8),
+               o_sa = carve((size_t)(cells_a + 1) * 4), o_sb = carve((size_t)(cells_b + 1) * 4),
+               o_ra = carve((size_t)na * 4), o_rb = carve((size_t)nb * 4), o_cla = carve((size_t)na * 4),
+               o_clb = carve((size_t)nb * 4), o_mx = carve(64);
+  VTRY(ensure_slot(ctx, kSlotHausdorff, off));
+  char* B = slot<char>(ctx, kSlotHausdorff);
+  cudaStream_t st = ctx->stream;
+  VCUDA(cudaMemcpyAsync(B + o_va, va, (size_t)nva * 24, cudaMemcpyHostToDevice, st));
+  VCUDA(cudaMemcpyAsync(B + o_ta, ta, (size_t)nta * 12, cudaMemcpyHostToDevice, st));
+  VCUDA(cudaMemcpyAsync(B + o_xa, xa, (size_t)na * 24, cudaMemcpyHostToDevice, st));
+  VCUDA(cudaMemcpyAsync(B + o_ia, ida, (size_t)na * 4, cudaMemcpyHostToDevice, st));
+  VCUDA(cudaMemcpyAsync(B + o_vb, vb, (size_t)nvb * 24, cudaMemcpyHostToDevice, st));
+  VCUDA(cudaMemcpyAsync(B + o_tb, tb, (size_t)ntb * 12, cudaMemcpyHostToDevice, st));
+  VCUDA(cudaMemcpyAsync(B + o_xb, xb, (size_t)nb * 24, cudaMemcpyHostToDevice, st));
+  VCUDA(cudaMemcpyAsync(B + o_ib, idb, (size_t)nb * 4, cudaMemcpyHostToDevice, st));
+  VCUDA(cudaMemsetAsync(B + o_ca, 0, (size_t)(cells_a + 1) * 4, st));
+  VCUDA(cudaMemsetAsync(B + o_cb, 0, (size_t)(cells_b + 1) * 4, st));
+  VCUDA(cudaMemsetAsync(B + o_fa, 0, (size_t)cells_a * 4, st));
+  VCUDA(cudaMemsetAsync(B + o_fb, 0, (size_t)cells_b * 4, st));
+  VCUDA(cudaMemsetAsync(B + o_mx, 0, 64, st));
+  ga.pts = (const double*)(B + o_xa);
+  gb.pts = (const double*)(B + o_xb);
+  // Bucket both sample sets.
+  struct Side { HGrid* g; int cells; size_t o_c, o_f, o_o, o_s, o_r, o_cl; int n; };
+  Side sides[2] = {{&ga, cells_a, o_ca, o_fa, o_oa, o_sa, o_ra, o_cla, na},
+                   {&gb, cells_b, o_cb, o_fb, o_ob, o_sb, o_rb, o_clb, nb}};
+  for (auto& sd : sides) {
+    int* counts = (int*)(B + sd.o_c);
+    int* cell_of = (int*)(B + sd.o_cl);
+    const unsigned gn = grid_for(sd.n, 256, 8LL * ctx->sm_count);
+    VLAUNCH(ctx, kKHausdorff, gn, 256, 0, hcount_kernel, *sd.g, counts, cell_of);
+    VTRY(exclusive_scan_u32_to_u64(ctx, (const uint32_t*)counts, (uint64_t*)(B + sd.o_o), sd.cells));
+    VLAUNCH(ctx, kKHausdorff, gn, 256, 0, hscatter_kernel, sd.n, cell_of,
+            (const unsigned long long*)(B + sd.o_o), (int*)(B + sd.o_f), (int*)(B + sd.o_r));
+    VLAUNCH(ctx, kKHausdorff, grid_for(sd.cells + 1, 256, 8LL * ctx->sm_count), 256, 0, hstart_kernel,
+            (const unsigned long long*)(B + sd.o_o), sd.cells, (int*)(B + sd.o_s));
+    sd.g->start = (const int*)(B + sd.o_s);
+    sd.g->order = (const int*)(B + sd.o_r);
+  }
+  unsigned long long* mx = (unsigned long long*)(B + o_mx);
+  // Queries of B against A's samples/triangles, then A against B.
+  VLAUNCH(ctx, kKHausdorff, grid_for(nb, 128, 8LL * ctx->sm_count), 128, 0, hquery_kernel,
+          (const double*)(B + o_xb), nb, ga, (const int*)(B + o_ia), (const double*)(B + o_va),
+          (const int*)(B + o_ta), mx);
+  VLAUNCH(ctx, kKHausdorff, grid_for(na, 128, 8LL * ctx->sm_count), 128, 0, hquery_kernel,
+          (const double*)(B + o_xa), na, gb, (const int*)(B + o_ib), (const double*)(B + o_vb),
+          (const int*)(B + o_tb), mx);
+  unsigned long long* h = nullptr;
+  VTRY(pinned(ctx, 8, (void**)&h));
+  VCUDA(cudaMemcpyAsync(h, mx, 8, cudaMemcpyDeviceToHost, st));
+  VCUDA(cudaStreamSynchronize(st));
+  double r;
+  memcpy(&r, h, 8);
+  *out = r;
+  return VISACD_OK;
+}

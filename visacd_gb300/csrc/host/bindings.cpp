@@ -87,7 +87,8 @@ PYBIND11_MODULE(visacd, m) {
       .def_readwrite("flat_surface_k", &Config::flat_surface_k)
       .def_readwrite("use_merging", &Config::use_merging)
       .def_readwrite("verbose", &Config::verbose)
-      .def_readwrite("gpu_clip", &Config::gpu_clip);
+      .def_readwrite("gpu_clip", &Config::gpu_clip)
+      .def_readwrite("gpu_concavity", &Config::gpu_concavity);
 
   m.def("make_vecarray3i", [](py::array_t<int, py::array::c_style | py::array::forcecast> a) {
     auto buf = a.request();

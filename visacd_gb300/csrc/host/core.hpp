@@ -91,7 +91,8 @@ struct Config {
   bool use_merging = false;
   // Additions of this implementation (not in the reference's Config).
   bool verbose = true;   // the "[visacd] ..." progress lines
-  bool gpu_clip = true;  // split parts with the GPU clip kernels (else the host clip)
+  bool gpu_clip = true;        // split parts with the GPU clip kernels (else the host clip)
+  bool gpu_concavity = true;   // Hausdorff term of the concavity metric on the GPU
 };
 
 Config& config();

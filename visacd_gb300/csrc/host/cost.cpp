@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "geometry.hpp"
+#include "gpu_bridge.hpp"
 
 namespace visacd {
 
@@ -191,6 +192,7 @@ double compute_hb(const Mesh& a, const Mesh& b, unsigned int resolution) {
   extract_point_set(a, s1, i1, resolution, 1, true);
   extract_point_set(b, s2, i2, resolution, 1, true);
   if (s1.empty() || s2.empty()) return kInf;
+  if (config().gpu_concavity) return gpu::face_hausdorff(a, s1, i1, b, s2, i2);
   return face_hausdorff(a, s1, i1, b, s2, i2);
 }
 

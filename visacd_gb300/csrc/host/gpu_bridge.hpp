@@ -27,6 +27,10 @@ std::vector<double> score_planes(const std::vector<Plane>& planes, const std::ve
 MeshList clip(const Mesh& mesh, const Plane& plane, std::vector<int>& pos_map,
               std::vector<int>& neg_map);
 
+// Sampled face Hausdorff distance on the GPU (visacd_face_hausdorff).
+double face_hausdorff(const Mesh& A, const std::vector<Vec3>& XA, const std::vector<int>& idA,
+                      const Mesh& B, const std::vector<Vec3>& XB, const std::vector<int>& idB);
+
 struct Counters {
   long long vis_calls = 0, vis_pairs = 0, vis_edges = 0, score_calls = 0, plane_edge_pairs = 0;
   double vis_ms = 0, score_ms = 0;
