@@ -452,6 +452,71 @@ def run_precision_sweep(args) -> dict:
     return {"precision_sweep": rows, "fp32_peak_tflops": fp32_peak}
 
 
+def batch_parts(n_parts: int, seed: int = 7):
+    """The batching workload: displaced blobs of subdivision drawn uniformly
+    from {2, 3, 4, 5} with independent seeds, 0.03 offset cages, and 512
+    candidate planes per part (normals uniform on the sphere, offsets uniform
+    over the part's projection on the normal)."""
+    from visacd_gb300 import meshgen
+
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n_parts):
+        lv = int(rng.integers(2, 6))
+        v, t = meshgen.displaced_blob(lv, seed=int(rng.integers(1 << 30)))
+        cv, ct = meshgen.offset_cage(v, t, 0.03)
+        nrm = rng.normal(size=(512, 3))
+        nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+        proj = v @ nrm.T
+        d = -rng.uniform(proj.min(0), proj.max(0))
+        out.append((v.astype(np.float32), t, cv, ct, np.concatenate([nrm, d[:, None]], 1).astype(np.float32)))
+    return out
+
+
+def run_batching(args) -> dict:
+    """One graph-captured launch sequence over all parts vs per-part calls of
+    the plain entry points (visibility then scoring, part by part)."""
+    import torch
+
+    from visacd_gb300 import _native, build
+
+    build.build_gpu()
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx = _native.Context(0, stream.cuda_stream)
+    parts = batch_parts(args.batch_parts)
+    bv = [(v, ctx.bvh(v, t), ctx.bvh(cv, ct), pl) for v, t, cv, ct, pl in parts]
+    batch = _native.Batch(ctx, bv)
+    pairs, planes = batch.info()
+    batch.run(True)  # capture + first replay
+    batch.results()
+    times = []
+    for _ in range(max(args.steps, 2)):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        batch.run(True)
+        b.record(stream)
+        torch.cuda.synchronize()
+        times.append(a.elapsed_time(b))
+    ne, scores, am, _ = batch.results()
+    t_batch = float(np.median(times)) / 1e3
+    # Plain: per-part C-ABI calls (device-resident points, host sync per call).
+    t0 = time.perf_counter()
+    for v, sb, cb, pl in bv:
+        e, _ = ctx.visibility(v, sb, cb)
+        if len(e):
+            ctx.score_planes(pl, v, e)
+    torch.cuda.synchronize()
+    t_plain = time.perf_counter() - t0
+    batch.close()
+    return {"batching": {"parts": len(parts), "pairs": pairs, "planes": planes, "edges": int(ne.sum()),
+                         "graph_run_s": t_batch, "plain_loop_s": t_plain,
+                         "batched_pairs_per_s": pairs / t_batch, "plain_pairs_per_s": pairs / t_plain,
+                         "parts_per_s_batched": len(parts) / t_batch, "parts_per_s_plain": len(parts) / t_plain,
+                         "speedup": t_plain / t_batch}}
+
+
 def run_reference(args) -> dict:
     """CPU restatement (oracle, FP64, OpenMP) on a bounded sample of pair rows."""
     import oracle
@@ -517,10 +582,15 @@ def main():
     ap.add_argument("--no-process", action="store_true", help="skip the end-to-end decompositions")
     ap.add_argument("--workload", default="blob_s5", choices=sorted(WORKLOADS))
     ap.add_argument("--sweep", action="store_true", help="scoring precision sweep only")
+    ap.add_argument("--batch", action="store_true", help="batching workload only")
+    ap.add_argument("--batch-parts", type=int, default=256)
     ap.add_argument("--sweep-sizes", type=int, nargs="+", default=[20, 22, 24, 26])
     args = ap.parse_args()
     if args.sweep:
         print(json.dumps(run_precision_sweep(args)))
+        return
+    if args.batch:
+        print(json.dumps(run_batching(args)))
         return
     if args.impl == "reference":
         out, rank = run_reference(args)

@@ -49,6 +49,7 @@ typedef enum {
 
 typedef struct visacd_ctx visacd_ctx;
 typedef struct visacd_bvh visacd_bvh;
+typedef struct visacd_batch visacd_batch;
 
 /* Counters of one visibility call. */
 typedef struct {
@@ -173,6 +174,30 @@ int visacd_compute_intersection_matrix(visacd_ctx* ctx, const float* verts, int3
 int visacd_score_planes(visacd_ctx* ctx, const float* planes, int32_t P, const float* points,
                         int32_t N, const uint32_t* edges, int64_t E, int device_ptrs,
                         double* scores, visacd_score_stats* stats);
+
+/* ---- batched visibility + scoring ----------------------------------------- */
+/* A batch of parts of uneven size, each with its points (n x 3 float32, host),
+   its own BVH (built from those points), its cage BVH and its candidate planes
+   (P x 4 float32, host). visacd_batch_run then computes every part's
+   visibility edges (all pairs i < j) and scores every part's planes against
+   them in one fixed kernel sequence whose sizes live in device memory; with
+   use_graph it is captured once as a CUDA graph and replayed. edge_capacity
+   bounds the edges of all parts together (0 = total pairs / 64 + 4096). The
+   BVHs must outlive the batch. Results equal per-part visacd_visibility +
+   visacd_score_planes. Not thread-safe; one run at a time per batch. */
+int visacd_batch_create(visacd_ctx* ctx, int32_t n_parts, const float* const* pts,
+                        const int32_t* n_pts, const visacd_bvh* const* self_bvhs,
+                        const visacd_bvh* const* cage_bvhs, const float* const* planes,
+                        const int32_t* n_planes, int64_t edge_capacity, visacd_batch** out);
+/* Enqueue one run on the context stream (asynchronous). */
+int visacd_batch_run(visacd_ctx* ctx, visacd_batch* b, int use_graph);
+/* Wait for the run and copy results: per-part edge counts, all scores
+   (float64, parts concatenated in order), per-part first argmax, and
+   optionally all edges (parts concatenated, part-local vertex ids). */
+int visacd_batch_results(visacd_ctx* ctx, visacd_batch* b, int64_t* n_edges, double* scores,
+                         int32_t* argmax, uint32_t* edges, int64_t edge_capacity);
+int visacd_batch_info(const visacd_batch* b, int64_t* total_pairs, int64_t* total_planes);
+int visacd_batch_destroy(visacd_batch* b);
 
 /* ---- per-part clipping --------------------------------------------------- */
 /* Split a mesh (float64 vertices nv x 3, int32 triangles nt x 3) by the plane

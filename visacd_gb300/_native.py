@@ -24,6 +24,8 @@ EXPORTED = [
     "visacd_vis_variant_count", "visacd_ctx_set_vis_variant", "visacd_autotune_visibility",
     "visacd_score_planes", "visacd_score_planes_noalloc", "classify_and_rate_planes",
     "visacd_clip", "visacd_clip_fetch", "visacd_measure_fp32_peak", "visacd_face_hausdorff",
+    "visacd_batch_create", "visacd_batch_run", "visacd_batch_results", "visacd_batch_info",
+    "visacd_batch_destroy",
 ]
 
 
@@ -86,6 +88,12 @@ def load() -> C.CDLL:
     lib.visacd_score_planes_noalloc.argtypes = [P, i32, P, i32, P, i64, P, P, P]
     lib.visacd_clip.argtypes = [P, P, i32, P, i32, P, C.POINTER(ClipResult)]
     lib.visacd_measure_fp32_peak.argtypes = [P, C.POINTER(C.c_double)]
+    lib.visacd_batch_create.argtypes = [P, i32, C.POINTER(P), P, C.POINTER(P), C.POINTER(P), C.POINTER(P),
+                                        P, i64, C.POINTER(P)]
+    lib.visacd_batch_run.argtypes = [P, P, C.c_int]
+    lib.visacd_batch_results.argtypes = [P, P, P, P, P, P, i64]
+    lib.visacd_batch_info.argtypes = [P, C.POINTER(i64), C.POINTER(i64)]
+    lib.visacd_batch_destroy.argtypes = [P]
     lib.visacd_face_hausdorff.argtypes = [P, P, i32, P, i32, P, P, i32, P, i32, P, i32, P, P, i32,
                                           C.POINTER(C.c_double)]
     lib.visacd_clip_fetch.argtypes = [P, P, P, P, P, P, P]
@@ -267,6 +275,68 @@ class Context:
                                          C.c_void_p(d_edges), E, 1, C.c_void_p(d_scores),
                                          C.byref(st) if stats else None), "visacd_score_planes")
         return st.as_dict() if stats else None
+
+
+class Batch:
+    """visacd_batch: many parts' visibility + scoring in one launch sequence."""
+
+    def __init__(self, ctx: "Context", parts):
+        """parts: list of (points (n,3), Bvh self, Bvh cage, planes (P,4))."""
+        self._ctx = ctx
+        self._keep = []
+        n = len(parts)
+        pts_ptrs = (C.c_void_p * n)()
+        sb = (C.c_void_p * n)()
+        cb = (C.c_void_p * n)()
+        pl_ptrs = (C.c_void_p * n)()
+        npts = np.zeros(n, np.int32)
+        npl = np.zeros(n, np.int32)
+        for k, (pts, s, c, pl) in enumerate(parts):
+            p = _f32(pts, 3)
+            q = _f32(pl, 4)
+            self._keep += [p, q, s, c]
+            pts_ptrs[k] = p.ctypes.data
+            pl_ptrs[k] = q.ctypes.data
+            sb[k] = s.handle.value
+            cb[k] = c.handle.value
+            npts[k] = len(p)
+            npl[k] = len(q)
+        self.n_planes = npl
+        self._h = C.c_void_p()
+        _check(lib().visacd_batch_create(ctx.handle, n, pts_ptrs, _ptr(npts), sb, cb, pl_ptrs, _ptr(npl), 0,
+                                         C.byref(self._h)), "visacd_batch_create")
+        self.n_parts = n
+
+    def run(self, use_graph: bool = True) -> None:
+        _check(lib().visacd_batch_run(self._ctx.handle, self._h, int(use_graph)), "visacd_batch_run")
+
+    def info(self):
+        a, b = C.c_int64(), C.c_int64()
+        _check(lib().visacd_batch_info(self._h, C.byref(a), C.byref(b)), "batch_info")
+        return a.value, b.value
+
+    def results(self, with_edges: bool = False):
+        ne = np.zeros(self.n_parts, np.int64)
+        scores = np.zeros(int(self.n_planes.sum()), np.float64)
+        am = np.zeros(self.n_parts, np.int32)
+        _check(lib().visacd_batch_results(self._ctx.handle, self._h, _ptr(ne), None, None, None, 0),
+               "batch_results")
+        edges = np.zeros((int(ne.sum()), 2), np.uint32) if with_edges else None
+        _check(lib().visacd_batch_results(self._ctx.handle, self._h, _ptr(ne), _ptr(scores), _ptr(am),
+                                          _ptr(edges) if with_edges else None, int(ne.sum())),
+               "batch_results")
+        return ne, scores, am, edges
+
+    def close(self):
+        if self._h:
+            lib().visacd_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):  # pragma: no cover
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Bvh:
