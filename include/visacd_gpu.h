@@ -230,6 +230,49 @@ int visacd_face_hausdorff(visacd_ctx* ctx, const double* va, int32_t nva, const 
                           const double* vb, int32_t nvb, const int32_t* tb, int32_t ntb,
                           const double* xb, const int32_t* idb, int32_t nb, double* out);
 
+/* ---- learned plane proposer ---------------------------------------------- */
+/* No counterpart in the reference: a small network that proposes split planes
+   in place of the random candidate draw of lib/src/process.cpp:28-72, whose
+   proposals the exact scoring above still ranks. Per part, 2048 visibility
+   edges are sampled (edge floor(s*E/2048), or s mod E when E < 2048) and
+   described by 7 features in the part's frame x' = (x - center) / scale:
+   midpoint, unit direction with its largest component positive, length.
+   Network: 7 (padded to 16) -> 64 -> 128 -> 256 shared per-edge layers (ReLU),
+   max over the edges, 256 -> 128 -> 64 (ReLU) -> 64 = 16 planes (normal xyz,
+   offset). BF16 tensor-core operands, FP32 accumulation, FP32 master weights.
+   Parameters are laid out layer by layer, each as W (out x in, row-major)
+   followed by b (out): 87,744 floats. */
+#define VISACD_LP_POINTS 2048
+#define VISACD_LP_FEATURES 7
+#define VISACD_LP_PLANES 16
+typedef struct visacd_lp visacd_lp;
+
+int visacd_lp_param_count(void);
+/* params: 87,744 floats, or NULL for a seeded He-uniform initialisation. */
+int visacd_lp_create(visacd_ctx* ctx, const float* params, uint32_t seed, visacd_lp** out);
+int visacd_lp_destroy(visacd_lp* lp);
+int visacd_lp_get_params(visacd_lp* lp, float* out);
+/* Features of one part (points n x 3 float32, edges E x 2 uint32, host) into
+   feats_out (2048 x 7 float32, host). */
+int visacd_lp_features(visacd_lp* lp, const float* points, int32_t n, const uint32_t* edges,
+                       int64_t E, const float* center, float scale, float* feats_out);
+/* Planes for B parts from their features (B x 2048 x 7): planes_out B x 16 x 4
+   float32 (unit normal, offset) in each part's normalised frame. */
+int visacd_lp_forward(visacd_lp* lp, const float* feats, int32_t B, float* planes_out);
+/* Features + forward for one part; planes_out 16 x 4 float64 in the input frame. */
+int visacd_lp_propose(visacd_lp* lp, const float* points, int32_t n, const uint32_t* edges,
+                      int64_t E, const float* center, float scale, double* planes_out);
+/* Loss and gradients for B parts with L label planes each (labels B x L x 4
+   float32 in the normalised frame, weights B x L; weight 0 = unused slot).
+   Loss per part: sum_l w_l min_q D(q,l) / sum_l w_l + 0.1/16 sum_q min_l D(q,l)
+   with D = min over the normal's sign of |n_q - n_l|^2 + (d_q - d_l)^2; the
+   batch loss is the mean. grads_out: 87,744 floats or NULL. */
+int visacd_lp_grads(visacd_lp* lp, const float* feats, const float* labels, const float* lw,
+                    int32_t B, int32_t L, float* grads_out, float* loss_out);
+/* visacd_lp_grads followed by one Adam step (beta 0.9 / 0.999, eps 1e-8). */
+int visacd_lp_train_step(visacd_lp* lp, const float* feats, const float* labels, const float* lw,
+                         int32_t B, int32_t L, float lr, float* loss_out);
+
 /* Allocation-free variant of visacd_score_planes. No counterpart in the
    reference: it exists for callers that cannot allocate — code running under a
    fixed, pre-reserved memory budget, or a latency-bound loop where cudaMalloc's

@@ -26,7 +26,14 @@ EXPORTED = [
     "visacd_clip", "visacd_clip_fetch", "visacd_measure_fp32_peak", "visacd_face_hausdorff",
     "visacd_batch_create", "visacd_batch_run", "visacd_batch_results", "visacd_batch_info",
     "visacd_batch_destroy",
+    "visacd_lp_param_count", "visacd_lp_create", "visacd_lp_destroy", "visacd_lp_get_params",
+    "visacd_lp_features", "visacd_lp_forward", "visacd_lp_propose", "visacd_lp_grads",
+    "visacd_lp_train_step",
 ]
+
+LP_POINTS = 2048
+LP_FEATURES = 7
+LP_PLANES = 16
 
 
 class ClipResult(C.Structure):
@@ -99,6 +106,15 @@ def load() -> C.CDLL:
     lib.visacd_clip_fetch.argtypes = [P, P, P, P, P, P, P]
     lib.classify_and_rate_planes.argtypes = [P, P, P, P, C.c_int, C.c_int, C.c_int]
     lib.classify_and_rate_planes.restype = None
+    lib.visacd_lp_param_count.argtypes = []
+    lib.visacd_lp_create.argtypes = [P, P, C.c_uint32, C.POINTER(P)]
+    lib.visacd_lp_destroy.argtypes = [P]
+    lib.visacd_lp_get_params.argtypes = [P, P]
+    lib.visacd_lp_features.argtypes = [P, P, i32, P, i64, P, C.c_float, P]
+    lib.visacd_lp_forward.argtypes = [P, P, i32, P]
+    lib.visacd_lp_propose.argtypes = [P, P, i32, P, i64, P, C.c_float, P]
+    lib.visacd_lp_grads.argtypes = [P, P, P, P, i32, i32, P, P]
+    lib.visacd_lp_train_step.argtypes = [P, P, P, P, i32, i32, C.c_float, P]
     return lib
 
 
@@ -381,3 +397,81 @@ def classify_and_rate_planes(planes, points, edges) -> np.ndarray:
     out = np.zeros(len(pl), dtype=np.float32)
     lib().classify_and_rate_planes(_ptr(pl), _ptr(pt), _ptr(ed), _ptr(out), len(pl), len(pt), len(ed))
     return out
+
+
+class PlaneProposer:
+    """The learned plane proposer (visacd_lp_*): BF16 tensor-core network over
+    2048 sampled visibility edges -> 16 planes. `params` None = seeded init."""
+
+    def __init__(self, ctx: Context, params=None, seed: int = 0):
+        self._ctx = ctx
+        self._h = C.c_void_p()
+        self.n_params = int(lib().visacd_lp_param_count())
+        p = None
+        if params is not None:
+            p = np.ascontiguousarray(np.asarray(params, dtype=np.float32).reshape(-1))
+            if p.size != self.n_params:
+                raise ValueError(f"expected {self.n_params} parameters, got {p.size}")
+        _check(lib().visacd_lp_create(ctx.handle, _ptr(p), seed, C.byref(self._h)), "visacd_lp_create")
+
+    def params(self) -> np.ndarray:
+        out = np.empty(self.n_params, dtype=np.float32)
+        _check(lib().visacd_lp_get_params(self._h, _ptr(out)), "visacd_lp_get_params")
+        return out
+
+    def features(self, points, edges, center, scale) -> np.ndarray:
+        pt = _f32(points, 3)
+        ed = _u32(edges, 2)
+        c = np.ascontiguousarray(np.asarray(center, dtype=np.float32).reshape(3))
+        out = np.empty((LP_POINTS, LP_FEATURES), dtype=np.float32)
+        _check(lib().visacd_lp_features(self._h, _ptr(pt), len(pt), _ptr(ed), len(ed), _ptr(c),
+                                        float(scale), _ptr(out)), "visacd_lp_features")
+        return out
+
+    def forward(self, feats) -> np.ndarray:
+        f = np.ascontiguousarray(np.asarray(feats, dtype=np.float32).reshape(-1, LP_POINTS, LP_FEATURES))
+        out = np.empty((len(f), LP_PLANES, 4), dtype=np.float32)
+        _check(lib().visacd_lp_forward(self._h, _ptr(f), len(f), _ptr(out)), "visacd_lp_forward")
+        return out
+
+    def propose(self, points, edges, center, scale) -> np.ndarray:
+        pt = _f32(points, 3)
+        ed = _u32(edges, 2)
+        c = np.ascontiguousarray(np.asarray(center, dtype=np.float32).reshape(3))
+        out = np.empty((LP_PLANES, 4), dtype=np.float64)
+        _check(lib().visacd_lp_propose(self._h, _ptr(pt), len(pt), _ptr(ed), len(ed), _ptr(c),
+                                       float(scale), _ptr(out)), "visacd_lp_propose")
+        return out
+
+    @staticmethod
+    def _batch(feats, labels, weights):
+        f = np.ascontiguousarray(np.asarray(feats, dtype=np.float32).reshape(-1, LP_POINTS, LP_FEATURES))
+        lab = np.ascontiguousarray(np.asarray(labels, dtype=np.float32).reshape(len(f), -1, 4))
+        w = np.ascontiguousarray(np.asarray(weights, dtype=np.float32).reshape(len(f), lab.shape[1]))
+        return f, lab, w
+
+    def grads(self, feats, labels, weights):
+        f, lab, w = self._batch(feats, labels, weights)
+        g = np.empty(self.n_params, dtype=np.float32)
+        loss = C.c_float()
+        _check(lib().visacd_lp_grads(self._h, _ptr(f), _ptr(lab), _ptr(w), len(f), lab.shape[1], _ptr(g),
+                                     C.byref(loss)), "visacd_lp_grads")
+        return float(loss.value), g
+
+    def train_step(self, feats, labels, weights, lr: float) -> float:
+        f, lab, w = self._batch(feats, labels, weights)
+        loss = C.c_float()
+        _check(lib().visacd_lp_train_step(self._h, _ptr(f), _ptr(lab), _ptr(w), len(f), lab.shape[1],
+                                          float(lr), C.byref(loss)), "visacd_lp_train_step")
+        return float(loss.value)
+
+    def close(self) -> None:
+        if self._h:
+            lib().visacd_lp_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):  # pragma: no cover
+        try:
+            self.close()
+        except Exception:
+            pass

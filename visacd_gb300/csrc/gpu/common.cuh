@@ -158,6 +158,12 @@ enum KernelId {
   kKClip,
   kKClipResolve,
   kKHausdorff,
+  kKLpFeatures,
+  kKLpGemm,
+  kKLpPool,
+  kKLpLoss,
+  kKLpAdam,
+  kKLpMisc,
   kKMisc,
   kKCount
 };

@@ -51,7 +51,9 @@ static const char* kNames[kKCount] = {
     "radix_scan",    "radix_scatter",  "karras_build", "aabb_fit",
     "node_layout",   "vis_prep",       "visibility",   "bitset_popc",
     "scan_blocks",   "scan_top",       "scan_add",     "bitset_emit",
-    "clip",          "clip_resolve",   "face_hausdorff", "misc"};
+    "clip",          "clip_resolve",   "face_hausdorff", "lp_features",
+    "lp_gemm",       "lp_pool",        "lp_loss",      "lp_adam",
+    "lp_misc",       "misc"};
 
 const char* kernel_name(int id) { return (id >= 0 && id < kKCount) ? kNames[id] : "?"; }
 
