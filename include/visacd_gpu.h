@@ -230,6 +230,20 @@ int visacd_face_hausdorff(visacd_ctx* ctx, const double* va, int32_t nva, const 
                           const double* vb, int32_t nvb, const int32_t* tb, int32_t ntb,
                           const double* xb, const int32_t* idb, int32_t nb, double* out);
 
+/* ---- SDF remeshing (cages) ------------------------------------------------ */
+/* The iso-surface at distance `level` outside the mesh on a grid of voxel size
+   1/scale: the manifold / cage step of lib/src/preprocess.cpp:18-67 (OpenVDB
+   meshToSignedDistanceField + volumeToMesh there). Narrow-band exact distance,
+   inside/outside by the majority of x/y/z ray-crossing parities, surface-nets
+   vertices and quads split in two triangles; the same mesh, bit for bit, as
+   this project's host restatement. verts nv x 3 float64, tris nt x 3 int32
+   (host). Writes the output sizes; the mesh stays on the device until
+   visacd_sdf_fetch. Synchronizes. */
+int visacd_sdf_remesh(visacd_ctx* ctx, const double* verts, int32_t nv, const int32_t* tris,
+                      int32_t nt, double scale, double level, int32_t* out_nv, int32_t* out_nt);
+/* Copies the last remesh result: verts out_nv x 3 float64, tris out_nt x 3 int32. */
+int visacd_sdf_fetch(visacd_ctx* ctx, double* verts, int32_t* tris);
+
 /* ---- learned plane proposer ---------------------------------------------- */
 /* No counterpart in the reference: a small network that proposes split planes
    in place of the random candidate draw of lib/src/process.cpp:28-72, whose

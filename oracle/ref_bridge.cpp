@@ -19,7 +19,8 @@ std::vector<std::array<int, 3>> hull_facets_for_ref(const std::vector<double>& c
   return std::vector<std::array<int, 3>>(h.triangles.begin(), h.triangles.end());
 }
 
-// OpenVDB stand-in: this project's SDF remesh.
+// OpenVDB stand-in: this project's SDF remesh (host restatement; the GPU
+// kernels produce the same mesh).
 void remesh_for_ref(const std::vector<double>& v, const std::vector<int>& t, double scale,
                     double level, std::vector<double>& ov, std::vector<int>& ot) {
   Mesh m;
@@ -27,7 +28,7 @@ void remesh_for_ref(const std::vector<double>& v, const std::vector<int>& t, dou
   for (size_t i = 0; i < m.vertices.size(); ++i) m.vertices[i] = {v[3 * i], v[3 * i + 1], v[3 * i + 2]};
   m.triangles.resize(t.size() / 3);
   for (size_t i = 0; i < m.triangles.size(); ++i) m.triangles[i] = {t[3 * i], t[3 * i + 1], t[3 * i + 2]};
-  manifold_preprocess(m, scale, level);
+  manifold_preprocess_host(m, scale, level);
   ov.clear();
   ot.clear();
   for (auto& p : m.vertices) ov.insert(ov.end(), p.begin(), p.end());

@@ -14,7 +14,8 @@ from visacd_gb300 import build, meshgen as mg
 def V():
     build.build_host()
     from visacd_gb300 import visacd
-    visacd.config.gpu_concavity = False  # host Hausdorff: these tests run without a GPU
+    visacd.config.gpu_concavity = False  # host Hausdorff and remesh: these tests run without a GPU
+    visacd.config.gpu_remesh = False
     return visacd
 
 

@@ -16,7 +16,8 @@ if not R.available():
 def V():
     build.build_host()
     from visacd_gb300 import visacd
-    visacd.config.gpu_concavity = False  # host Hausdorff: these tests run without a GPU
+    visacd.config.gpu_concavity = False  # host Hausdorff and remesh: these tests run without a GPU
+    visacd.config.gpu_remesh = False
     return visacd
 
 

@@ -29,6 +29,7 @@ EXPORTED = [
     "visacd_lp_param_count", "visacd_lp_create", "visacd_lp_destroy", "visacd_lp_get_params",
     "visacd_lp_features", "visacd_lp_forward", "visacd_lp_propose", "visacd_lp_grads",
     "visacd_lp_train_step",
+    "visacd_sdf_remesh", "visacd_sdf_fetch",
 ]
 
 LP_POINTS = 2048
@@ -106,6 +107,8 @@ def load() -> C.CDLL:
     lib.visacd_clip_fetch.argtypes = [P, P, P, P, P, P, P]
     lib.classify_and_rate_planes.argtypes = [P, P, P, P, C.c_int, C.c_int, C.c_int]
     lib.classify_and_rate_planes.restype = None
+    lib.visacd_sdf_remesh.argtypes = [P, P, i32, P, i32, C.c_double, C.c_double, C.POINTER(i32), C.POINTER(i32)]
+    lib.visacd_sdf_fetch.argtypes = [P, P, P]
     lib.visacd_lp_param_count.argtypes = []
     lib.visacd_lp_create.argtypes = [P, P, C.c_uint32, C.POINTER(P)]
     lib.visacd_lp_destroy.argtypes = [P]
@@ -272,6 +275,19 @@ class Context:
                "visacd_clip_fetch")
         out.update(pos_tris=pt, neg_tris=nt_, pos_map=m1, neg_map=m2, border=b, border_edges=be)
         return out
+
+    # ---- SDF remesh --------------------------------------------------------
+    def sdf_remesh(self, verts, tris, scale: float, level: float):
+        """Iso-surface at `level` outside the mesh (voxel 1/scale): (verts, tris)."""
+        v = np.ascontiguousarray(np.asarray(verts, dtype=np.float64)).reshape(-1, 3)
+        t = np.ascontiguousarray(np.asarray(tris, dtype=np.int32)).reshape(-1, 3)
+        nv, nt = C.c_int32(), C.c_int32()
+        _check(lib().visacd_sdf_remesh(self._h, _ptr(v), len(v), _ptr(t), len(t), float(scale), float(level),
+                                       C.byref(nv), C.byref(nt)), "visacd_sdf_remesh")
+        ov = np.empty((nv.value, 3), np.float64)
+        ot = np.empty((nt.value, 3), np.int32)
+        _check(lib().visacd_sdf_fetch(self._h, _ptr(ov), _ptr(ot)), "visacd_sdf_fetch")
+        return ov, ot
 
     # ---- scoring -----------------------------------------------------------
     def score_planes(self, planes, points, edges):

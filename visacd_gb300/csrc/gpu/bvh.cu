@@ -275,6 +275,9 @@ int bvh_build(visacd_ctx* ctx, const float* verts, int32_t nv, const uint32_t* t
   b->nt = nt;
   b->nv = nv;
   if (nt == 0) {
+    b->ctx = ctx;
+    b->stream = ctx->stream;
+    ctx->bvhs.push_back(b);
     *out = b;
     return VISACD_OK;
   }
@@ -340,11 +343,12 @@ int bvh_build(visacd_ctx* ctx, const float* verts, int32_t nv, const uint32_t* t
   VTRY(radix_sort_u64(ctx, keys, vals, keys2, vals2, nt, 64));
 
   size_t bytes_nodes = (size_t)n_int * 64, bytes_tris = (size_t)nt * 48;
-  cudaError_t e1 = cudaMalloc(&b->nodes, bytes_nodes);
-  cudaError_t e2 = e1 == cudaSuccess ? cudaMalloc(&b->tris, bytes_tris) : e1;
+  b->stream = ctx->stream;
+  cudaError_t e1 = cudaMallocAsync((void**)&b->nodes, bytes_nodes, ctx->stream);
+  cudaError_t e2 = e1 == cudaSuccess ? cudaMallocAsync((void**)&b->tris, bytes_tris, ctx->stream) : e1;
   if (e1 != cudaSuccess || e2 != cudaSuccess) {
     cudaGetLastError();
-    if (b->nodes) cudaFree(b->nodes);
+    if (b->nodes) cudaFreeAsync(b->nodes, ctx->stream);
     delete b;
     set_error("bvh_build: device allocation failed");
     return VISACD_ERR_NO_MEMORY;
@@ -363,16 +367,26 @@ int bvh_build(visacd_ctx* ctx, const float* verts, int32_t nv, const uint32_t* t
   VCUDA(cudaMemcpyAsync(hcnt, cnt, sizeof(BuildCounters), cudaMemcpyDeviceToHost, ctx->stream));
   VCUDA(cudaStreamSynchronize(ctx->stream));
   if (hcnt->bad_index) {
-    cudaFree(b->nodes);
-    cudaFree(b->tris);
+    cudaFreeAsync(b->nodes, ctx->stream);
+    cudaFreeAsync(b->tris, ctx->stream);
     delete b;
     set_error("bvh_build: a triangle references a vertex index >= %d", nv);
     return VISACD_ERR_INVALID_ARG;
   }
   b->depth = nt == 1 ? 1 : hcnt->depth;
   b->amax = __uint_as_float_host(hcnt->amax);
+  b->ctx = ctx;
+  ctx->bvhs.push_back(b);
   *out = b;
   return VISACD_OK;
+}
+
+void bvh_detach(visacd_bvh* b) {
+  if (b->nodes) cudaFreeAsync(b->nodes, b->stream);
+  if (b->tris) cudaFreeAsync(b->tris, b->stream);
+  b->nodes = b->tris = nullptr;
+  b->ctx = nullptr;
+  b->stream = nullptr;
 }
 
 }  // namespace vgpu
@@ -388,8 +402,11 @@ extern "C" int visacd_bvh_build(visacd_ctx* ctx, const float* verts, int32_t nv,
 extern "C" int visacd_bvh_destroy(visacd_bvh* b) {
   if (!b) return VISACD_OK;
   cudaSetDevice(b->device);
-  if (b->nodes) cudaFree(b->nodes);
-  if (b->tris) cudaFree(b->tris);
+  if (b->ctx) {
+    auto& v = b->ctx->bvhs;
+    v.erase(std::remove(v.begin(), v.end(), b), v.end());
+    bvh_detach(b);
+  }
   delete b;
   return VISACD_OK;
 }

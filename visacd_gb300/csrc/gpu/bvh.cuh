@@ -19,6 +19,8 @@ struct visacd_bvh {
   float amax = 0.f;  // largest |vertex coordinate|
   float4* nodes = nullptr;
   float4* tris = nullptr;
+  visacd_ctx* ctx = nullptr;       // owning context (null once it is destroyed)
+  cudaStream_t stream = nullptr;   // the owner's stream (stream-ordered allocations)
 };
 
 namespace vgpu {
@@ -31,5 +33,8 @@ inline float __uint_as_float_host(unsigned u) {
 
 int bvh_build(visacd_ctx* ctx, const float* verts, int32_t nv, const uint32_t* tris, int32_t nt,
               int device_ptrs, visacd_bvh** out);
+// Frees a BVH's device memory when its context goes away (the handle itself
+// stays valid until visacd_bvh_destroy, and is rejected by queries).
+void bvh_detach(visacd_bvh* b);
 
 }  // namespace vgpu

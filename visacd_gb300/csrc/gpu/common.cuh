@@ -56,12 +56,19 @@ enum : uint32_t {
 struct DevBuf {
   void* p = nullptr;
   size_t cap = 0;
+  cudaStream_t stream = nullptr;  // owner's stream: allocations are stream-ordered on it
 };
 
 // Grow-only device buffer: reallocates (without preserving contents) only when
 // the request exceeds the current capacity; capacities round up to 1.25x.
+// Buffers with a stream use the stream-ordered allocator (cudaMallocAsync /
+// cudaFreeAsync from the device's default pool, which keeps freed memory
+// cached), so growing one context's buffer never waits for other streams.
 int ensure(DevBuf& b, size_t bytes);
 void release(DevBuf& b);
+// Keep memory freed to the device's default pool cached in the pool (release
+// threshold = unlimited) for the life of the process. Idempotent.
+int keep_pool_cached(int device);
 
 struct KernelTime {
   const char* name;
@@ -101,6 +108,9 @@ enum CtxSlot {
   kSlotVisRowTiles,
   kSlotClip,
   kSlotHausdorff,
+  kSlotSdf,
+  kSlotSdfOut,
+  kSlotSdfTris,
   kSlotCount
 };
 
@@ -119,7 +129,9 @@ struct visacd_ctx {
   int vis_variant_override = -1;                  // forced launch shape, -1 = tuned/default
   std::unordered_map<uint32_t, int> vis_tuned;    // shape class -> autotuned variant
   visacd_clip_result clip_out{};                  // last clip result (device-resident)
+  std::vector<visacd_bvh*> bvhs;                  // live BVHs built on this context
   int clip_nv = 0;
+  int32_t sdf_nv = 0, sdf_nt = 0;                 // last SDF remesh result (device-resident)
   void* clip_ptrs[7] = {nullptr};
   // Per-kernel timing: events recorded around each launch when timing is on.
   struct Pending {
@@ -164,6 +176,7 @@ enum KernelId {
   kKLpLoss,
   kKLpAdam,
   kKLpMisc,
+  kKSdf,
   kKMisc,
   kKCount
 };

@@ -5,7 +5,10 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <mutex>
+
 #include "common.cuh"
+#include "bvh.cuh"
 
 namespace vgpu {
 
@@ -21,14 +24,17 @@ void set_error(const char* fmt, ...) {
 int ensure(DevBuf& b, size_t bytes) {
   if (bytes <= b.cap && b.p) return VISACD_OK;
   if (b.p) {
-    cudaFree(b.p);
+    if (b.stream)
+      cudaFreeAsync(b.p, b.stream);
+    else
+      cudaFree(b.p);
     b.p = nullptr;
     b.cap = 0;
   }
   size_t want = bytes + bytes / 4;
   if (want < 256) want = 256;
   want = (want + 255) & ~size_t(255);
-  cudaError_t e = cudaMalloc(&b.p, want);
+  cudaError_t e = b.stream ? cudaMallocAsync(&b.p, want, b.stream) : cudaMalloc(&b.p, want);
   if (e != cudaSuccess) {
     cudaGetLastError();
     b.p = nullptr;
@@ -40,9 +46,33 @@ int ensure(DevBuf& b, size_t bytes) {
 }
 
 void release(DevBuf& b) {
-  if (b.p) cudaFree(b.p);
+  if (b.p) {
+    if (b.stream)
+      cudaFreeAsync(b.p, b.stream);
+    else
+      cudaFree(b.p);
+  }
   b.p = nullptr;
   b.cap = 0;
+}
+
+int keep_pool_cached(int device) {
+  static std::mutex mu;
+  static bool done[64] = {false};
+  std::lock_guard<std::mutex> lock(mu);
+  if (device < 0 || device >= 64 || done[device]) return VISACD_OK;
+  cudaMemPool_t pool;
+  cudaError_t e = cudaDeviceGetDefaultMemPool(&pool, device);
+  if (e == cudaSuccess) {
+    uint64_t threshold = UINT64_MAX;
+    e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold);
+  }
+  if (e != cudaSuccess) {
+    set_error("default memory pool setup: %s", cudaGetErrorString(e));
+    return VISACD_ERR_CUDA;
+  }
+  done[device] = true;
+  return VISACD_OK;
 }
 
 static const char* kNames[kKCount] = {
@@ -53,7 +83,7 @@ static const char* kNames[kKCount] = {
     "scan_blocks",   "scan_top",       "scan_add",     "bitset_emit",
     "clip",          "clip_resolve",   "face_hausdorff", "lp_features",
     "lp_gemm",       "lp_pool",        "lp_loss",      "lp_adam",
-    "lp_misc",       "misc"};
+    "lp_misc",       "sdf_remesh",     "misc"};
 
 const char* kernel_name(int id) { return (id >= 0 && id < kKCount) ? kNames[id] : "?"; }
 
@@ -354,14 +384,13 @@ extern "C" int visacd_ctx_create(int device, void* cuda_stream, visacd_ctx** out
   VCUDA(cudaSetDevice(device));
   visacd_ctx* ctx = new visacd_ctx();
   ctx->device = device;
-  cudaDeviceProp prop;
-  cudaError_t e = cudaGetDeviceProperties(&prop, device);
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
   if (e != cudaSuccess) {
     delete ctx;
-    set_error("cudaGetDeviceProperties: %s", cudaGetErrorString(e));
+    set_error("device %d: %s", device, cudaGetErrorString(e));
     return VISACD_ERR_CUDA;
   }
-  ctx->sm_count = prop.multiProcessorCount;
   if (cuda_stream) {
     ctx->stream = (cudaStream_t)cuda_stream;
   } else {
@@ -383,6 +412,11 @@ extern "C" int visacd_ctx_create(int device, void* cuda_stream, visacd_ctx** out
   }
   ctx->times.resize(kKCount);
   for (int i = 0; i < kKCount; ++i) ctx->times[i].name = kernel_name(i);
+  for (int i = 0; i < kSlotCount; ++i) ctx->buf[i].stream = ctx->stream;
+  if (keep_pool_cached(device) != VISACD_OK) {
+    visacd_ctx_destroy(ctx);
+    return VISACD_ERR_CUDA;
+  }
   *out = ctx;
   return VISACD_OK;
 }
@@ -391,7 +425,11 @@ extern "C" int visacd_ctx_destroy(visacd_ctx* ctx) {
   if (!ctx) return VISACD_OK;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
+  // BVHs still alive lose their device memory with their context.
+  for (visacd_bvh* b : ctx->bvhs) bvh_detach(b);
+  ctx->bvhs.clear();
   for (int i = 0; i < kSlotCount; ++i) release(ctx->buf[i]);
+  cudaStreamSynchronize(ctx->stream);
   if (ctx->d_status) cudaFree(ctx->d_status);
   if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
   for (auto& p : ctx->pending) {

@@ -698,6 +698,11 @@ extern "C" int visacd_lp_create(visacd_ctx* ctx, const float* params, uint32_t s
   VCUDA(cudaSetDevice(ctx->device));
   visacd_lp* lp = new visacd_lp();
   lp->ctx = ctx;
+  for (DevBuf* b : {&lp->params, &lp->params_bf16, &lp->grads, &lp->adam_m, &lp->adam_v, &lp->x0, &lp->a1,
+                    &lp->a2, &lp->a3, &lp->poolkey, &lp->g, &lp->gb, &lp->arg, &lp->a4, &lp->a5, &lp->z6,
+                    &lp->dz6, &lp->dz5, &lp->dz4, &lp->dg, &lp->dz3, &lp->dz2, &lp->dz1, &lp->parts,
+                    &lp->labels, &lp->lw, &lp->loss, &lp->feats, &lp->planes, &lp->pts, &lp->edges})
+    b->stream = ctx->stream;
   const size_t pb = (size_t)kOff.total * 4;
   int rc = VISACD_OK;
   auto fail = [&](int code) {
@@ -721,9 +726,9 @@ extern "C" int visacd_lp_create(visacd_ctx* ctx, const float* params, uint32_t s
     }
     params = init.data();
   }
-  cudaError_t e = cudaMemcpy(lp->params.p, params, pb, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemset(lp->adam_m.p, 0, pb);
-  if (e == cudaSuccess) e = cudaMemset(lp->adam_v.p, 0, pb);
+  cudaError_t e = cudaMemcpyAsync(lp->params.p, params, pb, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(lp->adam_m.p, 0, pb, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(lp->adam_v.p, 0, pb, ctx->stream);
   if (e != cudaSuccess) {
     vgpu::set_error("lp_create: %s", cudaGetErrorString(e));
     return fail(VISACD_ERR_CUDA);
@@ -746,14 +751,15 @@ extern "C" int visacd_lp_destroy(visacd_lp* lp) {
                     &lp->dz6, &lp->dz5, &lp->dz4, &lp->dg, &lp->dz3, &lp->dz2, &lp->dz1, &lp->parts,
                     &lp->labels, &lp->lw, &lp->loss, &lp->feats, &lp->planes, &lp->pts, &lp->edges})
     vgpu::release(*b);
+  cudaStreamSynchronize(lp->ctx->stream);
   delete lp;
   return VISACD_OK;
 }
 
 extern "C" int visacd_lp_get_params(visacd_lp* lp, float* out) {
   VCHECK(lp && out, VISACD_ERR_INVALID_ARG, "lp_get_params: null argument");
+  VCUDA(cudaMemcpyAsync(out, lp->params.p, (size_t)kOff.total * 4, cudaMemcpyDeviceToHost, lp->ctx->stream));
   VCUDA(cudaStreamSynchronize(lp->ctx->stream));
-  VCUDA(cudaMemcpy(out, lp->params.p, (size_t)kOff.total * 4, cudaMemcpyDeviceToHost));
   return VISACD_OK;
 }
 

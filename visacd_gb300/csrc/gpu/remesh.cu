@@ -1,0 +1,376 @@
+// SDF remeshing on the GPU: the iso-surface at distance `level` outside a
+// mesh, on a grid of voxel size 1/scale — the cage / manifold step that
+// replaces OpenVDB in lib/src/preprocess.cpp:18-67.
+//
+// Same algorithm and arithmetic as the host restatement (manifold_preprocess in
+// csrc/host/remesh.cpp), so the output mesh is identical bit for bit:
+//  1. sdf_dist_kernel: one block per triangle; every voxel centre in the
+//     triangle's box grown by the band gets the exact FP64 point-triangle
+//     distance (rounded to float), combined with atomicMin (non-negative floats
+//     order like their bit patterns).
+//  2. For each axis: sdf_cross_kernel marks, for every ray through voxel
+//     centres (offset by 1.2345679e-6 / 2.3456789e-6 voxels) that crosses a
+//     triangle at x, the first voxel whose centre lies beyond x (XOR toggle);
+//     sdf_parity_kernel runs the prefix parity along each ray and adds a vote
+//     where it is odd. Inside = at least two of the three votes.
+//  3. Surface nets: a vertex per sign-changing cell at the mean of its edge
+//     crossings (cells in linear order, exclusive scan), two triangles per
+//     sign-changing grid edge whose four cells all have vertices (voxels in
+//     linear order, x / y / z edges, exclusive scan).
+#include "common.cuh"
+#include "geom64.cuh"
+
+namespace vgpu {
+
+namespace {
+
+struct SdfGrid {
+  int org[3], dim[3];
+  double band;
+  float fiso;
+  double scale;
+};
+
+__device__ __forceinline__ size_t vid(const SdfGrid& g, int i, int j, int k) {
+  return ((size_t)k * g.dim[1] + j) * g.dim[0] + i;
+}
+
+__device__ __forceinline__ void load_tri(const double* __restrict__ P, const int32_t* __restrict__ T, int t,
+                                         double (&A)[3], double (&B)[3], double (&C)[3]) {
+  const int a = T[3 * (size_t)t], b = T[3 * (size_t)t + 1], c = T[3 * (size_t)t + 2];
+  for (int k = 0; k < 3; ++k) {
+    A[k] = P[3 * (size_t)a + k];
+    B[k] = P[3 * (size_t)b + k];
+    C[k] = P[3 * (size_t)c + k];
+  }
+}
+
+__device__ __forceinline__ double min3(double a, double b, double c) { return fmin(fmin(a, b), c); }
+__device__ __forceinline__ double max3(double a, double b, double c) { return fmax(fmax(a, b), c); }
+
+__global__ void __launch_bounds__(128) sdf_dist_kernel(const double* __restrict__ P, const int32_t* __restrict__ T,
+                                                       int nt, SdfGrid g, uint32_t* __restrict__ dist) {
+  for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+    double A[3], B[3], C[3];
+    load_tri(P, T, t, A, B, C);
+    int lo[3], ext[3];
+    for (int a = 0; a < 3; ++a) {
+      const double mn = min3(A[a], B[a], C[a]), mx = max3(A[a], B[a], C[a]);
+      lo[a] = max(0, (int)floor(mn - g.band) - g.org[a]);
+      const int hi = min(g.dim[a] - 1, (int)ceil(mx + g.band) - g.org[a]);
+      ext[a] = hi - lo[a] + 1;
+    }
+    if (ext[0] <= 0 || ext[1] <= 0 || ext[2] <= 0) continue;
+    const int n = ext[0] * ext[1] * ext[2];
+    for (int r = threadIdx.x; r < n; r += blockDim.x) {
+      const int i = lo[0] + r % ext[0], j = lo[1] + (r / ext[0]) % ext[1], k = lo[2] + r / (ext[0] * ext[1]);
+      const double q[3] = {(double)(g.org[0] + i), (double)(g.org[1] + j), (double)(g.org[2] + k)};
+      const float d = __double2float_rn(point_tri_dist(q, A, B, C));
+      atomicMin(&dist[vid(g, i, j, k)], __float_as_uint(d));
+    }
+  }
+}
+
+__global__ void __launch_bounds__(128) sdf_cross_kernel(const double* __restrict__ P, const int32_t* __restrict__ T,
+                                                        int nt, SdfGrid g, int ax, uint32_t* __restrict__ toggle) {
+  const int u = (ax + 1) % 3, w = (ax + 2) % 3;
+  const double ou = 1.2345679e-6, ow = 2.3456789e-6;
+  for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+    double A[3], B[3], C[3];
+    load_tri(P, T, t, A, B, C);
+    const int u0 = max(0, (int)floor(min3(A[u], B[u], C[u]) - g.org[u]));
+    const int u1 = min(g.dim[u] - 1, (int)ceil(max3(A[u], B[u], C[u]) - g.org[u]));
+    const int w0 = max(0, (int)floor(min3(A[w], B[w], C[w]) - g.org[w]));
+    const int w1 = min(g.dim[w] - 1, (int)ceil(max3(A[w], B[w], C[w]) - g.org[w]));
+    const int eu = u1 - u0 + 1, ew = w1 - w0 + 1;
+    if (eu <= 0 || ew <= 0) continue;
+    for (int r = threadIdx.x; r < eu * ew; r += blockDim.x) {
+      const int ku = u0 + r % eu, kw = w0 + r / eu;
+      const double y = da((double)(g.org[u] + ku), ou), z = da((double)(g.org[w] + kw), ow);
+      const double e0 = ds(dm(ds(B[u], A[u]), ds(z, A[w])), dm(ds(B[w], A[w]), ds(y, A[u])));
+      const double e1 = ds(dm(ds(C[u], B[u]), ds(z, B[w])), dm(ds(C[w], B[w]), ds(y, B[u])));
+      const double e2 = ds(dm(ds(A[u], C[u]), ds(z, C[w])), dm(ds(A[w], C[w]), ds(y, C[u])));
+      const bool in = (e0 > 0 && e1 > 0 && e2 > 0) || (e0 < 0 && e1 < 0 && e2 < 0);
+      if (!in) continue;
+      const double sw = da(da(e0, e1), e2);
+      const double x = __ddiv_rn(da(da(dm(e1, A[ax]), dm(e2, B[ax])), dm(e0, C[ax])), sw);
+      // first voxel s whose centre org + s lies beyond x (integers compare exactly)
+      int s = (int)floor(x - (double)g.org[ax]) + 1;
+      while (s > 0 && (double)(g.org[ax] + s - 1) > x) --s;
+      while (s < g.dim[ax] && !((double)(g.org[ax] + s) > x)) ++s;
+      if (s < 0) s = 0;
+      if (s >= g.dim[ax]) continue;
+      int gi[3];
+      gi[ax] = s;
+      gi[u] = ku;
+      gi[w] = kw;
+      atomicXor(&toggle[vid(g, gi[0], gi[1], gi[2])], 1u);
+    }
+  }
+}
+
+__global__ void sdf_parity_kernel(SdfGrid g, int ax, const uint32_t* __restrict__ toggle,
+                                  uint8_t* __restrict__ votes) {
+  const int u = (ax + 1) % 3, w = (ax + 2) % 3;
+  const int ncol = g.dim[u] * g.dim[w];
+  for (int col = blockIdx.x * blockDim.x + threadIdx.x; col < ncol; col += gridDim.x * blockDim.x) {
+    int gi[3];
+    gi[u] = col % g.dim[u];
+    gi[w] = col / g.dim[u];
+    uint32_t par = 0;
+    for (int i = 0; i < g.dim[ax]; ++i) {
+      gi[ax] = i;
+      const size_t v = vid(g, gi[0], gi[1], gi[2]);
+      par ^= toggle[v];
+      if (par & 1u) votes[v] += 1;
+    }
+  }
+}
+
+__global__ void sdf_field_kernel(const uint32_t* __restrict__ dist, const uint8_t* __restrict__ votes, size_t n,
+                                 float* __restrict__ f) {
+  for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (size_t)gridDim.x * blockDim.x) {
+    const float d = __uint_as_float(dist[v]);
+    f[v] = votes[v] >= 2 ? -d : d;
+  }
+}
+
+__constant__ int kCorner[8][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {1, 1, 0},
+                                  {0, 0, 1}, {1, 0, 1}, {0, 1, 1}, {1, 1, 1}};
+__constant__ int kCedge[12][2] = {{0, 1}, {2, 3}, {4, 5}, {6, 7}, {0, 2}, {1, 3},
+                                  {4, 6}, {5, 7}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
+
+__device__ __forceinline__ int corner_values(const SdfGrid& g, const float* __restrict__ f, int i, int j, int k,
+                                             float (&cv)[8]) {
+  int nin = 0;
+  for (int c = 0; c < 8; ++c) {
+    cv[c] = f[vid(g, i + kCorner[c][0], j + kCorner[c][1], k + kCorner[c][2])];
+    nin += cv[c] < g.fiso;
+  }
+  return nin;
+}
+
+__global__ void sdf_cell_flag_kernel(SdfGrid g, const float* __restrict__ f, uint32_t* __restrict__ flag) {
+  const int cx = g.dim[0] - 1, cy = g.dim[1] - 1, cz = g.dim[2] - 1;
+  const size_t n = (size_t)cx * cy * cz;
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(c % cx), j = (int)((c / cx) % cy), k = (int)(c / ((size_t)cx * cy));
+    float cv[8];
+    const int nin = corner_values(g, f, i, j, k, cv);
+    flag[c] = (nin != 0 && nin != 8) ? 1u : 0u;
+  }
+}
+
+__global__ void sdf_cell_vertex_kernel(SdfGrid g, const float* __restrict__ f, const uint32_t* __restrict__ flag,
+                                       const uint64_t* __restrict__ off, int32_t* __restrict__ cell_vertex,
+                                       double* __restrict__ out_v) {
+  const int cx = g.dim[0] - 1, cy = g.dim[1] - 1, cz = g.dim[2] - 1;
+  const size_t n = (size_t)cx * cy * cz;
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+    if (!flag[c]) {
+      cell_vertex[c] = -1;
+      continue;
+    }
+    const int i = (int)(c % cx), j = (int)((c / cx) % cy), k = (int)(c / ((size_t)cx * cy));
+    float cv[8];
+    corner_values(g, f, i, j, k, cv);
+    double acc[3] = {0, 0, 0};
+    int ncross = 0;
+    for (int e = 0; e < 12; ++e) {
+      const int c0 = kCedge[e][0], c1 = kCedge[e][1];
+      if ((cv[c0] < g.fiso) == (cv[c1] < g.fiso)) continue;
+      const double t = __ddiv_rn((double)__fsub_rn(g.fiso, cv[c0]), (double)__fsub_rn(cv[c1], cv[c0]));
+      for (int a = 0; a < 3; ++a)
+        acc[a] = da(acc[a], da((double)kCorner[c0][a], dm(t, (double)(kCorner[c1][a] - kCorner[c0][a]))));
+      ++ncross;
+    }
+    const int vtx = (int)off[c];
+    cell_vertex[c] = vtx;
+    const int ijk[3] = {i, j, k};
+    for (int a = 0; a < 3; ++a) {
+      const double m = __ddiv_rn(acc[a], (double)ncross);
+      out_v[3 * (size_t)vtx + a] = __ddiv_rn(da((double)(g.org[a] + ijk[a]), m), g.scale);
+    }
+  }
+}
+
+// Quads of interior voxel (i, j, k) in the host's order (+x, +y, +z edges),
+// each as two triangles; returns the triangle count, writes them when out.
+__device__ __forceinline__ int voxel_quads(const SdfGrid& g, const float* __restrict__ f,
+                                           const int32_t* __restrict__ cv, int i, int j, int k,
+                                           int32_t* __restrict__ out) {
+  const int cx = g.dim[0] - 1, cy = g.dim[1] - 1;
+  auto cid = [&](int a, int b, int c) { return ((size_t)c * cy + b) * cx + a; };
+  const bool in0 = f[vid(g, i, j, k)] < g.fiso;
+  int n = 0;
+  auto emit = [&](int q0, int q1, int q2, int q3, bool flip) {
+    if (q0 < 0 || q1 < 0 || q2 < 0 || q3 < 0) return;
+    if (flip) {
+      const int t = q1;
+      q1 = q3;
+      q3 = t;
+    }
+    if (out) {
+      out[3 * n] = q0;
+      out[3 * n + 1] = q1;
+      out[3 * n + 2] = q2;
+      out[3 * n + 3] = q0;
+      out[3 * n + 4] = q2;
+      out[3 * n + 5] = q3;
+    }
+    n += 2;
+  };
+  if (in0 != (f[vid(g, i + 1, j, k)] < g.fiso))
+    emit(cv[cid(i, j - 1, k - 1)], cv[cid(i, j, k - 1)], cv[cid(i, j, k)], cv[cid(i, j - 1, k)], !in0);
+  if (in0 != (f[vid(g, i, j + 1, k)] < g.fiso))
+    emit(cv[cid(i - 1, j, k - 1)], cv[cid(i - 1, j, k)], cv[cid(i, j, k)], cv[cid(i, j, k - 1)], !in0);
+  if (in0 != (f[vid(g, i, j, k + 1)] < g.fiso))
+    emit(cv[cid(i - 1, j - 1, k)], cv[cid(i, j - 1, k)], cv[cid(i, j, k)], cv[cid(i - 1, j, k)], !in0);
+  return n;
+}
+
+__global__ void sdf_quad_kernel(SdfGrid g, const float* __restrict__ f, const int32_t* __restrict__ cell_vertex,
+                                uint32_t* __restrict__ count, const uint64_t* __restrict__ off,
+                                int32_t* __restrict__ out_t) {
+  const int ix = g.dim[0] - 2, iy = g.dim[1] - 2, iz = g.dim[2] - 2;
+  const size_t n = (size_t)ix * iy * iz;
+  for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (size_t)gridDim.x * blockDim.x) {
+    const int i = 1 + (int)(r % ix), j = 1 + (int)((r / ix) % iy), k = 1 + (int)(r / ((size_t)ix * iy));
+    if (off)
+      voxel_quads(g, f, cell_vertex, i, j, k, out_t + 3 * (size_t)off[r]);
+    else
+      count[r] = (uint32_t)voxel_quads(g, f, cell_vertex, i, j, k, nullptr);
+  }
+}
+
+__global__ void sdf_fill_kernel(uint32_t* __restrict__ p, size_t n, uint32_t v) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) p[i] = v;
+}
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+}  // namespace
+}  // namespace vgpu
+
+using namespace vgpu;
+
+extern "C" int visacd_sdf_remesh(visacd_ctx* ctx, const double* verts, int32_t nv, const int32_t* tris, int32_t nt,
+                                 double scale, double level, int32_t* out_nv, int32_t* out_nt) {
+  VCHECK(ctx && out_nv && out_nt, VISACD_ERR_INVALID_ARG, "sdf_remesh: null argument");
+  VCHECK(nv >= 0 && nt >= 0 && (nt == 0 || (verts && tris)), VISACD_ERR_INVALID_ARG, "sdf_remesh: bad sizes");
+  VCHECK(scale > 0, VISACD_ERR_INVALID_ARG, "sdf_remesh: scale must be positive");
+  ctx->sdf_nv = ctx->sdf_nt = 0;
+  *out_nv = *out_nt = 0;
+  if (nt == 0 || nv == 0) return VISACD_OK;
+  for (int64_t i = 0; i < 3 * (int64_t)nt; ++i)
+    VCHECK(tris[i] >= 0 && tris[i] < nv, VISACD_ERR_INVALID_ARG, "sdf_remesh: triangle index out of range");
+  VCUDA(cudaSetDevice(ctx->device));
+  // Grid (host arithmetic of manifold_preprocess).
+  std::vector<double> P(3 * (size_t)nv);
+  double lo[3] = {1e308, 1e308, 1e308}, hi[3] = {-1e308, -1e308, -1e308};
+  for (int32_t i = 0; i < nv; ++i)
+    for (int a = 0; a < 3; ++a) {
+      const double x = verts[3 * (size_t)i + a] * scale;
+      P[3 * (size_t)i + a] = x;
+      lo[a] = std::min(lo[a], x);
+      hi[a] = std::max(hi[a], x);
+    }
+  const double iso = level * scale;
+  SdfGrid g;
+  g.band = std::max(iso, 0.0) + 2.0;
+  g.fiso = (float)iso;
+  g.scale = scale;
+  for (int a = 0; a < 3; ++a) {
+    g.org[a] = (int)std::floor(lo[a] - g.band - 2.0);
+    g.dim[a] = (int)std::ceil(hi[a] + g.band + 2.0) - g.org[a] + 1;
+  }
+  VCHECK(g.dim[0] >= 3 && g.dim[1] >= 3 && g.dim[2] >= 3, VISACD_ERR_INVALID_ARG, "sdf_remesh: degenerate grid");
+  const size_t nvox = (size_t)g.dim[0] * g.dim[1] * g.dim[2];
+  VCHECK(nvox <= ((size_t)1 << 30), VISACD_ERR_CAPACITY, "sdf_remesh: grid of %zu voxels is too large", nvox);
+  const size_t ncell = (size_t)(g.dim[0] - 1) * (g.dim[1] - 1) * (g.dim[2] - 1);
+  const size_t nint = (size_t)(g.dim[0] - 2) * (g.dim[1] - 2) * (g.dim[2] - 2);
+  // Scratch layout in one buffer.
+  size_t at = 0;
+  auto take = [&](size_t bytes) {
+    const size_t o = at;
+    at += align256(bytes);
+    return o;
+  };
+  const size_t oP = take(P.size() * 8), oT = take(3 * (size_t)nt * 4), oDist = take(nvox * 4),
+               oTog = take(nvox * 4), oVotes = take(nvox), oF = take(nvox * 4), oFlag = take(ncell * 4),
+               oCoff = take((ncell + 1) * 8), oCv = take(ncell * 4), oQcnt = take(nint * 4),
+               oQoff = take((nint + 1) * 8);
+  VTRY(ensure_slot(ctx, kSlotSdf, at));
+  char* base = slot<char>(ctx, kSlotSdf);
+  double* dP = (double*)(base + oP);
+  int32_t* dT = (int32_t*)(base + oT);
+  uint32_t* dist = (uint32_t*)(base + oDist);
+  uint32_t* tog = (uint32_t*)(base + oTog);
+  uint8_t* votes = (uint8_t*)(base + oVotes);
+  float* f = (float*)(base + oF);
+  uint32_t* flag = (uint32_t*)(base + oFlag);
+  uint64_t* coff = (uint64_t*)(base + oCoff);
+  int32_t* cv = (int32_t*)(base + oCv);
+  uint32_t* qcnt = (uint32_t*)(base + oQcnt);
+  uint64_t* qoff = (uint64_t*)(base + oQoff);
+  cudaStream_t st = ctx->stream;
+  VCUDA(cudaMemcpyAsync(dP, P.data(), P.size() * 8, cudaMemcpyHostToDevice, st));
+  VCUDA(cudaMemcpyAsync(dT, tris, 3 * (size_t)nt * 4, cudaMemcpyHostToDevice, st));
+  const unsigned gv = grid_for((int64_t)nvox, 256, 16 * (int64_t)ctx->sm_count);
+  const float band_f = (float)g.band;
+  uint32_t band_bits;
+  std::memcpy(&band_bits, &band_f, 4);
+  VLAUNCH(ctx, kKSdf, gv, 256, 0, sdf_fill_kernel, dist, nvox, band_bits);
+  VCUDA(cudaMemsetAsync(votes, 0, nvox, st));
+  const unsigned gt = (unsigned)std::min<int64_t>(nt, 64 * (int64_t)ctx->sm_count);
+  VLAUNCH(ctx, kKSdf, gt, 128, 0, sdf_dist_kernel, dP, dT, nt, g, dist);
+  for (int ax = 0; ax < 3; ++ax) {
+    VCUDA(cudaMemsetAsync(tog, 0, nvox * 4, st));
+    VLAUNCH(ctx, kKSdf, gt, 128, 0, sdf_cross_kernel, dP, dT, nt, g, ax, tog);
+    const int u = (ax + 1) % 3, w = (ax + 2) % 3;
+    VLAUNCH(ctx, kKSdf, grid_for((int64_t)g.dim[u] * g.dim[w], 128, 1 << 20), 128, 0, sdf_parity_kernel, g, ax,
+            tog, votes);
+  }
+  VLAUNCH(ctx, kKSdf, gv, 256, 0, sdf_field_kernel, dist, votes, nvox, f);
+  const unsigned gc = grid_for((int64_t)ncell, 256, 16 * (int64_t)ctx->sm_count);
+  VLAUNCH(ctx, kKSdf, gc, 256, 0, sdf_cell_flag_kernel, g, f, flag);
+  VTRY(exclusive_scan_u32_to_u64(ctx, flag, coff, (int64_t)ncell));
+  const unsigned gq = grid_for((int64_t)nint, 256, 16 * (int64_t)ctx->sm_count);
+  uint64_t totals[2];
+  VCUDA(cudaMemcpyAsync(&totals[0], coff + ncell, 8, cudaMemcpyDeviceToHost, st));
+  VCUDA(cudaStreamSynchronize(st));
+  VCHECK(totals[0] < (1ull << 31), VISACD_ERR_CAPACITY, "sdf_remesh: too many vertices");
+  VTRY(ensure_slot(ctx, kSlotSdfOut, align256(totals[0] * 24) + 256));
+  double* out_v = slot<double>(ctx, kSlotSdfOut);
+  VLAUNCH(ctx, kKSdf, gc, 256, 0, sdf_cell_vertex_kernel, g, f, flag, coff, cv, out_v);
+  VLAUNCH(ctx, kKSdf, gq, 256, 0, sdf_quad_kernel, g, f, cv, qcnt, (const uint64_t*)nullptr,
+          (int32_t*)nullptr);
+  VTRY(exclusive_scan_u32_to_u64(ctx, qcnt, qoff, (int64_t)nint));
+  VCUDA(cudaMemcpyAsync(&totals[1], qoff + nint, 8, cudaMemcpyDeviceToHost, st));
+  VCUDA(cudaStreamSynchronize(st));
+  VCHECK(totals[1] < (1ull << 31), VISACD_ERR_CAPACITY, "sdf_remesh: too many triangles");
+  VTRY(ensure_slot(ctx, kSlotSdfTris, align256(totals[1] * 12) + 256));
+  VLAUNCH(ctx, kKSdf, gq, 256, 0, sdf_quad_kernel, g, f, cv, qcnt, qoff, slot<int32_t>(ctx, kSlotSdfTris));
+  ctx->sdf_nv = (int32_t)totals[0];
+  ctx->sdf_nt = (int32_t)totals[1];
+  *out_nv = ctx->sdf_nv;
+  *out_nt = ctx->sdf_nt;
+  return VISACD_OK;
+}
+
+extern "C" int visacd_sdf_fetch(visacd_ctx* ctx, double* verts, int32_t* tris) {
+  VCHECK(ctx, VISACD_ERR_INVALID_ARG, "sdf_fetch: null context");
+  VCUDA(cudaSetDevice(ctx->device));
+  if (ctx->sdf_nv > 0) {
+    VCHECK(verts, VISACD_ERR_INVALID_ARG, "sdf_fetch: null vertex buffer");
+    VCUDA(cudaMemcpyAsync(verts, slot<double>(ctx, kSlotSdfOut), (size_t)ctx->sdf_nv * 24, cudaMemcpyDeviceToHost,
+                          ctx->stream));
+  }
+  if (ctx->sdf_nt > 0) {
+    VCHECK(tris, VISACD_ERR_INVALID_ARG, "sdf_fetch: null triangle buffer");
+    VCUDA(cudaMemcpyAsync(tris, slot<int32_t>(ctx, kSlotSdfTris), (size_t)ctx->sdf_nt * 12, cudaMemcpyDeviceToHost,
+                          ctx->stream));
+  }
+  VCUDA(cudaStreamSynchronize(ctx->stream));
+  return VISACD_OK;
+}

@@ -497,6 +497,8 @@ int visibility_impl(visacd_ctx* ctx, const float* pts, int32_t n, const uint8_t*
                     int device_ptrs, const visacd_bvh* self_bvh, const visacd_bvh* cage_bvh,
                     int64_t* n_edges, visacd_vis_stats* stats) {
   VCHECK(ctx && self_bvh && cage_bvh, VISACD_ERR_INVALID_ARG, "visibility: null argument");
+  VCHECK(self_bvh->ctx && cage_bvh->ctx, VISACD_ERR_INVALID_ARG,
+         "visibility: a BVH outlived the context it was built on");
   VCHECK(n >= 0 && (n == 0 || pts), VISACD_ERR_INVALID_ARG, "visibility: bad points");
   VCHECK(n <= (1 << 24), VISACD_ERR_INVALID_ARG, "visibility: n = %d above the 2^24 limit", n);
   VCHECK(self_bvh->device == ctx->device && cage_bvh->device == ctx->device,
@@ -603,6 +605,8 @@ extern "C" int visacd_autotune_visibility(visacd_ctx* ctx, const float* pts, int
                                           const visacd_bvh* self_bvh, const visacd_bvh* cage_bvh,
                                           int* best_variant, double* ms_per_variant) {
   VCHECK(ctx && self_bvh && cage_bvh, VISACD_ERR_INVALID_ARG, "autotune: null argument");
+  VCHECK(self_bvh->ctx && cage_bvh->ctx, VISACD_ERR_INVALID_ARG,
+         "autotune: a BVH outlived the context it was built on");
   const int saved_override = ctx->vis_variant_override;
   const bool saved_timing = ctx->timing;
   int best = 0;

@@ -88,7 +88,12 @@ PYBIND11_MODULE(visacd, m) {
       .def_readwrite("use_merging", &Config::use_merging)
       .def_readwrite("verbose", &Config::verbose)
       .def_readwrite("gpu_clip", &Config::gpu_clip)
-      .def_readwrite("gpu_concavity", &Config::gpu_concavity);
+      .def_readwrite("gpu_concavity", &Config::gpu_concavity)
+      .def_readwrite("gpu_remesh", &Config::gpu_remesh)
+      .def_readwrite("plane_proposer", &Config::plane_proposer)
+      .def_readwrite("proposer_weights", &Config::proposer_weights)
+      .def_readwrite("proposer_probe_planes", &Config::proposer_probe_planes)
+      .def_readwrite("proposer_tolerance", &Config::proposer_tolerance);
 
   m.def("make_vecarray3i", [](py::array_t<int, py::array::c_style | py::array::forcecast> a) {
     auto buf = a.request();
@@ -102,6 +107,15 @@ PYBIND11_MODULE(visacd, m) {
 
   m.def("set_seed", &set_seed, py::arg("seed"));
   m.attr("config") = py::cast(&config(), py::return_value_policy::reference);
+  // The trained proposer ships next to this module (proposer_weights.bin).
+  if (config().proposer_weights.empty()) {
+    try {
+      auto os_path = py::module_::import("os.path");
+      py::object here = os_path.attr("dirname")(py::module_::import("visacd_gb300").attr("__file__"));
+      config().proposer_weights = py::cast<std::string>(os_path.attr("join")(here, "proposer_weights.bin"));
+    } catch (const py::error_already_set&) {
+    }
+  }
 
   py::class_<ProcessResult>(m, "ProcessResult")
       .def_readwrite("parts", &ProcessResult::parts)
@@ -110,6 +124,9 @@ PYBIND11_MODULE(visacd, m) {
 
   m.def("process", &process, py::arg("mesh"), py::arg("concavity"), py::arg("num_parts"),
         py::call_guard<py::gil_scoped_release>());
+  // Addition: many meshes at once (see process.hpp).
+  m.def("process_batch", &process_batch, py::arg("meshes"), py::arg("concavity"), py::arg("num_parts"),
+        py::arg("seeds"), py::arg("threads") = 0, py::call_guard<py::gil_scoped_release>());
 
   // ---- helpers for tests and benchmarks (not part of the reference surface) --
   m.def("_stage_times", []() {
@@ -130,11 +147,20 @@ PYBIND11_MODULE(visacd, m) {
     d["vis_edges"] = c.vis_edges;
     d["score_calls"] = c.score_calls;
     d["plane_edge_pairs"] = c.plane_edge_pairs;
+    d["lp_calls"] = c.lp_calls;
+    d["lp_fallbacks"] = c.lp_fallbacks;
+    d["lp_ms"] = c.lp_ms;
     return d;
   });
+  m.def("_reset_counters", []() { gpu::counters() = gpu::Counters(); });
   m.def("_manifold_preprocess", [](py::array_t<double> v, py::array_t<int> t, double scale, double level) {
     Mesh mm = np_to_mesh(v, t);
-    manifold_preprocess(mm, scale, level);
+    manifold_preprocess_host(mm, scale, level);
+    return mesh_dict(mm);
+  });
+  m.def("_manifold_preprocess_gpu", [](py::array_t<double> v, py::array_t<int> t, double scale, double level) {
+    Mesh mm = np_to_mesh(v, t);
+    gpu::sdf_remesh(mm, scale, level);
     return mesh_dict(mm);
   });
   m.def("_convex_hull", [](py::array_t<double> v) {

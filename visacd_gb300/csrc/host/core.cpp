@@ -27,10 +27,17 @@ Config& config() {
   return c;
 }
 
+namespace {
+thread_local std::mt19937* tl_engine = nullptr;  // per-thread engine of process_batch workers
+}
+
 std::mt19937& random_engine() {
+  if (tl_engine) return *tl_engine;
   static std::mt19937 eng(std::random_device{}());
   return eng;
 }
+
+void set_thread_engine(std::mt19937* eng) { tl_engine = eng; }
 
 void set_seed(unsigned int seed) { random_engine().seed(seed); }
 

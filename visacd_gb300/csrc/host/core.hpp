@@ -93,10 +93,23 @@ struct Config {
   bool verbose = true;   // the "[visacd] ..." progress lines
   bool gpu_clip = true;        // split parts with the GPU clip kernels (else the host clip)
   bool gpu_concavity = true;   // Hausdorff term of the concavity metric on the GPU
+  bool gpu_remesh = true;      // SDF remesh (manifold and cages) on the GPU
+  // Split-plane search: "exhaustive" (the reference's random candidate draw)
+  // or "learned" (16 planes from the learned proposer plus a probe of
+  // `proposer_probe_planes` random candidates; when the best proposal scores
+  // more than `proposer_tolerance` below the probe's best, the split falls back
+  // to the full candidate draw).
+  std::string plane_proposer = "exhaustive";
+  std::string proposer_weights;  // float32 parameter file of the proposer
+  int proposer_probe_planes = 64;
+  double proposer_tolerance = 0.01;
 };
 
 Config& config();
+// The process-wide engine, or the calling thread's own one while a
+// process_batch worker has installed it (set_thread_engine(nullptr) clears).
 std::mt19937& random_engine();
+void set_thread_engine(std::mt19937* eng);
 void set_seed(unsigned int seed);
 
 // Bounding box (xmin, xmax, ymin, ymax, zmin, zmax).

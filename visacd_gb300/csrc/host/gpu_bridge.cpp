@@ -31,18 +31,45 @@ double now_ms() {
 }  // namespace
 
 Counters& counters() {
-  static Counters c;
+  static thread_local Counters c;
   return c;
 }
 
+namespace {
+thread_local visacd_ctx* tl_ctx = nullptr;   // a process_batch worker's own context
+thread_local visacd_lp* tl_lp = nullptr;     // the proposer on this thread's context
+thread_local visacd_ctx* tl_lp_ctx = nullptr;
+}  // namespace
+
+ThreadContext::ThreadContext(int device) {
+  if (visacd_ctx_create(device, nullptr, &ctx_) != VISACD_OK)
+    throw std::runtime_error(std::string("cannot create a worker GPU context: ") + visacd_last_error());
+  prev_ = tl_ctx;
+  tl_ctx = ctx_;
+}
+
+ThreadContext::~ThreadContext() {
+  if (tl_lp && tl_lp_ctx == ctx_) {
+    visacd_lp_destroy(tl_lp);
+    tl_lp = nullptr;
+    tl_lp_ctx = nullptr;
+  }
+  tl_ctx = prev_;
+  visacd_ctx_destroy(ctx_);
+}
+
+int default_device() {
+  const char* dev = std::getenv("VISACD_DEVICE");
+  return dev ? std::atoi(dev) : 0;
+}
+
 visacd_ctx* context() {
+  if (tl_ctx) return tl_ctx;
   static std::once_flag once;
   static visacd_ctx* ctx = nullptr;
   static std::string err;
   std::call_once(once, [] {
-    const char* dev = std::getenv("VISACD_DEVICE");
-    int d = dev ? std::atoi(dev) : 0;
-    if (visacd_ctx_create(d, nullptr, &ctx) != VISACD_OK) {
+    if (visacd_ctx_create(default_device(), nullptr, &ctx) != VISACD_OK) {
       err = visacd_last_error();
       ctx = nullptr;
     }
@@ -63,7 +90,7 @@ std::vector<Edge> visibility_edges(const Mesh& mesh, const Mesh& cage) {
   std::vector<float> v, cv;
   to_f32(mesh.vertices, v);
   to_f32(cage.vertices, cv);
-  static_assert(sizeof(Tri) == 12, "triangles must be 3 packed ints");
+  static_assert(sizeof(Tri) == 12 && sizeof(Vec3) == 24, "packed vertex and triangle arrays");
   BvhHandle sb, cb;
   check(visacd_bvh_build(ctx, v.data(), (int32_t)mesh.vertices.size(),
                          reinterpret_cast<const uint32_t*>(mesh.triangles.data()),
@@ -160,5 +187,102 @@ MeshList clip(const Mesh& mesh, const Plane& plane, std::vector<int>& pos_map,
   return assemble_clip(mesh, plane, pt, ng, pos_map, neg_map, border, bedges);
 }
 
+void sdf_remesh(Mesh& m, double scale, double level) {
+  visacd_ctx* ctx = context();
+  std::vector<double> v(3 * m.vertices.size());
+  for (size_t i = 0; i < m.vertices.size(); ++i)
+    for (int k = 0; k < 3; ++k) v[3 * i + k] = m.vertices[i][k];
+  int32_t nv = 0, nt = 0;
+  check(visacd_sdf_remesh(ctx, v.data(), (int32_t)m.vertices.size(),
+                          reinterpret_cast<const int32_t*>(m.triangles.data()), (int32_t)m.triangles.size(),
+                          scale, level, &nv, &nt),
+        "visacd_sdf_remesh");
+  std::vector<Vec3> ov(nv);
+  std::vector<Tri> ot(nt);
+  check(visacd_sdf_fetch(ctx, reinterpret_cast<double*>(ov.data()), reinterpret_cast<int32_t*>(ot.data())),
+        "visacd_sdf_fetch");
+  m.clear();
+  m.is_new.clear();
+  m.intersecting_edges.clear();
+  m.vertices = std::move(ov);
+  m.triangles = std::move(ot);
+}
+
+namespace {
+// Proposer parameters by file path, read once per path.
+const std::vector<float>& proposer_params(const std::string& path) {
+  static std::mutex mu;
+  static std::string loaded_path;
+  static std::vector<float> params;
+  std::lock_guard<std::mutex> lock(mu);
+  if (path.empty())
+    throw std::runtime_error("plane_proposer is 'learned' but config.proposer_weights is empty");
+  if (path != loaded_path) {
+    std::FILE* f = std::fopen(path.c_str(), "rb");
+    if (!f) throw std::runtime_error("cannot open proposer weights " + path);
+    const int n = visacd_lp_param_count();
+    std::vector<float> p(n);
+    const size_t got = std::fread(p.data(), sizeof(float), n, f);
+    const bool extra = std::fgetc(f) != EOF;
+    std::fclose(f);
+    if (got != (size_t)n || extra)
+      throw std::runtime_error("proposer weights " + path + " must hold exactly " + std::to_string(n) +
+                               " float32 values");
+    params.swap(p);
+    loaded_path = path;
+  }
+  return params;
+}
+}  // namespace
+
+std::vector<Plane> propose_planes(const Mesh& mesh) {
+  double t0 = now_ms();
+  visacd_ctx* ctx = context();
+  if (!tl_lp || tl_lp_ctx != ctx) {
+    if (tl_lp) visacd_lp_destroy(tl_lp);
+    tl_lp = nullptr;
+    const auto& p = proposer_params(config().proposer_weights);
+    check(visacd_lp_create(ctx, p.data(), 0, &tl_lp), "visacd_lp_create");
+    tl_lp_ctx = ctx;
+  }
+  // The part's frame: bounding-box centre and half of the longest extent.
+  auto b = bbox(mesh);
+  const float center[3] = {(float)(0.5 * (b[0] + b[1])), (float)(0.5 * (b[2] + b[3])),
+                           (float)(0.5 * (b[4] + b[5]))};
+  double half = 0.5 * std::max(b[1] - b[0], std::max(b[3] - b[2], b[5] - b[4]));
+  if (!(half > 0)) half = 1.0;
+  std::vector<float> v;
+  to_f32(mesh.vertices, v);
+  std::vector<uint32_t> e(2 * mesh.intersecting_edges.size());
+  for (size_t k = 0; k < mesh.intersecting_edges.size(); ++k) {
+    e[2 * k] = mesh.intersecting_edges[k].first;
+    e[2 * k + 1] = mesh.intersecting_edges[k].second;
+  }
+  double out[VISACD_LP_PLANES * 4];
+  check(visacd_lp_propose(tl_lp, v.data(), (int32_t)mesh.vertices.size(), e.data(),
+                          (int64_t)mesh.intersecting_edges.size(), center, (float)half, out),
+        "visacd_lp_propose");
+  std::vector<Plane> planes;
+  for (int q = 0; q < VISACD_LP_PLANES; ++q)
+    planes.emplace_back(out[4 * q], out[4 * q + 1], out[4 * q + 2], out[4 * q + 3]);
+  auto& c = counters();
+  c.lp_calls++;
+  c.lp_ms += now_ms() - t0;
+  return planes;
+}
+
 }  // namespace gpu
+}  // namespace visacd
+
+namespace visacd {
+
+// SDF remesh dispatch (lib/src/preprocess.cpp:18-67): the GPU kernels, or the
+// host restatement they equal when config().gpu_remesh is off.
+void manifold_preprocess(Mesh& m, double scale, double level) {
+  if (config().gpu_remesh)
+    gpu::sdf_remesh(m, scale, level);
+  else
+    manifold_preprocess_host(m, scale, level);
+}
+
 }  // namespace visacd

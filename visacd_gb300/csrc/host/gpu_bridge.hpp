@@ -11,8 +11,30 @@ struct visacd_ctx;
 namespace visacd {
 namespace gpu {
 
-// Process-wide context on device VISACD_DEVICE (default 0), created on first use.
+// The calling thread's context: a ThreadContext installed on this thread, else
+// the process-wide context on device VISACD_DEVICE (default 0), created on
+// first use.
 visacd_ctx* context();
+int default_device();
+
+// A context (own stream and buffers) for the lifetime of the object, used by
+// context() on the creating thread; process_batch workers hold one each.
+class ThreadContext {
+ public:
+  explicit ThreadContext(int device);
+  ~ThreadContext();
+  ThreadContext(const ThreadContext&) = delete;
+  ThreadContext& operator=(const ThreadContext&) = delete;
+
+ private:
+  visacd_ctx* ctx_ = nullptr;
+  visacd_ctx* prev_ = nullptr;
+};
+
+// The learned proposer's 16 planes for a part with visibility edges, in the
+// part's own coordinates (network inputs are taken in the part's bounding-box
+// frame; parameters from config().proposer_weights).
+std::vector<Plane> propose_planes(const Mesh& mesh);
 
 // compute_intersection_matrix(mesh, cage) of lib/src/intersections.cpp:327-385:
 // pairs with a new endpoint when mesh.is_new is non-empty, else all pairs.
@@ -27,13 +49,20 @@ std::vector<double> score_planes(const std::vector<Plane>& planes, const std::ve
 MeshList clip(const Mesh& mesh, const Plane& plane, std::vector<int>& pos_map,
               std::vector<int>& neg_map);
 
+// SDF remesh on the GPU (visacd_sdf_remesh): replaces m by the iso-surface at
+// `level` outside it, on voxels of size 1/scale; same mesh as the host's
+// manifold_preprocess_host.
+void sdf_remesh(Mesh& m, double scale, double level);
+
 // Sampled face Hausdorff distance on the GPU (visacd_face_hausdorff).
 double face_hausdorff(const Mesh& A, const std::vector<Vec3>& XA, const std::vector<int>& idA,
                       const Mesh& B, const std::vector<Vec3>& XB, const std::vector<int>& idB);
 
+// Per-thread call counters.
 struct Counters {
   long long vis_calls = 0, vis_pairs = 0, vis_edges = 0, score_calls = 0, plane_edge_pairs = 0;
-  double vis_ms = 0, score_ms = 0;
+  long long lp_calls = 0, lp_fallbacks = 0;
+  double vis_ms = 0, score_ms = 0, lp_ms = 0;
 };
 Counters& counters();
 

@@ -6,26 +6,33 @@
 #include "process.hpp"
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <iostream>
 #include <sstream>
 #include <string>
+#include <thread>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 #include "gpu_bridge.hpp"
 
 namespace visacd {
 
 namespace {
-StageTimes g_times;
+thread_local StageTimes g_times;
+thread_local bool tl_quiet = false;  // process_batch workers do not log
 double now_ms() {
   return std::chrono::duration<double, std::milli>(
              std::chrono::steady_clock::now().time_since_epoch())
       .count();
 }
 void log(const std::string& msg) {
-  if (!config().verbose) return;
+  if (!config().verbose || tl_quiet) return;
   std::cout << "[visacd] " << msg << "\n";
   std::cout.flush();
 }
@@ -63,20 +70,105 @@ std::vector<Plane> get_candidate_planes(const std::vector<Vec3>& vertices,
   return planes;
 }
 
-bool decompose_iteration(Mesh& mesh, MeshList& parts, Mesh& cage,
-                         const std::vector<Plane>& flat_planes) {
-  double t0 = now_ms();
+namespace {
+
+// The reference's split-plane search (lib/src/process.cpp:96-134): 2500 random
+// candidates plus the flat-surface planes (scores x flat_surface_k), first
+// maximum. Returns false when there is nothing to score.
+bool exhaustive_plane(const Mesh& mesh, const std::vector<Plane>& flat_planes, Plane& out) {
   std::vector<Plane> planes = get_candidate_planes(mesh.vertices, mesh.intersecting_edges, 2500);
   const size_t flat_offset = planes.size();
   planes.insert(planes.end(), flat_planes.begin(), flat_planes.end());
-  if (planes.empty() || mesh.intersecting_edges.empty()) {
+  if (planes.empty() || mesh.intersecting_edges.empty()) return false;
+  std::vector<double> scores = gpu::score_planes(planes, mesh.vertices, mesh.intersecting_edges);
+  for (size_t i = flat_offset; i < planes.size(); ++i) scores[i] *= config().flat_surface_k;
+  out = planes[std::max_element(scores.begin(), scores.end()) - scores.begin()];
+  return true;
+}
+
+// Refinement of the proposals: for each proposal, the perpendicular-bisector
+// planes (the reference's candidate form, lib/src/process.cpp:45-53) of the
+// `per` visibility edges whose bisectors are nearest to it, under the distance
+// the proposer is trained with: 2 - 2|n_q . n_e| + ((s d_q - d_e) / half)^2,
+// s = sign(n_q . n_e). Returned in edge order, each edge once.
+std::vector<Plane> refine_proposals(const Mesh& mesh, const std::vector<Plane>& prop, int per) {
+  const auto& V = mesh.vertices;
+  const auto& E = mesh.intersecting_edges;
+  auto b = bbox(mesh);
+  double half = 0.5 * std::max(b[1] - b[0], std::max(b[3] - b[2], b[5] - b[4]));
+  if (!(half > 0)) half = 1.0;
+  std::vector<Plane> bis;
+  bis.reserve(E.size());
+  for (const auto& e : E) {
+    Vec3 n = V[e.second] - V[e.first];
+    const double ln = norm(n);
+    if (ln < 1e-6) continue;
+    n = n / ln;
+    const Vec3 m = (V[e.first] + V[e.second]) * 0.5;
+    bis.emplace_back(n[0], n[1], n[2], -dot(n, m));
+  }
+  std::vector<char> keep(bis.size(), 0);
+  std::vector<std::pair<double, int>> d(bis.size());
+  const int k = std::min<int>(per, (int)bis.size());
+  for (const auto& q : prop) {
+    for (size_t i = 0; i < bis.size(); ++i) {
+      const double c = q.a * bis[i].a + q.b * bis[i].b + q.c * bis[i].c;
+      const double s = c >= 0 ? 1.0 : -1.0;
+      const double dd = (s * q.d - bis[i].d) / half;
+      d[i] = {2.0 - 2.0 * std::fabs(c) + dd * dd, (int)i};
+    }
+    if (k <= 0) break;
+    std::nth_element(d.begin(), d.begin() + (k - 1), d.end());
+    for (int j = 0; j < k; ++j) keep[d[j].second] = 1;
+  }
+  std::vector<Plane> out;
+  for (size_t i = 0; i < bis.size(); ++i)
+    if (keep[i]) out.push_back(bis[i]);
+  return out;
+}
+
+// Learned search: the proposer's 16 planes refined by nearby bisector planes,
+// a probe of proposer_probe_planes random candidates (the reference's draw,
+// smaller) and the flat planes, scored together by the exact kernel. If the
+// best learned plane scores more than proposer_tolerance below the probe's
+// best, the proposals are not trusted for this split and the exhaustive search
+// runs instead.
+bool learned_plane(const Mesh& mesh, const std::vector<Plane>& flat_planes, Plane& out) {
+  if (mesh.intersecting_edges.empty()) return false;
+  std::vector<Plane> planes = gpu::propose_planes(mesh);
+  std::vector<Plane> refined = refine_proposals(mesh, planes, 8);
+  planes.insert(planes.end(), refined.begin(), refined.end());
+  const size_t n_prop = planes.size();
+  std::vector<Plane> probe =
+      get_candidate_planes(mesh.vertices, mesh.intersecting_edges, config().proposer_probe_planes);
+  planes.insert(planes.end(), probe.begin(), probe.end());
+  const size_t flat_offset = planes.size();
+  planes.insert(planes.end(), flat_planes.begin(), flat_planes.end());
+  std::vector<double> scores = gpu::score_planes(planes, mesh.vertices, mesh.intersecting_edges);
+  for (size_t i = flat_offset; i < planes.size(); ++i) scores[i] *= config().flat_surface_k;
+  const double best_prop = *std::max_element(scores.begin(), scores.begin() + n_prop);
+  double best_probe = 0;
+  for (size_t i = n_prop; i < flat_offset; ++i) best_probe = std::max(best_probe, scores[i]);
+  if (best_prop < (1.0 - config().proposer_tolerance) * best_probe) {
+    gpu::counters().lp_fallbacks++;
+    return exhaustive_plane(mesh, flat_planes, out);
+  }
+  out = planes[std::max_element(scores.begin(), scores.end()) - scores.begin()];
+  return true;
+}
+
+}  // namespace
+
+bool decompose_iteration(Mesh& mesh, MeshList& parts, Mesh& cage,
+                         const std::vector<Plane>& flat_planes) {
+  double t0 = now_ms();
+  Plane plane;
+  const bool ok = config().plane_proposer == "learned" ? learned_plane(mesh, flat_planes, plane)
+                                                       : exhaustive_plane(mesh, flat_planes, plane);
+  if (!ok) {
     parts.push_back(mesh);
     return true;
   }
-  std::vector<double> scores = gpu::score_planes(planes, mesh.vertices, mesh.intersecting_edges);
-  for (size_t i = flat_offset; i < planes.size(); ++i) scores[i] *= config().flat_surface_k;
-  const size_t best = std::max_element(scores.begin(), scores.end()) - scores.begin();
-  const Plane plane = planes[best];
   double t1 = now_ms();
   g_times.scoring += t1 - t0;
 
@@ -154,6 +246,8 @@ double compute_final_concavity(const MeshList& parts, const MeshList& hulls) {
 }
 
 ProcessResult process(Mesh mesh, double concavity, int num_parts) {
+  if (config().plane_proposer != "exhaustive" && config().plane_proposer != "learned")
+    throw std::runtime_error("config.plane_proposer must be 'exhaustive' or 'learned'");
   g_times = StageTimes();
   const double t_start = now_ms();
   gpu::context();
@@ -233,6 +327,74 @@ ProcessResult process(Mesh mesh, double concavity, int num_parts) {
   log(buf);
   g_times.total = now_ms() - t_start;
   return {out, final_c, n};
+}
+
+std::vector<ProcessResult> process_batch(const MeshList& meshes, double concavity, int num_parts,
+                                         const std::vector<unsigned int>& seeds, int threads) {
+  if (seeds.size() != meshes.size())
+    throw std::runtime_error("process_batch: one seed per mesh is required");
+  const int n = (int)meshes.size();
+  std::vector<ProcessResult> results(n);
+  if (n == 0) return results;
+  if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
+  threads = std::min(threads, n);
+  std::atomic<int> next{0};
+  std::vector<std::string> errors(n);
+  std::vector<StageTimes> times(threads);
+  auto worker = [&](int w) {
+    try {
+      gpu::ThreadContext tctx(gpu::default_device());
+      tl_quiet = true;
+#ifdef _OPENMP
+      omp_set_num_threads(1);  // the batch is the parallelism; no nested teams
+#endif
+      std::mt19937 eng;
+      set_thread_engine(&eng);
+      for (int i = next++; i < n; i = next++) {
+        eng.seed(seeds[i]);
+        try {
+          results[i] = process(meshes[i], concavity, num_parts);
+        } catch (const std::exception& e) {
+          errors[i] = e.what();
+        }
+        const StageTimes& t = g_times;
+        StageTimes& acc = times[w];
+        acc.preprocess += t.preprocess;
+        acc.visibility += t.visibility;
+        acc.scoring += t.scoring;
+        acc.clip += t.clip;
+        acc.concavity += t.concavity;
+        acc.cages += t.cages;
+        acc.hulls += t.hulls;
+        acc.total += t.total;
+        acc.iterations += t.iterations;
+      }
+      set_thread_engine(nullptr);
+      tl_quiet = false;
+    } catch (const std::exception& e) {
+      for (int i = next++; i < n; i = next++) errors[i] = e.what();
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int w = 0; w < threads; ++w) pool.emplace_back(worker, w);
+  for (auto& t : pool) t.join();
+  StageTimes sum;
+  for (const auto& t : times) {
+    sum.preprocess += t.preprocess;
+    sum.visibility += t.visibility;
+    sum.scoring += t.scoring;
+    sum.clip += t.clip;
+    sum.concavity += t.concavity;
+    sum.cages += t.cages;
+    sum.hulls += t.hulls;
+    sum.total += t.total;
+    sum.iterations += t.iterations;
+  }
+  g_times = sum;
+  for (int i = 0; i < n; ++i)
+    if (!errors[i].empty())
+      throw std::runtime_error("process_batch: mesh " + std::to_string(i) + ": " + errors[i]);
+  return results;
 }
 
 }  // namespace visacd

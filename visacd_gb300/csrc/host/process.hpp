@@ -31,7 +31,17 @@ double compute_final_concavity(const MeshList& parts, const MeshList& hulls);
 // lib/src/process.cpp:238-347.
 ProcessResult process(Mesh mesh, double concavity, int num_parts);
 
-// Per-stage wall time of the last process() call (ms), for benchmarks.
+// Many meshes decomposed concurrently (no counterpart in the reference, whose
+// process() takes one mesh): `threads` workers (0 = all hardware threads), each
+// with its own GPU context and stream, pull meshes from a shared counter. Mesh i
+// runs with its own std::mt19937 seeded with seeds[i], so its result equals
+// set_seed(seeds[i]); process(meshes[i], concavity, num_parts) whatever the
+// thread count or order. Worker threads do not log.
+std::vector<ProcessResult> process_batch(const MeshList& meshes, double concavity, int num_parts,
+                                         const std::vector<unsigned int>& seeds, int threads);
+
+// Per-stage wall time of the last process() call (ms), for benchmarks; after
+// process_batch, the sums over all its meshes (thread-seconds, not wall time).
 struct StageTimes {
   double preprocess = 0, visibility = 0, scoring = 0, clip = 0, concavity = 0, cages = 0,
          hulls = 0, total = 0;

@@ -62,7 +62,7 @@ double point_triangle_distance(const Vec3& p, const Vec3& a, const Vec3& b, cons
   return norm(p - closest_point_on_triangle(p, a, b, c));
 }
 
-void manifold_preprocess(Mesh& m, double scale, double level) {
+void manifold_preprocess_host(Mesh& m, double scale, double level) {
   const int nt = (int)m.triangles.size();
   if (nt == 0 || m.vertices.empty()) {
     m.clear();

@@ -13,6 +13,8 @@ All functions return (vertices float64 (n, 3), triangles int32 (m, 3)).
 """
 from __future__ import annotations
 
+import functools
+
 import numpy as np
 
 
@@ -53,6 +55,12 @@ def _icosahedron() -> tuple[np.ndarray, np.ndarray]:
 
 
 def icosphere(level: int) -> tuple[np.ndarray, np.ndarray]:
+    v, f = _icosphere_cached(level)
+    return v.copy(), f.copy()
+
+
+@functools.lru_cache(maxsize=8)
+def _icosphere_cached(level: int) -> tuple[np.ndarray, np.ndarray]:
     v, f = _icosahedron()
     for _ in range(level):
         e = np.concatenate([f[:, [0, 1]], f[:, [1, 2]], f[:, [2, 0]]], axis=0)
