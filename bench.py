@@ -340,6 +340,95 @@ def run_decompositions(args) -> dict:
     return out
 
 
+def run_learned_batch(args) -> dict:
+    """Decompositions/s of the batched + learned method against the plain one on
+    held-out blobs (displaced icospheres, subdivision 3-4, seeds 1,000,000+,
+    never seen in training), process(concavity 0.02, 64 parts):
+      plain    — the reference's loop, one mesh after another, exhaustive split
+                 search (set_seed(seed) per mesh);
+      batched  — process_batch over all meshes (one worker thread and GPU
+                 stream each), exhaustive search: bit-identical results;
+      batched + learned — process_batch with the learned proposer (probe of 64
+                 reference candidates, fallback to the exhaustive search).
+    The concavity gap of learned vs plain is set beside the plain method's own
+    seed-to-seed spread (same meshes, seed + 1000), its noise floor."""
+    from visacd_gb300 import build, proposer as pp
+
+    build.build_host()
+    from visacd_gb300 import visacd as V
+
+    V.config.verbose = False
+    seeds = list(range(pp.HELDOUT_SEED0, pp.HELDOUT_SEED0 + args.c5_blobs))
+    meshes = V.MeshList()
+    for s in seeds:
+        _, v, t, _, _ = pp.make_blob(s)
+        m = V.Mesh()
+        m.vertices = V.VecArray3d(v.tolist())
+        m.triangles = V.make_vecarray3i(t.astype(np.int32))
+        meshes.append(m)
+    conc, nparts = 0.02, 64
+    V.set_seed(0)
+    V.process(meshes[0], conc, nparts)  # warm-up (context, kernels, allocator)
+
+    def sequential(mode, seed_shift=0):
+        V.config.plane_proposer = mode
+        V._reset_counters()
+        t0 = time.perf_counter()
+        res = []
+        for m, s in zip(meshes, seeds):
+            V.set_seed(s + seed_shift)
+            res.append(V.process(m, conc, nparts))
+        dt = time.perf_counter() - t0
+        return dt, res, V._stage_times()
+
+    def batched(mode):
+        V.config.plane_proposer = mode
+        V._reset_counters()
+        t0 = time.perf_counter()
+        res = V.process_batch(meshes, conc, nparts, seeds, args.c5_threads)
+        return time.perf_counter() - t0, res, V._stage_times()
+
+    try:
+        t_plain, r_plain, st_plain = sequential("exhaustive")
+        t_bx, r_bx, _ = batched("exhaustive")
+        t_bl, r_bl, st_bl = batched("learned")
+        _, r_alt, _ = sequential("exhaustive", 1000) if args.c5_noise else (None, None, None)
+        _, _, st_l = sequential("learned") if args.c5_fallbacks else (None, None, None)
+    finally:
+        V.config.plane_proposer = "exhaustive"
+    n = len(seeds)
+    cp = np.array([r.concavity for r in r_plain])
+    cl = np.array([r.concavity for r in r_bl])
+    out = {
+        "workload": f"{n} held-out displaced-icosphere blobs (subdivision 3-4), process(0.02, 64)",
+        "plain_decomps_per_s": n / t_plain,
+        "batched_decomps_per_s": n / t_bx,
+        "batched_learned_decomps_per_s": n / t_bl,
+        "speedup_batched_learned_vs_plain": t_plain / t_bl,
+        "speedup_batched_vs_plain": t_plain / t_bx,
+        "batched_identical_to_plain": all(a.concavity == b.concavity and a.num_parts == b.num_parts
+                                          for a, b in zip(r_bx, r_plain)),
+        "threads": args.c5_threads or os.cpu_count(),
+        "concavity_plain_mean": float(cp.mean()),
+        "concavity_learned_mean": float(cl.mean()),
+        "concavity_gap_of_means": float(cl.mean() / cp.mean() - 1.0),
+        "parts_plain_mean": float(np.mean([r.num_parts for r in r_plain])),
+        "parts_learned_mean": float(np.mean([r.num_parts for r in r_bl])),
+        "stages_ms_plain_all_meshes": {k: round(v, 1) for k, v in st_plain.items()
+                                       if k.startswith("conc_") or k in ("vis_ms", "score_ms", "lp_ms")},
+        "stages_ms_batched_learned_thread_sum": {k: round(v, 1) if isinstance(v, float) else v
+                                                 for k, v in st_bl.items()},
+    }
+    if r_alt is not None:
+        ca = np.array([r.concavity for r in r_alt])
+        out["concavity_plain_reseeded_mean"] = float(ca.mean())
+        out["concavity_gap_of_means_plain_reseeded"] = float(ca.mean() / cp.mean() - 1.0)
+    if st_l is not None:
+        out["learned_fallback_rate"] = st_l["lp_fallbacks"] / max(st_l["lp_calls"], 1)
+        out["learned_splits"] = st_l["lp_calls"]
+    return out
+
+
 class RefScoringKernel:
     """The reference's plane_point_side_and_rate_kernel (lib/cuda/plane_intersections.cu),
     compiled unchanged from its source into a cubin, launched through the CUDA
@@ -585,7 +674,16 @@ def main():
     ap.add_argument("--batch", action="store_true", help="batching workload only")
     ap.add_argument("--batch-parts", type=int, default=256)
     ap.add_argument("--sweep-sizes", type=int, nargs="+", default=[20, 22, 24, 26])
+    ap.add_argument("--c5", action="store_true", help="batched + learned decompositions only")
+    ap.add_argument("--no-c5", action="store_true", help="skip the batched + learned decompositions")
+    ap.add_argument("--c5-blobs", type=int, default=64)
+    ap.add_argument("--c5-threads", type=int, default=0, help="process_batch workers (0 = all cores)")
+    ap.add_argument("--c5-noise", action="store_true", help="also run plain with other seeds (noise floor)")
+    ap.add_argument("--c5-fallbacks", action="store_true", help="also run learned sequentially (fallback rate)")
     args = ap.parse_args()
+    if args.c5:
+        print(json.dumps(run_learned_batch(args)))
+        return
     if args.sweep:
         print(json.dumps(run_precision_sweep(args)))
         return
@@ -600,6 +698,8 @@ def main():
             out["cpu_baseline"] = cpu_baseline_sample()
         if rank == 0 and out is not None and not args.no_process:
             out["process"] = run_decompositions(args)
+        if rank == 0 and out is not None and not args.no_c5:
+            out["decomps"] = run_learned_batch(args)
     if rank == 0 and out is not None:
         print(json.dumps(out))
 

@@ -244,6 +244,18 @@ int visacd_sdf_remesh(visacd_ctx* ctx, const double* verts, int32_t nv, const in
 /* Copies the last remesh result: verts out_nv x 3 float64, tris out_nt x 3 int32. */
 int visacd_sdf_fetch(visacd_ctx* ctx, double* verts, int32_t* tris);
 
+/* ---- hull merging ---------------------------------------------------------- */
+/* Exact minimum vertex-to-vertex distance between pairs of hulls: the
+   mesh_dist gate of multimerge_ch (lib/src/postprocess.cpp:64-200,
+   lib/src/cost.cpp:125-159). Hull h owns vertices [offsets[h], offsets[h+1])
+   of verts (float64 xyz, host); pairs is P x 2 hull indices; out[k] (host, P)
+   = the distance of pair k, equal bit for bit to the host's nearest-neighbour
+   result, or DBL_MAX when a hull is empty or the pair's bounding boxes are
+   farther apart than cutoff (pass DBL_MAX to compute every pair).
+   Synchronizes. */
+int visacd_hull_distances(visacd_ctx* ctx, const double* verts, const int64_t* offsets, int32_t H,
+                          const int32_t* pairs, int64_t P, double cutoff, double* out);
+
 /* ---- learned plane proposer ---------------------------------------------- */
 /* No counterpart in the reference: a small network that proposes split planes
    in place of the random candidate draw of lib/src/process.cpp:28-72, whose

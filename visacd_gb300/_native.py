@@ -29,7 +29,7 @@ EXPORTED = [
     "visacd_lp_param_count", "visacd_lp_create", "visacd_lp_destroy", "visacd_lp_get_params",
     "visacd_lp_features", "visacd_lp_forward", "visacd_lp_propose", "visacd_lp_grads",
     "visacd_lp_train_step",
-    "visacd_sdf_remesh", "visacd_sdf_fetch",
+    "visacd_sdf_remesh", "visacd_sdf_fetch", "visacd_hull_distances",
 ]
 
 LP_POINTS = 2048
@@ -109,6 +109,7 @@ def load() -> C.CDLL:
     lib.classify_and_rate_planes.restype = None
     lib.visacd_sdf_remesh.argtypes = [P, P, i32, P, i32, C.c_double, C.c_double, C.POINTER(i32), C.POINTER(i32)]
     lib.visacd_sdf_fetch.argtypes = [P, P, P]
+    lib.visacd_hull_distances.argtypes = [P, P, P, i32, P, i64, C.c_double, P]
     lib.visacd_lp_param_count.argtypes = []
     lib.visacd_lp_create.argtypes = [P, P, C.c_uint32, C.POINTER(P)]
     lib.visacd_lp_destroy.argtypes = [P]
@@ -288,6 +289,33 @@ class Context:
         ot = np.empty((nt.value, 3), np.int32)
         _check(lib().visacd_sdf_fetch(self._h, _ptr(ov), _ptr(ot)), "visacd_sdf_fetch")
         return ov, ot
+
+    # ---- concavity metric --------------------------------------------------
+    def face_hausdorff(self, va, ta, xa, ida, vb, tb, xb, idb) -> float:
+        """Sampled symmetric face Hausdorff distance (visacd_face_hausdorff)."""
+        f = lambda a, c: np.ascontiguousarray(np.asarray(a, dtype=np.float64)).reshape(-1, c)
+        g = lambda a, c: np.ascontiguousarray(np.asarray(a, dtype=np.int32)).reshape(-1, c)
+        va, xa, vb, xb = f(va, 3), f(xa, 3), f(vb, 3), f(xb, 3)
+        ta, tb, ida, idb = g(ta, 3), g(tb, 3), g(ida, 1), g(idb, 1)
+        out = C.c_double()
+        _check(lib().visacd_face_hausdorff(self._h, _ptr(va), len(va), _ptr(ta), len(ta), _ptr(xa), _ptr(ida),
+                                           len(xa), _ptr(vb), len(vb), _ptr(tb), len(tb), _ptr(xb), _ptr(idb),
+                                           len(xb), C.byref(out)), "visacd_face_hausdorff")
+        return out.value
+
+    # ---- hull merging ------------------------------------------------------
+    def hull_distances(self, hulls, pairs, cutoff: float = np.finfo(np.float64).max):
+        """Minimum vertex distance of each (a, b) in pairs between the vertex
+        arrays hulls[a] and hulls[b]."""
+        vs = [np.ascontiguousarray(np.asarray(h, dtype=np.float64)).reshape(-1, 3) for h in hulls]
+        off = np.zeros(len(vs) + 1, dtype=np.int64)
+        off[1:] = np.cumsum([len(v) for v in vs])
+        allv = np.ascontiguousarray(np.concatenate(vs) if vs else np.zeros((0, 3)))
+        pr = np.ascontiguousarray(np.asarray(pairs, dtype=np.int32)).reshape(-1, 2)
+        out = np.empty(len(pr), dtype=np.float64)
+        _check(lib().visacd_hull_distances(self._h, _ptr(allv), _ptr(off), len(vs), _ptr(pr), len(pr),
+                                           float(cutoff), _ptr(out)), "visacd_hull_distances")
+        return out
 
     # ---- scoring -----------------------------------------------------------
     def score_planes(self, planes, points, edges):

@@ -111,6 +111,7 @@ enum CtxSlot {
   kSlotSdf,
   kSlotSdfOut,
   kSlotSdfTris,
+  kSlotHull,
   kSlotCount
 };
 
@@ -177,6 +178,7 @@ enum KernelId {
   kKLpAdam,
   kKLpMisc,
   kKSdf,
+  kKHullDist,
   kKMisc,
   kKCount
 };

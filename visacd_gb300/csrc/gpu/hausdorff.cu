@@ -29,7 +29,9 @@ struct HGrid {
   const int* start;   // cell -> first sorted point (size cells + 1)
   const int* order;   // sorted point ids
   const double* pts;  // 3 doubles per point
+  const float4* spts; // points in cell order as float (x, y, z, id bits): the FP32 pre-filter
   int n;
+  float eabs;         // bound of |FP32 distance - exact distance| for this grid's points and queries
 };
 
 struct HCounters {
@@ -93,65 +95,100 @@ __global__ void hscatter_kernel(int n, const int* __restrict__ cell_of, const un
   }
 }
 
+__global__ void hsorted_kernel(const double* __restrict__ pts, const int* __restrict__ order, int n,
+                               float4* __restrict__ spts) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int i = order[k];
+    spts[k] = make_float4((float)pts[3 * (int64_t)i], (float)pts[3 * (int64_t)i + 1], (float)pts[3 * (int64_t)i + 2],
+                          __int_as_float(i));
+  }
+}
+
 __global__ void hstart_kernel(const unsigned long long* __restrict__ off, int cells, int* __restrict__ start) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= cells; i += gridDim.x * blockDim.x)
     start[i] = (int)off[i];
 }
 
-// One direction: queries Q against the other surface (grid G over its samples,
-// sample triangle ids, mesh verts/tris).
-__global__ void __launch_bounds__(128) hquery_kernel(const double* __restrict__ Q, int nq, HGrid G,
+// Exact k nearest samples of q by Chebyshev rings of grid cells around q's
+// cell, until the k found are settled (the k-th is no farther than the ring
+// radius) or every cell was seen.
+__device__ __forceinline__ void knn_rings(const HGrid& G, const double (&q)[3], double (&bd)[kKnn],
+                                          int (&bi)[kKnn], int& cnt) {
+  const int cx = cell_coord(q[0], G.lo[0], G.h, G.dim[0]);
+  const int cy = cell_coord(q[1], G.lo[1], G.h, G.dim[1]);
+  const int cz = cell_coord(q[2], G.lo[2], G.h, G.dim[2]);
+  const int rmax = max(G.dim[0], max(G.dim[1], G.dim[2]));
+  const float qf[3] = {(float)q[0], (float)q[1], (float)q[2]};
+  float thr = 3.4e38f;
+  for (int r = 0; r <= rmax; ++r) {
+    for (int dz = -r; dz <= r; ++dz) {
+      const int z = cz + dz;
+      if (z < 0 || z >= G.dim[2]) continue;
+      for (int dy = -r; dy <= r; ++dy) {
+        const int y = cy + dy;
+        if (y < 0 || y >= G.dim[1]) continue;
+        const bool face = abs(dz) == r || abs(dy) == r;
+        for (int dx = -r; dx <= r; dx += (face ? 1 : 2 * r > 0 ? 2 * r : 1)) {
+          const int x = cx + dx;
+          if (x >= 0 && x < G.dim[0]) {
+            const int c = (z * G.dim[1] + y) * G.dim[0] + x;
+            for (int k = G.start[c]; k < G.start[c + 1]; ++k) {
+              const float4 sp = G.spts[k];
+              // FP32 pre-filter: a candidate whose FP32 distance exceeds the
+              // current k-th distance by more than the rounding bound cannot
+              // enter the list; the rest are decided in FP64.
+              if (cnt == kKnn) {
+                const float fx = sp.x - qf[0], fy = sp.y - qf[1], fz = sp.z - qf[2];
+                if (fx * fx + fy * fy + fz * fz > thr) continue;
+              }
+              const int pi = __float_as_int(sp.w);
+              const double* pp = G.pts + 3 * (int64_t)pi;
+              const double ex = ds(pp[0], q[0]), ey = ds(pp[1], q[1]), ez = ds(pp[2], q[2]);
+              const double d2 = da(da(dm(ex, ex), dm(ey, ey)), dm(ez, ez));
+              if (cnt < kKnn || d2 < bd[cnt - 1]) {
+                int j = cnt < kKnn ? cnt++ : kKnn - 1;
+                while (j > 0 && bd[j - 1] > d2) {
+                  bd[j] = bd[j - 1];
+                  bi[j] = bi[j - 1];
+                  --j;
+                }
+                bd[j] = d2;
+                bi[j] = pi;
+                if (cnt == kKnn) {
+                  // (sqrt(kth) + eabs)^2, rounded up generously for the FP32 compare
+                  const double b = __dsqrt_rn(bd[kKnn - 1]) + (double)G.eabs;
+                  thr = __double2float_ru(b * b) * (1.0f + 1.0f / 65536.0f);
+                }
+              }
+            }
+          }
+          if (dx == r) break;
+        }
+      }
+    }
+    const double rad = (double)r * G.h;
+    if (cnt == kKnn && bd[kKnn - 1] <= rad * rad) return;
+  }
+}
+
+// One direction: queries Q (visited in the order qorder, their own grid's
+// cell order, so a warp searches one neighbourhood) against the other
+// surface (grid G over its samples, sample triangle ids, mesh verts/tris).
+// The result, a maximum, does not depend on the order.
+__global__ void __launch_bounds__(128) hquery_kernel(const double* __restrict__ Q, int nq,
+                                                     const int* __restrict__ qorder, HGrid G,
                                                      const int* __restrict__ ids,
                                                      const double* __restrict__ mv,
                                                      const int* __restrict__ mt,
                                                      unsigned long long* __restrict__ out_max) {
   double local = 0.0;
-  for (int qi = blockIdx.x * blockDim.x + threadIdx.x; qi < nq; qi += gridDim.x * blockDim.x) {
+  for (int qk = blockIdx.x * blockDim.x + threadIdx.x; qk < nq; qk += gridDim.x * blockDim.x) {
+    const int qi = qorder[qk];
     const double q[3] = {Q[3 * (int64_t)qi], Q[3 * (int64_t)qi + 1], Q[3 * (int64_t)qi + 2]};
     double bd[kKnn];
     int bi[kKnn];
     int cnt = 0;
-    const int cx = cell_coord(q[0], G.lo[0], G.h, G.dim[0]);
-    const int cy = cell_coord(q[1], G.lo[1], G.h, G.dim[1]);
-    const int cz = cell_coord(q[2], G.lo[2], G.h, G.dim[2]);
-    const int rmax = max(G.dim[0], max(G.dim[1], G.dim[2]));
-    for (int r = 0; r <= rmax; ++r) {
-      for (int dz = -r; dz <= r; ++dz) {
-        const int z = cz + dz;
-        if (z < 0 || z >= G.dim[2]) continue;
-        for (int dy = -r; dy <= r; ++dy) {
-          const int y = cy + dy;
-          if (y < 0 || y >= G.dim[1]) continue;
-          const bool face = abs(dz) == r || abs(dy) == r;
-          for (int dx = -r; dx <= r; dx += (face ? 1 : 2 * r > 0 ? 2 * r : 1)) {
-            const int x = cx + dx;
-            if (x >= 0 && x < G.dim[0]) {
-              const int c = (z * G.dim[1] + y) * G.dim[0] + x;
-              for (int k = G.start[c]; k < G.start[c + 1]; ++k) {
-                const int pi = G.order[k];
-                const double* pp = G.pts + 3 * (int64_t)pi;
-                const double ex = ds(pp[0], q[0]), ey = ds(pp[1], q[1]), ez = ds(pp[2], q[2]);
-                const double d2 = da(da(dm(ex, ex), dm(ey, ey)), dm(ez, ez));
-                if (cnt < kKnn || d2 < bd[cnt - 1]) {
-                  int j = cnt < kKnn ? cnt++ : kKnn - 1;
-                  while (j > 0 && bd[j - 1] > d2) {
-                    bd[j] = bd[j - 1];
-                    bi[j] = bi[j - 1];
-                    --j;
-                  }
-                  bd[j] = d2;
-                  bi[j] = pi;
-                }
-              }
-            }
-            if (dx == r) break;
-          }
-        }
-      }
-      const double rad = (double)r * G.h;
-      if (cnt == kKnn && bd[kKnn - 1] <= rad * rad) break;
-      if (cnt == G.n && r >= rmax) break;
-    }
+    knn_rings(G, q, bd, bi, cnt);
     double cmin = DBL_MAX;
     for (int j = 0; j < cnt; ++j) {
       const int tri = ids[bi[j]];
@@ -207,21 +244,42 @@ extern "C" int visacd_face_hausdorff(visacd_ctx* ctx, const double* va, int32_t 
     g.h = h;
     g.n = n;
   };
-  HGrid ga, gb;
-  grid_for_points(xa, na, ga);
-  grid_for_points(xb, nb, gb);
-  const int cells_a = ga.dim[0] * ga.dim[1] * ga.dim[2], cells_b = gb.dim[0] * gb.dim[1] * gb.dim[2];
+  // One grid over each sample set (g[0] over A, g[1] over B).
+  HGrid g[2];
+  grid_for_points(xa, na, g[0]);
+  grid_for_points(xb, nb, g[1]);
+  // FP32 pre-filter bound: coordinates rounded to float differ by at most
+  // 2^-24 |x| each, the difference and the squared sum add a few ulps; with
+  // M the largest |coordinate| of both sets, |d_f32 - d| <= 8 M 2^-24.
+  double M = 0;
+  for (int k = 0; k < 2; ++k)
+    for (int a = 0; a < 3; ++a)
+      M = std::max(M, std::max(std::fabs(g[k].lo[a]), std::fabs(g[k].lo[a] + g[k].h * g[k].dim[a])));
+  for (int k = 0; k < 2; ++k) g[k].eabs = (float)(M * std::ldexp(1.0, -21) + 1e-30);
+  int cells[2];
+  for (int k = 0; k < 2; ++k) cells[k] = g[k].dim[0] * g[k].dim[1] * g[k].dim[2];
   size_t off = 0;
   auto carve = [&](size_t b) { size_t o = off; off += al(b); return o; };
   const size_t o_va = carve((size_t)nva * 24), o_ta = carve((size_t)nta * 12), o_xa = carve((size_t)na * 24),
                o_ia = carve((size_t)na * 4), o_vb = carve((size_t)nvb * 24), o_tb = carve((size_t)ntb * 12),
-               o_xb = carve((size_t)nb * 24), o_ib = carve((size_t)nb * 4),
-               o_ca = carve((size_t)(cells_a + 1) * 4), o_cb = carve((size_t)(cells_b + 1) * 4),
-               o_fa = carve((size_t)cells_a * 4), o_fb = carve((size_t)cells_b * 4),
-               o_oa = carve((size_t)(cells_a + 1) * 8), o_ob = carve((size_t)(cells_b + 1) * 8),
-               o_sa = carve((size_t)(cells_a + 1) * 4), o_sb = carve((size_t)(cells_b + 1) * 4),
-               o_ra = carve((size_t)na * 4), o_rb = carve((size_t)nb * 4), o_cla = carve((size_t)na * 4),
-               o_clb = carve((size_t)nb * 4), o_mx = carve(64);
+               o_xb = carve((size_t)nb * 24), o_ib = carve((size_t)nb * 4), o_mx = carve(64);
+  // Per grid: counts + fill (zeroed together), offsets, starts, order, cell of point, sorted float points.
+  size_t zero_begin = off;
+  size_t o_cnt[2], o_fill[2];
+  for (int k = 0; k < 2; ++k) {
+    o_cnt[k] = carve((size_t)(cells[k] + 1) * 4);
+    o_fill[k] = carve((size_t)cells[k] * 4);
+  }
+  const size_t zero_end = off;
+  size_t o_off[2], o_start[2], o_order[2], o_cell[2], o_spts[2];
+  for (int k = 0; k < 2; ++k) {
+    const int n = k == 0 ? na : nb;
+    o_off[k] = carve((size_t)(cells[k] + 1) * 8);
+    o_start[k] = carve((size_t)(cells[k] + 1) * 4);
+    o_order[k] = carve((size_t)n * 4);
+    o_cell[k] = carve((size_t)n * 4);
+    o_spts[k] = carve((size_t)n * 16);
+  }
   VTRY(ensure_slot(ctx, kSlotHausdorff, off));
   char* B = slot<char>(ctx, kSlotHausdorff);
   cudaStream_t st = ctx->stream;
@@ -233,38 +291,37 @@ extern "C" int visacd_face_hausdorff(visacd_ctx* ctx, const double* va, int32_t 
   VCUDA(cudaMemcpyAsync(B + o_tb, tb, (size_t)ntb * 12, cudaMemcpyHostToDevice, st));
   VCUDA(cudaMemcpyAsync(B + o_xb, xb, (size_t)nb * 24, cudaMemcpyHostToDevice, st));
   VCUDA(cudaMemcpyAsync(B + o_ib, idb, (size_t)nb * 4, cudaMemcpyHostToDevice, st));
-  VCUDA(cudaMemsetAsync(B + o_ca, 0, (size_t)(cells_a + 1) * 4, st));
-  VCUDA(cudaMemsetAsync(B + o_cb, 0, (size_t)(cells_b + 1) * 4, st));
-  VCUDA(cudaMemsetAsync(B + o_fa, 0, (size_t)cells_a * 4, st));
-  VCUDA(cudaMemsetAsync(B + o_fb, 0, (size_t)cells_b * 4, st));
+  VCUDA(cudaMemsetAsync(B + zero_begin, 0, zero_end - zero_begin, st));
   VCUDA(cudaMemsetAsync(B + o_mx, 0, 64, st));
-  ga.pts = (const double*)(B + o_xa);
-  gb.pts = (const double*)(B + o_xb);
-  // Bucket both sample sets.
-  struct Side { HGrid* g; int cells; size_t o_c, o_f, o_o, o_s, o_r, o_cl; int n; };
-  Side sides[2] = {{&ga, cells_a, o_ca, o_fa, o_oa, o_sa, o_ra, o_cla, na},
-                   {&gb, cells_b, o_cb, o_fb, o_ob, o_sb, o_rb, o_clb, nb}};
-  for (auto& sd : sides) {
-    int* counts = (int*)(B + sd.o_c);
-    int* cell_of = (int*)(B + sd.o_cl);
-    const unsigned gn = grid_for(sd.n, 256, 8LL * ctx->sm_count);
-    VLAUNCH(ctx, kKHausdorff, gn, 256, 0, hcount_kernel, *sd.g, counts, cell_of);
-    VTRY(exclusive_scan_u32_to_u64(ctx, (const uint32_t*)counts, (uint64_t*)(B + sd.o_o), sd.cells));
-    VLAUNCH(ctx, kKHausdorff, gn, 256, 0, hscatter_kernel, sd.n, cell_of,
-            (const unsigned long long*)(B + sd.o_o), (int*)(B + sd.o_f), (int*)(B + sd.o_r));
-    VLAUNCH(ctx, kKHausdorff, grid_for(sd.cells + 1, 256, 8LL * ctx->sm_count), 256, 0, hstart_kernel,
-            (const unsigned long long*)(B + sd.o_o), sd.cells, (int*)(B + sd.o_s));
-    sd.g->start = (const int*)(B + sd.o_s);
-    sd.g->order = (const int*)(B + sd.o_r);
+  // Bucket both sample sets (counting sort by cell).
+  for (int k = 0; k < 2; ++k) {
+    const int n = k == 0 ? na : nb;
+    g[k].pts = (const double*)(B + (k == 0 ? o_xa : o_xb));
+    g[k].n = n;
+    int* counts = (int*)(B + o_cnt[k]);
+    int* cell_of = (int*)(B + o_cell[k]);
+    const unsigned gn = grid_for(n, 256, 8LL * ctx->sm_count);
+    VLAUNCH(ctx, kKHausdorff, gn, 256, 0, hcount_kernel, g[k], counts, cell_of);
+    VTRY(exclusive_scan_u32_to_u64(ctx, (const uint32_t*)counts, (uint64_t*)(B + o_off[k]), cells[k]));
+    VLAUNCH(ctx, kKHausdorff, gn, 256, 0, hscatter_kernel, n, cell_of,
+            (const unsigned long long*)(B + o_off[k]), (int*)(B + o_fill[k]), (int*)(B + o_order[k]));
+    VLAUNCH(ctx, kKHausdorff, grid_for(cells[k] + 1, 256, 8LL * ctx->sm_count), 256, 0, hstart_kernel,
+            (const unsigned long long*)(B + o_off[k]), cells[k], (int*)(B + o_start[k]));
+    VLAUNCH(ctx, kKHausdorff, gn, 256, 0, hsorted_kernel, g[k].pts, (const int*)(B + o_order[k]), n,
+            (float4*)(B + o_spts[k]));
+    g[k].start = (const int*)(B + o_start[k]);
+    g[k].order = (const int*)(B + o_order[k]);
+    g[k].spts = (const float4*)(B + o_spts[k]);
   }
   unsigned long long* mx = (unsigned long long*)(B + o_mx);
-  // Queries of B against A's samples/triangles, then A against B.
+  // Queries of B (in B's cell order) against A's samples/triangles, then A
+  // (in A's order) against B.
   VLAUNCH(ctx, kKHausdorff, grid_for(nb, 128, 8LL * ctx->sm_count), 128, 0, hquery_kernel,
-          (const double*)(B + o_xb), nb, ga, (const int*)(B + o_ia), (const double*)(B + o_va),
-          (const int*)(B + o_ta), mx);
+          (const double*)(B + o_xb), nb, g[1].order, g[0], (const int*)(B + o_ia),
+          (const double*)(B + o_va), (const int*)(B + o_ta), mx);
   VLAUNCH(ctx, kKHausdorff, grid_for(na, 128, 8LL * ctx->sm_count), 128, 0, hquery_kernel,
-          (const double*)(B + o_xa), na, gb, (const int*)(B + o_ib), (const double*)(B + o_vb),
-          (const int*)(B + o_tb), mx);
+          (const double*)(B + o_xa), na, g[0].order, g[1], (const int*)(B + o_ib),
+          (const double*)(B + o_vb), (const int*)(B + o_tb), mx);
   unsigned long long* h = nullptr;
   VTRY(pinned(ctx, 8, (void**)&h));
   VCUDA(cudaMemcpyAsync(h, mx, 8, cudaMemcpyDeviceToHost, st));

@@ -90,6 +90,7 @@ PYBIND11_MODULE(visacd, m) {
       .def_readwrite("gpu_clip", &Config::gpu_clip)
       .def_readwrite("gpu_concavity", &Config::gpu_concavity)
       .def_readwrite("gpu_remesh", &Config::gpu_remesh)
+      .def_readwrite("gpu_merge", &Config::gpu_merge)
       .def_readwrite("plane_proposer", &Config::plane_proposer)
       .def_readwrite("proposer_weights", &Config::proposer_weights)
       .def_readwrite("proposer_probe_planes", &Config::proposer_probe_planes)
@@ -150,9 +151,20 @@ PYBIND11_MODULE(visacd, m) {
     d["lp_calls"] = c.lp_calls;
     d["lp_fallbacks"] = c.lp_fallbacks;
     d["lp_ms"] = c.lp_ms;
+    d["vis_ms"] = c.vis_ms;
+    d["score_ms"] = c.score_ms;
+    const auto& ct = concavity_times();
+    d["conc_sample_ms"] = ct.sample_ms;
+    d["conc_hausdorff_ms"] = ct.hausdorff_ms;
+    d["conc_hull_ms"] = ct.hull_ms;
+    d["conc_samples"] = ct.samples;
+    d["conc_calls"] = ct.calls;
     return d;
   });
-  m.def("_reset_counters", []() { gpu::counters() = gpu::Counters(); });
+  m.def("_reset_counters", []() {
+    gpu::counters() = gpu::Counters();
+    concavity_times() = ConcavityTimes();
+  });
   m.def("_manifold_preprocess", [](py::array_t<double> v, py::array_t<int> t, double scale, double level) {
     Mesh mm = np_to_mesh(v, t);
     manifold_preprocess_host(mm, scale, level);
@@ -212,6 +224,17 @@ PYBIND11_MODULE(visacd, m) {
   });
   m.def("_compute_hb", [](py::array_t<double> v, py::array_t<int> t, py::array_t<double> hv, py::array_t<int> ht, unsigned res) {
     return compute_hb(np_to_mesh(v, t), np_to_mesh(hv, ht), res);
+  });
+  m.def("_sample_points", [](py::array_t<double> v, py::array_t<int> t, unsigned res) {
+    std::vector<Vec3> x;
+    std::vector<int> ids;
+    extract_point_set(np_to_mesh(v, t), x, ids, res, 1, true);
+    return py::make_tuple(verts_to_np(x), py::array_t<int>(ids.size(), ids.data()));
+  });
+  m.def("_mesh_dist", [](py::array_t<double> a, py::array_t<double> b) {
+    Mesh ma = np_to_mesh(a, py::array_t<int>(std::vector<py::ssize_t>{0, 3}));
+    Mesh mb = np_to_mesh(b, py::array_t<int>(std::vector<py::ssize_t>{0, 3}));
+    return mesh_dist(ma, mb);
   });
   m.def("_mesh_volume", [](py::array_t<double> v, py::array_t<int> t) { return mesh_volume(np_to_mesh(v, t)); });
   m.def("_separate_disjoint", [](py::array_t<double> v, py::array_t<int> t) {

@@ -94,6 +94,7 @@ struct Config {
   bool gpu_clip = true;        // split parts with the GPU clip kernels (else the host clip)
   bool gpu_concavity = true;   // Hausdorff term of the concavity metric on the GPU
   bool gpu_remesh = true;      // SDF remesh (manifold and cages) on the GPU
+  bool gpu_merge = true;       // hull-pair distances of hull merging on the GPU
   // Split-plane search: "exhaustive" (the reference's random candidate draw)
   // or "learned" (16 planes from the learned proposer plus a probe of
   // `proposer_probe_planes` random candidates; when the best proposal scores

@@ -10,9 +10,9 @@
 // project's kd-tree (the reference uses nanoflann); distances to the sampled
 // triangles use the exact closest-point test.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <queue>
-#include <unordered_set>
 #include <vector>
 
 #include "geometry.hpp"
@@ -36,26 +36,30 @@ void extract_point_set(const Mesh& m, std::vector<Vec3>& samples, std::vector<in
   std::discrete_distribution<size_t> pick(areas.begin(), areas.end());
   std::uniform_real_distribution<double> uni(0.0, 1.0);
   std::mt19937& eng = random_engine();
-  std::unordered_set<size_t> touched;
+  // Triangles drawn at least once (a bitmap: only membership matters, the
+  // untouched ones are visited in index order below).
+  std::vector<char> touched(m.triangles.size(), 0);
+  samples.reserve(samples.size() + resolution + (one_per_tri ? m.triangles.size() : 0));
+  tri_ids.reserve(samples.capacity());
   auto sample = [&](size_t ti) {
     const auto& t = m.triangles[ti];
     double a = uni(eng);
     double b = uni(eng);
     const Vec3 &v0 = m.vertices[t[0]], &v1 = m.vertices[t[1]], &v2 = m.vertices[t[2]];
+    const double sa = std::sqrt(a);  // correctly rounded: one evaluation serves all six uses
     Vec3 v;
-    for (int k = 0; k < 3; ++k)
-      v[k] = (1 - std::sqrt(a)) * v0[k] + (std::sqrt(a) * (1 - b)) * v1[k] + b * std::sqrt(a) * v2[k];
+    for (int k = 0; k < 3; ++k) v[k] = (1 - sa) * v0[k] + (sa * (1 - b)) * v1[k] + b * sa * v2[k];
     samples.push_back(v);
     tri_ids.push_back((int)ti);
   };
   for (size_t done = 0; done < resolution; ++done) {
     size_t ti = pick(eng);
     sample(ti);
-    touched.insert(ti);
+    touched[ti] = 1;
   }
   if (one_per_tri)
     for (size_t i = 0; i < m.triangles.size(); ++i)
-      if (touched.find(i) == touched.end()) sample(i);
+      if (!touched[i]) sample(i);
 }
 
 namespace {
@@ -187,13 +191,26 @@ double compute_rv3(const Mesh& c1, const Mesh& c2, const Mesh& ch) {
 }
 
 double compute_hb(const Mesh& a, const Mesh& b, unsigned int resolution) {
+  auto& tm = concavity_times();
+  const auto t0 = std::chrono::steady_clock::now();
   std::vector<Vec3> s1, s2;
   std::vector<int> i1, i2;
   extract_point_set(a, s1, i1, resolution, 1, true);
   extract_point_set(b, s2, i2, resolution, 1, true);
+  const auto t1 = std::chrono::steady_clock::now();
+  tm.sample_ms += std::chrono::duration<double, std::milli>(t1 - t0).count();
+  tm.samples += (long long)(s1.size() + s2.size());
   if (s1.empty() || s2.empty()) return kInf;
-  if (config().gpu_concavity) return gpu::face_hausdorff(a, s1, i1, b, s2, i2);
-  return face_hausdorff(a, s1, i1, b, s2, i2);
+  const double h = config().gpu_concavity ? gpu::face_hausdorff(a, s1, i1, b, s2, i2)
+                                          : face_hausdorff(a, s1, i1, b, s2, i2);
+  tm.hausdorff_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t1).count();
+  tm.calls++;
+  return h;
+}
+
+ConcavityTimes& concavity_times() {
+  static thread_local ConcavityTimes t;
+  return t;
 }
 
 // Merge cost between two hulls and their joint hull (lib/src/cost.cpp:87-105).

@@ -54,6 +54,13 @@ double compute_h(const Mesh& a, const Mesh& b, double k, unsigned int resolution
 double compute_h3(const Mesh& c1, const Mesh& c2, const Mesh& ch, double k, unsigned int resolution);
 double mesh_dist(const Mesh& a, const Mesh& b);
 
+// Per-thread time split of the concavity metric (ms) for benchmarks.
+struct ConcavityTimes {
+  double sample_ms = 0, hausdorff_ms = 0, hull_ms = 0;
+  long long samples = 0, calls = 0;
+};
+ConcavityTimes& concavity_times();
+
 // ---- surfaces.cpp: flat-surface planes (lib/src/support_surface.cpp:14-183).
 struct Surface {
   std::vector<int> triangle_ids;

@@ -208,6 +208,28 @@ void sdf_remesh(Mesh& m, double scale, double level) {
   m.triangles = std::move(ot);
 }
 
+std::vector<double> hull_distances(const MeshList& hulls, const std::vector<std::pair<int, int>>& pairs,
+                                   double cutoff) {
+  std::vector<double> out(pairs.size());
+  if (pairs.empty()) return out;
+  visacd_ctx* ctx = context();
+  std::vector<int64_t> off(hulls.size() + 1, 0);
+  for (size_t h = 0; h < hulls.size(); ++h) off[h + 1] = off[h] + (int64_t)hulls[h].vertices.size();
+  std::vector<double> v;
+  v.reserve(3 * (size_t)off.back());
+  for (const auto& h : hulls)
+    for (const auto& p : h.vertices) v.insert(v.end(), p.begin(), p.end());
+  std::vector<int32_t> pr(2 * pairs.size());
+  for (size_t k = 0; k < pairs.size(); ++k) {
+    pr[2 * k] = pairs[k].first;
+    pr[2 * k + 1] = pairs[k].second;
+  }
+  check(visacd_hull_distances(ctx, v.data(), off.data(), (int32_t)hulls.size(), pr.data(), (int64_t)pairs.size(),
+                              cutoff, out.data()),
+        "visacd_hull_distances");
+  return out;
+}
+
 namespace {
 // Proposer parameters by file path, read once per path.
 const std::vector<float>& proposer_params(const std::string& path) {

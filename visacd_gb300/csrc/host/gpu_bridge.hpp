@@ -54,6 +54,11 @@ MeshList clip(const Mesh& mesh, const Plane& plane, std::vector<int>& pos_map,
 // manifold_preprocess_host.
 void sdf_remesh(Mesh& m, double scale, double level);
 
+// mesh_dist of hull pairs on the GPU (visacd_hull_distances); DBL_MAX where the
+// bounding boxes are farther apart than cutoff.
+std::vector<double> hull_distances(const MeshList& hulls, const std::vector<std::pair<int, int>>& pairs,
+                                   double cutoff);
+
 // Sampled face Hausdorff distance on the GPU (visacd_face_hausdorff).
 double face_hausdorff(const Mesh& A, const std::vector<Vec3>& XA, const std::vector<int>& idA,
                       const Mesh& B, const std::vector<Vec3>& XB, const std::vector<int>& idB);

@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "geometry.hpp"
+#include "gpu_bridge.hpp"
 
 namespace visacd {
 
@@ -91,6 +92,18 @@ MeshList separate_step(const Mesh& part) {
   return out;
 }
 
+// mesh_dist of each listed hull pair, compared by the caller with `threshold`
+// only: the GPU kernel (visacd_hull_distances) returns the same value, or
+// DBL_MAX for pairs whose bounding boxes are already farther apart than
+// threshold.
+std::vector<double> pair_distances(const MeshList& cvxs, const std::vector<std::pair<int, int>>& pairs,
+                                   double threshold) {
+  if (config().gpu_merge) return gpu::hull_distances(cvxs, pairs, threshold);
+  std::vector<double> d(pairs.size());
+  for (size_t k = 0; k < pairs.size(); ++k) d[k] = mesh_dist(cvxs[pairs[k].first], cvxs[pairs[k].second]);
+  return d;
+}
+
 Mesh merged_hull(const Mesh& a, const Mesh& b) {
   std::vector<Vec3> pts = a.vertices;
   pts.insert(pts.end(), b.vertices.begin(), b.vertices.end());
@@ -112,12 +125,16 @@ void multimerge_ch(MeshList& meshes, MeshList& cvxs, double current_concavity, d
   if (n <= 1) return;
   const size_t bound = ((n - 1) * n) >> 1;
   std::vector<double> cost(bound), precost(bound);
+  std::vector<std::pair<int, int>> all_pairs(bound);
   for (size_t idx = 0; idx < bound; ++idx) {
     size_t p1 = (size_t)(std::sqrt(8.0 * idx + 1) - 1) >> 1;
     size_t sum = (p1 * (p1 + 1)) >> 1;
-    size_t p2 = idx - sum;
-    ++p1;
-    double dist = mesh_dist(cvxs[p1], cvxs[p2]);
+    all_pairs[idx] = {(int)(p1 + 1), (int)(idx - sum)};
+  }
+  const std::vector<double> all_dist = pair_distances(cvxs, all_pairs, threshold);
+  for (size_t idx = 0; idx < bound; ++idx) {
+    const size_t p1 = (size_t)all_pairs[idx].first, p2 = (size_t)all_pairs[idx].second;
+    double dist = all_dist[idx];
     if (dist < threshold) {
       Mesh ch = merged_hull(cvxs[p1], cvxs[p2]);
       cost[idx] = compute_h3(cvxs[p1], cvxs[p2], ch, 0.3, 10000);
@@ -155,9 +172,13 @@ void multimerge_ch(MeshList& meshes, MeshList& cvxs, double current_concavity, d
     cvxs.pop_back();
     cost_size -= 1;
     // Costs against the merged hull (row p2, then column p2).
+    std::vector<std::pair<int, int>> row_pairs;
+    for (size_t i = 0; i < cost_size; ++i)
+      if (i != p2) row_pairs.push_back({(int)p2, (int)i});
+    const std::vector<double> row_dist = pair_distances(cvxs, row_pairs, threshold);
     size_t row = ((p2 - 1) * p2) >> 1;
     for (size_t i = 0; i < p2; ++i) {
-      double dist = mesh_dist(cvxs[p2], cvxs[i]);
+      double dist = row_dist[i];
       if (dist < threshold) {
         Mesh ch = merged_hull(cvxs[p2], cvxs[i]);
         cost[row] = compute_h3(cvxs[p2], cvxs[i], ch, 0.3, 10000);
@@ -168,7 +189,7 @@ void multimerge_ch(MeshList& meshes, MeshList& cvxs, double current_concavity, d
     }
     row += p2;
     for (size_t i = p2 + 1; i < cost_size; ++i) {
-      double dist = mesh_dist(cvxs[p2], cvxs[i]);
+      double dist = row_dist[i - 1];
       if (dist < threshold) {
         Mesh ch = merged_hull(cvxs[p2], cvxs[i]);
         cost[row] = compute_h3(cvxs[p2], cvxs[i], ch, 0.3, 10000);

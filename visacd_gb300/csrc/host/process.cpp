@@ -222,9 +222,13 @@ int get_part_with_highest_score(const MeshList& parts) {
 }
 
 int get_part_with_highest_concavity(const MeshList& parts, double& max_concavity) {
-  MeshList hulls;
-  hulls.reserve(parts.size());
-  for (const auto& p : parts) hulls.push_back(convex_hull(p.vertices, true));
+  const auto t0 = std::chrono::steady_clock::now();
+  MeshList hulls(parts.size());
+  // Hulls draw no random numbers: built in parallel (same result in any order).
+#pragma omp parallel for schedule(dynamic, 1) if (parts.size() > 1)
+  for (int i = 0; i < (int)parts.size(); ++i) hulls[i] = convex_hull(parts[i].vertices, true);
+  concavity_times().hull_ms +=
+      std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   int idx = -1;
   for (int i = 0; i < (int)parts.size(); ++i) {
     double c = compute_h(parts[i], hulls[i], 0.3, 3000);
@@ -341,6 +345,8 @@ std::vector<ProcessResult> process_batch(const MeshList& meshes, double concavit
   std::atomic<int> next{0};
   std::vector<std::string> errors(n);
   std::vector<StageTimes> times(threads);
+  std::vector<gpu::Counters> counts(threads);
+  std::vector<ConcavityTimes> ctimes(threads);
   auto worker = [&](int w) {
     try {
       gpu::ThreadContext tctx(gpu::default_device());
@@ -350,6 +356,8 @@ std::vector<ProcessResult> process_batch(const MeshList& meshes, double concavit
 #endif
       std::mt19937 eng;
       set_thread_engine(&eng);
+      gpu::counters() = gpu::Counters();
+      concavity_times() = ConcavityTimes();
       for (int i = next++; i < n; i = next++) {
         eng.seed(seeds[i]);
         try {
@@ -371,6 +379,8 @@ std::vector<ProcessResult> process_batch(const MeshList& meshes, double concavit
       }
       set_thread_engine(nullptr);
       tl_quiet = false;
+      counts[w] = gpu::counters();
+      ctimes[w] = concavity_times();
     } catch (const std::exception& e) {
       for (int i = next++; i < n; i = next++) errors[i] = e.what();
     }
@@ -391,6 +401,27 @@ std::vector<ProcessResult> process_batch(const MeshList& meshes, double concavit
     sum.iterations += t.iterations;
   }
   g_times = sum;
+  // Counters of the workers (zeroed per thread) are added to the caller's.
+  auto& c = gpu::counters();
+  auto& ct = concavity_times();
+  for (int w = 0; w < threads; ++w) {
+    const auto& k = counts[w];
+    c.vis_calls += k.vis_calls;
+    c.vis_pairs += k.vis_pairs;
+    c.vis_edges += k.vis_edges;
+    c.score_calls += k.score_calls;
+    c.plane_edge_pairs += k.plane_edge_pairs;
+    c.lp_calls += k.lp_calls;
+    c.lp_fallbacks += k.lp_fallbacks;
+    c.vis_ms += k.vis_ms;
+    c.score_ms += k.score_ms;
+    c.lp_ms += k.lp_ms;
+    ct.sample_ms += ctimes[w].sample_ms;
+    ct.hausdorff_ms += ctimes[w].hausdorff_ms;
+    ct.hull_ms += ctimes[w].hull_ms;
+    ct.samples += ctimes[w].samples;
+    ct.calls += ctimes[w].calls;
+  }
   for (int i = 0; i < n; ++i)
     if (!errors[i].empty())
       throw std::runtime_error("process_batch: mesh " + std::to_string(i) + ": " + errors[i]);
