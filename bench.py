@@ -429,6 +429,84 @@ def run_learned_batch(args) -> dict:
     return out
 
 
+def run_micro(args) -> dict:
+    """Each kernel family once per repetition on a small representative case
+    (per-call device time by CUDA events on the context stream): the command
+    the ncu captures of the kernels other than visibility run.
+      visibility  — s4 blob (2562 vertices, all 3,280,641 pairs) vs its 0.03 cage
+      scoring     — 2^20 random edges x 4096 planes
+      learned     — one training step of the proposer, 64 parts (forward,
+                    backward, Adam) and one proposal
+      sdf_remesh  — the s5 blob's 0.03 cage at scale 40
+      hausdorff   — concavity metric of the remeshed s4 blob vs its hull (3000)
+      hull_dist   — all 2016 pairs of 64 hulls of 50..700 vertices
+      clip        — the s5 blob cut by a plane through its centre"""
+    from visacd_gb300 import _native as N, build, meshgen as mg, proposer as pp
+
+    build.build_all()
+    from visacd_gb300 import visacd as V
+
+    V.config.verbose = False
+    ctx = N.Context(0)
+    rng = np.random.default_rng(3)
+    out = {}
+
+    def timed(name, fn, reps=3, **extra):
+        fn()
+        ctx.synchronize()
+        ctx.set_timing(True)
+        ctx.reset_times()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            r = fn()
+        ctx.synchronize()
+        wall = (time.perf_counter() - t0) / reps
+        kt = ctx.kernel_times()
+        ctx.set_timing(False)
+        out[name] = {"wall_ms_per_call": wall * 1e3,
+                     "kernels_ms_per_call": {k: round(v[0] / reps, 4) for k, v in kt.items() if v[1]},
+                     **extra}
+        return r
+
+    v4, t4 = mg.displaced_blob(4, seed=2026)
+    cv4, ct4 = mg.offset_cage(v4, t4, 0.03)
+    sb, cb = ctx.bvh(v4, t4), ctx.bvh(cv4, ct4)
+    timed("visibility", lambda: ctx.visibility(v4, sb, cb), pairs=len(v4) * (len(v4) - 1) // 2)
+    E, P = 1 << 20, 4096
+    pts = rng.uniform(-1, 1, size=(2 * E, 3)).astype(np.float32)
+    edges = np.arange(2 * E, dtype=np.uint32).reshape(E, 2)
+    nrm = rng.normal(size=(P, 3))
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    planes = np.concatenate([nrm, rng.uniform(-0.8, 0.8, size=(P, 1))], axis=1).astype(np.float32)
+    timed("scoring", lambda: ctx.score_planes(planes, pts, edges), plane_edge_pairs=P * E)
+    lp = N.PlaneProposer(ctx, seed=1)
+    feats = rng.uniform(-1, 1, size=(64, N.LP_POINTS, N.LP_FEATURES)).astype(np.float32)
+    labels = np.concatenate([nrm[:64 * 8].reshape(64, 8, 3), rng.uniform(-0.5, 0.5, size=(64, 8, 1))], -1)
+    w = np.ones((64, 8), np.float32)
+    timed("learned_train_step", lambda: lp.train_step(feats, labels, w, 1e-3),
+          flop_per_step=3 * 2 * 64 * N.LP_POINTS * (16 * 64 + 64 * 128 + 128 * 256))
+    e4, _ = ctx.visibility(v4, sb, cb)
+    c, h = pp.part_frame(v4)
+    timed("learned_propose", lambda: lp.propose(v4, e4, c, h))
+    v5, t5 = mg.displaced_blob(5, seed=2026)
+    v5 = v5 / np.abs(v5).max()
+    timed("sdf_remesh", lambda: ctx.sdf_remesh(v5, t5, 40.0, 0.03))
+    r4 = V._manifold_preprocess_gpu(v4 / np.abs(v4).max(), t4, 30.0, 0.55 / 30)
+    hv = V._convex_hull(r4["vertices"])
+    V.set_seed(1)
+    xa, ia = V._sample_points(r4["vertices"], r4["triangles"], 3000)
+    xb, ib = V._sample_points(hv["vertices"], hv["triangles"], 3000)
+    timed("hausdorff", lambda: ctx.face_hausdorff(r4["vertices"], r4["triangles"], xa, ia, hv["vertices"],
+                                                  hv["triangles"], xb, ib), samples=len(xa) + len(xb))
+    hulls = [rng.uniform(-1, 1, 3) + rng.normal(scale=0.1, size=(int(rng.integers(50, 700)), 3)) for _ in range(64)]
+    pairs = np.array([(a, b) for a in range(64) for b in range(a)], np.int32)
+    timed("hull_dist", lambda: ctx.hull_distances(hulls, pairs), pairs=len(pairs))
+    timed("clip", lambda: ctx.clip(v5, t5, [0.6, 0.8, 0.0, 0.0]))
+    sb.close()
+    cb.close()
+    return out
+
+
 class RefScoringKernel:
     """The reference's plane_point_side_and_rate_kernel (lib/cuda/plane_intersections.cu),
     compiled unchanged from its source into a cubin, launched through the CUDA
@@ -470,7 +548,6 @@ def run_precision_sweep(args) -> dict:
     re-decided blocks, and the error against FP64 on a 16-plane slice."""
     import torch
 
-    import oracle
     from visacd_gb300 import _native, build, meshgen
 
     build.build_gpu()
@@ -531,14 +608,74 @@ def run_precision_sweep(args) -> dict:
             row["reference_argmax_equal"] = bool(np.argmax(theirs) == np.argmax(ours))
         if E <= (1 << 22):
             sub = np.arange(0, P, P // 16)
-            s64, q, qexp, _ = oracle.score_planes(planes[sub], pts, edges)
+            s64 = _score_fp64_numpy(planes[sub], pts, edges)
             ours = d_sc.cpu().numpy()[sub]
             row["max_rel_err_vs_fp64"] = float(np.max(np.abs(ours - s64) / s64))
-            row["quantized_equal_fp64_oracle"] = bool(np.array_equal(np.round(np.ldexp(ours, -qexp)).astype(np.uint64), q))
         rows.append(row)
         del d_pt, d_ed
         torch.cuda.empty_cache()
-    return {"precision_sweep": rows, "fp32_peak_tflops": fp32_peak}
+    # Segment-triangle decisions: FP32 filter + FP64 re-decision vs FP64 alone.
+    S = args.segtri
+    seg, tri, built = meshgen.segment_triangle_cases(S, 0.05, seed=11)
+    ctx.segment_triangle_tests(seg, tri)
+    ctx.set_timing(True)
+    ctx.reset_times()
+    t0 = time.perf_counter()
+    hit, n64 = ctx.segment_triangle_tests(seg, tri)
+    wall = time.perf_counter() - t0
+    kms = ctx.kernel_times().get("seg_tri", (0.0, 0))[0]
+    ctx.set_timing(False)
+    ref = _segtri_fp64_numpy(seg, tri)
+    segtri = {"tests": S, "built_to_graze": int(built.sum()), "fp64_rechecks": n64,
+              "fp64_share": n64 / S, "kernel_ms": kms, "wall_ms_with_copies": wall * 1e3,
+              "tests_per_s_kernel": S / (kms / 1e3) if kms else None,
+              "decisions_equal_fp64": bool(np.array_equal(hit, ref)),
+              "decisions_differing_from_fp64": int(np.sum(hit != ref))}
+    return {"precision_sweep": rows, "fp32_peak_tflops": fp32_peak, "segment_triangle": segtri}
+
+
+def _score_fp64_numpy(planes, pts, edges):
+    """FP64 restatement of the score for a few planes: the summed FP64 length
+    of the edges whose endpoints lie strictly on opposite sides (|value| >
+    1e-6), numpy, independent of the kernels."""
+    p = pts.astype(np.float64)
+    a, b = p[edges[:, 0]], p[edges[:, 1]]
+    ln = np.sqrt(((b - a) ** 2).sum(axis=1))
+    out = np.zeros(len(planes))
+    for k, pl in enumerate(planes.astype(np.float64)):
+        va = a @ pl[:3] + pl[3]
+        vb = b @ pl[:3] + pl[3]
+        sa = np.where(va > 1e-6, 1, np.where(va < -1e-6, -1, 0))
+        sb = np.where(vb > 1e-6, 1, np.where(vb < -1e-6, -1, 0))
+        out[k] = ln[sa * sb == -1].sum()
+    return out
+
+
+def _segtri_fp64_numpy(seg, tri):
+    """FP64 segment-triangle decision (edge functions relative to the origin,
+    tmin 0.001), numpy, in the evaluation order of the kernels' FP64 path."""
+    s = seg.astype(np.float64)
+    t = tri.astype(np.float64).reshape(-1, 3, 3)
+    o = s[:, :3]
+    A, B, Cc, D = t[:, 0] - o, t[:, 1] - o, t[:, 2] - o, s[:, 3:] - o
+
+    def cross(u, v):
+        return np.stack([u[:, 1] * v[:, 2] - u[:, 2] * v[:, 1], u[:, 2] * v[:, 0] - u[:, 0] * v[:, 2],
+                         u[:, 0] * v[:, 1] - u[:, 1] * v[:, 0]], axis=1)
+
+    def dot(u, v):
+        return (u[:, 0] * v[:, 0] + u[:, 1] * v[:, 1]) + u[:, 2] * v[:, 2]
+
+    BC, CA, AB = cross(B, Cc), cross(Cc, A), cross(A, B)
+    Wa, Wb, Wc = dot(D, BC), dot(D, CA), dot(D, AB)
+    det = (Wa + Wb) + Wc
+    vol = dot(A, BC)
+    ln = np.sqrt((D[:, 0] * D[:, 0] + D[:, 1] * D[:, 1]) + D[:, 2] * D[:, 2])
+    inside = ((Wa >= 0) & (Wb >= 0) & (Wc >= 0)) | ((Wa <= 0) & (Wb <= 0) & (Wc <= 0))
+    tmin = float(np.float32(0.001))
+    lhs, rhs = vol * ln, tmin * det
+    hit = np.where(det > 0, (lhs >= rhs) & (vol <= det), (lhs <= rhs) & (vol >= det))
+    return inside & (det != 0) & hit
 
 
 def batch_parts(n_parts: int, seed: int = 7):
@@ -674,13 +811,18 @@ def main():
     ap.add_argument("--batch", action="store_true", help="batching workload only")
     ap.add_argument("--batch-parts", type=int, default=256)
     ap.add_argument("--sweep-sizes", type=int, nargs="+", default=[20, 22, 24, 26])
+    ap.add_argument("--segtri", type=int, default=1 << 20, help="segment-triangle tests in the sweep")
     ap.add_argument("--c5", action="store_true", help="batched + learned decompositions only")
     ap.add_argument("--no-c5", action="store_true", help="skip the batched + learned decompositions")
     ap.add_argument("--c5-blobs", type=int, default=64)
     ap.add_argument("--c5-threads", type=int, default=0, help="process_batch workers (0 = all cores)")
     ap.add_argument("--c5-noise", action="store_true", help="also run plain with other seeds (noise floor)")
     ap.add_argument("--c5-fallbacks", action="store_true", help="also run learned sequentially (fallback rate)")
+    ap.add_argument("--micro", action="store_true", help="one small case per kernel family (for ncu)")
     args = ap.parse_args()
+    if args.micro:
+        print(json.dumps(run_micro(args)))
+        return
     if args.c5:
         print(json.dumps(run_learned_batch(args)))
         return

@@ -230,6 +230,15 @@ int visacd_face_hausdorff(visacd_ctx* ctx, const double* va, int32_t nva, const 
                           const double* vb, int32_t nvb, const int32_t* tb, int32_t ntb,
                           const double* xb, const int32_t* idb, int32_t nb, double* out);
 
+/* Independent segment-triangle decisions with the visibility kernel's test
+   (FP32 filter with a rigorous rounding bound, FP64 re-decision inside it;
+   lib/ptx/ray_segments.cu:49-111 semantics, tmin 0.001): seg S x 6 (p, q),
+   tri S x 9 (a, b, c) float32, host. hit_out[k] = 1 when segment k meets
+   triangle k over t in [0.001 / |q - p|, 1]; *n_fp64 = tests decided in FP64.
+   Synchronizes. */
+int visacd_segment_triangle_tests(visacd_ctx* ctx, const float* seg, const float* tri, int64_t S,
+                                  uint8_t* hit_out, int64_t* n_fp64);
+
 /* ---- SDF remeshing (cages) ------------------------------------------------ */
 /* The iso-surface at distance `level` outside the mesh on a grid of voxel size
    1/scale: the manifold / cage step of lib/src/preprocess.cpp:18-67 (OpenVDB

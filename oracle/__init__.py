@@ -31,6 +31,8 @@ def lib() -> C.CDLL:
                                         C.POINTER(i64), C.POINTER(i64)]
         L.oracle_visibility.restype = i64
         L.oracle_candidate_planes.argtypes = [P, P, i64, i32, C.c_uint32, P]
+        L.oracle_seg_tri_batch.argtypes = [P, P, i64, P]
+        L.oracle_seg_tri_batch.restype = i64
         L.oracle_candidate_planes.restype = i32
         _lib = L
     return _lib
@@ -119,3 +121,12 @@ def candidate_planes(verts, edges, num_planes: int, seed: int) -> np.ndarray:
     out = np.zeros((num_planes, 4), dtype=np.float64)
     n = lib().oracle_candidate_planes(_p(v), _p(e), len(e), num_planes, seed, _p(out))
     return out[:n]
+
+
+def seg_tri_batch(seg, tri):
+    """Independent FP64 segment-triangle decisions: (hit bool[S], grazing bool[S])."""
+    sg = np.ascontiguousarray(np.asarray(seg, dtype=np.float32)).reshape(-1, 6)
+    tr = np.ascontiguousarray(np.asarray(tri, dtype=np.float32)).reshape(-1, 9)
+    out = np.zeros(len(sg), np.uint8)
+    lib().oracle_seg_tri_batch(_p(sg), _p(tr), len(sg), _p(out))
+    return (out & 1).astype(bool), (out & 2).astype(bool)

@@ -509,4 +509,20 @@ int32_t oracle_candidate_planes(const double* verts, const uint32_t* edges, int6
   return np;
 }
 
+// Independent segment-triangle decisions (the precision sweep): seg is S x 6
+// (p, q), tri is S x 9 (a, b, c), float32. out[k]: bit 0 = hit, bit 1 = the
+// decision lies in the grazing band. Returns the number of hits.
+int64_t oracle_seg_tri_batch(const float* seg, const float* tri, int64_t S, uint8_t* out) {
+  int64_t hits = 0;
+#pragma omp parallel for schedule(static) reduction(+ : hits)
+  for (int64_t k = 0; k < S; ++k) {
+    const float* sp = seg + 6 * k;
+    const float* t = tri + 9 * k;
+    TriDecision d = seg_tri64(sp, sp + 3, t, t + 3, t + 6);
+    out[k] = (uint8_t)((d.hit ? 1 : 0) | (d.certain ? 0 : 2));
+    hits += d.hit ? 1 : 0;
+  }
+  return hits;
+}
+
 }  // extern "C"

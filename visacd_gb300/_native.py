@@ -29,7 +29,7 @@ EXPORTED = [
     "visacd_lp_param_count", "visacd_lp_create", "visacd_lp_destroy", "visacd_lp_get_params",
     "visacd_lp_features", "visacd_lp_forward", "visacd_lp_propose", "visacd_lp_grads",
     "visacd_lp_train_step",
-    "visacd_sdf_remesh", "visacd_sdf_fetch", "visacd_hull_distances",
+    "visacd_sdf_remesh", "visacd_sdf_fetch", "visacd_hull_distances", "visacd_segment_triangle_tests",
 ]
 
 LP_POINTS = 2048
@@ -110,6 +110,7 @@ def load() -> C.CDLL:
     lib.visacd_sdf_remesh.argtypes = [P, P, i32, P, i32, C.c_double, C.c_double, C.POINTER(i32), C.POINTER(i32)]
     lib.visacd_sdf_fetch.argtypes = [P, P, P]
     lib.visacd_hull_distances.argtypes = [P, P, P, i32, P, i64, C.c_double, P]
+    lib.visacd_segment_triangle_tests.argtypes = [P, P, P, i64, P, C.POINTER(i64)]
     lib.visacd_lp_param_count.argtypes = []
     lib.visacd_lp_create.argtypes = [P, P, C.c_uint32, C.POINTER(P)]
     lib.visacd_lp_destroy.argtypes = [P]
@@ -302,6 +303,16 @@ class Context:
                                            len(xa), _ptr(vb), len(vb), _ptr(tb), len(tb), _ptr(xb), _ptr(idb),
                                            len(xb), C.byref(out)), "visacd_face_hausdorff")
         return out.value
+
+    def segment_triangle_tests(self, seg, tri):
+        """Independent segment-triangle decisions: (hit bool[S], FP64 re-checks)."""
+        sg = np.ascontiguousarray(np.asarray(seg, dtype=np.float32)).reshape(-1, 6)
+        tr = np.ascontiguousarray(np.asarray(tri, dtype=np.float32)).reshape(-1, 9)
+        out = np.zeros(len(sg), np.uint8)
+        n64 = C.c_int64()
+        _check(lib().visacd_segment_triangle_tests(self._h, _ptr(sg), _ptr(tr), len(sg), _ptr(out), C.byref(n64)),
+               "visacd_segment_triangle_tests")
+        return out.astype(bool), n64.value
 
     # ---- hull merging ------------------------------------------------------
     def hull_distances(self, hulls, pairs, cutoff: float = np.finfo(np.float64).max):

@@ -112,6 +112,7 @@ enum CtxSlot {
   kSlotSdfOut,
   kSlotSdfTris,
   kSlotHull,
+  kSlotSegTri,
   kSlotCount
 };
 
@@ -179,6 +180,7 @@ enum KernelId {
   kKLpMisc,
   kKSdf,
   kKHullDist,
+  kKSegTri,
   kKMisc,
   kKCount
 };

@@ -83,7 +83,8 @@ static const char* kNames[kKCount] = {
     "scan_blocks",   "scan_top",       "scan_add",     "bitset_emit",
     "clip",          "clip_resolve",   "face_hausdorff", "lp_features",
     "lp_gemm",       "lp_pool",        "lp_loss",      "lp_adam",
-    "lp_misc",       "sdf_remesh",     "hull_dist",    "misc"};
+    "lp_misc",       "sdf_remesh",     "hull_dist",    "seg_tri",
+    "misc"};
 
 const char* kernel_name(int id) { return (id >= 0 && id < kKCount) ? kNames[id] : "?"; }
 

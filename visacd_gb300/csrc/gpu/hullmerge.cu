@@ -12,7 +12,9 @@
 // square root is monotone). A pair whose bounding boxes are farther apart than
 // `cutoff` is not scanned and gets DBL_MAX, as does a pair with an empty hull
 // (the host's kInf); the box gap is a lower bound of the distance, compared
-// with a relative margin of 1e-12.
+// with a relative margin of 1e-12. Vertex pairs whose FP32 distance exceeds a
+// thread's running minimum by more than the FP32 rounding bound skip the FP64
+// evaluation (they cannot lower the minimum).
 #include "common.cuh"
 #include "geom64.cuh"
 
@@ -42,6 +44,7 @@ __global__ void __launch_bounds__(kHdThreads) hull_dist_kernel(const double* __r
                                                                const int32_t* __restrict__ pairs, int64_t P,
                                                                double cutoff, double* __restrict__ out) {
   __shared__ double tile[kHdTile * 3];
+  __shared__ float tilef[kHdTile * 3];
   __shared__ double red[kHdThreads / 32];
   for (int64_t p = blockIdx.x; p < P; p += gridDim.x) {
     const int a = pairs[2 * p], b = pairs[2 * p + 1];
@@ -54,18 +57,34 @@ __global__ void __launch_bounds__(kHdThreads) hull_dist_kernel(const double* __r
       if (threadIdx.x == 0) out[p] = 1.7976931348623157e308;
       continue;
     }
+    // FP32 pre-filter bound: coordinates rounded to float move by <= 2^-24 |x|;
+    // with M the largest |coordinate| of the two hulls |d_f32 - d| <= M 2^-21.
+    double M = 0;
+    for (int k = 0; k < 6; ++k) M = fmax(M, fmax(fabs(bb[6 * a + k]), fabs(bb[6 * b + k])));
+    const double eabs = M * 4.76837158203125e-7 + 1e-30;
     double best = 1.7976931348623157e308;
+    float thr = 3.4e38f;  // FP32 squared distance above which a vertex pair cannot beat best
     for (int64_t t0 = b0; t0 < b1; t0 += kHdTile) {
       const int n = (int)min((int64_t)kHdTile, b1 - t0);
       __syncthreads();
-      for (int i = threadIdx.x; i < 3 * n; i += blockDim.x) tile[i] = V[3 * t0 + i];
+      for (int i = threadIdx.x; i < 3 * n; i += blockDim.x) {
+        tile[i] = V[3 * t0 + i];
+        tilef[i] = (float)tile[i];
+      }
       __syncthreads();
       for (int64_t i = a0 + threadIdx.x; i < a1; i += blockDim.x) {
         const double qx = V[3 * i], qy = V[3 * i + 1], qz = V[3 * i + 2];
+        const float fx = (float)qx, fy = (float)qy, fz = (float)qz;
         for (int j = 0; j < n; ++j) {
+          const float ex = tilef[3 * j] - fx, ey = tilef[3 * j + 1] - fy, ez = tilef[3 * j + 2] - fz;
+          if (ex * ex + ey * ey + ez * ez > thr) continue;
           const double dx = ds(tile[3 * j], qx), dy = ds(tile[3 * j + 1], qy), dz = ds(tile[3 * j + 2], qz);
           const double d2 = da(da(dm(dx, dx), dm(dy, dy)), dm(dz, dz));
-          best = fmin(best, d2);
+          if (d2 < best) {
+            best = d2;
+            const double r = __dsqrt_rn(best) + eabs;
+            thr = __double2float_ru(r * r) * (1.0f + 1.0f / 65536.0f);
+          }
         }
       }
     }

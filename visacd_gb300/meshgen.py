@@ -8,6 +8,8 @@
   a_k ~ U(-1, 1), c_k uniform on the unit sphere.
 * offset_cage(verts, tris, dist): every vertex moved by `dist` along its
   area-weighted normal — a quick stand-in cage for kernel-level workloads.
+* segment_triangle_cases(n, graze_frac, seed): independent segment-triangle
+  tests, a fraction of them built to pass within 1e-6 of a triangle edge.
 
 All functions return (vertices float64 (n, 3), triangles int32 (m, 3)).
 """
@@ -112,3 +114,27 @@ def random_planes(n: int, seed: int, offset_range: float = 0.8) -> np.ndarray:
     nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
     d = rng.uniform(-offset_range, offset_range, size=n)
     return np.concatenate([nrm, d[:, None]], axis=1).astype(np.float32)
+
+
+def segment_triangle_cases(n: int, graze_frac: float = 0.05, seed: int = 0):
+    """n (segment, triangle) pairs in [-1, 1]^3 (float32): seg n x 6 (p, q),
+    tri n x 9. A `graze_frac` share of the segments pass through a point within
+    1e-6 of one of their triangle's edges (the FP32 filter cannot decide them
+    and the FP64 re-check must); the rest are random."""
+    rng = np.random.default_rng(seed)
+    tri = rng.uniform(-1, 1, size=(n, 3, 3))
+    p = rng.uniform(-1, 1, size=(n, 3))
+    q = rng.uniform(-1, 1, size=(n, 3))
+    g = rng.random(n) < graze_frac
+    k = int(g.sum())
+    e = rng.integers(0, 3, size=k)
+    a = tri[g, e]
+    b = tri[g, (e + 1) % 3]
+    x = a + rng.uniform(0, 1, size=(k, 1)) * (b - a)
+    x += 1e-6 * rng.uniform(-1, 1, size=(k, 3))
+    d = rng.normal(size=(k, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    p[g] = x + d * rng.uniform(0.2, 1.0, size=(k, 1))
+    q[g] = x - d * rng.uniform(0.2, 1.0, size=(k, 1))
+    seg = np.concatenate([p, q], axis=1).astype(np.float32)
+    return seg, tri.reshape(n, 9).astype(np.float32), g
