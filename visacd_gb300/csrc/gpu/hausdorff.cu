@@ -175,11 +175,43 @@ __device__ __forceinline__ void knn_rings(const HGrid& G, const double (&q)[3], 
 // cell order, so a warp searches one neighbourhood) against the other
 // surface (grid G over its samples, sample triangle ids, mesh verts/tris).
 // The result, a maximum, does not depend on the order.
+// Per triangle of a mesh, FP32 bounds for the distance pre-filter: box lo
+// (rounded down), box hi (rounded up), unit normal + offset (w = 0 and a zero
+// normal for degenerate triangles).
+__global__ void htri_bounds_kernel(const double* __restrict__ mv, const int* __restrict__ mt, int nt,
+                                   float4* __restrict__ out) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += gridDim.x * blockDim.x) {
+    const double* a = mv + 3 * (int64_t)mt[3 * (int64_t)t];
+    const double* b = mv + 3 * (int64_t)mt[3 * (int64_t)t + 1];
+    const double* c = mv + 3 * (int64_t)mt[3 * (int64_t)t + 2];
+    float lo[3], hi[3];
+    for (int k = 0; k < 3; ++k) {
+      lo[k] = __double2float_rd(fmin(fmin(a[k], b[k]), c[k]));
+      hi[k] = __double2float_ru(fmax(fmax(a[k], b[k]), c[k]));
+    }
+    const double ux = b[0] - a[0], uy = b[1] - a[1], uz = b[2] - a[2];
+    const double vx = c[0] - a[0], vy = c[1] - a[1], vz = c[2] - a[2];
+    double nx = uy * vz - uz * vy, ny = uz * vx - ux * vz, nz = ux * vy - uy * vx;
+    const double nl = sqrt(nx * nx + ny * ny + nz * nz);
+    float4 pl = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (nl > 1e-30) {
+      nx /= nl;
+      ny /= nl;
+      nz /= nl;
+      pl = make_float4((float)nx, (float)ny, (float)nz, (float)-(nx * a[0] + ny * a[1] + nz * a[2]));
+    }
+    out[3 * (int64_t)t] = make_float4(lo[0], lo[1], lo[2], 0.f);
+    out[3 * (int64_t)t + 1] = make_float4(hi[0], hi[1], hi[2], 0.f);
+    out[3 * (int64_t)t + 2] = pl;
+  }
+}
+
 __global__ void __launch_bounds__(128) hquery_kernel(const double* __restrict__ Q, int nq,
                                                      const int* __restrict__ qorder, HGrid G,
                                                      const int* __restrict__ ids,
                                                      const double* __restrict__ mv,
                                                      const int* __restrict__ mt,
+                                                     const float4* __restrict__ tb, float tmargin,
                                                      unsigned long long* __restrict__ out_max) {
   double local = 0.0;
   for (int qk = blockIdx.x * blockDim.x + threadIdx.x; qk < nq; qk += gridDim.x * blockDim.x) {
@@ -189,9 +221,27 @@ __global__ void __launch_bounds__(128) hquery_kernel(const double* __restrict__ 
     int bi[kKnn];
     int cnt = 0;
     knn_rings(G, q, bd, bi, cnt);
+    // Smallest distance to the triangles of the k nearest samples, in their
+    // order, stopping below 1e-14. A triangle already seen, or whose FP32
+    // lower bound (box gap or plane distance, minus the rounding margin) is not
+    // below the current minimum, cannot lower it and is not evaluated.
     double cmin = DBL_MAX;
+    int seen[kKnn];
+    const float qfx = (float)q[0], qfy = (float)q[1], qfz = (float)q[2];
     for (int j = 0; j < cnt; ++j) {
       const int tri = ids[bi[j]];
+      bool dup = false;
+      for (int u = 0; u < j; ++u) dup |= seen[u] == tri;
+      seen[j] = tri;
+      if (dup) continue;
+      if (cmin < DBL_MAX) {
+        const float4 lo = tb[3 * (int64_t)tri], hi = tb[3 * (int64_t)tri + 1], pl = tb[3 * (int64_t)tri + 2];
+        const float gx = fmaxf(fmaxf(lo.x - qfx, qfx - hi.x), 0.f);
+        const float gy = fmaxf(fmaxf(lo.y - qfy, qfy - hi.y), 0.f);
+        const float gz = fmaxf(fmaxf(lo.z - qfz, qfz - hi.z), 0.f);
+        const float lb = fmaxf(sqrtf(gx * gx + gy * gy + gz * gz), fabsf(pl.x * qfx + pl.y * qfy + pl.z * qfz + pl.w));
+        if ((double)(lb - tmargin) >= cmin) continue;
+      }
       const int* t = mt + 3 * (int64_t)tri;
       const double d = point_tri_dist(q, mv + 3 * (int64_t)t[0], mv + 3 * (int64_t)t[1], mv + 3 * (int64_t)t[2]);
       if (d < cmin) {
@@ -262,7 +312,8 @@ extern "C" int visacd_face_hausdorff(visacd_ctx* ctx, const double* va, int32_t 
   auto carve = [&](size_t b) { size_t o = off; off += al(b); return o; };
   const size_t o_va = carve((size_t)nva * 24), o_ta = carve((size_t)nta * 12), o_xa = carve((size_t)na * 24),
                o_ia = carve((size_t)na * 4), o_vb = carve((size_t)nvb * 24), o_tb = carve((size_t)ntb * 12),
-               o_xb = carve((size_t)nb * 24), o_ib = carve((size_t)nb * 4), o_mx = carve(64);
+               o_xb = carve((size_t)nb * 24), o_ib = carve((size_t)nb * 4), o_mx = carve(64),
+               o_tba = carve((size_t)nta * 48), o_tbb = carve((size_t)ntb * 48);
   // Per grid: counts + fill (zeroed together), offsets, starts, order, cell of point, sorted float points.
   size_t zero_begin = off;
   size_t o_cnt[2], o_fill[2];
@@ -314,14 +365,22 @@ extern "C" int visacd_face_hausdorff(visacd_ctx* ctx, const double* va, int32_t 
     g[k].spts = (const float4*)(B + o_spts[k]);
   }
   unsigned long long* mx = (unsigned long long*)(B + o_mx);
+  VLAUNCH(ctx, kKHausdorff, grid_for(nta, 256, 8LL * ctx->sm_count), 256, 0, htri_bounds_kernel,
+          (const double*)(B + o_va), (const int*)(B + o_ta), nta, (float4*)(B + o_tba));
+  VLAUNCH(ctx, kKHausdorff, grid_for(ntb, 256, 8LL * ctx->sm_count), 256, 0, htri_bounds_kernel,
+          (const double*)(B + o_vb), (const int*)(B + o_tb), ntb, (float4*)(B + o_tbb));
+  // Margin of the FP32 lower bounds: the plane evaluation's rounding (normal
+  // and offset rounded to float, a few ulps of the largest coordinate), with
+  // room to spare; the box gap is conservative by construction.
+  const float tmargin = (float)(1e-9 + 256.0 * std::ldexp(1.0, -24) * (M + 4.0));
   // Queries of B (in B's cell order) against A's samples/triangles, then A
   // (in A's order) against B.
   VLAUNCH(ctx, kKHausdorff, grid_for(nb, 128, 8LL * ctx->sm_count), 128, 0, hquery_kernel,
           (const double*)(B + o_xb), nb, g[1].order, g[0], (const int*)(B + o_ia),
-          (const double*)(B + o_va), (const int*)(B + o_ta), mx);
+          (const double*)(B + o_va), (const int*)(B + o_ta), (const float4*)(B + o_tba), tmargin, mx);
   VLAUNCH(ctx, kKHausdorff, grid_for(na, 128, 8LL * ctx->sm_count), 128, 0, hquery_kernel,
           (const double*)(B + o_xa), na, g[0].order, g[1], (const int*)(B + o_ib),
-          (const double*)(B + o_vb), (const int*)(B + o_tb), mx);
+          (const double*)(B + o_vb), (const int*)(B + o_tb), (const float4*)(B + o_tbb), tmargin, mx);
   unsigned long long* h = nullptr;
   VTRY(pinned(ctx, 8, (void**)&h));
   VCUDA(cudaMemcpyAsync(h, mx, 8, cudaMemcpyDeviceToHost, st));

@@ -29,6 +29,7 @@ struct SdfGrid {
   double band;
   float fiso;
   double scale;
+  float margin;  // FP32 lower-bound margin (voxels): 1e-3 + 1e-6 max |grid coordinate|
 };
 
 __device__ __forceinline__ size_t vid(const SdfGrid& g, int i, int j, int k) {
@@ -48,25 +49,60 @@ __device__ __forceinline__ void load_tri(const double* __restrict__ P, const int
 __device__ __forceinline__ double min3(double a, double b, double c) { return fmin(fmin(a, b), c); }
 __device__ __forceinline__ double max3(double a, double b, double c) { return fmax(fmax(a, b), c); }
 
+// Lower-bound pre-filter of the exact distance: a voxel whose distance to the
+// triangle's bounding box or plane (FP32, minus a margin of 1e-3 voxel plus
+// 1e-6 of the largest grid coordinate, which covers the FP32 rounding of the
+// plane evaluation) is not below the
+// voxel's current minimum cannot lower it — the exact FP64 distance is at
+// least as large, and rounding to float is monotone — so its FP64 evaluation
+// is skipped. The stored result is the same minimum as without the filter.
 __global__ void __launch_bounds__(128) sdf_dist_kernel(const double* __restrict__ P, const int32_t* __restrict__ T,
                                                        int nt, SdfGrid g, uint32_t* __restrict__ dist) {
   for (int t = blockIdx.x; t < nt; t += gridDim.x) {
     double A[3], B[3], C[3];
     load_tri(P, T, t, A, B, C);
     int lo[3], ext[3];
+    float blo[3], bhi[3];
     for (int a = 0; a < 3; ++a) {
       const double mn = min3(A[a], B[a], C[a]), mx = max3(A[a], B[a], C[a]);
       lo[a] = max(0, (int)floor(mn - g.band) - g.org[a]);
       const int hi = min(g.dim[a] - 1, (int)ceil(mx + g.band) - g.org[a]);
       ext[a] = hi - lo[a] + 1;
+      blo[a] = __double2float_rd(mn);
+      bhi[a] = __double2float_ru(mx);
     }
     if (ext[0] <= 0 || ext[1] <= 0 || ext[2] <= 0) continue;
+    // unit normal and plane offset (FP32 copies; degenerate triangles get none)
+    const double ux = B[0] - A[0], uy = B[1] - A[1], uz = B[2] - A[2];
+    const double vx = C[0] - A[0], vy = C[1] - A[1], vz = C[2] - A[2];
+    double nx = uy * vz - uz * vy, ny = uz * vx - ux * vz, nz = ux * vy - uy * vx;
+    const double nl = sqrt(nx * nx + ny * ny + nz * nz);
+    const bool has_plane = nl > 1e-12;
+    float fnx = 0.f, fny = 0.f, fnz = 0.f, foff = 0.f;
+    if (has_plane) {
+      nx /= nl;
+      ny /= nl;
+      nz /= nl;
+      fnx = (float)nx;
+      fny = (float)ny;
+      fnz = (float)nz;
+      foff = (float)-(nx * A[0] + ny * A[1] + nz * A[2]);
+    }
     const int n = ext[0] * ext[1] * ext[2];
     for (int r = threadIdx.x; r < n; r += blockDim.x) {
       const int i = lo[0] + r % ext[0], j = lo[1] + (r / ext[0]) % ext[1], k = lo[2] + r / (ext[0] * ext[1]);
+      const size_t v = vid(g, i, j, k);
+      const float qx = (float)(g.org[0] + i), qy = (float)(g.org[1] + j), qz = (float)(g.org[2] + k);
+      const float gx = fmaxf(fmaxf(blo[0] - qx, qx - bhi[0]), 0.f);
+      const float gy = fmaxf(fmaxf(blo[1] - qy, qy - bhi[1]), 0.f);
+      const float gz = fmaxf(fmaxf(blo[2] - qz, qz - bhi[2]), 0.f);
+      float lb = sqrtf(gx * gx + gy * gy + gz * gz);
+      if (has_plane) lb = fmaxf(lb, fabsf(fnx * qx + fny * qy + fnz * qz + foff));
+      const float cur = __uint_as_float(*(volatile const uint32_t*)&dist[v]);
+      if (lb - g.margin >= cur) continue;
       const double q[3] = {(double)(g.org[0] + i), (double)(g.org[1] + j), (double)(g.org[2] + k)};
       const float d = __double2float_rn(point_tri_dist(q, A, B, C));
-      atomicMin(&dist[vid(g, i, j, k)], __float_as_uint(d));
+      atomicMin(&dist[v], __float_as_uint(d));
     }
   }
 }
@@ -285,6 +321,10 @@ extern "C" int visacd_sdf_remesh(visacd_ctx* ctx, const double* verts, int32_t n
     g.dim[a] = (int)std::ceil(hi[a] + g.band + 2.0) - g.org[a] + 1;
   }
   VCHECK(g.dim[0] >= 3 && g.dim[1] >= 3 && g.dim[2] >= 3, VISACD_ERR_INVALID_ARG, "sdf_remesh: degenerate grid");
+  double qmax = 0;
+  for (int a = 0; a < 3; ++a)
+    qmax = std::max(qmax, std::max(std::fabs((double)g.org[a]), std::fabs((double)g.org[a] + g.dim[a])));
+  g.margin = (float)(1e-3 + 1e-6 * qmax);
   const size_t nvox = (size_t)g.dim[0] * g.dim[1] * g.dim[2];
   VCHECK(nvox <= ((size_t)1 << 30), VISACD_ERR_CAPACITY, "sdf_remesh: grid of %zu voxels is too large", nvox);
   const size_t ncell = (size_t)(g.dim[0] - 1) * (g.dim[1] - 1) * (g.dim[2] - 1);
