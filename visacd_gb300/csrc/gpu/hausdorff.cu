@@ -155,9 +155,9 @@ __device__ __forceinline__ void knn_rings(const HGrid& G, const double (&q)[3], 
                 bd[j] = d2;
                 bi[j] = pi;
                 if (cnt == kKnn) {
-                  // (sqrt(kth) + eabs)^2, rounded up generously for the FP32 compare
-                  const double b = __dsqrt_rn(bd[kKnn - 1]) + (double)G.eabs;
-                  thr = __double2float_ru(b * b) * (1.0f + 1.0f / 65536.0f);
+                  // (sqrt(kth) + eabs)^2 with every FP32 step rounded upwards
+                  const float b = __fadd_ru(__fsqrt_ru(__double2float_ru(bd[kKnn - 1])), G.eabs);
+                  thr = __fmul_ru(__fmul_ru(b, b), 1.0f + 1.0f / 65536.0f);
                 }
               }
             }
@@ -169,6 +169,90 @@ __device__ __forceinline__ void knn_rings(const HGrid& G, const double (&q)[3], 
     const double rad = (double)r * G.h;
     if (cnt == kKnn && bd[kKnn - 1] <= rad * rad) return;
   }
+}
+
+// FP32 ranking variant of knn_rings: candidates are ranked by their FP32
+// squared distance (kKnnF best kept), the rings stop once the 10th FP32
+// distance plus the rounding bound lies inside the ring radius, and the exact
+// 10 nearest are then chosen by FP64 among the kKnnF. Returns false when the
+// FP32 list cannot prove it holds the exact 10 nearest (the 10th and the
+// kKnnF-th FP32 distances closer than twice the bound), in which case the
+// caller runs the exact FP64 walk.
+constexpr int kKnnF = 16;
+__device__ __forceinline__ bool knn_rings_f32(const HGrid& G, const double (&q)[3], double (&bd)[kKnn],
+                                              int (&bi)[kKnn], int& cnt) {
+  const int cx = cell_coord(q[0], G.lo[0], G.h, G.dim[0]);
+  const int cy = cell_coord(q[1], G.lo[1], G.h, G.dim[1]);
+  const int cz = cell_coord(q[2], G.lo[2], G.h, G.dim[2]);
+  const int rmax = max(G.dim[0], max(G.dim[1], G.dim[2]));
+  const float qf[3] = {(float)q[0], (float)q[1], (float)q[2]};
+  const float hf = (float)G.h;
+  float fd[kKnnF];
+  int fi[kKnnF];
+  int nf = 0;
+  for (int r = 0; r <= rmax; ++r) {
+    for (int dz = -r; dz <= r; ++dz) {
+      const int z = cz + dz;
+      if (z < 0 || z >= G.dim[2]) continue;
+      for (int dy = -r; dy <= r; ++dy) {
+        const int y = cy + dy;
+        if (y < 0 || y >= G.dim[1]) continue;
+        const bool face = abs(dz) == r || abs(dy) == r;
+        for (int dx = -r; dx <= r; dx += (face ? 1 : 2 * r > 0 ? 2 * r : 1)) {
+          const int x = cx + dx;
+          if (x >= 0 && x < G.dim[0]) {
+            const int c = (z * G.dim[1] + y) * G.dim[0] + x;
+            for (int k = G.start[c]; k < G.start[c + 1]; ++k) {
+              const float4 sp = G.spts[k];
+              const float ex = sp.x - qf[0], ey = sp.y - qf[1], ez = sp.z - qf[2];
+              const float d2 = ex * ex + ey * ey + ez * ez;
+              if (nf < kKnnF || d2 < fd[nf - 1]) {
+                int j = nf < kKnnF ? nf++ : kKnnF - 1;
+                while (j > 0 && fd[j - 1] > d2) {
+                  fd[j] = fd[j - 1];
+                  fi[j] = fi[j - 1];
+                  --j;
+                }
+                fd[j] = d2;
+                fi[j] = __float_as_int(sp.w);
+              }
+            }
+          }
+          if (dx == r) break;
+        }
+      }
+    }
+    // Settled: 10 candidates whose exact distance is at most
+    // sqrt(fd[9]) (1 + 2^-20) + eabs lie within the radius r h (less a
+    // 1e-6 h allowance for the query's cell), so nothing unvisited is nearer.
+    if (nf >= kKnn && __fadd_ru(__fmul_ru(__fsqrt_ru(fd[kKnn - 1]), 1.0f + 1.0f / 1048576.0f), G.eabs) <=
+                          __fmul_rd((float)r, hf) * (1.0f - 1e-6f))
+      break;
+  }
+  // The exact 10 nearest are among the kept ones when the kKnnF-th FP32
+  // distance exceeds the 10th by more than twice the bound (or all were kept).
+  if (nf == kKnnF &&
+      !(__fsqrt_rd(fd[kKnnF - 1]) * (1.0f - 1.0f / 1048576.0f) >
+        __fadd_ru(__fadd_ru(__fmul_ru(__fsqrt_ru(fd[kKnn - 1]), 1.0f + 1.0f / 1048576.0f), G.eabs), G.eabs)))
+    return false;
+  cnt = 0;
+  for (int m = 0; m < nf; ++m) {
+    const int pi = fi[m];
+    const double* pp = G.pts + 3 * (int64_t)pi;
+    const double ex = ds(pp[0], q[0]), ey = ds(pp[1], q[1]), ez = ds(pp[2], q[2]);
+    const double d2 = da(da(dm(ex, ex), dm(ey, ey)), dm(ez, ez));
+    if (cnt < kKnn || d2 < bd[cnt - 1]) {
+      int j = cnt < kKnn ? cnt++ : kKnn - 1;
+      while (j > 0 && bd[j - 1] > d2) {
+        bd[j] = bd[j - 1];
+        bi[j] = bi[j - 1];
+        --j;
+      }
+      bd[j] = d2;
+      bi[j] = pi;
+    }
+  }
+  return true;
 }
 
 // One direction: queries Q (visited in the order qorder, their own grid's
@@ -220,7 +304,10 @@ __global__ void __launch_bounds__(128) hquery_kernel(const double* __restrict__ 
     double bd[kKnn];
     int bi[kKnn];
     int cnt = 0;
-    knn_rings(G, q, bd, bi, cnt);
+    if (!knn_rings_f32(G, q, bd, bi, cnt)) {
+      cnt = 0;
+      knn_rings(G, q, bd, bi, cnt);
+    }
     // Smallest distance to the triangles of the k nearest samples, in their
     // order, stopping below 1e-14. A triangle already seen, or whose FP32
     // lower bound (box gap or plane distance, minus the rounding margin) is not
