@@ -172,6 +172,9 @@ enum KernelId {
   kKClip,
   kKClipResolve,
   kKHausdorff,
+  kKHausdorffBound,
+  kKHausdorffQuery,
+  kKHausdorffHead,
   kKLpFeatures,
   kKLpGemm,
   kKLpPool,

@@ -81,7 +81,8 @@ static const char* kNames[kKCount] = {
     "radix_scan",    "radix_scatter",  "karras_build", "aabb_fit",
     "node_layout",   "vis_prep",       "visibility",   "bitset_popc",
     "scan_blocks",   "scan_top",       "scan_add",     "bitset_emit",
-    "clip",          "clip_resolve",   "face_hausdorff", "lp_features",
+    "clip",          "clip_resolve",   "face_hausdorff", "hd_bound",
+    "hd_query",      "hd_head",        "lp_features",
     "lp_gemm",       "lp_pool",        "lp_loss",      "lp_adam",
     "lp_misc",       "sdf_remesh",     "hull_dist",    "seg_tri",
     "misc"};

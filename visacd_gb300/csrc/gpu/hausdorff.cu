@@ -255,13 +255,9 @@ __device__ __forceinline__ bool knn_rings_f32(const HGrid& G, const double (&q)[
   return true;
 }
 
-// One direction: queries Q (visited in the order qorder, their own grid's
-// cell order, so a warp searches one neighbourhood) against the other
-// surface (grid G over its samples, sample triangle ids, mesh verts/tris).
-// The result, a maximum, does not depend on the order.
 // Per triangle of a mesh, FP32 bounds for the distance pre-filter: box lo
-// (rounded down), box hi (rounded up), unit normal + offset (w = 0 and a zero
-// normal for degenerate triangles).
+// (rounded down), box hi (rounded up), unit normal + offset (a zero normal for
+// degenerate triangles).
 __global__ void htri_bounds_kernel(const double* __restrict__ mv, const int* __restrict__ mt, int nt,
                                    float4* __restrict__ out) {
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += gridDim.x * blockDim.x) {
@@ -290,53 +286,307 @@ __global__ void htri_bounds_kernel(const double* __restrict__ mv, const int* __r
   }
 }
 
-__global__ void __launch_bounds__(128) hquery_kernel(const double* __restrict__ Q, int nq,
-                                                     const int* __restrict__ qorder, HGrid G,
-                                                     const int* __restrict__ ids,
-                                                     const double* __restrict__ mv,
-                                                     const int* __restrict__ mt,
-                                                     const float4* __restrict__ tb, float tmargin,
+// One direction's data: queries Q against the other surface (grid G over its
+// samples, the triangle each sample was drawn from, that mesh and its FP32
+// triangle bounds).
+struct HSide {
+  const double* Q;
+  int nq;
+  HGrid G;
+  const int* ids;
+  const double* mv;
+  const int* mt;
+  const float4* tb;
+};
+
+// The query's term of the directed distance: the smallest FP64 distance to the
+// triangles of its k nearest samples, in their order, stopping below 1e-14;
+// the nearest-sample distance when that exceeds 10; DBL_MAX without samples.
+// A triangle already seen, or whose FP32 lower bound (box gap or plane
+// distance, minus the rounding margin) is not below the current minimum,
+// cannot lower it and is not evaluated.
+__device__ double query_term(const HSide& S, int qi, float tmargin) {
+  const double q[3] = {S.Q[3 * (int64_t)qi], S.Q[3 * (int64_t)qi + 1], S.Q[3 * (int64_t)qi + 2]};
+  double bd[kKnn];
+  int bi[kKnn];
+  int cnt = 0;
+  if (!knn_rings_f32(S.G, q, bd, bi, cnt)) {
+    cnt = 0;
+    knn_rings(S.G, q, bd, bi, cnt);
+  }
+  double cmin = DBL_MAX;
+  int seen[kKnn];
+  const float qfx = (float)q[0], qfy = (float)q[1], qfz = (float)q[2];
+  for (int j = 0; j < cnt; ++j) {
+    const int tri = S.ids[bi[j]];
+    bool dup = false;
+    for (int u = 0; u < j; ++u) dup |= seen[u] == tri;
+    seen[j] = tri;
+    if (dup) continue;
+    if (cmin < DBL_MAX) {
+      const float4 lo = S.tb[3 * (int64_t)tri], hi = S.tb[3 * (int64_t)tri + 1], pl = S.tb[3 * (int64_t)tri + 2];
+      const float gx = fmaxf(fmaxf(lo.x - qfx, qfx - hi.x), 0.f);
+      const float gy = fmaxf(fmaxf(lo.y - qfy, qfy - hi.y), 0.f);
+      const float gz = fmaxf(fmaxf(lo.z - qfz, qfz - hi.z), 0.f);
+      const float lb = fmaxf(sqrtf(gx * gx + gy * gy + gz * gz), fabsf(pl.x * qfx + pl.y * qfy + pl.z * qfz + pl.w));
+      if ((double)(lb - tmargin) >= cmin) continue;
+    }
+    const int* t = S.mt + 3 * (int64_t)tri;
+    const double d = point_tri_dist(q, S.mv + 3 * (int64_t)t[0], S.mv + 3 * (int64_t)t[1], S.mv + 3 * (int64_t)t[2]);
+    if (d < cmin) {
+      cmin = d;
+      if (cmin < 1e-14) break;
+    }
+  }
+  if (cmin > 10 && cnt > 0) cmin = __dsqrt_rn(bd[0]);
+  return cmin;
+}
+
+// The smallest not-yet-taken value across the warp's sorted per-lane lists
+// (fd[ptr..]), taken: returns it and its id; ties go to the lower lane.
+__device__ __forceinline__ float warp_take_min(const float (&fd)[kKnnF], const int (&fi)[kKnnF], int nf, int& ptr,
+                                               int& id_out) {
+  const int lane = threadIdx.x & 31;
+  const float mine = ptr < nf ? fd[ptr] : 3.4e38f;
+  float m = mine;
+  for (int o = 16; o; o >>= 1) m = fminf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  const unsigned who = __ballot_sync(0xffffffffu, mine == m && ptr < nf);
+  const int src = who ? __ffs(who) - 1 : 0;
+  int id = ptr < nf ? fi[ptr] : -1;
+  id = __shfl_sync(0xffffffffu, id, src);
+  if (who && lane == src) ++ptr;
+  id_out = who ? id : -1;
+  return who ? m : 3.4e38f;
+}
+
+// query_term for one query by a whole warp (used for the few queries with the
+// largest bounds, which are far from the other surface and walk many rings):
+// the lanes split each ring's cells and each keeps its kKnnF smallest FP32
+// distances, so the warp's kKnnF smallest are exact (a candidate a lane drops
+// has kKnnF smaller ones in that lane alone); a warp tournament takes them in
+// order. Same stop rule, same FP32-to-FP64 selection proof and the same term
+// as query_term; returns false (on all lanes) when the proof fails, and the
+// caller then uses query_term.
+__device__ bool query_term_warp(const HSide& S, int qi, double& term) {
+  const int lane = threadIdx.x & 31;
+  const HGrid& G = S.G;
+  const double q[3] = {S.Q[3 * (int64_t)qi], S.Q[3 * (int64_t)qi + 1], S.Q[3 * (int64_t)qi + 2]};
+  const int cx = cell_coord(q[0], G.lo[0], G.h, G.dim[0]);
+  const int cy = cell_coord(q[1], G.lo[1], G.h, G.dim[1]);
+  const int cz = cell_coord(q[2], G.lo[2], G.h, G.dim[2]);
+  const int rmax = max(G.dim[0], max(G.dim[1], G.dim[2]));
+  const float qf[3] = {(float)q[0], (float)q[1], (float)q[2]};
+  const float hf = (float)G.h;
+  float fd[kKnnF];
+  int fi[kKnnF];
+  int nf = 0;
+  int total = 0;  // candidates seen by the warp
+  float g10 = 3.4e38f;
+  for (int r = 0; r <= rmax; ++r) {
+    const int side = 2 * r + 1;
+    const int cube = side * side * side;
+    int seen = 0;
+    for (int t = lane; t < cube; t += 32) {
+      const int dx = t % side - r, dy = (t / side) % side - r, dz = t / (side * side) - r;
+      if (max(abs(dx), max(abs(dy), abs(dz))) != r) continue;
+      const int x = cx + dx, y = cy + dy, z = cz + dz;
+      if (x < 0 || x >= G.dim[0] || y < 0 || y >= G.dim[1] || z < 0 || z >= G.dim[2]) continue;
+      const int c = (z * G.dim[1] + y) * G.dim[0] + x;
+      for (int k = G.start[c]; k < G.start[c + 1]; ++k) {
+        const float4 sp = G.spts[k];
+        const float ex = sp.x - qf[0], ey = sp.y - qf[1], ez = sp.z - qf[2];
+        const float d2 = ex * ex + ey * ey + ez * ez;
+        ++seen;
+        if (nf < kKnnF || d2 < fd[nf - 1]) {
+          int j = nf < kKnnF ? nf++ : kKnnF - 1;
+          while (j > 0 && fd[j - 1] > d2) {
+            fd[j] = fd[j - 1];
+            fi[j] = fi[j - 1];
+            --j;
+          }
+          fd[j] = d2;
+          fi[j] = __float_as_int(sp.w);
+        }
+      }
+    }
+    for (int o = 16; o; o >>= 1) seen += __shfl_xor_sync(0xffffffffu, seen, o);
+    total += seen;
+    if (total >= kKnn) {
+      int ptr = 0, id;
+      float v = 3.4e38f;
+      for (int m = 0; m < kKnn; ++m) v = warp_take_min(fd, fi, nf, ptr, id);
+      g10 = v;
+      if (__fadd_ru(__fmul_ru(__fsqrt_ru(g10), 1.0f + 1.0f / 1048576.0f), G.eabs) <=
+          __fmul_rd((float)r, hf) * (1.0f - 1e-6f))
+        break;
+    }
+  }
+  // The warp's kKnnF smallest (value, id) in order: lane m holds the m-th.
+  float myv = 3.4e38f;
+  int myid = -1;
+  {
+    int ptr = 0;
+    for (int m = 0; m < kKnnF; ++m) {
+      int id;
+      const float v = warp_take_min(fd, fi, nf, ptr, id);
+      if (lane == m) {
+        myv = v;
+        myid = id;
+      }
+    }
+  }
+  // The exact 10 nearest are among these when the kKnnF-th FP32 distance
+  // exceeds the 10th by more than twice the bound (or all were kept).
+  if (total > kKnnF) {
+    const float v16 = __shfl_sync(0xffffffffu, myv, kKnnF - 1);
+    const bool ok = __fsqrt_rd(v16) * (1.0f - 1.0f / 1048576.0f) >
+                    __fadd_ru(__fadd_ru(__fmul_ru(__fsqrt_ru(g10), 1.0f + 1.0f / 1048576.0f), G.eabs), G.eabs);
+    if (!ok) return false;
+  }
+  // Exact FP64 distances of the (up to) kKnnF candidates, the 10 nearest kept
+  // in order (insertion in candidate order, as query_term).
+  double d2 = DBL_MAX;
+  if (myid >= 0) {
+    const double* pp = G.pts + 3 * (int64_t)myid;
+    const double ex = ds(pp[0], q[0]), ey = ds(pp[1], q[1]), ez = ds(pp[2], q[2]);
+    d2 = da(da(dm(ex, ex), dm(ey, ey)), dm(ez, ez));
+  }
+  double bd[kKnn];
+  int bi[kKnn];
+  int cnt = 0;
+  for (int m = 0; m < kKnnF; ++m) {
+    const double v = __shfl_sync(0xffffffffu, d2, m);
+    const int id = __shfl_sync(0xffffffffu, myid, m);
+    if (id < 0) continue;
+    if (cnt < kKnn || v < bd[cnt - 1]) {
+      int j = cnt < kKnn ? cnt++ : kKnn - 1;
+      while (j > 0 && bd[j - 1] > v) {
+        bd[j] = bd[j - 1];
+        bi[j] = bi[j - 1];
+        --j;
+      }
+      bd[j] = v;
+      bi[j] = id;
+    }
+  }
+  // Point-triangle distances of the k nearest in parallel (lane j), then the
+  // sequential minimum with the early stop below 1e-14, in order.
+  double dj = DBL_MAX;
+  int which = -1;
+#pragma unroll
+  for (int j = 0; j < kKnn; ++j)
+    if (j == lane && j < cnt) which = bi[j];
+  if (which >= 0) {
+    const int tj = S.ids[which];
+    const int* t = S.mt + 3 * (int64_t)tj;
+    dj = point_tri_dist(q, S.mv + 3 * (int64_t)t[0], S.mv + 3 * (int64_t)t[1], S.mv + 3 * (int64_t)t[2]);
+  }
+  double cmin = DBL_MAX;
+  for (int j = 0; j < cnt; ++j) {
+    const double d = __shfl_sync(0xffffffffu, dj, j);
+    if (d < cmin) {
+      cmin = d;
+      if (cmin < 1e-14) break;
+    }
+  }
+  if (cmin > 10 && cnt > 0) cmin = __dsqrt_rn(bd[0]);
+  term = cmin;
+  return true;
+}
+
+// Upper bound of every query's term, one thread per query in its own grid's
+// cell order: the distance to the nearest sample within two rings of cells
+// around the query, in FP32 rounded upwards plus the coordinate rounding
+// bound (the term is at most the distance to the nearest sample, itself at
+// most this). A query with no sample that close gets no bound (+inf) and is
+// appended to farlist (*far entries): those are evaluated one warp each.
+// Entry e = base + position holds the bound and the query's id (bit 31:
+// direction).
+constexpr int kBoundRings = 2;
+__global__ void __launch_bounds__(128) hbound_kernel(HSide S, int dir, const int* __restrict__ qorder,
+                                                     float* __restrict__ ubs, uint32_t* __restrict__ vals,
+                                                     int base, unsigned* __restrict__ far,
+                                                     int* __restrict__ farlist) {
+  const HGrid& G = S.G;
+  for (int qk = blockIdx.x * blockDim.x + threadIdx.x; qk < S.nq; qk += gridDim.x * blockDim.x) {
+    const int qi = qorder[qk];
+    const double* qq = S.Q + 3 * (int64_t)qi;
+    const double q[3] = {qq[0], qq[1], qq[2]};
+    const int cx = cell_coord(q[0], G.lo[0], G.h, G.dim[0]);
+    const int cy = cell_coord(q[1], G.lo[1], G.h, G.dim[1]);
+    const int cz = cell_coord(q[2], G.lo[2], G.h, G.dim[2]);
+    const float qf[3] = {(float)q[0], (float)q[1], (float)q[2]};
+    float best = 3.4e38f;
+    for (int r = 0; r <= kBoundRings; ++r) {
+      for (int dz = -r; dz <= r; ++dz) {
+        const int z = cz + dz;
+        if (z < 0 || z >= G.dim[2]) continue;
+        for (int dy = -r; dy <= r; ++dy) {
+          const int y = cy + dy;
+          if (y < 0 || y >= G.dim[1]) continue;
+          const bool face = abs(dz) == r || abs(dy) == r;
+          for (int dx = -r; dx <= r; dx += (face ? 1 : 2 * r > 0 ? 2 * r : 1)) {
+            const int x = cx + dx;
+            if (x >= 0 && x < G.dim[0]) {
+              const int c = (z * G.dim[1] + y) * G.dim[0] + x;
+              for (int k = G.start[c]; k < G.start[c + 1]; ++k) {
+                const float4 sp = G.spts[k];
+                const float ex = sp.x - qf[0], ey = sp.y - qf[1], ez = sp.z - qf[2];
+                best = fminf(best, ex * ex + ey * ey + ez * ez);
+              }
+            }
+            if (dx == r) break;
+          }
+        }
+      }
+      if (r >= 1 && best < 3.4e38f) break;
+    }
+    float ub = __int_as_float(0x7f800000);  // +inf: no bound
+    if (best < 3.4e38f)
+      ub = __fadd_ru(__fmul_ru(__fsqrt_ru(best), 1.0f + 1.0f / 1048576.0f), G.eabs);
+    else
+      farlist[atomicAdd(far, 1u)] = base + qk;
+    ubs[base + qk] = ub;
+    vals[base + qk] = (uint32_t)qi | ((uint32_t)dir << 31);
+  }
+}
+
+// Terms of the queries without a bound (the farlist), one warp each: they are
+// far from the other surface, walk many rings, and their exact terms start
+// the running maximum that prunes the rest.
+__global__ void __launch_bounds__(128) hhead_kernel(HSide A, HSide B, const uint32_t* __restrict__ vals,
+                                                    const int* __restrict__ farlist,
+                                                    const unsigned* __restrict__ far, float tmargin,
+                                                    unsigned long long* __restrict__ out_max) {
+  const int head = (int)*far;
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < head; w += warps) {
+    const uint32_t v = vals[farlist[w]];
+    const int qi = (int)(v & 0x7FFFFFFFu);
+    const HSide& S = (v >> 31) ? B : A;
+    double term;
+    if (!query_term_warp(S, qi, term)) term = query_term(S, qi, tmargin);
+    if ((threadIdx.x & 31) == 0 && term < DBL_MAX)
+      atomicMax(out_max, (unsigned long long)__double_as_longlong(term));
+  }
+}
+
+// Terms of the queries with a bound (both directions, each in its own grid's
+// cell order), maximum into out_max. A query whose bound does not exceed the
+// maximum found so far cannot raise it and is skipped: the result is the same
+// maximum.
+__global__ void __launch_bounds__(128) hquery_kernel(HSide A, HSide B, const float* __restrict__ ubs,
+                                                     const uint32_t* __restrict__ vals, int end, float tmargin,
                                                      unsigned long long* __restrict__ out_max) {
   double local = 0.0;
-  for (int qk = blockIdx.x * blockDim.x + threadIdx.x; qk < nq; qk += gridDim.x * blockDim.x) {
-    const int qi = qorder[qk];
-    const double q[3] = {Q[3 * (int64_t)qi], Q[3 * (int64_t)qi + 1], Q[3 * (int64_t)qi + 2]};
-    double bd[kKnn];
-    int bi[kKnn];
-    int cnt = 0;
-    if (!knn_rings_f32(G, q, bd, bi, cnt)) {
-      cnt = 0;
-      knn_rings(G, q, bd, bi, cnt);
-    }
-    // Smallest distance to the triangles of the k nearest samples, in their
-    // order, stopping below 1e-14. A triangle already seen, or whose FP32
-    // lower bound (box gap or plane distance, minus the rounding margin) is not
-    // below the current minimum, cannot lower it and is not evaluated.
-    double cmin = DBL_MAX;
-    int seen[kKnn];
-    const float qfx = (float)q[0], qfy = (float)q[1], qfz = (float)q[2];
-    for (int j = 0; j < cnt; ++j) {
-      const int tri = ids[bi[j]];
-      bool dup = false;
-      for (int u = 0; u < j; ++u) dup |= seen[u] == tri;
-      seen[j] = tri;
-      if (dup) continue;
-      if (cmin < DBL_MAX) {
-        const float4 lo = tb[3 * (int64_t)tri], hi = tb[3 * (int64_t)tri + 1], pl = tb[3 * (int64_t)tri + 2];
-        const float gx = fmaxf(fmaxf(lo.x - qfx, qfx - hi.x), 0.f);
-        const float gy = fmaxf(fmaxf(lo.y - qfy, qfy - hi.y), 0.f);
-        const float gz = fmaxf(fmaxf(lo.z - qfz, qfz - hi.z), 0.f);
-        const float lb = fmaxf(sqrtf(gx * gx + gy * gy + gz * gz), fabsf(pl.x * qfx + pl.y * qfy + pl.z * qfz + pl.w));
-        if ((double)(lb - tmargin) >= cmin) continue;
-      }
-      const int* t = mt + 3 * (int64_t)tri;
-      const double d = point_tri_dist(q, mv + 3 * (int64_t)t[0], mv + 3 * (int64_t)t[1], mv + 3 * (int64_t)t[2]);
-      if (d < cmin) {
-        cmin = d;
-        if (cmin < 1e-14) break;
-      }
-    }
-    if (cmin > 10 && cnt > 0) cmin = __dsqrt_rn(bd[0]);
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < end; e += gridDim.x * blockDim.x) {
+    const float ub = ubs[e];
+    if (!(ub < __int_as_float(0x7f800000))) continue;  // no bound: evaluated by hhead_kernel
+    const double cur = __longlong_as_double((long long)*(volatile unsigned long long*)out_max);
+    if ((double)ub <= fmax(cur, local)) continue;
+    const uint32_t v = vals[e];
+    const int qi = (int)(v & 0x7FFFFFFFu);
+    const double cmin = (v >> 31) ? query_term(B, qi, tmargin) : query_term(A, qi, tmargin);
     if (cmin > local && DBL_MAX > cmin) local = cmin;
   }
   for (int o = 16; o; o >>= 1) local = fmax(local, __shfl_xor_sync(0xffffffffu, local, o));
@@ -400,7 +650,9 @@ extern "C" int visacd_face_hausdorff(visacd_ctx* ctx, const double* va, int32_t 
   const size_t o_va = carve((size_t)nva * 24), o_ta = carve((size_t)nta * 12), o_xa = carve((size_t)na * 24),
                o_ia = carve((size_t)na * 4), o_vb = carve((size_t)nvb * 24), o_tb = carve((size_t)ntb * 12),
                o_xb = carve((size_t)nb * 24), o_ib = carve((size_t)nb * 4), o_mx = carve(64),
-               o_tba = carve((size_t)nta * 48), o_tbb = carve((size_t)ntb * 48);
+               o_tba = carve((size_t)nta * 48), o_tbb = carve((size_t)ntb * 48),
+               o_keys = carve((size_t)(na + nb) * 4), o_vals = carve((size_t)(na + nb) * 4),
+               o_keys2 = carve((size_t)(na + nb) * 4);
   // Per grid: counts + fill (zeroed together), offsets, starts, order, cell of point, sorted float points.
   size_t zero_begin = off;
   size_t o_cnt[2], o_fill[2];
@@ -460,14 +712,26 @@ extern "C" int visacd_face_hausdorff(visacd_ctx* ctx, const double* va, int32_t 
   // and offset rounded to float, a few ulps of the largest coordinate), with
   // room to spare; the box gap is conservative by construction.
   const float tmargin = (float)(1e-9 + 256.0 * std::ldexp(1.0, -24) * (M + 4.0));
-  // Queries of B (in B's cell order) against A's samples/triangles, then A
-  // (in A's order) against B.
-  VLAUNCH(ctx, kKHausdorff, grid_for(nb, 128, 8LL * ctx->sm_count), 128, 0, hquery_kernel,
-          (const double*)(B + o_xb), nb, g[1].order, g[0], (const int*)(B + o_ia),
-          (const double*)(B + o_va), (const int*)(B + o_ta), (const float4*)(B + o_tba), tmargin, mx);
-  VLAUNCH(ctx, kKHausdorff, grid_for(na, 128, 8LL * ctx->sm_count), 128, 0, hquery_kernel,
-          (const double*)(B + o_xa), na, g[0].order, g[1], (const int*)(B + o_ib),
-          (const double*)(B + o_vb), (const int*)(B + o_tb), (const float4*)(B + o_tbb), tmargin, mx);
+  // Direction 0: queries of B against A's samples / triangles; direction 1:
+  // queries of A against B.
+  HSide sd0{(const double*)(B + o_xb), nb, g[0], (const int*)(B + o_ia), (const double*)(B + o_va),
+            (const int*)(B + o_ta), (const float4*)(B + o_tba)};
+  HSide sd1{(const double*)(B + o_xa), na, g[1], (const int*)(B + o_ib), (const double*)(B + o_vb),
+            (const int*)(B + o_tb), (const float4*)(B + o_tbb)};
+  const int ntot = na + nb;
+  uint32_t* vals = (uint32_t*)(B + o_vals);
+  unsigned* far = (unsigned*)(B + o_mx + 8);  // zeroed with the maximum
+  float* ubs = (float*)(B + o_keys);
+  int* farlist = (int*)(B + o_keys2);
+  VLAUNCH(ctx, kKHausdorffBound, grid_for(nb, 128, 8LL * ctx->sm_count), 128, 0, hbound_kernel, sd0, 0,
+          g[1].order, ubs, vals, 0, far, farlist);
+  VLAUNCH(ctx, kKHausdorffBound, grid_for(na, 128, 8LL * ctx->sm_count), 128, 0, hbound_kernel, sd1, 1,
+          g[0].order, ubs, vals, nb, far, farlist);
+  // The queries without a bound one warp each, then the rest with pruning.
+  VLAUNCH(ctx, kKHausdorffHead, grid_for(32LL * ntot, 128, 8LL * ctx->sm_count), 128, 0, hhead_kernel, sd0, sd1,
+          (const uint32_t*)vals, (const int*)farlist, (const unsigned*)far, tmargin, mx);
+  VLAUNCH(ctx, kKHausdorffQuery, grid_for(ntot, 128, 8LL * ctx->sm_count), 128, 0, hquery_kernel, sd0, sd1,
+          (const float*)ubs, (const uint32_t*)vals, ntot, tmargin, mx);
   unsigned long long* h = nullptr;
   VTRY(pinned(ctx, 8, (void**)&h));
   VCUDA(cudaMemcpyAsync(h, mx, 8, cudaMemcpyDeviceToHost, st));

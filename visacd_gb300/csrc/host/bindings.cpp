@@ -94,6 +94,7 @@ PYBIND11_MODULE(visacd, m) {
       .def_readwrite("plane_proposer", &Config::plane_proposer)
       .def_readwrite("proposer_weights", &Config::proposer_weights)
       .def_readwrite("proposer_probe_planes", &Config::proposer_probe_planes)
+      .def_readwrite("proposer_refine", &Config::proposer_refine)
       .def_readwrite("proposer_tolerance", &Config::proposer_tolerance);
 
   m.def("make_vecarray3i", [](py::array_t<int, py::array::c_style | py::array::forcecast> a) {

@@ -103,6 +103,7 @@ struct Config {
   std::string plane_proposer = "exhaustive";
   std::string proposer_weights;  // float32 parameter file of the proposer
   int proposer_probe_planes = 64;
+  int proposer_refine = 32;  // bisector planes kept per proposal in the refinement
   double proposer_tolerance = 0.01;
 };
 

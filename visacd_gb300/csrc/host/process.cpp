@@ -136,7 +136,7 @@ std::vector<Plane> refine_proposals(const Mesh& mesh, const std::vector<Plane>& 
 bool learned_plane(const Mesh& mesh, const std::vector<Plane>& flat_planes, Plane& out) {
   if (mesh.intersecting_edges.empty()) return false;
   std::vector<Plane> planes = gpu::propose_planes(mesh);
-  std::vector<Plane> refined = refine_proposals(mesh, planes, 8);
+  std::vector<Plane> refined = refine_proposals(mesh, planes, config().proposer_refine);
   planes.insert(planes.end(), refined.begin(), refined.end());
   const size_t n_prop = planes.size();
   std::vector<Plane> probe =
