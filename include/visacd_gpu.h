@@ -100,6 +100,12 @@ int visacd_ctx_kernel_times(visacd_ctx* ctx, const char** names, double* total_m
 int64_t visacd_ctx_launch_count(const visacd_ctx* ctx);
 int visacd_ctx_sm_count(const visacd_ctx* ctx);
 
+/* How host threads wait for this process's work on `device`: blocking = 1
+   makes waiting threads sleep until the GPU finishes (cudaDeviceScheduleBlockingSync)
+   instead of spinning, which frees host cores when many threads drive the GPU
+   (process_batch); 0 restores the default (automatic) policy. Per process. */
+int visacd_set_blocking_sync(int device, int blocking);
+
 /* FP32 FMA throughput of this GPU in TFLOP/s (packed f32x2 FMA loop, best of
    3 timed launches): the denominator of the FP32-bound rooflines. */
 int visacd_measure_fp32_peak(visacd_ctx* ctx, double* tflops);

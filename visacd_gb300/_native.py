@@ -30,6 +30,7 @@ EXPORTED = [
     "visacd_lp_features", "visacd_lp_forward", "visacd_lp_propose", "visacd_lp_grads",
     "visacd_lp_train_step",
     "visacd_sdf_remesh", "visacd_sdf_fetch", "visacd_hull_distances", "visacd_segment_triangle_tests",
+    "visacd_set_blocking_sync",
 ]
 
 LP_POINTS = 2048
@@ -111,6 +112,7 @@ def load() -> C.CDLL:
     lib.visacd_sdf_fetch.argtypes = [P, P, P]
     lib.visacd_hull_distances.argtypes = [P, P, P, i32, P, i64, C.c_double, P]
     lib.visacd_segment_triangle_tests.argtypes = [P, P, P, i64, P, C.POINTER(i64)]
+    lib.visacd_set_blocking_sync.argtypes = [C.c_int, C.c_int]
     lib.visacd_lp_param_count.argtypes = []
     lib.visacd_lp_create.argtypes = [P, P, C.c_uint32, C.POINTER(P)]
     lib.visacd_lp_destroy.argtypes = [P]

@@ -286,10 +286,10 @@ int bvh_build(visacd_ctx* ctx, const float* verts, int32_t nv, const uint32_t* t
   if (!device_ptrs) {
     VTRY(ensure_slot(ctx, kSlotBuildVerts, (size_t)nv * 12));
     VTRY(ensure_slot(ctx, kSlotBuildTris, (size_t)nt * 12));
-    VCUDA(cudaMemcpyAsync(ctx->buf[kSlotBuildVerts].p, verts, (size_t)nv * 12,
-                          cudaMemcpyHostToDevice, ctx->stream));
-    VCUDA(cudaMemcpyAsync(ctx->buf[kSlotBuildTris].p, tris, (size_t)nt * 12,
-                          cudaMemcpyHostToDevice, ctx->stream));
+    Stager up(ctx);
+    VTRY(up.reserve((size_t)nv * 12 + (size_t)nt * 12, 2));
+    VTRY(up.put(ctx->buf[kSlotBuildVerts].p, verts, (size_t)nv * 12));
+    VTRY(up.put(ctx->buf[kSlotBuildTris].p, tris, (size_t)nt * 12));
     dv = slot<float>(ctx, kSlotBuildVerts);
     dt = slot<uint32_t>(ctx, kSlotBuildTris);
   }

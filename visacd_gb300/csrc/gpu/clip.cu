@@ -541,9 +541,11 @@ extern "C" int visacd_clip(visacd_ctx* ctx, const double* verts, int32_t nv, con
   int *outp = (int*)(B + o_outp), *outn = (int*)(B + o_outn), *mapp = (int*)(B + o_mapp),
       *mapn = (int*)(B + o_mapn);
   cudaStream_t st = ctx->stream;
-  VCUDA(cudaMemcpyAsync(dv, verts, (size_t)nv * 24, cudaMemcpyHostToDevice, st));
-  VCUDA(cudaMemcpyAsync(dt, tris, (size_t)nt * 12, cudaMemcpyHostToDevice, st));
-  VCUDA(cudaMemcpyAsync(dpl, plane, 32, cudaMemcpyHostToDevice, st));
+  Stager up(ctx);
+  VTRY(up.reserve((size_t)nv * 24 + (size_t)nt * 12 + 32, 3));
+  VTRY(up.put(dv, verts, (size_t)nv * 24));
+  VTRY(up.put(dt, tris, (size_t)nt * 12));
+  VTRY(up.put(dpl, plane, 32));
   VCUDA(cudaMemsetAsync(kp, 0, nv, st));
   VCUDA(cudaMemsetAsync(kn, 0, nv, st));
   VCUDA(cudaMemsetAsync(cnt, 0, sizeof(ClipCounters), st));

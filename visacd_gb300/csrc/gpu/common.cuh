@@ -125,6 +125,8 @@ struct visacd_ctx {
   uint32_t* d_status = nullptr;      // device status word
   void* h_pinned = nullptr;          // small pinned staging area
   size_t h_pinned_cap = 0;
+  void* h_upload = nullptr;          // pinned upload buffer (Stager)
+  size_t h_upload_cap = 0;
   int64_t launches = 0;
   int64_t last_n_edges = 0;
   bool timing = false;
@@ -202,6 +204,23 @@ int check_status(visacd_ctx* ctx, const char* what);
 
 // Pinned host staging of at least `bytes`.
 int pinned(visacd_ctx* ctx, size_t bytes, void** out);
+
+// Host-to-device uploads of one call through the context's pinned upload
+// buffer: a host memcpy into pinned memory, then an asynchronous DMA from it,
+// so contexts driven by several host threads do not contend on the driver's
+// pageable-copy staging. reserve(total) first waits for the context stream
+// (the previous call's DMAs may still read the buffer) and grows it; put()
+// places each array at the next 64-byte boundary.
+class Stager {
+ public:
+  explicit Stager(visacd_ctx* ctx) : ctx_(ctx) {}
+  int reserve(size_t total_bytes, int arrays);
+  int put(void* dst, const void* src, size_t bytes);
+
+ private:
+  visacd_ctx* ctx_;
+  size_t used_ = 0, cap_ = 0;
+};
 
 template <class T>
 inline T* slot(visacd_ctx* ctx, int s) {

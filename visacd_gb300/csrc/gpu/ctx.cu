@@ -148,6 +148,37 @@ int pinned(visacd_ctx* ctx, size_t bytes, void** out) {
   return VISACD_OK;
 }
 
+int Stager::reserve(size_t total_bytes, int arrays) {
+  const size_t need = total_bytes + 64 * (size_t)(arrays + 1);
+  VCUDA(cudaStreamSynchronize(ctx_->stream));
+  if (need > ctx_->h_upload_cap) {
+    if (ctx_->h_upload) cudaFreeHost(ctx_->h_upload);
+    ctx_->h_upload = nullptr;
+    ctx_->h_upload_cap = 0;
+    const size_t want = need + need / 4;
+    cudaError_t e = cudaMallocHost(&ctx_->h_upload, want);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      set_error("cudaMallocHost(%zu) failed: %s", want, cudaGetErrorString(e));
+      return VISACD_ERR_NO_MEMORY;
+    }
+    ctx_->h_upload_cap = want;
+  }
+  used_ = 0;
+  cap_ = need;
+  return VISACD_OK;
+}
+
+int Stager::put(void* dst, const void* src, size_t bytes) {
+  if (bytes == 0) return VISACD_OK;
+  VCHECK(used_ + bytes <= cap_, VISACD_ERR_INVALID_ARG, "upload larger than reserved");
+  char* h = static_cast<char*>(ctx_->h_upload) + used_;
+  std::memcpy(h, src, bytes);
+  VCUDA(cudaMemcpyAsync(dst, h, bytes, cudaMemcpyHostToDevice, ctx_->stream));
+  used_ += (bytes + 63) & ~size_t(63);
+  return VISACD_OK;
+}
+
 int check_status(visacd_ctx* ctx, const char* what) {
   uint32_t* h = nullptr;
   VTRY(pinned(ctx, 64, (void**)&h));
@@ -434,6 +465,7 @@ extern "C" int visacd_ctx_destroy(visacd_ctx* ctx) {
   cudaStreamSynchronize(ctx->stream);
   if (ctx->d_status) cudaFree(ctx->d_status);
   if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
+  if (ctx->h_upload) cudaFreeHost(ctx->h_upload);
   for (auto& p : ctx->pending) {
     cudaEventDestroy(p.a);
     cudaEventDestroy(p.b);
@@ -501,3 +533,9 @@ extern "C" int visacd_ctx_kernel_times(visacd_ctx* ctx, const char** names, doub
 
 extern "C" int64_t visacd_ctx_launch_count(const visacd_ctx* ctx) { return ctx ? ctx->launches : 0; }
 extern "C" int visacd_ctx_sm_count(const visacd_ctx* ctx) { return ctx ? ctx->sm_count : 0; }
+
+extern "C" int visacd_set_blocking_sync(int device, int blocking) {
+  VCUDA(cudaSetDevice(device));
+  VCUDA(cudaSetDeviceFlags(blocking ? cudaDeviceScheduleBlockingSync : cudaDeviceScheduleAuto));
+  return VISACD_OK;
+}

@@ -673,14 +673,18 @@ extern "C" int visacd_face_hausdorff(visacd_ctx* ctx, const double* va, int32_t 
   VTRY(ensure_slot(ctx, kSlotHausdorff, off));
   char* B = slot<char>(ctx, kSlotHausdorff);
   cudaStream_t st = ctx->stream;
-  VCUDA(cudaMemcpyAsync(B + o_va, va, (size_t)nva * 24, cudaMemcpyHostToDevice, st));
-  VCUDA(cudaMemcpyAsync(B + o_ta, ta, (size_t)nta * 12, cudaMemcpyHostToDevice, st));
-  VCUDA(cudaMemcpyAsync(B + o_xa, xa, (size_t)na * 24, cudaMemcpyHostToDevice, st));
-  VCUDA(cudaMemcpyAsync(B + o_ia, ida, (size_t)na * 4, cudaMemcpyHostToDevice, st));
-  VCUDA(cudaMemcpyAsync(B + o_vb, vb, (size_t)nvb * 24, cudaMemcpyHostToDevice, st));
-  VCUDA(cudaMemcpyAsync(B + o_tb, tb, (size_t)ntb * 12, cudaMemcpyHostToDevice, st));
-  VCUDA(cudaMemcpyAsync(B + o_xb, xb, (size_t)nb * 24, cudaMemcpyHostToDevice, st));
-  VCUDA(cudaMemcpyAsync(B + o_ib, idb, (size_t)nb * 4, cudaMemcpyHostToDevice, st));
+  Stager up(ctx);
+  VTRY(up.reserve((size_t)nva * 24 + (size_t)nta * 12 + (size_t)na * 28 + (size_t)nvb * 24 + (size_t)ntb * 12 +
+                      (size_t)nb * 28,
+                  8));
+  VTRY(up.put(B + o_va, va, (size_t)nva * 24));
+  VTRY(up.put(B + o_ta, ta, (size_t)nta * 12));
+  VTRY(up.put(B + o_xa, xa, (size_t)na * 24));
+  VTRY(up.put(B + o_ia, ida, (size_t)na * 4));
+  VTRY(up.put(B + o_vb, vb, (size_t)nvb * 24));
+  VTRY(up.put(B + o_tb, tb, (size_t)ntb * 12));
+  VTRY(up.put(B + o_xb, xb, (size_t)nb * 24));
+  VTRY(up.put(B + o_ib, idb, (size_t)nb * 4));
   VCUDA(cudaMemsetAsync(B + zero_begin, 0, zero_end - zero_begin, st));
   VCUDA(cudaMemsetAsync(B + o_mx, 0, 64, st));
   // Bucket both sample sets (counting sort by cell).

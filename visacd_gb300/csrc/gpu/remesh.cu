@@ -354,8 +354,10 @@ extern "C" int visacd_sdf_remesh(visacd_ctx* ctx, const double* verts, int32_t n
   uint32_t* qcnt = (uint32_t*)(base + oQcnt);
   uint64_t* qoff = (uint64_t*)(base + oQoff);
   cudaStream_t st = ctx->stream;
-  VCUDA(cudaMemcpyAsync(dP, P.data(), P.size() * 8, cudaMemcpyHostToDevice, st));
-  VCUDA(cudaMemcpyAsync(dT, tris, 3 * (size_t)nt * 4, cudaMemcpyHostToDevice, st));
+  Stager up(ctx);
+  VTRY(up.reserve(P.size() * 8 + 3 * (size_t)nt * 4, 2));
+  VTRY(up.put(dP, P.data(), P.size() * 8));
+  VTRY(up.put(dT, tris, 3 * (size_t)nt * 4));
   const unsigned gv = grid_for((int64_t)nvox, 256, 16 * (int64_t)ctx->sm_count);
   const float band_f = (float)g.band;
   uint32_t band_bits;

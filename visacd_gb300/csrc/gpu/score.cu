@@ -339,9 +339,11 @@ int score_planes_impl(visacd_ctx* ctx, const float* planes, int32_t P, const flo
     VTRY(ensure_slot(ctx, kSlotPoints, (size_t)(N > 0 ? N : 1) * 12));
     VTRY(ensure_slot(ctx, kSlotEdgesIn, (size_t)(E > 0 ? E : 1) * 8));
     VTRY(ensure_slot(ctx, kSlotScores, (size_t)(P > 0 ? P : 1) * 8));
-    if (P) VCUDA(cudaMemcpyAsync(ctx->buf[kSlotPlanes].p, planes, (size_t)P * 16, cudaMemcpyHostToDevice, ctx->stream));
-    if (N) VCUDA(cudaMemcpyAsync(ctx->buf[kSlotPoints].p, points, (size_t)N * 12, cudaMemcpyHostToDevice, ctx->stream));
-    if (E) VCUDA(cudaMemcpyAsync(ctx->buf[kSlotEdgesIn].p, edges, (size_t)E * 8, cudaMemcpyHostToDevice, ctx->stream));
+    Stager up(ctx);
+    VTRY(up.reserve((size_t)P * 16 + (size_t)N * 12 + (size_t)E * 8, 3));
+    if (P) VTRY(up.put(ctx->buf[kSlotPlanes].p, planes, (size_t)P * 16));
+    if (N) VTRY(up.put(ctx->buf[kSlotPoints].p, points, (size_t)N * 12));
+    if (E) VTRY(up.put(ctx->buf[kSlotEdgesIn].p, edges, (size_t)E * 8));
     d_planes = slot<float>(ctx, kSlotPlanes);
     d_pts = slot<float>(ctx, kSlotPoints);
     d_edges = slot<uint32_t>(ctx, kSlotEdgesIn);

@@ -513,13 +513,13 @@ int visibility_impl(visacd_ctx* ctx, const float* pts, int32_t n, const uint8_t*
   const uint8_t* d_new = is_new;
   if (!device_ptrs && n > 0) {
     VTRY(ensure_slot(ctx, kSlotPoints, (size_t)n * 12));
-    VCUDA(cudaMemcpyAsync(ctx->buf[kSlotPoints].p, pts, (size_t)n * 12, cudaMemcpyHostToDevice,
-                          ctx->stream));
+    if (is_new) VTRY(ensure_slot(ctx, kSlotMask, (size_t)n));
+    Stager up(ctx);
+    VTRY(up.reserve((size_t)n * 13, 2));
+    VTRY(up.put(ctx->buf[kSlotPoints].p, pts, (size_t)n * 12));
     d_pts = slot<float>(ctx, kSlotPoints);
     if (is_new) {
-      VTRY(ensure_slot(ctx, kSlotMask, (size_t)n));
-      VCUDA(cudaMemcpyAsync(ctx->buf[kSlotMask].p, is_new, (size_t)n, cudaMemcpyHostToDevice,
-                            ctx->stream));
+      VTRY(up.put(ctx->buf[kSlotMask].p, is_new, (size_t)n));
       d_new = slot<uint8_t>(ctx, kSlotMask);
     }
   }
