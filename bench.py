@@ -436,7 +436,8 @@ def run_micro(args) -> dict:
       visibility  — s4 blob (2562 vertices, all 3,280,641 pairs) vs its 0.03 cage
       scoring     — 2^20 random edges x 4096 planes
       learned     — one training step of the proposer, 64 parts (forward,
-                    backward, Adam) and one proposal
+                    backward, Adam; forward per-edge layers on tcgen05 and on
+                    mma.sync), the forward alone on both paths, one proposal
       sdf_remesh  — the s5 blob's 0.03 cage at scale 40
       hausdorff   — concavity metric of the remeshed s4 blob vs its hull (3000)
       hull_dist   — all 2016 pairs of 64 hulls of 50..700 vertices
@@ -485,6 +486,15 @@ def run_micro(args) -> dict:
     w = np.ones((64, 8), np.float32)
     timed("learned_train_step", lambda: lp.train_step(feats, labels, w, 1e-3),
           flop_per_step=3 * 2 * 64 * N.LP_POINTS * (16 * 64 + 64 * 128 + 128 * 256))
+    lp.set_tcgen05(False)
+    timed("learned_train_step_mma_sync", lambda: lp.train_step(feats, labels, w, 1e-3),
+          flop_per_step=3 * 2 * 64 * N.LP_POINTS * (16 * 64 + 64 * 128 + 128 * 256))
+    lp.set_tcgen05(True)
+    fwd_flop = 2 * 64 * N.LP_POINTS * (16 * 64 + 64 * 128 + 128 * 256)
+    timed("learned_forward_tcgen05", lambda: lp.forward(feats), flop=fwd_flop)
+    lp.set_tcgen05(False)
+    timed("learned_forward_mma_sync", lambda: lp.forward(feats), flop=fwd_flop)
+    lp.set_tcgen05(True)
     e4, _ = ctx.visibility(v4, sb, cb)
     c, h = pp.part_frame(v4)
     timed("learned_propose", lambda: lp.propose(v4, e4, c, h))

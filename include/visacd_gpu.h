@@ -310,6 +310,9 @@ int visacd_lp_propose(visacd_lp* lp, const float* points, int32_t n, const uint3
    batch loss is the mean. grads_out: 87,744 floats or NULL. */
 int visacd_lp_grads(visacd_lp* lp, const float* feats, const float* labels, const float* lw,
                     int32_t B, int32_t L, float* grads_out, float* loss_out);
+/* Forward per-edge layers on the Blackwell tensor-core path (tcgen05.mma with
+   the accumulator in tensor memory, the default) or on mma.sync (enable = 0). */
+int visacd_lp_set_tcgen05(visacd_lp* lp, int enable);
 /* visacd_lp_grads followed by one Adam step (beta 0.9 / 0.999, eps 1e-8). */
 int visacd_lp_train_step(visacd_lp* lp, const float* feats, const float* labels, const float* lw,
                          int32_t B, int32_t L, float lr, float* loss_out);

@@ -78,3 +78,24 @@ def test_training_lowers_loss_and_is_deterministic(native, ctx):
         runs.append((first, last, lp.params()))
     assert runs[0][1] < 0.6 * runs[0][0], runs[0][:2]
     np.testing.assert_array_equal(runs[0][2], runs[1][2])
+
+
+def test_tcgen05_forward_matches_mma_sync(native, ctx):
+    """The tcgen05 (tensor-memory) forward of the per-edge layers against the
+    mma.sync one: same BF16 operands, FP32 accumulation in another order, so
+    the planes and every gradient agree to BF16 rounding."""
+    params = lr.init_params(5)
+    feats, labels, w = _case(13, B=3)
+    a = native.PlaneProposer(ctx, params=params)
+    a.set_tcgen05(False)
+    b = native.PlaneProposer(ctx, params=params)
+    b.set_tcgen05(True)
+    pa, pb = a.forward(feats), b.forward(feats)
+    np.testing.assert_allclose(pb, pa, atol=2e-2)
+    la, ga = a.grads(feats, labels, w)
+    lb, gb = b.grads(feats, labels, w)
+    assert abs(la - lb) <= 1e-2 * abs(la)
+    assert np.linalg.norm(ga - gb) <= 2e-2 * np.linalg.norm(ga)
+    # and the oracle (BF16-emulated) agrees with the tcgen05 path as with mma.sync
+    rloss, rg, _ = lr.forward_backward(params, feats, labels, w, emulate_bf16=True)
+    assert abs(lb - rloss) <= 1e-2 * abs(rloss)

@@ -30,7 +30,7 @@ EXPORTED = [
     "visacd_lp_features", "visacd_lp_forward", "visacd_lp_propose", "visacd_lp_grads",
     "visacd_lp_train_step",
     "visacd_sdf_remesh", "visacd_sdf_fetch", "visacd_hull_distances", "visacd_segment_triangle_tests",
-    "visacd_set_blocking_sync",
+    "visacd_set_blocking_sync", "visacd_lp_set_tcgen05",
 ]
 
 LP_POINTS = 2048
@@ -122,6 +122,7 @@ def load() -> C.CDLL:
     lib.visacd_lp_propose.argtypes = [P, P, i32, P, i64, P, C.c_float, P]
     lib.visacd_lp_grads.argtypes = [P, P, P, P, i32, i32, P, P]
     lib.visacd_lp_train_step.argtypes = [P, P, P, P, i32, i32, C.c_float, P]
+    lib.visacd_lp_set_tcgen05.argtypes = [P, C.c_int]
     return lib
 
 
@@ -470,6 +471,10 @@ class PlaneProposer:
             if p.size != self.n_params:
                 raise ValueError(f"expected {self.n_params} parameters, got {p.size}")
         _check(lib().visacd_lp_create(ctx.handle, _ptr(p), seed, C.byref(self._h)), "visacd_lp_create")
+
+    def set_tcgen05(self, enable: bool) -> None:
+        """Forward per-edge layers on tcgen05 (tensor memory) instead of mma.sync."""
+        _check(lib().visacd_lp_set_tcgen05(self._h, int(bool(enable))), "visacd_lp_set_tcgen05")
 
     def params(self) -> np.ndarray:
         out = np.empty(self.n_params, dtype=np.float32)

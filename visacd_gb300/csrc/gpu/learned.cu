@@ -243,6 +243,178 @@ __global__ void __launch_bounds__(128) lp_gemm_kernel(const bf16* __restrict__ A
     }
 }
 
+// ---------------------------------------------------------------------------
+// Blackwell tensor-core path of the forward per-edge layers (tcgen05):
+// Y = relu(X W^T + b), X [M x K], W [N x K], K in {16, 64, 128}, N in
+// {64, 128, 256}, accumulators in tensor memory. Persistent CTAs (4 warps)
+// walk 128-row tiles of X:
+//  * W is copied once into shared memory, X tiles are double-buffered with
+//    cp.async; both in the canonical K-major no-swizzle layout: 8-row x
+//    16-byte core matrices, core (row group g, k group j) at
+//    ((j * groups) + g) * 128 bytes (stride 128 B between row groups = SBO,
+//    groups * 128 B between k groups = LBO);
+//  * two accumulators of N tensor-memory columns: thread 0 issues the
+//    tcgen05.mma chain (M = 128, N, K = 16 each, BF16 -> FP32) of tile i + 1
+//    and commits it to that accumulator's mbarrier while the four warps read
+//    tile i back with tcgen05.ld (32 lanes x 16 columns per load), add the
+//    bias, apply ReLU and store BF16;
+//  * every mbarrier wait has an iteration limit (status bit on expiry).
+// The dynamic shared memory (160 KB) leaves room for any stride reading of
+// the W and X regions.
+// ---------------------------------------------------------------------------
+constexpr int kTcM = 128;
+constexpr int kTcSmem = 160 * 1024;
+constexpr int kTcW = 0, kTcX0 = 64 * 1024, kTcX1 = 96 * 1024, kTcBar = 128 * 1024;
+
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+__device__ __forceinline__ bool tc_wait(uint32_t bar_addr, uint32_t parity) {
+  for (int it = 0; it < (1 << 24); ++it) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar_addr), "r"(parity));
+    if (ok) return true;
+  }
+  return false;
+}
+
+// cp.async of one 128-row X tile into the core-matrix layout (rows past M: zeros).
+__device__ __forceinline__ void tc_load_x(unsigned char* buf, const bf16* __restrict__ X, int M, int K, int row0,
+                                          int tid) {
+  const int kg = K / 8, ag = kTcM / 8;
+  for (int c = tid; c < kTcM * kg; c += 128) {
+    const int r = c / kg, j = c % kg;
+    const bool ok = row0 + r < M;
+    cp_async16(smem_u32(buf + ((j * ag) + (r >> 3)) * 128 + (r & 7) * 16),
+               ok ? X + (size_t)(row0 + r) * K + j * 8 : X, ok);
+  }
+  asm volatile("cp.async.commit_group;\n" ::);
+}
+
+__global__ void __launch_bounds__(128, 1) lp_gemm_tc_kernel(const bf16* __restrict__ X, int M, int K,
+                                                           const bf16* __restrict__ W, int N,
+                                                           const float* __restrict__ bias, bf16* __restrict__ Y,
+                                                           uint32_t* __restrict__ status) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int ntiles = (M + kTcM - 1) / kTcM;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + kTcBar);  // two mbarriers
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + kTcBar + 32);
+  const uint32_t s_base = smem_u32(smem);
+  const uint32_t bar0 = smem_u32(&bar[0]), bar1 = smem_u32(&bar[1]);
+  const int kg = K / 8, ag = kTcM / 8, bg = N / 8;
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar0));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar1));
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::);
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tslot)),
+                 "r"(2 * N));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+  }
+  // W once, then the first X tile.
+  for (int c = tid; c < N * kg; c += 128) {
+    const int r = c / kg, j = c % kg;
+    cp_async16(smem_u32(smem + kTcW + ((j * bg) + (r >> 3)) * 128 + (r & 7) * 16), W + (size_t)r * K + j * 8, true);
+  }
+  int t0 = blockIdx.x;
+  if (t0 < ntiles) tc_load_x(smem + kTcX0, X, M, K, t0 * kTcM, tid);
+  else asm volatile("cp.async.commit_group;\n" ::);
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+  const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(tslot);
+  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
+                         ((uint32_t)(kTcM >> 4) << 24);
+  // MMA chain of local tile i (buffer and accumulator i % 2) by thread 0.
+  auto issue = [&](int i) {
+    if (tid == 0) {
+      const uint32_t xb = s_base + ((i & 1) ? kTcX1 : kTcX0);
+      const uint32_t acc = tmem + (uint32_t)((i & 1) * N);
+      for (int s = 0; s < K / 16; ++s) {
+        const uint64_t ad = tc_desc(xb + s * 2 * ag * 128, ag * 128, 128);
+        const uint64_t bd = tc_desc(s_base + kTcW + s * 2 * bg * 128, bg * 128, 128);
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(acc),
+            "l"(ad), "l"(bd), "r"(idesc), "r"(s > 0 ? 1 : 0));
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+          (i & 1) ? bar1 : bar0));
+    }
+  };
+  bool ok = true;
+  // tile 0 of this CTA: wait for its data, issue, prefetch tile 1
+  asm volatile("cp.async.wait_group 0;\n" ::);
+  asm volatile("fence.proxy.async.shared::cta;\n" ::);
+  __syncthreads();
+  const int nlocal = t0 < ntiles ? (ntiles - 1 - t0) / gridDim.x + 1 : 0;
+  if (nlocal > 0) issue(0);
+  if (nlocal > 1) tc_load_x(smem + kTcX1, X, M, K, (t0 + gridDim.x) * kTcM, tid);
+  for (int i = 0; i < nlocal && ok; ++i) {
+    // start tile i + 1 while tile i drains
+    if (i + 1 < nlocal) {
+      asm volatile("cp.async.wait_group 0;\n" ::);
+      asm volatile("fence.proxy.async.shared::cta;\n" ::);
+      asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+      __syncthreads();
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+      issue(i + 1);
+    }
+    // tile i's MMAs done: its buffer is free for tile i + 2
+    ok = tc_wait((i & 1) ? bar1 : bar0, (uint32_t)((i >> 1) & 1));
+    if (!ok) break;
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+    if (i + 2 < nlocal) tc_load_x(smem + ((i & 1) ? kTcX1 : kTcX0), X, M, K, (t0 + (i + 2) * gridDim.x) * kTcM, tid);
+    const int row = (t0 + i * gridDim.x) * kTcM + warp * 32 + lane;
+    const uint32_t acc = tmem + (uint32_t)((i & 1) * N);
+    for (int c0 = 0; c0 < N; c0 += 16) {
+      uint32_t r[16];
+      const uint32_t taddr = acc + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+          : "r"(taddr));
+      asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::);
+      if (row < M) {
+        uint32_t o[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          float v0 = __uint_as_float(r[2 * k]) + bias[c0 + 2 * k];
+          float v1 = __uint_as_float(r[2 * k + 1]) + bias[c0 + 2 * k + 1];
+          v0 = v0 > 0.f ? v0 : 0.f;
+          v1 = v1 > 0.f ? v1 : 0.f;
+          o[k] = pack_bf16(v0, v1);
+        }
+        uint4* dst = reinterpret_cast<uint4*>(Y + (size_t)row * N + c0);
+        dst[0] = make_uint4(o[0], o[1], o[2], o[3]);
+        dst[1] = make_uint4(o[4], o[5], o[6], o[7]);
+      }
+    }
+    // the accumulator of tile i is read before tile i + 2 reuses it
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+  }
+  if (!ok) {
+    if (tid == 0) atomicOr(status, vgpu::kStatusMbarrierTimeout);
+    // MMAs possibly still in flight get a second bounded wait on both barriers
+    tc_wait(bar0, 0);
+    tc_wait(bar1, 0);
+  }
+  asm volatile("cp.async.wait_group 0;\n" ::);
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(2 * N));
+}
+
 // Sum of `parts` partial arrays of `count` floats, in order, into out.
 __global__ void lp_sum_parts_kernel(const float* __restrict__ parts, int nparts, int count,
                                     float* __restrict__ out) {
@@ -489,6 +661,7 @@ __global__ void lp_to_bf16_kernel(const float* __restrict__ p, int count, bf16* 
 struct visacd_lp {
   visacd_ctx* ctx = nullptr;
   int max_batch = 0;
+  bool tcgen05 = false;  // forward per-edge layers on the tcgen05 path (on after create)
   int64_t step = 0;
   DevBuf params, params_bf16, grads, adam_m, adam_v;
   DevBuf x0, a1, a2, a3, poolkey, g, gb, arg, a4, a5, z6;
@@ -601,12 +774,22 @@ int forward(visacd_lp* lp, int B) {
   const int M = B * kPts;
   const bf16* W = P<bf16>(lp->params_bf16);
   const float* Pf = P<float>(lp->params);
-  VTRY((gemm<true, true, kEpiBiasReluBf16>(lp, P<bf16>(lp->x0), kIn, W + kOff.w[0], kIn, lp->a1.p, 64, M,
-                                           64, kIn, 0, Pf + kOff.b[0])));
-  VTRY((gemm<true, true, kEpiBiasReluBf16>(lp, P<bf16>(lp->a1), 64, W + kOff.w[1], 64, lp->a2.p, 128, M,
-                                           128, 64, 0, Pf + kOff.b[1])));
-  VTRY((gemm<true, true, kEpiBiasReluBf16>(lp, P<bf16>(lp->a2), 128, W + kOff.w[2], 128, lp->a3.p, 256,
-                                           M, 256, 128, 0, Pf + kOff.b[2])));
+  if (lp->tcgen05) {
+    const bf16* xin[3] = {P<bf16>(lp->x0), P<bf16>(lp->a1), P<bf16>(lp->a2)};
+    bf16* yout[3] = {P<bf16>(lp->a1), P<bf16>(lp->a2), P<bf16>(lp->a3)};
+    const int tiles = (M + kTcM - 1) / kTcM;
+    const int grid = std::max(1, std::min(tiles, ctx->sm_count));
+    for (int l = 0; l < 3; ++l)
+      VLAUNCH(ctx, vgpu::kKLpGemm, grid, 128, kTcSmem, lp_gemm_tc_kernel, xin[l], M, kK[l], W + kOff.w[l], kN[l],
+              Pf + kOff.b[l], yout[l], ctx->d_status);
+  } else {
+    VTRY((gemm<true, true, kEpiBiasReluBf16>(lp, P<bf16>(lp->x0), kIn, W + kOff.w[0], kIn, lp->a1.p, 64, M,
+                                             64, kIn, 0, Pf + kOff.b[0])));
+    VTRY((gemm<true, true, kEpiBiasReluBf16>(lp, P<bf16>(lp->a1), 64, W + kOff.w[1], 64, lp->a2.p, 128, M,
+                                             128, 64, 0, Pf + kOff.b[1])));
+    VTRY((gemm<true, true, kEpiBiasReluBf16>(lp, P<bf16>(lp->a2), 128, W + kOff.w[2], 128, lp->a3.p, 256,
+                                             M, 256, 128, 0, Pf + kOff.b[2])));
+  }
   VCUDA(cudaMemsetAsync(lp->poolkey.p, 0, (size_t)B * 256 * 8, ctx->stream));
   VLAUNCH(ctx, vgpu::kKLpPool, dim3(B, 8), 256, 0, lp_pool_kernel, P<bf16>(lp->a3),
           P<unsigned long long>(lp->poolkey));
@@ -733,6 +916,13 @@ extern "C" int visacd_lp_create(visacd_ctx* ctx, const float* params, uint32_t s
     vgpu::set_error("lp_create: %s", cudaGetErrorString(e));
     return fail(VISACD_ERR_CUDA);
   }
+  // The forward per-edge layers run on tcgen05 (tensor memory) by default.
+  if ((e = cudaFuncSetAttribute(lp_gemm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem)) !=
+      cudaSuccess) {
+    vgpu::set_error("lp_create: %s", cudaGetErrorString(e));
+    return fail(VISACD_ERR_CUDA);
+  }
+  lp->tcgen05 = true;
   lp_to_bf16_kernel<<<(kOff.total + 255) / 256, 256, 0, ctx->stream>>>(P<float>(lp->params), kOff.total,
                                                                       P<bf16>(lp->params_bf16));
   if ((rc = vgpu::after_launch(ctx, "lp_to_bf16_kernel")) != VISACD_OK) return fail(rc);
@@ -850,5 +1040,15 @@ extern "C" int visacd_lp_train_step(visacd_lp* lp, const float* feats, const flo
   VLAUNCH(ctx, vgpu::kKLpAdam, (kOff.total + 255) / 256, 256, 0, lp_adam_kernel, P<float>(lp->params),
           P<float>(lp->grads), P<float>(lp->adam_m), P<float>(lp->adam_v), P<bf16>(lp->params_bf16),
           kOff.total, lr, bc1, bc2);
+  return VISACD_OK;
+}
+
+extern "C" int visacd_lp_set_tcgen05(visacd_lp* lp, int enable) {
+  VCHECK(lp, VISACD_ERR_INVALID_ARG, "lp_set_tcgen05: null proposer");
+  if (enable) {
+    VCUDA(cudaSetDevice(lp->ctx->device));
+    VCUDA(cudaFuncSetAttribute(lp_gemm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem));
+  }
+  lp->tcgen05 = enable != 0;
   return VISACD_OK;
 }
