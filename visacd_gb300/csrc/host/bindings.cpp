@@ -11,6 +11,7 @@
 #include "geometry.hpp"
 #include "gpu_bridge.hpp"
 #include "process.hpp"
+#include "visacd_gpu.h"
 
 namespace py = pybind11;
 using namespace visacd;
@@ -160,6 +161,21 @@ PYBIND11_MODULE(visacd, m) {
     d["conc_hull_ms"] = ct.hull_ms;
     d["conc_samples"] = ct.samples;
     d["conc_calls"] = ct.calls;
+    return d;
+  });
+  m.def("_gpu_timing", [](bool on) {
+    visacd_ctx_set_timing(gpu::context(), on ? 1 : 0);
+    visacd_ctx_reset_times(gpu::context());
+  });
+  m.def("_gpu_kernel_times", []() {
+    const char* names[96];
+    double ms[96];
+    int64_t launches[96];
+    int n = 0;
+    py::dict d;
+    if (visacd_ctx_kernel_times(gpu::context(), names, ms, launches, 96, &n) == VISACD_OK)
+      for (int i = 0; i < n; ++i)
+        if (launches[i]) d[names[i]] = py::make_tuple(ms[i], launches[i]);
     return d;
   });
   m.def("_reset_counters", []() {
