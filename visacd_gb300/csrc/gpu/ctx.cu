@@ -5,6 +5,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <atomic>
 #include <mutex>
 
 #include "common.cuh"
@@ -366,9 +367,77 @@ __global__ void radix_scatter_kernel(const uint64_t* __restrict__ keys,
   }
 }
 
+// Small inputs (n <= kSmallSort) in one CTA: bitonic sort in shared memory of
+// (key restricted to key_bits, input position), which is exactly the order of
+// the stable LSD radix sort below, in one launch instead of 5 per key byte.
+constexpr int kSmallSort = 8192;
+constexpr size_t kSmallSortSmem = (size_t)kSmallSort * 16;
+
+__global__ void __launch_bounds__(1024) small_sort_kernel(uint64_t* __restrict__ keys, uint32_t* __restrict__ vals,
+                                                          int n, uint64_t mask) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  uint64_t* K = reinterpret_cast<uint64_t*>(sm);
+  uint32_t* V = reinterpret_cast<uint32_t*>(sm + (size_t)kSmallSort * 8);
+  uint32_t* Pos = reinterpret_cast<uint32_t*>(sm + (size_t)kSmallSort * 12);
+  int n2 = 1;
+  while (n2 < n) n2 <<= 1;
+  for (int i = threadIdx.x; i < n2; i += blockDim.x) {
+    if (i < n) {
+      K[i] = keys[i];
+      V[i] = vals[i];
+    } else {
+      K[i] = ~0ull;
+      V[i] = 0;
+    }
+    Pos[i] = (uint32_t)i;
+  }
+  __syncthreads();
+  for (int k = 2; k <= n2; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = threadIdx.x; i < n2; i += blockDim.x) {
+        const int ixj = i ^ j;
+        if (ixj > i) {
+          // pads (position >= n) order after every real element
+          const uint64_t ka = Pos[i] < (uint32_t)n ? (K[i] & mask) : ~0ull;
+          const uint64_t kb = Pos[ixj] < (uint32_t)n ? (K[ixj] & mask) : ~0ull;
+          const bool gt = ka > kb || (ka == kb && Pos[i] > Pos[ixj]);
+          const bool asc = (i & k) == 0;
+          if (gt == asc) {
+            const uint64_t tk = K[i];
+            K[i] = K[ixj];
+            K[ixj] = tk;
+            const uint32_t tv = V[i];
+            V[i] = V[ixj];
+            V[ixj] = tv;
+            const uint32_t tp = Pos[i];
+            Pos[i] = Pos[ixj];
+            Pos[ixj] = tp;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    keys[i] = K[i];
+    vals[i] = V[i];
+  }
+}
+
 int radix_sort_u64(visacd_ctx* ctx, uint64_t* keys, uint32_t* vals, uint64_t* keys_alt,
                    uint32_t* vals_alt, int32_t n, int key_bits) {
   if (n <= 1) return VISACD_OK;
+  if (n <= kSmallSort) {
+    static std::atomic<bool> attr_set[64];
+    if (ctx->device < 0 || ctx->device >= 64 || !attr_set[ctx->device].load()) {
+      VCUDA(cudaFuncSetAttribute(small_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kSmallSortSmem));
+      if (ctx->device >= 0 && ctx->device < 64) attr_set[ctx->device].store(true);
+    }
+    const uint64_t mask = key_bits >= 64 ? ~0ull : ((1ull << key_bits) - 1);
+    VLAUNCH(ctx, kKSortScatter, 1, 1024, kSmallSortSmem, small_sort_kernel, keys, vals, n, mask);
+    return VISACD_OK;
+  }
   int nblocks = (int)((n + kSortTile - 1) / kSortTile);
   size_t hist_n = (size_t)256 * nblocks;
   VTRY(ensure_slot(ctx, kSlotSortHist, hist_n * sizeof(uint32_t) + (hist_n + 1) * sizeof(uint64_t) + 16));

@@ -3,12 +3,19 @@
 //
 // For every sample q of one surface: its 10 nearest samples on the other
 // surface (exact k-NN, FP64 squared distances), then the smallest distance
-// from q to the triangles those samples were drawn from; a lane whose minimum
-// exceeds 10 falls back to the nearest-sample distance; the result is the
-// largest minimum over both directions.
-//  * Samples are bucketed in a uniform grid (counting sort: atomic counts,
-//    exclusive scan, scatter); a query walks Chebyshev rings of cells until it
-//    holds 10 candidates no farther than the ring radius.
+// from q to the triangles those samples were drawn from (stopping below
+// 1e-14); a minimum above 10 is replaced by the nearest-sample distance; the
+// result is the largest minimum over both directions. Organised as a bounded
+// max-min search with every shortcut exact:
+//  * both sample sets are bucketed in uniform grids (counting sort) and both
+//    meshes get FP32 triangle bounds (box, plane), in four launches plus a scan;
+//  * a two-ring search gives each query an upper bound of its term (the
+//    nearest sample's distance, rounded up); queries with no sample that
+//    close are evaluated one warp each (hhead_kernel);
+//  * the rest skip when their bound does not exceed the running maximum;
+//  * k-NN candidates are ranked in FP32 with a proven rounding margin and the
+//    exact 10 chosen in FP64; triangle distances whose FP32 lower bound cannot
+//    lower the minimum are skipped.
 //  * Point-triangle distance: closest point by Voronoi region (Ericson,
 //    Real-Time Collision Detection 5.1.5) in FP64 with explicit round-to-
 //    nearest intrinsics in the host's operation order, so values equal the
@@ -34,79 +41,9 @@ struct HGrid {
   float eabs;         // bound of |FP32 distance - exact distance| for this grid's points and queries
 };
 
-struct HCounters {
-  unsigned long long max_bits;  // FP64 bits of the running maximum
-  double bbox[2][6];            // per grid: lo xyz, hi xyz (ordered bits)
-  unsigned long long lo_bits[2][3], hi_bits[2][3];
-};
-
-__device__ __forceinline__ unsigned long long d2o(double d) {
-  unsigned long long b = __double_as_longlong(d);
-  return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
-}
-__device__ __forceinline__ double o2d(unsigned long long o) {
-  unsigned long long b = (o & 0x8000000000000000ull) ? (o & 0x7fffffffffffffffull) : ~o;
-  return __longlong_as_double(b);
-}
-
-__global__ void hbbox_kernel(const double* __restrict__ p, int n, unsigned long long* lo,
-                             unsigned long long* hi) {
-  double l[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, u[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    for (int a = 0; a < 3; ++a) {
-      l[a] = fmin(l[a], p[3 * (int64_t)i + a]);
-      u[a] = fmax(u[a], p[3 * (int64_t)i + a]);
-    }
-  for (int a = 0; a < 3; ++a) {
-    for (int o = 16; o; o >>= 1) {
-      l[a] = fmin(l[a], __shfl_xor_sync(0xffffffffu, l[a], o));
-      u[a] = fmax(u[a], __shfl_xor_sync(0xffffffffu, u[a], o));
-    }
-    if ((threadIdx.x & 31) == 0) {
-      atomicMin(&lo[a], d2o(l[a]));
-      atomicMax(&hi[a], d2o(u[a]));
-    }
-  }
-}
-
 __device__ __forceinline__ int cell_coord(double x, double lo, double h, int dim) {
   int c = (int)floor((x - lo) / h);
   return c < 0 ? 0 : (c >= dim ? dim - 1 : c);
-}
-
-__global__ void hcount_kernel(HGrid g, int* __restrict__ counts, int* __restrict__ cell_of) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += gridDim.x * blockDim.x) {
-    const double* p = g.pts + 3 * (int64_t)i;
-    int cx = cell_coord(p[0], g.lo[0], g.h, g.dim[0]);
-    int cy = cell_coord(p[1], g.lo[1], g.h, g.dim[1]);
-    int cz = cell_coord(p[2], g.lo[2], g.h, g.dim[2]);
-    int c = (cz * g.dim[1] + cy) * g.dim[0] + cx;
-    cell_of[i] = c;
-    atomicAdd(&counts[c], 1);
-  }
-}
-
-__global__ void hscatter_kernel(int n, const int* __restrict__ cell_of, const unsigned long long* __restrict__ off,
-                                int* __restrict__ fill, int* __restrict__ order) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    int c = cell_of[i];
-    int k = atomicAdd(&fill[c], 1);
-    order[off[c] + k] = i;
-  }
-}
-
-__global__ void hsorted_kernel(const double* __restrict__ pts, const int* __restrict__ order, int n,
-                               float4* __restrict__ spts) {
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-    const int i = order[k];
-    spts[k] = make_float4((float)pts[3 * (int64_t)i], (float)pts[3 * (int64_t)i + 1], (float)pts[3 * (int64_t)i + 2],
-                          __int_as_float(i));
-  }
-}
-
-__global__ void hstart_kernel(const unsigned long long* __restrict__ off, int cells, int* __restrict__ start) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= cells; i += gridDim.x * blockDim.x)
-    start[i] = (int)off[i];
 }
 
 // Exact k nearest samples of q by Chebyshev rings of grid cells around q's
@@ -253,37 +190,6 @@ __device__ __forceinline__ bool knn_rings_f32(const HGrid& G, const double (&q)[
     }
   }
   return true;
-}
-
-// Per triangle of a mesh, FP32 bounds for the distance pre-filter: box lo
-// (rounded down), box hi (rounded up), unit normal + offset (a zero normal for
-// degenerate triangles).
-__global__ void htri_bounds_kernel(const double* __restrict__ mv, const int* __restrict__ mt, int nt,
-                                   float4* __restrict__ out) {
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += gridDim.x * blockDim.x) {
-    const double* a = mv + 3 * (int64_t)mt[3 * (int64_t)t];
-    const double* b = mv + 3 * (int64_t)mt[3 * (int64_t)t + 1];
-    const double* c = mv + 3 * (int64_t)mt[3 * (int64_t)t + 2];
-    float lo[3], hi[3];
-    for (int k = 0; k < 3; ++k) {
-      lo[k] = __double2float_rd(fmin(fmin(a[k], b[k]), c[k]));
-      hi[k] = __double2float_ru(fmax(fmax(a[k], b[k]), c[k]));
-    }
-    const double ux = b[0] - a[0], uy = b[1] - a[1], uz = b[2] - a[2];
-    const double vx = c[0] - a[0], vy = c[1] - a[1], vz = c[2] - a[2];
-    double nx = uy * vz - uz * vy, ny = uz * vx - ux * vz, nz = ux * vy - uy * vx;
-    const double nl = sqrt(nx * nx + ny * ny + nz * nz);
-    float4 pl = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (nl > 1e-30) {
-      nx /= nl;
-      ny /= nl;
-      nz /= nl;
-      pl = make_float4((float)nx, (float)ny, (float)nz, (float)-(nx * a[0] + ny * a[1] + nz * a[2]));
-    }
-    out[3 * (int64_t)t] = make_float4(lo[0], lo[1], lo[2], 0.f);
-    out[3 * (int64_t)t + 1] = make_float4(hi[0], hi[1], hi[2], 0.f);
-    out[3 * (int64_t)t + 2] = pl;
-  }
 }
 
 // One direction's data: queries Q against the other surface (grid G over its
@@ -503,13 +409,17 @@ __device__ bool query_term_warp(const HSide& S, int qi, double& term) {
 // Entry e = base + position holds the bound and the query's id (bit 31:
 // direction).
 constexpr int kBoundRings = 2;
-__global__ void __launch_bounds__(128) hbound_kernel(HSide S, int dir, const int* __restrict__ qorder,
-                                                     float* __restrict__ ubs, uint32_t* __restrict__ vals,
-                                                     int base, unsigned* __restrict__ far,
+__global__ void __launch_bounds__(128) hbound_kernel(HSide S0, const int* __restrict__ qorder0, HSide S1,
+                                                     const int* __restrict__ qorder1, float* __restrict__ ubs,
+                                                     uint32_t* __restrict__ vals, unsigned* __restrict__ far,
                                                      int* __restrict__ farlist) {
-  const HGrid& G = S.G;
-  for (int qk = blockIdx.x * blockDim.x + threadIdx.x; qk < S.nq; qk += gridDim.x * blockDim.x) {
-    const int qi = qorder[qk];
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < S0.nq + S1.nq; e += gridDim.x * blockDim.x) {
+    const int dir = e < S0.nq ? 0 : 1;
+    const HSide& S = dir ? S1 : S0;
+    const int qk = dir ? e - S0.nq : e;
+    const int base = dir ? S0.nq : 0;
+    const HGrid& G = S.G;
+    const int qi = (dir ? qorder1 : qorder0)[qk];
     const double* qq = S.Q + 3 * (int64_t)qi;
     const double q[3] = {qq[0], qq[1], qq[2]};
     const int cx = cell_coord(q[0], G.lo[0], G.h, G.dim[0]);
@@ -597,6 +507,99 @@ __global__ void __launch_bounds__(128) hquery_kernel(HSide A, HSide B, const flo
 
 using namespace vgpu;
 
+// Fused set-up of both sample sets and both meshes (one launch): the cell of
+// every sample with per-cell counts (set B's cells follow set A's in one count
+// array), and the FP32 triangle bounds of both meshes.
+__global__ void hprep_kernel(HGrid ga, HGrid gb, int cells_a, int* __restrict__ cnt, int* __restrict__ cell_a,
+                             int* __restrict__ cell_b, const double* __restrict__ mva, const int* __restrict__ mta,
+                             int nta, float4* __restrict__ tba, const double* __restrict__ mvb,
+                             const int* __restrict__ mtb, int ntb, float4* __restrict__ tbb) {
+  const int64_t total = (int64_t)ga.n + gb.n + nta + ntb;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    if (i < ga.n || i < (int64_t)ga.n + gb.n) {
+      const bool isa = i < ga.n;
+      const HGrid& g = isa ? ga : gb;
+      const int k = isa ? (int)i : (int)(i - ga.n);
+      const double* p = g.pts + 3 * (int64_t)k;
+      const int cx = cell_coord(p[0], g.lo[0], g.h, g.dim[0]);
+      const int cy = cell_coord(p[1], g.lo[1], g.h, g.dim[1]);
+      const int cz = cell_coord(p[2], g.lo[2], g.h, g.dim[2]);
+      const int c = (cz * g.dim[1] + cy) * g.dim[0] + cx;
+      (isa ? cell_a : cell_b)[k] = c;
+      atomicAdd(&cnt[(isa ? 0 : cells_a) + c], 1);
+    } else {
+      const int64_t j = i - ga.n - gb.n;
+      const bool isa = j < nta;
+      const int t = isa ? (int)j : (int)(j - nta);
+      const double* mv = isa ? mva : mvb;
+      const int* mt = isa ? mta : mtb;
+      float4* out = isa ? tba : tbb;
+      const double* a = mv + 3 * (int64_t)mt[3 * (int64_t)t];
+      const double* b = mv + 3 * (int64_t)mt[3 * (int64_t)t + 1];
+      const double* c = mv + 3 * (int64_t)mt[3 * (int64_t)t + 2];
+      float lo[3], hi[3];
+      for (int q = 0; q < 3; ++q) {
+        lo[q] = __double2float_rd(fmin(fmin(a[q], b[q]), c[q]));
+        hi[q] = __double2float_ru(fmax(fmax(a[q], b[q]), c[q]));
+      }
+      const double ux = b[0] - a[0], uy = b[1] - a[1], uz = b[2] - a[2];
+      const double vx = c[0] - a[0], vy = c[1] - a[1], vz = c[2] - a[2];
+      double nx = uy * vz - uz * vy, ny = uz * vx - ux * vz, nz = ux * vy - uy * vx;
+      const double nl = sqrt(nx * nx + ny * ny + nz * nz);
+      float4 pl = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (nl > 1e-30) {
+        nx /= nl;
+        ny /= nl;
+        nz /= nl;
+        pl = make_float4((float)nx, (float)ny, (float)nz, (float)-(nx * a[0] + ny * a[1] + nz * a[2]));
+      }
+      out[3 * (int64_t)t] = make_float4(lo[0], lo[1], lo[2], 0.f);
+      out[3 * (int64_t)t + 1] = make_float4(hi[0], hi[1], hi[2], 0.f);
+      out[3 * (int64_t)t + 2] = pl;
+    }
+  }
+}
+
+// Counting-sort scatter of both sets (one launch) from the scanned counts.
+__global__ void hscatter2_kernel(int na, int nb, int cells_a, const int* __restrict__ cell_a,
+                                 const int* __restrict__ cell_b, const unsigned long long* __restrict__ off,
+                                 int* __restrict__ fill, int* __restrict__ order_a, int* __restrict__ order_b) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < na + nb; i += gridDim.x * blockDim.x) {
+    if (i < na) {
+      const int c = cell_a[i];
+      order_a[off[c] + atomicAdd(&fill[c], 1)] = i;
+    } else {
+      const int j = i - na, c = cells_a + cell_b[j];
+      order_b[off[c] - off[cells_a] + atomicAdd(&fill[c], 1)] = j;
+    }
+  }
+}
+
+// Cell starts of both grids and the float copies of both sets in cell order.
+__global__ void hfinish_kernel(int cells_a, int cells_b, const unsigned long long* __restrict__ off,
+                               int* __restrict__ start_a, int* __restrict__ start_b, const double* __restrict__ pa,
+                               const int* __restrict__ order_a, int na, float4* __restrict__ spa,
+                               const double* __restrict__ pb, const int* __restrict__ order_b, int nb,
+                               float4* __restrict__ spb) {
+  const int64_t total = (int64_t)cells_a + 1 + cells_b + 1 + na + nb;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    if (i <= cells_a) {
+      start_a[i] = (int)off[i];
+    } else if (i <= (int64_t)cells_a + 1 + cells_b) {
+      const int c = (int)(i - cells_a - 1);
+      start_b[c] = (int)(off[cells_a + c] - off[cells_a]);
+    } else {
+      const int64_t k0 = i - cells_a - cells_b - 2;
+      const bool isa = k0 < na;
+      const int k = isa ? (int)k0 : (int)(k0 - na);
+      const double* pts = isa ? pa : pb;
+      const int q = (isa ? order_a : order_b)[k];
+      (isa ? spa : spb)[k] = make_float4((float)pts[3 * (int64_t)q], (float)pts[3 * (int64_t)q + 1],
+                                         (float)pts[3 * (int64_t)q + 2], __int_as_float(q));
+    }
+  }
+}
+
 namespace {
 size_t al(size_t x) { return (x + 255) & ~size_t(255); }
 }
@@ -645,31 +648,22 @@ extern "C" int visacd_face_hausdorff(visacd_ctx* ctx, const double* va, int32_t 
   for (int k = 0; k < 2; ++k) g[k].eabs = (float)(M * std::ldexp(1.0, -21) + 1e-30);
   int cells[2];
   for (int k = 0; k < 2; ++k) cells[k] = g[k].dim[0] * g[k].dim[1] * g[k].dim[2];
+  const int ncell = cells[0] + cells[1];
   size_t off = 0;
   auto carve = [&](size_t b) { size_t o = off; off += al(b); return o; };
   const size_t o_va = carve((size_t)nva * 24), o_ta = carve((size_t)nta * 12), o_xa = carve((size_t)na * 24),
                o_ia = carve((size_t)na * 4), o_vb = carve((size_t)nvb * 24), o_tb = carve((size_t)ntb * 12),
-               o_xb = carve((size_t)nb * 24), o_ib = carve((size_t)nb * 4), o_mx = carve(64),
-               o_tba = carve((size_t)nta * 48), o_tbb = carve((size_t)ntb * 48),
-               o_keys = carve((size_t)(na + nb) * 4), o_vals = carve((size_t)(na + nb) * 4),
-               o_keys2 = carve((size_t)(na + nb) * 4);
-  // Per grid: counts + fill (zeroed together), offsets, starts, order, cell of point, sorted float points.
-  size_t zero_begin = off;
-  size_t o_cnt[2], o_fill[2];
-  for (int k = 0; k < 2; ++k) {
-    o_cnt[k] = carve((size_t)(cells[k] + 1) * 4);
-    o_fill[k] = carve((size_t)cells[k] * 4);
-  }
+               o_xb = carve((size_t)nb * 24), o_ib = carve((size_t)nb * 4), o_tba = carve((size_t)nta * 48),
+               o_tbb = carve((size_t)ntb * 48), o_ub = carve((size_t)(na + nb) * 4),
+               o_vals = carve((size_t)(na + nb) * 4), o_far = carve((size_t)(na + nb) * 4);
+  // Zeroed together: maximum + far count, per-cell counts and fills of both grids.
+  const size_t zero_begin = off;
+  const size_t o_mx = carve(64), o_cnt = carve((size_t)(ncell + 1) * 4), o_fill = carve((size_t)ncell * 4);
   const size_t zero_end = off;
-  size_t o_off[2], o_start[2], o_order[2], o_cell[2], o_spts[2];
-  for (int k = 0; k < 2; ++k) {
-    const int n = k == 0 ? na : nb;
-    o_off[k] = carve((size_t)(cells[k] + 1) * 8);
-    o_start[k] = carve((size_t)(cells[k] + 1) * 4);
-    o_order[k] = carve((size_t)n * 4);
-    o_cell[k] = carve((size_t)n * 4);
-    o_spts[k] = carve((size_t)n * 16);
-  }
+  const size_t o_off = carve((size_t)(ncell + 1) * 8), o_sa = carve((size_t)(cells[0] + 1) * 4),
+               o_sb = carve((size_t)(cells[1] + 1) * 4), o_oa = carve((size_t)na * 4), o_ob = carve((size_t)nb * 4),
+               o_ca = carve((size_t)na * 4), o_cb = carve((size_t)nb * 4), o_pa = carve((size_t)na * 16),
+               o_pb = carve((size_t)nb * 16);
   VTRY(ensure_slot(ctx, kSlotHausdorff, off));
   char* B = slot<char>(ctx, kSlotHausdorff);
   cudaStream_t st = ctx->stream;
@@ -686,32 +680,32 @@ extern "C" int visacd_face_hausdorff(visacd_ctx* ctx, const double* va, int32_t 
   VTRY(up.put(B + o_xb, xb, (size_t)nb * 24));
   VTRY(up.put(B + o_ib, idb, (size_t)nb * 4));
   VCUDA(cudaMemsetAsync(B + zero_begin, 0, zero_end - zero_begin, st));
-  VCUDA(cudaMemsetAsync(B + o_mx, 0, 64, st));
-  // Bucket both sample sets (counting sort by cell).
-  for (int k = 0; k < 2; ++k) {
-    const int n = k == 0 ? na : nb;
-    g[k].pts = (const double*)(B + (k == 0 ? o_xa : o_xb));
-    g[k].n = n;
-    int* counts = (int*)(B + o_cnt[k]);
-    int* cell_of = (int*)(B + o_cell[k]);
-    const unsigned gn = grid_for(n, 256, 8LL * ctx->sm_count);
-    VLAUNCH(ctx, kKHausdorff, gn, 256, 0, hcount_kernel, g[k], counts, cell_of);
-    VTRY(exclusive_scan_u32_to_u64(ctx, (const uint32_t*)counts, (uint64_t*)(B + o_off[k]), cells[k]));
-    VLAUNCH(ctx, kKHausdorff, gn, 256, 0, hscatter_kernel, n, cell_of,
-            (const unsigned long long*)(B + o_off[k]), (int*)(B + o_fill[k]), (int*)(B + o_order[k]));
-    VLAUNCH(ctx, kKHausdorff, grid_for(cells[k] + 1, 256, 8LL * ctx->sm_count), 256, 0, hstart_kernel,
-            (const unsigned long long*)(B + o_off[k]), cells[k], (int*)(B + o_start[k]));
-    VLAUNCH(ctx, kKHausdorff, gn, 256, 0, hsorted_kernel, g[k].pts, (const int*)(B + o_order[k]), n,
-            (float4*)(B + o_spts[k]));
-    g[k].start = (const int*)(B + o_start[k]);
-    g[k].order = (const int*)(B + o_order[k]);
-    g[k].spts = (const float4*)(B + o_spts[k]);
-  }
+  g[0].pts = (const double*)(B + o_xa);
+  g[1].pts = (const double*)(B + o_xb);
+  g[0].n = na;
+  g[1].n = nb;
+  const unsigned long long* offs = (const unsigned long long*)(B + o_off);
+  // Both sets bucketed by counting sort (counts, one scan, scatter, starts)
+  // and both meshes' triangle bounds: four launches plus the scan.
+  VLAUNCH(ctx, kKHausdorff, grid_for((int64_t)na + nb + nta + ntb, 256, 8LL * ctx->sm_count), 256, 0, hprep_kernel,
+          g[0], g[1], cells[0], (int*)(B + o_cnt), (int*)(B + o_ca), (int*)(B + o_cb), (const double*)(B + o_va),
+          (const int*)(B + o_ta), nta, (float4*)(B + o_tba), (const double*)(B + o_vb), (const int*)(B + o_tb), ntb,
+          (float4*)(B + o_tbb));
+  VTRY(exclusive_scan_u32_to_u64(ctx, (const uint32_t*)(B + o_cnt), (uint64_t*)(B + o_off), ncell));
+  VLAUNCH(ctx, kKHausdorff, grid_for((int64_t)na + nb, 256, 8LL * ctx->sm_count), 256, 0, hscatter2_kernel, na, nb,
+          cells[0], (const int*)(B + o_ca), (const int*)(B + o_cb), offs, (int*)(B + o_fill), (int*)(B + o_oa),
+          (int*)(B + o_ob));
+  VLAUNCH(ctx, kKHausdorff, grid_for((int64_t)ncell + 2 + na + nb, 256, 8LL * ctx->sm_count), 256, 0,
+          hfinish_kernel, cells[0], cells[1], offs, (int*)(B + o_sa), (int*)(B + o_sb), (const double*)(B + o_xa),
+          (const int*)(B + o_oa), na, (float4*)(B + o_pa), (const double*)(B + o_xb), (const int*)(B + o_ob), nb,
+          (float4*)(B + o_pb));
+  g[0].start = (const int*)(B + o_sa);
+  g[1].start = (const int*)(B + o_sb);
+  g[0].order = (const int*)(B + o_oa);
+  g[1].order = (const int*)(B + o_ob);
+  g[0].spts = (const float4*)(B + o_pa);
+  g[1].spts = (const float4*)(B + o_pb);
   unsigned long long* mx = (unsigned long long*)(B + o_mx);
-  VLAUNCH(ctx, kKHausdorff, grid_for(nta, 256, 8LL * ctx->sm_count), 256, 0, htri_bounds_kernel,
-          (const double*)(B + o_va), (const int*)(B + o_ta), nta, (float4*)(B + o_tba));
-  VLAUNCH(ctx, kKHausdorff, grid_for(ntb, 256, 8LL * ctx->sm_count), 256, 0, htri_bounds_kernel,
-          (const double*)(B + o_vb), (const int*)(B + o_tb), ntb, (float4*)(B + o_tbb));
   // Margin of the FP32 lower bounds: the plane evaluation's rounding (normal
   // and offset rounded to float, a few ulps of the largest coordinate), with
   // room to spare; the box gap is conservative by construction.
@@ -725,12 +719,10 @@ extern "C" int visacd_face_hausdorff(visacd_ctx* ctx, const double* va, int32_t 
   const int ntot = na + nb;
   uint32_t* vals = (uint32_t*)(B + o_vals);
   unsigned* far = (unsigned*)(B + o_mx + 8);  // zeroed with the maximum
-  float* ubs = (float*)(B + o_keys);
-  int* farlist = (int*)(B + o_keys2);
-  VLAUNCH(ctx, kKHausdorffBound, grid_for(nb, 128, 8LL * ctx->sm_count), 128, 0, hbound_kernel, sd0, 0,
-          g[1].order, ubs, vals, 0, far, farlist);
-  VLAUNCH(ctx, kKHausdorffBound, grid_for(na, 128, 8LL * ctx->sm_count), 128, 0, hbound_kernel, sd1, 1,
-          g[0].order, ubs, vals, nb, far, farlist);
+  float* ubs = (float*)(B + o_ub);
+  int* farlist = (int*)(B + o_far);
+  VLAUNCH(ctx, kKHausdorffBound, grid_for(ntot, 128, 8LL * ctx->sm_count), 128, 0, hbound_kernel, sd0, g[1].order,
+          sd1, g[0].order, ubs, vals, far, farlist);
   // The queries without a bound one warp each, then the rest with pruning.
   VLAUNCH(ctx, kKHausdorffHead, grid_for(32LL * ntot, 128, 8LL * ctx->sm_count), 128, 0, hhead_kernel, sd0, sd1,
           (const uint32_t*)vals, (const int*)farlist, (const unsigned*)far, tmargin, mx);
