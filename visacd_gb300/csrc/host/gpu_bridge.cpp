@@ -2,6 +2,7 @@
 
 #include <chrono>
 #include <cstdlib>
+#include <memory>
 #include <mutex>
 #include <stdexcept>
 #include <string>
@@ -39,6 +40,7 @@ namespace {
 thread_local visacd_ctx* tl_ctx = nullptr;   // a process_batch worker's own context
 thread_local visacd_lp* tl_lp = nullptr;     // the proposer on this thread's context
 thread_local visacd_ctx* tl_lp_ctx = nullptr;
+thread_local std::string tl_lp_path;             // the weights file it was made from
 }  // namespace
 
 ThreadContext::ThreadContext(int device) {
@@ -232,10 +234,10 @@ std::vector<double> hull_distances(const MeshList& hulls, const std::vector<std:
 
 namespace {
 // Proposer parameters by file path, read once per path.
-const std::vector<float>& proposer_params(const std::string& path) {
+std::shared_ptr<const std::vector<float>> proposer_params(const std::string& path) {
   static std::mutex mu;
   static std::string loaded_path;
-  static std::vector<float> params;
+  static std::shared_ptr<const std::vector<float>> params;
   std::lock_guard<std::mutex> lock(mu);
   if (path.empty())
     throw std::runtime_error("plane_proposer is 'learned' but config.proposer_weights is empty");
@@ -250,7 +252,7 @@ const std::vector<float>& proposer_params(const std::string& path) {
     if (got != (size_t)n || extra)
       throw std::runtime_error("proposer weights " + path + " must hold exactly " + std::to_string(n) +
                                " float32 values");
-    params.swap(p);
+    params = std::make_shared<const std::vector<float>>(std::move(p));
     loaded_path = path;
   }
   return params;
@@ -260,12 +262,13 @@ const std::vector<float>& proposer_params(const std::string& path) {
 std::vector<Plane> propose_planes(const Mesh& mesh) {
   double t0 = now_ms();
   visacd_ctx* ctx = context();
-  if (!tl_lp || tl_lp_ctx != ctx) {
+  if (!tl_lp || tl_lp_ctx != ctx || tl_lp_path != config().proposer_weights) {
     if (tl_lp) visacd_lp_destroy(tl_lp);
     tl_lp = nullptr;
-    const auto& p = proposer_params(config().proposer_weights);
-    check(visacd_lp_create(ctx, p.data(), 0, &tl_lp), "visacd_lp_create");
+    const auto p = proposer_params(config().proposer_weights);
+    check(visacd_lp_create(ctx, p->data(), 0, &tl_lp), "visacd_lp_create");
     tl_lp_ctx = ctx;
+    tl_lp_path = config().proposer_weights;
   }
   // The part's frame: bounding-box centre and half of the longest extent.
   auto b = bbox(mesh);
