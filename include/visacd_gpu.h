@@ -236,6 +236,17 @@ int visacd_face_hausdorff(visacd_ctx* ctx, const double* va, int32_t nva, const 
                           const double* vb, int32_t nvb, const int32_t* tb, int32_t ntb,
                           const double* xb, const int32_t* idb, int32_t nb, double* out);
 
+/* visacd_face_hausdorff for a caller that only needs values at or above
+   `floor` (the largest of several concavities, lib/src/process.cpp:208-236):
+   *out is the exact distance when that is >= floor, and otherwise some value
+   strictly below floor. Sample terms whose upper bound lies below floor are
+   not evaluated. floor <= 0 gives the exact distance. */
+int visacd_face_hausdorff_floor(visacd_ctx* ctx, const double* va, int32_t nva, const int32_t* ta,
+                                int32_t nta, const double* xa, const int32_t* ida, int32_t na,
+                                const double* vb, int32_t nvb, const int32_t* tb, int32_t ntb,
+                                const double* xb, const int32_t* idb, int32_t nb, double floor,
+                                double* out);
+
 /* Independent segment-triangle decisions with the visibility kernel's test
    (FP32 filter with a rigorous rounding bound, FP64 re-decision inside it;
    lib/ptx/ray_segments.cu:49-111 semantics, tmin 0.001): seg S x 6 (p, q),

@@ -83,3 +83,46 @@ def test_gpu_concavity_metric_equals_host(visacd):
         V.set_seed(5)
         b = V._compute_hb(v, t, hv["vertices"], hv["triangles"], 10000)
         assert a == b
+
+
+def test_face_hausdorff_floor(visacd):
+    """visacd_face_hausdorff_floor: exact at or above the floor, below it otherwise."""
+    from visacd_gb300 import _native as N
+    from visacd_gb300 import visacd as V
+    ctx = N.Context(0)
+    try:
+        for seed, level in [(3, 3), (8, 4)]:
+            v, t = mg.displaced_blob(level, seed=seed)
+            hv = V._convex_hull(v)
+            V.set_seed(seed)
+            xa, ia = V._sample_points(v, t, 3000)
+            xb, ib = V._sample_points(hv["vertices"], hv["triangles"], 3000)
+            args = (v, t, xa, ia, hv["vertices"], hv["triangles"], xb, ib)
+            exact = ctx.face_hausdorff(*args)
+            assert exact > 0
+            for f in (0.0, 0.3 * exact, exact * (1 - 1e-12), exact):
+                assert ctx.face_hausdorff(*args, floor=f) == exact
+            for f in (exact * (1 + 1e-12), 1.5 * exact, 10.0):
+                assert ctx.face_hausdorff(*args, floor=f) < f
+    finally:
+        ctx.close()
+
+
+def test_process_gpu_metric_equals_host_metric(visacd):
+    """process() with the floored GPU metric (values evaluated largest volume
+    term first) picks the same parts and returns the same concavity as with
+    the exact host metric evaluated in part order."""
+    from visacd_gb300 import visacd as V
+    v, t = mg.displaced_blob(3, seed=21)
+    out = []
+    for gpu in (False, True):
+        V.config.gpu_concavity = gpu
+        V.set_seed(3)
+        try:
+            out.append(V.process(_mesh(V, v, t), 0.02, 10))
+        finally:
+            V.config.gpu_concavity = True
+    a, b = out
+    assert a.num_parts == b.num_parts and a.concavity == b.concavity
+    for pa, pb in zip(a.parts, b.parts):
+        np.testing.assert_array_equal(np.array(pa.vertices), np.array(pb.vertices))

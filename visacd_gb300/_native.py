@@ -24,6 +24,7 @@ EXPORTED = [
     "visacd_vis_variant_count", "visacd_ctx_set_vis_variant", "visacd_autotune_visibility",
     "visacd_score_planes", "visacd_score_planes_noalloc", "classify_and_rate_planes",
     "visacd_clip", "visacd_clip_fetch", "visacd_measure_fp32_peak", "visacd_face_hausdorff",
+    "visacd_face_hausdorff_floor",
     "visacd_batch_create", "visacd_batch_run", "visacd_batch_results", "visacd_batch_info",
     "visacd_batch_destroy",
     "visacd_lp_param_count", "visacd_lp_create", "visacd_lp_destroy", "visacd_lp_get_params",
@@ -105,6 +106,8 @@ def load() -> C.CDLL:
     lib.visacd_batch_destroy.argtypes = [P]
     lib.visacd_face_hausdorff.argtypes = [P, P, i32, P, i32, P, P, i32, P, i32, P, i32, P, P, i32,
                                           C.POINTER(C.c_double)]
+    lib.visacd_face_hausdorff_floor.argtypes = [P, P, i32, P, i32, P, P, i32, P, i32, P, i32, P, P, i32,
+                                                C.c_double, C.POINTER(C.c_double)]
     lib.visacd_clip_fetch.argtypes = [P, P, P, P, P, P, P]
     lib.classify_and_rate_planes.argtypes = [P, P, P, P, C.c_int, C.c_int, C.c_int]
     lib.classify_and_rate_planes.restype = None
@@ -295,16 +298,24 @@ class Context:
         return ov, ot
 
     # ---- concavity metric --------------------------------------------------
-    def face_hausdorff(self, va, ta, xa, ida, vb, tb, xb, idb) -> float:
-        """Sampled symmetric face Hausdorff distance (visacd_face_hausdorff)."""
+    def face_hausdorff(self, va, ta, xa, ida, vb, tb, xb, idb, floor: float | None = None) -> float:
+        """Sampled symmetric face Hausdorff distance (visacd_face_hausdorff).
+        With `floor`: exact when the distance is >= floor, else some value
+        below floor (visacd_face_hausdorff_floor)."""
         f = lambda a, c: np.ascontiguousarray(np.asarray(a, dtype=np.float64)).reshape(-1, c)
         g = lambda a, c: np.ascontiguousarray(np.asarray(a, dtype=np.int32)).reshape(-1, c)
         va, xa, vb, xb = f(va, 3), f(xa, 3), f(vb, 3), f(xb, 3)
         ta, tb, ida, idb = g(ta, 3), g(tb, 3), g(ida, 1), g(idb, 1)
         out = C.c_double()
-        _check(lib().visacd_face_hausdorff(self._h, _ptr(va), len(va), _ptr(ta), len(ta), _ptr(xa), _ptr(ida),
-                                           len(xa), _ptr(vb), len(vb), _ptr(tb), len(tb), _ptr(xb), _ptr(idb),
-                                           len(xb), C.byref(out)), "visacd_face_hausdorff")
+        if floor is None:
+            _check(lib().visacd_face_hausdorff(self._h, _ptr(va), len(va), _ptr(ta), len(ta), _ptr(xa), _ptr(ida),
+                                               len(xa), _ptr(vb), len(vb), _ptr(tb), len(tb), _ptr(xb), _ptr(idb),
+                                               len(xb), C.byref(out)), "visacd_face_hausdorff")
+        else:
+            _check(lib().visacd_face_hausdorff_floor(self._h, _ptr(va), len(va), _ptr(ta), len(ta), _ptr(xa),
+                                                     _ptr(ida), len(xa), _ptr(vb), len(vb), _ptr(tb), len(tb),
+                                                     _ptr(xb), _ptr(idb), len(xb), float(floor), C.byref(out)),
+                   "visacd_face_hausdorff_floor")
         return out.value
 
     def segment_triangle_tests(self, seg, tri):

@@ -272,8 +272,12 @@ __device__ __forceinline__ float warp_take_min(const float (&fd)[kKnnF], const i
 // has kKnnF smaller ones in that lane alone); a warp tournament takes them in
 // order. Same stop rule, same FP32-to-FP64 selection proof and the same term
 // as query_term; returns false (on all lanes) when the proof fails, and the
-// caller then uses query_term.
-__device__ bool query_term_warp(const HSide& S, int qi, double& term) {
+// caller then uses query_term. Returns kTermSkipped (on all lanes) as soon as
+// the nearest sample found bounds the term at or below *out_max, or strictly
+// below `floor`: such a term cannot change the result.
+constexpr int kTermOk = 0, kTermUnproven = 1, kTermSkipped = 2;
+__device__ int query_term_warp(const HSide& S, int qi, double floor, const unsigned long long* out_max,
+                               double& term) {
   const int lane = threadIdx.x & 31;
   const HGrid& G = S.G;
   const double q[3] = {S.Q[3 * (int64_t)qi], S.Q[3 * (int64_t)qi + 1], S.Q[3 * (int64_t)qi + 2]};
@@ -317,6 +321,15 @@ __device__ bool query_term_warp(const HSide& S, int qi, double& term) {
     }
     for (int o = 16; o; o >>= 1) seen += __shfl_xor_sync(0xffffffffu, seen, o);
     total += seen;
+    if (seen > 0) {
+      // The term is at most the nearest sample's distance, itself at most the
+      // warp's smallest FP32 distance so far rounded upwards plus the bound.
+      float m = nf > 0 ? fd[0] : 3.4e38f;
+      for (int o = 16; o; o >>= 1) m = fminf(m, __shfl_xor_sync(0xffffffffu, m, o));
+      const double ub = (double)__fadd_ru(__fmul_ru(__fsqrt_ru(m), 1.0f + 1.0f / 1048576.0f), G.eabs);
+      const double cur = __longlong_as_double((long long)*(const volatile unsigned long long*)out_max);
+      if (__shfl_sync(0xffffffffu, (ub <= cur || ub < floor) ? 1 : 0, 0)) return kTermSkipped;
+    }
     if (total >= kKnn) {
       int ptr = 0, id;
       float v = 3.4e38f;
@@ -347,7 +360,7 @@ __device__ bool query_term_warp(const HSide& S, int qi, double& term) {
     const float v16 = __shfl_sync(0xffffffffu, myv, kKnnF - 1);
     const bool ok = __fsqrt_rd(v16) * (1.0f - 1.0f / 1048576.0f) >
                     __fadd_ru(__fadd_ru(__fmul_ru(__fsqrt_ru(g10), 1.0f + 1.0f / 1048576.0f), G.eabs), G.eabs);
-    if (!ok) return false;
+    if (!ok) return kTermUnproven;
   }
   // Exact FP64 distances of the (up to) kKnnF candidates, the 10 nearest kept
   // in order (insertion in candidate order, as query_term).
@@ -397,7 +410,7 @@ __device__ bool query_term_warp(const HSide& S, int qi, double& term) {
   }
   if (cmin > 10 && cnt > 0) cmin = __dsqrt_rn(bd[0]);
   term = cmin;
-  return true;
+  return kTermOk;
 }
 
 // Upper bound of every query's term, one thread per query in its own grid's
@@ -466,7 +479,7 @@ __global__ void __launch_bounds__(128) hbound_kernel(HSide S0, const int* __rest
 // the running maximum that prunes the rest.
 __global__ void __launch_bounds__(128) hhead_kernel(HSide A, HSide B, const uint32_t* __restrict__ vals,
                                                     const int* __restrict__ farlist,
-                                                    const unsigned* __restrict__ far, float tmargin,
+                                                    const unsigned* __restrict__ far, float tmargin, double floor,
                                                     unsigned long long* __restrict__ out_max) {
   const int head = (int)*far;
   const int warps = (gridDim.x * blockDim.x) >> 5;
@@ -475,7 +488,9 @@ __global__ void __launch_bounds__(128) hhead_kernel(HSide A, HSide B, const uint
     const int qi = (int)(v & 0x7FFFFFFFu);
     const HSide& S = (v >> 31) ? B : A;
     double term;
-    if (!query_term_warp(S, qi, term)) term = query_term(S, qi, tmargin);
+    const int status = query_term_warp(S, qi, floor, out_max, term);
+    if (status == kTermSkipped) continue;
+    if (status == kTermUnproven) term = query_term(S, qi, tmargin);
     if ((threadIdx.x & 31) == 0 && term < DBL_MAX)
       atomicMax(out_max, (unsigned long long)__double_as_longlong(term));
   }
@@ -484,16 +499,16 @@ __global__ void __launch_bounds__(128) hhead_kernel(HSide A, HSide B, const uint
 // Terms of the queries with a bound (both directions, each in its own grid's
 // cell order), maximum into out_max. A query whose bound does not exceed the
 // maximum found so far cannot raise it and is skipped: the result is the same
-// maximum.
+// maximum. So is a query whose bound lies strictly below `floor`.
 __global__ void __launch_bounds__(128) hquery_kernel(HSide A, HSide B, const float* __restrict__ ubs,
                                                      const uint32_t* __restrict__ vals, int end, float tmargin,
-                                                     unsigned long long* __restrict__ out_max) {
+                                                     double floor, unsigned long long* __restrict__ out_max) {
   double local = 0.0;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < end; e += gridDim.x * blockDim.x) {
     const float ub = ubs[e];
     if (!(ub < __int_as_float(0x7f800000))) continue;  // no bound: evaluated by hhead_kernel
     const double cur = __longlong_as_double((long long)*(volatile unsigned long long*)out_max);
-    if ((double)ub <= fmax(cur, local)) continue;
+    if ((double)ub <= fmax(cur, local) || (double)ub < floor) continue;
     const uint32_t v = vals[e];
     const int qi = (int)(v & 0x7FFFFFFFu);
     const double cmin = (v >> 31) ? query_term(B, qi, tmargin) : query_term(A, qi, tmargin);
@@ -604,11 +619,13 @@ namespace {
 size_t al(size_t x) { return (x + 255) & ~size_t(255); }
 }
 
-extern "C" int visacd_face_hausdorff(visacd_ctx* ctx, const double* va, int32_t nva, const int32_t* ta,
-                                     int32_t nta, const double* xa, const int32_t* ida, int32_t na,
-                                     const double* vb, int32_t nvb, const int32_t* tb, int32_t ntb,
-                                     const double* xb, const int32_t* idb, int32_t nb, double* out) {
+extern "C" int visacd_face_hausdorff_floor(visacd_ctx* ctx, const double* va, int32_t nva, const int32_t* ta,
+                                           int32_t nta, const double* xa, const int32_t* ida, int32_t na,
+                                           const double* vb, int32_t nvb, const int32_t* tb, int32_t ntb,
+                                           const double* xb, const int32_t* idb, int32_t nb, double floor,
+                                           double* out) {
   VCHECK(ctx && out, VISACD_ERR_INVALID_ARG, "face_hausdorff: null argument");
+  VCHECK(floor == floor, VISACD_ERR_INVALID_ARG, "face_hausdorff: floor is NaN");
   VCHECK(na > 0 && nb > 0 && nva > 0 && nvb > 0 && nta > 0 && ntb > 0, VISACD_ERR_INVALID_ARG,
          "face_hausdorff: empty input");
   VCUDA(cudaSetDevice(ctx->device));
@@ -725,9 +742,9 @@ extern "C" int visacd_face_hausdorff(visacd_ctx* ctx, const double* va, int32_t 
           sd1, g[0].order, ubs, vals, far, farlist);
   // The queries without a bound one warp each, then the rest with pruning.
   VLAUNCH(ctx, kKHausdorffHead, grid_for(32LL * ntot, 128, 8LL * ctx->sm_count), 128, 0, hhead_kernel, sd0, sd1,
-          (const uint32_t*)vals, (const int*)farlist, (const unsigned*)far, tmargin, mx);
+          (const uint32_t*)vals, (const int*)farlist, (const unsigned*)far, tmargin, floor, mx);
   VLAUNCH(ctx, kKHausdorffQuery, grid_for(ntot, 128, 8LL * ctx->sm_count), 128, 0, hquery_kernel, sd0, sd1,
-          (const float*)ubs, (const uint32_t*)vals, ntot, tmargin, mx);
+          (const float*)ubs, (const uint32_t*)vals, ntot, tmargin, floor, mx);
   unsigned long long* h = nullptr;
   VTRY(pinned(ctx, 8, (void**)&h));
   VCUDA(cudaMemcpyAsync(h, mx, 8, cudaMemcpyDeviceToHost, st));
@@ -736,4 +753,11 @@ extern "C" int visacd_face_hausdorff(visacd_ctx* ctx, const double* va, int32_t 
   memcpy(&r, h, 8);
   *out = r;
   return VISACD_OK;
+}
+
+extern "C" int visacd_face_hausdorff(visacd_ctx* ctx, const double* va, int32_t nva, const int32_t* ta,
+                                     int32_t nta, const double* xa, const int32_t* ida, int32_t na,
+                                     const double* vb, int32_t nvb, const int32_t* tb, int32_t ntb,
+                                     const double* xb, const int32_t* idb, int32_t nb, double* out) {
+  return visacd_face_hausdorff_floor(ctx, va, nva, ta, nta, xa, ida, na, vb, nvb, tb, ntb, xb, idb, nb, 0.0, out);
 }

@@ -12,7 +12,10 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <limits>
+#include <numeric>
 #include <queue>
+#include <random>
 #include <vector>
 
 #include "geometry.hpp"
@@ -21,6 +24,50 @@
 namespace visacd {
 
 constexpr double kPi = 3.14159265;  // the reference's constant (lib/include/cost.hpp:6)
+
+namespace {
+
+// The draws of std::discrete_distribution<size_t> over the same weights, made
+// faster: its result is the first index of the cumulative probabilities not
+// below a canonical uniform p, found here through a guide table (bucket
+// floor(p n) -> first index whose cumulative value reaches the bucket's
+// start) and a short forward scan; every result is checked to be that first
+// index, falling back to a binary search, so it equals the distribution's
+// draw for the same engine state.
+class DiscreteSampler {
+ public:
+  explicit DiscreteSampler(const std::discrete_distribution<size_t>& d) {
+    const auto prob = d.probabilities();
+    cp_.resize(prob.size());
+    std::partial_sum(prob.begin(), prob.end(), cp_.begin());
+    if (!cp_.empty()) cp_.back() = 1.0;
+    const size_t n = cp_.size();
+    scale_ = (double)n;
+    guide_.resize(n + 1);
+    size_t i = 0;
+    for (size_t j = 0; j <= n; ++j) {
+      const double lo = (double)j / scale_;
+      while (i < n && cp_[i] < lo) ++i;
+      guide_[j] = i;
+    }
+  }
+  size_t operator()(std::mt19937& eng) const {
+    const double p = std::generate_canonical<double, std::numeric_limits<double>::digits>(eng);
+    size_t j = (size_t)(p * scale_);
+    if (j >= guide_.size()) j = guide_.size() - 1;
+    size_t i = guide_[j];
+    if (i > 0 && cp_[i - 1] >= p) return std::lower_bound(cp_.begin(), cp_.end(), p) - cp_.begin();
+    while (i < cp_.size() && cp_[i] < p) ++i;
+    return i;
+  }
+
+ private:
+  std::vector<double> cp_;
+  std::vector<size_t> guide_;
+  double scale_ = 0;
+};
+
+}  // namespace
 
 void extract_point_set(const Mesh& m, std::vector<Vec3>& samples, std::vector<int>& tri_ids,
                        size_t resolution, double base, bool one_per_tri) {
@@ -52,10 +99,19 @@ void extract_point_set(const Mesh& m, std::vector<Vec3>& samples, std::vector<in
     samples.push_back(v);
     tri_ids.push_back((int)ti);
   };
-  for (size_t done = 0; done < resolution; ++done) {
-    size_t ti = pick(eng);
-    sample(ti);
-    touched[ti] = 1;
+  if (total > 0 && std::isfinite(total)) {
+    const DiscreteSampler fast(pick);
+    for (size_t done = 0; done < resolution; ++done) {
+      const size_t ti = fast(eng);
+      sample(ti);
+      touched[ti] = 1;
+    }
+  } else {
+    for (size_t done = 0; done < resolution; ++done) {
+      const size_t ti = pick(eng);
+      sample(ti);
+      touched[ti] = 1;
+    }
   }
   if (one_per_tri)
     for (size_t i = 0; i < m.triangles.size(); ++i)
@@ -190,22 +246,30 @@ double compute_rv3(const Mesh& c1, const Mesh& c2, const Mesh& ch) {
   return std::pow(3 * std::fabs(v1 + v2 - v3) / (4 * kPi), 1.0 / 3);
 }
 
-double compute_hb(const Mesh& a, const Mesh& b, unsigned int resolution) {
+void sample_hb(const Mesh& a, const Mesh& b, unsigned int resolution, HbSamples& s) {
   auto& tm = concavity_times();
   const auto t0 = std::chrono::steady_clock::now();
-  std::vector<Vec3> s1, s2;
-  std::vector<int> i1, i2;
-  extract_point_set(a, s1, i1, resolution, 1, true);
-  extract_point_set(b, s2, i2, resolution, 1, true);
-  const auto t1 = std::chrono::steady_clock::now();
-  tm.sample_ms += std::chrono::duration<double, std::milli>(t1 - t0).count();
-  tm.samples += (long long)(s1.size() + s2.size());
-  if (s1.empty() || s2.empty()) return kInf;
-  const double h = config().gpu_concavity ? gpu::face_hausdorff(a, s1, i1, b, s2, i2)
-                                          : face_hausdorff(a, s1, i1, b, s2, i2);
-  tm.hausdorff_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t1).count();
+  extract_point_set(a, s.s1, s.i1, resolution, 1, true);
+  extract_point_set(b, s.s2, s.i2, resolution, 1, true);
+  tm.sample_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  tm.samples += (long long)(s.s1.size() + s.s2.size());
+}
+
+double eval_hb(const Mesh& a, const Mesh& b, const HbSamples& s, double floor) {
+  if (s.s1.empty() || s.s2.empty()) return kInf;
+  auto& tm = concavity_times();
+  const auto t0 = std::chrono::steady_clock::now();
+  const double h = config().gpu_concavity ? gpu::face_hausdorff(a, s.s1, s.i1, b, s.s2, s.i2, floor)
+                                          : face_hausdorff(a, s.s1, s.i1, b, s.s2, s.i2);
+  tm.hausdorff_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   tm.calls++;
   return h;
+}
+
+double compute_hb(const Mesh& a, const Mesh& b, unsigned int resolution) {
+  HbSamples s;
+  sample_hb(a, b, resolution, s);
+  return eval_hb(a, b, s);
 }
 
 ConcavityTimes& concavity_times() {

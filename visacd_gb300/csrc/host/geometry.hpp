@@ -49,6 +49,16 @@ void extract_point_set(const Mesh& m, std::vector<Vec3>& samples, std::vector<in
 double compute_rv(const Mesh& a, const Mesh& b);
 double compute_rv3(const Mesh& c1, const Mesh& c2, const Mesh& ch);
 double compute_hb(const Mesh& a, const Mesh& b, unsigned int resolution);
+// compute_hb in two steps: the samples of both surfaces (the random draws, in
+// the reference's order), then the value. With floor > 0 the value is exact
+// when it is >= floor and some value below floor otherwise (the GPU skips the
+// sample terms that cannot reach floor); the host metric is always exact.
+struct HbSamples {
+  std::vector<Vec3> s1, s2;
+  std::vector<int> i1, i2;
+};
+void sample_hb(const Mesh& a, const Mesh& b, unsigned int resolution, HbSamples& s);
+double eval_hb(const Mesh& a, const Mesh& b, const HbSamples& s, double floor = 0.0);
 double compute_hb3(const Mesh& c1, const Mesh& c2, const Mesh& ch, unsigned int resolution);
 double compute_h(const Mesh& a, const Mesh& b, double k, unsigned int resolution);
 double compute_h3(const Mesh& c1, const Mesh& c2, const Mesh& ch, double k, unsigned int resolution);

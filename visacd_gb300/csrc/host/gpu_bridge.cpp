@@ -153,16 +153,18 @@ std::vector<double> score_planes(const std::vector<Plane>& planes, const std::ve
 }
 
 double face_hausdorff(const Mesh& A, const std::vector<Vec3>& XA, const std::vector<int>& idA,
-                      const Mesh& B, const std::vector<Vec3>& XB, const std::vector<int>& idB) {
+                      const Mesh& B, const std::vector<Vec3>& XB, const std::vector<int>& idB,
+                      double floor) {
   visacd_ctx* ctx = context();
   double out = 0;
-  check(visacd_face_hausdorff(ctx, reinterpret_cast<const double*>(A.vertices.data()), (int32_t)A.vertices.size(),
+  check(visacd_face_hausdorff_floor(ctx, reinterpret_cast<const double*>(A.vertices.data()), (int32_t)A.vertices.size(),
                               reinterpret_cast<const int32_t*>(A.triangles.data()), (int32_t)A.triangles.size(),
                               reinterpret_cast<const double*>(XA.data()), idA.data(), (int32_t)XA.size(),
                               reinterpret_cast<const double*>(B.vertices.data()), (int32_t)B.vertices.size(),
                               reinterpret_cast<const int32_t*>(B.triangles.data()), (int32_t)B.triangles.size(),
-                              reinterpret_cast<const double*>(XB.data()), idB.data(), (int32_t)XB.size(), &out),
-        "visacd_face_hausdorff");
+                              reinterpret_cast<const double*>(XB.data()), idB.data(), (int32_t)XB.size(), floor,
+                              &out),
+        "visacd_face_hausdorff_floor");
   return out;
 }
 

@@ -59,9 +59,11 @@ void sdf_remesh(Mesh& m, double scale, double level);
 std::vector<double> hull_distances(const MeshList& hulls, const std::vector<std::pair<int, int>>& pairs,
                                    double cutoff);
 
-// Sampled face Hausdorff distance on the GPU (visacd_face_hausdorff).
+// Sampled face Hausdorff distance on the GPU (visacd_face_hausdorff_floor):
+// exact when it is >= floor, otherwise some value below floor.
 double face_hausdorff(const Mesh& A, const std::vector<Vec3>& XA, const std::vector<int>& idA,
-                      const Mesh& B, const std::vector<Vec3>& XB, const std::vector<int>& idB);
+                      const Mesh& B, const std::vector<Vec3>& XB, const std::vector<int>& idB,
+                      double floor = 0.0);
 
 // Per-thread call counters.
 struct Counters {

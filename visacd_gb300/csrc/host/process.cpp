@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstdio>
 #include <iostream>
+#include <numeric>
 #include <sstream>
 #include <string>
 #include <thread>
@@ -229,11 +230,31 @@ int get_part_with_highest_concavity(const MeshList& parts, double& max_concavity
   for (int i = 0; i < (int)parts.size(); ++i) hulls[i] = convex_hull(parts[i].vertices, true);
   concavity_times().hull_ms +=
       std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  // compute_h(part, hull, 0.3, 3000) of every part, of which only the first
+  // maximum and its value are used. The samples are drawn in the reference's
+  // order (part i, then its hull, for i = 0, 1, ...); the sampled terms are
+  // then evaluated in descending order of the volume term with the running
+  // maximum as the floor, so a part below it gets some value below it (never
+  // the maximum) and every other part its exact value.
+  const int n = (int)parts.size();
+  std::vector<HbSamples> smp(n);
+  std::vector<double> c(n);
+  for (int i = 0; i < n; ++i) {
+    c[i] = compute_rv(parts[i], hulls[i]) * 0.3;
+    sample_hb(parts[i], hulls[i], 3000, smp[i]);
+  }
+  std::vector<int> order(n);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return c[a] > c[b]; });
+  double run = max_concavity;
+  for (int i : order) {
+    c[i] = std::max(c[i], eval_hb(parts[i], hulls[i], smp[i], std::max(run, 0.0)));
+    run = std::max(run, c[i]);
+  }
   int idx = -1;
-  for (int i = 0; i < (int)parts.size(); ++i) {
-    double c = compute_h(parts[i], hulls[i], 0.3, 3000);
-    if (c > max_concavity) {
-      max_concavity = c;
+  for (int i = 0; i < n; ++i) {
+    if (c[i] > max_concavity) {
+      max_concavity = c[i];
       idx = i;
     }
   }
@@ -241,9 +262,22 @@ int get_part_with_highest_concavity(const MeshList& parts, double& max_concavity
 }
 
 double compute_final_concavity(const MeshList& parts, const MeshList& hulls) {
+  // The largest compute_hb(part, hull, 10000): samples drawn in order, values
+  // evaluated with the running maximum as the floor (largest volume term
+  // first), as in get_part_with_highest_concavity.
+  const size_t n = parts.size();
+  std::vector<HbSamples> smp(n);
+  std::vector<double> rv(n);
+  for (size_t i = 0; i < n; ++i) {
+    rv[i] = compute_rv(parts[i], hulls[i]);
+    sample_hb(parts[i], hulls[i], 10000, smp[i]);
+  }
+  std::vector<size_t> order(n);
+  std::iota(order.begin(), order.end(), size_t(0));
+  std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return rv[a] > rv[b]; });
   double h = 0;
-  for (size_t i = 0; i < parts.size(); ++i) {
-    double c = compute_hb(parts[i], hulls[i], 10000);
+  for (size_t i : order) {
+    const double c = eval_hb(parts[i], hulls[i], smp[i], h);
     if (c > h) h = c;
   }
   return h;
