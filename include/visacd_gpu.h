@@ -55,8 +55,8 @@ typedef struct visacd_batch visacd_batch;
 typedef struct {
   int64_t pairs_tested;   /* pairs whose segment was traced (mask applied) */
   int64_t n_edges;        /* visibility edges: cage hit and no self hit */
-  int64_t self_hits;      /* pairs whose segment crosses the part itself */
-  int64_t cage_hits;      /* pairs with no self hit whose segment leaves the cage */
+  int64_t self_hits;      /* pairs whose segment leaves the cage and crosses the part */
+  int64_t cage_hits;      /* pairs whose segment leaves the cage (tested first) */
   int64_t fp64_rechecks;  /* segment-triangle tests re-decided in FP64 */
   int64_t degenerate;     /* pairs with coincident endpoints (never edges) */
   int64_t node_visits;    /* BVH node records fetched (per warp packet) */

@@ -98,13 +98,15 @@ __global__ void __launch_bounds__(kVisThreads, 6)
     make_seg(s, p, q, (int)i, (int)j);
     bool active = valid && seg_len(s) > 0.f;
     if (!__ballot_sync(0xffffffffu, active)) continue;
-    const bool self_hit = packet_any_hit(P.self_nodes, P.self_tris, P.self_nt, s, P.pts, active, wstk,
-                                         rechecks, status_bits, visits, tri_tests);
-    active = active && !self_hit;
+    // The cage first; the self test only for segments that leave it.
     s.exclude = false;
     const bool cage_hit = packet_any_hit(P.cage_nodes, P.cage_tris, P.cage_nt, s, P.pts, active, wstk,
                                          rechecks, status_bits, visits, tri_tests);
-    if (active && cage_hit) {
+    active = active && cage_hit;
+    s.exclude = true;
+    const bool self_hit = packet_any_hit(P.self_nodes, P.self_tris, P.self_nt, s, P.pts, active, wstk,
+                                         rechecks, status_bits, visits, tri_tests);
+    if (active && !self_hit) {
       const int64_t k = row_start(i, P.n) + (int64_t)(j - i - 1);
       atomicOr(&bitset[P.word_begin + (k >> 5)], 1u << (k & 31));
     }

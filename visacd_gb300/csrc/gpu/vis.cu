@@ -14,8 +14,9 @@
 //  * Warp-packet any-hit traversal of a 64-byte-node LBVH (both child boxes per
 //    node): the warp follows one path (ballot of per-lane box tests), node
 //    records are broadcast loads, a per-warp stack lives in shared memory; the
-//    self test runs first and the cage test only for lanes whose segment does
-//    not cross the part.
+//    cage test runs first and the self test only for lanes whose segment
+//    leaves the cage (few: most vertex pairs of a part are interior chords,
+//    which cross neither surface).
 //  * Segment-triangle test: edge functions W = D.(B x C), ... relative to the
 //    origin in FP32 with an a-priori rounding bound (8 roundings per term,
 //    bounded by 17u |D|_1 L^2). Only tests whose signs fall inside the bound
@@ -130,15 +131,17 @@ __global__ void __launch_bounds__(kVisThreads, MINB) visibility_kernel(VisParams
       active = false;
     }
     if (!__ballot_sync(0xffffffffu, active)) continue;
-    const bool self_hit = packet_any_hit(P.self_nodes, P.self_tris, P.self_nt, s, P.pts, active, wstk,
-                                         rechecks, status_bits, visits, tri_tests);
-    if (active && self_hit) ++c_self;
-    active = active && !self_hit;
+    // The cage first: few segments leave it, so the self test runs for few.
     s.exclude = false;
     const bool cage_hit = packet_any_hit(P.cage_nodes, P.cage_tris, P.cage_nt, s, P.pts, active, wstk,
                                          rechecks, status_bits, visits, tri_tests);
-    if (active && cage_hit) {
-      ++c_cage;
+    if (active && cage_hit) ++c_cage;
+    active = active && cage_hit;
+    s.exclude = true;
+    const bool self_hit = packet_any_hit(P.self_nodes, P.self_tris, P.self_nt, s, P.pts, active, wstk,
+                                         rechecks, status_bits, visits, tri_tests);
+    if (active && self_hit) ++c_self;
+    if (active && !self_hit) {
       ++c_edges;
       const int64_t k = row_start(i, n) + (int64_t)(j - i - 1);
       atomicOr(&P.bitset[k >> 5], 1u << (k & 31));
