@@ -82,3 +82,20 @@ def test_gpu_clip_raw_outputs(ctx, V):
     np.testing.assert_array_equal(r["neg_tris"], a[1]["triangles"][: r["n_neg"]])
     np.testing.assert_array_equal(r["border"], a[0]["vertices"][r["nv_pos"]:])
     assert r["n_touching"] > 0 and r["n_border_edges"] >= r["n_border"] - 2
+
+
+def test_gpu_clip_both_resolver_modes(ctx, V):
+    """The ordered resolver keeps its tables in shared memory up to 1024
+    touching triangles and in global memory beyond: both equal the host."""
+    pl = np.array([0.3, 0.5, 0.81])
+    pl = list(pl / np.linalg.norm(pl)) + [0.01]
+    seen = []
+    for level in (5, 7):
+        v, t = mg.icosphere(level)
+        seen.append(ctx.clip(v, t, pl)["n_touching"])
+        a, am1, am2 = V._clip(v, t, pl)
+        b, bm1, bm2 = V._clip_gpu(v, t, pl)
+        np.testing.assert_array_equal(am1, bm1)
+        np.testing.assert_array_equal(am2, bm2)
+        _same(a, b)
+    assert seen[0] <= 1024 < seen[1]

@@ -143,7 +143,20 @@ struct Resolver {
   int bcap;
   int max_border;
   ClipCounters* cnt;
+  unsigned* n_border;   // border point count (cnt->n_border, or a shared-memory copy)
+  unsigned* n_bedges;   // border edge count (likewise)
 };
+
+// Shared-memory mode of the resolver: up to kSmemTouch touching triangles have
+// at most 3 border points each, at most 6 directed-edge entries each and at
+// most one border edge each, so tables of these capacities never fill.
+constexpr int kSmemTouch = 1024;
+constexpr int kSmemBorder = 3 * kSmemTouch + 16;
+constexpr int kSmemEcap = 8192;
+constexpr int kSmemBcap = 4096;
+constexpr int kChunk = 32;
+constexpr size_t kResolveSmem = (size_t)kSmemBorder * 24 + (size_t)kSmemEcap * 12 + (size_t)kSmemBcap * 8 +
+                                (size_t)kChunk * 18 * 8 + (size_t)kChunk * 7 * 4 + 16;
 
 // One warp resolves the touching triangles in order. Lane 0 owns every table
 // update; the position scan runs across the 32 lanes (first match = smallest
@@ -196,7 +209,7 @@ __device__ int append_border(Resolver& R, const double* p, int n) {
     R.border[3 * n] = p[0];
     R.border[3 * n + 1] = p[1];
     R.border[3 * n + 2] = p[2];
-    R.cnt->n_border = n + 1;
+    *R.n_border = n + 1;
     return n;
   }
   R.cnt->overflow = 1;
@@ -208,7 +221,7 @@ __device__ int vertex_point(Resolver& R, int id) {
   int have = lane0() ? R.vmap[id] : 0;
   have = __shfl_sync(0xffffffffu, have, 0);
   if (have >= 0) return have;
-  const int n = (int)R.cnt->n_border;
+  const int n = (int)*(volatile unsigned*)R.n_border;
   int f = find_near(R, R.v + 3 * (int64_t)id, n);
   if (lane0()) {
     if (f < 0) f = append_border(R, R.v + 3 * (int64_t)id, n);
@@ -228,7 +241,7 @@ __device__ int edge_point(Resolver& R, int a, int b, const double* p) {
   }
   have = __shfl_sync(0xffffffffu, have, 0);
   if (have >= 0) return have;
-  const int n = (int)R.cnt->n_border;
+  const int n = (int)*(volatile unsigned*)R.n_border;
   int f = find_near(R, p, n);
   if (lane0()) {
     if (f < 0) f = append_border(R, p, n);
@@ -249,10 +262,10 @@ __device__ void add_bedge(Resolver& R, int a, int b) {
     if (R.bkeys[2 * h] == -1) {
       R.bkeys[2 * h] = lo;
       R.bkeys[2 * h + 1] = hi;
-      unsigned k = R.cnt->n_bedges;
+      unsigned k = *R.n_bedges;
       R.bedge_a[k] = a;
       R.bedge_b[k] = b;
-      R.cnt->n_bedges = k + 1;
+      *R.n_bedges = k + 1;
       return;
     }
   }
@@ -261,19 +274,78 @@ __device__ void add_bedge(Resolver& R, int a, int b) {
 
 __device__ __forceinline__ int bref(int b) { return -b - 1; }
 
+// With at most kSmemTouch touching triangles the tables, the border points and
+// the counters live in shared memory (copied out at the end); otherwise in
+// the global buffers sized by the triangle count. Either way the triangles
+// are staged 32 at a time, one lane each, together with everything about them
+// that does not depend on the tables (sides with the coplanar rule, the three
+// edge-plane intersections): the FP64 work runs once per triangle across the
+// lanes, and the ordered walk reads the results from shared memory.
 __global__ void __launch_bounds__(kClipResolveThreads) clip_resolve_kernel(
     const double* __restrict__ v, const int* __restrict__ t, const double* __restrict__ plp,
     const signed char* __restrict__ side, const int* __restrict__ list, Resolver R,
     PieceSlot* __restrict__ slots, unsigned char* __restrict__ keep_pos,
     unsigned char* __restrict__ keep_neg) {
+  extern __shared__ __align__(16) unsigned char rsm[];
+  double* sm_border = reinterpret_cast<double*>(rsm);
+  int* sm_ekeys = reinterpret_cast<int*>(sm_border + 3 * kSmemBorder);
+  int* sm_evals = sm_ekeys + 2 * kSmemEcap;
+  int* sm_bkeys = sm_evals + kSmemEcap;
+  double* ch_p = reinterpret_cast<double*>(sm_bkeys + 2 * kSmemBcap);  // kChunk x 9 vertex coordinates
+  double* ch_pi = ch_p + kChunk * 9;                                   // kChunk x 9 edge intersections
+  int* ch_id = reinterpret_cast<int*>(ch_pi + kChunk * 9);             // kChunk x 3
+  int* ch_s = ch_id + kChunk * 3;                                      // kChunk x 3
+  int* ch_f = ch_s + kChunk * 3;                                       // kChunk intersection flags
+  unsigned* sm_cnt = reinterpret_cast<unsigned*>(ch_f + kChunk);       // n_border, n_bedges
+  const int lane = threadIdx.x & 31;
   double pl[4] = {plp[0], plp[1], plp[2], plp[3]};
   const int ntouch = (int)R.cnt->n_touch;
+  double* const global_border = R.border;
+  const bool smem = ntouch <= kSmemTouch;
+  if (smem) {
+    for (int i = lane; i < 2 * kSmemEcap; i += 32) sm_ekeys[i] = -1;
+    for (int i = lane; i < 2 * kSmemBcap; i += 32) sm_bkeys[i] = -1;
+    if (lane == 0) sm_cnt[0] = sm_cnt[1] = 0;
+    R.border = sm_border;
+    R.ekeys = sm_ekeys;
+    R.evals = sm_evals;
+    R.ecap = kSmemEcap;
+    R.bkeys = sm_bkeys;
+    R.bcap = kSmemBcap;
+    R.max_border = kSmemBorder;
+    R.n_border = sm_cnt;
+    R.n_bedges = sm_cnt + 1;
+  } else {
+    R.n_border = &R.cnt->n_border;
+    R.n_bedges = &R.cnt->n_bedges;
+  }
+  __syncwarp();
   for (int li = 0; li < ntouch; ++li) {
-    const int tri = list[li];
-    const int id[3] = {t[3 * tri], t[3 * tri + 1], t[3 * tri + 2]};
-    const double* p[3] = {v + 3 * (int64_t)id[0], v + 3 * (int64_t)id[1], v + 3 * (int64_t)id[2]};
-    int s[3] = {side[id[0]], side[id[1]], side[id[2]]};
-    if (s[0] == 0 && s[1] == 0 && s[2] == 0) s[0] = s[1] = s[2] = coplanar_side(p[0], p[1], p[2], pl);
+    const int cc = li % kChunk;
+    if (cc == 0) {
+      __syncwarp();
+      if (li + lane < ntouch) {
+        const int tr = list[li + lane];
+        int sl[3];
+        for (int k = 0; k < 3; ++k) {
+          const int vk = t[3 * tr + k];
+          ch_id[3 * lane + k] = vk;
+          sl[k] = side[vk];
+          for (int a = 0; a < 3; ++a) ch_p[9 * lane + 3 * k + a] = v[3 * (int64_t)vk + a];
+        }
+        const double* q = ch_p + 9 * lane;
+        if (sl[0] == 0 && sl[1] == 0 && sl[2] == 0) sl[0] = sl[1] = sl[2] = coplanar_side(q, q + 3, q + 6, pl);
+        int fl = 0;
+        for (int e = 0; e < 3; ++e)
+          if (intersect_segment(pl, q + 3 * e, q + 3 * ((e + 1) % 3), ch_pi + 9 * lane + 3 * e)) fl |= 1 << e;
+        for (int k = 0; k < 3; ++k) ch_s[3 * lane + k] = sl[k];
+        ch_f[lane] = fl;
+      }
+      __syncwarp();
+    }
+    const int id[3] = {ch_id[3 * cc], ch_id[3 * cc + 1], ch_id[3 * cc + 2]};
+    const double* p[3] = {ch_p + 9 * cc, ch_p + 9 * cc + 3, ch_p + 9 * cc + 6};
+    const int s[3] = {ch_s[3 * cc], ch_s[3 * cc + 1], ch_s[3 * cc + 2]};
     const int sum = s[0] + s[1] + s[2];
     const int nzero = (s[0] == 0) + (s[1] == 0) + (s[2] == 0);
     PieceSlot out;
@@ -321,9 +393,9 @@ __global__ void __launch_bounds__(kClipResolveThreads) clip_resolve_kernel(
           if (k != z) keep(sg > 0, id[k]);
       }
     } else {
-      double pi[3][3];
-      bool f[3];
-      for (int e = 0; e < 3; ++e) f[e] = intersect_segment(pl, p[e], p[(e + 1) % 3], pi[e]);
+      const double* pi[3] = {ch_pi + 9 * cc, ch_pi + 9 * cc + 3, ch_pi + 9 * cc + 6};
+      const int fl = ch_f[cc];
+      const bool f[3] = {(fl & 1) != 0, (fl & 2) != 0, (fl & 4) != 0};
       int e = -1;
       if (f[0] && f[1] && !f[2]) e = 0;
       else if (f[1] && f[2] && !f[0]) e = 1;
@@ -404,6 +476,14 @@ __global__ void __launch_bounds__(kClipResolveThreads) clip_resolve_kernel(
     }
     if (lane0()) slots[li] = out;
     __syncwarp();
+  }
+  if (smem) {
+    const unsigned nb = sm_cnt[0];
+    for (unsigned i = lane; i < 3 * nb; i += 32) global_border[i] = sm_border[i];
+    if (lane == 0) {
+      R.cnt->n_border = nb;
+      R.cnt->n_bedges = sm_cnt[1];
+    }
   }
 }
 
@@ -558,7 +638,8 @@ extern "C" int visacd_clip(visacd_ctx* ctx, const double* verts, int32_t nv, con
   VTRY(exclusive_scan_u32_to_u64(ctx, tf, toff, nt));
   VLAUNCH(ctx, kKClip, gt, 256, 0, clip_compact_kernel, tf, toff, nt, list);
   VCUDA(cudaMemcpyAsync(&cnt->n_touch, toff + nt, 4, cudaMemcpyDeviceToDevice, st));
-  VLAUNCH(ctx, kKClipResolve, 1, kClipResolveThreads, 0, clip_resolve_kernel, dv, dt, dpl, side,
+  VCUDA(cudaFuncSetAttribute(clip_resolve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kResolveSmem));
+  VLAUNCH(ctx, kKClipResolve, 1, kClipResolveThreads, kResolveSmem, clip_resolve_kernel, dv, dt, dpl, side,
           list, R, slots, kp, kn);
   VLAUNCH(ctx, kKClip, gt, 256, 0, clip_counts_kernel, code, toff, slots, nt, cp, cn);
   VTRY(exclusive_scan_u32_to_u64(ctx, cp, op, nt));

@@ -49,13 +49,18 @@ __device__ __forceinline__ void load_tri(const double* __restrict__ P, const int
 __device__ __forceinline__ double min3(double a, double b, double c) { return fmin(fmin(a, b), c); }
 __device__ __forceinline__ double max3(double a, double b, double c) { return fmax(fmax(a, b), c); }
 
-// Lower-bound pre-filter of the exact distance: a voxel whose distance to the
-// triangle's bounding box or plane (FP32, minus a margin of 1e-3 voxel plus
-// 1e-6 of the largest grid coordinate, which covers the FP32 rounding of the
-// plane evaluation) is not below the
-// voxel's current minimum cannot lower it — the exact FP64 distance is at
-// least as large, and rounding to float is monotone — so its FP64 evaluation
-// is skipped. The stored result is the same minimum as without the filter.
+// Lower-bound pre-filter of the exact distance: a voxel whose lower bound
+// (FP32, less twice a margin of 1e-3 voxel plus 1e-6 of the largest grid
+// coordinate, which covers the FP32 rounding of the plane evaluations) is not
+// below the voxel's current minimum cannot lower it — the exact FP64 distance
+// is at least as large, and rounding to float is monotone — so its FP64
+// evaluation is skipped. The stored result is the same minimum as without the
+// filter. The bound is the larger of the gap to the triangle's bounding box
+// and sqrt(p^2 + s^2), with p the distance to the triangle's plane and s the
+// largest distance beyond one of its edges in the plane: with n the unit
+// normal and m_e the unit in-plane normal of edge e pointing away from the
+// triangle (offset so that no vertex lies beyond it), every triangle point x
+// has |q - x|^2 >= (n.(q - x))^2 + (m_e.(q - x))^2 >= p^2 + s_e^2.
 __global__ void __launch_bounds__(128) sdf_dist_kernel(const double* __restrict__ P, const int32_t* __restrict__ T,
                                                        int nt, SdfGrid g, uint32_t* __restrict__ dist) {
   for (int t = blockIdx.x; t < nt; t += gridDim.x) {
@@ -79,6 +84,8 @@ __global__ void __launch_bounds__(128) sdf_dist_kernel(const double* __restrict_
     const double nl = sqrt(nx * nx + ny * ny + nz * nz);
     const bool has_plane = nl > 1e-12;
     float fnx = 0.f, fny = 0.f, fnz = 0.f, foff = 0.f;
+    float4 fe[3] = {make_float4(0.f, 0.f, 0.f, -1e30f), make_float4(0.f, 0.f, 0.f, -1e30f),
+                    make_float4(0.f, 0.f, 0.f, -1e30f)};
     if (has_plane) {
       nx /= nl;
       ny /= nl;
@@ -87,6 +94,27 @@ __global__ void __launch_bounds__(128) sdf_dist_kernel(const double* __restrict_
       fny = (float)ny;
       fnz = (float)nz;
       foff = (float)-(nx * A[0] + ny * A[1] + nz * A[2]);
+      const double* V[3] = {A, B, C};
+      for (int e = 0; e < 3; ++e) {
+        const double* P0 = V[e];
+        const double* P1 = V[(e + 1) % 3];
+        const double* P2 = V[(e + 2) % 3];
+        const double ex = P1[0] - P0[0], ey = P1[1] - P0[1], ez = P1[2] - P0[2];
+        double mx = ny * ez - nz * ey, my = nz * ex - nx * ez, mz = nx * ey - ny * ex;
+        const double ml = sqrt(mx * mx + my * my + mz * mz);
+        if (!(ml > 1e-12)) continue;
+        mx /= ml;
+        my /= ml;
+        mz /= ml;
+        if (mx * (P2[0] - P0[0]) + my * (P2[1] - P0[1]) + mz * (P2[2] - P0[2]) > 0) {
+          mx = -mx;
+          my = -my;
+          mz = -mz;
+        }
+        const double top = fmax(fmax(mx * A[0] + my * A[1] + mz * A[2], mx * B[0] + my * B[1] + mz * B[2]),
+                                mx * C[0] + my * C[1] + mz * C[2]);
+        fe[e] = make_float4((float)mx, (float)my, (float)mz, (float)-top);
+      }
     }
     const int n = ext[0] * ext[1] * ext[2];
     for (int r = threadIdx.x; r < n; r += blockDim.x) {
@@ -97,9 +125,14 @@ __global__ void __launch_bounds__(128) sdf_dist_kernel(const double* __restrict_
       const float gy = fmaxf(fmaxf(blo[1] - qy, qy - bhi[1]), 0.f);
       const float gz = fmaxf(fmaxf(blo[2] - qz, qz - bhi[2]), 0.f);
       float lb = sqrtf(gx * gx + gy * gy + gz * gz);
-      if (has_plane) lb = fmaxf(lb, fabsf(fnx * qx + fny * qy + fnz * qz + foff));
+      if (has_plane) {
+        const float pd = fabsf(fnx * qx + fny * qy + fnz * qz + foff);
+        float se = 0.f;
+        for (int e = 0; e < 3; ++e) se = fmaxf(se, fe[e].x * qx + fe[e].y * qy + fe[e].z * qz + fe[e].w);
+        lb = fmaxf(lb, sqrtf(pd * pd + se * se));
+      }
       const float cur = __uint_as_float(*(volatile const uint32_t*)&dist[v]);
-      if (lb - g.margin >= cur) continue;
+      if (lb - 2.0f * g.margin >= cur) continue;
       const double q[3] = {(double)(g.org[0] + i), (double)(g.org[1] + j), (double)(g.org[2] + k)};
       const float d = __double2float_rn(point_tri_dist(q, A, B, C));
       atomicMin(&dist[v], __float_as_uint(d));
