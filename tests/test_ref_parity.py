@@ -63,6 +63,25 @@ def test_candidate_planes_bit_exact_with_reference(V):
         np.testing.assert_array_equal(a, b)
 
 
+def test_candidate_planes_with_near_duplicates_bit_exact_with_reference(V):
+    # nearly parallel edges with close midpoints: many candidates are dropped
+    # as similar (normals within 5 degrees and offsets within 1e-3)
+    rng = np.random.default_rng(4)
+    n = 300
+    v = np.stack([rng.uniform(0, 0.05, n), rng.uniform(-2e-3, 2e-3, n), rng.uniform(-2e-3, 2e-3, n)], 1)
+    i = rng.integers(0, n, 4000)
+    j = rng.integers(0, n, 4000)
+    keep = i != j
+    e = np.stack([np.minimum(i, j), np.maximum(i, j)], 1)[keep].astype(np.uint32)
+    for seed in (0, 42):
+        R.set_seed(seed)
+        a = R.candidate_planes(v, e, 2500)
+        V.set_seed(seed)
+        b = V._candidate_planes(v, e, 2500)
+        np.testing.assert_array_equal(a, b)
+        assert 0 < len(b) < 2500
+
+
 def test_flat_surfaces_match_reference(V):
     g = np.linspace(-0.5, 0.5, 4)
     xx, yy = np.meshgrid(g, g)

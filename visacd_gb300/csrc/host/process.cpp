@@ -15,6 +15,7 @@
 #include <sstream>
 #include <string>
 #include <thread>
+#include <unordered_map>
 
 #ifdef _OPENMP
 #include <omp.h>
@@ -49,6 +50,13 @@ std::vector<Plane> get_candidate_planes(const std::vector<Vec3>& vertices,
   const double normal_eps = std::cos(5.0 * M_PI / 180.0);
   const double dist_eps = 1e-3;
   std::mt19937& eng = random_engine();
+  // A candidate is dropped when any kept plane has |d - d'| < dist_eps and a
+  // normal within 5 degrees; only whether one exists matters, so the kept
+  // planes are bucketed by floor(d / dist_eps) and a candidate is compared
+  // with the planes of the buckets within two of its own (every plane with
+  // |d - d'| < dist_eps lies there), with the same two tests.
+  std::unordered_map<long long, std::vector<int>> by_d;
+  auto bucket = [&](double d) { return (long long)std::floor(d / dist_eps); };
   for (int i = 0; i < num_planes * 5 && (int)planes.size() < num_planes; ++i) {
     int idx = dis(eng);
     const Vec3 p1 = vertices[edges[idx].first];
@@ -59,14 +67,23 @@ std::vector<Plane> get_candidate_planes(const std::vector<Vec3>& vertices,
     Vec3 m = (p1 + p2) * 0.5;
     double d = -(n[0] * m[0] + n[1] * m[1] + n[2] * m[2]);
     bool similar = false;
-    for (const auto& p : planes) {
-      double dt = std::fabs(n[0] * p.a + n[1] * p.b + n[2] * p.c);
-      if (dt > normal_eps && std::fabs(d - p.d) < dist_eps) {
-        similar = true;
-        break;
+    const long long key = bucket(d);
+    for (long long k = key - 2; k <= key + 2 && !similar; ++k) {
+      auto it = by_d.find(k);
+      if (it == by_d.end()) continue;
+      for (int j : it->second) {
+        const Plane& p = planes[j];
+        double dt = std::fabs(n[0] * p.a + n[1] * p.b + n[2] * p.c);
+        if (dt > normal_eps && std::fabs(d - p.d) < dist_eps) {
+          similar = true;
+          break;
+        }
       }
     }
-    if (!similar) planes.emplace_back(n[0], n[1], n[2], d);
+    if (!similar) {
+      by_d[key].push_back((int)planes.size());
+      planes.emplace_back(n[0], n[1], n[2], d);
+    }
   }
   return planes;
 }
