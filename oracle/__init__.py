@@ -34,6 +34,8 @@ def lib() -> C.CDLL:
         L.oracle_seg_tri_batch.argtypes = [P, P, i64, P]
         L.oracle_seg_tri_batch.restype = i64
         L.oracle_candidate_planes.restype = i32
+        L.oracle_sample_points.argtypes = [P, P, i32, i32, C.c_uint32, P, P, i64, P]
+        L.oracle_sample_points.restype = i64
         _lib = L
     return _lib
 
@@ -130,3 +132,19 @@ def seg_tri_batch(seg, tri):
     out = np.zeros(len(sg), np.uint8)
     lib().oracle_seg_tri_batch(_p(sg), _p(tr), len(sg), _p(out))
     return (out & 1).astype(bool), (out & 2).astype(bool)
+
+
+def sample_points(verts, tris, res: int, seed: int):
+    """Surface samples of the reference's extract_point_set (base 1, one per
+    untouched triangle) on std::mt19937(seed): (xyz, triangle ids, the
+    engine's next four outputs)."""
+    v = np.ascontiguousarray(verts, dtype=np.float64).reshape(-1, 3)
+    t = np.ascontiguousarray(tris, dtype=np.int32).reshape(-1, 3)
+    cap = 64 * max(res, 1000) + 2 * len(t) + 16
+    xyz = np.zeros((cap, 3), dtype=np.float64)
+    ids = np.zeros(cap, dtype=np.int32)
+    nxt = np.zeros(4, dtype=np.uint32)
+    n = lib().oracle_sample_points(_p(v), _p(t), len(t), res, seed, _p(xyz), _p(ids), cap, _p(nxt))
+    if n < 0:
+        raise ValueError("sample capacity too small")
+    return xyz[:n], ids[:n], nxt

@@ -525,4 +525,60 @@ int64_t oracle_seg_tri_batch(const float* seg, const float* tri, int64_t S, uint
   return hits;
 }
 
+// ---------------------------------------------------------------------------
+// Surface samples — Mesh::extract_point_set, lib/src/core.cpp:144-232, with
+// base 1 and one_per_tri: triangle areas (the reference's triangle_area
+// expression, lib/include/core.hpp:119-130), resolution max(1000, res * area),
+// triangles drawn by std::discrete_distribution<size_t> over the areas, each
+// sample at (1 - sqrt(a)) p0 + sqrt(a)(1 - b) p1 + b sqrt(a) p2 with a, b from
+// std::uniform_real_distribution<double>(0, 1), all on std::mt19937(seed), one
+// at a time; then one sample on every triangle not drawn, in index order.
+// out_xyz / out_ids hold up to cap samples; next4 = the engine's next four
+// outputs afterwards. Returns the sample count (or -1 when cap is too small).
+// ---------------------------------------------------------------------------
+int64_t oracle_sample_points(const double* verts, const int32_t* tris, int32_t nt, int32_t res, uint32_t seed,
+                             double* out_xyz, int32_t* out_ids, int64_t cap, uint32_t* next4) {
+  if (nt <= 0) return 0;
+  std::vector<double> areas(nt);
+  double total = 0;
+  for (int32_t i = 0; i < nt; ++i) {
+    const double* p0 = verts + 3 * (int64_t)tris[3 * i];
+    const double* p1 = verts + 3 * (int64_t)tris[3 * i + 1];
+    const double* p2 = verts + 3 * (int64_t)tris[3 * i + 2];
+    double a = p1[0] * p0[1] - p2[0] * p0[1] - p0[0] * p1[1] + p2[0] * p1[1] + p0[0] * p2[1] - p1[0] * p2[1];
+    double b = p1[0] * p0[2] - p2[0] * p0[2] - p0[0] * p1[2] + p2[0] * p1[2] + p0[0] * p2[2] - p1[0] * p2[2];
+    double c = p1[1] * p0[2] - p2[1] * p0[2] - p0[1] * p1[2] + p2[1] * p1[2] + p0[1] * p2[2] - p1[1] * p2[2];
+    areas[i] = 0.5 * sqrt(pow(a, 2) + pow(b, 2) + pow(c, 2));
+    total += areas[i];
+  }
+  const size_t resolution = (size_t)std::max(1000, (int)(res * (total / 1.0)));
+  std::mt19937 eng(seed);
+  std::discrete_distribution<size_t> pick(areas.begin(), areas.end());
+  std::uniform_real_distribution<double> uni(0.0, 1.0);
+  std::vector<char> drawn(nt, 0);
+  int64_t n = 0;
+  auto emit = [&](size_t ti) {
+    double a = uni(eng);
+    double b = uni(eng);
+    const double* p0 = verts + 3 * (int64_t)tris[3 * ti];
+    const double* p1 = verts + 3 * (int64_t)tris[3 * ti + 1];
+    const double* p2 = verts + 3 * (int64_t)tris[3 * ti + 2];
+    if (n < cap) {
+      for (int k = 0; k < 3; ++k)
+        out_xyz[3 * n + k] = (1 - sqrt(a)) * p0[k] + (sqrt(a) * (1 - b)) * p1[k] + b * sqrt(a) * p2[k];
+      out_ids[n] = (int32_t)ti;
+    }
+    ++n;
+  };
+  for (size_t s = 0; s < resolution; ++s) {
+    const size_t ti = pick(eng);
+    emit(ti);
+    drawn[ti] = 1;
+  }
+  for (int32_t i = 0; i < nt; ++i)
+    if (!drawn[i]) emit((size_t)i);
+  for (int k = 0; k < 4; ++k) next4[k] = (uint32_t)eng();
+  return n <= cap ? n : -1;
+}
+
 }  // extern "C"

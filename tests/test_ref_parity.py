@@ -132,3 +132,23 @@ def test_hull_matches_reference(V):
     h = V._convex_hull(p)
     assert len(h["triangles"]) == nt
     assert abs(V._mesh_volume(h["vertices"], h["triangles"]) - vol) < 1e-12
+
+
+def test_surface_sampling_matches_one_by_one_draws(V):
+    """extract_point_set (engine outputs taken in bulk, guide-table triangle
+    draws) against the reference's one-draw-at-a-time loop on std::mt19937:
+    same samples, same triangles, same engine position afterwards; including
+    single-triangle and two-triangle meshes and a large sample count."""
+    cases = [mg.displaced_blob(2, seed=3), mg.displaced_blob(4, seed=5)]
+    one = (np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], float), np.array([[0, 1, 2]], np.int32))
+    two = (np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [1, 1, 0.5]], float), np.array([[0, 1, 2], [1, 3, 2]], np.int32))
+    cases += [one, two]
+    for (v, t), res in zip(cases, (3000, 10000, 3000, 2000)):
+        for seed in (0, 77):
+            xo, io, no = oracle.sample_points(v, t, res, seed)
+            V.set_seed(seed)
+            xp, ip = V._sample_points(v, t, res)
+            npx = V._engine_next(4)
+            np.testing.assert_array_equal(io, ip)
+            np.testing.assert_array_equal(xo, xp)
+            np.testing.assert_array_equal(no, npx)

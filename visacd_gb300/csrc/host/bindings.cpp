@@ -242,6 +242,11 @@ PYBIND11_MODULE(visacd, m) {
   m.def("_compute_hb", [](py::array_t<double> v, py::array_t<int> t, py::array_t<double> hv, py::array_t<int> ht, unsigned res) {
     return compute_hb(np_to_mesh(v, t), np_to_mesh(hv, ht), res);
   });
+  m.def("_engine_next", [](int n) {
+    std::vector<uint32_t> w((size_t)std::max(n, 0));
+    random_engine().fill(w.data(), w.size());
+    return py::array_t<uint32_t>(w.size(), w.data());
+  });
   m.def("_sample_points", [](py::array_t<double> v, py::array_t<int> t, unsigned res) {
     std::vector<Vec3> x;
     std::vector<int> ids;

@@ -27,17 +27,49 @@ Config& config() {
   return c;
 }
 
-namespace {
-thread_local std::mt19937* tl_engine = nullptr;  // per-thread engine of process_batch workers
+void Mt19937::seed(result_type s) {
+  x_[0] = s;
+  for (int i = 1; i < kN; ++i) x_[i] = 1812433253u * (x_[i - 1] ^ (x_[i - 1] >> 30)) + (uint32_t)i;
+  pos_ = kN;
 }
 
-std::mt19937& random_engine() {
+// One pass of the recurrence x_k = x_{k+M} ^ A((x_k & upper) | (x_{k+1} & lower))
+// over the state, in three runs with fixed index offsets (each run's source
+// words are final before it reads them).
+void Mt19937::twist() {
+  auto mix = [](uint32_t a, uint32_t b, uint32_t c) {
+    const uint32_t y = (a & 0x80000000u) | (b & 0x7fffffffu);
+    return c ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+  };
+  int k = 0;
+  for (; k < kN - kM; ++k) x_[k] = mix(x_[k], x_[k + 1], x_[k + kM]);
+  for (; k < kN - 1; ++k) x_[k] = mix(x_[k], x_[k + 1], x_[k + kM - kN]);
+  x_[kN - 1] = mix(x_[kN - 1], x_[0], x_[kM - 1]);
+  pos_ = 0;
+}
+
+void Mt19937::fill(uint32_t* out, size_t n) {
+  while (n > 0) {
+    if (pos_ >= kN) twist();
+    const size_t take = std::min(n, (size_t)(kN - pos_));
+    for (size_t i = 0; i < take; ++i) out[i] = temper(x_[pos_ + (int)i]);
+    pos_ += (int)take;
+    out += take;
+    n -= take;
+  }
+}
+
+namespace {
+thread_local Mt19937* tl_engine = nullptr;  // per-thread engine of process_batch workers
+}
+
+Mt19937& random_engine() {
   if (tl_engine) return *tl_engine;
-  static std::mt19937 eng(std::random_device{}());
+  static Mt19937 eng(std::random_device{}());
   return eng;
 }
 
-void set_thread_engine(std::mt19937* eng) { tl_engine = eng; }
+void set_thread_engine(Mt19937* eng) { tl_engine = eng; }
 
 void set_seed(unsigned int seed) { random_engine().seed(seed); }
 

@@ -108,10 +108,52 @@ struct Config {
 };
 
 Config& config();
+
+// The 32-bit Mersenne Twister MT19937 (Matsumoto and Nishimura, 1998) with the
+// parameters and seeding std::mt19937 is defined with, so the same seed gives
+// the same output sequence (the engine of lib/src/core.cpp:27). A class of its
+// own so that many outputs can be taken in one call (fill), which the sampling
+// loops use; it meets the uniform random bit generator requirements, so the
+// standard distributions draw from it exactly as from std::mt19937.
+class Mt19937 {
+ public:
+  using result_type = uint32_t;
+  static constexpr result_type min() { return 0u; }
+  static constexpr result_type max() { return 0xffffffffu; }
+  explicit Mt19937(result_type s = 5489u) { seed(s); }
+  void seed(result_type s);
+  result_type operator()() {
+    if (pos_ >= kN) twist();
+    return temper(x_[pos_++]);
+  }
+  // The next n outputs, in order.
+  void fill(uint32_t* out, size_t n);
+
+ private:
+  static constexpr int kN = 624, kM = 397;
+  static uint32_t temper(uint32_t y) {
+    y ^= y >> 11;
+    y ^= (y << 7) & 0x9d2c5680u;
+    y ^= (y << 15) & 0xefc60000u;
+    return y ^ (y >> 18);
+  }
+  void twist();
+  uint32_t x_[kN];
+  int pos_ = kN;
+};
+
+// std::generate_canonical<double, 53> of two successive outputs (lo, hi) of a
+// 32-bit engine: (lo + hi 2^32) / 2^64 with the sum rounded to double, and the
+// largest double below 1 in place of 1.
+inline double canonical53(uint32_t lo, uint32_t hi) {
+  const double r = ((double)lo + (double)hi * 0x1p32) * 0x1p-64;
+  return r < 1.0 ? r : 0x1.fffffffffffffp-1;
+}
+
 // The process-wide engine, or the calling thread's own one while a
 // process_batch worker has installed it (set_thread_engine(nullptr) clears).
-std::mt19937& random_engine();
-void set_thread_engine(std::mt19937* eng);
+Mt19937& random_engine();
+void set_thread_engine(Mt19937* eng);
 void set_seed(unsigned int seed);
 
 // Bounding box (xmin, xmax, ymin, ymax, zmin, zmax).

@@ -27,13 +27,13 @@ constexpr double kPi = 3.14159265;  // the reference's constant (lib/include/cos
 
 namespace {
 
-// The draws of std::discrete_distribution<size_t> over the same weights, made
-// faster: its result is the first index of the cumulative probabilities not
-// below a canonical uniform p, found here through a guide table (bucket
-// floor(p n) -> first index whose cumulative value reaches the bucket's
-// start) and a short forward scan; every result is checked to be that first
-// index, falling back to a binary search, so it equals the distribution's
-// draw for the same engine state.
+// The draws of std::discrete_distribution<size_t> over the same weights (two
+// or more), made faster: its result is the first index of the cumulative
+// probabilities not below a canonical uniform p, found here through a guide
+// table (bucket floor(p n) -> first index whose cumulative value reaches the
+// bucket's start) and a short forward scan; every result is checked to be that
+// first index, falling back to a binary search, so it equals the
+// distribution's draw for the same p.
 class DiscreteSampler {
  public:
   explicit DiscreteSampler(const std::discrete_distribution<size_t>& d) {
@@ -51,8 +51,7 @@ class DiscreteSampler {
       guide_[j] = i;
     }
   }
-  size_t operator()(std::mt19937& eng) const {
-    const double p = std::generate_canonical<double, std::numeric_limits<double>::digits>(eng);
+  size_t find(double p) const {
     size_t j = (size_t)(p * scale_);
     if (j >= guide_.size()) j = guide_.size() - 1;
     size_t i = guide_[j];
@@ -67,55 +66,89 @@ class DiscreteSampler {
   double scale_ = 0;
 };
 
+// A sample of triangle ti at barycentric draws a, b (lib/src/core.cpp:176-191).
+inline Vec3 tri_sample(const Mesh& m, size_t ti, double a, double b) {
+  const auto& t = m.triangles[ti];
+  const Vec3 &v0 = m.vertices[t[0]], &v1 = m.vertices[t[1]], &v2 = m.vertices[t[2]];
+  const double sa = std::sqrt(a);  // correctly rounded: one evaluation serves all six uses
+  Vec3 v;
+  for (int k = 0; k < 3; ++k) v[k] = (1 - sa) * v0[k] + (sa * (1 - b)) * v1[k] + b * sa * v2[k];
+  return v;
+}
+
 }  // namespace
 
+// Engine outputs are taken in bulk: a draw of the triangle distribution takes
+// two outputs (one canonical double; none when there is a single triangle,
+// which std::discrete_distribution returns without drawing), each of the two
+// uniform doubles two, so sample j of the first loop reads a fixed window of
+// the output stream and the samples are computed independently (in parallel
+// for large counts); the untouched triangles then take four outputs each, in
+// index order. Same values as drawing one by one.
 void extract_point_set(const Mesh& m, std::vector<Vec3>& samples, std::vector<int>& tri_ids,
                        size_t resolution, double base, bool one_per_tri) {
   if (m.triangles.empty() || m.vertices.empty()) return;
-  std::vector<double> areas(m.triangles.size());
+  const size_t T = m.triangles.size();
+  std::vector<double> areas(T);
   double total = 0;
-  for (size_t i = 0; i < m.triangles.size(); ++i) {
+  for (size_t i = 0; i < T; ++i) {
     const auto& t = m.triangles[i];
     areas[i] = triangle_area(m.vertices[t[0]], m.vertices[t[1]], m.vertices[t[2]]);
     total += areas[i];
   }
   if (base != 0) resolution = size_t(std::max(1000, int(resolution * (total / base))));
   std::discrete_distribution<size_t> pick(areas.begin(), areas.end());
-  std::uniform_real_distribution<double> uni(0.0, 1.0);
-  std::mt19937& eng = random_engine();
+  Mt19937& eng = random_engine();
   // Triangles drawn at least once (a bitmap: only membership matters, the
   // untouched ones are visited in index order below).
-  std::vector<char> touched(m.triangles.size(), 0);
-  samples.reserve(samples.size() + resolution + (one_per_tri ? m.triangles.size() : 0));
-  tri_ids.reserve(samples.capacity());
-  auto sample = [&](size_t ti) {
-    const auto& t = m.triangles[ti];
-    double a = uni(eng);
-    double b = uni(eng);
-    const Vec3 &v0 = m.vertices[t[0]], &v1 = m.vertices[t[1]], &v2 = m.vertices[t[2]];
-    const double sa = std::sqrt(a);  // correctly rounded: one evaluation serves all six uses
-    Vec3 v;
-    for (int k = 0; k < 3; ++k) v[k] = (1 - sa) * v0[k] + (sa * (1 - b)) * v1[k] + b * sa * v2[k];
-    samples.push_back(v);
-    tri_ids.push_back((int)ti);
-  };
-  if (total > 0 && std::isfinite(total)) {
+  std::vector<char> touched(T, 0);
+  const size_t b0 = samples.size();
+  if ((total > 0 && std::isfinite(total)) || T == 1) {
+    const int per = T == 1 ? 4 : 6;
+    std::vector<uint32_t> w((size_t)per * resolution);
+    eng.fill(w.data(), w.size());
+    samples.resize(b0 + resolution);
+    tri_ids.resize(b0 + resolution);
     const DiscreteSampler fast(pick);
-    for (size_t done = 0; done < resolution; ++done) {
-      const size_t ti = fast(eng);
-      sample(ti);
-      touched[ti] = 1;
+#pragma omp parallel for schedule(static) if (resolution >= 16384)
+    for (long j = 0; j < (long)resolution; ++j) {
+      const uint32_t* q = w.data() + (size_t)per * j;
+      size_t ti = 0;
+      if (T > 1) {
+        ti = fast.find(canonical53(q[0], q[1]));
+        q += 2;
+      }
+      samples[b0 + j] = tri_sample(m, ti, canonical53(q[0], q[1]), canonical53(q[2], q[3]));
+      tri_ids[b0 + j] = (int)ti;
     }
+    for (size_t j = 0; j < resolution; ++j) touched[tri_ids[b0 + j]] = 1;
   } else {
+    // Degenerate weights (zero or non-finite total): the distribution itself.
+    std::uniform_real_distribution<double> uni(0.0, 1.0);
     for (size_t done = 0; done < resolution; ++done) {
       const size_t ti = pick(eng);
-      sample(ti);
+      const double a = uni(eng);
+      const double b = uni(eng);
+      samples.push_back(tri_sample(m, ti, a, b));
+      tri_ids.push_back((int)ti);
       touched[ti] = 1;
     }
   }
-  if (one_per_tri)
-    for (size_t i = 0; i < m.triangles.size(); ++i)
-      if (!touched[i]) sample(i);
+  if (!one_per_tri) return;
+  std::vector<int> rest;
+  for (size_t i = 0; i < T; ++i)
+    if (!touched[i]) rest.push_back((int)i);
+  std::vector<uint32_t> w(4 * rest.size());
+  eng.fill(w.data(), w.size());
+  const size_t b1 = samples.size();
+  samples.resize(b1 + rest.size());
+  tri_ids.resize(b1 + rest.size());
+#pragma omp parallel for schedule(static) if (rest.size() >= 16384)
+  for (long k = 0; k < (long)rest.size(); ++k) {
+    const uint32_t* q = w.data() + 4 * k;
+    samples[b1 + k] = tri_sample(m, (size_t)rest[k], canonical53(q[0], q[1]), canonical53(q[2], q[3]));
+    tri_ids[b1 + k] = rest[k];
+  }
 }
 
 namespace {

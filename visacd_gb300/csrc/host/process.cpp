@@ -49,7 +49,7 @@ std::vector<Plane> get_candidate_planes(const std::vector<Vec3>& vertices,
   std::uniform_int_distribution<> dis(0, (int)edges.size() - 1);
   const double normal_eps = std::cos(5.0 * M_PI / 180.0);
   const double dist_eps = 1e-3;
-  std::mt19937& eng = random_engine();
+  Mt19937& eng = random_engine();
   // A candidate is dropped when any kept plane has |d - d'| < dist_eps and a
   // normal within 5 degrees; only whether one exists matters, so the kept
   // planes are bucketed by floor(d / dist_eps) and a candidate is compared
@@ -239,12 +239,24 @@ int get_part_with_highest_score(const MeshList& parts) {
   return idx;
 }
 
-int get_part_with_highest_concavity(const MeshList& parts, double& max_concavity) {
-  const auto t0 = std::chrono::steady_clock::now();
-  MeshList hulls(parts.size());
+const MeshList& HullCache::update(const MeshList& parts) {
+  const size_t n = parts.size();
+  hulls.resize(n);
+  valid.resize(n, 0);
+  std::vector<int> todo;
+  for (size_t i = 0; i < n; ++i)
+    if (!valid[i]) todo.push_back((int)i);
   // Hulls draw no random numbers: built in parallel (same result in any order).
-#pragma omp parallel for schedule(dynamic, 1) if (parts.size() > 1)
-  for (int i = 0; i < (int)parts.size(); ++i) hulls[i] = convex_hull(parts[i].vertices, true);
+#pragma omp parallel for schedule(dynamic, 1) if (todo.size() > 1)
+  for (int k = 0; k < (int)todo.size(); ++k) hulls[todo[k]] = convex_hull(parts[todo[k]].vertices, true);
+  for (int i : todo) valid[i] = 1;
+  return hulls;
+}
+
+int get_part_with_highest_concavity(const MeshList& parts, double& max_concavity, HullCache* cache) {
+  const auto t0 = std::chrono::steady_clock::now();
+  HullCache local;
+  const MeshList& hulls = (cache ? *cache : local).update(parts);
   concavity_times().hull_ms +=
       std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   // compute_h(part, hull, 0.3, 3000) of every part, of which only the first
@@ -335,6 +347,7 @@ ProcessResult process(Mesh mesh, double concavity, int num_parts) {
     }
     g_times.visibility += now_ms() - t0;
   }
+  HullCache hull_cache;
   log("Starting decomposition (max parts=" + std::to_string(num_parts) + ", concavity threshold=" +
       std::to_string(concavity) + ", mode=" + config().score_mode + ").");
   for (int i = 0; i < num_parts - 1; ++i) {
@@ -344,7 +357,7 @@ ProcessResult process(Mesh mesh, double concavity, int num_parts) {
     } else if (config().score_mode == "concavity") {
       double t0 = now_ms();
       double mc = -1;
-      idx = get_part_with_highest_concavity(parts, mc);
+      idx = get_part_with_highest_concavity(parts, mc, &hull_cache);
       g_times.concavity += now_ms() - t0;
       if (mc < concavity) {
         log("Step " + std::to_string(i + 1) + ": concavity " + std::to_string(mc).substr(0, 6) +
@@ -357,6 +370,7 @@ ProcessResult process(Mesh mesh, double concavity, int num_parts) {
         std::to_string(idx) + " (" + std::to_string(parts.size()) + " parts total).");
     Mesh part = parts[idx];
     parts.erase(parts.begin() + idx);
+    hull_cache.erase((size_t)idx);
     g_times.iterations++;
     if (decompose_iteration(part, parts, cage, flat_planes)) {
       log("No more intersecting edges, stopping early.");
@@ -365,8 +379,7 @@ ProcessResult process(Mesh mesh, double concavity, int num_parts) {
   }
   log("Computing convex hulls for " + std::to_string(parts.size()) + " parts...");
   double th = now_ms();
-  MeshList hulls;
-  for (const auto& p : parts) hulls.push_back(convex_hull(p.vertices, true));
+  MeshList hulls = hull_cache.update(parts);
   double final_c = compute_final_concavity(parts, hulls);
   if (config().use_merging) {
     log("Merging parts...");
@@ -405,7 +418,7 @@ std::vector<ProcessResult> process_batch(const MeshList& meshes, double concavit
 #ifdef _OPENMP
       omp_set_num_threads(1);  // the batch is the parallelism; no nested teams
 #endif
-      std::mt19937 eng;
+      Mt19937 eng;
       set_thread_engine(&eng);
       gpu::counters() = gpu::Counters();
       concavity_times() = ConcavityTimes();

@@ -25,7 +25,24 @@ bool decompose_iteration(Mesh& mesh, MeshList& parts, Mesh& cage,
 
 double compute_part_score(const Mesh& part);
 int get_part_with_highest_score(const MeshList& parts);
-int get_part_with_highest_concavity(const MeshList& parts, double& max_concavity);
+// Convex hulls of the parts kept from one iteration to the next (a hull
+// depends on the part's vertices alone and draws no random numbers): entry i
+// belongs to parts[i] while valid[i]; process() erases the entry of the part
+// it splits, and entries past the end are built when needed.
+struct HullCache {
+  MeshList hulls;
+  std::vector<char> valid;
+  void erase(size_t i) {
+    if (i < hulls.size()) {
+      hulls.erase(hulls.begin() + (long)i);
+      valid.erase(valid.begin() + (long)i);
+    }
+  }
+  // Hulls of all parts: cached ones kept, missing ones built in parallel.
+  const MeshList& update(const MeshList& parts);
+};
+
+int get_part_with_highest_concavity(const MeshList& parts, double& max_concavity, HullCache* cache = nullptr);
 double compute_final_concavity(const MeshList& parts, const MeshList& hulls);
 
 // lib/src/process.cpp:238-347.
