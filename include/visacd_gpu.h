@@ -247,6 +247,26 @@ int visacd_face_hausdorff_floor(visacd_ctx* ctx, const double* va, int32_t nva, 
                                 const double* xb, const int32_t* idb, int32_t nb, double floor,
                                 double* out);
 
+/* Many face Hausdorff distances in one call: job j compares surface A_j (mesh
+   2j, samples of set 2j) with surface B_j (mesh 2j + 1, set 2j + 1). Meshes
+   are concatenated: vertices 3 x vert_off[2J] float64, triangles 3 x
+   tri_off[2J] int32 with indices local to their mesh; samples 3 x
+   sample_off[2J] float64 with the (local) triangle each was drawn from.
+   Offsets have 2J + 1 entries starting at 0; every surface and sample set
+   must be non-empty.
+   independent != 0: out[j] is every job's exact distance H_j.
+   independent == 0 (the part selection of lib/src/process.cpp:208-236): with
+   lower[j] a known lower bound of job j's concavity (NULL: 0) and
+   M = max(floor, max_j max(lower[j], H_j)), out[j] = H_j for every job with
+   H_j = M and out[j] <= H_j otherwise, so max(lower[j], out[j]) is exact for
+   the jobs that attain M and below M for the rest. Sample terms that cannot
+   reach the running maximum are not evaluated. Host pointers; synchronizes. */
+int visacd_face_hausdorff_batch(visacd_ctx* ctx, int32_t njobs, const double* verts,
+                                const int64_t* vert_off, const int32_t* tris, const int64_t* tri_off,
+                                const double* samples, const int32_t* sample_tri,
+                                const int64_t* sample_off, const double* lower, double floor,
+                                int32_t independent, double* out);
+
 /* Independent segment-triangle decisions with the visibility kernel's test
    (FP32 filter with a rigorous rounding bound, FP64 re-decision inside it;
    lib/ptx/ray_segments.cu:49-111 semantics, tmin 0.001): seg S x 6 (p, q),

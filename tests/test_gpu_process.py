@@ -126,3 +126,39 @@ def test_process_gpu_metric_equals_host_metric(visacd):
     assert a.num_parts == b.num_parts and a.concavity == b.concavity
     for pa, pb in zip(a.parts, b.parts):
         np.testing.assert_array_equal(np.array(pa.vertices), np.array(pb.vertices))
+
+
+def test_face_hausdorff_batch(visacd):
+    """visacd_face_hausdorff_batch: independent jobs equal single calls; with
+    pruning across jobs, the jobs attaining the largest concavity keep their
+    exact value, the others stay at or below theirs, and the first maximum of
+    max(lower, value) is unchanged."""
+    from visacd_gb300 import _native as N
+    from visacd_gb300 import visacd as V
+    ctx = N.Context(0)
+    try:
+        jobs, lower = [], []
+        for seed, level in [(3, 2), (8, 3), (11, 3), (12, 2), (14, 3)]:
+            v, t = mg.displaced_blob(level, seed=seed)
+            hv = V._convex_hull(v)
+            V.set_seed(seed)
+            xa, ia = V._sample_points(v, t, 3000)
+            xb, ib = V._sample_points(hv["vertices"], hv["triangles"], 3000)
+            jobs.append((v, t, xa, ia, hv["vertices"], hv["triangles"], xb, ib))
+            vol = abs(V._mesh_volume(hv["vertices"], hv["triangles"]) - V._mesh_volume(v, t))
+            lower.append(0.3 * (3 * vol / (4 * 3.14159265)) ** (1 / 3))
+        single = np.array([ctx.face_hausdorff(*j) for j in jobs])
+        np.testing.assert_array_equal(ctx.face_hausdorff_batch(jobs), single)
+        lower = np.array(lower)
+        for low, floor in ((lower, 0.0), (np.zeros(len(jobs)), 0.0), (lower, 0.5 * single.max())):
+            got = ctx.face_hausdorff_batch(jobs, lower=low, floor=floor, independent=False)
+            M = max(floor, np.maximum(low, single).max())
+            assert np.all(got <= single)
+            for j in range(len(jobs)):
+                if single[j] == M:
+                    assert got[j] == single[j]
+            c_true, c_got = np.maximum(low, single), np.maximum(low, got)
+            if c_true.max() >= floor:
+                assert c_got.max() == c_true.max() and np.argmax(c_got) == np.argmax(c_true)
+    finally:
+        ctx.close()

@@ -24,7 +24,7 @@ EXPORTED = [
     "visacd_vis_variant_count", "visacd_ctx_set_vis_variant", "visacd_autotune_visibility",
     "visacd_score_planes", "visacd_score_planes_noalloc", "classify_and_rate_planes",
     "visacd_clip", "visacd_clip_fetch", "visacd_measure_fp32_peak", "visacd_face_hausdorff",
-    "visacd_face_hausdorff_floor",
+    "visacd_face_hausdorff_floor", "visacd_face_hausdorff_batch",
     "visacd_batch_create", "visacd_batch_run", "visacd_batch_results", "visacd_batch_info",
     "visacd_batch_destroy",
     "visacd_lp_param_count", "visacd_lp_create", "visacd_lp_destroy", "visacd_lp_get_params",
@@ -108,6 +108,7 @@ def load() -> C.CDLL:
                                           C.POINTER(C.c_double)]
     lib.visacd_face_hausdorff_floor.argtypes = [P, P, i32, P, i32, P, P, i32, P, i32, P, i32, P, P, i32,
                                                 C.c_double, C.POINTER(C.c_double)]
+    lib.visacd_face_hausdorff_batch.argtypes = [P, i32, P, P, P, P, P, P, P, P, C.c_double, i32, P]
     lib.visacd_clip_fetch.argtypes = [P, P, P, P, P, P, P]
     lib.classify_and_rate_planes.argtypes = [P, P, P, P, C.c_int, C.c_int, C.c_int]
     lib.classify_and_rate_planes.restype = None
@@ -317,6 +318,33 @@ class Context:
                                                      _ptr(xb), _ptr(idb), len(xb), float(floor), C.byref(out)),
                    "visacd_face_hausdorff_floor")
         return out.value
+
+    def face_hausdorff_batch(self, jobs, lower=None, floor: float = 0.0, independent: bool = True):
+        """visacd_face_hausdorff_batch over jobs = [(va, ta, xa, ida, vb, tb, xb, idb), ...];
+        returns one value per job."""
+        f = lambda a, c: np.ascontiguousarray(np.asarray(a, dtype=np.float64)).reshape(-1, c)
+        g = lambda a, c: np.ascontiguousarray(np.asarray(a, dtype=np.int32)).reshape(-1, c)
+        vs, ts, xs, ids = [], [], [], []
+        for va, ta, xa, ida, vb, tb, xb, idb in jobs:
+            vs += [f(va, 3), f(vb, 3)]
+            ts += [g(ta, 3), g(tb, 3)]
+            xs += [f(xa, 3), f(xb, 3)]
+            ids += [g(ida, 1).reshape(-1), g(idb, 1).reshape(-1)]
+        cum = lambda arrs: np.concatenate([[0], np.cumsum([len(a) for a in arrs])]).astype(np.int64)
+        voff, toff, soff = cum(vs), cum(ts), cum(xs)
+        cat = lambda arrs, shape, dt: (np.ascontiguousarray(np.concatenate(arrs)) if arrs
+                                       else np.zeros(shape, dt))
+        V = cat(vs, (0, 3), np.float64)
+        T = cat(ts, (0, 3), np.int32)
+        X = cat(xs, (0, 3), np.float64)
+        I = cat(ids, (0,), np.int32)
+        low = None if lower is None else np.ascontiguousarray(np.asarray(lower, dtype=np.float64))
+        out = np.zeros(len(jobs), dtype=np.float64)
+        _check(lib().visacd_face_hausdorff_batch(self._h, len(jobs), _ptr(V), _ptr(voff), _ptr(T), _ptr(toff),
+                                                 _ptr(X), _ptr(I), _ptr(soff), _ptr(low), float(floor),
+                                                 int(bool(independent)), _ptr(out)),
+               "visacd_face_hausdorff_batch")
+        return out
 
     def segment_triangle_tests(self, seg, tri):
         """Independent segment-triangle decisions: (hit bool[S], FP64 re-checks)."""

@@ -216,6 +216,10 @@ class Stager {
   explicit Stager(visacd_ctx* ctx) : ctx_(ctx) {}
   int reserve(size_t total_bytes, int arrays);
   int put(void* dst, const void* src, size_t bytes);
+  // The pinned buffer itself (after reserve): filled in the device layout and
+  // sent with one copy.
+  char* host() { return static_cast<char*>(ctx_->h_upload); }
+  int copy(void* dst, size_t bytes);
 
  private:
   visacd_ctx* ctx_;

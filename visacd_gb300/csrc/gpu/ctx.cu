@@ -180,6 +180,12 @@ int Stager::put(void* dst, const void* src, size_t bytes) {
   return VISACD_OK;
 }
 
+int Stager::copy(void* dst, size_t bytes) {
+  VCHECK(bytes <= cap_, VISACD_ERR_INVALID_ARG, "upload larger than reserved");
+  if (bytes) VCUDA(cudaMemcpyAsync(dst, ctx_->h_upload, bytes, cudaMemcpyHostToDevice, ctx_->stream));
+  return VISACD_OK;
+}
+
 int check_status(visacd_ctx* ctx, const char* what) {
   uint32_t* h = nullptr;
   VTRY(pinned(ctx, 64, (void**)&h));

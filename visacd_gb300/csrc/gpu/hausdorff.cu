@@ -273,11 +273,11 @@ __device__ __forceinline__ float warp_take_min(const float (&fd)[kKnnF], const i
 // order. Same stop rule, same FP32-to-FP64 selection proof and the same term
 // as query_term; returns false (on all lanes) when the proof fails, and the
 // caller then uses query_term. Returns kTermSkipped (on all lanes) as soon as
-// the nearest sample found bounds the term at or below *out_max, or strictly
-// below `floor`: such a term cannot change the result.
+// the nearest sample found bounds the term by a value `prune` accepts (a
+// bound that cannot change the result).
 constexpr int kTermOk = 0, kTermUnproven = 1, kTermSkipped = 2;
-__device__ int query_term_warp(const HSide& S, int qi, double floor, const unsigned long long* out_max,
-                               double& term) {
+template <class Prune>
+__device__ int query_term_warp(const HSide& S, int qi, const Prune& prune, double& term) {
   const int lane = threadIdx.x & 31;
   const HGrid& G = S.G;
   const double q[3] = {S.Q[3 * (int64_t)qi], S.Q[3 * (int64_t)qi + 1], S.Q[3 * (int64_t)qi + 2]};
@@ -327,8 +327,7 @@ __device__ int query_term_warp(const HSide& S, int qi, double floor, const unsig
       float m = nf > 0 ? fd[0] : 3.4e38f;
       for (int o = 16; o; o >>= 1) m = fminf(m, __shfl_xor_sync(0xffffffffu, m, o));
       const double ub = (double)__fadd_ru(__fmul_ru(__fsqrt_ru(m), 1.0f + 1.0f / 1048576.0f), G.eabs);
-      const double cur = __longlong_as_double((long long)*(const volatile unsigned long long*)out_max);
-      if (__shfl_sync(0xffffffffu, (ub <= cur || ub < floor) ? 1 : 0, 0)) return kTermSkipped;
+      if (__shfl_sync(0xffffffffu, prune(ub) ? 1 : 0, 0)) return kTermSkipped;
     }
     if (total >= kKnn) {
       int ptr = 0, id;
@@ -413,26 +412,167 @@ __device__ int query_term_warp(const HSide& S, int qi, double floor, const unsig
   return kTermOk;
 }
 
-// Upper bound of every query's term, one thread per query in its own grid's
-// cell order: the distance to the nearest sample within two rings of cells
-// around the query, in FP32 rounded upwards plus the coordinate rounding
-// bound (the term is at most the distance to the nearest sample, itself at
-// most this). A query with no sample that close gets no bound (+inf) and is
-// appended to farlist (*far entries): those are evaluated one warp each.
-// Entry e = base + position holds the bound and the query's id (bit 31:
-// direction).
+// ---- batched evaluation ----------------------------------------------------
+// A batch holds J jobs; job j compares surface A_j (mesh 2j, sample set 2j)
+// with surface B_j (mesh 2j + 1, sample set 2j + 1). Queries of set s are
+// evaluated against the grid, samples and mesh of set s ^ 1 (sides[s]). All
+// sets, meshes and grids are concatenated; a sample or a triangle finds its
+// set / mesh by binary search in the offset tables.
+struct HBatch {
+  int nsets;                          // 2 J
+  const long long* sample_off;        // nsets + 1
+  const long long* tri_off;           // nsets + 1
+  const long long* vert_off;          // nsets + 1
+  const int* cell0;                   // nsets + 1: first cell of each set's grid
+  const HGrid* grids;                 // nsets (start / order / spts filled in)
+  const HSide* sides;                 // nsets
+  const double* pts;                  // all samples
+  const double* mv;                   // all vertices
+  const int* mt;                      // all triangles (vertex indices local to their mesh)
+  float4* tb;                         // FP32 bounds of all triangles (3 per triangle)
+  const double* lower;                // per job: a known lower bound of the job's concavity (volume term)
+  unsigned long long* job_max;        // per job: largest term found (double bits)
+  unsigned long long* gmax;           // largest of the floor, the lower bounds and every term found
+  const float* tmargin;               // per job
+  int independent;                    // 1: no pruning across jobs
+};
+
+__device__ __forceinline__ int find_seg(const long long* __restrict__ off, int n, long long i) {
+  int lo = 0, hi = n;  // off[lo] <= i < off[hi]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (off[mid] <= i) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ double load_max(const unsigned long long* p) {
+  return __longlong_as_double((long long)*(const volatile unsigned long long*)p);
+}
+
+// Raise the job's maximum and the batch maximum with an exact term.
+__device__ __forceinline__ void publish(const HBatch& H, int job, double term) {
+  atomicMax(H.job_max + job, (unsigned long long)__double_as_longlong(term));
+  if (!H.independent)
+    atomicMax(H.gmax, (unsigned long long)__double_as_longlong(fmax(term, H.lower[job])));
+}
+
+// A term bounded by ub cannot change a result the caller uses when ub is at
+// most the job's own maximum so far, or (pruning across jobs) strictly below
+// the batch maximum: the jobs that attain the batch's largest concavity keep
+// their exact values.
+__device__ __forceinline__ bool prunable(const HBatch& H, int job, double ub) {
+  if (ub <= load_max(H.job_max + job)) return true;
+  return !H.independent && ub < load_max(H.gmax);
+}
+
+// Set-up (one launch): each sample's cell with per-cell counts, and the FP32
+// bounds (box, plane) of every triangle.
+__global__ void hprep_kernel(HBatch H, long long nsamp, long long ntri, int* __restrict__ cnt,
+                             int* __restrict__ cell_of) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nsamp + ntri;
+       i += (long long)gridDim.x * blockDim.x) {
+    if (i < nsamp) {
+      const int s = find_seg(H.sample_off, H.nsets, i);
+      const HGrid& g = H.grids[s];
+      const double* p = H.pts + 3 * i;
+      const int cx = cell_coord(p[0], g.lo[0], g.h, g.dim[0]);
+      const int cy = cell_coord(p[1], g.lo[1], g.h, g.dim[1]);
+      const int cz = cell_coord(p[2], g.lo[2], g.h, g.dim[2]);
+      const int c = (cz * g.dim[1] + cy) * g.dim[0] + cx;
+      cell_of[i] = c;
+      atomicAdd(&cnt[H.cell0[s] + c], 1);
+    } else {
+      const long long j = i - nsamp;
+      const int m = find_seg(H.tri_off, H.nsets, j);
+      const double* mv = H.mv + 3 * H.vert_off[m];
+      const int* t = H.mt + 3 * j;
+      const double* a = mv + 3 * (int64_t)t[0];
+      const double* b = mv + 3 * (int64_t)t[1];
+      const double* c = mv + 3 * (int64_t)t[2];
+      float lo[3], hi[3];
+      for (int q = 0; q < 3; ++q) {
+        lo[q] = __double2float_rd(fmin(fmin(a[q], b[q]), c[q]));
+        hi[q] = __double2float_ru(fmax(fmax(a[q], b[q]), c[q]));
+      }
+      const double ux = b[0] - a[0], uy = b[1] - a[1], uz = b[2] - a[2];
+      const double vx = c[0] - a[0], vy = c[1] - a[1], vz = c[2] - a[2];
+      double nx = uy * vz - uz * vy, ny = uz * vx - ux * vz, nz = ux * vy - uy * vx;
+      const double nl = sqrt(nx * nx + ny * ny + nz * nz);
+      float4 pl = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (nl > 1e-30) {
+        nx /= nl;
+        ny /= nl;
+        nz /= nl;
+        pl = make_float4((float)nx, (float)ny, (float)nz, (float)-(nx * a[0] + ny * a[1] + nz * a[2]));
+      }
+      H.tb[3 * j] = make_float4(lo[0], lo[1], lo[2], 0.f);
+      H.tb[3 * j + 1] = make_float4(hi[0], hi[1], hi[2], 0.f);
+      H.tb[3 * j + 2] = pl;
+    }
+  }
+}
+
+// Counting-sort scatter of every set from the scanned counts: order holds,
+// per set, its local sample indices in cell order.
+__global__ void hscatter_kernel(HBatch H, long long nsamp, const int* __restrict__ cell_of,
+                                const unsigned long long* __restrict__ off, int* __restrict__ fill,
+                                int* __restrict__ order) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nsamp;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int s = find_seg(H.sample_off, H.nsets, i);
+    const int c = H.cell0[s] + cell_of[i];
+    const long long s0 = H.sample_off[s];
+    order[s0 + (long long)(off[c] - off[H.cell0[s]]) + atomicAdd(&fill[c], 1)] = (int)(i - s0);
+  }
+}
+
+// Cell starts of every grid (set s's at start[cell0[s] + s ...], cells + 1
+// entries) and the float copies of every set in cell order (w = local index).
+__global__ void hfinish_kernel(HBatch H, long long nsamp, int ncells, const unsigned long long* __restrict__ off,
+                               const int* __restrict__ order, int* __restrict__ start, float4* __restrict__ spts) {
+  const long long nstart = (long long)ncells + H.nsets;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nstart + nsamp;
+       i += (long long)gridDim.x * blockDim.x) {
+    if (i < nstart) {
+      // entry i belongs to the set s with cell0[s] + s <= i < cell0[s + 1] + s + 1
+      int lo = 0, hi = H.nsets;
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if ((long long)H.cell0[mid] + mid <= i) lo = mid;
+        else hi = mid;
+      }
+      const int c = (int)(i - H.cell0[lo] - lo);
+      start[i] = (int)(off[H.cell0[lo] + c] - off[H.cell0[lo]]);
+    } else {
+      const long long k = i - nstart;
+      const int s = find_seg(H.sample_off, H.nsets, k);
+      const long long s0 = H.sample_off[s];
+      const int q = order[k];
+      const double* p = H.pts + 3 * (s0 + q);
+      spts[k] = make_float4((float)p[0], (float)p[1], (float)p[2], __int_as_float(q));
+    }
+  }
+}
+
+// Upper bound of every query's term, one thread per query (all sets, each in
+// its own grid's cell order): the distance to the nearest sample within two
+// rings of cells around the query, in FP32 rounded upwards plus the
+// coordinate rounding bound (the term is at most the distance to the nearest
+// sample, itself at most this). A query with no sample that close gets no
+// bound (+inf) and is appended to farlist (*far entries): those are evaluated
+// one warp each. qref[e] = (set, local query index).
 constexpr int kBoundRings = 2;
-__global__ void __launch_bounds__(128) hbound_kernel(HSide S0, const int* __restrict__ qorder0, HSide S1,
-                                                     const int* __restrict__ qorder1, float* __restrict__ ubs,
-                                                     uint32_t* __restrict__ vals, unsigned* __restrict__ far,
-                                                     int* __restrict__ farlist) {
-  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < S0.nq + S1.nq; e += gridDim.x * blockDim.x) {
-    const int dir = e < S0.nq ? 0 : 1;
-    const HSide& S = dir ? S1 : S0;
-    const int qk = dir ? e - S0.nq : e;
-    const int base = dir ? S0.nq : 0;
+__global__ void __launch_bounds__(128) hbound_kernel(HBatch H, long long nsamp, const int* __restrict__ order,
+                                                     float* __restrict__ ubs, int2* __restrict__ qref,
+                                                     unsigned* __restrict__ far, long long* __restrict__ farlist) {
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < nsamp;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int s = find_seg(H.sample_off, H.nsets, e);
+    const int qi = order[e];
+    const HSide& S = H.sides[s];
     const HGrid& G = S.G;
-    const int qi = (dir ? qorder1 : qorder0)[qk];
     const double* qq = S.Q + 3 * (int64_t)qi;
     const double q[3] = {qq[0], qq[1], qq[2]};
     const int cx = cell_coord(q[0], G.lo[0], G.h, G.dim[0]);
@@ -468,155 +608,240 @@ __global__ void __launch_bounds__(128) hbound_kernel(HSide S0, const int* __rest
     if (best < 3.4e38f)
       ub = __fadd_ru(__fmul_ru(__fsqrt_ru(best), 1.0f + 1.0f / 1048576.0f), G.eabs);
     else
-      farlist[atomicAdd(far, 1u)] = base + qk;
-    ubs[base + qk] = ub;
-    vals[base + qk] = (uint32_t)qi | ((uint32_t)dir << 31);
+      farlist[atomicAdd(far, 1u)] = e;
+    ubs[e] = ub;
+    qref[e] = make_int2(s, qi);
   }
 }
 
 // Terms of the queries without a bound (the farlist), one warp each: they are
-// far from the other surface, walk many rings, and their exact terms start
-// the running maximum that prunes the rest.
-__global__ void __launch_bounds__(128) hhead_kernel(HSide A, HSide B, const uint32_t* __restrict__ vals,
-                                                    const int* __restrict__ farlist,
-                                                    const unsigned* __restrict__ far, float tmargin, double floor,
-                                                    unsigned long long* __restrict__ out_max) {
+// far from the other surface, walk many rings, and their exact terms raise the
+// maxima that prune the rest.
+__global__ void __launch_bounds__(128) hhead_kernel(HBatch H, const int2* __restrict__ qref,
+                                                    const long long* __restrict__ farlist,
+                                                    const unsigned* __restrict__ far) {
   const int head = (int)*far;
   const int warps = (gridDim.x * blockDim.x) >> 5;
   for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < head; w += warps) {
-    const uint32_t v = vals[farlist[w]];
-    const int qi = (int)(v & 0x7FFFFFFFu);
-    const HSide& S = (v >> 31) ? B : A;
+    const int2 r = qref[farlist[w]];
+    const int job = r.x >> 1;
+    const HSide& S = H.sides[r.x];
     double term;
-    const int status = query_term_warp(S, qi, floor, out_max, term);
+    const int status = query_term_warp(S, r.y, [&](double ub) { return prunable(H, job, ub); }, term);
     if (status == kTermSkipped) continue;
-    if (status == kTermUnproven) term = query_term(S, qi, tmargin);
-    if ((threadIdx.x & 31) == 0 && term < DBL_MAX)
-      atomicMax(out_max, (unsigned long long)__double_as_longlong(term));
+    if (status == kTermUnproven) term = query_term(S, r.y, H.tmargin[job]);
+    if ((threadIdx.x & 31) == 0 && term < DBL_MAX) publish(H, job, term);
   }
 }
 
-// Terms of the queries with a bound (both directions, each in its own grid's
-// cell order), maximum into out_max. A query whose bound does not exceed the
-// maximum found so far cannot raise it and is skipped: the result is the same
-// maximum. So is a query whose bound lies strictly below `floor`.
-__global__ void __launch_bounds__(128) hquery_kernel(HSide A, HSide B, const float* __restrict__ ubs,
-                                                     const uint32_t* __restrict__ vals, int end, float tmargin,
-                                                     double floor, unsigned long long* __restrict__ out_max) {
-  double local = 0.0;
-  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < end; e += gridDim.x * blockDim.x) {
+// Terms of the queries with a bound; a query whose bound cannot change a used
+// result (prunable) is skipped.
+__global__ void __launch_bounds__(128) hquery_kernel(HBatch H, const float* __restrict__ ubs,
+                                                     const int2* __restrict__ qref, long long nsamp) {
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < nsamp;
+       e += (long long)gridDim.x * blockDim.x) {
     const float ub = ubs[e];
     if (!(ub < __int_as_float(0x7f800000))) continue;  // no bound: evaluated by hhead_kernel
-    const double cur = __longlong_as_double((long long)*(volatile unsigned long long*)out_max);
-    if ((double)ub <= fmax(cur, local) || (double)ub < floor) continue;
-    const uint32_t v = vals[e];
-    const int qi = (int)(v & 0x7FFFFFFFu);
-    const double cmin = (v >> 31) ? query_term(B, qi, tmargin) : query_term(A, qi, tmargin);
-    if (cmin > local && DBL_MAX > cmin) local = cmin;
+    const int2 r = qref[e];
+    const int job = r.x >> 1;
+    if (prunable(H, job, (double)ub)) continue;
+    const double cmin = query_term(H.sides[r.x], r.y, H.tmargin[job]);
+    if (DBL_MAX > cmin) publish(H, job, cmin);
   }
-  for (int o = 16; o; o >>= 1) local = fmax(local, __shfl_xor_sync(0xffffffffu, local, o));
-  if ((threadIdx.x & 31) == 0) atomicMax(out_max, (unsigned long long)__double_as_longlong(local));
 }
 
 }  // namespace vgpu
 
 using namespace vgpu;
 
-// Fused set-up of both sample sets and both meshes (one launch): the cell of
-// every sample with per-cell counts (set B's cells follow set A's in one count
-// array), and the FP32 triangle bounds of both meshes.
-__global__ void hprep_kernel(HGrid ga, HGrid gb, int cells_a, int* __restrict__ cnt, int* __restrict__ cell_a,
-                             int* __restrict__ cell_b, const double* __restrict__ mva, const int* __restrict__ mta,
-                             int nta, float4* __restrict__ tba, const double* __restrict__ mvb,
-                             const int* __restrict__ mtb, int ntb, float4* __restrict__ tbb) {
-  const int64_t total = (int64_t)ga.n + gb.n + nta + ntb;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-    if (i < ga.n || i < (int64_t)ga.n + gb.n) {
-      const bool isa = i < ga.n;
-      const HGrid& g = isa ? ga : gb;
-      const int k = isa ? (int)i : (int)(i - ga.n);
-      const double* p = g.pts + 3 * (int64_t)k;
-      const int cx = cell_coord(p[0], g.lo[0], g.h, g.dim[0]);
-      const int cy = cell_coord(p[1], g.lo[1], g.h, g.dim[1]);
-      const int cz = cell_coord(p[2], g.lo[2], g.h, g.dim[2]);
-      const int c = (cz * g.dim[1] + cy) * g.dim[0] + cx;
-      (isa ? cell_a : cell_b)[k] = c;
-      atomicAdd(&cnt[(isa ? 0 : cells_a) + c], 1);
-    } else {
-      const int64_t j = i - ga.n - gb.n;
-      const bool isa = j < nta;
-      const int t = isa ? (int)j : (int)(j - nta);
-      const double* mv = isa ? mva : mvb;
-      const int* mt = isa ? mta : mtb;
-      float4* out = isa ? tba : tbb;
-      const double* a = mv + 3 * (int64_t)mt[3 * (int64_t)t];
-      const double* b = mv + 3 * (int64_t)mt[3 * (int64_t)t + 1];
-      const double* c = mv + 3 * (int64_t)mt[3 * (int64_t)t + 2];
-      float lo[3], hi[3];
-      for (int q = 0; q < 3; ++q) {
-        lo[q] = __double2float_rd(fmin(fmin(a[q], b[q]), c[q]));
-        hi[q] = __double2float_ru(fmax(fmax(a[q], b[q]), c[q]));
-      }
-      const double ux = b[0] - a[0], uy = b[1] - a[1], uz = b[2] - a[2];
-      const double vx = c[0] - a[0], vy = c[1] - a[1], vz = c[2] - a[2];
-      double nx = uy * vz - uz * vy, ny = uz * vx - ux * vz, nz = ux * vy - uy * vx;
-      const double nl = sqrt(nx * nx + ny * ny + nz * nz);
-      float4 pl = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (nl > 1e-30) {
-        nx /= nl;
-        ny /= nl;
-        nz /= nl;
-        pl = make_float4((float)nx, (float)ny, (float)nz, (float)-(nx * a[0] + ny * a[1] + nz * a[2]));
-      }
-      out[3 * (int64_t)t] = make_float4(lo[0], lo[1], lo[2], 0.f);
-      out[3 * (int64_t)t + 1] = make_float4(hi[0], hi[1], hi[2], 0.f);
-      out[3 * (int64_t)t + 2] = pl;
-    }
-  }
-}
-
-// Counting-sort scatter of both sets (one launch) from the scanned counts.
-__global__ void hscatter2_kernel(int na, int nb, int cells_a, const int* __restrict__ cell_a,
-                                 const int* __restrict__ cell_b, const unsigned long long* __restrict__ off,
-                                 int* __restrict__ fill, int* __restrict__ order_a, int* __restrict__ order_b) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < na + nb; i += gridDim.x * blockDim.x) {
-    if (i < na) {
-      const int c = cell_a[i];
-      order_a[off[c] + atomicAdd(&fill[c], 1)] = i;
-    } else {
-      const int j = i - na, c = cells_a + cell_b[j];
-      order_b[off[c] - off[cells_a] + atomicAdd(&fill[c], 1)] = j;
-    }
-  }
-}
-
-// Cell starts of both grids and the float copies of both sets in cell order.
-__global__ void hfinish_kernel(int cells_a, int cells_b, const unsigned long long* __restrict__ off,
-                               int* __restrict__ start_a, int* __restrict__ start_b, const double* __restrict__ pa,
-                               const int* __restrict__ order_a, int na, float4* __restrict__ spa,
-                               const double* __restrict__ pb, const int* __restrict__ order_b, int nb,
-                               float4* __restrict__ spb) {
-  const int64_t total = (int64_t)cells_a + 1 + cells_b + 1 + na + nb;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-    if (i <= cells_a) {
-      start_a[i] = (int)off[i];
-    } else if (i <= (int64_t)cells_a + 1 + cells_b) {
-      const int c = (int)(i - cells_a - 1);
-      start_b[c] = (int)(off[cells_a + c] - off[cells_a]);
-    } else {
-      const int64_t k0 = i - cells_a - cells_b - 2;
-      const bool isa = k0 < na;
-      const int k = isa ? (int)k0 : (int)(k0 - na);
-      const double* pts = isa ? pa : pb;
-      const int q = (isa ? order_a : order_b)[k];
-      (isa ? spa : spb)[k] = make_float4((float)pts[3 * (int64_t)q], (float)pts[3 * (int64_t)q + 1],
-                                         (float)pts[3 * (int64_t)q + 2], __int_as_float(q));
-    }
-  }
-}
-
 namespace {
 size_t al(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Grid over a sample set: about 2 samples per occupied cell on a surface, at
+// most 160 cells per axis.
+void grid_for_points(const double* x, long long n, HGrid& g) {
+  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+  for (long long i = 0; i < n; ++i)
+    for (int a = 0; a < 3; ++a) {
+      lo[a] = std::min(lo[a], x[3 * i + a]);
+      hi[a] = std::max(hi[a], x[3 * i + a]);
+    }
+  double ext = std::max(hi[0] - lo[0], std::max(hi[1] - lo[1], hi[2] - lo[2]));
+  double area_like = 0;
+  for (int a = 0; a < 3; ++a) area_like += (hi[a] - lo[a]) * (hi[(a + 1) % 3] - lo[(a + 1) % 3]);
+  double h = std::sqrt(std::max(area_like, 1e-30) * 2.0 / (double)std::max(n, 1LL));
+  h = std::max(h, ext / 160.0);
+  if (!(h > 0)) h = 1.0;
+  for (int a = 0; a < 3; ++a) {
+    g.lo[a] = lo[a];
+    g.dim[a] = std::max(1, (int)std::ceil((hi[a] - lo[a]) / h) + 1);
+  }
+  g.h = h;
+  g.n = (int)n;
+}
+}  // namespace
+
+extern "C" int visacd_face_hausdorff_batch(visacd_ctx* ctx, int32_t njobs, const double* verts,
+                                           const int64_t* vert_off, const int32_t* tris, const int64_t* tri_off,
+                                           const double* samples, const int32_t* sample_tri,
+                                           const int64_t* sample_off, const double* lower, double floor,
+                                           int32_t independent, double* out) {
+  VCHECK(ctx && out && vert_off && tri_off && sample_off, VISACD_ERR_INVALID_ARG,
+         "face_hausdorff_batch: null argument");
+  VCHECK(njobs >= 0, VISACD_ERR_INVALID_ARG, "face_hausdorff_batch: negative job count");
+  VCHECK(floor == floor, VISACD_ERR_INVALID_ARG, "face_hausdorff_batch: floor is NaN");
+  if (njobs == 0) return VISACD_OK;
+  const int S = 2 * njobs;
+  VCHECK(vert_off[0] == 0 && tri_off[0] == 0 && sample_off[0] == 0, VISACD_ERR_INVALID_ARG,
+         "face_hausdorff_batch: offsets must start at 0");
+  for (int s = 0; s < S; ++s) {
+    const int64_t nv = vert_off[s + 1] - vert_off[s], nt = tri_off[s + 1] - tri_off[s],
+                  ns = sample_off[s + 1] - sample_off[s];
+    VCHECK(nv > 0 && nt > 0 && ns > 0, VISACD_ERR_INVALID_ARG, "face_hausdorff_batch: empty surface %d", s);
+    for (int64_t k = 3 * tri_off[s]; k < 3 * tri_off[s + 1]; ++k)
+      VCHECK(tris[k] >= 0 && tris[k] < nv, VISACD_ERR_INVALID_ARG,
+             "face_hausdorff_batch: vertex index out of range");
+    for (int64_t k = sample_off[s]; k < sample_off[s + 1]; ++k)
+      VCHECK(sample_tri[k] >= 0 && sample_tri[k] < nt, VISACD_ERR_INVALID_ARG,
+             "face_hausdorff_batch: sample triangle out of range");
+  }
+  VCHECK(verts && tris && samples && sample_tri, VISACD_ERR_INVALID_ARG, "face_hausdorff_batch: null array");
+  if (lower)
+    for (int j = 0; j < njobs; ++j)
+      VCHECK(lower[j] == lower[j], VISACD_ERR_INVALID_ARG, "face_hausdorff_batch: lower bound is NaN");
+  VCUDA(cudaSetDevice(ctx->device));
+  const long long NV = vert_off[S], NT = tri_off[S], NS = sample_off[S];
+  // Grids and rounding bounds per job (both sets of a job share M).
+  std::vector<HGrid> grids(S);
+  std::vector<float> tmargin(njobs);
+  std::vector<int> cell0(S + 1, 0);
+  for (int s = 0; s < S; ++s) grid_for_points(samples + 3 * sample_off[s], sample_off[s + 1] - sample_off[s], grids[s]);
+  for (int j = 0; j < njobs; ++j) {
+    // FP32 pre-filter bound: coordinates rounded to float differ by at most
+    // 2^-24 |x| each, the difference and the squared sum add a few ulps; with
+    // M the largest |coordinate| of both sets, |d_f32 - d| <= 8 M 2^-24.
+    double M = 0;
+    for (int k = 2 * j; k < 2 * j + 2; ++k)
+      for (int a = 0; a < 3; ++a)
+        M = std::max(M, std::max(std::fabs(grids[k].lo[a]), std::fabs(grids[k].lo[a] + grids[k].h * grids[k].dim[a])));
+    for (int k = 2 * j; k < 2 * j + 2; ++k) grids[k].eabs = (float)(M * std::ldexp(1.0, -21) + 1e-30);
+    // Margin of the FP32 triangle lower bounds: the plane evaluation's rounding
+    // (normal and offset rounded to float, a few ulps of the largest
+    // coordinate), with room to spare; the box gap is conservative.
+    tmargin[j] = (float)(1e-9 + 256.0 * std::ldexp(1.0, -24) * (M + 4.0));
+  }
+  for (int s = 0; s < S; ++s) cell0[s + 1] = cell0[s] + grids[s].dim[0] * grids[s].dim[1] * grids[s].dim[2];
+  const int ncell = cell0[S];
+  double gmax0 = std::max(floor, 0.0);
+  std::vector<double> low(njobs, 0.0);
+  if (lower)
+    for (int j = 0; j < njobs; ++j) {
+      low[j] = std::max(lower[j], 0.0);
+      gmax0 = std::max(gmax0, low[j]);
+    }
+  // Device layout: the uploaded block first (one copy), then the scratch.
+  size_t off = 0;
+  auto carve = [&](size_t b) { size_t o = off; off += al(b); return o; };
+  const size_t o_v = carve((size_t)NV * 24), o_t = carve((size_t)NT * 12), o_x = carve((size_t)NS * 24),
+               o_id = carve((size_t)NS * 4), o_soff = carve((size_t)(S + 1) * 8), o_toff = carve((size_t)(S + 1) * 8),
+               o_voff = carve((size_t)(S + 1) * 8), o_c0 = carve((size_t)(S + 1) * 4),
+               o_low = carve((size_t)njobs * 8), o_tm = carve((size_t)njobs * 4), o_gm = carve(8),
+               o_grids = carve(sizeof(HGrid) * S), o_sides = carve(sizeof(HSide) * S);
+  const size_t upload = off;
+  // Zeroed together: job maxima, far count, per-cell counts and fills.
+  const size_t zero_begin = off;
+  const size_t o_jm = carve((size_t)njobs * 8), o_far = carve(8), o_cnt = carve((size_t)(ncell + 1) * 4),
+               o_fill = carve((size_t)ncell * 4);
+  const size_t zero_end = off;
+  const size_t o_off = carve((size_t)(ncell + 1) * 8), o_cell = carve((size_t)NS * 4),
+               o_order = carve((size_t)NS * 4), o_start = carve((size_t)(ncell + S) * 4),
+               o_spts = carve((size_t)NS * 16), o_tb = carve((size_t)NT * 48), o_ub = carve((size_t)NS * 4),
+               o_qref = carve((size_t)NS * 8), o_farl = carve((size_t)NS * 8);
+  VTRY(ensure_slot(ctx, kSlotHausdorff, off));
+  char* D = slot<char>(ctx, kSlotHausdorff);
+  cudaStream_t st = ctx->stream;
+  // Device pointers of every grid and side.
+  for (int s = 0; s < S; ++s) {
+    HGrid& g = grids[s];
+    g.start = (const int*)(D + o_start) + cell0[s] + s;
+    g.order = (const int*)(D + o_order) + sample_off[s];
+    g.pts = (const double*)(D + o_x) + 3 * sample_off[s];
+    g.spts = (const float4*)(D + o_spts) + sample_off[s];
+  }
+  std::vector<HSide> sides(S);
+  for (int s = 0; s < S; ++s) {
+    const int o = s ^ 1;
+    HSide& d = sides[s];
+    d.Q = (const double*)(D + o_x) + 3 * sample_off[s];
+    d.nq = (int)(sample_off[s + 1] - sample_off[s]);
+    d.G = grids[o];
+    d.ids = (const int*)(D + o_id) + sample_off[o];
+    d.mv = (const double*)(D + o_v) + 3 * vert_off[o];
+    d.mt = (const int*)(D + o_t) + 3 * tri_off[o];
+    d.tb = (const float4*)(D + o_tb) + 3 * tri_off[o];
+  }
+  Stager up(ctx);
+  VTRY(up.reserve(upload, 1));
+  char* h = up.host();
+  auto put = [&](size_t o, const void* src, size_t bytes) {
+    if (bytes) std::memcpy(h + o, src, bytes);
+  };
+  put(o_v, verts, (size_t)NV * 24);
+  put(o_t, tris, (size_t)NT * 12);
+  put(o_x, samples, (size_t)NS * 24);
+  put(o_id, sample_tri, (size_t)NS * 4);
+  put(o_soff, sample_off, (size_t)(S + 1) * 8);
+  put(o_toff, tri_off, (size_t)(S + 1) * 8);
+  put(o_voff, vert_off, (size_t)(S + 1) * 8);
+  put(o_c0, cell0.data(), (size_t)(S + 1) * 4);
+  put(o_low, low.data(), (size_t)njobs * 8);
+  put(o_tm, tmargin.data(), (size_t)njobs * 4);
+  put(o_gm, &gmax0, 8);
+  put(o_grids, grids.data(), sizeof(HGrid) * S);
+  put(o_sides, sides.data(), sizeof(HSide) * S);
+  VTRY(up.copy(D, upload));
+  VCUDA(cudaMemsetAsync(D + zero_begin, 0, zero_end - zero_begin, st));
+  HBatch H;
+  H.nsets = S;
+  H.sample_off = (const long long*)(D + o_soff);
+  H.tri_off = (const long long*)(D + o_toff);
+  H.vert_off = (const long long*)(D + o_voff);
+  H.cell0 = (const int*)(D + o_c0);
+  H.grids = (const HGrid*)(D + o_grids);
+  H.sides = (const HSide*)(D + o_sides);
+  H.pts = (const double*)(D + o_x);
+  H.mv = (const double*)(D + o_v);
+  H.mt = (const int*)(D + o_t);
+  H.tb = (float4*)(D + o_tb);
+  H.lower = (const double*)(D + o_low);
+  H.job_max = (unsigned long long*)(D + o_jm);
+  H.gmax = (unsigned long long*)(D + o_gm);
+  H.tmargin = (const float*)(D + o_tm);
+  H.independent = independent ? 1 : 0;
+  int* cnt = (int*)(D + o_cnt);
+  unsigned long long* offs = (unsigned long long*)(D + o_off);
+  const unsigned gp = grid_for(NS + NT, 256, 8LL * ctx->sm_count), gs = grid_for(NS, 256, 8LL * ctx->sm_count);
+  VLAUNCH(ctx, kKHausdorff, gp, 256, 0, hprep_kernel, H, NS, NT, cnt, (int*)(D + o_cell));
+  VTRY(exclusive_scan_u32_to_u64(ctx, (const uint32_t*)cnt, (uint64_t*)offs, ncell));
+  VLAUNCH(ctx, kKHausdorff, gs, 256, 0, hscatter_kernel, H, NS, (const int*)(D + o_cell),
+          (const unsigned long long*)offs, (int*)(D + o_fill), (int*)(D + o_order));
+  VLAUNCH(ctx, kKHausdorff, grid_for(NS + ncell + S, 256, 8LL * ctx->sm_count), 256, 0, hfinish_kernel, H, NS,
+          ncell, (const unsigned long long*)offs, (const int*)(D + o_order), (int*)(D + o_start),
+          (float4*)(D + o_spts));
+  unsigned* far = (unsigned*)(D + o_far);
+  VLAUNCH(ctx, kKHausdorffBound, grid_for(NS, 128, 8LL * ctx->sm_count), 128, 0, hbound_kernel, H, NS,
+          (const int*)(D + o_order), (float*)(D + o_ub), (int2*)(D + o_qref), far, (long long*)(D + o_farl));
+  // The queries without a bound one warp each, then the rest with pruning.
+  VLAUNCH(ctx, kKHausdorffHead, grid_for(32LL * NS, 128, 8LL * ctx->sm_count), 128, 0, hhead_kernel, H,
+          (const int2*)(D + o_qref), (const long long*)(D + o_farl), (const unsigned*)far);
+  VLAUNCH(ctx, kKHausdorffQuery, grid_for(NS, 128, 8LL * ctx->sm_count), 128, 0, hquery_kernel, H,
+          (const float*)(D + o_ub), (const int2*)(D + o_qref), NS);
+  double* hres = nullptr;
+  VTRY(pinned(ctx, (size_t)njobs * 8, (void**)&hres));
+  VCUDA(cudaMemcpyAsync(hres, D + o_jm, (size_t)njobs * 8, cudaMemcpyDeviceToHost, st));
+  VCUDA(cudaStreamSynchronize(st));
+  std::memcpy(out, hres, (size_t)njobs * 8);
+  return VISACD_OK;
 }
 
 extern "C" int visacd_face_hausdorff_floor(visacd_ctx* ctx, const double* va, int32_t nva, const int32_t* ta,
@@ -625,134 +850,24 @@ extern "C" int visacd_face_hausdorff_floor(visacd_ctx* ctx, const double* va, in
                                            const double* xb, const int32_t* idb, int32_t nb, double floor,
                                            double* out) {
   VCHECK(ctx && out, VISACD_ERR_INVALID_ARG, "face_hausdorff: null argument");
-  VCHECK(floor == floor, VISACD_ERR_INVALID_ARG, "face_hausdorff: floor is NaN");
   VCHECK(na > 0 && nb > 0 && nva > 0 && nvb > 0 && nta > 0 && ntb > 0, VISACD_ERR_INVALID_ARG,
          "face_hausdorff: empty input");
-  VCUDA(cudaSetDevice(ctx->device));
-  // Grid shape from the sample counts: about 2 samples per occupied cell on a
-  // surface; at most 160 cells per axis.
-  auto grid_for_points = [](const double* x, int n, HGrid& g) {
-    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-    for (int i = 0; i < n; ++i)
-      for (int a = 0; a < 3; ++a) {
-        lo[a] = std::min(lo[a], x[3 * (int64_t)i + a]);
-        hi[a] = std::max(hi[a], x[3 * (int64_t)i + a]);
-      }
-    double ext = std::max(hi[0] - lo[0], std::max(hi[1] - lo[1], hi[2] - lo[2]));
-    double area_like = 0;
-    for (int a = 0; a < 3; ++a) area_like += (hi[a] - lo[a]) * (hi[(a + 1) % 3] - lo[(a + 1) % 3]);
-    double h = std::sqrt(std::max(area_like, 1e-30) * 2.0 / std::max(n, 1));
-    h = std::max(h, ext / 160.0);
-    if (!(h > 0)) h = 1.0;
-    for (int a = 0; a < 3; ++a) {
-      g.lo[a] = lo[a];
-      g.dim[a] = std::max(1, (int)std::ceil((hi[a] - lo[a]) / h) + 1);
-    }
-    g.h = h;
-    g.n = n;
-  };
-  // One grid over each sample set (g[0] over A, g[1] over B).
-  HGrid g[2];
-  grid_for_points(xa, na, g[0]);
-  grid_for_points(xb, nb, g[1]);
-  // FP32 pre-filter bound: coordinates rounded to float differ by at most
-  // 2^-24 |x| each, the difference and the squared sum add a few ulps; with
-  // M the largest |coordinate| of both sets, |d_f32 - d| <= 8 M 2^-24.
-  double M = 0;
-  for (int k = 0; k < 2; ++k)
-    for (int a = 0; a < 3; ++a)
-      M = std::max(M, std::max(std::fabs(g[k].lo[a]), std::fabs(g[k].lo[a] + g[k].h * g[k].dim[a])));
-  for (int k = 0; k < 2; ++k) g[k].eabs = (float)(M * std::ldexp(1.0, -21) + 1e-30);
-  int cells[2];
-  for (int k = 0; k < 2; ++k) cells[k] = g[k].dim[0] * g[k].dim[1] * g[k].dim[2];
-  const int ncell = cells[0] + cells[1];
-  size_t off = 0;
-  auto carve = [&](size_t b) { size_t o = off; off += al(b); return o; };
-  const size_t o_va = carve((size_t)nva * 24), o_ta = carve((size_t)nta * 12), o_xa = carve((size_t)na * 24),
-               o_ia = carve((size_t)na * 4), o_vb = carve((size_t)nvb * 24), o_tb = carve((size_t)ntb * 12),
-               o_xb = carve((size_t)nb * 24), o_ib = carve((size_t)nb * 4), o_tba = carve((size_t)nta * 48),
-               o_tbb = carve((size_t)ntb * 48), o_ub = carve((size_t)(na + nb) * 4),
-               o_vals = carve((size_t)(na + nb) * 4), o_far = carve((size_t)(na + nb) * 4);
-  // Zeroed together: maximum + far count, per-cell counts and fills of both grids.
-  const size_t zero_begin = off;
-  const size_t o_mx = carve(64), o_cnt = carve((size_t)(ncell + 1) * 4), o_fill = carve((size_t)ncell * 4);
-  const size_t zero_end = off;
-  const size_t o_off = carve((size_t)(ncell + 1) * 8), o_sa = carve((size_t)(cells[0] + 1) * 4),
-               o_sb = carve((size_t)(cells[1] + 1) * 4), o_oa = carve((size_t)na * 4), o_ob = carve((size_t)nb * 4),
-               o_ca = carve((size_t)na * 4), o_cb = carve((size_t)nb * 4), o_pa = carve((size_t)na * 16),
-               o_pb = carve((size_t)nb * 16);
-  VTRY(ensure_slot(ctx, kSlotHausdorff, off));
-  char* B = slot<char>(ctx, kSlotHausdorff);
-  cudaStream_t st = ctx->stream;
-  Stager up(ctx);
-  VTRY(up.reserve((size_t)nva * 24 + (size_t)nta * 12 + (size_t)na * 28 + (size_t)nvb * 24 + (size_t)ntb * 12 +
-                      (size_t)nb * 28,
-                  8));
-  VTRY(up.put(B + o_va, va, (size_t)nva * 24));
-  VTRY(up.put(B + o_ta, ta, (size_t)nta * 12));
-  VTRY(up.put(B + o_xa, xa, (size_t)na * 24));
-  VTRY(up.put(B + o_ia, ida, (size_t)na * 4));
-  VTRY(up.put(B + o_vb, vb, (size_t)nvb * 24));
-  VTRY(up.put(B + o_tb, tb, (size_t)ntb * 12));
-  VTRY(up.put(B + o_xb, xb, (size_t)nb * 24));
-  VTRY(up.put(B + o_ib, idb, (size_t)nb * 4));
-  VCUDA(cudaMemsetAsync(B + zero_begin, 0, zero_end - zero_begin, st));
-  g[0].pts = (const double*)(B + o_xa);
-  g[1].pts = (const double*)(B + o_xb);
-  g[0].n = na;
-  g[1].n = nb;
-  const unsigned long long* offs = (const unsigned long long*)(B + o_off);
-  // Both sets bucketed by counting sort (counts, one scan, scatter, starts)
-  // and both meshes' triangle bounds: four launches plus the scan.
-  VLAUNCH(ctx, kKHausdorff, grid_for((int64_t)na + nb + nta + ntb, 256, 8LL * ctx->sm_count), 256, 0, hprep_kernel,
-          g[0], g[1], cells[0], (int*)(B + o_cnt), (int*)(B + o_ca), (int*)(B + o_cb), (const double*)(B + o_va),
-          (const int*)(B + o_ta), nta, (float4*)(B + o_tba), (const double*)(B + o_vb), (const int*)(B + o_tb), ntb,
-          (float4*)(B + o_tbb));
-  VTRY(exclusive_scan_u32_to_u64(ctx, (const uint32_t*)(B + o_cnt), (uint64_t*)(B + o_off), ncell));
-  VLAUNCH(ctx, kKHausdorff, grid_for((int64_t)na + nb, 256, 8LL * ctx->sm_count), 256, 0, hscatter2_kernel, na, nb,
-          cells[0], (const int*)(B + o_ca), (const int*)(B + o_cb), offs, (int*)(B + o_fill), (int*)(B + o_oa),
-          (int*)(B + o_ob));
-  VLAUNCH(ctx, kKHausdorff, grid_for((int64_t)ncell + 2 + na + nb, 256, 8LL * ctx->sm_count), 256, 0,
-          hfinish_kernel, cells[0], cells[1], offs, (int*)(B + o_sa), (int*)(B + o_sb), (const double*)(B + o_xa),
-          (const int*)(B + o_oa), na, (float4*)(B + o_pa), (const double*)(B + o_xb), (const int*)(B + o_ob), nb,
-          (float4*)(B + o_pb));
-  g[0].start = (const int*)(B + o_sa);
-  g[1].start = (const int*)(B + o_sb);
-  g[0].order = (const int*)(B + o_oa);
-  g[1].order = (const int*)(B + o_ob);
-  g[0].spts = (const float4*)(B + o_pa);
-  g[1].spts = (const float4*)(B + o_pb);
-  unsigned long long* mx = (unsigned long long*)(B + o_mx);
-  // Margin of the FP32 lower bounds: the plane evaluation's rounding (normal
-  // and offset rounded to float, a few ulps of the largest coordinate), with
-  // room to spare; the box gap is conservative by construction.
-  const float tmargin = (float)(1e-9 + 256.0 * std::ldexp(1.0, -24) * (M + 4.0));
-  // Direction 0: queries of B against A's samples / triangles; direction 1:
-  // queries of A against B.
-  HSide sd0{(const double*)(B + o_xb), nb, g[0], (const int*)(B + o_ia), (const double*)(B + o_va),
-            (const int*)(B + o_ta), (const float4*)(B + o_tba)};
-  HSide sd1{(const double*)(B + o_xa), na, g[1], (const int*)(B + o_ib), (const double*)(B + o_vb),
-            (const int*)(B + o_tb), (const float4*)(B + o_tbb)};
-  const int ntot = na + nb;
-  uint32_t* vals = (uint32_t*)(B + o_vals);
-  unsigned* far = (unsigned*)(B + o_mx + 8);  // zeroed with the maximum
-  float* ubs = (float*)(B + o_ub);
-  int* farlist = (int*)(B + o_far);
-  VLAUNCH(ctx, kKHausdorffBound, grid_for(ntot, 128, 8LL * ctx->sm_count), 128, 0, hbound_kernel, sd0, g[1].order,
-          sd1, g[0].order, ubs, vals, far, farlist);
-  // The queries without a bound one warp each, then the rest with pruning.
-  VLAUNCH(ctx, kKHausdorffHead, grid_for(32LL * ntot, 128, 8LL * ctx->sm_count), 128, 0, hhead_kernel, sd0, sd1,
-          (const uint32_t*)vals, (const int*)farlist, (const unsigned*)far, tmargin, floor, mx);
-  VLAUNCH(ctx, kKHausdorffQuery, grid_for(ntot, 128, 8LL * ctx->sm_count), 128, 0, hquery_kernel, sd0, sd1,
-          (const float*)ubs, (const uint32_t*)vals, ntot, tmargin, floor, mx);
-  unsigned long long* h = nullptr;
-  VTRY(pinned(ctx, 8, (void**)&h));
-  VCUDA(cudaMemcpyAsync(h, mx, 8, cudaMemcpyDeviceToHost, st));
-  VCUDA(cudaStreamSynchronize(st));
-  double r;
-  memcpy(&r, h, 8);
-  *out = r;
-  return VISACD_OK;
+  VCHECK(va && ta && xa && ida && vb && tb && xb && idb, VISACD_ERR_INVALID_ARG, "face_hausdorff: null array");
+  // One job: the two surfaces' arrays side by side.
+  std::vector<double> v((size_t)(nva + nvb) * 3), x((size_t)(na + nb) * 3);
+  std::vector<int32_t> t((size_t)(nta + ntb) * 3), id((size_t)(na + nb));
+  std::memcpy(v.data(), va, (size_t)nva * 24);
+  std::memcpy(v.data() + 3 * (size_t)nva, vb, (size_t)nvb * 24);
+  std::memcpy(t.data(), ta, (size_t)nta * 12);
+  std::memcpy(t.data() + 3 * (size_t)nta, tb, (size_t)ntb * 12);
+  std::memcpy(x.data(), xa, (size_t)na * 24);
+  std::memcpy(x.data() + 3 * (size_t)na, xb, (size_t)nb * 24);
+  std::memcpy(id.data(), ida, (size_t)na * 4);
+  std::memcpy(id.data() + na, idb, (size_t)nb * 4);
+  const int64_t voff[3] = {0, nva, (int64_t)nva + nvb}, toff[3] = {0, nta, (int64_t)nta + ntb},
+                soff[3] = {0, na, (int64_t)na + nb};
+  return visacd_face_hausdorff_batch(ctx, 1, v.data(), voff, t.data(), toff, x.data(), id.data(), soff, nullptr,
+                                     floor, 0, out);
 }
 
 extern "C" int visacd_face_hausdorff(visacd_ctx* ctx, const double* va, int32_t nva, const int32_t* ta,

@@ -150,6 +150,13 @@ inline double canonical53(uint32_t lo, uint32_t hi) {
   return r < 1.0 ? r : 0x1.fffffffffffffp-1;
 }
 
+// Surface samples of a pair of meshes for the concavity metric (points and the
+// triangle each was drawn from).
+struct HbSamples {
+  std::vector<Vec3> s1, s2;
+  std::vector<int> i1, i2;
+};
+
 // The process-wide engine, or the calling thread's own one while a
 // process_batch worker has installed it (set_thread_engine(nullptr) clears).
 Mt19937& random_engine();

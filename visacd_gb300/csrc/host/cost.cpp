@@ -299,6 +299,43 @@ double eval_hb(const Mesh& a, const Mesh& b, const HbSamples& s, double floor) {
   return h;
 }
 
+std::vector<double> eval_hb_batch(const std::vector<const Mesh*>& a, const std::vector<const Mesh*>& b,
+                                  const std::vector<const HbSamples*>& s, const std::vector<double>& lower,
+                                  double floor, bool independent) {
+  const size_t J = a.size();
+  std::vector<double> out(J, kInf);
+  if (!config().gpu_concavity) {
+    for (size_t j = 0; j < J; ++j) out[j] = eval_hb(*a[j], *b[j], *s[j]);
+    return out;
+  }
+  auto& tm = concavity_times();
+  const auto t0 = std::chrono::steady_clock::now();
+  // Jobs without samples are kInf (as eval_hb); the rest go in one call, with
+  // the floor raised to the kInf concavities when pruning across jobs.
+  std::vector<const Mesh*> ga, gb;
+  std::vector<const HbSamples*> gs;
+  std::vector<double> gl;
+  std::vector<size_t> where;
+  for (size_t j = 0; j < J; ++j) {
+    if (s[j]->s1.empty() || s[j]->s2.empty()) {
+      floor = std::max(floor, kInf);
+      continue;
+    }
+    ga.push_back(a[j]);
+    gb.push_back(b[j]);
+    gs.push_back(s[j]);
+    if (!lower.empty()) gl.push_back(lower[j]);
+    where.push_back(j);
+  }
+  if (!where.empty()) {
+    const std::vector<double> r = gpu::face_hausdorff_batch(ga, gb, gs, gl, independent ? 0.0 : floor, independent);
+    for (size_t k = 0; k < where.size(); ++k) out[where[k]] = r[k];
+  }
+  tm.hausdorff_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  tm.calls += (long long)where.size();
+  return out;
+}
+
 double compute_hb(const Mesh& a, const Mesh& b, unsigned int resolution) {
   HbSamples s;
   sample_hb(a, b, resolution, s);

@@ -53,12 +53,16 @@ double compute_hb(const Mesh& a, const Mesh& b, unsigned int resolution);
 // the reference's order), then the value. With floor > 0 the value is exact
 // when it is >= floor and some value below floor otherwise (the GPU skips the
 // sample terms that cannot reach floor); the host metric is always exact.
-struct HbSamples {
-  std::vector<Vec3> s1, s2;
-  std::vector<int> i1, i2;
-};
 void sample_hb(const Mesh& a, const Mesh& b, unsigned int resolution, HbSamples& s);
 double eval_hb(const Mesh& a, const Mesh& b, const HbSamples& s, double floor = 0.0);
+// eval_hb of many pairs in one GPU call: job j is (a[j], b[j], s[j]). With
+// `independent` every value is exact; otherwise, with lower[j] a known lower
+// bound of job j's concavity and M the largest of floor and every
+// max(lower[j], value[j]), the jobs whose value equals M get it exactly and the
+// others some value not above theirs (the host metric is always exact).
+std::vector<double> eval_hb_batch(const std::vector<const Mesh*>& a, const std::vector<const Mesh*>& b,
+                                  const std::vector<const HbSamples*>& s, const std::vector<double>& lower,
+                                  double floor, bool independent);
 double compute_hb3(const Mesh& c1, const Mesh& c2, const Mesh& ch, unsigned int resolution);
 double compute_h(const Mesh& a, const Mesh& b, double k, unsigned int resolution);
 double compute_h3(const Mesh& c1, const Mesh& c2, const Mesh& ch, double k, unsigned int resolution);

@@ -1,6 +1,7 @@
 #include "gpu_bridge.hpp"
 
 #include <chrono>
+#include <cstring>
 #include <cstdlib>
 #include <memory>
 #include <mutex>
@@ -165,6 +166,49 @@ double face_hausdorff(const Mesh& A, const std::vector<Vec3>& XA, const std::vec
                               reinterpret_cast<const double*>(XB.data()), idB.data(), (int32_t)XB.size(), floor,
                               &out),
         "visacd_face_hausdorff_floor");
+  return out;
+}
+
+std::vector<double> face_hausdorff_batch(const std::vector<const Mesh*>& a, const std::vector<const Mesh*>& b,
+                                         const std::vector<const HbSamples*>& s, const std::vector<double>& lower,
+                                         double floor, bool independent) {
+  const size_t J = a.size();
+  std::vector<double> out(J, 0.0);
+  if (J == 0) return out;
+  visacd_ctx* ctx = context();
+  // Concatenated surfaces: mesh / set 2j = a[j], 2j + 1 = b[j].
+  thread_local std::vector<double> V, X;
+  thread_local std::vector<int32_t> T, I;
+  std::vector<int64_t> voff(2 * J + 1, 0), toff(2 * J + 1, 0), soff(2 * J + 1, 0);
+  for (size_t j = 0; j < J; ++j) {
+    const Mesh* m[2] = {a[j], b[j]};
+    const size_t ns[2] = {s[j]->s1.size(), s[j]->s2.size()};
+    for (int k = 0; k < 2; ++k) {
+      voff[2 * j + k + 1] = voff[2 * j + k] + (int64_t)m[k]->vertices.size();
+      toff[2 * j + k + 1] = toff[2 * j + k] + (int64_t)m[k]->triangles.size();
+      soff[2 * j + k + 1] = soff[2 * j + k] + (int64_t)ns[k];
+    }
+  }
+  V.resize(3 * (size_t)voff[2 * J]);
+  T.resize(3 * (size_t)toff[2 * J]);
+  X.resize(3 * (size_t)soff[2 * J]);
+  I.resize((size_t)soff[2 * J]);
+  for (size_t j = 0; j < J; ++j) {
+    const Mesh* m[2] = {a[j], b[j]};
+    const std::vector<Vec3>* xs[2] = {&s[j]->s1, &s[j]->s2};
+    const std::vector<int>* is[2] = {&s[j]->i1, &s[j]->i2};
+    for (int k = 0; k < 2; ++k) {
+      const size_t q = 2 * j + k;
+      std::memcpy(V.data() + 3 * voff[q], m[k]->vertices.data(), m[k]->vertices.size() * 24);
+      std::memcpy(T.data() + 3 * toff[q], m[k]->triangles.data(), m[k]->triangles.size() * 12);
+      std::memcpy(X.data() + 3 * soff[q], xs[k]->data(), xs[k]->size() * 24);
+      std::memcpy(I.data() + soff[q], is[k]->data(), is[k]->size() * 4);
+    }
+  }
+  check(visacd_face_hausdorff_batch(ctx, (int32_t)J, V.data(), voff.data(), T.data(), toff.data(), X.data(),
+                                    I.data(), soff.data(), lower.empty() ? nullptr : lower.data(), floor,
+                                    independent ? 1 : 0, out.data()),
+        "visacd_face_hausdorff_batch");
   return out;
 }
 

@@ -65,6 +65,13 @@ double face_hausdorff(const Mesh& A, const std::vector<Vec3>& XA, const std::vec
                       const Mesh& B, const std::vector<Vec3>& XB, const std::vector<int>& idB,
                       double floor = 0.0);
 
+// Face Hausdorff distances of many surface pairs in one call
+// (visacd_face_hausdorff_batch): job j compares *a[j] (samples s[j]->s1 / i1)
+// with *b[j] (s[j]->s2 / i2); lower, floor and independent as there.
+std::vector<double> face_hausdorff_batch(const std::vector<const Mesh*>& a, const std::vector<const Mesh*>& b,
+                                         const std::vector<const HbSamples*>& s, const std::vector<double>& lower,
+                                         double floor, bool independent);
+
 // Per-thread call counters.
 struct Counters {
   long long vis_calls = 0, vis_pairs = 0, vis_edges = 0, score_calls = 0, plane_edge_pairs = 0;

@@ -261,10 +261,11 @@ int get_part_with_highest_concavity(const MeshList& parts, double& max_concavity
       std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   // compute_h(part, hull, 0.3, 3000) of every part, of which only the first
   // maximum and its value are used. The samples are drawn in the reference's
-  // order (part i, then its hull, for i = 0, 1, ...); the sampled terms are
-  // then evaluated in descending order of the volume term with the running
-  // maximum as the floor, so a part below it gets some value below it (never
-  // the maximum) and every other part its exact value.
+  // order (part i, then its hull, for i = 0, 1, ...); the sampled terms of all
+  // parts are then evaluated in one batch that skips sample terms unable to
+  // reach the batch's running maximum (seeded with the volume terms), so the
+  // parts attaining the largest concavity get their exact values and every
+  // other part a value below it.
   const int n = (int)parts.size();
   std::vector<HbSamples> smp(n);
   std::vector<double> c(n);
@@ -272,14 +273,15 @@ int get_part_with_highest_concavity(const MeshList& parts, double& max_concavity
     c[i] = compute_rv(parts[i], hulls[i]) * 0.3;
     sample_hb(parts[i], hulls[i], 3000, smp[i]);
   }
-  std::vector<int> order(n);
-  std::iota(order.begin(), order.end(), 0);
-  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return c[a] > c[b]; });
-  double run = max_concavity;
-  for (int i : order) {
-    c[i] = std::max(c[i], eval_hb(parts[i], hulls[i], smp[i], std::max(run, 0.0)));
-    run = std::max(run, c[i]);
+  std::vector<const Mesh*> pa(n), pb(n);
+  std::vector<const HbSamples*> ps(n);
+  for (int i = 0; i < n; ++i) {
+    pa[i] = &parts[i];
+    pb[i] = &hulls[i];
+    ps[i] = &smp[i];
   }
+  const std::vector<double> hb = eval_hb_batch(pa, pb, ps, c, std::max(max_concavity, 0.0), false);
+  for (int i = 0; i < n; ++i) c[i] = std::max(c[i], hb[i]);
   int idx = -1;
   for (int i = 0; i < n; ++i) {
     if (c[i] > max_concavity) {
@@ -292,23 +294,22 @@ int get_part_with_highest_concavity(const MeshList& parts, double& max_concavity
 
 double compute_final_concavity(const MeshList& parts, const MeshList& hulls) {
   // The largest compute_hb(part, hull, 10000): samples drawn in order, values
-  // evaluated with the running maximum as the floor (largest volume term
-  // first), as in get_part_with_highest_concavity.
+  // evaluated in one batch pruned against its running maximum, as in
+  // get_part_with_highest_concavity.
   const size_t n = parts.size();
   std::vector<HbSamples> smp(n);
-  std::vector<double> rv(n);
+  for (size_t i = 0; i < n; ++i) sample_hb(parts[i], hulls[i], 10000, smp[i]);
+  std::vector<const Mesh*> pa(n), pb(n);
+  std::vector<const HbSamples*> ps(n);
   for (size_t i = 0; i < n; ++i) {
-    rv[i] = compute_rv(parts[i], hulls[i]);
-    sample_hb(parts[i], hulls[i], 10000, smp[i]);
+    pa[i] = &parts[i];
+    pb[i] = &hulls[i];
+    ps[i] = &smp[i];
   }
-  std::vector<size_t> order(n);
-  std::iota(order.begin(), order.end(), size_t(0));
-  std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return rv[a] > rv[b]; });
+  const std::vector<double> hb = eval_hb_batch(pa, pb, ps, {}, 0.0, false);
   double h = 0;
-  for (size_t i : order) {
-    const double c = eval_hb(parts[i], hulls[i], smp[i], h);
-    if (c > h) h = c;
-  }
+  for (size_t i = 0; i < n; ++i)
+    if (hb[i] > h) h = hb[i];
   return h;
 }
 
