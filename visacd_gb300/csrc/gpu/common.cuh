@@ -184,6 +184,8 @@ enum KernelId {
   kKLpAdam,
   kKLpMisc,
   kKSdf,
+  kKSdfDist,
+  kKSdfCross,
   kKHullDist,
   kKSegTri,
   kKMisc,

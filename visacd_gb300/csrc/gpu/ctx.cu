@@ -85,7 +85,8 @@ static const char* kNames[kKCount] = {
     "clip",          "clip_resolve",   "face_hausdorff", "hd_bound",
     "hd_query",      "hd_head",        "lp_features",
     "lp_gemm",       "lp_pool",        "lp_loss",      "lp_adam",
-    "lp_misc",       "sdf_remesh",     "hull_dist",    "seg_tri",
+    "lp_misc",       "sdf_remesh",     "sdf_dist",     "sdf_cross",
+    "hull_dist",     "seg_tri",
     "misc"};
 
 const char* kernel_name(int id) { return (id >= 0 && id < kKCount) ? kNames[id] : "?"; }

@@ -4,10 +4,12 @@
 //
 // Same algorithm and arithmetic as the host restatement (manifold_preprocess in
 // csrc/host/remesh.cpp), so the output mesh is identical bit for bit:
-//  1. sdf_dist_kernel: one block per triangle; every voxel centre in the
-//     triangle's box grown by the band gets the exact FP64 point-triangle
-//     distance (rounded to float), combined with atomicMin (non-negative floats
-//     order like their bit patterns).
+//  1. sdf_tri_prep_kernel computes each triangle's set-up once (voxel box,
+//     FP32 bounds and planes); sdf_dist_kernel, one block per triangle, gives
+//     every voxel centre in the triangle's box grown by the band the exact FP64
+//     point-triangle distance (rounded to float) unless a lower bound rules it
+//     out, combined with atomicMin (non-negative floats order like their bit
+//     patterns).
 //  2. For each axis: sdf_cross_kernel marks, for every ray through voxel
 //     centres (offset by 1.2345679e-6 / 2.3456789e-6 voxels) that crosses a
 //     triangle at x, the first voxel whose centre lies beyond x (XOR toggle);
@@ -61,39 +63,45 @@ __device__ __forceinline__ double max3(double a, double b, double c) { return fm
 // normal and m_e the unit in-plane normal of edge e pointing away from the
 // triangle (offset so that no vertex lies beyond it), every triangle point x
 // has |q - x|^2 >= (n.(q - x))^2 + (m_e.(q - x))^2 >= p^2 + s_e^2.
-__global__ void __launch_bounds__(128) sdf_dist_kernel(const double* __restrict__ P, const int32_t* __restrict__ T,
-                                                       int nt, SdfGrid g, uint32_t* __restrict__ dist) {
-  for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+// Per-triangle set-up of the band distances (one thread per triangle, once):
+// the voxel box grown by the band, the FP32 bounding box, and the FP32 plane
+// and edge planes of the lower bound.
+struct SdfTri {
+  int lo[3], ext[3];      // voxel box (ext[0] <= 0: nothing in the grid)
+  float blo[3], bhi[3];   // bounding box rounded outwards
+  float4 pl;              // unit normal, offset; w of fe[0] = -1e30 without a plane
+  float4 fe[3];           // unit in-plane edge normals, offsets (no vertex beyond)
+  int has_plane, pad[3];
+};
+
+__global__ void sdf_tri_prep_kernel(const double* __restrict__ P, const int32_t* __restrict__ T, int nt, SdfGrid g,
+                                    SdfTri* __restrict__ out) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += gridDim.x * blockDim.x) {
     double A[3], B[3], C[3];
     load_tri(P, T, t, A, B, C);
-    int lo[3], ext[3];
-    float blo[3], bhi[3];
+    SdfTri r;
     for (int a = 0; a < 3; ++a) {
       const double mn = min3(A[a], B[a], C[a]), mx = max3(A[a], B[a], C[a]);
-      lo[a] = max(0, (int)floor(mn - g.band) - g.org[a]);
+      r.lo[a] = max(0, (int)floor(mn - g.band) - g.org[a]);
       const int hi = min(g.dim[a] - 1, (int)ceil(mx + g.band) - g.org[a]);
-      ext[a] = hi - lo[a] + 1;
-      blo[a] = __double2float_rd(mn);
-      bhi[a] = __double2float_ru(mx);
+      r.ext[a] = hi - r.lo[a] + 1;
+      r.blo[a] = __double2float_rd(mn);
+      r.bhi[a] = __double2float_ru(mx);
     }
-    if (ext[0] <= 0 || ext[1] <= 0 || ext[2] <= 0) continue;
+    if (r.ext[0] <= 0 || r.ext[1] <= 0 || r.ext[2] <= 0) r.ext[0] = 0;
     // unit normal and plane offset (FP32 copies; degenerate triangles get none)
     const double ux = B[0] - A[0], uy = B[1] - A[1], uz = B[2] - A[2];
     const double vx = C[0] - A[0], vy = C[1] - A[1], vz = C[2] - A[2];
     double nx = uy * vz - uz * vy, ny = uz * vx - ux * vz, nz = ux * vy - uy * vx;
     const double nl = sqrt(nx * nx + ny * ny + nz * nz);
-    const bool has_plane = nl > 1e-12;
-    float fnx = 0.f, fny = 0.f, fnz = 0.f, foff = 0.f;
-    float4 fe[3] = {make_float4(0.f, 0.f, 0.f, -1e30f), make_float4(0.f, 0.f, 0.f, -1e30f),
-                    make_float4(0.f, 0.f, 0.f, -1e30f)};
-    if (has_plane) {
+    r.has_plane = nl > 1e-12;
+    r.pl = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int e = 0; e < 3; ++e) r.fe[e] = make_float4(0.f, 0.f, 0.f, -1e30f);
+    if (r.has_plane) {
       nx /= nl;
       ny /= nl;
       nz /= nl;
-      fnx = (float)nx;
-      fny = (float)ny;
-      fnz = (float)nz;
-      foff = (float)-(nx * A[0] + ny * A[1] + nz * A[2]);
+      r.pl = make_float4((float)nx, (float)ny, (float)nz, (float)-(nx * A[0] + ny * A[1] + nz * A[2]));
       const double* V[3] = {A, B, C};
       for (int e = 0; e < 3; ++e) {
         const double* P0 = V[e];
@@ -113,26 +121,46 @@ __global__ void __launch_bounds__(128) sdf_dist_kernel(const double* __restrict_
         }
         const double top = fmax(fmax(mx * A[0] + my * A[1] + mz * A[2], mx * B[0] + my * B[1] + mz * B[2]),
                                 mx * C[0] + my * C[1] + mz * C[2]);
-        fe[e] = make_float4((float)mx, (float)my, (float)mz, (float)-top);
+        r.fe[e] = make_float4((float)mx, (float)my, (float)mz, (float)-top);
       }
     }
-    const int n = ext[0] * ext[1] * ext[2];
-    for (int r = threadIdx.x; r < n; r += blockDim.x) {
-      const int i = lo[0] + r % ext[0], j = lo[1] + (r / ext[0]) % ext[1], k = lo[2] + r / (ext[0] * ext[1]);
+    out[t] = r;
+  }
+}
+
+__global__ void __launch_bounds__(128) sdf_dist_kernel(const double* __restrict__ P, const int32_t* __restrict__ T,
+                                                       int nt, SdfGrid g, const SdfTri* __restrict__ prep,
+                                                       uint32_t* __restrict__ dist) {
+  for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+    const SdfTri& r = prep[t];
+    const int ex0 = r.ext[0], ex1 = r.ext[1], ex2 = r.ext[2];
+    if (ex0 <= 0) continue;
+    const int lo0 = r.lo[0], lo1 = r.lo[1], lo2 = r.lo[2];
+    const float blo0 = r.blo[0], blo1 = r.blo[1], blo2 = r.blo[2];
+    const float bhi0 = r.bhi[0], bhi1 = r.bhi[1], bhi2 = r.bhi[2];
+    const bool has_plane = r.has_plane != 0;
+    const float4 pl = r.pl, fe0 = r.fe[0], fe1 = r.fe[1], fe2 = r.fe[2];
+    const int n = ex0 * ex1 * ex2;
+    for (int q0 = threadIdx.x; q0 < n; q0 += blockDim.x) {
+      const int i = lo0 + q0 % ex0, j = lo1 + (q0 / ex0) % ex1, k = lo2 + q0 / (ex0 * ex1);
       const size_t v = vid(g, i, j, k);
       const float qx = (float)(g.org[0] + i), qy = (float)(g.org[1] + j), qz = (float)(g.org[2] + k);
-      const float gx = fmaxf(fmaxf(blo[0] - qx, qx - bhi[0]), 0.f);
-      const float gy = fmaxf(fmaxf(blo[1] - qy, qy - bhi[1]), 0.f);
-      const float gz = fmaxf(fmaxf(blo[2] - qz, qz - bhi[2]), 0.f);
+      const float gx = fmaxf(fmaxf(blo0 - qx, qx - bhi0), 0.f);
+      const float gy = fmaxf(fmaxf(blo1 - qy, qy - bhi1), 0.f);
+      const float gz = fmaxf(fmaxf(blo2 - qz, qz - bhi2), 0.f);
       float lb = sqrtf(gx * gx + gy * gy + gz * gz);
       if (has_plane) {
-        const float pd = fabsf(fnx * qx + fny * qy + fnz * qz + foff);
+        const float pd = fabsf(pl.x * qx + pl.y * qy + pl.z * qz + pl.w);
         float se = 0.f;
-        for (int e = 0; e < 3; ++e) se = fmaxf(se, fe[e].x * qx + fe[e].y * qy + fe[e].z * qz + fe[e].w);
+        se = fmaxf(se, fe0.x * qx + fe0.y * qy + fe0.z * qz + fe0.w);
+        se = fmaxf(se, fe1.x * qx + fe1.y * qy + fe1.z * qz + fe1.w);
+        se = fmaxf(se, fe2.x * qx + fe2.y * qy + fe2.z * qz + fe2.w);
         lb = fmaxf(lb, sqrtf(pd * pd + se * se));
       }
       const float cur = __uint_as_float(*(volatile const uint32_t*)&dist[v]);
       if (lb - 2.0f * g.margin >= cur) continue;
+      double A[3], B[3], C[3];
+      load_tri(P, T, t, A, B, C);
       const double q[3] = {(double)(g.org[0] + i), (double)(g.org[1] + j), (double)(g.org[2] + k)};
       const float d = __double2float_rn(point_tri_dist(q, A, B, C));
       atomicMin(&dist[v], __float_as_uint(d));
@@ -369,7 +397,8 @@ extern "C" int visacd_sdf_remesh(visacd_ctx* ctx, const double* verts, int32_t n
     at += align256(bytes);
     return o;
   };
-  const size_t oP = take(P.size() * 8), oT = take(3 * (size_t)nt * 4), oDist = take(nvox * 4),
+  const size_t oP = take(P.size() * 8), oT = take(3 * (size_t)nt * 4), oPrep = take((size_t)nt * sizeof(SdfTri)),
+               oDist = take(nvox * 4),
                oTog = take(nvox * 4), oVotes = take(nvox), oF = take(nvox * 4), oFlag = take(ncell * 4),
                oCoff = take((ncell + 1) * 8), oCv = take(ncell * 4), oQcnt = take(nint * 4),
                oQoff = take((nint + 1) * 8);
@@ -398,12 +427,15 @@ extern "C" int visacd_sdf_remesh(visacd_ctx* ctx, const double* verts, int32_t n
   VLAUNCH(ctx, kKSdf, gv, 256, 0, sdf_fill_kernel, dist, nvox, band_bits);
   VCUDA(cudaMemsetAsync(votes, 0, nvox, st));
   const unsigned gt = (unsigned)std::min<int64_t>(nt, 64 * (int64_t)ctx->sm_count);
-  VLAUNCH(ctx, kKSdf, gt, 128, 0, sdf_dist_kernel, dP, dT, nt, g, dist);
+  SdfTri* prep = (SdfTri*)(base + oPrep);
+  VLAUNCH(ctx, kKSdfDist, grid_for(nt, 128, 16 * (int64_t)ctx->sm_count), 128, 0, sdf_tri_prep_kernel, dP, dT, nt,
+          g, prep);
+  VLAUNCH(ctx, kKSdfDist, gt, 128, 0, sdf_dist_kernel, dP, dT, nt, g, (const SdfTri*)prep, dist);
   for (int ax = 0; ax < 3; ++ax) {
     VCUDA(cudaMemsetAsync(tog, 0, nvox * 4, st));
-    VLAUNCH(ctx, kKSdf, gt, 128, 0, sdf_cross_kernel, dP, dT, nt, g, ax, tog);
+    VLAUNCH(ctx, kKSdfCross, gt, 128, 0, sdf_cross_kernel, dP, dT, nt, g, ax, tog);
     const int u = (ax + 1) % 3, w = (ax + 2) % 3;
-    VLAUNCH(ctx, kKSdf, grid_for((int64_t)g.dim[u] * g.dim[w], 128, 1 << 20), 128, 0, sdf_parity_kernel, g, ax,
+    VLAUNCH(ctx, kKSdfCross, grid_for((int64_t)g.dim[u] * g.dim[w], 128, 1 << 20), 128, 0, sdf_parity_kernel, g, ax,
             tog, votes);
   }
   VLAUNCH(ctx, kKSdf, gv, 256, 0, sdf_field_kernel, dist, votes, nvox, f);

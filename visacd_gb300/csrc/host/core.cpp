@@ -39,7 +39,7 @@ void Mt19937::seed(result_type s) {
 void Mt19937::twist() {
   auto mix = [](uint32_t a, uint32_t b, uint32_t c) {
     const uint32_t y = (a & 0x80000000u) | (b & 0x7fffffffu);
-    return c ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+    return c ^ (y >> 1) ^ ((0u - (y & 1u)) & 0x9908b0dfu);
   };
   int k = 0;
   for (; k < kN - kM; ++k) x_[k] = mix(x_[k], x_[k + 1], x_[k + kM]);
