@@ -37,8 +37,8 @@ UNIT = "pairs/s"
 N_PLANES = 2500
 L2_BYTES = 129 * 1024 * 1024
 # DRAM bytes (read + write) per visibility launch from one ncu capture of the
-# same workload (profiles/visibility_blob_s5_ncu.txt).
-VIS_DRAM_BYTES_PER_LAUNCH: dict = {"blob_s5": 4841984 + 0}
+# same workload (profiles/visibility_blob_s5_dram.md).
+VIS_DRAM_BYTES_PER_LAUNCH: dict = {"blob_s5": 2969344 + 0}
 
 
 WORKLOADS = {"blob_s5": 5, "blob_s4": 4, "blob_s3": 3}

@@ -62,3 +62,21 @@ def test_gpu_remesh_edge_cases(native, ctx):
     e = np.sort(np.concatenate([t[:, [0, 1]], t[:, [1, 2]], t[:, [2, 0]]]), 1)
     _, cnt = np.unique(e, axis=0, return_counts=True)
     assert (cnt == 2).all()
+
+
+def test_gpu_remesh_degenerate_triangles(V):
+    """Zero-area and sliver triangles (no plane, near-parallel edges) in a
+    closed mesh: the GPU bounds must stay conservative; same mesh as the host."""
+    from visacd_gb300 import meshgen as mg
+    v, t = mg.displaced_blob(3, seed=4)
+    v = v / np.abs(v).max()
+    n = len(v)
+    # a duplicated vertex (zero-area triangles) and a sliver fan on one face
+    extra_v = np.array([v[t[0, 0]], 0.5 * (v[t[1, 0]] + v[t[1, 1]]) + 1e-9], float)
+    v2 = np.concatenate([v, extra_v])
+    t2 = np.concatenate([t, [[t[0, 0], t[0, 1], n], [t[1, 0], t[1, 1], n + 1], [n, n + 1, t[2, 2]]]]).astype(np.int32)
+    for scale, level in [(40.0, 0.02), (30.0, 0.55 / 30)]:
+        h = V._manifold_preprocess(v2, t2, scale, level)
+        g = V._manifold_preprocess_gpu(v2, t2, scale, level)
+        np.testing.assert_array_equal(g["triangles"], h["triangles"])
+        np.testing.assert_array_equal(g["vertices"], h["vertices"])

@@ -26,6 +26,8 @@ namespace vgpu {
 
 namespace {
 
+constexpr float kSdfU = 5.9604645e-8f;  // 2^-24
+
 struct SdfGrid {
   int org[3], dim[3];
   double band;
@@ -128,9 +130,101 @@ __global__ void sdf_tri_prep_kernel(const double* __restrict__ P, const int32_t*
   }
 }
 
+// FP32 upper bound of the distance from q to triangle (A, B, C): the distance
+// to a point of the triangle chosen in FP32 by the closest-point regions
+// (Ericson, Real-Time Collision Detection 5.1.5), taken as A + v AB + w AC
+// with v, w clamped to v, w >= 0, v + w <= 1 so that the exact point with
+// these weights lies on the triangle; `slack` covers the FP32 rounding of the
+// point and of the distance.
+__device__ float tri_dist_ub32(float qx, float qy, float qz, const float (&A)[3], const float (&B)[3],
+                               const float (&C)[3], float slack) {
+  const float ab[3] = {B[0] - A[0], B[1] - A[1], B[2] - A[2]};
+  const float ac[3] = {C[0] - A[0], C[1] - A[1], C[2] - A[2]};
+  const float ap[3] = {qx - A[0], qy - A[1], qz - A[2]};
+  const float bp[3] = {qx - B[0], qy - B[1], qz - B[2]};
+  const float cp[3] = {qx - C[0], qy - C[1], qz - C[2]};
+  auto dot = [](const float (&x)[3], const float (&y)[3]) { return x[0] * y[0] + x[1] * y[1] + x[2] * y[2]; };
+  const float d1 = dot(ab, ap), d2 = dot(ac, ap), d3 = dot(ab, bp), d4 = dot(ac, bp), d5 = dot(ab, cp),
+              d6 = dot(ac, cp);
+  float v = 0.f, w = 0.f;
+  const float vc = d1 * d4 - d3 * d2, vb = d5 * d2 - d1 * d6, va = d3 * d6 - d5 * d4;
+  if (d1 <= 0.f && d2 <= 0.f) {
+  } else if (d3 >= 0.f && d4 <= d3) {
+    v = 1.f;
+  } else if (vc <= 0.f && d1 >= 0.f && d3 <= 0.f) {
+    v = d1 / (d1 - d3);
+  } else if (d6 >= 0.f && d5 <= d6) {
+    w = 1.f;
+  } else if (vb <= 0.f && d2 >= 0.f && d6 <= 0.f) {
+    w = d2 / (d2 - d6);
+  } else if (va <= 0.f && (d4 - d3) >= 0.f && (d5 - d6) >= 0.f) {
+    w = (d4 - d3) / ((d4 - d3) + (d5 - d6));
+    v = 1.f - w;
+  } else {
+    const float den = 1.f / (va + vb + vc);
+    v = vb * den;
+    w = vc * den;
+  }
+  v = fminf(fmaxf(v, 0.f), 1.f);  // NaN (degenerate triangle) becomes 0
+  w = fminf(fmaxf(w, 0.f), 1.f - v);
+  const float px = A[0] + v * ab[0] + w * ac[0], py = A[1] + v * ab[1] + w * ac[1], pz = A[2] + v * ab[2] + w * ac[2];
+  const float ex = qx - px, ey = qy - py, ez = qz - pz;
+  return __fadd_ru(__fmul_ru(__fsqrt_ru(__fadd_ru(__fadd_ru(__fmul_ru(ex, ex), __fmul_ru(ey, ey)), __fmul_ru(ez, ez))),
+                             1.0f + 1.0f / 65536.0f),
+                   slack);
+}
+
+// FP32 band voxel bound between the triangle's lower bound and its FP32 upper
+// bound (first pass): ub[v] ends at or above the voxel's exact distance, so
+// the exact pass can skip every triangle whose lower bound reaches it.
+__device__ __forceinline__ float sdf_lower_bound(const SdfTri& r, float qx, float qy, float qz) {
+  const float gx = fmaxf(fmaxf(r.blo[0] - qx, qx - r.bhi[0]), 0.f);
+  const float gy = fmaxf(fmaxf(r.blo[1] - qy, qy - r.bhi[1]), 0.f);
+  const float gz = fmaxf(fmaxf(r.blo[2] - qz, qz - r.bhi[2]), 0.f);
+  float lb = sqrtf(gx * gx + gy * gy + gz * gz);
+  if (r.has_plane) {
+    const float pd = fabsf(r.pl.x * qx + r.pl.y * qy + r.pl.z * qz + r.pl.w);
+    float se = 0.f;
+    for (int e = 0; e < 3; ++e) se = fmaxf(se, r.fe[e].x * qx + r.fe[e].y * qy + r.fe[e].z * qz + r.fe[e].w);
+    lb = fmaxf(lb, sqrtf(pd * pd + se * se));
+  }
+  return lb;
+}
+
+__global__ void __launch_bounds__(128) sdf_ub_kernel(const double* __restrict__ P, const int32_t* __restrict__ T,
+                                                     int nt, SdfGrid g, const SdfTri* __restrict__ prep,
+                                                     uint32_t* __restrict__ ub) {
+  for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+    const SdfTri r = prep[t];
+    if (r.ext[0] <= 0) continue;
+    double Ad[3], Bd[3], Cd[3];
+    load_tri(P, T, t, Ad, Bd, Cd);
+    const float A[3] = {(float)Ad[0], (float)Ad[1], (float)Ad[2]};
+    const float B[3] = {(float)Bd[0], (float)Bd[1], (float)Bd[2]};
+    const float C[3] = {(float)Cd[0], (float)Cd[1], (float)Cd[2]};
+    // rounding of the vertices to float, of the chosen point and of its
+    // distance: a few units of 2^-24 of the largest coordinate involved
+    float mabs = 0.f;
+    for (int a = 0; a < 3; ++a) mabs = fmaxf(mabs, fmaxf(fabsf(A[a]), fmaxf(fabsf(B[a]), fabsf(C[a]))));
+    const int n = r.ext[0] * r.ext[1] * r.ext[2];
+    for (int q0 = threadIdx.x; q0 < n; q0 += blockDim.x) {
+      const int i = r.lo[0] + q0 % r.ext[0], j = r.lo[1] + (q0 / r.ext[0]) % r.ext[1],
+                k = r.lo[2] + q0 / (r.ext[0] * r.ext[1]);
+      const size_t v = vid(g, i, j, k);
+      const float qx = (float)(g.org[0] + i), qy = (float)(g.org[1] + j), qz = (float)(g.org[2] + k);
+      const float lb = sdf_lower_bound(r, qx, qy, qz);
+      const float cur = __uint_as_float(*(volatile const uint32_t*)&ub[v]);
+      if (lb - 2.0f * g.margin >= cur) continue;
+      const float qa = fmaxf(fabsf(qx), fmaxf(fabsf(qy), fabsf(qz)));
+      const float slack = 64.0f * kSdfU * fmaxf(mabs, qa) + g.margin;
+      atomicMin(&ub[v], __float_as_uint(tri_dist_ub32(qx, qy, qz, A, B, C, slack)));
+    }
+  }
+}
+
 __global__ void __launch_bounds__(128) sdf_dist_kernel(const double* __restrict__ P, const int32_t* __restrict__ T,
                                                        int nt, SdfGrid g, const SdfTri* __restrict__ prep,
-                                                       uint32_t* __restrict__ dist) {
+                                                       const uint32_t* __restrict__ ub, uint32_t* __restrict__ dist) {
   for (int t = blockIdx.x; t < nt; t += gridDim.x) {
     const SdfTri& r = prep[t];
     const int ex0 = r.ext[0], ex1 = r.ext[1], ex2 = r.ext[2];
@@ -157,7 +251,7 @@ __global__ void __launch_bounds__(128) sdf_dist_kernel(const double* __restrict_
         se = fmaxf(se, fe2.x * qx + fe2.y * qy + fe2.z * qz + fe2.w);
         lb = fmaxf(lb, sqrtf(pd * pd + se * se));
       }
-      const float cur = __uint_as_float(*(volatile const uint32_t*)&dist[v]);
+      const float cur = fminf(__uint_as_float(*(volatile const uint32_t*)&dist[v]), __uint_as_float(ub[v]));
       if (lb - 2.0f * g.margin >= cur) continue;
       double A[3], B[3], C[3];
       load_tri(P, T, t, A, B, C);
@@ -430,7 +524,12 @@ extern "C" int visacd_sdf_remesh(visacd_ctx* ctx, const double* verts, int32_t n
   SdfTri* prep = (SdfTri*)(base + oPrep);
   VLAUNCH(ctx, kKSdfDist, grid_for(nt, 128, 16 * (int64_t)ctx->sm_count), 128, 0, sdf_tri_prep_kernel, dP, dT, nt,
           g, prep);
-  VLAUNCH(ctx, kKSdfDist, gt, 128, 0, sdf_dist_kernel, dP, dT, nt, g, (const SdfTri*)prep, dist);
+  // First pass: FP32 upper bounds per voxel in the toggle buffer (free until
+  // the crossings), then the exact pass.
+  VLAUNCH(ctx, kKSdf, gv, 256, 0, sdf_fill_kernel, tog, nvox, band_bits);
+  VLAUNCH(ctx, kKSdfDist, gt, 128, 0, sdf_ub_kernel, dP, dT, nt, g, (const SdfTri*)prep, tog);
+  VLAUNCH(ctx, kKSdfDist, gt, 128, 0, sdf_dist_kernel, dP, dT, nt, g, (const SdfTri*)prep, (const uint32_t*)tog,
+          dist);
   for (int ax = 0; ax < 3; ++ax) {
     VCUDA(cudaMemsetAsync(tog, 0, nvox * 4, st));
     VLAUNCH(ctx, kKSdfCross, gt, 128, 0, sdf_cross_kernel, dP, dT, nt, g, ax, tog);
