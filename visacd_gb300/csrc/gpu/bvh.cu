@@ -2,7 +2,8 @@
 //
 // Replaces the OptiX GAS build of the reference (lib/src/intersections.cpp:131-180).
 //  1. tri_prep: per triangle centroid, conservatively widened AABB, index check.
-//  2. morton: 63-bit Morton code of the centroid (21 bits per axis).
+//  2. morton: Morton code of the centroid, 10 to 21 bits per axis by triangle
+//     count (morton_bits), sorted on exactly those bits.
 //  3. stable LSD radix sort of (code, triangle) pairs (own kernels, ctx.cu).
 //  4. karras_build: Karras (2012) "Maximizing parallelism in the construction of
 //     BVHs, octrees and k-d trees" — each internal node finds its key range and
@@ -103,14 +104,15 @@ __device__ __forceinline__ uint64_t spread21(uint64_t x) {
 }
 
 __global__ void morton_kernel(const float* __restrict__ cent, int32_t n,
-                              const BuildCounters* __restrict__ c, uint64_t* __restrict__ keys,
+                              const BuildCounters* __restrict__ c, int bits, uint64_t* __restrict__ keys,
                               uint32_t* __restrict__ vals) {
   float lo[3], sc[3];
+  const float top = (float)((1u << bits) - 1u);
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     lo[a] = o2f(c->cmin[a]);
     float ext = o2f(c->cmax[a]) - lo[a];
-    sc[a] = ext > 0.f ? 2097151.0f / ext : 0.f;
+    sc[a] = ext > 0.f ? top / ext : 0.f;
   }
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
@@ -118,7 +120,7 @@ __global__ void morton_kernel(const float* __restrict__ cent, int32_t n,
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
       float x = (cent[3 * i + a] - lo[a]) * sc[a];
-      x = fminf(fmaxf(x, 0.f), 2097151.0f);  // NaN -> 0
+      x = fminf(fmaxf(x, 0.f), top);  // NaN -> 0
       q[a] = (uint64_t)x;
     }
     keys[i] = (spread21(q[0]) << 2) | (spread21(q[1]) << 1) | spread21(q[2]);
@@ -339,8 +341,9 @@ int bvh_build(visacd_ctx* ctx, const float* verts, int32_t nv, const uint32_t* t
   VLAUNCH(ctx, kKTriPrep, grid_for(3LL * nv, 256, 8LL * ctx->sm_count), 256, 0,
           vert_absmax_kernel, dv, nv, cnt);
   VLAUNCH(ctx, kKTriPrep, g, 256, 0, tri_prep_kernel, dv, nv, dt, nt, cent, cnt);
-  VLAUNCH(ctx, kKMorton, g, 256, 0, morton_kernel, cent, nt, cnt, keys, vals);
-  VTRY(radix_sort_u64(ctx, keys, vals, keys2, vals2, nt, 64));
+  const int mb = morton_bits(nt);
+  VLAUNCH(ctx, kKMorton, g, 256, 0, morton_kernel, cent, nt, cnt, mb, keys, vals);
+  VTRY(radix_sort_u64(ctx, keys, vals, keys2, vals2, nt, 3 * mb));
 
   size_t bytes_nodes = (size_t)n_int * 64, bytes_tris = (size_t)nt * 48;
   b->stream = ctx->stream;

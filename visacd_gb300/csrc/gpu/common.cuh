@@ -241,6 +241,17 @@ inline unsigned grid_for(int64_t n, int block, int64_t cap) {
   return (unsigned)g;
 }
 
+// Bits per axis of the Morton codes that order n primitives: about 4 bits
+// finer than the mean spacing (the orders only shape the BVHs and the pair
+// tiles, never a result), at least 10 and at most 21, so the radix sort runs
+// ceil(3 bits / 8) passes (4 up to about 2^21 primitives).
+inline int morton_bits(int64_t n) {
+  int len = 0;
+  while (len < 62 && (int64_t(1) << len) <= n) ++len;
+  const int b = (len + 2) / 3 + 4;
+  return b < 10 ? 10 : (b > 21 ? 21 : b);
+}
+
 // Exclusive scan of n uint32 counts into uint64 offsets (device), total also
 // written to offsets[n]. Uses ctx scan scratch.
 int exclusive_scan_u32_to_u64(visacd_ctx* ctx, const uint32_t* in, uint64_t* out, int64_t n);

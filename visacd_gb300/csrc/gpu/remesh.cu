@@ -222,9 +222,18 @@ __global__ void __launch_bounds__(128) sdf_ub_kernel(const double* __restrict__ 
   }
 }
 
+// The box is filtered in chunks of kSdfChunk voxels; the voxels that pass are
+// appended to a shared list and evaluated in FP64 by all threads together, so
+// the FP64 pipe (slow on this part) runs with full warps instead of the few
+// lanes that pass the filter in each warp.
+constexpr int kSdfChunk = 1024;
+
 __global__ void __launch_bounds__(128) sdf_dist_kernel(const double* __restrict__ P, const int32_t* __restrict__ T,
                                                        int nt, SdfGrid g, const SdfTri* __restrict__ prep,
                                                        const uint32_t* __restrict__ ub, uint32_t* __restrict__ dist) {
+  __shared__ int list[kSdfChunk];
+  __shared__ int count;
+  const int lane = threadIdx.x & 31;
   for (int t = blockIdx.x; t < nt; t += gridDim.x) {
     const SdfTri& r = prep[t];
     const int ex0 = r.ext[0], ex1 = r.ext[1], ex2 = r.ext[2];
@@ -234,30 +243,52 @@ __global__ void __launch_bounds__(128) sdf_dist_kernel(const double* __restrict_
     const float bhi0 = r.bhi[0], bhi1 = r.bhi[1], bhi2 = r.bhi[2];
     const bool has_plane = r.has_plane != 0;
     const float4 pl = r.pl, fe0 = r.fe[0], fe1 = r.fe[1], fe2 = r.fe[2];
+    double A[3], B[3], C[3];
+    load_tri(P, T, t, A, B, C);
     const int n = ex0 * ex1 * ex2;
-    for (int q0 = threadIdx.x; q0 < n; q0 += blockDim.x) {
-      const int i = lo0 + q0 % ex0, j = lo1 + (q0 / ex0) % ex1, k = lo2 + q0 / (ex0 * ex1);
-      const size_t v = vid(g, i, j, k);
-      const float qx = (float)(g.org[0] + i), qy = (float)(g.org[1] + j), qz = (float)(g.org[2] + k);
-      const float gx = fmaxf(fmaxf(blo0 - qx, qx - bhi0), 0.f);
-      const float gy = fmaxf(fmaxf(blo1 - qy, qy - bhi1), 0.f);
-      const float gz = fmaxf(fmaxf(blo2 - qz, qz - bhi2), 0.f);
-      float lb = sqrtf(gx * gx + gy * gy + gz * gz);
-      if (has_plane) {
-        const float pd = fabsf(pl.x * qx + pl.y * qy + pl.z * qz + pl.w);
-        float se = 0.f;
-        se = fmaxf(se, fe0.x * qx + fe0.y * qy + fe0.z * qz + fe0.w);
-        se = fmaxf(se, fe1.x * qx + fe1.y * qy + fe1.z * qz + fe1.w);
-        se = fmaxf(se, fe2.x * qx + fe2.y * qy + fe2.z * qz + fe2.w);
-        lb = fmaxf(lb, sqrtf(pd * pd + se * se));
+    for (int c0 = 0; c0 < n; c0 += kSdfChunk) {
+      if (threadIdx.x == 0) count = 0;
+      __syncthreads();
+      const int c1 = min(n, c0 + kSdfChunk);
+      for (int base = c0; base < c1; base += blockDim.x) {
+        const int q0 = base + threadIdx.x;
+        bool keep = false;
+        if (q0 < c1) {
+          const int i = lo0 + q0 % ex0, j = lo1 + (q0 / ex0) % ex1, k = lo2 + q0 / (ex0 * ex1);
+          const size_t v = vid(g, i, j, k);
+          const float qx = (float)(g.org[0] + i), qy = (float)(g.org[1] + j), qz = (float)(g.org[2] + k);
+          const float gx = fmaxf(fmaxf(blo0 - qx, qx - bhi0), 0.f);
+          const float gy = fmaxf(fmaxf(blo1 - qy, qy - bhi1), 0.f);
+          const float gz = fmaxf(fmaxf(blo2 - qz, qz - bhi2), 0.f);
+          float lb = sqrtf(gx * gx + gy * gy + gz * gz);
+          if (has_plane) {
+            const float pd = fabsf(pl.x * qx + pl.y * qy + pl.z * qz + pl.w);
+            float se = 0.f;
+            se = fmaxf(se, fe0.x * qx + fe0.y * qy + fe0.z * qz + fe0.w);
+            se = fmaxf(se, fe1.x * qx + fe1.y * qy + fe1.z * qz + fe1.w);
+            se = fmaxf(se, fe2.x * qx + fe2.y * qy + fe2.z * qz + fe2.w);
+            lb = fmaxf(lb, sqrtf(pd * pd + se * se));
+          }
+          const float cur = fminf(__uint_as_float(*(volatile const uint32_t*)&dist[v]), __uint_as_float(ub[v]));
+          keep = lb - 2.0f * g.margin < cur;
+        }
+        // warp-aggregated append (at most kSdfChunk entries per chunk)
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        int at = 0;
+        if (lane == 0 && m) at = atomicAdd(&count, __popc(m));
+        at = __shfl_sync(0xffffffffu, at, 0);
+        if (keep) list[at + __popc(m & ((1u << lane) - 1u))] = q0;
       }
-      const float cur = fminf(__uint_as_float(*(volatile const uint32_t*)&dist[v]), __uint_as_float(ub[v]));
-      if (lb - 2.0f * g.margin >= cur) continue;
-      double A[3], B[3], C[3];
-      load_tri(P, T, t, A, B, C);
-      const double q[3] = {(double)(g.org[0] + i), (double)(g.org[1] + j), (double)(g.org[2] + k)};
-      const float d = __double2float_rn(point_tri_dist(q, A, B, C));
-      atomicMin(&dist[v], __float_as_uint(d));
+      __syncthreads();
+      const int nc = count;
+      for (int e = threadIdx.x; e < nc; e += blockDim.x) {
+        const int q0 = list[e];
+        const int i = lo0 + q0 % ex0, j = lo1 + (q0 / ex0) % ex1, k = lo2 + q0 / (ex0 * ex1);
+        const double q[3] = {(double)(g.org[0] + i), (double)(g.org[1] + j), (double)(g.org[2] + k)};
+        const float d = __double2float_rn(point_tri_dist(q, A, B, C));
+        atomicMin(&dist[vid(g, i, j, k)], __float_as_uint(d));
+      }
+      __syncthreads();
     }
   }
 }
@@ -266,7 +297,9 @@ __global__ void __launch_bounds__(128) sdf_cross_kernel(const double* __restrict
                                                         int nt, SdfGrid g, int ax, uint32_t* __restrict__ toggle) {
   const int u = (ax + 1) % 3, w = (ax + 2) % 3;
   const double ou = 1.2345679e-6, ow = 2.3456789e-6;
-  for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+  // One thread per triangle: a triangle covers a few rays (its projected box
+  // on the grid plane), far fewer than a block's threads.
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += gridDim.x * blockDim.x) {
     double A[3], B[3], C[3];
     load_tri(P, T, t, A, B, C);
     const int u0 = max(0, (int)floor(min3(A[u], B[u], C[u]) - g.org[u]));
@@ -275,7 +308,7 @@ __global__ void __launch_bounds__(128) sdf_cross_kernel(const double* __restrict
     const int w1 = min(g.dim[w] - 1, (int)ceil(max3(A[w], B[w], C[w]) - g.org[w]));
     const int eu = u1 - u0 + 1, ew = w1 - w0 + 1;
     if (eu <= 0 || ew <= 0) continue;
-    for (int r = threadIdx.x; r < eu * ew; r += blockDim.x) {
+    for (int r = 0; r < eu * ew; ++r) {
       const int ku = u0 + r % eu, kw = w0 + r / eu;
       const double y = da((double)(g.org[u] + ku), ou), z = da((double)(g.org[w] + kw), ow);
       const double e0 = ds(dm(ds(B[u], A[u]), ds(z, A[w])), dm(ds(B[w], A[w]), ds(y, A[u])));
@@ -532,7 +565,8 @@ extern "C" int visacd_sdf_remesh(visacd_ctx* ctx, const double* verts, int32_t n
           dist);
   for (int ax = 0; ax < 3; ++ax) {
     VCUDA(cudaMemsetAsync(tog, 0, nvox * 4, st));
-    VLAUNCH(ctx, kKSdfCross, gt, 128, 0, sdf_cross_kernel, dP, dT, nt, g, ax, tog);
+    VLAUNCH(ctx, kKSdfCross, grid_for(nt, 128, 16 * (int64_t)ctx->sm_count), 128, 0, sdf_cross_kernel, dP, dT, nt,
+            g, ax, tog);
     const int u = (ax + 1) % 3, w = (ax + 2) % 3;
     VLAUNCH(ctx, kKSdfCross, grid_for((int64_t)g.dim[u] * g.dim[w], 128, 1 << 20), 128, 0, sdf_parity_kernel, g, ax,
             tog, votes);

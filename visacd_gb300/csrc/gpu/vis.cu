@@ -216,14 +216,15 @@ __device__ __forceinline__ uint64_t spread21_v(uint64_t x) {
 }
 
 __global__ void point_morton_kernel(const float* __restrict__ pts, int32_t n,
-                                    const VisCounters* __restrict__ c, uint64_t* __restrict__ keys,
+                                    const VisCounters* __restrict__ c, int bits, uint64_t* __restrict__ keys,
                                     uint32_t* __restrict__ vals) {
   float lo[3], sc[3];
+  const float top = (float)((1u << bits) - 1u);
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     lo[a] = o2f_v(c->pmin[a]);
     float ext = o2f_v(c->pmax[a]) - lo[a];
-    sc[a] = ext > 0.f ? 2097151.0f / ext : 0.f;
+    sc[a] = ext > 0.f ? top / ext : 0.f;
   }
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
@@ -231,7 +232,7 @@ __global__ void point_morton_kernel(const float* __restrict__ pts, int32_t n,
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
       float x = (pts[3 * i + a] - lo[a]) * sc[a];
-      x = fminf(fmaxf(x, 0.f), 2097151.0f);
+      x = fminf(fmaxf(x, 0.f), top);
       q[a] = (uint64_t)x;
     }
     keys[i] = (spread21_v(q[0]) << 2) | (spread21_v(q[1]) << 1) | spread21_v(q[2]);
@@ -358,9 +359,9 @@ int vis_morton_order(visacd_ctx* ctx, const float* d_pts, int32_t n, uint32_t* p
   uint64_t* keys = slot<uint64_t>(ctx, kSlotVisKeys);
   const unsigned gp = grid_for(n, 256, 4LL * ctx->sm_count);
   VLAUNCH(ctx, kKVisPrep, gp, 256, 0, point_bounds_kernel, d_pts, n, cnt);
-  VLAUNCH(ctx, kKVisPrep, gp, 256, 0, point_morton_kernel, d_pts, n, cnt, keys, perm);
+  VLAUNCH(ctx, kKVisPrep, gp, 256, 0, point_morton_kernel, d_pts, n, cnt, morton_bits(n), keys, perm);
   VTRY(radix_sort_u64(ctx, keys, perm, slot<uint64_t>(ctx, kSlotVisKeysAlt),
-                      slot<uint32_t>(ctx, kSlotVisPermAlt), n, 64));
+                      slot<uint32_t>(ctx, kSlotVisPermAlt), n, 3 * morton_bits(n)));
   VCUDA(cudaStreamSynchronize(ctx->stream));
   return VISACD_OK;
 }
@@ -398,9 +399,9 @@ static int vis_device(visacd_ctx* ctx, const float* d_pts, int32_t n, const uint
   uint32_t* perm = slot<uint32_t>(ctx, kSlotVisPerm);
   const unsigned gp = grid_for(n, 256, 4LL * ctx->sm_count);
   VLAUNCH(ctx, kKVisPrep, gp, 256, 0, point_bounds_kernel, d_pts, n, cnt);
-  VLAUNCH(ctx, kKVisPrep, gp, 256, 0, point_morton_kernel, d_pts, n, cnt, keys, perm);
+  VLAUNCH(ctx, kKVisPrep, gp, 256, 0, point_morton_kernel, d_pts, n, cnt, morton_bits(n), keys, perm);
   VTRY(radix_sort_u64(ctx, keys, perm, slot<uint64_t>(ctx, kSlotVisKeysAlt),
-                      slot<uint32_t>(ctx, kSlotVisPermAlt), n, 64));
+                      slot<uint32_t>(ctx, kSlotVisPermAlt), n, 3 * morton_bits(n)));
 
   const int variant = choose_vis_variant(ctx, n, d_new != nullptr, self_bvh, cage_bvh);
   const int TR = kVisVariants[variant].tr, TC = 32 / TR;
