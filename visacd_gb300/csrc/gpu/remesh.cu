@@ -293,43 +293,87 @@ __global__ void __launch_bounds__(128) sdf_dist_kernel(const double* __restrict_
   }
 }
 
-__global__ void __launch_bounds__(128) sdf_cross_kernel(const double* __restrict__ P, const int32_t* __restrict__ T,
-                                                        int nt, SdfGrid g, int ax, uint32_t* __restrict__ toggle) {
-  const int u = (ax + 1) % 3, w = (ax + 2) % 3;
+// Crossing of one ray (grid column (ku, kw) along axis ax) with a triangle:
+// toggles the first voxel whose centre lies beyond the crossing.
+__device__ __forceinline__ void cross_ray(const double (&A)[3], const double (&B)[3], const double (&C)[3],
+                                          const SdfGrid& g, int ax, int u, int w, int ku, int kw,
+                                          uint32_t* __restrict__ toggle) {
   const double ou = 1.2345679e-6, ow = 2.3456789e-6;
-  // One thread per triangle: a triangle covers a few rays (its projected box
-  // on the grid plane), far fewer than a block's threads.
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += gridDim.x * blockDim.x) {
+  const double y = da((double)(g.org[u] + ku), ou), z = da((double)(g.org[w] + kw), ow);
+  const double e0 = ds(dm(ds(B[u], A[u]), ds(z, A[w])), dm(ds(B[w], A[w]), ds(y, A[u])));
+  const double e1 = ds(dm(ds(C[u], B[u]), ds(z, B[w])), dm(ds(C[w], B[w]), ds(y, B[u])));
+  const double e2 = ds(dm(ds(A[u], C[u]), ds(z, C[w])), dm(ds(A[w], C[w]), ds(y, C[u])));
+  const bool in = (e0 > 0 && e1 > 0 && e2 > 0) || (e0 < 0 && e1 < 0 && e2 < 0);
+  if (!in) return;
+  const double sw = da(da(e0, e1), e2);
+  const double x = __ddiv_rn(da(da(dm(e1, A[ax]), dm(e2, B[ax])), dm(e0, C[ax])), sw);
+  // first voxel s whose centre org + s lies beyond x (integers compare exactly)
+  int s = (int)floor(x - (double)g.org[ax]) + 1;
+  while (s > 0 && (double)(g.org[ax] + s - 1) > x) --s;
+  while (s < g.dim[ax] && !((double)(g.org[ax] + s) > x)) ++s;
+  if (s < 0) s = 0;
+  if (s >= g.dim[ax]) return;
+  int gi[3];
+  gi[ax] = s;
+  gi[u] = ku;
+  gi[w] = kw;
+  atomicXor(&toggle[vid(g, gi[0], gi[1], gi[2])], 1u);
+}
+
+// The rays a triangle covers: its box projected on the grid plane.
+__device__ __forceinline__ bool ray_box(const double (&A)[3], const double (&B)[3], const double (&C)[3],
+                                        const SdfGrid& g, int u, int w, int& u0, int& w0, int& eu, int& ew) {
+  u0 = max(0, (int)floor(min3(A[u], B[u], C[u]) - g.org[u]));
+  const int u1 = min(g.dim[u] - 1, (int)ceil(max3(A[u], B[u], C[u]) - g.org[u]));
+  w0 = max(0, (int)floor(min3(A[w], B[w], C[w]) - g.org[w]));
+  const int w1 = min(g.dim[w] - 1, (int)ceil(max3(A[w], B[w], C[w]) - g.org[w]));
+  eu = u1 - u0 + 1;
+  ew = w1 - w0 + 1;
+  return eu > 0 && ew > 0;
+}
+
+// Triangles covering at most kCrossSmall rays (nearly all): kCrossLanes lanes
+// each, over its rays. Larger ones (the long triangles of clipped parts' caps,
+// big faces): one block each (sdf_cross_wide_kernel).
+constexpr int kCrossSmall = 32;
+constexpr int kCrossLanes = 8;
+
+__global__ void __launch_bounds__(128) sdf_cross_kernel(const double* __restrict__ P, const int32_t* __restrict__ T,
+                                                        int nt, SdfGrid g, int ax, uint32_t* __restrict__ toggle,
+                                                        int* __restrict__ wide, unsigned* __restrict__ n_wide) {
+  const int u = (ax + 1) % 3, w = (ax + 2) % 3;
+  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int sub = gid % kCrossLanes;
+  const int groups = (gridDim.x * blockDim.x) / kCrossLanes;
+  for (int t = gid / kCrossLanes; t < nt; t += groups) {
     double A[3], B[3], C[3];
     load_tri(P, T, t, A, B, C);
-    const int u0 = max(0, (int)floor(min3(A[u], B[u], C[u]) - g.org[u]));
-    const int u1 = min(g.dim[u] - 1, (int)ceil(max3(A[u], B[u], C[u]) - g.org[u]));
-    const int w0 = max(0, (int)floor(min3(A[w], B[w], C[w]) - g.org[w]));
-    const int w1 = min(g.dim[w] - 1, (int)ceil(max3(A[w], B[w], C[w]) - g.org[w]));
-    const int eu = u1 - u0 + 1, ew = w1 - w0 + 1;
-    if (eu <= 0 || ew <= 0) continue;
-    for (int r = 0; r < eu * ew; ++r) {
-      const int ku = u0 + r % eu, kw = w0 + r / eu;
-      const double y = da((double)(g.org[u] + ku), ou), z = da((double)(g.org[w] + kw), ow);
-      const double e0 = ds(dm(ds(B[u], A[u]), ds(z, A[w])), dm(ds(B[w], A[w]), ds(y, A[u])));
-      const double e1 = ds(dm(ds(C[u], B[u]), ds(z, B[w])), dm(ds(C[w], B[w]), ds(y, B[u])));
-      const double e2 = ds(dm(ds(A[u], C[u]), ds(z, C[w])), dm(ds(A[w], C[w]), ds(y, C[u])));
-      const bool in = (e0 > 0 && e1 > 0 && e2 > 0) || (e0 < 0 && e1 < 0 && e2 < 0);
-      if (!in) continue;
-      const double sw = da(da(e0, e1), e2);
-      const double x = __ddiv_rn(da(da(dm(e1, A[ax]), dm(e2, B[ax])), dm(e0, C[ax])), sw);
-      // first voxel s whose centre org + s lies beyond x (integers compare exactly)
-      int s = (int)floor(x - (double)g.org[ax]) + 1;
-      while (s > 0 && (double)(g.org[ax] + s - 1) > x) --s;
-      while (s < g.dim[ax] && !((double)(g.org[ax] + s) > x)) ++s;
-      if (s < 0) s = 0;
-      if (s >= g.dim[ax]) continue;
-      int gi[3];
-      gi[ax] = s;
-      gi[u] = ku;
-      gi[w] = kw;
-      atomicXor(&toggle[vid(g, gi[0], gi[1], gi[2])], 1u);
+    int u0, w0, eu, ew;
+    if (!ray_box(A, B, C, g, u, w, u0, w0, eu, ew)) continue;
+    if (eu * ew > kCrossSmall) {
+      if (sub == 0) wide[atomicAdd(n_wide, 1u)] = t;
+      continue;
     }
+    for (int r = sub; r < eu * ew; r += kCrossLanes)
+      cross_ray(A, B, C, g, ax, u, w, u0 + r % eu, w0 + r / eu, toggle);
+  }
+}
+
+__global__ void __launch_bounds__(128) sdf_cross_wide_kernel(const double* __restrict__ P,
+                                                             const int32_t* __restrict__ T, SdfGrid g, int ax,
+                                                             const int* __restrict__ wide,
+                                                             const unsigned* __restrict__ n_wide,
+                                                             uint32_t* __restrict__ toggle) {
+  const int u = (ax + 1) % 3, w = (ax + 2) % 3;
+  const int nw = (int)*n_wide;
+  for (int k = blockIdx.x; k < nw; k += gridDim.x) {
+    const int t = wide[k];
+    double A[3], B[3], C[3];
+    load_tri(P, T, t, A, B, C);
+    int u0, w0, eu, ew;
+    if (!ray_box(A, B, C, g, u, w, u0, w0, eu, ew)) continue;
+    for (int r = threadIdx.x; r < eu * ew; r += blockDim.x)
+      cross_ray(A, B, C, g, ax, u, w, u0 + r % eu, w0 + r / eu, toggle);
   }
 }
 
@@ -525,6 +569,7 @@ extern "C" int visacd_sdf_remesh(visacd_ctx* ctx, const double* verts, int32_t n
     return o;
   };
   const size_t oP = take(P.size() * 8), oT = take(3 * (size_t)nt * 4), oPrep = take((size_t)nt * sizeof(SdfTri)),
+               oWide = take(3 * (size_t)nt * 4), oNWide = take(16),
                oDist = take(nvox * 4),
                oTog = take(nvox * 4), oVotes = take(nvox), oF = take(nvox * 4), oFlag = take(ncell * 4),
                oCoff = take((ncell + 1) * 8), oCv = take(ncell * 4), oQcnt = take(nint * 4),
@@ -563,10 +608,18 @@ extern "C" int visacd_sdf_remesh(visacd_ctx* ctx, const double* verts, int32_t n
   VLAUNCH(ctx, kKSdfDist, gt, 128, 0, sdf_ub_kernel, dP, dT, nt, g, (const SdfTri*)prep, tog);
   VLAUNCH(ctx, kKSdfDist, gt, 128, 0, sdf_dist_kernel, dP, dT, nt, g, (const SdfTri*)prep, (const uint32_t*)tog,
           dist);
+  // Per axis: the triangles covering many rays are listed by the first
+  // kernel and done one block each by the second (lists and counts per axis).
+  int* wide = (int*)(base + oWide);
+  unsigned* n_wide = (unsigned*)(base + oNWide);
+  VCUDA(cudaMemsetAsync(n_wide, 0, 16, st));
   for (int ax = 0; ax < 3; ++ax) {
     VCUDA(cudaMemsetAsync(tog, 0, nvox * 4, st));
-    VLAUNCH(ctx, kKSdfCross, grid_for(nt, 128, 16 * (int64_t)ctx->sm_count), 128, 0, sdf_cross_kernel, dP, dT, nt,
-            g, ax, tog);
+    VLAUNCH(ctx, kKSdfCross, grid_for((int64_t)kCrossLanes * nt, 128, 16 * (int64_t)ctx->sm_count), 128, 0,
+            sdf_cross_kernel, dP, dT, nt, g, ax, tog, wide + (size_t)ax * nt, n_wide + ax);
+    VLAUNCH(ctx, kKSdfCross, (unsigned)std::min<int64_t>(nt, 4 * (int64_t)ctx->sm_count), 128, 0,
+            sdf_cross_wide_kernel, dP, dT, g, ax, (const int*)(wide + (size_t)ax * nt),
+            (const unsigned*)(n_wide + ax), tog);
     const int u = (ax + 1) % 3, w = (ax + 2) % 3;
     VLAUNCH(ctx, kKSdfCross, grid_for((int64_t)g.dim[u] * g.dim[w], 128, 1 << 20), 128, 0, sdf_parity_kernel, g, ax,
             tog, votes);
