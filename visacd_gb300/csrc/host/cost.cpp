@@ -110,7 +110,7 @@ void extract_point_set(const Mesh& m, std::vector<Vec3>& samples, std::vector<in
     samples.resize(b0 + resolution);
     tri_ids.resize(b0 + resolution);
     const DiscreteSampler fast(pick);
-#pragma omp parallel for schedule(static) if (resolution >= 16384)
+#pragma omp parallel for schedule(static) if (resolution >= 2048)
     for (long j = 0; j < (long)resolution; ++j) {
       const uint32_t* q = w.data() + (size_t)per * j;
       size_t ti = 0;
@@ -143,7 +143,7 @@ void extract_point_set(const Mesh& m, std::vector<Vec3>& samples, std::vector<in
   const size_t b1 = samples.size();
   samples.resize(b1 + rest.size());
   tri_ids.resize(b1 + rest.size());
-#pragma omp parallel for schedule(static) if (rest.size() >= 16384)
+#pragma omp parallel for schedule(static) if (rest.size() >= 2048)
   for (long k = 0; k < (long)rest.size(); ++k) {
     const uint32_t* q = w.data() + 4 * k;
     samples[b1 + k] = tri_sample(m, (size_t)rest[k], canonical53(q[0], q[1]), canonical53(q[2], q[3]));

@@ -10,6 +10,7 @@
 // as they are (they decide which hulls merge).
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <map>
 #include <numeric>
 #include <unordered_map>
@@ -30,23 +31,40 @@ int find_root(std::vector<int>& p, int x) {
   return x;
 }
 
+// Edge-connected components with flat structures: an open-addressing table
+// from undirected edge to the first triangle holding it (the union of every
+// triangle with that one gives the components whatever the order), then each
+// component's triangles in index order with its vertices numbered on first use
+// (a stamp per vertex marks the component being built).
 MeshList separate_step(const Mesh& part) {
   const int T = (int)part.triangles.size();
   if (T == 0) return {};
   std::vector<int> uf(T);
   std::iota(uf.begin(), uf.end(), 0);
-  std::map<std::pair<int, int>, int> first_tri;
+  size_t cap = 64;
+  while (cap < 6 * (size_t)T) cap <<= 1;
+  std::vector<uint64_t> keys(cap, ~0ull);
+  std::vector<int> first(cap);
+  const uint64_t mask = cap - 1;
   for (int i = 0; i < T; ++i) {
     const auto& t = part.triangles[i];
     const std::pair<int, int> e[3] = {std::minmax(t[0], t[1]), std::minmax(t[1], t[2]),
                                       std::minmax(t[0], t[2])};
     for (const auto& k : e) {
-      auto it = first_tri.find(k);
-      if (it == first_tri.end()) {
-        first_tri[k] = i;
-      } else {
-        int a = find_root(uf, it->second), b = find_root(uf, i);
-        if (a != b) uf[std::max(a, b)] = std::min(a, b);
+      const uint64_t key = ((uint64_t)(uint32_t)k.first << 32) | (uint32_t)k.second;
+      uint64_t h = (key * 0x9E3779B97F4A7C15ull) >> 20;
+      for (;; ++h) {
+        const uint64_t slot = h & mask;
+        if (keys[slot] == ~0ull) {
+          keys[slot] = key;
+          first[slot] = i;
+          break;
+        }
+        if (keys[slot] == key) {
+          int a = find_root(uf, first[slot]), b = find_root(uf, i);
+          if (a != b) uf[std::max(a, b)] = std::min(a, b);
+          break;
+        }
       }
     }
   }
@@ -58,34 +76,44 @@ MeshList separate_step(const Mesh& part) {
     if (comp_of_root[r] < 0) comp_of_root[r] = nparts++;
     comp[i] = comp_of_root[r];
   }
-  MeshList out(nparts);
-  std::vector<std::unordered_map<int, int>> remap(nparts);
-  const bool has_new = !part.is_new.empty();
-  for (int i = 0; i < T; ++i) {
-    Mesh& m = out[comp[i]];
-    auto& rm = remap[comp[i]];
-    Tri nt;
-    for (int k = 0; k < 3; ++k) {
-      int g = part.triangles[i][k];
-      auto it = rm.find(g);
-      if (it == rm.end()) {
-        int id = (int)m.vertices.size();
-        rm[g] = id;
-        m.vertices.push_back(part.vertices[g]);
-        if (has_new) m.is_new.push_back(part.is_new[g]);
-        nt[k] = id;
-      } else {
-        nt[k] = it->second;
-      }
-    }
-    m.triangles.push_back(nt);
+  // Triangles grouped by component, in index order within each.
+  std::vector<int> start(nparts + 1, 0), order(T);
+  for (int i = 0; i < T; ++i) ++start[comp[i] + 1];
+  for (int p = 0; p < nparts; ++p) start[p + 1] += start[p];
+  {
+    std::vector<int> fill(start.begin(), start.end() - 1);
+    for (int i = 0; i < T; ++i) order[fill[comp[i]]++] = i;
   }
-  for (const auto& e : part.intersecting_edges) {
-    for (int p = 0; p < nparts; ++p) {
-      auto a = remap[p].find((int)e.first), b = remap[p].find((int)e.second);
-      if (a != remap[p].end() && b != remap[p].end()) {
-        out[p].intersecting_edges.push_back({(unsigned)a->second, (unsigned)b->second});
-        break;
+  MeshList out(nparts);
+  const bool has_new = !part.is_new.empty();
+  const size_t NV = part.vertices.size();
+  std::vector<int> stamp(NV, -1), local(NV);
+  std::vector<char> taken(part.intersecting_edges.size(), 0);
+  for (int p = 0; p < nparts; ++p) {
+    Mesh& m = out[p];
+    m.triangles.reserve(start[p + 1] - start[p]);
+    for (int k0 = start[p]; k0 < start[p + 1]; ++k0) {
+      const int i = order[k0];
+      Tri nt;
+      for (int k = 0; k < 3; ++k) {
+        const int g = part.triangles[i][k];
+        if (stamp[g] != p) {
+          stamp[g] = p;
+          local[g] = (int)m.vertices.size();
+          m.vertices.push_back(part.vertices[g]);
+          if (has_new) m.is_new.push_back(part.is_new[g]);
+        }
+        nt[k] = local[g];
+      }
+      m.triangles.push_back(nt);
+    }
+    // Each visibility edge goes to the first component holding both endpoints.
+    for (size_t k = 0; k < part.intersecting_edges.size(); ++k) {
+      if (taken[k]) continue;
+      const auto& e = part.intersecting_edges[k];
+      if (stamp[e.first] == p && stamp[e.second] == p) {
+        m.intersecting_edges.push_back({(unsigned)local[e.first], (unsigned)local[e.second]});
+        taken[k] = 1;
       }
     }
   }
