@@ -125,3 +125,20 @@ def test_every_launch_shape_gives_the_same_edges(ctx, native, orc):
     assert 0 <= best < len(ms) and all(x > 0 for x in ms)
     e, _ = ctx.visibility(v, sb, cb)
     np.testing.assert_array_equal(e, ref)
+
+
+def test_bvh_depth(ctx):
+    """The tree depth reported by the build (root height in edges, taken in the
+    bottom-up fit): within [ceil(log2 n), n - 1], exact for small trees."""
+    import math
+    from visacd_gb300 import meshgen as mg
+    tri = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [1, 1, 0]], np.float32)
+    b = ctx.bvh(tri, np.array([[0, 1, 2], [1, 3, 2]], np.int32))
+    assert b.info() == (2, 1)
+    b.close()
+    for level in (2, 4):
+        v, t = mg.displaced_blob(level, seed=1)
+        b = ctx.bvh(v, t)
+        nt, depth = b.info()
+        assert nt == len(t) and math.ceil(math.log2(nt)) <= depth <= nt - 1
+        b.close()

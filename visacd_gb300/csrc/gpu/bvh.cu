@@ -199,15 +199,18 @@ __global__ void leaf_kernel(const float* __restrict__ v, int32_t nv,
 
 __global__ void fit_kernel(const int2* __restrict__ child, const int* __restrict__ parent_int,
                            const int* __restrict__ parent_leaf, const float* __restrict__ leafbox,
-                           float* __restrict__ nodebox, unsigned* __restrict__ visits, int32_t n,
-                           BuildCounters* __restrict__ c) {
+                           float* __restrict__ nodebox, unsigned* __restrict__ visits, int* __restrict__ height,
+                           int32_t n, BuildCounters* __restrict__ c) {
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
     int node = parent_leaf[s];
-    int depth = 1;
     for (int guard = 0; node >= 0 && guard < n + 1; ++guard) {
       __threadfence();
       if (atomicAdd(&visits[node], 1u) == 0u) break;
       int2 ch = child[node];
+      // Height in edges (leaves 0); the root's is the tree depth.
+      const int h = 1 + max(ch.x < 0 ? 0 : __ldcg(&height[ch.x]), ch.y < 0 ? 0 : __ldcg(&height[ch.y]));
+      __stcg(&height[node], h);
+      if (node == 0) atomicMax(&c->depth, h);
       float b[6];
 #pragma unroll
       for (int a = 0; a < 3; ++a) {
@@ -221,18 +224,7 @@ __global__ void fit_kernel(const int2* __restrict__ child, const int* __restrict
 #pragma unroll
       for (int a = 0; a < 6; ++a) __stcg(&nodebox[6 * (int64_t)node + a], b[a]);
       node = parent_int[node];
-      ++depth;
     }
-  }
-  // Tree depth (root-to-deepest-leaf edges), a separate walk per leaf.
-  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
-    int node = parent_leaf[s];
-    int depth = 1;
-    for (int guard = 0; node > 0 && guard < n + 1; ++guard) {
-      node = parent_int[node];
-      ++depth;
-    }
-    atomicMax(&c->depth, depth);
   }
 }
 
@@ -307,7 +299,7 @@ int bvh_build(visacd_ctx* ctx, const float* verts, int32_t nv, const uint32_t* t
          o_v = carve((size_t)nt * 4), o_v2 = carve((size_t)nt * 4),
          o_child = carve((size_t)n_int * 8), o_pi = carve((size_t)n_int * 4),
          o_pl = carve((size_t)nt * 4), o_lb = carve((size_t)nt * 24),
-         o_nb = carve((size_t)n_int * 24), o_vis = carve((size_t)n_int * 4),
+         o_nb = carve((size_t)n_int * 24), o_vis = carve((size_t)n_int * 4), o_h = carve((size_t)n_int * 4),
          o_cnt = carve(sizeof(BuildCounters));
   VTRY(ensure_slot(ctx, kSlotTmpTris, off));
   char* base = slot<char>(ctx, kSlotTmpTris);
@@ -320,6 +312,7 @@ int bvh_build(visacd_ctx* ctx, const float* verts, int32_t nv, const uint32_t* t
   float* leafbox = (float*)(base + o_lb);
   float* nodebox = (float*)(base + o_nb);
   unsigned* visits = (unsigned*)(base + o_vis);
+  int* height = (int*)(base + o_h);
   BuildCounters* cnt = (BuildCounters*)(base + o_cnt);
 
   BuildCounters init;
@@ -362,7 +355,7 @@ int bvh_build(visacd_ctx* ctx, const float* verts, int32_t nv, const uint32_t* t
   } else {
     const unsigned gi = grid_for(n_int, 256, 8LL * ctx->sm_count);
     VLAUNCH(ctx, kKKarras, gi, 256, 0, karras_kernel, keys, nt, child, pint, pleaf);
-    VLAUNCH(ctx, kKFit, g, 256, 0, fit_kernel, child, pint, pleaf, leafbox, nodebox, visits, nt,
+    VLAUNCH(ctx, kKFit, g, 256, 0, fit_kernel, child, pint, pleaf, leafbox, nodebox, visits, height, nt,
             cnt);
     VLAUNCH(ctx, kKNodeLayout, gi, 256, 0, node_layout_kernel, child, leafbox, nodebox, n_int,
             b->nodes);

@@ -290,7 +290,40 @@ __global__ void scan_add_kernel(const uint32_t* __restrict__ in, int64_t n,
   if (blockIdx.x == 0 && threadIdx.x == 0) out[n] = block_sums[nb];
 }
 
+// Small scans (up to kScanSingle elements) in one launch: one block walks
+// the tiles in order with a running carry.
+constexpr int64_t kScanSingle = 4 * kScanTile;
+
+__global__ void scan_single_kernel(const uint32_t* __restrict__ in, int64_t n, uint64_t* __restrict__ out) {
+  uint64_t carry = 0;
+  for (int64_t t0 = 0; t0 < n; t0 += kScanTile) {
+    const int64_t base = t0 + (int64_t)threadIdx.x * kScanItems;
+    uint32_t v[kScanItems];
+    uint64_t s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+      const int64_t i = base + k;
+      v[k] = i < n ? in[i] : 0u;
+      s += v[k];
+    }
+    uint64_t total;
+    uint64_t ex = block_exclusive_scan_u64(s, &total) + carry;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+      const int64_t i = base + k;
+      if (i < n) out[i] = ex;
+      ex += v[k];
+    }
+    carry += total;
+  }
+  if (threadIdx.x == 0) out[n] = carry;
+}
+
 int exclusive_scan_u32_to_u64(visacd_ctx* ctx, const uint32_t* in, uint64_t* out, int64_t n) {
+  if (n <= kScanSingle) {
+    VLAUNCH(ctx, kKScanAdd, 1, kScanThreads, 0, scan_single_kernel, in, n, out);
+    return VISACD_OK;
+  }
   int64_t nb = (n + kScanTile - 1) / kScanTile;
   if (nb < 1) nb = 1;
   VCHECK(nb < (1ll << 31), VISACD_ERR_INVALID_ARG, "scan too large: %lld", (long long)n);
