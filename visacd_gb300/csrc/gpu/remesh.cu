@@ -5,11 +5,12 @@
 // Same algorithm and arithmetic as the host restatement (manifold_preprocess in
 // csrc/host/remesh.cpp), so the output mesh is identical bit for bit:
 //  1. sdf_tri_prep_kernel computes each triangle's set-up once (voxel box,
-//     FP32 bounds and planes); sdf_dist_kernel, one block per triangle, gives
-//     every voxel centre in the triangle's box grown by the band the exact FP64
-//     point-triangle distance (rounded to float) unless a lower bound rules it
-//     out, combined with atomicMin (non-negative floats order like their bit
-//     patterns).
+//     FP32 bounds and planes); the boxes are cut into work items of 1024
+//     voxels; sdf_ub_kernel gives every band voxel an FP32 upper bound of its
+//     distance, then sdf_dist_kernel gives every voxel centre in each
+//     triangle's box grown by the band the exact FP64 point-triangle distance
+//     (rounded to float) unless a lower bound rules it out, combined with
+//     atomicMin (non-negative floats order like their bit patterns).
 //  2. For each axis: sdf_cross_kernel marks, for every ray through voxel
 //     centres (offset by 1.2345679e-6 / 2.3456789e-6 voxels) that crosses a
 //     triangle at x, the first voxel whose centre lies beyond x (XOR toggle);
@@ -76,8 +77,10 @@ struct SdfTri {
   int has_plane, pad[3];
 };
 
+constexpr int kSdfChunk = 1024;  // box voxels per work item of the distance passes
+
 __global__ void sdf_tri_prep_kernel(const double* __restrict__ P, const int32_t* __restrict__ T, int nt, SdfGrid g,
-                                    SdfTri* __restrict__ out) {
+                                    SdfTri* __restrict__ out, uint32_t* __restrict__ chunks) {
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += gridDim.x * blockDim.x) {
     double A[3], B[3], C[3];
     load_tri(P, T, t, A, B, C);
@@ -127,7 +130,36 @@ __global__ void sdf_tri_prep_kernel(const double* __restrict__ P, const int32_t*
       }
     }
     out[t] = r;
+    chunks[t] = r.ext[0] > 0 ? (uint32_t)((r.ext[0] * r.ext[1] * r.ext[2] + kSdfChunk - 1) / kSdfChunk) : 0u;
   }
+}
+
+// Work items of the distance passes: (triangle, chunk of kSdfChunk voxels of
+// its box), numbered by the scanned chunk counts. Block b takes a contiguous
+// range of items, so a triangle with a large box (the long triangles of a
+// clipped part's cap) is spread over several blocks instead of holding one
+// while the rest of the grid idles.
+struct SdfItems {
+  const uint64_t* off;  // nt + 1 scanned chunk counts
+  int nt;
+};
+
+__device__ __forceinline__ void item_range(const SdfItems& W, long long& w0, long long& w1) {
+  const long long total = (long long)W.off[W.nt];
+  const long long per = (total + gridDim.x - 1) / gridDim.x;
+  w0 = (long long)blockIdx.x * per;
+  w1 = min(total, w0 + per);
+}
+
+// Triangle of item w (off[t] <= w < off[t + 1]).
+__device__ __forceinline__ int item_triangle(const SdfItems& W, long long w) {
+  int lo = 0, hi = W.nt;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if ((long long)W.off[mid] <= w) lo = mid;
+    else hi = mid;
+  }
+  return lo;
 }
 
 // FP32 upper bound of the distance from q to triangle (A, B, C): the distance
@@ -192,11 +224,14 @@ __device__ __forceinline__ float sdf_lower_bound(const SdfTri& r, float qx, floa
 }
 
 __global__ void __launch_bounds__(128) sdf_ub_kernel(const double* __restrict__ P, const int32_t* __restrict__ T,
-                                                     int nt, SdfGrid g, const SdfTri* __restrict__ prep,
+                                                     SdfItems W, SdfGrid g, const SdfTri* __restrict__ prep,
                                                      uint32_t* __restrict__ ub) {
-  for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+  long long w0, w1;
+  item_range(W, w0, w1);
+  int t = w0 < w1 ? item_triangle(W, w0) : 0;
+  for (long long w = w0; w < w1; ++w) {
+    while ((long long)W.off[t + 1] <= w) ++t;
     const SdfTri r = prep[t];
-    if (r.ext[0] <= 0) continue;
     double Ad[3], Bd[3], Cd[3];
     load_tri(P, T, t, Ad, Bd, Cd);
     const float A[3] = {(float)Ad[0], (float)Ad[1], (float)Ad[2]};
@@ -207,7 +242,8 @@ __global__ void __launch_bounds__(128) sdf_ub_kernel(const double* __restrict__ 
     float mabs = 0.f;
     for (int a = 0; a < 3; ++a) mabs = fmaxf(mabs, fmaxf(fabsf(A[a]), fmaxf(fabsf(B[a]), fabsf(C[a]))));
     const int n = r.ext[0] * r.ext[1] * r.ext[2];
-    for (int q0 = threadIdx.x; q0 < n; q0 += blockDim.x) {
+    const int c0 = (int)(w - (long long)W.off[t]) * kSdfChunk, c1 = min(n, c0 + kSdfChunk);
+    for (int q0 = c0 + threadIdx.x; q0 < c1; q0 += blockDim.x) {
       const int i = r.lo[0] + q0 % r.ext[0], j = r.lo[1] + (q0 / r.ext[0]) % r.ext[1],
                 k = r.lo[2] + q0 / (r.ext[0] * r.ext[1]);
       const size_t v = vid(g, i, j, k);
@@ -222,22 +258,23 @@ __global__ void __launch_bounds__(128) sdf_ub_kernel(const double* __restrict__ 
   }
 }
 
-// The box is filtered in chunks of kSdfChunk voxels; the voxels that pass are
-// appended to a shared list and evaluated in FP64 by all threads together, so
-// the FP64 pipe (slow on this part) runs with full warps instead of the few
-// lanes that pass the filter in each warp.
-constexpr int kSdfChunk = 1024;
-
+// Each work item (a chunk of kSdfChunk box voxels) is filtered first; the
+// voxels that pass are appended to a shared list and evaluated in FP64 by all
+// threads together, so the FP64 pipe (slow on this part) runs with full warps
+// instead of the few lanes that pass the filter in each warp.
 __global__ void __launch_bounds__(128) sdf_dist_kernel(const double* __restrict__ P, const int32_t* __restrict__ T,
-                                                       int nt, SdfGrid g, const SdfTri* __restrict__ prep,
+                                                       SdfItems W, SdfGrid g, const SdfTri* __restrict__ prep,
                                                        const uint32_t* __restrict__ ub, uint32_t* __restrict__ dist) {
   __shared__ int list[kSdfChunk];
   __shared__ int count;
   const int lane = threadIdx.x & 31;
-  for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+  long long w0, w1;
+  item_range(W, w0, w1);
+  int t = w0 < w1 ? item_triangle(W, w0) : 0;
+  for (long long w = w0; w < w1; ++w) {
+    while ((long long)W.off[t + 1] <= w) ++t;
     const SdfTri& r = prep[t];
     const int ex0 = r.ext[0], ex1 = r.ext[1], ex2 = r.ext[2];
-    if (ex0 <= 0) continue;
     const int lo0 = r.lo[0], lo1 = r.lo[1], lo2 = r.lo[2];
     const float blo0 = r.blo[0], blo1 = r.blo[1], blo2 = r.blo[2];
     const float bhi0 = r.bhi[0], bhi1 = r.bhi[1], bhi2 = r.bhi[2];
@@ -246,50 +283,48 @@ __global__ void __launch_bounds__(128) sdf_dist_kernel(const double* __restrict_
     double A[3], B[3], C[3];
     load_tri(P, T, t, A, B, C);
     const int n = ex0 * ex1 * ex2;
-    for (int c0 = 0; c0 < n; c0 += kSdfChunk) {
-      if (threadIdx.x == 0) count = 0;
-      __syncthreads();
-      const int c1 = min(n, c0 + kSdfChunk);
-      for (int base = c0; base < c1; base += blockDim.x) {
-        const int q0 = base + threadIdx.x;
-        bool keep = false;
-        if (q0 < c1) {
-          const int i = lo0 + q0 % ex0, j = lo1 + (q0 / ex0) % ex1, k = lo2 + q0 / (ex0 * ex1);
-          const size_t v = vid(g, i, j, k);
-          const float qx = (float)(g.org[0] + i), qy = (float)(g.org[1] + j), qz = (float)(g.org[2] + k);
-          const float gx = fmaxf(fmaxf(blo0 - qx, qx - bhi0), 0.f);
-          const float gy = fmaxf(fmaxf(blo1 - qy, qy - bhi1), 0.f);
-          const float gz = fmaxf(fmaxf(blo2 - qz, qz - bhi2), 0.f);
-          float lb = sqrtf(gx * gx + gy * gy + gz * gz);
-          if (has_plane) {
-            const float pd = fabsf(pl.x * qx + pl.y * qy + pl.z * qz + pl.w);
-            float se = 0.f;
-            se = fmaxf(se, fe0.x * qx + fe0.y * qy + fe0.z * qz + fe0.w);
-            se = fmaxf(se, fe1.x * qx + fe1.y * qy + fe1.z * qz + fe1.w);
-            se = fmaxf(se, fe2.x * qx + fe2.y * qy + fe2.z * qz + fe2.w);
-            lb = fmaxf(lb, sqrtf(pd * pd + se * se));
-          }
-          const float cur = fminf(__uint_as_float(*(volatile const uint32_t*)&dist[v]), __uint_as_float(ub[v]));
-          keep = lb - 2.0f * g.margin < cur;
-        }
-        // warp-aggregated append (at most kSdfChunk entries per chunk)
-        const unsigned m = __ballot_sync(0xffffffffu, keep);
-        int at = 0;
-        if (lane == 0 && m) at = atomicAdd(&count, __popc(m));
-        at = __shfl_sync(0xffffffffu, at, 0);
-        if (keep) list[at + __popc(m & ((1u << lane) - 1u))] = q0;
-      }
-      __syncthreads();
-      const int nc = count;
-      for (int e = threadIdx.x; e < nc; e += blockDim.x) {
-        const int q0 = list[e];
+    const int c0 = (int)(w - (long long)W.off[t]) * kSdfChunk, c1 = min(n, c0 + kSdfChunk);
+    if (threadIdx.x == 0) count = 0;
+    __syncthreads();
+    for (int base = c0; base < c1; base += blockDim.x) {
+      const int q0 = base + threadIdx.x;
+      bool keep = false;
+      if (q0 < c1) {
         const int i = lo0 + q0 % ex0, j = lo1 + (q0 / ex0) % ex1, k = lo2 + q0 / (ex0 * ex1);
-        const double q[3] = {(double)(g.org[0] + i), (double)(g.org[1] + j), (double)(g.org[2] + k)};
-        const float d = __double2float_rn(point_tri_dist(q, A, B, C));
-        atomicMin(&dist[vid(g, i, j, k)], __float_as_uint(d));
+        const size_t v = vid(g, i, j, k);
+        const float qx = (float)(g.org[0] + i), qy = (float)(g.org[1] + j), qz = (float)(g.org[2] + k);
+        const float gx = fmaxf(fmaxf(blo0 - qx, qx - bhi0), 0.f);
+        const float gy = fmaxf(fmaxf(blo1 - qy, qy - bhi1), 0.f);
+        const float gz = fmaxf(fmaxf(blo2 - qz, qz - bhi2), 0.f);
+        float lb = sqrtf(gx * gx + gy * gy + gz * gz);
+        if (has_plane) {
+          const float pd = fabsf(pl.x * qx + pl.y * qy + pl.z * qz + pl.w);
+          float se = 0.f;
+          se = fmaxf(se, fe0.x * qx + fe0.y * qy + fe0.z * qz + fe0.w);
+          se = fmaxf(se, fe1.x * qx + fe1.y * qy + fe1.z * qz + fe1.w);
+          se = fmaxf(se, fe2.x * qx + fe2.y * qy + fe2.z * qz + fe2.w);
+          lb = fmaxf(lb, sqrtf(pd * pd + se * se));
+        }
+        const float cur = fminf(__uint_as_float(*(volatile const uint32_t*)&dist[v]), __uint_as_float(ub[v]));
+        keep = lb - 2.0f * g.margin < cur;
       }
-      __syncthreads();
+      // warp-aggregated append (at most kSdfChunk entries per item)
+      const unsigned m = __ballot_sync(0xffffffffu, keep);
+      int at = 0;
+      if (lane == 0 && m) at = atomicAdd(&count, __popc(m));
+      at = __shfl_sync(0xffffffffu, at, 0);
+      if (keep) list[at + __popc(m & ((1u << lane) - 1u))] = q0;
     }
+    __syncthreads();
+    const int nc = count;
+    for (int e = threadIdx.x; e < nc; e += blockDim.x) {
+      const int q0 = list[e];
+      const int i = lo0 + q0 % ex0, j = lo1 + (q0 / ex0) % ex1, k = lo2 + q0 / (ex0 * ex1);
+      const double q[3] = {(double)(g.org[0] + i), (double)(g.org[1] + j), (double)(g.org[2] + k)};
+      const float d = __double2float_rn(point_tri_dist(q, A, B, C));
+      atomicMin(&dist[vid(g, i, j, k)], __float_as_uint(d));
+    }
+    __syncthreads();
   }
 }
 
@@ -569,7 +604,8 @@ extern "C" int visacd_sdf_remesh(visacd_ctx* ctx, const double* verts, int32_t n
     return o;
   };
   const size_t oP = take(P.size() * 8), oT = take(3 * (size_t)nt * 4), oPrep = take((size_t)nt * sizeof(SdfTri)),
-               oWide = take(3 * (size_t)nt * 4), oNWide = take(16),
+               oWide = take(3 * (size_t)nt * 4), oNWide = take(16), oChunks = take((size_t)nt * 4),
+               oChunkOff = take(((size_t)nt + 1) * 8),
                oDist = take(nvox * 4),
                oTog = take(nvox * 4), oVotes = take(nvox), oF = take(nvox * 4), oFlag = take(ncell * 4),
                oCoff = take((ncell + 1) * 8), oCv = take(ncell * 4), oQcnt = take(nint * 4),
@@ -598,15 +634,21 @@ extern "C" int visacd_sdf_remesh(visacd_ctx* ctx, const double* verts, int32_t n
   std::memcpy(&band_bits, &band_f, 4);
   VLAUNCH(ctx, kKSdf, gv, 256, 0, sdf_fill_kernel, dist, nvox, band_bits);
   VCUDA(cudaMemsetAsync(votes, 0, nvox, st));
-  const unsigned gt = (unsigned)std::min<int64_t>(nt, 64 * (int64_t)ctx->sm_count);
   SdfTri* prep = (SdfTri*)(base + oPrep);
+  uint32_t* chunks = (uint32_t*)(base + oChunks);
+  uint64_t* chunk_off = (uint64_t*)(base + oChunkOff);
   VLAUNCH(ctx, kKSdfDist, grid_for(nt, 128, 16 * (int64_t)ctx->sm_count), 128, 0, sdf_tri_prep_kernel, dP, dT, nt,
-          g, prep);
+          g, prep, chunks);
+  VTRY(exclusive_scan_u32_to_u64(ctx, chunks, chunk_off, nt));
+  SdfItems items;
+  items.off = chunk_off;
+  items.nt = nt;
+  const unsigned gw = (unsigned)(8 * (int64_t)ctx->sm_count);
   // First pass: FP32 upper bounds per voxel in the toggle buffer (free until
   // the crossings), then the exact pass.
   VLAUNCH(ctx, kKSdf, gv, 256, 0, sdf_fill_kernel, tog, nvox, band_bits);
-  VLAUNCH(ctx, kKSdfDist, gt, 128, 0, sdf_ub_kernel, dP, dT, nt, g, (const SdfTri*)prep, tog);
-  VLAUNCH(ctx, kKSdfDist, gt, 128, 0, sdf_dist_kernel, dP, dT, nt, g, (const SdfTri*)prep, (const uint32_t*)tog,
+  VLAUNCH(ctx, kKSdfDist, gw, 128, 0, sdf_ub_kernel, dP, dT, items, g, (const SdfTri*)prep, tog);
+  VLAUNCH(ctx, kKSdfDist, gw, 128, 0, sdf_dist_kernel, dP, dT, items, g, (const SdfTri*)prep, (const uint32_t*)tog,
           dist);
   // Per axis: the triangles covering many rays are listed by the first
   // kernel and done one block each by the second (lists and counts per axis).
