@@ -135,3 +135,78 @@ def test_concavity_metric_deterministic_under_seed(V):
     # samples on the other surface, so a surface against itself is small, not 0.
     V.set_seed(3)
     assert V._compute_hb(hv["vertices"], hv["triangles"], hv["vertices"], hv["triangles"], 3000) < 0.05
+
+
+def _separate_reference(v, t, is_new, edges):
+    """Plain restatement of lib/src/postprocess.cpp:202-326 for the test:
+    edge-connected components numbered by their lowest triangle, vertices
+    renumbered in first-use order, is_new carried, each edge to the first
+    component holding both endpoints, |volume| < 1e-6 dropped."""
+    T = len(t)
+    parent = list(range(T))
+
+    def root(x):
+        while parent[x] != x:
+            parent[x] = parent[parent[x]]
+            x = parent[x]
+        return x
+
+    first = {}
+    for i, tri in enumerate(t):
+        for a, b in ((tri[0], tri[1]), (tri[1], tri[2]), (tri[0], tri[2])):
+            k = (min(a, b), max(a, b))
+            if k in first:
+                ra, rb = root(first[k]), root(i)
+                if ra != rb:
+                    parent[max(ra, rb)] = min(ra, rb)
+            else:
+                first[k] = i
+    comp_of_root, comp = {}, []
+    for i in range(T):
+        r = root(i)
+        comp_of_root.setdefault(r, len(comp_of_root))
+        comp.append(comp_of_root[r])
+    parts = [{"v": [], "t": [], "new": [], "map": {}, "e": []} for _ in comp_of_root]
+    for i, tri in enumerate(t):
+        p = parts[comp[i]]
+        nt = []
+        for g in tri:
+            if g not in p["map"]:
+                p["map"][g] = len(p["v"])
+                p["v"].append(v[g])
+                p["new"].append(is_new[g])
+            nt.append(p["map"][g])
+        p["t"].append(nt)
+    for a, b in edges:
+        for p in parts:
+            if a in p["map"] and b in p["map"]:
+                p["e"].append((p["map"][a], p["map"][b]))
+                break
+    out = []
+    for p in parts:
+        pv, pt = np.array(p["v"]), np.array(p["t"])
+        vol = sum(np.dot(pv[a], np.cross(pv[b], pv[c])) for a, b, c in pt) / 6.0
+        if abs(vol) >= 1e-6:
+            out.append(p)
+    return out
+
+
+def test_separate_disjoint_edges_and_flags(V):
+    v1, t1 = mg.displaced_blob(2, seed=1)
+    v2, t2 = mg.displaced_blob(2, seed=2)
+    v = np.concatenate([v1, v2 + 3.0, v1 * 1e-3 + 9.0])
+    n1, n2 = len(v1), len(v2)
+    # the second blob's triangles first, so component order differs from vertex order
+    t = np.concatenate([t2 + n1, t1, t1 + n1 + n2]).astype(np.int32)
+    rng = np.random.default_rng(5)
+    is_new = (rng.random(len(v)) < 0.3).astype(np.uint8)
+    e = rng.integers(0, len(v), size=(400, 2))
+    e = e[e[:, 0] != e[:, 1]].astype(np.uint32)
+    got = V._separate_disjoint(v, t, is_new, e)
+    ref = _separate_reference(v, t.tolist(), is_new.tolist(), e.tolist())
+    assert len(got) == len(ref) == 2
+    for g, r in zip(got, ref):
+        np.testing.assert_array_equal(g["vertices"], np.array(r["v"]))
+        np.testing.assert_array_equal(g["triangles"], np.array(r["t"]))
+        np.testing.assert_array_equal(g["is_new"], np.array(r["new"], np.uint8))
+        np.testing.assert_array_equal(g["edges"].reshape(-1, 2), np.array(r["e"], np.uint32).reshape(-1, 2))

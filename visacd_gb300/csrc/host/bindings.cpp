@@ -259,13 +259,25 @@ PYBIND11_MODULE(visacd, m) {
     return mesh_dist(ma, mb);
   });
   m.def("_mesh_volume", [](py::array_t<double> v, py::array_t<int> t) { return mesh_volume(np_to_mesh(v, t)); });
-  m.def("_separate_disjoint", [](py::array_t<double> v, py::array_t<int> t) {
-    MeshList parts{np_to_mesh(v, t)};
-    separate_disjoint(parts);
-    py::list out;
-    for (const auto& p : parts) out.append(mesh_dict(p));
-    return out;
-  });
+  m.def(
+      "_separate_disjoint",
+      [](py::array_t<double> v, py::array_t<int> t, py::object is_new, py::object edges) {
+        Mesh mm = np_to_mesh(v, t);
+        if (!is_new.is_none()) {
+          auto a = py::array_t<uint8_t, py::array::c_style | py::array::forcecast>(is_new);
+          for (py::ssize_t i = 0; i < a.size(); ++i) mm.is_new.push_back(a.data()[i] != 0);
+        }
+        if (!edges.is_none()) {
+          auto a = py::array_t<uint32_t, py::array::c_style | py::array::forcecast>(edges);
+          for (py::ssize_t i = 0; i + 1 < a.size(); i += 2) mm.intersecting_edges.push_back({a.data()[i], a.data()[i + 1]});
+        }
+        MeshList parts{mm};
+        separate_disjoint(parts);
+        py::list out;
+        for (const auto& p : parts) out.append(mesh_dict(p));
+        return out;
+      },
+      py::arg("v"), py::arg("t"), py::arg("is_new") = py::none(), py::arg("edges") = py::none());
   m.def("_visibility", [](py::array_t<double> v, py::array_t<int> t, py::array_t<double> cv, py::array_t<int> ct) {
     Mesh mm = np_to_mesh(v, t), cage = np_to_mesh(cv, ct);
     auto e = gpu::visibility_edges(mm, cage);
