@@ -210,3 +210,34 @@ def test_separate_disjoint_edges_and_flags(V):
         np.testing.assert_array_equal(g["triangles"], np.array(r["t"]))
         np.testing.assert_array_equal(g["is_new"], np.array(r["new"], np.uint8))
         np.testing.assert_array_equal(g["edges"].reshape(-1, 2), np.array(r["e"], np.uint32).reshape(-1, 2))
+
+
+def test_refine_proposals_selects_nearest_bisectors(V):
+    """The learned search's refinement: per proposal, the `per` bisector
+    planes nearest under 2 - 2|n.n'| + ((s d - d') / half)^2 (ties by edge
+    index), union in edge order: against a numpy restatement."""
+    v, t = mg.displaced_blob(3, seed=6)
+    rng = np.random.default_rng(2)
+    e = rng.integers(0, len(v), size=(3000, 2))
+    e = e[e[:, 0] != e[:, 1]]
+    e = np.sort(e, 1).astype(np.uint32)
+    prop = rng.normal(size=(16, 4))
+    prop[:, :3] /= np.linalg.norm(prop[:, :3], axis=1, keepdims=True)
+    prop[:, 3] *= 0.3
+    got = V._refine_proposals(v, e, prop, 32)
+    p1, p2 = v[e[:, 0]], v[e[:, 1]]
+    n = p2 - p1
+    ln = np.sqrt((n ** 2).sum(1))
+    ok = ln >= 1e-6
+    n = n[ok] / ln[ok, None]
+    m = (p1[ok] + p2[ok]) * 0.5
+    bis = np.concatenate([n, -(n * m).sum(1, keepdims=True)], 1)
+    half = 0.5 * (v.max(0) - v.min(0)).max()
+    keep = np.zeros(len(bis), bool)
+    for q in prop:
+        c = bis[:, :3] @ q[:3]
+        s = np.where(c >= 0, 1.0, -1.0)
+        d = 2.0 - 2.0 * np.abs(c) + ((s * q[3] - bis[:, 3]) / half) ** 2
+        order = np.lexsort((np.arange(len(d)), d))
+        keep[order[:32]] = True
+    np.testing.assert_allclose(got, bis[keep], rtol=0, atol=1e-15)

@@ -242,6 +242,26 @@ PYBIND11_MODULE(visacd, m) {
   m.def("_compute_hb", [](py::array_t<double> v, py::array_t<int> t, py::array_t<double> hv, py::array_t<int> ht, unsigned res) {
     return compute_hb(np_to_mesh(v, t), np_to_mesh(hv, ht), res);
   });
+  m.def("_refine_proposals", [](py::array_t<double> v, py::array_t<uint32_t> edges, py::array_t<double> planes,
+                                int per) {
+    Mesh mm;
+    auto vv = v.unchecked<2>();
+    for (py::ssize_t i = 0; i < vv.shape(0); ++i) mm.vertices.push_back({vv(i, 0), vv(i, 1), vv(i, 2)});
+    auto ee = edges.unchecked<2>();
+    for (py::ssize_t i = 0; i < ee.shape(0); ++i) mm.intersecting_edges.push_back({ee(i, 0), ee(i, 1)});
+    auto pp = planes.unchecked<2>();
+    std::vector<Plane> prop;
+    for (py::ssize_t i = 0; i < pp.shape(0); ++i) prop.emplace_back(pp(i, 0), pp(i, 1), pp(i, 2), pp(i, 3));
+    const auto out = refine_proposals(mm, prop, per);
+    py::array_t<double> r({(py::ssize_t)out.size(), (py::ssize_t)4});
+    for (size_t i = 0; i < out.size(); ++i) {
+      r.mutable_at(i, 0) = out[i].a;
+      r.mutable_at(i, 1) = out[i].b;
+      r.mutable_at(i, 2) = out[i].c;
+      r.mutable_at(i, 3) = out[i].d;
+    }
+    return r;
+  });
   m.def("_engine_next", [](int n) {
     std::vector<uint32_t> w((size_t)std::max(n, 0));
     random_engine().fill(w.data(), w.size());

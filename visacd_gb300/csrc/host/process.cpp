@@ -104,6 +104,8 @@ bool exhaustive_plane(const Mesh& mesh, const std::vector<Plane>& flat_planes, P
   return true;
 }
 
+}  // namespace
+
 // Refinement of the proposals: for each proposal, the perpendicular-bisector
 // planes (the reference's candidate form, lib/src/process.cpp:45-53) of the
 // `per` visibility edges whose bisectors are nearest to it, under the distance
@@ -125,25 +127,43 @@ std::vector<Plane> refine_proposals(const Mesh& mesh, const std::vector<Plane>& 
     const Vec3 m = (V[e.first] + V[e.second]) * 0.5;
     bis.emplace_back(n[0], n[1], n[2], -dot(n, m));
   }
-  std::vector<char> keep(bis.size(), 0);
-  std::vector<std::pair<double, int>> d(bis.size());
   const int k = std::min<int>(per, (int)bis.size());
-  for (const auto& q : prop) {
+  std::vector<char> keep(bis.size(), 0);
+  if (k > 0) {
+    // The k smallest (distance, index) pairs per proposal (a unique set: the
+    // pairs are distinct), in one pass over the bisectors with a bounded
+    // max-heap per proposal.
+    using Item = std::pair<double, int>;
+    std::vector<std::vector<Item>> heaps(prop.size());
+    for (auto& h : heaps) h.reserve(k + 1);
     for (size_t i = 0; i < bis.size(); ++i) {
-      const double c = q.a * bis[i].a + q.b * bis[i].b + q.c * bis[i].c;
-      const double s = c >= 0 ? 1.0 : -1.0;
-      const double dd = (s * q.d - bis[i].d) / half;
-      d[i] = {2.0 - 2.0 * std::fabs(c) + dd * dd, (int)i};
+      for (size_t q = 0; q < prop.size(); ++q) {
+        const Plane& p = prop[q];
+        const double c = p.a * bis[i].a + p.b * bis[i].b + p.c * bis[i].c;
+        const double s = c >= 0 ? 1.0 : -1.0;
+        const double dd = (s * p.d - bis[i].d) / half;
+        const Item it{2.0 - 2.0 * std::fabs(c) + dd * dd, (int)i};
+        auto& h = heaps[q];
+        if ((int)h.size() < k) {
+          h.push_back(it);
+          std::push_heap(h.begin(), h.end());
+        } else if (it < h.front()) {
+          std::pop_heap(h.begin(), h.end());
+          h.back() = it;
+          std::push_heap(h.begin(), h.end());
+        }
+      }
     }
-    if (k <= 0) break;
-    std::nth_element(d.begin(), d.begin() + (k - 1), d.end());
-    for (int j = 0; j < k; ++j) keep[d[j].second] = 1;
+    for (const auto& h : heaps)
+      for (const auto& it : h) keep[it.second] = 1;
   }
   std::vector<Plane> out;
   for (size_t i = 0; i < bis.size(); ++i)
     if (keep[i]) out.push_back(bis[i]);
   return out;
 }
+
+namespace {
 
 // Learned search: the proposer's 16 planes refined by nearby bisector planes,
 // a probe of proposer_probe_planes random candidates (the reference's draw,

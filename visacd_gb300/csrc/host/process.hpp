@@ -23,6 +23,11 @@ std::vector<Plane> get_candidate_planes(const std::vector<Vec3>& vertices,
 bool decompose_iteration(Mesh& mesh, MeshList& parts, Mesh& cage,
                          const std::vector<Plane>& flat_planes);
 
+// The learned search's refinement: for each proposal, the perpendicular-
+// bisector planes of the `per` visibility edges nearest to it under the
+// proposer's training distance, in edge order, each edge once.
+std::vector<Plane> refine_proposals(const Mesh& mesh, const std::vector<Plane>& prop, int per);
+
 double compute_part_score(const Mesh& part);
 int get_part_with_highest_score(const MeshList& parts);
 // Convex hulls of the parts kept from one iteration to the next (a hull
