@@ -1,6 +1,7 @@
 #include "core.hpp"
 
 #include <algorithm>
+#include <cstring>
 
 namespace visacd {
 
@@ -34,17 +35,20 @@ void Mt19937::seed(result_type s) {
 }
 
 // One pass of the recurrence x_k = x_{k+M} ^ A((x_k & upper) | (x_{k+1} & lower))
-// over the state, in three runs with fixed index offsets (each run's source
-// words are final before it reads them).
+// over the state, in runs with fixed index offsets (each run's source words
+// are final before it reads them) and trip counts that are multiples of 4 so
+// the loops vectorise; then the whole block's outputs are tempered at once.
 void Mt19937::twist() {
   auto mix = [](uint32_t a, uint32_t b, uint32_t c) {
     const uint32_t y = (a & 0x80000000u) | (b & 0x7fffffffu);
     return c ^ (y >> 1) ^ ((0u - (y & 1u)) & 0x9908b0dfu);
   };
-  int k = 0;
-  for (; k < kN - kM; ++k) x_[k] = mix(x_[k], x_[k + 1], x_[k + kM]);
-  for (; k < kN - 1; ++k) x_[k] = mix(x_[k], x_[k + 1], x_[k + kM - kN]);
+  static_assert(kN - kM == 227 && kN - 1 - (kN - kM) == 396, "MT19937 run lengths");
+  for (int k = 0; k < 224; ++k) x_[k] = mix(x_[k], x_[k + 1], x_[k + kM]);
+  for (int k = 224; k < kN - kM; ++k) x_[k] = mix(x_[k], x_[k + 1], x_[k + kM]);
+  for (int k = kN - kM; k < kN - 1; ++k) x_[k] = mix(x_[k], x_[k + 1], x_[k + kM - kN]);
   x_[kN - 1] = mix(x_[kN - 1], x_[0], x_[kM - 1]);
+  for (int k = 0; k < kN; ++k) out_[k] = temper(x_[k]);
   pos_ = 0;
 }
 
@@ -52,7 +56,7 @@ void Mt19937::fill(uint32_t* out, size_t n) {
   while (n > 0) {
     if (pos_ >= kN) twist();
     const size_t take = std::min(n, (size_t)(kN - pos_));
-    for (size_t i = 0; i < take; ++i) out[i] = temper(x_[pos_ + (int)i]);
+    std::memcpy(out, out_ + pos_, take * sizeof(uint32_t));
     pos_ += (int)take;
     out += take;
     n -= take;

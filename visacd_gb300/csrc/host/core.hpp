@@ -124,7 +124,7 @@ class Mt19937 {
   void seed(result_type s);
   result_type operator()() {
     if (pos_ >= kN) twist();
-    return temper(x_[pos_++]);
+    return out_[pos_++];
   }
   // The next n outputs, in order.
   void fill(uint32_t* out, size_t n);
@@ -139,6 +139,7 @@ class Mt19937 {
   }
   void twist();
   uint32_t x_[kN];
+  uint32_t out_[kN];  // the current block's outputs (tempered state)
   int pos_ = kN;
 };
 
