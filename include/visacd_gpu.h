@@ -91,6 +91,10 @@ int visacd_ctx_destroy(visacd_ctx* ctx);
 int visacd_ctx_synchronize(visacd_ctx* ctx);
 /* Per-kernel CUDA-event timing on the context stream (off by default). */
 int visacd_ctx_set_timing(visacd_ctx* ctx, int enable);
+/* How this context's calls wait for the GPU: 0 (default) spins, the lowest
+   latency for a single caller; 1 sleeps on a blocking-sync event, leaving the
+   cores to other host threads when many contexts share one machine. */
+int visacd_ctx_set_blocking_wait(visacd_ctx* ctx, int enable);
 int visacd_ctx_reset_times(visacd_ctx* ctx);
 /* Accumulated time and launch count per kernel name since the last reset.
    Synchronizes the stream. names[i] stay valid for the life of the library. */

@@ -31,7 +31,7 @@ EXPORTED = [
     "visacd_lp_features", "visacd_lp_forward", "visacd_lp_propose", "visacd_lp_grads",
     "visacd_lp_train_step",
     "visacd_sdf_remesh", "visacd_sdf_fetch", "visacd_hull_distances", "visacd_segment_triangle_tests",
-    "visacd_set_blocking_sync", "visacd_lp_set_tcgen05",
+    "visacd_set_blocking_sync", "visacd_lp_set_tcgen05", "visacd_ctx_set_blocking_wait",
 ]
 
 LP_POINTS = 2048

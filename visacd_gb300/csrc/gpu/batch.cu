@@ -687,7 +687,7 @@ extern "C" int visacd_batch_run(visacd_ctx* ctx, visacd_batch* b, int use_graph)
 extern "C" int visacd_batch_results(visacd_ctx* ctx, visacd_batch* b, int64_t* n_edges, double* scores,
                                     int32_t* argmax, uint32_t* edges, int64_t edge_capacity) {
   VCHECK(ctx && b, VISACD_ERR_INVALID_ARG, "batch_results: null argument");
-  VCUDA(cudaStreamSynchronize(ctx->stream));
+  VCUDA(stream_wait(ctx));
   VTRY(check_status(ctx, "batch run"));
   std::vector<BatchDyn> dyn(b->n_parts);
   VCUDA(cudaMemcpy(dyn.data(), b->d_dyn, dyn.size() * sizeof(BatchDyn), cudaMemcpyDeviceToHost));

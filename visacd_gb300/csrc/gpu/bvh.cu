@@ -361,7 +361,7 @@ int bvh_build(visacd_ctx* ctx, const float* verts, int32_t nv, const uint32_t* t
             b->nodes);
   }
   VCUDA(cudaMemcpyAsync(hcnt, cnt, sizeof(BuildCounters), cudaMemcpyDeviceToHost, ctx->stream));
-  VCUDA(cudaStreamSynchronize(ctx->stream));
+  VCUDA(stream_wait(ctx));
   if (hcnt->bad_index) {
     cudaFreeAsync(b->nodes, ctx->stream);
     cudaFreeAsync(b->tris, ctx->stream);

@@ -660,7 +660,7 @@ extern "C" int visacd_clip(visacd_ctx* ctx, const double* verts, int32_t nv, con
   VCUDA(cudaMemcpyAsync(h64 + 1, on + nt, 8, cudaMemcpyDeviceToHost, st));
   VCUDA(cudaMemcpyAsync(h64 + 2, mp + nv, 8, cudaMemcpyDeviceToHost, st));
   VCUDA(cudaMemcpyAsync(h64 + 3, mn + nv, 8, cudaMemcpyDeviceToHost, st));
-  VCUDA(cudaStreamSynchronize(st));
+  VCUDA(stream_wait(ctx));
   VCHECK(!h->overflow, VISACD_ERR_CAPACITY, "visacd_clip: internal table overflow");
   ctx->clip_out.n_pos = (int32_t)h64[0];
   ctx->clip_out.n_neg = (int32_t)h64[1];
@@ -697,12 +697,12 @@ extern "C" int visacd_clip_fetch(visacd_ctx* ctx, int32_t* pos_tris, int32_t* ne
     std::vector<int32_t> a(r.n_border_edges), b(r.n_border_edges);
     VCUDA(cudaMemcpyAsync(a.data(), ctx->clip_ptrs[5], (size_t)r.n_border_edges * 4, cudaMemcpyDeviceToHost, st));
     VCUDA(cudaMemcpyAsync(b.data(), ctx->clip_ptrs[6], (size_t)r.n_border_edges * 4, cudaMemcpyDeviceToHost, st));
-    VCUDA(cudaStreamSynchronize(st));
+    VCUDA(stream_wait(ctx));
     for (int32_t k = 0; k < r.n_border_edges; ++k) {
       border_edges[2 * k] = a[k];
       border_edges[2 * k + 1] = b[k];
     }
   }
-  VCUDA(cudaStreamSynchronize(st));
+  VCUDA(stream_wait(ctx));
   return VISACD_OK;
 }

@@ -121,6 +121,8 @@ struct visacd_ctx {
   int sm_count = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
+  bool blocking_wait = false;        // host waits block (no spinning): see stream_wait
+  cudaEvent_t wait_event = nullptr;  // blocking-sync event for those waits
   vgpu::DevBuf buf[kSlotCount];
   uint32_t* d_status = nullptr;      // device status word
   void* h_pinned = nullptr;          // small pinned staging area
@@ -233,6 +235,18 @@ inline T* slot(visacd_ctx* ctx, int s) {
   return reinterpret_cast<T*>(ctx->buf[s].p);
 }
 inline int ensure_slot(visacd_ctx* ctx, int s, size_t bytes) { return ensure(ctx->buf[s], bytes); }
+
+// Wait for the context's stream. By default the host thread spins (lowest
+// latency for one caller); with blocking_wait it sleeps on a blocking-sync
+// event, which leaves the cores to the other host threads when many
+// contexts share the machine (process_batch workers).
+inline cudaError_t stream_wait(visacd_ctx* ctx) {
+  if (ctx->blocking_wait && ctx->wait_event) {
+    cudaError_t e = cudaEventRecord(ctx->wait_event, ctx->stream);
+    return e != cudaSuccess ? e : cudaEventSynchronize(ctx->wait_event);
+  }
+  return cudaStreamSynchronize(ctx->stream);
+}
 
 inline unsigned grid_for(int64_t n, int block, int64_t cap) {
   int64_t g = (n + block - 1) / block;

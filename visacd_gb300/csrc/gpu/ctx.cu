@@ -152,7 +152,7 @@ int pinned(visacd_ctx* ctx, size_t bytes, void** out) {
 
 int Stager::reserve(size_t total_bytes, int arrays) {
   const size_t need = total_bytes + 64 * (size_t)(arrays + 1);
-  VCUDA(cudaStreamSynchronize(ctx_->stream));
+  VCUDA(stream_wait(ctx_));
   if (need > ctx_->h_upload_cap) {
     if (ctx_->h_upload) cudaFreeHost(ctx_->h_upload);
     ctx_->h_upload = nullptr;
@@ -191,7 +191,7 @@ int check_status(visacd_ctx* ctx, const char* what) {
   uint32_t* h = nullptr;
   VTRY(pinned(ctx, 64, (void**)&h));
   VCUDA(cudaMemcpyAsync(h, ctx->d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
-  VCUDA(cudaStreamSynchronize(ctx->stream));
+  VCUDA(stream_wait(ctx));
   uint32_t s = h[0];
   if (s) {
     VCUDA(cudaMemsetAsync(ctx->d_status, 0, sizeof(uint32_t), ctx->stream));
@@ -544,10 +544,18 @@ extern "C" int visacd_ctx_create(int device, void* cuda_stream, visacd_ctx** out
     }
     ctx->own_stream = true;
   }
+  e = cudaEventCreateWithFlags(&ctx->wait_event, cudaEventBlockingSync | cudaEventDisableTiming);
+  if (e != cudaSuccess) {
+    if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    set_error("cudaEventCreate: %s", cudaGetErrorString(e));
+    return VISACD_ERR_CUDA;
+  }
   e = cudaMalloc(&ctx->d_status, 256);
   if (e == cudaSuccess) e = cudaMemset(ctx->d_status, 0, 256);
   if (e != cudaSuccess) {
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+    cudaEventDestroy(ctx->wait_event);
     delete ctx;
     set_error("status word allocation: %s", cudaGetErrorString(e));
     return VISACD_ERR_NO_MEMORY;
@@ -580,6 +588,7 @@ extern "C" int visacd_ctx_destroy(visacd_ctx* ctx) {
     cudaEventDestroy(p.b);
   }
   for (auto e : ctx->event_pool) cudaEventDestroy(e);
+  if (ctx->wait_event) cudaEventDestroy(ctx->wait_event);
   if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return VISACD_OK;
@@ -587,7 +596,13 @@ extern "C" int visacd_ctx_destroy(visacd_ctx* ctx) {
 
 extern "C" int visacd_ctx_synchronize(visacd_ctx* ctx) {
   VCHECK(ctx, VISACD_ERR_INVALID_ARG, "null context");
-  VCUDA(cudaStreamSynchronize(ctx->stream));
+  VCUDA(stream_wait(ctx));
+  return VISACD_OK;
+}
+
+extern "C" int visacd_ctx_set_blocking_wait(visacd_ctx* ctx, int enable) {
+  VCHECK(ctx, VISACD_ERR_INVALID_ARG, "null context");
+  ctx->blocking_wait = enable != 0;
   return VISACD_OK;
 }
 
@@ -599,7 +614,7 @@ extern "C" int visacd_ctx_set_timing(visacd_ctx* ctx, int enable) {
 
 static int drain_pending(visacd_ctx* ctx) {
   if (ctx->pending.empty()) return VISACD_OK;
-  VCUDA(cudaStreamSynchronize(ctx->stream));
+  VCUDA(stream_wait(ctx));
   for (auto& p : ctx->pending) {
     float ms = 0.f;
     VCUDA(cudaEventElapsedTime(&ms, p.a, p.b));

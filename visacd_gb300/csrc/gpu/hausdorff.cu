@@ -839,7 +839,7 @@ extern "C" int visacd_face_hausdorff_batch(visacd_ctx* ctx, int32_t njobs, const
   double* hres = nullptr;
   VTRY(pinned(ctx, (size_t)njobs * 8, (void**)&hres));
   VCUDA(cudaMemcpyAsync(hres, D + o_jm, (size_t)njobs * 8, cudaMemcpyDeviceToHost, st));
-  VCUDA(cudaStreamSynchronize(st));
+  VCUDA(stream_wait(ctx));
   std::memcpy(out, hres, (size_t)njobs * 8);
   return VISACD_OK;
 }

@@ -168,6 +168,6 @@ extern "C" int visacd_hull_distances(visacd_ctx* ctx, const double* verts, const
           (const int64_t*)(base + oOff), (const double*)(base + oBB), (const int32_t*)(base + oPairs), P,
           cutoff, (double*)(base + oOut));
   VCUDA(cudaMemcpyAsync(out, base + oOut, (size_t)P * 8, cudaMemcpyDeviceToHost, st));
-  VCUDA(cudaStreamSynchronize(st));
+  VCUDA(stream_wait(ctx));
   return VISACD_OK;
 }

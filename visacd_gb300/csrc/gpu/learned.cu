@@ -949,7 +949,7 @@ extern "C" int visacd_lp_destroy(visacd_lp* lp) {
 extern "C" int visacd_lp_get_params(visacd_lp* lp, float* out) {
   VCHECK(lp && out, VISACD_ERR_INVALID_ARG, "lp_get_params: null argument");
   VCUDA(cudaMemcpyAsync(out, lp->params.p, (size_t)kOff.total * 4, cudaMemcpyDeviceToHost, lp->ctx->stream));
-  VCUDA(cudaStreamSynchronize(lp->ctx->stream));
+  VCUDA(vgpu::stream_wait(lp->ctx));
   return VISACD_OK;
 }
 
@@ -978,7 +978,7 @@ extern "C" int visacd_lp_forward(visacd_lp* lp, const float* feats, int32_t B, f
           P<float>(lp->z6), B, P<float>(lp->planes));
   VCUDA(cudaMemcpyAsync(planes_out, lp->planes.p, (size_t)B * kPlanes * 16, cudaMemcpyDeviceToHost,
                         ctx->stream));
-  VCUDA(cudaStreamSynchronize(ctx->stream));
+  VCUDA(vgpu::stream_wait(ctx));
   return VISACD_OK;
 }
 
@@ -1021,7 +1021,7 @@ extern "C" int visacd_lp_grads(visacd_lp* lp, const float* feats, const float* l
   if (grads_out)
     VCUDA(cudaMemcpyAsync(grads_out, lp->grads.p, (size_t)kOff.total * 4, cudaMemcpyDeviceToHost,
                           ctx->stream));
-  VCUDA(cudaStreamSynchronize(ctx->stream));
+  VCUDA(vgpu::stream_wait(ctx));
   if (loss_out) {
     double s = 0;
     for (float v : loss) s += v;

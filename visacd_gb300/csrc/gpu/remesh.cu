@@ -673,7 +673,7 @@ extern "C" int visacd_sdf_remesh(visacd_ctx* ctx, const double* verts, int32_t n
   const unsigned gq = grid_for((int64_t)nint, 256, 16 * (int64_t)ctx->sm_count);
   uint64_t totals[2];
   VCUDA(cudaMemcpyAsync(&totals[0], coff + ncell, 8, cudaMemcpyDeviceToHost, st));
-  VCUDA(cudaStreamSynchronize(st));
+  VCUDA(stream_wait(ctx));
   VCHECK(totals[0] < (1ull << 31), VISACD_ERR_CAPACITY, "sdf_remesh: too many vertices");
   VTRY(ensure_slot(ctx, kSlotSdfOut, align256(totals[0] * 24) + 256));
   double* out_v = slot<double>(ctx, kSlotSdfOut);
@@ -682,7 +682,7 @@ extern "C" int visacd_sdf_remesh(visacd_ctx* ctx, const double* verts, int32_t n
           (int32_t*)nullptr);
   VTRY(exclusive_scan_u32_to_u64(ctx, qcnt, qoff, (int64_t)nint));
   VCUDA(cudaMemcpyAsync(&totals[1], qoff + nint, 8, cudaMemcpyDeviceToHost, st));
-  VCUDA(cudaStreamSynchronize(st));
+  VCUDA(stream_wait(ctx));
   VCHECK(totals[1] < (1ull << 31), VISACD_ERR_CAPACITY, "sdf_remesh: too many triangles");
   VTRY(ensure_slot(ctx, kSlotSdfTris, align256(totals[1] * 12) + 256));
   VLAUNCH(ctx, kKSdf, gq, 256, 0, sdf_quad_kernel, g, f, cv, qcnt, qoff, slot<int32_t>(ctx, kSlotSdfTris));
@@ -706,6 +706,6 @@ extern "C" int visacd_sdf_fetch(visacd_ctx* ctx, double* verts, int32_t* tris) {
     VCUDA(cudaMemcpyAsync(tris, slot<int32_t>(ctx, kSlotSdfTris), (size_t)ctx->sdf_nt * 12, cudaMemcpyDeviceToHost,
                           ctx->stream));
   }
-  VCUDA(cudaStreamSynchronize(ctx->stream));
+  VCUDA(stream_wait(ctx));
   return VISACD_OK;
 }

@@ -357,7 +357,7 @@ int score_planes_impl(visacd_ctx* ctx, const float* planes, int32_t P, const flo
     ScoreCounters* h = nullptr;
     VTRY(pinned(ctx, sizeof(ScoreCounters), (void**)&h));
     VCUDA(cudaMemcpyAsync(h, cnt, sizeof(ScoreCounters), cudaMemcpyDeviceToHost, ctx->stream));
-    VCUDA(cudaStreamSynchronize(ctx->stream));
+    VCUDA(stream_wait(ctx));
     ScoreCounters hc = *h;
     if (hc.recheck_count > rcap) {
       // The FP64 queue overflowed: rerun with room for every queued block.
@@ -365,13 +365,13 @@ int score_planes_impl(visacd_ctx* ctx, const float* planes, int32_t P, const flo
       rcap = hc.recheck_count;
       VTRY(score_device(ctx, d_planes, P, d_pts, N, d_edges, E, d_scores, d_scores_f32, &cnt, rcap));
       VCUDA(cudaMemcpyAsync(h, cnt, sizeof(ScoreCounters), cudaMemcpyDeviceToHost, ctx->stream));
-      VCUDA(cudaStreamSynchronize(ctx->stream));
+      VCUDA(stream_wait(ctx));
       hc = *h;
     }
     VTRY(check_status(ctx, "score_planes"));
     if (!device_ptrs && P) {
       VCUDA(cudaMemcpyAsync(scores, d_scores, (size_t)P * 8, cudaMemcpyDeviceToHost, ctx->stream));
-      VCUDA(cudaStreamSynchronize(ctx->stream));
+      VCUDA(stream_wait(ctx));
     }
     if (stats) {
       stats->quantum_exp = hc.argmax[1];

@@ -59,7 +59,7 @@ extern "C" int visacd_segment_triangle_tests(visacd_ctx* ctx, const float* seg, 
   unsigned long long cnt = 0;
   VCUDA(cudaMemcpyAsync(hit_out, B + o_out, (size_t)S, cudaMemcpyDeviceToHost, st));
   VCUDA(cudaMemcpyAsync(&cnt, B + o_cnt, 8, cudaMemcpyDeviceToHost, st));
-  VCUDA(cudaStreamSynchronize(st));
+  VCUDA(stream_wait(ctx));
   if (n_fp64) *n_fp64 = (int64_t)cnt;
   return VISACD_OK;
 }

@@ -362,7 +362,7 @@ int vis_morton_order(visacd_ctx* ctx, const float* d_pts, int32_t n, uint32_t* p
   VLAUNCH(ctx, kKVisPrep, gp, 256, 0, point_morton_kernel, d_pts, n, cnt, morton_bits(n), keys, perm);
   VTRY(radix_sort_u64(ctx, keys, perm, slot<uint64_t>(ctx, kSlotVisKeysAlt),
                       slot<uint32_t>(ctx, kSlotVisPermAlt), n, 3 * morton_bits(n)));
-  VCUDA(cudaStreamSynchronize(ctx->stream));
+  VCUDA(stream_wait(ctx));
   return VISACD_OK;
 }
 
@@ -427,7 +427,7 @@ static int vis_device(visacd_ctx* ctx, const float* d_pts, int32_t n, const uint
     uint64_t* hn = nullptr;
     VTRY(pinned(ctx, 8, (void**)&hn));
     VCUDA(cudaMemcpyAsync(hn, off + n, 8, cudaMemcpyDeviceToHost, ctx->stream));
-    VCUDA(cudaStreamSynchronize(ctx->stream));
+    VCUDA(stream_wait(ctx));
     P.rows = rows;
     P.nr = (int32_t)*hn;
     P.triangular = 0;
@@ -449,7 +449,7 @@ static int vis_device(visacd_ctx* ctx, const float* d_pts, int32_t n, const uint
     uint64_t* ht = nullptr;
     VTRY(pinned(ctx, 8, (void**)&ht));
     VCUDA(cudaMemcpyAsync(ht, rs + P.ntr, 8, cudaMemcpyDeviceToHost, ctx->stream));
-    VCUDA(cudaStreamSynchronize(ctx->stream));
+    VCUDA(stream_wait(ctx));
     P.row_start = reinterpret_cast<const unsigned long long*>(rs);
     P.total_tiles = (unsigned long long)*ht;
   }
@@ -474,7 +474,7 @@ static int vis_device(visacd_ctx* ctx, const float* d_pts, int32_t n, const uint
   VLAUNCH(ctx, kKBitPopc, gw, 256, 0, bit_popc_kernel, P.bitset, nw, wc);
   VTRY(exclusive_scan_u32_to_u64(ctx, wc, wo, nw));
   VCUDA(cudaMemcpyAsync(h, cnt, sizeof(VisCounters), cudaMemcpyDeviceToHost, ctx->stream));
-  VCUDA(cudaStreamSynchronize(ctx->stream));
+  VCUDA(stream_wait(ctx));
   VTRY(check_status(ctx, "visibility"));
   const int64_t ne = (int64_t)h->edges;
   VTRY(ensure_slot(ctx, kSlotEdgesOut, (size_t)(ne > 0 ? ne : 1) * 8));
@@ -551,7 +551,7 @@ extern "C" int visacd_visibility_edges(visacd_ctx* ctx, uint32_t* edges_out,
   VCHECK(edges_out, VISACD_ERR_INVALID_ARG, "visibility_edges: edges_out is NULL");
   VCUDA(cudaMemcpyAsync(edges_out, ctx->buf[kSlotEdgesOut].p, (size_t)ctx->last_n_edges * 8,
                         cudaMemcpyDeviceToHost, ctx->stream));
-  VCUDA(cudaStreamSynchronize(ctx->stream));
+  VCUDA(stream_wait(ctx));
   return VISACD_OK;
 }
 

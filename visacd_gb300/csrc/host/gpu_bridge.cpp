@@ -44,9 +44,10 @@ thread_local visacd_ctx* tl_lp_ctx = nullptr;
 thread_local std::string tl_lp_path;             // the weights file it was made from
 }  // namespace
 
-ThreadContext::ThreadContext(int device) {
+ThreadContext::ThreadContext(int device, bool blocking_wait) {
   if (visacd_ctx_create(device, nullptr, &ctx_) != VISACD_OK)
     throw std::runtime_error(std::string("cannot create a worker GPU context: ") + visacd_last_error());
+  if (blocking_wait) visacd_ctx_set_blocking_wait(ctx_, 1);
   prev_ = tl_ctx;
   tl_ctx = ctx_;
 }

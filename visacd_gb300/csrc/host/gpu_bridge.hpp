@@ -21,7 +21,9 @@ int default_device();
 // context() on the creating thread; process_batch workers hold one each.
 class ThreadContext {
  public:
-  explicit ThreadContext(int device);
+  // blocking_wait: the context's waits sleep instead of spinning (many
+  // workers sharing the host cores).
+  explicit ThreadContext(int device, bool blocking_wait = false);
   ~ThreadContext();
   ThreadContext(const ThreadContext&) = delete;
   ThreadContext& operator=(const ThreadContext&) = delete;

@@ -434,7 +434,7 @@ std::vector<ProcessResult> process_batch(const MeshList& meshes, double concavit
   std::vector<ConcavityTimes> ctimes(threads);
   auto worker = [&](int w) {
     try {
-      gpu::ThreadContext tctx(gpu::default_device());
+      gpu::ThreadContext tctx(gpu::default_device(), threads > 1);
       tl_quiet = true;
 #ifdef _OPENMP
       omp_set_num_threads(1);  // the batch is the parallelism; no nested teams
