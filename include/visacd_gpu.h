@@ -146,7 +146,8 @@ int visacd_visibility_edges_device(visacd_ctx* ctx, const uint32_t** d_edges, in
 
 /* Launch shapes of the visibility kernel (tile rows x columns per warp and the
    resident-CTA target). variant -1 restores automatic choice: the autotuned
-   shape for the call's shape class if one was measured, else variant 0. */
+   shape for the call's shape class if one was measured, else variant 1 (8 x 4
+   tiles, 8 resident CTAs per SM). */
 int visacd_vis_variant_count(void);
 int visacd_ctx_set_vis_variant(visacd_ctx* ctx, int variant);
 /* Autotuner: times every launch shape on this exact call (twice each, CUDA

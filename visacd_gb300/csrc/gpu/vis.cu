@@ -308,6 +308,9 @@ struct VisVariant {
 };
 static const VisVariant kVisVariants[] = {{8, 6}, {8, 8}, {4, 6}, {16, 6}, {2, 6}, {1, 6}, {32, 6}};
 constexpr int kNumVisVariants = sizeof(kVisVariants) / sizeof(kVisVariants[0]);
+// Untuned calls: 8 x 4 tiles at 8 resident CTAs per SM, the autotuner's pick
+// on the s5 blob and the fastest on clipped parts (masked) by 3-6 %.
+constexpr int kDefaultVisVariant = 1;
 
 static int launch_vis_variant(visacd_ctx* ctx, int v, const VisParams& P) {
   const unsigned grid = (unsigned)(ctx->sm_count * kVisVariants[v].minb);
@@ -337,7 +340,7 @@ static int choose_vis_variant(visacd_ctx* ctx, int32_t n, bool masked, const vis
     return ctx->vis_variant_override;
   auto it = ctx->vis_tuned.find(vis_shape_class(n, masked, a, b));
   if (it != ctx->vis_tuned.end()) return it->second;
-  return 0;
+  return kDefaultVisVariant;
 }
 
 // Morton order of n device points into perm (sorted position -> vertex).
