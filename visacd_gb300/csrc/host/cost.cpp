@@ -6,7 +6,9 @@
 // sampling of lib/src/core.cpp:144-232 (area-weighted triangle choice by
 // std::discrete_distribution, two std::uniform_real_distribution draws per
 // sample, one extra sample per untouched triangle, all from the process-wide
-// std::mt19937 in the reference's order). The nearest-sample search is this
+// engine, the std::mt19937 sequence, in the reference's order; the draws are
+// made in bulk with the same values, see extract_point_set). The host
+// nearest-sample search is this
 // project's kd-tree (the reference uses nanoflann); distances to the sampled
 // triangles use the exact closest-point test.
 #include <algorithm>

@@ -56,7 +56,7 @@ ProcessResult process(Mesh mesh, double concavity, int num_parts);
 // Many meshes decomposed concurrently (no counterpart in the reference, whose
 // process() takes one mesh): `threads` workers (0 = all hardware threads), each
 // with its own GPU context and stream, pull meshes from a shared counter. Mesh i
-// runs with its own std::mt19937 seeded with seeds[i], so its result equals
+// runs with its own engine (the std::mt19937 sequence) seeded with seeds[i], so its result equals
 // set_seed(seeds[i]); process(meshes[i], concavity, num_parts) whatever the
 // thread count or order. Worker threads do not log.
 std::vector<ProcessResult> process_batch(const MeshList& meshes, double concavity, int num_parts,
