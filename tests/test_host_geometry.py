@@ -241,3 +241,26 @@ def test_refine_proposals_selects_nearest_bisectors(V):
         order = np.lexsort((np.arange(len(d)), d))
         keep[order[:32]] = True
     np.testing.assert_allclose(got, bis[keep], rtol=0, atol=1e-15)
+
+
+def test_mesh_zero_copy_views(V):
+    """Mesh.vertex_array() / triangle_array(): numpy views of the mesh's own
+    storage (no copy), keeping the mesh alive, also through a MeshList."""
+    import gc
+    v, t = mg.displaced_blob(2, seed=3)
+    m = V.Mesh()
+    m.vertices = V.VecArray3d(v.tolist())
+    m.triangles = V.make_vecarray3i(t.astype(np.int32))
+    a, b = m.vertex_array(), m.triangle_array()
+    assert not a.flags["OWNDATA"] and not b.flags["OWNDATA"]
+    np.testing.assert_array_equal(a, v)
+    np.testing.assert_array_equal(b, t)
+    a[0, 0] = 42.0
+    assert m.vertices[0][0] == 42.0
+    ml = V.MeshList([m])
+    del m
+    gc.collect()
+    c = ml[0].vertex_array()
+    del ml
+    gc.collect()
+    assert c[0, 0] == 42.0 and c.shape == v.shape

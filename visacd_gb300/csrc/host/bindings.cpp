@@ -75,7 +75,23 @@ PYBIND11_MODULE(visacd, m) {
   py::class_<Mesh>(m, "Mesh")
       .def(py::init<>())
       .def_readwrite("vertices", &Mesh::vertices)
-      .def_readwrite("triangles", &Mesh::triangles);
+      .def_readwrite("triangles", &Mesh::triangles)
+      // Additions: zero-copy numpy views of the mesh's own storage (N x 3
+      // float64 / int32). A view keeps the mesh alive and stays valid until
+      // the mesh's vertices / triangles are reassigned or resized.
+      .def("vertex_array",
+           [](py::object self) {
+             Mesh& mm = self.cast<Mesh&>();
+             return py::array_t<double>({(py::ssize_t)mm.vertices.size(), (py::ssize_t)3},
+                                        {(py::ssize_t)sizeof(Vec3), (py::ssize_t)sizeof(double)},
+                                        reinterpret_cast<const double*>(mm.vertices.data()), self);
+           })
+      .def("triangle_array", [](py::object self) {
+        Mesh& mm = self.cast<Mesh&>();
+        return py::array_t<int>({(py::ssize_t)mm.triangles.size(), (py::ssize_t)3},
+                                {(py::ssize_t)sizeof(Tri), (py::ssize_t)sizeof(int)},
+                                reinterpret_cast<const int*>(mm.triangles.data()), self);
+      });
 
   py::bind_vector<MeshList>(m, "MeshList");
 
