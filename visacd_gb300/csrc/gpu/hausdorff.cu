@@ -28,6 +28,7 @@
 namespace vgpu {
 
 constexpr int kKnn = 10;
+constexpr int kBoundRings = 2;  // rings of cells searched for each query's upper bound
 
 struct HGrid {
   double lo[3];
@@ -276,8 +277,10 @@ __device__ __forceinline__ float warp_take_min(const float (&fd)[kKnnF], const i
 // the nearest sample found bounds the term by a value `prune` accepts (a
 // bound that cannot change the result).
 constexpr int kTermOk = 0, kTermUnproven = 1, kTermSkipped = 2;
+// r0: the first ring to walk; the rings inside it are known to hold no sample
+// of G (a query without a bound found none within kBoundRings rings).
 template <class Prune>
-__device__ int query_term_warp(const HSide& S, int qi, const Prune& prune, double& term) {
+__device__ int query_term_warp(const HSide& S, int qi, int r0, const Prune& prune, double& term) {
   const int lane = threadIdx.x & 31;
   const HGrid& G = S.G;
   const double q[3] = {S.Q[3 * (int64_t)qi], S.Q[3 * (int64_t)qi + 1], S.Q[3 * (int64_t)qi + 2]};
@@ -292,7 +295,7 @@ __device__ int query_term_warp(const HSide& S, int qi, const Prune& prune, doubl
   int nf = 0;
   int total = 0;  // candidates seen by the warp
   float g10 = 3.4e38f;
-  for (int r = 0; r <= rmax; ++r) {
+  for (int r = r0; r <= rmax; ++r) {
     const int side = 2 * r + 1;
     const int cube = side * side * side;
     int seen = 0;
@@ -563,7 +566,6 @@ __global__ void hfinish_kernel(HBatch H, long long nsamp, int ncells, const unsi
 // sample, itself at most this). A query with no sample that close gets no
 // bound (+inf) and is appended to farlist (*far entries): those are evaluated
 // one warp each. qref[e] = (set, local query index).
-constexpr int kBoundRings = 2;
 __global__ void __launch_bounds__(128) hbound_kernel(HBatch H, long long nsamp, const int* __restrict__ order,
                                                      float* __restrict__ ubs, int2* __restrict__ qref,
                                                      unsigned* __restrict__ far, long long* __restrict__ farlist) {
@@ -627,7 +629,8 @@ __global__ void __launch_bounds__(128) hhead_kernel(HBatch H, const int2* __rest
     const int job = r.x >> 1;
     const HSide& S = H.sides[r.x];
     double term;
-    const int status = query_term_warp(S, r.y, [&](double ub) { return prunable(H, job, ub); }, term);
+    const int status =
+        query_term_warp(S, r.y, kBoundRings + 1, [&](double ub) { return prunable(H, job, ub); }, term);
     if (status == kTermSkipped) continue;
     if (status == kTermUnproven) term = query_term(S, r.y, H.tmargin[job]);
     if ((threadIdx.x & 31) == 0 && term < DBL_MAX) publish(H, job, term);
