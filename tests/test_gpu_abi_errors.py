@@ -63,3 +63,23 @@ def test_learned_mode_without_weights_fails_loudly(native):
             V.process(m, 0.01, 4)
         finally:
             V.config.plane_proposer = old_mode
+
+
+def test_face_hausdorff_batch_bad_indices(native, ctx):
+    v = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], float)
+    t = np.array([[0, 1, 2]], np.int32)
+    x = v.copy()
+    ok = (v, t, x, np.zeros(3, np.int32), v, t, x, np.zeros(3, np.int32))
+    assert len(ctx.face_hausdorff_batch([ok])) == 1
+    with pytest.raises(native.VisacdError):
+        ctx.face_hausdorff_batch([(v, t, x, np.array([0, 1, 0], np.int32), v, t, x, np.zeros(3, np.int32))])
+    with pytest.raises(native.VisacdError):
+        ctx.face_hausdorff_batch([(v, np.array([[0, 1, 3]], np.int32), x, np.zeros(3, np.int32), v, t, x,
+                                   np.zeros(3, np.int32))])
+    assert len(ctx.face_hausdorff_batch([])) == 0
+
+
+def test_clip_bad_triangle_index(native, ctx):
+    v = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], float)
+    with pytest.raises(native.VisacdError):
+        ctx.clip(v, np.array([[0, 1, -1]], np.int32), [1.0, 0.0, 0.0, -0.5])

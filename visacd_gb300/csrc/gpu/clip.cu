@@ -564,8 +564,7 @@ extern "C" int visacd_clip(visacd_ctx* ctx, const double* verts, int32_t nv, con
          "visacd_clip: bad mesh");
   memset(res, 0, sizeof(*res));
   if (nt == 0 || nv == 0) return VISACD_OK;
-  for (int64_t i = 0; i < 3LL * nt; ++i)
-    VCHECK(tris[i] >= 0 && tris[i] < nv, VISACD_ERR_INVALID_ARG, "visacd_clip: triangle index out of range");
+  VCHECK(indices_in_range(tris, 3LL * nt, nv), VISACD_ERR_INVALID_ARG, "visacd_clip: triangle index out of range");
   VCUDA(cudaSetDevice(ctx->device));
   // Border points are bounded by the touching triangles (3 each).
   const int max_border = 3 * nt + 16;

@@ -2,6 +2,7 @@
 // grow-only device buffers and per-kernel CUDA-event timing.
 #pragma once
 
+#include <cstdint>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -235,6 +236,17 @@ inline T* slot(visacd_ctx* ctx, int s) {
   return reinterpret_cast<T*>(ctx->buf[s].p);
 }
 inline int ensure_slot(visacd_ctx* ctx, int s, size_t bytes) { return ensure(ctx->buf[s], bytes); }
+
+// True when every p[0..n) lies in [0, bound) (host side, branch-free so the
+// argument checks of the entry points stay cheap on large inputs).
+inline bool indices_in_range(const int32_t* p, int64_t n, int64_t bound) {
+  if (n <= 0) return true;
+  if (bound <= 0) return false;
+  const uint32_t b = bound > INT32_MAX ? 0xffffffffu : (uint32_t)bound;
+  uint32_t bad = 0;
+  for (int64_t k = 0; k < n; ++k) bad |= (uint32_t)((uint32_t)p[k] >= b);
+  return bad == 0;
+}
 
 // Wait for the context's stream. By default the host thread spins (lowest
 // latency for one caller); with blocking_wait it sleeps on a blocking-sync

@@ -697,18 +697,16 @@ extern "C" int visacd_face_hausdorff_batch(visacd_ctx* ctx, int32_t njobs, const
   const int S = 2 * njobs;
   VCHECK(vert_off[0] == 0 && tri_off[0] == 0 && sample_off[0] == 0, VISACD_ERR_INVALID_ARG,
          "face_hausdorff_batch: offsets must start at 0");
+  VCHECK(verts && tris && samples && sample_tri, VISACD_ERR_INVALID_ARG, "face_hausdorff_batch: null array");
   for (int s = 0; s < S; ++s) {
     const int64_t nv = vert_off[s + 1] - vert_off[s], nt = tri_off[s + 1] - tri_off[s],
                   ns = sample_off[s + 1] - sample_off[s];
     VCHECK(nv > 0 && nt > 0 && ns > 0, VISACD_ERR_INVALID_ARG, "face_hausdorff_batch: empty surface %d", s);
-    for (int64_t k = 3 * tri_off[s]; k < 3 * tri_off[s + 1]; ++k)
-      VCHECK(tris[k] >= 0 && tris[k] < nv, VISACD_ERR_INVALID_ARG,
-             "face_hausdorff_batch: vertex index out of range");
-    for (int64_t k = sample_off[s]; k < sample_off[s + 1]; ++k)
-      VCHECK(sample_tri[k] >= 0 && sample_tri[k] < nt, VISACD_ERR_INVALID_ARG,
-             "face_hausdorff_batch: sample triangle out of range");
+    VCHECK(indices_in_range(tris + 3 * tri_off[s], 3 * nt, nv), VISACD_ERR_INVALID_ARG,
+           "face_hausdorff_batch: vertex index out of range (surface %d)", s);
+    VCHECK(indices_in_range(sample_tri + sample_off[s], ns, nt), VISACD_ERR_INVALID_ARG,
+           "face_hausdorff_batch: sample triangle out of range (surface %d)", s);
   }
-  VCHECK(verts && tris && samples && sample_tri, VISACD_ERR_INVALID_ARG, "face_hausdorff_batch: null array");
   if (lower)
     for (int j = 0; j < njobs; ++j)
       VCHECK(lower[j] == lower[j], VISACD_ERR_INVALID_ARG, "face_hausdorff_batch: lower bound is NaN");

@@ -565,8 +565,7 @@ extern "C" int visacd_sdf_remesh(visacd_ctx* ctx, const double* verts, int32_t n
   ctx->sdf_nv = ctx->sdf_nt = 0;
   *out_nv = *out_nt = 0;
   if (nt == 0 || nv == 0) return VISACD_OK;
-  for (int64_t i = 0; i < 3 * (int64_t)nt; ++i)
-    VCHECK(tris[i] >= 0 && tris[i] < nv, VISACD_ERR_INVALID_ARG, "sdf_remesh: triangle index out of range");
+  VCHECK(indices_in_range(tris, 3LL * nt, nv), VISACD_ERR_INVALID_ARG, "sdf_remesh: triangle index out of range");
   VCUDA(cudaSetDevice(ctx->device));
   // Grid (host arithmetic of manifold_preprocess).
   std::vector<double> P(3 * (size_t)nv);
