@@ -33,3 +33,32 @@ def test_abi_version_and_error_string_without_gpu():
     lib = _native.lib()
     assert lib.visacd_abi_version() == 1
     assert isinstance(lib.visacd_last_error(), bytes)
+
+
+def test_header_is_plain_c_and_links(tmp_path):
+    """include/visacd_gpu.h compiles as C99 (no C++ or torch types in the
+    signatures) and a C program links against the library by those names."""
+    import shutil
+    import subprocess
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        import pytest
+        pytest.skip("gcc not found")
+    lib_path = build.build_gpu()
+    src = tmp_path / "abi_check.c"
+    src.write_text(
+        '#include "visacd_gpu.h"\n'
+        "#include <stdio.h>\n"
+        "int main(void) {\n"
+        "  visacd_vis_stats st;\n"
+        "  (void)st;\n"
+        '  printf("%d %d\\n", visacd_abi_version(), visacd_vis_variant_count());\n'
+        "  return visacd_abi_version() == 1 ? 0 : 1;\n"
+        "}\n")
+    exe = tmp_path / "abi_check"
+    r = subprocess.run([gcc, "-std=c99", "-Wall", "-Werror", f"-I{ROOT / 'include'}", str(src), "-o", str(exe),
+                        str(lib_path), f"-Wl,-rpath,{lib_path.parent}"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, out.stderr
+    assert out.stdout.split()[0] == "1"
