@@ -846,11 +846,14 @@ def main():
         out, rank = run_reference(args)
     else:
         out, rank = run_ours(args)
-        if rank == 0 and out is not None and not args.no_cpu_baseline and out["n_gpus"] >= 1:
+        # The CPU baseline and the single-GPU decomposition workloads run on
+        # rank 0 at N = 1 only (replica runs report the visibility step alone).
+        single = out is not None and out["n_gpus"] == 1
+        if rank == 0 and single and not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline_sample()
-        if rank == 0 and out is not None and not args.no_process:
+        if rank == 0 and single and not args.no_process:
             out["process"] = run_decompositions(args)
-        if rank == 0 and out is not None and not args.no_c5:
+        if rank == 0 and single and not args.no_c5:
             out["decomps"] = run_learned_batch(args)
     if rank == 0 and out is not None:
         print(json.dumps(out))
