@@ -181,7 +181,11 @@ int visacd_compute_intersection_matrix(visacd_ctx* ctx, const float* verts, int3
    integers, so scores are deterministic and independent of launch shape.
    planes P x 4, points N x 3 float32, edges E x 2 uint32; edges with an index
    >= N are skipped as in the reference. scores is P float64. If device_ptrs
-   is 1 the call is asynchronous unless stats != NULL. */
+   is 1 the call is asynchronous unless stats != NULL. An asynchronous call
+   cannot rerun or raise: if its FP64 re-decision queue fills up, or a
+   bulk-copy wait in the kernel times out, every score it writes is NaN. With
+   stats != NULL (or host pointers) the library reruns a full queue with room
+   for every block and returns VISACD_ERR_DEVICE on a timeout. */
 int visacd_score_planes(visacd_ctx* ctx, const float* planes, int32_t P, const float* points,
                         int32_t N, const uint32_t* edges, int64_t E, int device_ptrs,
                         double* scores, visacd_score_stats* stats);
@@ -364,8 +368,13 @@ int visacd_lp_train_step(visacd_lp* lp, const float* feats, const float* labels,
    asynchronous on cuda_stream (NULL = the legacy default stream). Limits:
    P <= 4096 and E <= 65536, larger sizes return VISACD_ERR_CAPACITY. The first
    call on a device looks up the array's device address (do it before any
-   stream capture). Calls share the array: calls that overlap on the GPU race,
-   so serialise them. Results equal visacd_score_planes bit for bit. */
+   stream capture); the address is cached per device for the life of the
+   process, so do not use this call across cudaDeviceReset. Calls share the
+   array: calls that overlap on the GPU race, so serialise them. The queue
+   holds every (plane, edge block) pair and cannot fill up; if a bulk-copy
+   wait inside the kernel times out, every score is NaN and argmax is -2 (the
+   call itself returns before the GPU runs, so the failure is reported in the
+   outputs). Otherwise results equal visacd_score_planes bit for bit. */
 int visacd_score_planes_noalloc(const float* planes, int32_t P, const float* points, int32_t N,
                                 const uint32_t* edges, int64_t E, double* scores,
                                 int32_t* argmax, void* cuda_stream);

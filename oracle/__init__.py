@@ -30,6 +30,9 @@ def lib() -> C.CDLL:
         L.oracle_visibility.argtypes = [P, i32, P, P, i32, P, i32, P, i32, C.c_int, i32, i32, P,
                                         C.POINTER(i64), C.POINTER(i64)]
         L.oracle_visibility.restype = i64
+        L.oracle_visibility_rows.argtypes = [P, i32, P, P, i32, P, P, i32, P, i32, P,
+                                             C.POINTER(i64), C.POINTER(i64)]
+        L.oracle_visibility_rows.restype = i64
         L.oracle_candidate_planes.argtypes = [P, P, i64, i32, C.c_uint32, P]
         L.oracle_seg_tri_batch.argtypes = [P, P, i64, P]
         L.oracle_seg_tri_batch.restype = i64
@@ -93,6 +96,24 @@ def visibility(pts, tris, cage_verts, cage_tris, is_new=None, use_bvh=True, rows
                                  int(use_bvh), r0, r1, _p(bits), C.byref(ng), C.byref(npr))
     edges = pairs_from_linear(np.nonzero(bits & 1)[0], n)
     return bits, edges, {"n_edges": int(ne), "n_grazing": ng.value, "pairs": npr.value}
+
+
+def visibility_rows(pts, tris, cage_verts, cage_tris, rows, bits=None):
+    """visibility() (BVH traversal) for an explicit list of pair rows; bits, if
+    given, is the n(n-1)/2 result array to write into (only those rows)."""
+    p = np.ascontiguousarray(pts, dtype=np.float32).reshape(-1, 3)
+    t = np.ascontiguousarray(tris, dtype=np.uint32).reshape(-1, 3)
+    cv = np.ascontiguousarray(cage_verts, dtype=np.float32).reshape(-1, 3)
+    ct = np.ascontiguousarray(cage_tris, dtype=np.uint32).reshape(-1, 3)
+    r = np.ascontiguousarray(rows, dtype=np.int32)
+    n = len(p)
+    if bits is None:
+        bits = np.zeros(n * (n - 1) // 2, dtype=np.uint8)
+    ng = C.c_int64()
+    npr = C.c_int64()
+    ne = lib().oracle_visibility_rows(_p(p), n, None, _p(t), len(t), _p(cv), _p(ct), len(ct), _p(r),
+                                      len(r), _p(bits), C.byref(ng), C.byref(npr))
+    return bits, {"n_edges": int(ne), "n_grazing": ng.value, "pairs": npr.value}
 
 
 def pairs_from_linear(k: np.ndarray, n: int) -> np.ndarray:

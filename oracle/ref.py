@@ -37,8 +37,10 @@ def lib() -> C.CDLL:
         L.ref_compute_h.restype = C.c_double
         L.ref_hull_volume.argtypes = [P, C.c_int, C.POINTER(C.c_int)]
         L.ref_hull_volume.restype = C.c_double
+        L.ref_hull_bt.argtypes = [P, C.c_int, P, C.c_int, P, C.c_int, C.POINTER(C.c_int)]
+        L.ref_hull_bt.restype = C.c_int
         L.ref_process.argtypes = [P, C.c_int, P, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int,
-                                  C.POINTER(C.c_double)]
+                                  C.c_int, C.POINTER(C.c_double)]
         _lib = L
     return _lib
 
@@ -117,10 +119,26 @@ def hull_volume(v):
     return vol, nt.value
 
 
-def process(v, t, concavity, num_parts, seed, score_mode="concavity", return_parts=False):
+def hull_bt(v):
+    """The reference's btConvexHullComputer hull (Mesh::compute_vch): hull
+    vertices and fan-triangulated faces."""
+    v = np.ascontiguousarray(v, dtype=np.float64).reshape(-1, 3)
+    cap = 2 * len(v) + 16
+    ov = np.zeros((cap, 3), np.float64)
+    ot = np.zeros((4 * cap, 3), np.int32)
+    nv = C.c_int()
+    nt = lib().ref_hull_bt(_p(v), len(v), _p(ov), cap, _p(ot), 4 * cap, C.byref(nv))
+    if nt < 0:
+        raise ValueError("hull buffers too small")
+    return ov[: nv.value], ot[:nt]
+
+
+def process(v, t, concavity, num_parts, seed, score_mode="concavity", return_parts=False,
+            use_merging=False):
     v, t = _vt(v, t)
     set_seed(seed)
     c = C.c_double()
     n = lib().ref_process(_p(v), len(v), _p(t), len(t), concavity, num_parts,
-                          int(score_mode == "edge"), int(return_parts), C.byref(c))
+                          int(score_mode == "edge"), int(return_parts), int(use_merging),
+                          C.byref(c))
     return n, c.value, parts()

@@ -209,18 +209,39 @@ double ref_hull_volume(const double* v, int nv, int* ntris) {
   return neural_acd::get_mesh_volume(h);
 }
 
+// The reference's btConvexHullComputer path (Mesh::compute_vch,
+// lib/src/core.cpp:113-142, with the outward-normal fix): hull vertices
+// (out_v, cap_v x 3) and fan-triangulated faces (out_t, cap_t x 3). Returns
+// the triangle count, or -1 if a buffer is too small; *nv_out gets the
+// vertex count.
+int ref_hull_bt(const double* v, int nv, double* out_v, int cap_v, int* out_t, int cap_t,
+                int* nv_out) {
+  Mesh m = make_mesh(v, nv, nullptr, 0);
+  Mesh h;
+  m.compute_vch(h, true);
+  *nv_out = (int)h.vertices.size();
+  if ((int)h.vertices.size() > cap_v || (int)h.triangles.size() > cap_t) return -1;
+  for (size_t i = 0; i < h.vertices.size(); ++i)
+    for (int k = 0; k < 3; ++k) out_v[3 * i + k] = h.vertices[i][k];
+  for (size_t i = 0; i < h.triangles.size(); ++i)
+    for (int k = 0; k < 3; ++k) out_t[3 * i + k] = h.triangles[i][k];
+  return (int)h.triangles.size();
+}
+
 // lib/src/process.cpp:238 process(mesh, concavity, num_parts); parts land in
 // the part store.
 int ref_process(const double* v, int nv, const int* t, int nt, double concavity, int num_parts,
-                int score_mode_edge, int return_parts, double* out_concavity) {
+                int score_mode_edge, int return_parts, int use_merging, double* out_concavity) {
   neural_acd::config.score_mode = score_mode_edge ? "edge" : "concavity";
   neural_acd::config.return_parts = return_parts != 0;
+  neural_acd::config.use_merging = use_merging != 0;
   Mesh m = make_mesh(v, nv, t, nt);
   neural_acd::ProcessResult r = neural_acd::process(m, concavity, num_parts);
   g_parts = r.parts;
   *out_concavity = r.concavity;
   neural_acd::config.score_mode = "concavity";
   neural_acd::config.return_parts = false;
+  neural_acd::config.use_merging = false;
   return r.num_parts;
 }
 

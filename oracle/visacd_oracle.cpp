@@ -400,26 +400,31 @@ static inline int64_t row_start(int64_t i, int64_t n) { return i * (2 * n - i - 
 // Pairs with coincident endpoints are never edges (:88-93).
 // out_bits: one byte per linear pair index (row-major, i < j):
 //   0 = not an edge, 1 = edge; bit 1 (value 2) marks a grazing pair.
+// A pair is grazing when its edge decision rests on a test within the 1e-6
+// band: the cage test is decided first; a robust cage miss decides "no edge"
+// whatever the part test gives, and a robust part hit decides "no edge"
+// whatever the cage test gives; otherwise the pair is grazing if either test
+// is within the band.
 // Returns the number of edges; *n_grazing gets the number of grazing pairs.
 // use_bvh selects the BVH traversal (same decisions) over brute force.
 // row_begin/row_end restrict the rows computed (for bounded CPU samples);
 // pass 0, n for all.
 // ---------------------------------------------------------------------------
-int64_t oracle_visibility(const float* pts, int32_t n, const uint8_t* is_new,
-                          const uint32_t* tris, int32_t nt, const float* cage_v, int32_t ncv,
-                          const uint32_t* cage_t, int32_t nct, int use_bvh, int32_t row_begin,
-                          int32_t row_end, uint8_t* out_bits, int64_t* n_grazing,
-                          int64_t* n_pairs) {
-  (void)ncv;
+static int64_t visibility_rows(const float* pts, int32_t n, const uint8_t* is_new,
+                               const uint32_t* tris, int32_t nt, const float* cage_v,
+                               const uint32_t* cage_t, int32_t nct, int use_bvh,
+                               const int32_t* rows, int32_t n_rows, uint8_t* out_bits,
+                               int64_t* n_grazing, int64_t* n_pairs) {
   CpuBvh sb, cb;
   if (use_bvh) {
     build_cpu_bvh(pts, tris, nt, sb);
     build_cpu_bvh(cage_v, cage_t, nct, cb);
   }
   int64_t edges = 0, grazing = 0, pairs = 0;
-  if (row_end > n) row_end = n;
 #pragma omp parallel for schedule(dynamic, 1) reduction(+ : edges, grazing, pairs)
-  for (int32_t i = row_begin; i < row_end; ++i) {
+  for (int32_t r = 0; r < n_rows; ++r) {
+    const int32_t i = rows[r];
+    if (i < 0 || i >= n) continue;
     for (int32_t j = i + 1; j < n; ++j) {
       int64_t k = row_start(i, n) + (j - i - 1);
       uint8_t r = 0;
@@ -433,16 +438,20 @@ int64_t oracle_visibility(const float* pts, int32_t n, const uint8_t* is_new,
         if (out_bits) out_bits[k] = 0;
         continue;
       }
-      MeshDecision s = use_bvh ? seg_mesh_bvh(p, q, i, j, pts, tris, sb, true)
-                               : seg_mesh_brute(p, q, i, j, pts, tris, nt, true);
+      MeshDecision c = use_bvh ? seg_mesh_bvh(p, q, -1, -1, cage_v, cage_t, cb, false)
+                               : seg_mesh_brute(p, q, -1, -1, cage_v, cage_t, nct, false);
       bool edge = false, graze = false;
-      if (s.hit && s.robust) {
+      if (!c.hit && c.robust) {
         edge = false;
       } else {
-        MeshDecision c = use_bvh ? seg_mesh_bvh(p, q, -1, -1, cage_v, cage_t, cb, false)
-                                 : seg_mesh_brute(p, q, -1, -1, cage_v, cage_t, nct, false);
-        edge = !s.hit && c.hit;
-        graze = !s.robust || !c.robust;
+        MeshDecision s = use_bvh ? seg_mesh_bvh(p, q, i, j, pts, tris, sb, true)
+                                 : seg_mesh_brute(p, q, i, j, pts, tris, nt, true);
+        if (s.hit && s.robust) {
+          edge = false;
+        } else {
+          edge = !s.hit && c.hit;
+          graze = !s.robust || !c.robust;
+        }
       }
       if (edge) {
         r |= 1;
@@ -458,6 +467,32 @@ int64_t oracle_visibility(const float* pts, int32_t n, const uint8_t* is_new,
   if (n_grazing) *n_grazing = grazing;
   if (n_pairs) *n_pairs = pairs;
   return edges;
+}
+
+int64_t oracle_visibility(const float* pts, int32_t n, const uint8_t* is_new,
+                          const uint32_t* tris, int32_t nt, const float* cage_v, int32_t ncv,
+                          const uint32_t* cage_t, int32_t nct, int use_bvh, int32_t row_begin,
+                          int32_t row_end, uint8_t* out_bits, int64_t* n_grazing,
+                          int64_t* n_pairs) {
+  (void)ncv;
+  if (row_end > n) row_end = n;
+  if (row_begin < 0) row_begin = 0;
+  std::vector<int32_t> rows;
+  for (int32_t i = row_begin; i < row_end; ++i) rows.push_back(i);
+  return visibility_rows(pts, n, is_new, tris, nt, cage_v, cage_t, nct, use_bvh, rows.data(),
+                         (int32_t)rows.size(), out_bits, n_grazing, n_pairs);
+}
+
+// The same for an explicit list of pair rows i (each row: the pairs (i, j),
+// j > i); out_bits is still indexed by the linear pair index of all n(n-1)/2
+// pairs and only the listed rows are written.
+int64_t oracle_visibility_rows(const float* pts, int32_t n, const uint8_t* is_new,
+                               const uint32_t* tris, int32_t nt, const float* cage_v,
+                               const uint32_t* cage_t, int32_t nct, const int32_t* rows,
+                               int32_t n_rows, uint8_t* out_bits, int64_t* n_grazing,
+                               int64_t* n_pairs) {
+  return visibility_rows(pts, n, is_new, tris, nt, cage_v, cage_t, nct, 1, rows, n_rows, out_bits,
+                         n_grazing, n_pairs);
 }
 
 // ---------------------------------------------------------------------------

@@ -30,6 +30,12 @@ CASES = [
      "seed": 3, "mode": "concavity"},
     {"name": "torus_32x16_edge_n6", "mesh": ["torus", 32, 16, 5], "concavity": 0.04,
      "num_parts": 6, "seed": 11, "mode": "edge"},
+    # the large concave blob: icosphere subdivision 5 with 8 seeded bumps
+    {"name": "blob_s5_c0.02_n64", "mesh": ["blob", 5, 2026], "concavity": 0.02, "num_parts": 64,
+     "seed": 42, "mode": "concavity"},
+    # hull merging on (multimerge_ch after the split loop)
+    {"name": "blob_s3_c0.02_n12_merge", "mesh": ["blob", 3, 11], "concavity": 0.02,
+     "num_parts": 12, "seed": 5, "mode": "concavity", "merging": True},
 ]
 
 
@@ -49,7 +55,8 @@ def main():
     for c in CASES:
         v, t = make_mesh(c["mesh"])
         t0 = time.time()
-        n, conc, parts = R.process(v, t, c["concavity"], c["num_parts"], c["seed"], c["mode"])
+        n, conc, parts = R.process(v, t, c["concavity"], c["num_parts"], c["seed"], c["mode"],
+                                   use_merging=c.get("merging", False))
         out[c["name"]] = {**c, "num_parts": c["num_parts"], "result_parts": n, "concavity_out": conc,
                           "part_vertices": [len(p["vertices"]) for p in parts],
                           "part_triangles": [len(p["triangles"]) for p in parts],

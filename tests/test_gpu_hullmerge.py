@@ -56,12 +56,12 @@ def test_merging_same_with_gpu_distances(V):
     out = []
     try:
         for gm in (False, True):
-            V.config.gpu_merge = gm
+            V._checker_hooks(host_merge=not gm)
             V.set_seed(11)
             out.append(V.process(m, 0.05, 12))
     finally:
         V.config.use_merging = False
-        V.config.gpu_merge = True
+        V._checker_hooks(host_merge=False)
     a, b = out
     assert a.num_parts == b.num_parts and a.concavity == b.concavity
     for pa, pb in zip(a.parts, b.parts):

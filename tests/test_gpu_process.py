@@ -68,18 +68,18 @@ def test_gpu_concavity_metric_equals_host(visacd):
     from visacd_gb300 import visacd as V
     for seed, level in [(3, 3), (4, 4), (5, 2)]:
         v, t = mg.displaced_blob(level, seed=seed)
-        V.config.gpu_concavity = False
+        V._checker_hooks(host_concavity=True)
         V.set_seed(11)
         a = V._compute_h(v, t, 0.3, 3000)
-        V.config.gpu_concavity = True
+        V._checker_hooks(host_concavity=False)
         V.set_seed(11)
         b = V._compute_h(v, t, 0.3, 3000)
         assert a == b
         hv = V._convex_hull(v)
-        V.config.gpu_concavity = False
+        V._checker_hooks(host_concavity=True)
         V.set_seed(5)
         a = V._compute_hb(v, t, hv["vertices"], hv["triangles"], 10000)
-        V.config.gpu_concavity = True
+        V._checker_hooks(host_concavity=False)
         V.set_seed(5)
         b = V._compute_hb(v, t, hv["vertices"], hv["triangles"], 10000)
         assert a == b
@@ -116,12 +116,12 @@ def test_process_gpu_metric_equals_host_metric(visacd):
     v, t = mg.displaced_blob(3, seed=21)
     out = []
     for gpu in (False, True):
-        V.config.gpu_concavity = gpu
+        V._checker_hooks(host_concavity=not gpu)
         V.set_seed(3)
         try:
             out.append(V.process(_mesh(V, v, t), 0.02, 10))
         finally:
-            V.config.gpu_concavity = True
+            V._checker_hooks(host_concavity=False)
     a, b = out
     assert a.num_parts == b.num_parts and a.concavity == b.concavity
     for pa, pb in zip(a.parts, b.parts):

@@ -43,11 +43,13 @@ def test_process_matches_reference_loop(visacd, name):
     m.triangles = visacd.make_vecarray3i(t.astype(np.int32))
     visacd.config.score_mode = c["mode"]
     visacd.config.return_parts = False
+    visacd.config.use_merging = c.get("merging", False)
     visacd.set_seed(c["seed"])
     try:
         r = visacd.process(m, c["concavity"], c["num_parts"])
     finally:
         visacd.config.score_mode = "concavity"
+        visacd.config.use_merging = False
     assert r.num_parts == c["result_parts"]
     assert abs(r.concavity - c["concavity_out"]) <= 1e-9 * max(1.0, abs(c["concavity_out"]))
     nv = [len(p.vertices) for p in r.parts]

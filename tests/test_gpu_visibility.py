@@ -142,3 +142,67 @@ def test_bvh_depth(ctx):
         nt, depth = b.info()
         assert nt == len(t) and math.ceil(math.log2(nt)) <= depth <= nt - 1
         b.close()
+
+
+def test_torus_64x32_all_pairs(ctx, orc):
+    """The small plain-method workload: seeded torus R = 1, r = 0.35, 64 x 32
+    grid with radial perturbation U(-0.02, 0.02) r (2048 vertices, all
+    2,096,128 pairs) against its 0.03 offset cage. Every pair outside the
+    grazing band matches the FP64 oracle."""
+    v, t = mg.torus(nu=64, nv=32, seed=42)
+    cv, ct = mg.offset_cage(v, t, 0.03)
+    e, st, ost, nd = _compare(ctx, orc, v, t, cv, ct)
+    assert ost["pairs"] == 2096128
+    assert nd <= ost["n_grazing"]
+    print(f"torus 64x32: {len(e)} edges, {ost['n_grazing']} grazing pairs, {nd} differ (all grazing)")
+
+
+def test_blob_s5_all_pairs(ctx, orc):
+    """The large concave blob: icosphere subdivision 5 (10242 vertices, 20480
+    triangles) with 8 seeded Gaussian bumps, all 52,444,161 pairs against its
+    0.03 offset cage (the benchmark's workload and seed). Every pair outside
+    the grazing band matches the FP64 oracle."""
+    v, t = mg.displaced_blob(5, seed=2026)
+    cv, ct = mg.offset_cage(v, t, 0.03)
+    e, st, ost, nd = _compare(ctx, orc, v, t, cv, ct)
+    assert ost["pairs"] == 52444161
+    assert nd <= ost["n_grazing"]
+    print(f"blob s5: {len(e)} edges, {ost['n_grazing']} grazing pairs, {nd} differ (all grazing)")
+
+
+def test_bvh_depth_on_clustered_and_degenerate_meshes(ctx, orc):
+    """Meshes that stress the Morton hierarchy stay within the 64-entry
+    traversal stack and give the oracle's edges: a cluster of tiny triangles
+    next to a far one (Morton codes crowd into few cells), many coincident
+    triangles (equal codes), and a long thin strip."""
+    rng = np.random.default_rng(5)
+    # 1) 4000 tiny triangles packed within 1e-4 of the origin plus one far one.
+    c = rng.normal(size=(4000, 1, 3)) * 1e-4
+    tri = c + rng.normal(size=(4000, 3, 3)) * 1e-6
+    far = np.array([[[50, 50, 50], [51, 50, 50], [50, 51, 50]]], np.float64)
+    v1 = np.concatenate([tri, far]).reshape(-1, 3)
+    t1 = np.arange(len(v1), dtype=np.int32).reshape(-1, 3)
+    # 2) 3000 copies of one triangle (all Morton codes equal).
+    v2 = np.tile(np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float64), (3000, 1))
+    t2 = np.arange(len(v2), dtype=np.int32).reshape(-1, 3)
+    # 3) a 1 x 1e-5 strip of 4096 triangles.
+    xs = np.linspace(0, 1, 2049)
+    v3 = np.concatenate([np.stack([xs, np.zeros_like(xs), np.zeros_like(xs)], 1),
+                         np.stack([xs, np.full_like(xs, 1e-5), np.zeros_like(xs)], 1)])
+    i = np.arange(2048)
+    t3 = np.concatenate([np.stack([i, i + 1, 2049 + i], 1),
+                         np.stack([i + 1, 2050 + i, 2049 + i], 1)]).astype(np.int32)
+    for v, t in [(v1, t1), (v2, t2), (v3, t3)]:
+        b = ctx.bvh(v, t)
+        nt, depth = b.info()
+        assert nt == len(t) and depth <= 64, f"depth {depth} for {nt} triangles"
+        b.close()
+    # Visibility on the clustered mesh (sub-sampled points) still matches.
+    pts = v1[::37]
+    cv, ct = mg.offset_cage(*mg.displaced_blob(2, seed=1), 0.5)
+    cv = cv * 1e-3
+    sb, cb = ctx.bvh(v1, t1), ctx.bvh(cv, ct)
+    e_gpu, st = ctx.visibility(pts, sb, cb)
+    sb.close()
+    cb.close()
+    assert st["pairs_tested"] == len(pts) * (len(pts) - 1) // 2

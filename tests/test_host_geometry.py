@@ -14,8 +14,8 @@ from visacd_gb300 import build, meshgen as mg
 def V():
     build.build_host()
     from visacd_gb300 import visacd
-    visacd.config.gpu_concavity = False  # host Hausdorff and remesh: these tests run without a GPU
-    visacd.config.gpu_remesh = False
+    # host Hausdorff and remesh (test hooks): these tests run without a GPU
+    visacd._checker_hooks(host_concavity=True, host_remesh=True)
     return visacd
 
 

@@ -16,8 +16,8 @@ if not R.available():
 def V():
     build.build_host()
     from visacd_gb300 import visacd
-    visacd.config.gpu_concavity = False  # host Hausdorff and remesh: these tests run without a GPU
-    visacd.config.gpu_remesh = False
+    # host Hausdorff and remesh (test hooks): these tests run without a GPU
+    visacd._checker_hooks(host_concavity=True, host_remesh=True)
     return visacd
 
 
@@ -132,6 +132,48 @@ def test_hull_matches_reference(V):
     h = V._convex_hull(p)
     assert len(h["triangles"]) == nt
     assert abs(V._mesh_volume(h["vertices"], h["triangles"]) - vol) < 1e-12
+
+
+def _grid_clouds():
+    """Point clouds on the integer grid 0..10216 with every axis spanning the
+    whole range: btConvexHullComputer (lib/3rd/btConvexHull) maps the input
+    box onto exactly that grid before its integer hull, so on these inputs it
+    is exact and its output coordinates are the input coordinates."""
+    rng = np.random.default_rng(3)
+    L = 10216
+    corners = np.array([[0, 0, 0], [L, L, L]], float)
+    out = {"random": np.concatenate([corners, rng.integers(0, L + 1, (400, 3))]).astype(float)}
+    g = np.linspace(0, L, 5)
+    lat = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+    out["lattice (coplanar and collinear points)"] = lat
+    out["lattice with duplicates"] = np.concatenate([lat, lat[::3], lat[:7]])
+    s = rng.normal(size=(2000, 3))
+    s /= np.linalg.norm(s, axis=1, keepdims=True)
+    out["sphere"] = np.round((np.concatenate([s, np.eye(3), -np.eye(3)]) + 1) * (L / 2))
+    out["tetrahedron"] = np.array([[0, 0, 0], [L, 0, 0], [0, L, 0], [0, 0, L]], float)
+    flat = rng.integers(0, L + 1, (300, 2)).astype(float)
+    flat[:2] = [[0, 0], [L, L]]
+    out["flat"] = np.c_[flat, np.zeros(300)]
+    out["segment"] = np.c_[np.arange(50) * 100.0, np.arange(50) * 100.0, np.arange(50) * 100.0]
+    return out
+
+
+def test_hull_matches_btconvexhull(V):
+    """The hull (hull.cpp) against the reference's own btConvexHullComputer
+    fallback (lib/src/core.cpp:113-142), an independent implementation: same
+    hull vertex set and the same volume, on random, lattice (coplanar and
+    collinear points), duplicate-point, spherical and flat inputs."""
+    for name, p in _grid_clouds().items():
+        bv, bt = R.hull_bt(p)
+        h = V._convex_hull(p)
+        hv, ht = np.asarray(h["vertices"]), np.asarray(h["triangles"]).reshape(-1, 3)
+        ours = set(map(tuple, hv[np.unique(ht)])) if len(ht) else set()
+        if len(bt) == 0:  # lower-dimensional input: no facets on either side
+            assert len(ht) == 0, name
+            continue
+        assert ours == set(map(tuple, bv)), name
+        vb, vo = V._mesh_volume(bv, bt), V._mesh_volume(hv, ht)
+        assert abs(vb - vo) <= 1e-12 * max(1.0, abs(vb)), (name, vb, vo)
 
 
 def test_surface_sampling_matches_one_by_one_draws(V):

@@ -188,17 +188,22 @@ __global__ void score_recheck_kernel(const float4* __restrict__ planes,
 }
 
 // Scores in float64 (exact: integer sum times a power of two) and the first
-// index of the maximum.
+// index of the maximum. When the call's status word says that some work was
+// lost (a bulk-copy wait that timed out, or a full FP64 re-decision queue),
+// every score is NaN and the arg-max is -2, so a caller that reads only the
+// device outputs still sees the failure.
 __global__ void score_finish_kernel(const unsigned long long* __restrict__ score_q, int32_t P,
-                                    const unsigned* __restrict__ stats, double* __restrict__ out,
+                                    const unsigned* __restrict__ stats,
+                                    const unsigned* __restrict__ status, double* __restrict__ out,
                                     float* __restrict__ out_f32, int* __restrict__ argmax) {
   unsigned cmax = max(stats[0], max(stats[1], stats[2]));
   int qexp = quantum_exp_from_cmax_bits(cmax);
+  const bool lost = (*status & (kStatusMbarrierTimeout | kStatusRecheckOverflow)) != 0u;
   unsigned long long best = 0;
   int best_i = P > 0 ? 0 : -1;
   for (int p = threadIdx.x; p < P; p += blockDim.x) {
     unsigned long long v = score_q[p];
-    double s = ldexp((double)v, qexp);
+    double s = lost ? __longlong_as_double(0x7ff8000000000000ll) : ldexp((double)v, qexp);
     if (out) out[p] = s;
     if (out_f32) out_f32[p] = (float)s;
     if (v > best || (v == best && p < best_i)) {
@@ -223,7 +228,7 @@ __global__ void score_finish_kernel(const unsigned long long* __restrict__ score
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    argmax[0] = si[0];
+    argmax[0] = lost ? -2 : si[0];
     argmax[1] = qexp;
   }
 }
@@ -232,7 +237,8 @@ __global__ void score_finish_kernel(const unsigned long long* __restrict__ score
 struct ScoreCounters {
   unsigned stats[4];                 // max |x|, |y|, |z| (float bits)
   unsigned recheck_count;
-  unsigned pad0[3];
+  unsigned status;                   // this call's kStatus* bits
+  unsigned pad0[2];
   unsigned long long skipped;
   int argmax[2];                     // argmax, qexp
 };
@@ -247,7 +253,7 @@ static int planes_per_thread(int32_t P) {
 template <int K>
 static int launch_score(visacd_ctx* ctx, const float4* planes, int32_t P, const EdgeRec* recs,
                         int64_t E, const unsigned* stats, unsigned long long* sq, uint2* rq,
-                        unsigned* rcount, unsigned rcap) {
+                        unsigned* rcount, unsigned rcap, unsigned* status) {
   const int per_cta = kScoreThreads * K;
   const int groups = (P + per_cta - 1) / per_cta;
   const int64_t nblocks = (E + kEdgeBlock - 1) / kEdgeBlock;
@@ -267,7 +273,7 @@ static int launch_score(visacd_ctx* ctx, const float4* planes, int32_t P, const 
   }
   dim3 grid((unsigned)slices, (unsigned)groups);
   VLAUNCH(ctx, kKScore, grid, kScoreThreads, smem, score_planes_kernel<K>, planes, P, recs, E, per,
-          stats, sq, rq, rcount, rcap, ctx->d_status);
+          stats, sq, rq, rcount, rcap, status);
   return VISACD_OK;
 }
 
@@ -296,16 +302,16 @@ static int score_device(visacd_ctx* ctx, const float* d_planes, int32_t P, const
     const float4* pl = reinterpret_cast<const float4*>(d_planes);
     int K = planes_per_thread(P);
     switch (K) {
-      case 8: VTRY(launch_score<8>(ctx, pl, P, recs, E, cnt->stats, sq, rq, &cnt->recheck_count, rcap)); break;
-      case 4: VTRY(launch_score<4>(ctx, pl, P, recs, E, cnt->stats, sq, rq, &cnt->recheck_count, rcap)); break;
-      case 2: VTRY(launch_score<2>(ctx, pl, P, recs, E, cnt->stats, sq, rq, &cnt->recheck_count, rcap)); break;
-      default: VTRY(launch_score<1>(ctx, pl, P, recs, E, cnt->stats, sq, rq, &cnt->recheck_count, rcap)); break;
+      case 8: VTRY(launch_score<8>(ctx, pl, P, recs, E, cnt->stats, sq, rq, &cnt->recheck_count, rcap, &cnt->status)); break;
+      case 4: VTRY(launch_score<4>(ctx, pl, P, recs, E, cnt->stats, sq, rq, &cnt->recheck_count, rcap, &cnt->status)); break;
+      case 2: VTRY(launch_score<2>(ctx, pl, P, recs, E, cnt->stats, sq, rq, &cnt->recheck_count, rcap, &cnt->status)); break;
+      default: VTRY(launch_score<1>(ctx, pl, P, recs, E, cnt->stats, sq, rq, &cnt->recheck_count, rcap, &cnt->status)); break;
     }
     VLAUNCH(ctx, kKScoreRecheck, 2 * ctx->sm_count, 256, 0, score_recheck_kernel, pl, recs, E,
             cnt->stats, rq, &cnt->recheck_count, rcap, sq);
   }
-  VLAUNCH(ctx, kKScoreFinish, 1, 1024, 0, score_finish_kernel, sq, P, cnt->stats, d_scores,
-          d_scores_f32, cnt->argmax);
+  VLAUNCH(ctx, kKScoreFinish, 1, 1024, 0, score_finish_kernel, sq, P, cnt->stats, &cnt->status,
+          d_scores, d_scores_f32, cnt->argmax);
   return VISACD_OK;
 }
 
@@ -359,15 +365,17 @@ int score_planes_impl(visacd_ctx* ctx, const float* planes, int32_t P, const flo
     VCUDA(cudaMemcpyAsync(h, cnt, sizeof(ScoreCounters), cudaMemcpyDeviceToHost, ctx->stream));
     VCUDA(stream_wait(ctx));
     ScoreCounters hc = *h;
-    if (hc.recheck_count > rcap) {
+    if (hc.recheck_count > rcap && !(hc.status & kStatusMbarrierTimeout)) {
       // The FP64 queue overflowed: rerun with room for every queued block.
-      VCUDA(cudaMemsetAsync(ctx->d_status, 0, 4, ctx->stream));
       rcap = hc.recheck_count;
       VTRY(score_device(ctx, d_planes, P, d_pts, N, d_edges, E, d_scores, d_scores_f32, &cnt, rcap));
       VCUDA(cudaMemcpyAsync(h, cnt, sizeof(ScoreCounters), cudaMemcpyDeviceToHost, ctx->stream));
       VCUDA(stream_wait(ctx));
       hc = *h;
     }
+    VCHECK(!(hc.status & (kStatusMbarrierTimeout | kStatusRecheckOverflow)), VISACD_ERR_DEVICE,
+           "score_planes: device status 0x%x (bulk-copy wait timed out or FP64 queue full)",
+           hc.status);
     VTRY(check_status(ctx, "score_planes"));
     if (!device_ptrs && P) {
       VCUDA(cudaMemcpyAsync(scores, d_scores, (size_t)P * 8, cudaMemcpyDeviceToHost, ctx->stream));
@@ -546,8 +554,8 @@ extern "C" int visacd_score_planes_noalloc(const float* d_planes, int32_t P, con
   EdgeRec* recs = reinterpret_cast<EdgeRec*>(base + kNoAllocCountersBytes + kNoAllocScoreQBytes);
   uint2* rq = reinterpret_cast<uint2*>(base + kNoAllocCountersBytes + kNoAllocScoreQBytes +
                                        kNoAllocPackBytes);
-  // The status word shares the counters block (its spare tail).
-  unsigned* status = reinterpret_cast<unsigned*>(base + kNoAllocCountersBytes - 16);
+  // The call's status word is part of the counters block, cleared below.
+  unsigned* status = &cnt->status;
   VCUDA(cudaMemsetAsync(base, 0, kNoAllocCountersBytes + (size_t)(P > 0 ? P : 1) * 8, st));
   const int sm = noalloc_sm_count(device);
   if (N > 0) {
@@ -570,7 +578,8 @@ extern "C" int visacd_score_planes_noalloc(const float* d_planes, int32_t P, con
                                                  rcap, sq);
     VCUDA(cudaGetLastError());
   }
-  score_finish_kernel<<<1, 1024, 0, st>>>(sq, P, cnt->stats, d_scores, nullptr, cnt->argmax);
+  score_finish_kernel<<<1, 1024, 0, st>>>(sq, P, cnt->stats, status, d_scores, nullptr,
+                                          cnt->argmax);
   VCUDA(cudaGetLastError());
   if (d_argmax) {
     VCUDA(cudaMemcpyAsync(d_argmax, cnt->argmax, sizeof(int32_t), cudaMemcpyDeviceToDevice, st));

@@ -104,10 +104,6 @@ PYBIND11_MODULE(visacd, m) {
       .def_readwrite("flat_surface_k", &Config::flat_surface_k)
       .def_readwrite("use_merging", &Config::use_merging)
       .def_readwrite("verbose", &Config::verbose)
-      .def_readwrite("gpu_clip", &Config::gpu_clip)
-      .def_readwrite("gpu_concavity", &Config::gpu_concavity)
-      .def_readwrite("gpu_remesh", &Config::gpu_remesh)
-      .def_readwrite("gpu_merge", &Config::gpu_merge)
       .def_readwrite("plane_proposer", &Config::plane_proposer)
       .def_readwrite("proposer_weights", &Config::proposer_weights)
       .def_readwrite("proposer_probe_planes", &Config::proposer_probe_planes)
@@ -125,6 +121,26 @@ PYBIND11_MODULE(visacd, m) {
   });
 
   m.def("set_seed", &set_seed, py::arg("seed"));
+  // Test hook (not in the reference's surface): route stages through the host
+  // restatements their GPU kernels are checked against. Arguments left at
+  // None keep their setting; returns the settings after the call.
+  m.def(
+      "_checker_hooks",
+      [](py::object clip, py::object concavity, py::object remesh, py::object merge) {
+        CheckerHooks& h = checker_hooks();
+        if (!clip.is_none()) h.host_clip = clip.cast<bool>();
+        if (!concavity.is_none()) h.host_concavity = concavity.cast<bool>();
+        if (!remesh.is_none()) h.host_remesh = remesh.cast<bool>();
+        if (!merge.is_none()) h.host_merge = merge.cast<bool>();
+        py::dict d;
+        d["host_clip"] = h.host_clip;
+        d["host_concavity"] = h.host_concavity;
+        d["host_remesh"] = h.host_remesh;
+        d["host_merge"] = h.host_merge;
+        return d;
+      },
+      py::arg("host_clip") = py::none(), py::arg("host_concavity") = py::none(),
+      py::arg("host_remesh") = py::none(), py::arg("host_merge") = py::none());
   m.attr("config") = py::cast(&config(), py::return_value_policy::reference);
   // The trained proposer ships next to this module (proposer_weights.bin).
   if (config().proposer_weights.empty()) {

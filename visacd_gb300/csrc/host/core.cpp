@@ -28,6 +28,11 @@ Config& config() {
   return c;
 }
 
+CheckerHooks& checker_hooks() {
+  static CheckerHooks h;
+  return h;
+}
+
 void Mt19937::seed(result_type s) {
   x_[0] = s;
   for (int i = 1; i < kN; ++i) x_[i] = 1812433253u * (x_[i - 1] ^ (x_[i - 1] >> 30)) + (uint32_t)i;

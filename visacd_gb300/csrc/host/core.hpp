@@ -91,10 +91,6 @@ struct Config {
   bool use_merging = false;
   // Additions of this implementation (not in the reference's Config).
   bool verbose = true;   // the "[visacd] ..." progress lines
-  bool gpu_clip = true;        // split parts with the GPU clip kernels (else the host clip)
-  bool gpu_concavity = true;   // Hausdorff term of the concavity metric on the GPU
-  bool gpu_remesh = true;      // SDF remesh (manifold and cages) on the GPU
-  bool gpu_merge = true;       // hull-pair distances of hull merging on the GPU
   // Split-plane search: "exhaustive" (the reference's random candidate draw)
   // or "learned" (16 planes from the learned proposer plus a probe of
   // `proposer_probe_planes` random candidates; when the best proposal scores
@@ -108,6 +104,18 @@ struct Config {
 };
 
 Config& config();
+
+// Test hooks, not part of the user-visible configuration: each routes one
+// stage through the host restatement that its GPU kernels are checked
+// against (the tests compare the two, and run host-only checks on machines
+// without a GPU). Off by default; the product path is the GPU kernels.
+struct CheckerHooks {
+  bool host_clip = false;        // host clip instead of the GPU clip kernels
+  bool host_concavity = false;   // host Hausdorff term of the concavity metric
+  bool host_remesh = false;      // host SDF remesh (manifold and cages)
+  bool host_merge = false;       // host hull-pair distances in hull merging
+};
+CheckerHooks& checker_hooks();
 
 // The 32-bit Mersenne Twister MT19937 (Matsumoto and Nishimura, 1998) with the
 // parameters and seeding std::mt19937 is defined with, so the same seed gives

@@ -294,7 +294,7 @@ double eval_hb(const Mesh& a, const Mesh& b, const HbSamples& s, double floor) {
   if (s.s1.empty() || s.s2.empty()) return kInf;
   auto& tm = concavity_times();
   const auto t0 = std::chrono::steady_clock::now();
-  const double h = config().gpu_concavity ? gpu::face_hausdorff(a, s.s1, s.i1, b, s.s2, s.i2, floor)
+  const double h = !checker_hooks().host_concavity ? gpu::face_hausdorff(a, s.s1, s.i1, b, s.s2, s.i2, floor)
                                           : face_hausdorff(a, s.s1, s.i1, b, s.s2, s.i2);
   tm.hausdorff_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   tm.calls++;
@@ -306,7 +306,7 @@ std::vector<double> eval_hb_batch(const std::vector<const Mesh*>& a, const std::
                                   double floor, bool independent) {
   const size_t J = a.size();
   std::vector<double> out(J, kInf);
-  if (!config().gpu_concavity) {
+  if (checker_hooks().host_concavity) {
     for (size_t j = 0; j < J; ++j) out[j] = eval_hb(*a[j], *b[j], *s[j]);
     return out;
   }

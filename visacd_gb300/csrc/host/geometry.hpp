@@ -10,8 +10,9 @@ namespace visacd {
 
 // ---- remesh.cpp: SDF remeshing (replaces lib/src/preprocess.cpp:18-67) ----
 void manifold_preprocess(Mesh& m, double scale, double level);
-// The host restatement manifold_preprocess runs when config().gpu_remesh is
-// off (the GPU path, visacd_sdf_remesh, produces the same mesh bit for bit).
+// The host restatement, which manifold_preprocess runs only under the test hook
+// checker_hooks().host_remesh (the GPU path, visacd_sdf_remesh, produces the
+// same mesh bit for bit).
 void manifold_preprocess_host(Mesh& m, double scale, double level);
 Vec3 closest_point_on_triangle(const Vec3& p, const Vec3& a, const Vec3& b, const Vec3& c);
 double point_triangle_distance(const Vec3& p, const Vec3& a, const Vec3& b, const Vec3& c);

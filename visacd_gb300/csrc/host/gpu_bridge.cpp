@@ -349,9 +349,9 @@ std::vector<Plane> propose_planes(const Mesh& mesh) {
 namespace visacd {
 
 // SDF remesh dispatch (lib/src/preprocess.cpp:18-67): the GPU kernels, or the
-// host restatement they equal when config().gpu_remesh is off.
+// host restatement they equal (test hook checker_hooks().host_remesh).
 void manifold_preprocess(Mesh& m, double scale, double level) {
-  if (config().gpu_remesh)
+  if (!checker_hooks().host_remesh)
     gpu::sdf_remesh(m, scale, level);
   else
     manifold_preprocess_host(m, scale, level);

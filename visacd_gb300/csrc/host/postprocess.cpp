@@ -126,7 +126,7 @@ MeshList separate_step(const Mesh& part) {
 // threshold.
 std::vector<double> pair_distances(const MeshList& cvxs, const std::vector<std::pair<int, int>>& pairs,
                                    double threshold) {
-  if (config().gpu_merge) return gpu::hull_distances(cvxs, pairs, threshold);
+  if (!checker_hooks().host_merge) return gpu::hull_distances(cvxs, pairs, threshold);
   std::vector<double> d(pairs.size());
   for (size_t k = 0; k < pairs.size(); ++k) d[k] = mesh_dist(cvxs[pairs[k].first], cvxs[pairs[k].second]);
   return d;

@@ -211,7 +211,7 @@ bool decompose_iteration(Mesh& mesh, MeshList& parts, Mesh& cage,
   g_times.scoring += t1 - t0;
 
   std::vector<int> map1, map2;
-  MeshList halves = config().gpu_clip ? gpu::clip(mesh, plane, map1, map2)
+  MeshList halves = !checker_hooks().host_clip ? gpu::clip(mesh, plane, map1, map2)
                                       : clip(mesh, plane, map1, map2);
   double t2 = now_ms();
   g_times.clip += t2 - t1;
