@@ -43,6 +43,24 @@ L2_BYTES = 129 * 1024 * 1024
 TRAFFIC_FILE = ROOT / "profiles" / "dram_traffic.txt"
 
 
+THROUGHPUT_FILE = ROOT / "profiles" / "visibility_throughput.txt"
+
+
+def measured_throughput(workload_name: str, kernel: str) -> dict:
+    """ncu's L1 / L2 throughput, issue activity and occupancy of a kernel on a
+    workload ("workload kernel l1 l2 issue occupancy" lines, percent)."""
+    if not THROUGHPUT_FILE.exists():
+        return {}
+    for line in THROUGHPUT_FILE.read_text().splitlines():
+        f = line.split()
+        if len(f) == 6 and not line.startswith("#") and f[0] == workload_name and f[1] == kernel:
+            return {"l1_pct": float(f[2]), "l2_pct": float(f[3]), "issue_active_pct": float(f[4]),
+                    "achieved_occupancy_pct": float(f[5]),
+                    "survey_roofline_max_l1_l2_pct": max(float(f[2]), float(f[3])),
+                    "source": "ncu --set full of this launch (profiles/visibility_kernel_blob_s5_full.md)"}
+    return {}
+
+
 def measured_traffic(workload_name: str, kernel: str):
     if not TRAFFIC_FILE.exists():
         return None
@@ -307,6 +325,7 @@ def run_ours(args) -> dict:
                      "achieved": vis_achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": vis_achieved / fp32_peak if vis_achieved else None,
                      "traffic": measured_traffic(args.workload, "visibility_kernel"),
+                     "ncu": measured_throughput(args.workload, "visibility_kernel"),
                      "ms_per_launch": vis_ms / max(vis_n, 1),
                      "pairs_per_s": n_pairs / vis_launch_s if vis_ms else None,
                      "work_model": "packet node visits x 32 lanes x 2 boxes x 12 FLOP + triangle tests x 60 FLOP",

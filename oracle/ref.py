@@ -39,6 +39,8 @@ def lib() -> C.CDLL:
         L.ref_hull_volume.restype = C.c_double
         L.ref_hull_bt.argtypes = [P, C.c_int, P, C.c_int, P, C.c_int, C.POINTER(C.c_int)]
         L.ref_hull_bt.restype = C.c_int
+        L.ref_multimerge.argtypes = [P, P, P, P, C.c_int, C.c_double, C.c_double, C.c_uint]
+        L.ref_multimerge.restype = C.c_int
         L.ref_process.argtypes = [P, C.c_int, P, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int,
                                   C.c_int, C.POINTER(C.c_double)]
         _lib = L
@@ -131,6 +133,18 @@ def hull_bt(v):
     if nt < 0:
         raise ValueError("hull buffers too small")
     return ov[: nv.value], ot[:nt]
+
+
+def multimerge(meshes, current_concavity, threshold, seed):
+    """The reference's multimerge_ch on parts [(v, t), ...] (hulls from
+    compute_ch, engine seeded with seed): the merged hulls."""
+    v = np.ascontiguousarray(np.concatenate([p[0] for p in meshes]), dtype=np.float64)
+    t = np.ascontiguousarray(np.concatenate([p[1] for p in meshes]), dtype=np.int32)
+    nv = np.array([len(p[0]) for p in meshes], np.int32)
+    nt = np.array([len(p[1]) for p in meshes], np.int32)
+    lib().ref_multimerge(_p(v), _p(nv), _p(t), _p(nt), len(meshes), current_concavity, threshold,
+                         seed)
+    return parts()
 
 
 def process(v, t, concavity, num_parts, seed, score_mode="concavity", return_parts=False,

@@ -228,6 +228,29 @@ int ref_hull_bt(const double* v, int nv, double* out_v, int cap_v, int* out_t, i
   return (int)h.triangles.size();
 }
 
+// multimerge_ch (lib/src/postprocess.cpp:64-200) on the given parts
+// (concatenated: part k has nv[k] vertices and nt[k] triangles), with their
+// hulls from compute_ch and the engine seeded with `seed` first. The merged
+// hulls land in the part store; returns their count.
+int ref_multimerge(const double* v, const int* nv, const int* t, const int* nt, int nparts,
+                   double current_concavity, double threshold, unsigned seed) {
+  neural_acd::MeshList parts, hulls;
+  for (int k = 0; k < nparts; ++k) {
+    parts.push_back(make_mesh(v, nv[k], t, nt[k]));
+    v += 3 * (size_t)nv[k];
+    t += 3 * (size_t)nt[k];
+  }
+  for (auto& p : parts) {
+    Mesh h;
+    p.compute_ch(h, true);
+    hulls.push_back(h);
+  }
+  neural_acd::set_seed(seed);
+  neural_acd::multimerge_ch(parts, hulls, current_concavity, threshold);
+  g_parts = hulls;
+  return (int)hulls.size();
+}
+
 // lib/src/process.cpp:238 process(mesh, concavity, num_parts); parts land in
 // the part store.
 int ref_process(const double* v, int nv, const int* t, int nt, double concavity, int num_parts,

@@ -176,6 +176,43 @@ def test_hull_matches_btconvexhull(V):
         assert abs(vb - vo) <= 1e-12 * max(1.0, abs(vb)), (name, vb, vo)
 
 
+def _octants(level, seed):
+    """A displaced blob cut into octants by the reference's clip."""
+    v, t = mg.displaced_blob(level, seed=seed)
+    parts = [(v, t)]
+    for axis in range(3):
+        nxt = []
+        for pv, pt in parts:
+            pl = np.zeros(4)
+            pl[axis] = 1.0
+            halves, _, _ = R.clip(pv, pt, pl)
+            nxt += [(h["vertices"], h["triangles"]) for h in halves if len(h["triangles"])]
+        parts = nxt
+    return parts
+
+
+def test_multimerge_matches_reference(V):
+    """multimerge_ch (hull-pair distances, merge costs with their sampled
+    terms, the packed cost matrix and its updates) against the reference's own
+    multimerge_ch compiled in place, on the same parts and engine seed: the
+    same merged hulls in the same order."""
+    parts = _octants(2, 4)
+    threshold, current = 0.2, 1.0
+    for seed in (0,):
+        ref = R.multimerge(parts, current, threshold, seed)
+        V._checker_hooks(host_merge=True)
+        try:
+            V.set_seed(seed)
+            ours = V._multimerge(parts, current, threshold)
+        finally:
+            V._checker_hooks(host_merge=False)
+        assert len(ours) == len(ref) < len(parts)
+        for a, b in zip(ref, ours):
+            np.testing.assert_array_equal(a["vertices"], b["vertices"])
+            assert abs(V._mesh_volume(a["vertices"], a["triangles"]) -
+                       V._mesh_volume(b["vertices"], b["triangles"])) < 1e-12
+
+
 def test_surface_sampling_matches_one_by_one_draws(V):
     """extract_point_set (engine outputs taken in bulk, guide-table triangle
     draws) against the reference's one-draw-at-a-time loop on std::mt19937:

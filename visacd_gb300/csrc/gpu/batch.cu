@@ -245,21 +245,17 @@ __global__ void __launch_bounds__(kScoreThreads, (K <= 4 ? 2 : 1))
   const int nb = (int)d.n_blocks;
   const int64_t blk0 = (int64_t)(d.rec_begin / kEdgeBlock);
   const int plane_base = grp * kScoreThreads * K;
-  unsigned long long a2[K], b2[K], c2[K], d2[K];
-  float nlo[K], nhi[K];
-  uint32_t acc_lo[K], acc_hi[K];
+  PlaneAcc pa[K];
+  uint32_t acc[K], dmin[K];
 #pragma unroll
   for (int k = 0; k < K; ++k) {
     const int lp = plane_base + k * kScoreThreads + tid;
     float4 pl = lp < Pp.P ? planes[Pp.plane_begin + lp]
                           : make_float4(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000),
                                         __int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
-    a2[k] = pack2(pl.x, pl.x);
-    b2[k] = pack2(pl.y, pl.y);
-    c2[k] = pack2(pl.z, pl.z);
-    d2[k] = pack2(pl.w, pl.w);
-    plane_thresholds(pl, Pp.stats, nlo[k], nhi[k]);
-    acc_lo[k] = acc_hi[k] = 0u;
+    pa[k] = plane_acc(pl, Pp.stats);
+    acc[k] = 0u;
+    dmin[k] = 0xffffffffu;
     tot[k * kScoreThreads + tid] = 0ull;
   }
   if (nb == 0 || plane_base >= Pp.P) return;
@@ -284,34 +280,20 @@ __global__ void __launch_bounds__(kScoreThreads, (K <= 4 ? 2 : 1))
       break;
     }
     const ulonglong2* sm = reinterpret_cast<const ulonglong2*>(buf + cur * kEdgeBlock);
-#pragma unroll 2
-    for (int e = 0; e < kEdgeBlock; ++e) {
-      ulonglong2 r0 = sm[2 * e];
-      ulonglong2 r1 = sm[2 * e + 1];
-      uint32_t q = (uint32_t)(r1.y & 0xffffffffull);
-#pragma unroll
-      for (int k = 0; k < K; ++k) {
-        unsigned long long v = ffma2(c2[k], r1.x, d2[k]);
-        v = ffma2(b2[k], r0.y, v);
-        v = ffma2(a2[k], r0.x, v);
-        float v1, v2;
-        unpack2(v, v1, v2);
-        float sv = fmaxf(fminf(v1, v2), -fmaxf(v1, v2));
-        acc_hi[k] += sv < nhi[k] ? q : 0u;
-        acc_lo[k] += sv < nlo[k] ? q : 0u;
-      }
-    }
+    score_edge_block<K>(sm, kEdgeBlock, pa, acc, dmin);
 #pragma unroll
     for (int k = 0; k < K; ++k) {
-      if (acc_lo[k] == acc_hi[k]) {
-        tot[k * kScoreThreads + tid] += acc_hi[k];
-      } else {
-        const int gp = Pp.plane_begin + plane_base + k * kScoreThreads + tid;
+      const int lp = plane_base + k * kScoreThreads + tid;
+      if (dmin[k] > pa[k].wbits) {
+        tot[k * kScoreThreads + tid] += acc[k];
+      } else if (lp < Pp.P) {
+        const int gp = Pp.plane_begin + lp;
         unsigned idx = atomicAdd(recheck_count, 1u);
         if (idx < recheck_cap) recheck[idx] = make_uint2((unsigned)gp, (unsigned)(blk0 + it));
         else atomicOr(status, kStatusRecheckOverflow);
       }
-      acc_lo[k] = acc_hi[k] = 0u;
+      acc[k] = 0u;
+      dmin[k] = 0xffffffffu;
     }
     __syncthreads();
   }

@@ -47,21 +47,17 @@ __global__ void __launch_bounds__(kScoreThreads, (K <= 4 ? 2 : 1))
   const int nb = (int)(b_end > b_begin ? b_end - b_begin : 0);
   const int plane_base = blockIdx.y * (kScoreThreads * K);
 
-  unsigned long long a2[K], b2[K], c2[K], d2[K];
-  float nlo[K], nhi[K];
-  uint32_t acc_lo[K], acc_hi[K];
+  PlaneAcc pa[K];
+  uint32_t acc[K], dmin[K];
 #pragma unroll
   for (int k = 0; k < K; ++k) {
     int p = plane_base + k * kScoreThreads + tid;
-    float4 pl = p < P ? planes[p] : make_float4(__int_as_float(0x7fc00000), 0.f, 0.f, 0.f);
-    if (p >= P) pl = make_float4(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000),
-                                 __int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
-    a2[k] = pack2(pl.x, pl.x);
-    b2[k] = pack2(pl.y, pl.y);
-    c2[k] = pack2(pl.z, pl.z);
-    d2[k] = pack2(pl.w, pl.w);
-    plane_thresholds(pl, stats, nlo[k], nhi[k]);
-    acc_lo[k] = acc_hi[k] = 0u;
+    float4 pl = p < P ? planes[p]
+                      : make_float4(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000),
+                                    __int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
+    pa[k] = plane_acc(pl, stats);
+    acc[k] = 0u;
+    dmin[k] = 0xffffffffu;
     tot[k * kScoreThreads + tid] = 0ull;
   }
   if (nb == 0) return;
@@ -96,31 +92,15 @@ __global__ void __launch_bounds__(kScoreThreads, (K <= 4 ? 2 : 1))
     const int64_t e0 = (b_begin + it) * kEdgeBlock;
     const int cnt = (int)(E - e0 < kEdgeBlock ? E - e0 : kEdgeBlock);
     const ulonglong2* s = reinterpret_cast<const ulonglong2*>(buf + cur * kEdgeBlock);
-#pragma unroll 2
-    for (int e = 0; e < cnt; ++e) {
-      ulonglong2 r0 = s[2 * e];      // (x1,x2), (y1,y2)
-      ulonglong2 r1 = s[2 * e + 1];  // (z1,z2), (q,pad)
-      uint32_t q = (uint32_t)(r1.y & 0xffffffffull);
-#pragma unroll
-      for (int k = 0; k < K; ++k) {
-        unsigned long long v = ffma2(c2[k], r1.x, d2[k]);
-        v = ffma2(b2[k], r0.y, v);
-        v = ffma2(a2[k], r0.x, v);
-        float v1, v2;
-        unpack2(v, v1, v2);
-        float sv = fmaxf(fminf(v1, v2), -fmaxf(v1, v2));
-        acc_hi[k] += sv < nhi[k] ? q : 0u;
-        acc_lo[k] += sv < nlo[k] ? q : 0u;
-      }
-    }
-    // Close the block: certain sums go to the total; blocks with band pairs
-    // are queued for the FP64 re-decision and contribute nothing here.
+    score_edge_block<K>(s, cnt, pa, acc, dmin);
+    // Close the block: certain sums go to the total; blocks that may hold band
+    // pairs are queued for the FP64 re-decision and contribute nothing here.
 #pragma unroll
     for (int k = 0; k < K; ++k) {
-      if (acc_lo[k] == acc_hi[k]) {
-        tot[k * kScoreThreads + tid] += acc_hi[k];
-      } else {
-        int p = plane_base + k * kScoreThreads + tid;
+      int p = plane_base + k * kScoreThreads + tid;
+      if (dmin[k] > pa[k].wbits) {
+        tot[k * kScoreThreads + tid] += acc[k];
+      } else if (p < P) {
         unsigned idx = atomicAdd(recheck_count, 1u);
         if (idx < recheck_cap) {
           recheck[idx] = make_uint2((unsigned)p, (unsigned)(b_begin + it));
@@ -128,7 +108,8 @@ __global__ void __launch_bounds__(kScoreThreads, (K <= 4 ? 2 : 1))
           atomicOr(status, kStatusRecheckOverflow);
         }
       }
-      acc_lo[k] = acc_hi[k] = 0u;
+      acc[k] = 0u;
+      dmin[k] = 0xffffffffu;
     }
     __syncthreads();
   }

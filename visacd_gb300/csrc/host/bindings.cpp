@@ -311,6 +311,20 @@ PYBIND11_MODULE(visacd, m) {
     return mesh_dist(ma, mb);
   });
   m.def("_mesh_volume", [](py::array_t<double> v, py::array_t<int> t) { return mesh_volume(np_to_mesh(v, t)); });
+  // multimerge_ch on parts [(v, t), ...] with their hulls (as process() builds
+  // them) and the engine as it stands: the merged hulls.
+  m.def("_multimerge", [](py::list parts, double current_concavity, double threshold) {
+    MeshList ps, hs;
+    for (auto item : parts) {
+      auto tup = item.cast<py::tuple>();
+      ps.push_back(np_to_mesh(tup[0].cast<py::array_t<double>>(), tup[1].cast<py::array_t<int>>()));
+    }
+    for (const auto& p : ps) hs.push_back(convex_hull(p.vertices, true));
+    multimerge_ch(ps, hs, current_concavity, threshold);
+    py::list out;
+    for (const auto& h : hs) out.append(mesh_dict(h));
+    return out;
+  });
   m.def(
       "_separate_disjoint",
       [](py::array_t<double> v, py::array_t<int> t, py::object is_new, py::object edges) {
