@@ -25,6 +25,10 @@
  *                                     lib/ptx/ray_segments.cu:49-125
  *   visacd_compute_intersection_matrix  compute_intersection_matrix,
  *                                     lib/include/intersections.hpp:24
+ *   visacd_candidate_planes ......... get_candidate_planes after the draws,
+ *                                     lib/src/process.cpp:28-72
+ *   visacd_split_search ............. the split search of decompose_iteration,
+ *                                     lib/src/process.cpp:96-134
  */
 #ifndef VISACD_GPU_H
 #define VISACD_GPU_H
@@ -189,6 +193,44 @@ int visacd_compute_intersection_matrix(visacd_ctx* ctx, const float* verts, int3
 int visacd_score_planes(visacd_ctx* ctx, const float* planes, int32_t P, const float* points,
                         int32_t N, const uint32_t* edges, int64_t E, int device_ptrs,
                         double* scores, visacd_score_stats* stats);
+
+/* ---- candidate planes and the split search -------------------------------- */
+/* Candidate split planes from drawn visibility edges. Replaces the plane
+   construction and near-duplicate filter of get_candidate_planes
+   (lib/src/process.cpp:28-72); the draws themselves stay with the caller's
+   random engine. draws[k] is the edge index of draw k (the reference's
+   uniform_int_distribution(0, E - 1) outputs, in order; pass the most the
+   reference could use, 5 num_planes). For each draw, in order, the plane with
+   unit normal n = unit(p2 - p1) and d = -n . midpoint (FP64, the reference's
+   operation order) is kept unless |p2 - p1| < 1e-6 or a kept plane has
+   |n . n'| > cos 5 deg and |d - d'| < 1e-3; drawing stops once num_planes are
+   kept. verts n x 3 float64, edges E x 2 uint32, host pointers. planes_out:
+   num_planes x 4 float64 (a, b, c, d); *n_planes gets the count kept and
+   *draws_used how many draws the reference's loop consumed (advance the
+   engine by exactly those draws). Bit-identical to the reference. */
+int visacd_candidate_planes(visacd_ctx* ctx, const double* verts, int32_t n, const uint32_t* edges,
+                            int64_t E, const int32_t* draws, int32_t n_draws, int32_t num_planes,
+                            double* planes_out, int32_t* n_planes, int32_t* draws_used);
+
+typedef struct visacd_split_info {
+  int32_t best_index;    /* in [candidates..., flat planes...]; -1 when nothing was scored */
+  int32_t n_candidates;  /* candidate planes kept */
+  int32_t draws_used;    /* draws the reference's candidate loop consumed */
+  int32_t pad;
+  double best_score;     /* the winning score (flat planes: times flat_k) */
+} visacd_split_info;
+
+/* The split-plane search of one part (lib/src/process.cpp:96-134) in one
+   call: the candidate planes of visacd_candidate_planes, then the flat-surface
+   planes (n_flat x 4 float64), all scored by visacd_score_planes' kernels
+   (FP32 points from the FP64 vertices), flat scores multiplied by flat_k, and
+   the first maximum in that order. best_plane: 4 float64 (the chosen
+   candidate's FP64 coefficients, or the flat plane's). Host pointers,
+   synchronous. */
+int visacd_split_search(visacd_ctx* ctx, const double* verts, int32_t n, const uint32_t* edges,
+                        int64_t E, const int32_t* draws, int32_t n_draws, int32_t num_planes,
+                        const double* flat_planes, int32_t n_flat, double flat_k,
+                        double* best_plane, visacd_split_info* info);
 
 /* ---- batched visibility + scoring ----------------------------------------- */
 /* A batch of parts of uneven size, each with its points (n x 3 float32, host),

@@ -33,7 +33,8 @@ def lib() -> C.CDLL:
         L.oracle_visibility_rows.argtypes = [P, i32, P, P, i32, P, P, i32, P, i32, P,
                                              C.POINTER(i64), C.POINTER(i64)]
         L.oracle_visibility_rows.restype = i64
-        L.oracle_candidate_planes.argtypes = [P, P, i64, i32, C.c_uint32, P]
+        L.oracle_candidate_planes.argtypes = [P, P, i64, i32, C.c_uint32, P, C.POINTER(i32)]
+        L.oracle_edge_draws.argtypes = [i64, i32, C.c_uint32, P]
         L.oracle_seg_tri_batch.argtypes = [P, P, i64, P]
         L.oracle_seg_tri_batch.restype = i64
         L.oracle_candidate_planes.restype = i32
@@ -142,8 +143,21 @@ def candidate_planes(verts, edges, num_planes: int, seed: int) -> np.ndarray:
     v = np.ascontiguousarray(verts, dtype=np.float64).reshape(-1, 3)
     e = np.ascontiguousarray(edges, dtype=np.uint32).reshape(-1, 2)
     out = np.zeros((num_planes, 4), dtype=np.float64)
-    n = lib().oracle_candidate_planes(_p(v), _p(e), len(e), num_planes, seed, _p(out))
+    n = lib().oracle_candidate_planes(_p(v), _p(e), len(e), num_planes, seed, _p(out), None)
     return out[:n]
+
+
+def candidate_planes_with_draws(verts, edges, num_planes: int, seed: int):
+    """candidate_planes plus the raw edge draws (5 num_planes of them) and how
+    many the loop consumed."""
+    v = np.ascontiguousarray(verts, dtype=np.float64).reshape(-1, 3)
+    e = np.ascontiguousarray(edges, dtype=np.uint32).reshape(-1, 2)
+    out = np.zeros((max(num_planes, 1), 4), dtype=np.float64)
+    used = C.c_int32()
+    n = lib().oracle_candidate_planes(_p(v), _p(e), len(e), num_planes, seed, _p(out), C.byref(used))
+    draws = np.zeros(5 * num_planes, dtype=np.int32)
+    lib().oracle_edge_draws(len(e), len(draws), seed, _p(draws))
+    return out[:n], draws, used.value
 
 
 def seg_tri_batch(seg, tri):

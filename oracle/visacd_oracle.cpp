@@ -504,7 +504,9 @@ int64_t oracle_visibility_rows(const float* pts, int32_t n, const uint8_t* is_ne
 // out: num_planes x 4 doubles (a, b, c, d). Returns the number of planes.
 // ---------------------------------------------------------------------------
 int32_t oracle_candidate_planes(const double* verts, const uint32_t* edges, int64_t E,
-                                int32_t num_planes, uint32_t seed, double* out) {
+                                int32_t num_planes, uint32_t seed, double* out,
+                                int32_t* draws_used) {
+  if (draws_used) *draws_used = 0;
   if (E == 0) return 0;
   std::mt19937 eng(seed);
   std::uniform_int_distribution<> dis(0, (int)(E - 1));
@@ -512,6 +514,7 @@ int32_t oracle_candidate_planes(const double* verts, const uint32_t* edges, int6
   const double dist_eps = 1e-3;
   int32_t np = 0;
   for (int i = 0; i < num_planes * 5 && np < num_planes; ++i) {
+    if (draws_used) *draws_used = i + 1;
     int idx = dis(eng);
     const double* p1 = verts + 3 * (int64_t)edges[2 * (int64_t)idx];
     const double* p2 = verts + 3 * (int64_t)edges[2 * (int64_t)idx + 1];
@@ -542,6 +545,15 @@ int32_t oracle_candidate_planes(const double* verts, const uint32_t* edges, int6
     }
   }
   return np;
+}
+
+// The first n edge draws of the loop above: uniform_int_distribution<int>(0,
+// E - 1) on std::mt19937(seed), in order.
+void oracle_edge_draws(int64_t E, int32_t n, uint32_t seed, int32_t* out) {
+  if (E <= 0) return;
+  std::mt19937 eng(seed);
+  std::uniform_int_distribution<> dis(0, (int)(E - 1));
+  for (int32_t k = 0; k < n; ++k) out[k] = dis(eng);
 }
 
 // Independent segment-triangle decisions (the precision sweep): seg is S x 6

@@ -32,6 +32,7 @@ EXPORTED = [
     "visacd_lp_train_step",
     "visacd_sdf_remesh", "visacd_sdf_fetch", "visacd_hull_distances", "visacd_segment_triangle_tests",
     "visacd_set_blocking_sync", "visacd_lp_set_tcgen05", "visacd_ctx_set_blocking_wait",
+    "visacd_candidate_planes", "visacd_split_search",
 ]
 
 LP_POINTS = 2048
@@ -60,6 +61,14 @@ class ScoreStats(C.Structure):
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class SplitInfo(C.Structure):
+    _fields_ = [("best_index", C.c_int32), ("n_candidates", C.c_int32), ("draws_used", C.c_int32),
+                ("pad", C.c_int32), ("best_score", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "pad"}
 
 
 def load() -> C.CDLL:
@@ -96,6 +105,10 @@ def load() -> C.CDLL:
     lib.visacd_score_planes.argtypes = [P, P, i32, P, i32, P, i64, C.c_int, P,
                                         C.POINTER(ScoreStats)]
     lib.visacd_score_planes_noalloc.argtypes = [P, i32, P, i32, P, i64, P, P, P]
+    lib.visacd_candidate_planes.argtypes = [P, P, i32, P, i64, P, i32, i32, P, C.POINTER(i32),
+                                            C.POINTER(i32)]
+    lib.visacd_split_search.argtypes = [P, P, i32, P, i64, P, i32, i32, P, i32, C.c_double, P,
+                                        C.POINTER(SplitInfo)]
     lib.visacd_clip.argtypes = [P, P, i32, P, i32, P, C.POINTER(ClipResult)]
     lib.visacd_measure_fp32_peak.argtypes = [P, C.POINTER(C.c_double)]
     lib.visacd_batch_create.argtypes = [P, i32, C.POINTER(P), P, C.POINTER(P), C.POINTER(P), C.POINTER(P),
@@ -380,6 +393,33 @@ class Context:
         _check(lib().visacd_score_planes(self._h, _ptr(pl), len(pl), _ptr(pt), len(pt), _ptr(ed),
                                          len(ed), 0, _ptr(scores), C.byref(st)), "visacd_score_planes")
         return scores, st.as_dict()
+
+    def candidate_planes(self, verts, edges, draws, num_planes: int):
+        """Candidate planes from the given edge draws: (planes n x 4 float64,
+        draws used)."""
+        v = np.ascontiguousarray(np.asarray(verts, dtype=np.float64).reshape(-1, 3))
+        ed = _u32(edges, 2)
+        dr = np.ascontiguousarray(np.asarray(draws, dtype=np.int32))
+        out = np.zeros((max(num_planes, 1), 4), np.float64)
+        got, used = C.c_int32(), C.c_int32()
+        _check(lib().visacd_candidate_planes(self._h, _ptr(v), len(v), _ptr(ed), len(ed), _ptr(dr), len(dr),
+                                             num_planes, _ptr(out), C.byref(got), C.byref(used)),
+               "visacd_candidate_planes")
+        return out[: got.value], used.value
+
+    def split_search(self, verts, edges, draws, num_planes: int, flat_planes=None, flat_k: float = 2.0):
+        """The split search: (best plane 4 float64, info dict)."""
+        v = np.ascontiguousarray(np.asarray(verts, dtype=np.float64).reshape(-1, 3))
+        ed = _u32(edges, 2)
+        dr = np.ascontiguousarray(np.asarray(draws, dtype=np.int32))
+        fl = None if flat_planes is None or len(flat_planes) == 0 else \
+            np.ascontiguousarray(np.asarray(flat_planes, dtype=np.float64).reshape(-1, 4))
+        best = np.zeros(4, np.float64)
+        info = SplitInfo()
+        _check(lib().visacd_split_search(self._h, _ptr(v), len(v), _ptr(ed), len(ed), _ptr(dr), len(dr),
+                                         num_planes, _ptr(fl), 0 if fl is None else len(fl), flat_k,
+                                         _ptr(best), C.byref(info)), "visacd_split_search")
+        return best, info.as_dict()
 
     def score_planes_device(self, d_planes: int, P: int, d_points: int, N: int, d_edges: int,
                             E: int, d_scores: int, stats: bool = False):

@@ -114,6 +114,8 @@ enum CtxSlot {
   kSlotSdfTris,
   kSlotHull,
   kSlotSegTri,
+  kSlotCandidates,
+  kSlotCandLinks,
   kSlotCount
 };
 
@@ -191,6 +193,7 @@ enum KernelId {
   kKSdfCross,
   kKHullDist,
   kKSegTri,
+  kKCandidates,
   kKMisc,
   kKCount
 };
@@ -287,6 +290,13 @@ int exclusive_scan_u32_to_u64(visacd_ctx* ctx, const uint32_t* in, uint64_t* out
 // keys/vals (the alt buffers are scratch of the same size).
 int radix_sort_u64(visacd_ctx* ctx, uint64_t* keys, uint32_t* vals, uint64_t* keys_alt,
                    uint32_t* vals_alt, int32_t n, int key_bits);
+
+// Plane scoring on device pointers without a host wait (score.cu): the call's
+// status word and FP64 queue demand are left in device memory.
+int score_planes_device_async(visacd_ctx* ctx, const float* d_planes, int32_t P, const float* d_pts,
+                              int32_t N, const uint32_t* d_edges, int64_t E, double* d_scores,
+                              unsigned rcap, const unsigned** d_status, const unsigned** d_recheck_count);
+unsigned score_recheck_capacity(int32_t P, int64_t E);
 
 }  // namespace vgpu
 

@@ -86,7 +86,7 @@ static const char* kNames[kKCount] = {
     "hd_query",      "hd_head",        "lp_features",
     "lp_gemm",       "lp_pool",        "lp_loss",      "lp_adam",
     "lp_misc",       "sdf_remesh",     "sdf_dist",     "sdf_cross",
-    "hull_dist",     "seg_tri",
+    "hull_dist",     "seg_tri",        "candidates",
     "misc"};
 
 const char* kernel_name(int id) { return (id >= 0 && id < kKCount) ? kNames[id] : "?"; }

@@ -307,6 +307,21 @@ static unsigned recheck_capacity(int32_t P, int64_t E) {
   return (unsigned)cap;
 }
 
+// Device-pointer scoring without a host wait, for callers that read the
+// outcome later: the call's status word (kStatus* bits; a full FP64 queue or a
+// timed-out wait) and its queue demand stay in device memory.
+int score_planes_device_async(visacd_ctx* ctx, const float* d_planes, int32_t P, const float* d_pts,
+                              int32_t N, const uint32_t* d_edges, int64_t E, double* d_scores,
+                              unsigned rcap, const unsigned** d_status, const unsigned** d_recheck_count) {
+  ScoreCounters* cnt = nullptr;
+  VTRY(score_device(ctx, d_planes, P, d_pts, N, d_edges, E, d_scores, nullptr, &cnt, rcap));
+  *d_status = &cnt->status;
+  *d_recheck_count = &cnt->recheck_count;
+  return VISACD_OK;
+}
+
+unsigned score_recheck_capacity(int32_t P, int64_t E) { return recheck_capacity(P, E); }
+
 int score_planes_impl(visacd_ctx* ctx, const float* planes, int32_t P, const float* points,
                       int32_t N, const uint32_t* edges, int64_t E, int device_ptrs,
                       double* scores, float* scores_f32, visacd_score_stats* stats) {

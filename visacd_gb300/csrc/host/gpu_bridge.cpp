@@ -88,6 +88,111 @@ static void to_f32(const std::vector<Vec3>& v, std::vector<float>& out) {
     for (int k = 0; k < 3; ++k) out[3 * i + k] = (float)v[i][k];
 }
 
+namespace {
+
+// The edge draws of one candidate-plane generation, taken in advance from a
+// copy of the process engine: draws[k] is what the reference's
+// uniform_int_distribution(0, E - 1) returns at draw k, consumed[k] the engine
+// outputs used by draws 0..k (a draw takes more than one when it rejects).
+struct DrawPlan {
+  std::vector<int32_t> draws;
+  std::vector<uint64_t> consumed;
+};
+
+struct CountingEngine {
+  using result_type = uint32_t;
+  Mt19937& eng;
+  uint64_t n = 0;
+  static constexpr result_type min() { return Mt19937::min(); }
+  static constexpr result_type max() { return Mt19937::max(); }
+  result_type operator()() {
+    ++n;
+    return eng();
+  }
+};
+
+DrawPlan plan_draws(size_t n_edges, int num_planes) {
+  DrawPlan plan;
+  Mt19937 copy = random_engine();
+  CountingEngine ce{copy};
+  std::uniform_int_distribution<> dis(0, (int)n_edges - 1);
+  const int D = num_planes > 0 ? 5 * num_planes : 0;
+  plan.draws.resize(D);
+  plan.consumed.resize(D);
+  for (int k = 0; k < D; ++k) {
+    plan.draws[k] = dis(ce);
+    plan.consumed[k] = ce.n;
+  }
+  return plan;
+}
+
+// Moves the process engine past the draws the reference's loop consumed.
+void take_draws(const DrawPlan& plan, int32_t draws_used) {
+  if (draws_used <= 0) return;
+  uint64_t left = plan.consumed[(size_t)draws_used - 1];
+  uint32_t sink[256];
+  Mt19937& eng = random_engine();
+  while (left) {
+    const size_t n = left < 256 ? (size_t)left : 256;
+    eng.fill(sink, n);
+    left -= n;
+  }
+}
+
+}  // namespace
+
+std::vector<Plane> candidate_planes(const std::vector<Vec3>& vertices, const std::vector<Edge>& edges,
+                                    int num_planes) {
+  std::vector<Plane> planes;
+  if (edges.empty() || num_planes <= 0) return planes;
+  visacd_ctx* ctx = context();
+  const DrawPlan plan = plan_draws(edges.size(), num_planes);
+  std::vector<double> out(4 * (size_t)num_planes);
+  int32_t got = 0, used = 0;
+  static_assert(sizeof(Edge) == 8, "packed edge pairs");
+  check(visacd_candidate_planes(ctx, reinterpret_cast<const double*>(vertices.data()),
+                                (int32_t)vertices.size(), reinterpret_cast<const uint32_t*>(edges.data()),
+                                (int64_t)edges.size(), plan.draws.data(), (int32_t)plan.draws.size(),
+                                num_planes, out.data(), &got, &used),
+        "visacd_candidate_planes");
+  take_draws(plan, used);
+  planes.reserve(got);
+  for (int32_t i = 0; i < got; ++i) planes.emplace_back(out[4 * i], out[4 * i + 1], out[4 * i + 2], out[4 * i + 3]);
+  return planes;
+}
+
+bool split_search(const Mesh& mesh, const std::vector<Plane>& flat_planes, double flat_k, int num_planes,
+                  Plane& out) {
+  const auto& edges = mesh.intersecting_edges;
+  if (edges.empty()) return false;
+  double t0 = now_ms();
+  visacd_ctx* ctx = context();
+  const DrawPlan plan = plan_draws(edges.size(), num_planes);
+  std::vector<double> flat(4 * flat_planes.size());
+  for (size_t i = 0; i < flat_planes.size(); ++i) {
+    flat[4 * i] = flat_planes[i].a;
+    flat[4 * i + 1] = flat_planes[i].b;
+    flat[4 * i + 2] = flat_planes[i].c;
+    flat[4 * i + 3] = flat_planes[i].d;
+  }
+  double best[4];
+  visacd_split_info info{};
+  check(visacd_split_search(ctx, reinterpret_cast<const double*>(mesh.vertices.data()),
+                            (int32_t)mesh.vertices.size(), reinterpret_cast<const uint32_t*>(edges.data()),
+                            (int64_t)edges.size(), plan.draws.data(), (int32_t)plan.draws.size(), num_planes,
+                            flat.empty() ? nullptr : flat.data(), (int32_t)flat_planes.size(), flat_k, best,
+                            &info),
+        "visacd_split_search");
+  take_draws(plan, info.draws_used);
+  auto& c = counters();
+  c.score_calls++;
+  c.plane_edge_pairs += (long long)(info.n_candidates + (int)flat_planes.size()) * (long long)edges.size();
+  c.score_ms += now_ms() - t0;
+  if (info.best_index < 0) return false;
+  out = Plane(best[0], best[1], best[2], best[3]);
+  return true;
+}
+
 std::vector<Edge> visibility_edges(const Mesh& mesh, const Mesh& cage) {
   double t0 = now_ms();
   visacd_ctx* ctx = context();

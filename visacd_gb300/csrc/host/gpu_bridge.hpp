@@ -46,6 +46,19 @@ std::vector<Edge> visibility_edges(const Mesh& mesh, const Mesh& cage);
 std::vector<double> score_planes(const std::vector<Plane>& planes, const std::vector<Vec3>& pts,
                                  const std::vector<Edge>& edges);
 
+// get_candidate_planes (lib/src/process.cpp:28-72) with the planes and their
+// near-duplicate filter on the GPU (visacd_candidate_planes): the edge draws
+// come from the process engine, which ends where the reference's loop leaves
+// it. Same planes, in the same order, as the host restatement.
+std::vector<Plane> candidate_planes(const std::vector<Vec3>& vertices, const std::vector<Edge>& edges,
+                                    int num_planes);
+
+// The split search of lib/src/process.cpp:96-134 on the GPU
+// (visacd_split_search): num_planes candidate planes, then the flat planes
+// with scores times flat_k; the first maximum. False when nothing is scored.
+bool split_search(const Mesh& mesh, const std::vector<Plane>& flat_planes, double flat_k,
+                  int num_planes, Plane& out);
+
 // Per-part clipping on the GPU (visacd_clip) + host cap: same parts and maps
 // as clip() in clip.cpp.
 MeshList clip(const Mesh& mesh, const Plane& plane, std::vector<int>& pos_map,

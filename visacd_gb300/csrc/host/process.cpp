@@ -92,16 +92,10 @@ namespace {
 
 // The reference's split-plane search (lib/src/process.cpp:96-134): 2500 random
 // candidates plus the flat-surface planes (scores x flat_surface_k), first
-// maximum. Returns false when there is nothing to score.
+// maximum, all on the GPU after the edge draws. Returns false when there is
+// nothing to score.
 bool exhaustive_plane(const Mesh& mesh, const std::vector<Plane>& flat_planes, Plane& out) {
-  std::vector<Plane> planes = get_candidate_planes(mesh.vertices, mesh.intersecting_edges, 2500);
-  const size_t flat_offset = planes.size();
-  planes.insert(planes.end(), flat_planes.begin(), flat_planes.end());
-  if (planes.empty() || mesh.intersecting_edges.empty()) return false;
-  std::vector<double> scores = gpu::score_planes(planes, mesh.vertices, mesh.intersecting_edges);
-  for (size_t i = flat_offset; i < planes.size(); ++i) scores[i] *= config().flat_surface_k;
-  out = planes[std::max_element(scores.begin(), scores.end()) - scores.begin()];
-  return true;
+  return gpu::split_search(mesh, flat_planes, config().flat_surface_k, 2500, out);
 }
 
 }  // namespace
@@ -178,7 +172,7 @@ bool learned_plane(const Mesh& mesh, const std::vector<Plane>& flat_planes, Plan
   planes.insert(planes.end(), refined.begin(), refined.end());
   const size_t n_prop = planes.size();
   std::vector<Plane> probe =
-      get_candidate_planes(mesh.vertices, mesh.intersecting_edges, config().proposer_probe_planes);
+      gpu::candidate_planes(mesh.vertices, mesh.intersecting_edges, config().proposer_probe_planes);
   planes.insert(planes.end(), probe.begin(), probe.end());
   const size_t flat_offset = planes.size();
   planes.insert(planes.end(), flat_planes.begin(), flat_planes.end());
