@@ -444,11 +444,11 @@ def run_learned_batch(args) -> dict:
         dt = time.perf_counter() - t0
         return dt, res, V._stage_times()
 
-    def batched(mode):
+    def batched(mode, seed_shift=0):
         V.config.plane_proposer = mode
         V._reset_counters()
         t0 = time.perf_counter()
-        res = V.process_batch(meshes, conc, nparts, seeds, args.c5_threads)
+        res = V.process_batch(meshes, conc, nparts, [s + seed_shift for s in seeds], args.c5_threads)
         return time.perf_counter() - t0, res, V._stage_times()
 
     try:
@@ -457,6 +457,14 @@ def run_learned_batch(args) -> dict:
         t_bl, r_bl, st_bl = batched("learned")
         _, r_alt, _ = sequential("exhaustive", 1000) if args.c5_noise else (None, None, None)
         _, _, st_l = sequential("learned") if args.c5_fallbacks else (None, None, None)
+        # Seed spread: the same meshes under other engine seeds, both methods
+        # (batched exhaustive results equal plain ones, so the batch runs them).
+        spread = []
+        for k in range(1, args.c5_seeds):
+            _, ra, _ = batched("exhaustive", 1000 * k)
+            _, rb, _ = batched("learned", 1000 * k)
+            spread.append((np.mean([r.concavity for r in ra]), np.mean([r.concavity for r in rb]),
+                           np.mean([r.num_parts for r in ra]), np.mean([r.num_parts for r in rb])))
     finally:
         V.config.plane_proposer = "exhaustive"
     n = len(seeds)
@@ -482,6 +490,21 @@ def run_learned_batch(args) -> dict:
         "stages_ms_batched_learned_thread_sum": {k: round(v, 1) if isinstance(v, float) else v
                                                  for k, v in st_bl.items()},
     }
+    if spread:
+        pm = [float(cp.mean())] + [float(x[0]) for x in spread]
+        lm = [float(cl.mean())] + [float(x[1]) for x in spread]
+        gaps = [b / a - 1.0 for a, b in zip(pm, lm)]
+        out["seed_spread"] = {
+            "engine_seeds": [f"seed + {1000 * k}" for k in range(args.c5_seeds)],
+            "concavity_plain_mean_per_seed": pm,
+            "concavity_learned_mean_per_seed": lm,
+            "parts_plain_mean_per_seed": [out["parts_plain_mean"]] + [float(x[2]) for x in spread],
+            "parts_learned_mean_per_seed": [out["parts_learned_mean"]] + [float(x[3]) for x in spread],
+            "gap_per_seed": gaps,
+            "gap_of_means_over_seeds": float(np.mean(lm) / np.mean(pm) - 1.0),
+            "plain_seed_to_seed_rel_std": float(np.std(pm, ddof=1) / np.mean(pm)),
+            "learned_seed_to_seed_rel_std": float(np.std(lm, ddof=1) / np.mean(lm)),
+        }
     if r_alt is not None:
         ca = np.array([r.concavity for r in r_alt])
         out["concavity_plain_reseeded_mean"] = float(ca.mean())
@@ -897,6 +920,8 @@ def main():
     ap.add_argument("--c5-threads", type=int, default=0, help="process_batch workers (0 = all cores)")
     ap.add_argument("--c5-noise", action="store_true", help="also run plain with other seeds (noise floor)")
     ap.add_argument("--c5-fallbacks", action="store_true", help="also run learned sequentially (fallback rate)")
+    ap.add_argument("--c5-seeds", type=int, default=4,
+                    help="engine seeds for the concavity spread of both methods (batched runs)")
     ap.add_argument("--micro", action="store_true", help="one small case per kernel family (for ncu)")
     args = ap.parse_args()
     if args.micro:

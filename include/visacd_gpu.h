@@ -217,16 +217,17 @@ typedef struct visacd_split_info {
   int32_t n_candidates;  /* candidate planes kept */
   int32_t draws_used;    /* draws the reference's candidate loop consumed */
   int32_t pad;
-  double best_score;     /* the winning score (flat planes: times flat_k) */
+  double best_score;     /* the winning float score (flat planes: times flat_k) */
 } visacd_split_info;
 
 /* The split-plane search of one part (lib/src/process.cpp:96-134) in one
    call: the candidate planes of visacd_candidate_planes, then the flat-surface
    planes (n_flat x 4 float64), all scored by visacd_score_planes' kernels
-   (FP32 points from the FP64 vertices), flat scores multiplied by flat_k, and
-   the first maximum in that order. best_plane: 4 float64 (the chosen
-   candidate's FP64 coefficients, or the flat plane's). Host pointers,
-   synchronous. */
+   (FP32 points from the FP64 vertices). As in the reference, the scores are
+   compared as float: flat scores are multiplied by flat_k in double and
+   rounded to float, and the first maximum in that order wins. best_plane: 4
+   float64 (the chosen candidate's FP64 coefficients, or the flat plane's).
+   Host pointers, synchronous. */
 int visacd_split_search(visacd_ctx* ctx, const double* verts, int32_t n, const uint32_t* edges,
                         int64_t E, const int32_t* draws, int32_t n_draws, int32_t num_planes,
                         const double* flat_planes, int32_t n_flat, double flat_k,

@@ -76,14 +76,16 @@ def test_split_search_picks_the_first_maximum(ctx, orc, flat_k):
     flat = np.concatenate([nrm, rng.uniform(-0.3, 0.3, (6, 1))], 1)
     flat = np.concatenate([flat, want[:2]])  # ties between a flat plane and a candidate
     planes = np.concatenate([want, flat])
-    s, _ = ctx.score_planes(planes.astype(np.float32), v.astype(np.float32), e)
-    s[len(want):] *= flat_k
+    s64, _ = ctx.score_planes(planes.astype(np.float32), v.astype(np.float32), e)
+    # the reference compares float scores; flat ones times flat_k in double
+    s = s64.astype(np.float32)
+    s[len(want):] = (s[len(want):].astype(np.float64) * flat_k).astype(np.float32)
     best = int(np.argmax(s))
     plane, info = ctx.split_search(v, e, draws, 2500, flat, flat_k)
     assert info["best_index"] == best
     assert info["n_candidates"] == len(want) and info["draws_used"] == used
     np.testing.assert_array_equal(plane, planes[best])
-    assert info["best_score"] == s[best]
+    assert info["best_score"] == float(s[best])
     # without flat planes, and with no scoreable edge
     plane, info = ctx.split_search(v, e, draws, 2500)
     assert info["best_index"] == int(np.argmax(s[: len(want)]))

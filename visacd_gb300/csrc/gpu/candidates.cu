@@ -252,7 +252,11 @@ __global__ void place_flat_kernel(const double* __restrict__ flat, int32_t F, in
   }
 }
 
-// First maximum over [kept candidates, flat planes x flat_k] in that order.
+// First maximum over [kept candidates, flat planes x flat_k] in that order,
+// compared as the reference compares them (lib/src/process.cpp:118-131): the
+// scores are float, and a flat plane's score is multiplied by flat_k in double
+// and stored back as float. Float rounding can make distinct exact sums equal,
+// and then the first of them wins, as in the reference.
 struct SplitOut {
   double plane[4];
   double score;
@@ -271,25 +275,25 @@ __global__ void split_argmax_kernel(const double* __restrict__ scores, const Pla
                                     SplitOut* __restrict__ out) {
   const int n_out = info[0];
   const int total = n_out + F;
-  double best = -1.0;
+  float best = -1.0f;
   int best_i = 0x7fffffff;
   for (int r = threadIdx.x; r < total; r += blockDim.x) {
     const int slot = r < n_out ? r : cand_slots + (r - n_out);
-    double s = scores[slot];
-    if (r >= n_out) s = __dmul_rn(s, flat_k);
+    float s = __double2float_rn(scores[slot]);
+    if (r >= n_out) s = __double2float_rn(__dmul_rn((double)s, flat_k));
     if (s > best || (s == best && r < best_i)) {
       best = s;
       best_i = r;
     }
   }
-  __shared__ double sv[1024];
+  __shared__ float sv[1024];
   __shared__ int si[1024];
   sv[threadIdx.x] = best;
   si[threadIdx.x] = best_i;
   __syncthreads();
   for (int o = blockDim.x / 2; o; o >>= 1) {
     if ((int)threadIdx.x < o) {
-      const double v2 = sv[threadIdx.x + o];
+      const float v2 = sv[threadIdx.x + o];
       const int i2 = si[threadIdx.x + o];
       if (v2 > sv[threadIdx.x] || (v2 == sv[threadIdx.x] && i2 < si[threadIdx.x])) {
         sv[threadIdx.x] = v2;
@@ -312,7 +316,7 @@ __global__ void split_argmax_kernel(const double* __restrict__ scores, const Pla
       const int slot = r < n_out ? r : cand_slots + (r - n_out);
       const Plane64 p = planes[slot];
       out->index = r;
-      out->score = sv[0];
+      out->score = (double)sv[0];
       out->plane[0] = p.x;
       out->plane[1] = p.y;
       out->plane[2] = p.z;

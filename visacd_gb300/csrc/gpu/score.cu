@@ -26,7 +26,7 @@
 namespace vgpu {
 
 template <int K>
-__global__ void __launch_bounds__(kScoreThreads, (K <= 4 ? 2 : 1))
+__global__ void __launch_bounds__(kScoreThreads, (K <= 4 ? 3 : 2))
     score_planes_kernel(const float4* __restrict__ planes, int32_t P,
                         const EdgeRec* __restrict__ recs, int64_t E, int64_t blocks_per_cta,
                         const unsigned* __restrict__ stats,
@@ -238,8 +238,10 @@ static int launch_score(visacd_ctx* ctx, const float4* planes, int32_t P, const 
   const int per_cta = kScoreThreads * K;
   const int groups = (P + per_cta - 1) / per_cta;
   const int64_t nblocks = (E + kEdgeBlock - 1) / kEdgeBlock;
-  // Aim for ~2 CTAs per SM in total; each CTA streams a contiguous run of blocks.
-  int64_t target_ctas = 2LL * ctx->sm_count;
+  // Aim for ~4 CTAs per SM in total (3 resident for K <= 4, 2 for K = 8, so
+  // the edge slices keep every SM busy to the end); each CTA streams a
+  // contiguous run of blocks.
+  int64_t target_ctas = 4LL * ctx->sm_count;
   int64_t slices = (target_ctas + groups - 1) / groups;
   if (slices > nblocks) slices = nblocks;
   if (slices < 1) slices = 1;
@@ -507,7 +509,7 @@ static int noalloc_launch_score(cudaStream_t st, int sm_count, const float4* pla
   const int per_cta = kScoreThreads * K;
   const int groups = (P + per_cta - 1) / per_cta;
   const int64_t nblocks = (E + kEdgeBlock - 1) / kEdgeBlock;
-  int64_t slices = (2LL * sm_count + groups - 1) / groups;
+  int64_t slices = (4LL * sm_count + groups - 1) / groups;
   if (slices > nblocks) slices = nblocks;
   if (slices < 1) slices = 1;
   int64_t per = (nblocks + slices - 1) / slices;

@@ -171,7 +171,10 @@ def refine(prop: np.ndarray, bis: np.ndarray, per: int = 8, half: float = 1.0) -
 def evaluate(ctx, lp, seeds, probe: int = 64, tol: float = 0.01, per: int = 8):
     """Per held-out blob: exhaustive best score, best proposal score, best probe
     score (the reference's draw limited to `probe` planes after
-    set_seed(seed + 1)), and the score of the plane the learned rule picks."""
+    set_seed(seed + 1)), the score of the plane the learned rule picks, and the
+    method without the network at the same budget: the reference's draw of as
+    many planes as the learned rule scores (proposals + refined + probe), after
+    set_seed(seed + 2)."""
     import visacd_gb300.visacd as V
     rows = []
     for seed in seeds:
@@ -192,15 +195,22 @@ def evaluate(ctx, lp, seeds, probe: int = 64, tol: float = 0.01, per: int = 8):
         V.set_seed(seed + 1)
         pr = np.asarray(V._candidate_planes(v, edges, probe), dtype=np.float64).reshape(-1, 4)
         qs, _ = ctx.score_planes(pr, v, edges) if len(pr) else (np.zeros(1), None)
+        budget = len(prop) + len(ref) + len(pr)
+        V.set_seed(seed + 2)
+        nn = np.asarray(V._candidate_planes(v, edges, budget), dtype=np.float64).reshape(-1, 4)
+        ns, _ = ctx.score_planes(nn, v, edges) if len(nn) else (np.zeros(1), None)
         best, bp, bq = float(scores.max()), float(ps.max()), float(qs.max())
         fallback = bp < (1.0 - tol) * bq
         chosen = best if fallback else max(bp, bq)
         rows.append({"seed": int(seed), "edges": int(len(edges)), "exhaustive": best, "raw": raw,
                      "refined_planes": int(len(ref)), "proposal": bp,
-                     "probe": bq, "fallback": bool(fallback), "chosen": chosen})
+                     "probe": bq, "fallback": bool(fallback), "chosen": chosen,
+                     "learned_no_fallback": max(bp, bq), "budget": int(budget),
+                     "no_network": float(ns.max())})
     r = np.array([[x["proposal"] / x["exhaustive"], x["probe"] / x["exhaustive"],
                    x["chosen"] / x["exhaustive"], x["fallback"], x["raw"] / x["exhaustive"],
-                   x["refined_planes"]] for x in rows])
+                   x["refined_planes"], x["learned_no_fallback"] / x["exhaustive"],
+                   x["no_network"] / x["exhaustive"], x["budget"]] for x in rows])
     summary = {
         "blobs": len(rows),
         "mean_raw_proposal_ratio": float(r[:, 4].mean()),
@@ -211,6 +221,11 @@ def evaluate(ctx, lp, seeds, probe: int = 64, tol: float = 0.01, per: int = 8):
         "fallback_rate": float(r[:, 3].mean()),
         "mean_chosen_ratio": float(r[:, 2].mean()),
         "frac_chosen_within_1pct": float((r[:, 2] >= 0.99).mean()),
+        "mean_planes_scored": float(r[:, 8].mean()),
+        "mean_learned_no_fallback_ratio": float(r[:, 6].mean()),
+        "frac_learned_no_fallback_within_1pct": float((r[:, 6] >= 0.99).mean()),
+        "mean_no_network_same_budget_ratio": float(r[:, 7].mean()),
+        "frac_no_network_same_budget_within_1pct": float((r[:, 7] >= 0.99).mean()),
     }
     return summary, rows
 
