@@ -145,6 +145,21 @@ int visacd_visibility(visacd_ctx* ctx, const float* pts, int32_t n, const uint8_
                       int64_t* n_edges, visacd_vis_stats* stats);
 /* Copy the last visibility result (2 x n_edges uint32, i < j) to host memory. */
 int visacd_visibility_edges(visacd_ctx* ctx, uint32_t* edges_out, int64_t capacity_edges);
+/* Several parts in one call: the pending sub-parts of a decomposition step.
+   Part p has n_pts[p] points pts[p] (float32 n x 3, host), an optional is_new
+   mask (is_new may be NULL, or is_new[p] NULL for an unmasked part), its own
+   BVH and its cage BVH. Each part is prepared on its own (Morton order, the
+   masked rows), then one persistent visibility launch covers the work items of
+   all parts and one compaction emits every part's edges, parts in order, each
+   as visacd_visibility would (row-major, its own vertex indices). n_edges[p]
+   gets part p's edge count; visacd_visibility_edges then returns all of them
+   concatenated. stats (may be NULL) sums the counters over the parts. Results
+   equal one visacd_visibility call per part. Replaces the per-part
+   compute_intersection_matrix calls of lib/src/process.cpp:165-178. */
+int visacd_visibility_batch(visacd_ctx* ctx, int32_t n_parts, const float* const* pts,
+                            const int32_t* n_pts, const uint8_t* const* is_new,
+                            const visacd_bvh* const* self_bvhs, const visacd_bvh* const* cage_bvhs,
+                            int64_t* n_edges, visacd_vis_stats* stats);
 /* Device pointer to the last visibility result (valid until the next call). */
 int visacd_visibility_edges_device(visacd_ctx* ctx, const uint32_t** d_edges, int64_t* n_edges);
 

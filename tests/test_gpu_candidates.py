@@ -46,13 +46,15 @@ def test_candidate_planes_bit_exact(ctx, orc, case, seed):
         v = np.concatenate([v, v[e[:40, 0]]])
         extra = np.stack([e[:40, 0], len(v) - 40 + np.arange(40)], 1).astype(np.uint32)
         e = np.concatenate([extra, e[:200]])
+    kept = {}
     for num in (2500, 64):
         want, draws, used = orc.candidate_planes_with_draws(v, e, num, seed)
         got, got_used = ctx.candidate_planes(v, e, draws, num)
         np.testing.assert_array_equal(got, want)
         assert got_used == used
-    if case == "near_duplicates":
-        assert 0 < len(want) < 64
+        kept[num] = len(want)
+    if case == "near_duplicates":  # many draws dropped as similar
+        assert 0 < kept[2500] < 2500
 
 
 def test_candidate_planes_edge_cases(ctx, orc):

@@ -203,3 +203,34 @@ def test_bvh_depth_on_clustered_and_degenerate_meshes(ctx, orc):
     ct = np.array([[0, 2, 1], [0, 3, 2], [4, 5, 6], [4, 6, 7], [0, 1, 5], [0, 5, 4],
                    [1, 2, 6], [1, 6, 5], [2, 3, 7], [2, 7, 6], [3, 0, 4], [3, 4, 7]], np.int32)
     _compare(ctx, orc, v3[::8], np.zeros((0, 3), np.int32), cv, ct)
+
+
+def test_visibility_batch_equals_per_part_calls(ctx, orc):
+    """Several parts of uneven size in one call (one persistent launch over
+    all parts' work items): unmasked, masked and tiny parts give the edges of
+    one call per part, in part order."""
+    rng = np.random.default_rng(3)
+    parts = []
+    for level, seed, masked in [(3, 1, False), (2, 2, True), (3, 3, True), (2, 4, False)]:
+        v, t = mg.displaced_blob(level, seed=seed)
+        cv, ct = mg.offset_cage(v, t, 0.03)
+        m = (rng.random(len(v)) < 0.15).astype(np.uint8) if masked else None
+        parts.append((v, ctx.bvh(v, t), ctx.bvh(cv, ct), m))
+    tiny = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float64)
+    parts.append((tiny[:1], ctx.bvh(tiny[:1], np.zeros((0, 3), np.int32)), parts[0][2], None))
+    got, st = ctx.visibility_batch(parts)
+    assert len(got) == len(parts)
+    pairs = 0
+    for (v, sb, cb, m), e in zip(parts, got):
+        want, s1 = ctx.visibility(v, sb, cb, is_new=m)
+        np.testing.assert_array_equal(e, want)
+        pairs += s1["pairs_tested"]
+    assert st["pairs_tested"] == pairs
+    # the batch is what the oracle gives for a masked part too
+    v, sb, cb, m = parts[1]
+    t = mg.displaced_blob(2, seed=2)[1]
+    bits, _, _ = orc.visibility(v, t, *mg.offset_cage(v, t, 0.03), is_new=m)
+    k = orc.linear_from_pairs(got[1], len(v)) if len(got[1]) else np.zeros(0, np.int64)
+    gb = np.zeros(len(bits), bool)
+    gb[k] = True
+    assert not np.any((gb != (bits & 1).astype(bool)) & ~(bits & 2).astype(bool))

@@ -32,7 +32,7 @@ EXPORTED = [
     "visacd_lp_train_step",
     "visacd_sdf_remesh", "visacd_sdf_fetch", "visacd_hull_distances", "visacd_segment_triangle_tests",
     "visacd_set_blocking_sync", "visacd_lp_set_tcgen05", "visacd_ctx_set_blocking_wait",
-    "visacd_candidate_planes", "visacd_split_search",
+    "visacd_candidate_planes", "visacd_split_search", "visacd_visibility_batch",
 ]
 
 LP_POINTS = 2048
@@ -105,6 +105,8 @@ def load() -> C.CDLL:
     lib.visacd_score_planes.argtypes = [P, P, i32, P, i32, P, i64, C.c_int, P,
                                         C.POINTER(ScoreStats)]
     lib.visacd_score_planes_noalloc.argtypes = [P, i32, P, i32, P, i64, P, P, P]
+    lib.visacd_visibility_batch.argtypes = [P, i32, C.POINTER(P), P, C.POINTER(P), C.POINTER(P),
+                                            C.POINTER(P), P, C.POINTER(VisStats)]
     lib.visacd_candidate_planes.argtypes = [P, P, i32, P, i64, P, i32, i32, P, C.POINTER(i32),
                                             C.POINTER(i32)]
     lib.visacd_split_search.argtypes = [P, P, i32, P, i64, P, i32, i32, P, i32, C.c_double, P,
@@ -239,6 +241,30 @@ class Context:
                                        cage_bvh.handle, C.byref(ne), C.byref(st)), "visacd_visibility")
         out = np.empty((ne.value, 2), dtype=np.uint32)
         _check(lib().visacd_visibility_edges(self._h, _ptr(out), ne.value), "visibility_edges")
+        return out, st.as_dict()
+
+    def visibility_batch(self, parts):
+        """Several parts in one call: parts = [(pts, self_bvh, cage_bvh, is_new or None)].
+        Returns (list of per-part edge arrays, summed counters)."""
+        K = len(parts)
+        pts = [_f32(p[0], 3) for p in parts]
+        masks = [None if p[3] is None else np.ascontiguousarray(np.asarray(p[3], dtype=np.uint8)) for p in parts]
+        pp = (C.c_void_p * K)(*[x.ctypes.data for x in pts])
+        mp = (C.c_void_p * K)(*[None if m is None else m.ctypes.data for m in masks])
+        n = np.array([len(x) for x in pts], np.int32)
+        sb = (C.c_void_p * K)(*[p[1].handle.value for p in parts])
+        cb = (C.c_void_p * K)(*[p[2].handle.value for p in parts])
+        ne = np.zeros(K, np.int64)
+        st = VisStats()
+        _check(lib().visacd_visibility_batch(self._h, K, pp, _ptr(n), mp, sb, cb, _ptr(ne), C.byref(st)),
+               "visacd_visibility_batch")
+        total = int(ne.sum())
+        flat = np.empty((total, 2), dtype=np.uint32)
+        _check(lib().visacd_visibility_edges(self._h, _ptr(flat), total), "visibility_edges")
+        out, at = [], 0
+        for k in range(K):
+            out.append(flat[at:at + ne[k]])
+            at += int(ne[k])
         return out, st.as_dict()
 
     def set_vis_variant(self, v: int) -> None:

@@ -547,13 +547,16 @@ extern "C" int visacd_split_search(visacd_ctx* ctx, const double* verts, int32_t
     VCHECK(attempt == 0, VISACD_ERR_DEVICE, "split_search: FP64 queue overflow after a rerun");
     rcap = h->recheck_count;
   }
+  // The read-back shares the pinned staging area with the status check: copy
+  // it out first.
+  const SplitOut r = *h;
   VTRY(check_status(ctx, "split_search"));
-  for (int c = 0; c < 4; ++c) best_plane[c] = h->plane[c];
+  for (int c = 0; c < 4; ++c) best_plane[c] = r.plane[c];
   if (info) {
-    info->best_index = h->index;
-    info->n_candidates = h->n_planes;
-    info->draws_used = h->draws_used;
-    info->best_score = h->score;
+    info->best_index = r.index;
+    info->n_candidates = r.n_planes;
+    info->draws_used = r.draws_used;
+    info->best_score = r.score;
   }
   return VISACD_OK;
 }

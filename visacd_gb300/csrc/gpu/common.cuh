@@ -116,6 +116,7 @@ enum CtxSlot {
   kSlotSegTri,
   kSlotCandidates,
   kSlotCandLinks,
+  kSlotVisMulti,
   kSlotCount
 };
 

@@ -136,9 +136,8 @@ __device__ __forceinline__ void plane_thresholds(float4 pl, const unsigned* stat
 // is a certain crossing when the signs differ and m = min(|v1|, |v2|) > th
 // (th = eps + B, the negated nhi above); it lies in the rounding band when
 // m is in [eps - B, th]. With dh = th - m (FP32), "m > th" is the sign bit of
-// dh, and "the signs differ" is the sign bit of the product v1 v2 (IEEE gives
-// the product the exclusive or of the signs, also for zeros and overflow), so
-// the certain test is one logic op: bit 31 of (v1 v2) & dh. For m <= th,
+// dh, so the certain test is one logic op on sign bits: bit 31 of
+// (v1 ^ v2) & dh. For m <= th,
 // dh >= +0 and its bits order like the values, while dh < 0 has bit 31 set;
 // so the smallest dh (as unsigned bits) over a block is at most the bits of
 // th - (eps - B) exactly when some pair of the block may be in the band. Such
@@ -166,9 +165,10 @@ __device__ __forceinline__ PlaneAcc plane_acc(float4 pl, const unsigned* stats) 
 // One shared-memory block of cnt edge records against K planes: acc[k] gets
 // the quantised length of every certain crossing, dmin[k] the smallest dh
 // bits (the band flag). Per (plane, edge): 3 packed FMAs, the FP32 add and
-// product, and the accumulation on the FMA pipe; min-abs, the sign logic and
-// the unsigned min on the integer side. The accumulation adds the high word
-// of (sign bit) x (2 q): 2^31 x 2q / 2^32 = q for a crossing, 0 otherwise.
+// the multiply-add of the masked length on the FMA pipe; min-abs, the sign
+// logic, the shift and the unsigned min on the integer side. (Moving the
+// shift to the FMA pipe as a high-word multiply measured slower: that pipe
+// then limits.)
 template <int K>
 __device__ __forceinline__ void score_edge_block(const ulonglong2* __restrict__ s, int cnt,
                                                  const PlaneAcc (&pa)[K], uint32_t (&acc)[K],
@@ -177,7 +177,7 @@ __device__ __forceinline__ void score_edge_block(const ulonglong2* __restrict__ 
   for (int e = 0; e < cnt; ++e) {
     const ulonglong2 r0 = s[2 * e];      // (x1,x2), (y1,y2)
     const ulonglong2 r1 = s[2 * e + 1];  // (z1,z2), (q,pad)
-    const uint32_t q2 = (uint32_t)(r1.y & 0xffffffffull) << 1;
+    const uint32_t q = (uint32_t)(r1.y & 0xffffffffull);
 #pragma unroll
     for (int k = 0; k < K; ++k) {
       unsigned long long v = ffma2(pa[k].c2, r1.x, pa[k].d2);
@@ -187,9 +187,8 @@ __device__ __forceinline__ void score_edge_block(const ulonglong2* __restrict__ 
       unpack2(v, v1, v2);
       const float m = fminf(fabsf(v1), fabsf(v2));
       const float dh = __fsub_rn(pa[k].th, m);
-      const float pr = __fmul_rn(v1, v2);
-      const uint32_t c = __float_as_uint(pr) & __float_as_uint(dh) & 0x80000000u;
-      acc[k] += __umulhi(c, q2);
+      const uint32_t c = (__float_as_uint(v1) ^ __float_as_uint(v2)) & __float_as_uint(dh);
+      acc[k] += (c >> 31) * q;
       dmin[k] = min(dmin[k], __float_as_uint(dh));
     }
   }

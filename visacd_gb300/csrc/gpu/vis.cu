@@ -82,93 +82,141 @@ __global__ void tile_row_counts_kernel(int64_t ntr, int64_t ntc, int TR, int TC,
   }
 }
 
+// Per-lane counters of a visibility launch, reduced over the warp at the end.
+struct VisLaneCounters {
+  unsigned long long pairs = 0, edges = 0, self = 0, cage = 0, deg = 0;
+  unsigned rechecks = 0, status_bits = 0, visits = 0, tri_tests = 0;
+};
+
+// One tile (work item w of P's tile space) for the calling warp: the cage
+// test, then the self test for lanes whose segment leaves the cage, and the
+// edge bits.
+template <int TR>
+__device__ __forceinline__ void vis_tile(const VisParams& P, unsigned long long w, int lane,
+                                         int* __restrict__ wstk, VisLaneCounters& c) {
+  constexpr int TC = 32 / TR;
+  const int64_t n = P.n;
+  int64_t tr, tc;
+  tile_of(P, w, tr, tc, TR, TC);
+  const int64_t a = tr * TR + lane / TC;
+  const int64_t b = tc * TC + lane % TC;
+  bool valid;
+  uint32_t oi = 0, oj = 0;
+  if (P.triangular) {
+    valid = a < b && b < P.nc;
+    if (valid) {
+      oi = P.rows[a];
+      oj = P.cols[b];
+    }
+  } else {
+    valid = a < P.nr && b < P.nc;
+    if (valid) {
+      oi = P.rows[a];
+      oj = P.cols[b];
+      valid = oi != oj && (!P.is_new[oj] || P.newrank[oj] > a);
+    }
+  }
+  const uint32_t i = min(oi, oj), j = max(oi, oj);
+  Seg s;
+  float3 p = make_float3(0.f, 0.f, 0.f), q = make_float3(0.f, 0.f, 0.f);
+  if (valid) {
+    ++c.pairs;
+    p = make_float3(P.pts[3 * (int64_t)i], P.pts[3 * (int64_t)i + 1], P.pts[3 * (int64_t)i + 2]);
+    q = make_float3(P.pts[3 * (int64_t)j], P.pts[3 * (int64_t)j + 1], P.pts[3 * (int64_t)j + 2]);
+  }
+  make_seg(s, p, q, (int)i, (int)j);
+  bool active = valid;
+  if (valid && !(seg_len(s) > 0.f)) {  // coincident endpoints (or NaN): never an edge
+    ++c.deg;
+    active = false;
+  }
+  if (!__ballot_sync(0xffffffffu, active)) return;
+  // The cage first: few segments leave it, so the self test runs for few.
+  s.exclude = false;
+  const bool cage_hit = packet_any_hit(P.cage_nodes, P.cage_tris, P.cage_nt, s, P.pts, active, wstk,
+                                       c.rechecks, c.status_bits, c.visits, c.tri_tests);
+  if (active && cage_hit) ++c.cage;
+  active = active && cage_hit;
+  s.exclude = true;
+  const bool self_hit = packet_any_hit(P.self_nodes, P.self_tris, P.self_nt, s, P.pts, active, wstk,
+                                       c.rechecks, c.status_bits, c.visits, c.tri_tests);
+  if (active && self_hit) ++c.self;
+  if (active && !self_hit) {
+    ++c.edges;
+    const int64_t k = row_start(i, n) + (int64_t)(j - i - 1);
+    atomicOr(&P.bitset[k >> 5], 1u << (k & 31));
+  }
+}
+
+__device__ __forceinline__ void vis_flush_counters(VisCounters* cnt, unsigned* status, int lane,
+                                                   VisLaneCounters& c) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    c.pairs += __shfl_xor_sync(0xffffffffu, c.pairs, o);
+    c.edges += __shfl_xor_sync(0xffffffffu, c.edges, o);
+    c.self += __shfl_xor_sync(0xffffffffu, c.self, o);
+    c.cage += __shfl_xor_sync(0xffffffffu, c.cage, o);
+    c.deg += __shfl_xor_sync(0xffffffffu, c.deg, o);
+    c.rechecks += __shfl_xor_sync(0xffffffffu, c.rechecks, o);
+    c.tri_tests += __shfl_xor_sync(0xffffffffu, c.tri_tests, o);
+    c.status_bits |= __shfl_xor_sync(0xffffffffu, c.status_bits, o);
+  }
+  if (lane == 0) {
+    atomicAdd(&cnt->pairs, c.pairs);
+    atomicAdd(&cnt->edges, c.edges);
+    atomicAdd(&cnt->self_hits, c.self);
+    atomicAdd(&cnt->cage_hits, c.cage);
+    atomicAdd(&cnt->degenerate, c.deg);
+    atomicAdd(&cnt->rechecks, (unsigned long long)c.rechecks);
+    atomicAdd(&cnt->node_visits, (unsigned long long)c.visits);
+    atomicAdd(&cnt->tri_tests, (unsigned long long)c.tri_tests);
+    if (c.status_bits) atomicOr(status, c.status_bits);
+  }
+}
+
 template <int TR, int MINB>
 __global__ void __launch_bounds__(kVisThreads, MINB) visibility_kernel(VisParams P) {
-  constexpr int TC = 32 / TR;
   __shared__ int stk_all[kStack * (kVisThreads / 32)];
   const int lane = threadIdx.x & 31;
   int* wstk = stk_all + (threadIdx.x >> 5) * kStack;
-  unsigned long long c_pairs = 0, c_edges = 0, c_self = 0, c_cage = 0, c_deg = 0;
-  unsigned rechecks = 0, status_bits = 0, visits = 0, tri_tests = 0;
-  const int64_t n = P.n;
+  VisLaneCounters c;
   for (int guard = 0; guard < (1 << 30); ++guard) {
     unsigned long long w = 0;
     if (lane == 0) w = atomicAdd(&P.cnt->work, 1ull);
     w = __shfl_sync(0xffffffffu, w, 0);
     if (w >= P.total_tiles) break;
-    int64_t tr, tc;
-    tile_of(P, w, tr, tc, TR, TC);
-    const int64_t a = tr * TR + lane / TC;
-    const int64_t b = tc * TC + lane % TC;
-    bool valid;
-    uint32_t oi = 0, oj = 0;
-    if (P.triangular) {
-      valid = a < b && b < P.nc;
-      if (valid) {
-        oi = P.rows[a];
-        oj = P.cols[b];
-      }
-    } else {
-      valid = a < P.nr && b < P.nc;
-      if (valid) {
-        oi = P.rows[a];
-        oj = P.cols[b];
-        valid = oi != oj && (!P.is_new[oj] || P.newrank[oj] > a);
-      }
-    }
-    const uint32_t i = min(oi, oj), j = max(oi, oj);
-    Seg s;
-    float3 p = make_float3(0.f, 0.f, 0.f), q = make_float3(0.f, 0.f, 0.f);
-    if (valid) {
-      ++c_pairs;
-      p = make_float3(P.pts[3 * (int64_t)i], P.pts[3 * (int64_t)i + 1], P.pts[3 * (int64_t)i + 2]);
-      q = make_float3(P.pts[3 * (int64_t)j], P.pts[3 * (int64_t)j + 1], P.pts[3 * (int64_t)j + 2]);
-    }
-    make_seg(s, p, q, (int)i, (int)j);
-    bool active = valid;
-    if (valid && !(seg_len(s) > 0.f)) {  // coincident endpoints (or NaN): never an edge
-      ++c_deg;
-      active = false;
-    }
-    if (!__ballot_sync(0xffffffffu, active)) continue;
-    // The cage first: few segments leave it, so the self test runs for few.
-    s.exclude = false;
-    const bool cage_hit = packet_any_hit(P.cage_nodes, P.cage_tris, P.cage_nt, s, P.pts, active, wstk,
-                                         rechecks, status_bits, visits, tri_tests);
-    if (active && cage_hit) ++c_cage;
-    active = active && cage_hit;
-    s.exclude = true;
-    const bool self_hit = packet_any_hit(P.self_nodes, P.self_tris, P.self_nt, s, P.pts, active, wstk,
-                                         rechecks, status_bits, visits, tri_tests);
-    if (active && self_hit) ++c_self;
-    if (active && !self_hit) {
-      ++c_edges;
-      const int64_t k = row_start(i, n) + (int64_t)(j - i - 1);
-      atomicOr(&P.bitset[k >> 5], 1u << (k & 31));
-    }
+    vis_tile<TR>(P, w, lane, wstk, c);
   }
-#pragma unroll
-  for (int o = 16; o; o >>= 1) {
-    c_pairs += __shfl_xor_sync(0xffffffffu, c_pairs, o);
-    c_edges += __shfl_xor_sync(0xffffffffu, c_edges, o);
-    c_self += __shfl_xor_sync(0xffffffffu, c_self, o);
-    c_cage += __shfl_xor_sync(0xffffffffu, c_cage, o);
-    c_deg += __shfl_xor_sync(0xffffffffu, c_deg, o);
-    rechecks += __shfl_xor_sync(0xffffffffu, rechecks, o);
-    tri_tests += __shfl_xor_sync(0xffffffffu, tri_tests, o);
-    status_bits |= __shfl_xor_sync(0xffffffffu, status_bits, o);
+  vis_flush_counters(P.cnt, P.status, lane, c);
+}
+
+// Many parts in one persistent launch: the work items of all parts are
+// numbered consecutively (part p owns [tile_start[p], tile_start[p + 1])),
+// and each warp finds the part of its item by binary search. Every part keeps
+// its own tile space, mask and bitset region; the counters are shared.
+template <int TR, int MINB>
+__global__ void __launch_bounds__(kVisThreads, MINB)
+    visibility_multi_kernel(const VisParams* __restrict__ parts, int n_parts,
+                            const unsigned long long* __restrict__ tile_start,
+                            unsigned long long total_tiles, VisCounters* __restrict__ cnt,
+                            unsigned* __restrict__ status) {
+  __shared__ int stk_all[kStack * (kVisThreads / 32)];
+  const int lane = threadIdx.x & 31;
+  int* wstk = stk_all + (threadIdx.x >> 5) * kStack;
+  VisLaneCounters c;
+  for (int guard = 0; guard < (1 << 30); ++guard) {
+    unsigned long long w = 0;
+    if (lane == 0) w = atomicAdd(&cnt->work, 1ull);
+    w = __shfl_sync(0xffffffffu, w, 0);
+    if (w >= total_tiles) break;
+    int lo = 0, hi = n_parts - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (tile_start[mid] <= w) lo = mid; else hi = mid - 1;
+    }
+    vis_tile<TR>(parts[lo], w - tile_start[lo], lane, wstk, c);
   }
-  if (lane == 0) {
-    atomicAdd(&P.cnt->pairs, c_pairs);
-    atomicAdd(&P.cnt->edges, c_edges);
-    atomicAdd(&P.cnt->self_hits, c_self);
-    atomicAdd(&P.cnt->cage_hits, c_cage);
-    atomicAdd(&P.cnt->degenerate, c_deg);
-    atomicAdd(&P.cnt->rechecks, (unsigned long long)rechecks);
-    atomicAdd(&P.cnt->node_visits, (unsigned long long)visits);
-    atomicAdd(&P.cnt->tri_tests, (unsigned long long)tri_tests);
-    if (status_bits) atomicOr(P.status, status_bits);
-  }
+  vis_flush_counters(cnt, status, lane, c);
 }
 
 // ---- vertex ordering ------------------------------------------------------
@@ -500,6 +548,294 @@ static int vis_device(visacd_ctx* ctx, const float* d_pts, int32_t n, const uint
   return VISACD_OK;
 }
 
+// ---- several parts in one launch ------------------------------------------
+// The edge list of all parts: word w of the concatenated bitset belongs to the
+// part found by binary search over the parts' first words; its edges go to
+// the global offset of the word (parts stay in order, each row-major).
+__global__ void multi_emit_kernel(const VisParams* __restrict__ parts, int n_parts,
+                                  const unsigned long long* __restrict__ word_start,
+                                  const uint32_t* __restrict__ bits, int64_t nw,
+                                  const uint64_t* __restrict__ off, uint32_t* __restrict__ edges) {
+  for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < nw;
+       w += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t m = bits[w];
+    if (!m) continue;
+    int lo = 0, hi = n_parts - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (word_start[mid] <= (unsigned long long)w) lo = mid; else hi = mid - 1;
+    }
+    const int64_t n = parts[lo].n;
+    const int64_t k0 = (w - (int64_t)word_start[lo]) * 32;
+    uint64_t o = off[w];
+    double b2 = (double)(2 * n - 1);
+    double disc = b2 * b2 - 8.0 * (double)k0;
+    int64_t i = (int64_t)((b2 - sqrt(disc > 0 ? disc : 0.0)) * 0.5);
+    if (i < 0) i = 0;
+    if (i > n - 2) i = n - 2;
+    while (i > 0 && row_start(i, n) > k0) --i;
+    while (i + 1 <= n - 2 && row_start(i + 1, n) <= k0) ++i;
+    while (m) {
+      const int bpos = __ffs(m) - 1;
+      m &= m - 1;
+      const int64_t k = k0 + bpos;
+      while (i + 1 <= n - 2 && row_start(i + 1, n) <= k) ++i;
+      const int64_t j = k - row_start(i, n) + i + 1;
+      edges[2 * o] = (uint32_t)i;
+      edges[2 * o + 1] = (uint32_t)j;
+      ++o;
+    }
+  }
+}
+
+// Edge offsets of the parts' first words (and the total) for the read-back.
+__global__ void multi_part_offsets_kernel(const unsigned long long* __restrict__ word_start, int n_parts,
+                                          const uint64_t* __restrict__ off, uint64_t* __restrict__ out) {
+  for (int p = threadIdx.x; p <= n_parts; p += blockDim.x) out[p] = off[word_start[p]];
+}
+
+// Rows of a masked part (new vertices in Morton order) and their count.
+__global__ void copy_count_kernel(const uint64_t* __restrict__ off, int32_t n, int32_t* __restrict__ out) {
+  *out = (int32_t)off[n];
+}
+
+int visibility_multi_impl(visacd_ctx* ctx, int32_t n_parts, const float* const* pts, const int32_t* n_pts,
+                          const uint8_t* const* is_new, const visacd_bvh* const* self_bvhs,
+                          const visacd_bvh* const* cage_bvhs, int64_t* n_edges, visacd_vis_stats* stats) {
+  VCHECK(ctx && n_parts > 0 && pts && n_pts && self_bvhs && cage_bvhs && n_edges, VISACD_ERR_INVALID_ARG,
+         "visibility_batch: null argument");
+  VCUDA(cudaSetDevice(ctx->device));
+  constexpr int TR = 8, TC = 4;
+  // Layout of the per-part arrays in one buffer (256-byte aligned pieces).
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  std::vector<size_t> o_pts(n_parts), o_mask(n_parts), o_perm(n_parts), o_rows(n_parts),
+      o_rank(n_parts), o_rs(n_parts);
+  std::vector<int64_t> ntr_tri(n_parts, 0);
+  size_t total = al(sizeof(int32_t) * (size_t)n_parts);  // masked row counts
+  const size_t o_nr = 0;
+  unsigned long long words = 0;
+  std::vector<unsigned long long> word_start(n_parts + 1);
+  for (int p = 0; p < n_parts; ++p) {
+    const int32_t n = n_pts[p];
+    const visacd_bvh* sb = self_bvhs[p];
+    const visacd_bvh* cb = cage_bvhs[p];
+    VCHECK(n >= 0 && (n == 0 || pts[p]) && sb && cb, VISACD_ERR_INVALID_ARG, "visibility_batch: bad part %d", p);
+    VCHECK(n <= (1 << 24), VISACD_ERR_INVALID_ARG, "visibility_batch: part %d has n = %d above 2^24", p, n);
+    VCHECK(sb->ctx && cb->ctx && sb->device == ctx->device && cb->device == ctx->device,
+           VISACD_ERR_INVALID_ARG, "visibility_batch: part %d BVH is not on this context's device", p);
+    VCHECK(sb->depth <= kStack && cb->depth <= kStack, VISACD_ERR_INVALID_ARG,
+           "visibility_batch: part %d BVH depth %d/%d exceeds the traversal stack (%d)", p, sb->depth,
+           cb->depth, kStack);
+    VCHECK(sb->nt == 0 || sb->nv == n, VISACD_ERR_INVALID_ARG,
+           "visibility_batch: part %d self BVH has %d vertices, points have %d", p, sb->nv, n);
+    o_pts[p] = total;  total += al((size_t)std::max(n, 1) * 12);
+    o_mask[p] = total; total += al((size_t)std::max(n, 1));
+    o_perm[p] = total; total += al((size_t)std::max(n, 1) * 4);
+    o_rows[p] = total; total += al((size_t)std::max(n, 1) * 4);
+    o_rank[p] = total; total += al((size_t)std::max(n, 1) * 4);
+    ntr_tri[p] = (n + TR - 1) / TR;
+    o_rs[p] = total;   total += al((size_t)(ntr_tri[p] + 1) * 8);
+    word_start[p] = words;
+    const unsigned long long np = (unsigned long long)n * (unsigned long long)(n > 0 ? n - 1 : 0) / 2;
+    words += (np + 31) / 32;
+  }
+  word_start[n_parts] = words;
+  const size_t o_desc = total;
+  total += al(sizeof(VisParams) * (size_t)n_parts);
+  const size_t o_tiles = total;
+  total += al(8 * (size_t)(n_parts + 1));
+  const size_t o_words = total;
+  total += al(8 * (size_t)(n_parts + 1));
+  const size_t o_poff = total;
+  total += al(8 * (size_t)(n_parts + 1));
+  VTRY(ensure_slot(ctx, kSlotVisMulti, total));
+  char* base = slot<char>(ctx, kSlotVisMulti);
+  // Upload points, masks and the triangular tile-row starts.
+  {
+    size_t up_bytes = 0;
+    for (int p = 0; p < n_parts; ++p) up_bytes += (size_t)n_pts[p] * 13 + (size_t)(ntr_tri[p] + 1) * 8;
+    Stager up(ctx);
+    VTRY(up.reserve(up_bytes + 8 * (size_t)(n_parts + 1), 3 * n_parts + 1));
+    std::vector<uint64_t> rs;
+    for (int p = 0; p < n_parts; ++p) {
+      const int32_t n = n_pts[p];
+      if (n) VTRY(up.put(base + o_pts[p], pts[p], (size_t)n * 12));
+      if (n && is_new && is_new[p]) VTRY(up.put(base + o_mask[p], is_new[p], (size_t)n));
+      const int64_t ntr = ntr_tri[p], ntc = (n + TC - 1) / TC;
+      rs.assign((size_t)ntr + 1, 0);
+      for (int64_t r = 0; r < ntr; ++r) {
+        const int64_t c = ntc - (r * TR) / TC;
+        rs[r + 1] = rs[r] + (uint64_t)(c > 0 ? c : 0);
+      }
+      VTRY(up.put(base + o_rs[p], rs.data(), rs.size() * 8));
+    }
+    VTRY(up.put(base + o_words, word_start.data(), 8 * (size_t)(n_parts + 1)));
+  }
+  // Morton order of each part; rows and ranks of the masked ones.
+  int32_t* d_nr = reinterpret_cast<int32_t*>(base + o_nr);
+  for (int p = 0; p < n_parts; ++p) {
+    const int32_t n = n_pts[p];
+    if (n < 2) continue;
+    const float* dp = reinterpret_cast<const float*>(base + o_pts[p]);
+    uint32_t* perm = reinterpret_cast<uint32_t*>(base + o_perm[p]);
+    VTRY(ensure_slot(ctx, kSlotCounters, sizeof(VisCounters)));
+    VTRY(ensure_slot(ctx, kSlotVisKeys, (size_t)n * 8));
+    VTRY(ensure_slot(ctx, kSlotVisKeysAlt, (size_t)n * 8));
+    VTRY(ensure_slot(ctx, kSlotVisPermAlt, (size_t)n * 4));
+    VisCounters* cnt = slot<VisCounters>(ctx, kSlotCounters);
+    VisCounters* h = nullptr;
+    VTRY(pinned(ctx, sizeof(VisCounters), (void**)&h));
+    memset(h, 0, sizeof(VisCounters));
+    for (int a = 0; a < 3; ++a) {
+      h->pmin[a] = 0xffffffffu;
+      h->pmax[a] = 0u;
+    }
+    VCUDA(cudaMemcpyAsync(cnt, h, sizeof(VisCounters), cudaMemcpyHostToDevice, ctx->stream));
+    uint64_t* keys = slot<uint64_t>(ctx, kSlotVisKeys);
+    const unsigned gp = grid_for(n, 256, 4LL * ctx->sm_count);
+    VLAUNCH(ctx, kKVisPrep, gp, 256, 0, point_bounds_kernel, dp, n, cnt);
+    VLAUNCH(ctx, kKVisPrep, gp, 256, 0, point_morton_kernel, dp, n, cnt, morton_bits(n), keys, perm);
+    VTRY(radix_sort_u64(ctx, keys, perm, slot<uint64_t>(ctx, kSlotVisKeysAlt),
+                        slot<uint32_t>(ctx, kSlotVisPermAlt), n, 3 * morton_bits(n)));
+    if (is_new && is_new[p]) {
+      VTRY(ensure_slot(ctx, kSlotWordCounts, (size_t)n * 4));
+      VTRY(ensure_slot(ctx, kSlotWordOffsets, (size_t)(n + 1) * 8));
+      uint32_t* flags = slot<uint32_t>(ctx, kSlotWordCounts);
+      uint64_t* off = slot<uint64_t>(ctx, kSlotWordOffsets);
+      const uint8_t* dm = reinterpret_cast<const uint8_t*>(base + o_mask[p]);
+      VLAUNCH(ctx, kKVisPrep, gp, 256, 0, new_flags_kernel, perm, dm, n, flags);
+      VTRY(exclusive_scan_u32_to_u64(ctx, flags, off, n));
+      VLAUNCH(ctx, kKVisPrep, gp, 256, 0, new_rows_kernel, perm, flags, off, n,
+              reinterpret_cast<uint32_t*>(base + o_rows[p]), reinterpret_cast<int32_t*>(base + o_rank[p]));
+      VLAUNCH(ctx, kKVisPrep, 1, 1, 0, copy_count_kernel, off, n, d_nr + p);
+    }
+  }
+  std::vector<int32_t> nr(n_parts, 0);
+  {
+    int32_t* h = nullptr;
+    VTRY(pinned(ctx, 4 * (size_t)n_parts, (void**)&h));
+    VCUDA(cudaMemcpyAsync(h, d_nr, 4 * (size_t)n_parts, cudaMemcpyDeviceToHost, ctx->stream));
+    VCUDA(stream_wait(ctx));
+    memcpy(nr.data(), h, 4 * (size_t)n_parts);
+  }
+  // Part descriptors and the global work numbering.
+  VTRY(ensure_slot(ctx, kSlotBitset, (size_t)std::max<unsigned long long>(words, 1) * 4));
+  uint32_t* bits = slot<uint32_t>(ctx, kSlotBitset);
+  VTRY(ensure_slot(ctx, kSlotCounters, sizeof(VisCounters)));
+  VisCounters* cnt = slot<VisCounters>(ctx, kSlotCounters);
+  std::vector<VisParams> desc(n_parts);
+  std::vector<unsigned long long> tile_start(n_parts + 1, 0);
+  unsigned long long tiles = 0;
+  for (int p = 0; p < n_parts; ++p) {
+    const int32_t n = n_pts[p];
+    VisParams& P = desc[p];
+    memset(&P, 0, sizeof(P));
+    P.pts = reinterpret_cast<const float*>(base + o_pts[p]);
+    P.n = n;
+    P.cols = reinterpret_cast<const uint32_t*>(base + o_perm[p]);
+    P.nc = n;
+    P.ntc = (n + TC - 1) / TC;
+    const bool masked = is_new && is_new[p];
+    if (masked) {
+      P.rows = reinterpret_cast<const uint32_t*>(base + o_rows[p]);
+      P.nr = nr[p];
+      P.triangular = 0;
+      P.is_new = reinterpret_cast<const uint8_t*>(base + o_mask[p]);
+      P.newrank = reinterpret_cast<const int32_t*>(base + o_rank[p]);
+      P.ntr = (P.nr + TR - 1) / TR;
+      P.total_tiles = n >= 2 ? (unsigned long long)P.ntr * (unsigned long long)P.ntc : 0ull;
+    } else {
+      P.rows = P.cols;
+      P.nr = n;
+      P.triangular = 1;
+      P.ntr = ntr_tri[p];
+      P.row_start = reinterpret_cast<const unsigned long long*>(base + o_rs[p]);
+      unsigned long long t = 0;
+      for (int64_t r = 0; r < P.ntr; ++r) {
+        const int64_t c = P.ntc - (r * TR) / TC;
+        t += (unsigned long long)(c > 0 ? c : 0);
+      }
+      P.total_tiles = n >= 2 ? t : 0ull;
+    }
+    P.self_nodes = self_bvhs[p]->nodes;
+    P.self_tris = self_bvhs[p]->tris;
+    P.self_nt = self_bvhs[p]->nt;
+    P.cage_nodes = cage_bvhs[p]->nodes;
+    P.cage_tris = cage_bvhs[p]->tris;
+    P.cage_nt = cage_bvhs[p]->nt;
+    P.bitset = bits + word_start[p];
+    P.cnt = cnt;
+    P.status = ctx->d_status;
+    tile_start[p] = tiles;
+    tiles += P.total_tiles;
+  }
+  tile_start[n_parts] = tiles;
+  {
+    VisCounters init;
+    memset(&init, 0, sizeof(init));
+    Stager up(ctx);
+    VTRY(up.reserve(sizeof(VisParams) * (size_t)n_parts + 8 * (size_t)(n_parts + 1) + sizeof(VisCounters), 3));
+    VTRY(up.put(base + o_desc, desc.data(), sizeof(VisParams) * (size_t)n_parts));
+    VTRY(up.put(base + o_tiles, tile_start.data(), 8 * (size_t)(n_parts + 1)));
+    VTRY(up.put(cnt, &init, sizeof(VisCounters)));
+  }
+  if (words) VCUDA(cudaMemsetAsync(bits, 0, (size_t)words * 4, ctx->stream));
+  const VisParams* d_desc = reinterpret_cast<const VisParams*>(base + o_desc);
+  const unsigned long long* d_tiles = reinterpret_cast<const unsigned long long*>(base + o_tiles);
+  const unsigned long long* d_words = reinterpret_cast<const unsigned long long*>(base + o_words);
+  if (tiles) {
+    VLAUNCH(ctx, kKVisibility, (unsigned)(ctx->sm_count * 8), kVisThreads, 0, (visibility_multi_kernel<8, 8>),
+            d_desc, n_parts, d_tiles, tiles, cnt, ctx->d_status);
+  }
+  // Compaction over the concatenated bitset.
+  const int64_t nw = (int64_t)words;
+  VTRY(ensure_slot(ctx, kSlotWordCounts, (size_t)std::max<int64_t>(nw, 1) * 4));
+  VTRY(ensure_slot(ctx, kSlotWordOffsets, (size_t)(nw + 1) * 8));
+  uint32_t* wc = slot<uint32_t>(ctx, kSlotWordCounts);
+  uint64_t* wo = slot<uint64_t>(ctx, kSlotWordOffsets);
+  const unsigned gw = grid_for(std::max<int64_t>(nw, 1), 256, 16LL * ctx->sm_count);
+  if (nw) {
+    VLAUNCH(ctx, kKBitPopc, gw, 256, 0, bit_popc_kernel, bits, nw, wc);
+    VTRY(exclusive_scan_u32_to_u64(ctx, wc, wo, nw));
+  } else {
+    VCUDA(cudaMemsetAsync(wo, 0, 8, ctx->stream));
+  }
+  uint64_t* d_poff = reinterpret_cast<uint64_t*>(base + o_poff);
+  VLAUNCH(ctx, kKVisPrep, 1, 256, 0, multi_part_offsets_kernel, d_words, n_parts, wo, d_poff);
+  char* hb = nullptr;
+  VTRY(pinned(ctx, sizeof(VisCounters) + 8 * (size_t)(n_parts + 1), (void**)&hb));
+  VCUDA(cudaMemcpyAsync(hb, cnt, sizeof(VisCounters), cudaMemcpyDeviceToHost, ctx->stream));
+  VCUDA(cudaMemcpyAsync(hb + sizeof(VisCounters), d_poff, 8 * (size_t)(n_parts + 1), cudaMemcpyDeviceToHost,
+                        ctx->stream));
+  VCUDA(stream_wait(ctx));
+  // Copy the read-back out of the pinned staging area before the status
+  // check reuses it.
+  VisCounters hc;
+  memcpy(&hc, hb, sizeof(hc));
+  std::vector<uint64_t> poff(n_parts + 1);
+  memcpy(poff.data(), hb + sizeof(VisCounters), 8 * (size_t)(n_parts + 1));
+  VTRY(check_status(ctx, "visibility_batch"));
+  for (int p = 0; p < n_parts; ++p) n_edges[p] = (int64_t)(poff[p + 1] - poff[p]);
+  const int64_t ne = (int64_t)poff[n_parts];
+  VTRY(ensure_slot(ctx, kSlotEdgesOut, (size_t)(ne > 0 ? ne : 1) * 8));
+  if (ne > 0) {
+    VLAUNCH(ctx, kKBitEmit, gw, 256, 0, multi_emit_kernel, d_desc, n_parts, d_words, bits, nw, wo,
+            slot<uint32_t>(ctx, kSlotEdgesOut));
+  }
+  ctx->last_n_edges = ne;
+  if (stats) {
+    stats->pairs_tested = (int64_t)hc.pairs;
+    stats->n_edges = ne;
+    stats->self_hits = (int64_t)hc.self_hits;
+    stats->cage_hits = (int64_t)hc.cage_hits;
+    stats->fp64_rechecks = (int64_t)hc.rechecks;
+    stats->degenerate = (int64_t)hc.degenerate;
+    stats->node_visits = (int64_t)hc.node_visits;
+    stats->tri_tests = (int64_t)hc.tri_tests;
+  }
+  return VISACD_OK;
+}
+
 int visibility_impl(visacd_ctx* ctx, const float* pts, int32_t n, const uint8_t* is_new,
                     int device_ptrs, const visacd_bvh* self_bvh, const visacd_bvh* cage_bvh,
                     int64_t* n_edges, visacd_vis_stats* stats) {
@@ -542,6 +878,14 @@ extern "C" int visacd_visibility(visacd_ctx* ctx, const float* pts, int32_t n,
                                  const visacd_bvh* self_bvh, const visacd_bvh* cage_bvh,
                                  int64_t* n_edges, visacd_vis_stats* stats) {
   return visibility_impl(ctx, pts, n, is_new, device_ptrs, self_bvh, cage_bvh, n_edges, stats);
+}
+
+extern "C" int visacd_visibility_batch(visacd_ctx* ctx, int32_t n_parts, const float* const* pts,
+                                       const int32_t* n_pts, const uint8_t* const* is_new,
+                                       const visacd_bvh* const* self_bvhs,
+                                       const visacd_bvh* const* cage_bvhs, int64_t* n_edges,
+                                       visacd_vis_stats* stats) {
+  return visibility_multi_impl(ctx, n_parts, pts, n_pts, is_new, self_bvhs, cage_bvhs, n_edges, stats);
 }
 
 extern "C" int visacd_visibility_edges(visacd_ctx* ctx, uint32_t* edges_out,

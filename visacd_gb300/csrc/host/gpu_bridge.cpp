@@ -88,6 +88,65 @@ static void to_f32(const std::vector<Vec3>& v, std::vector<float>& out) {
     for (int k = 0; k < 3; ++k) out[3 * i + k] = (float)v[i][k];
 }
 
+std::vector<std::vector<Edge>> visibility_edges_batch(const std::vector<const Mesh*>& parts,
+                                                      const std::vector<const Mesh*>& cages) {
+  const size_t K = parts.size();
+  std::vector<std::vector<Edge>> out(K);
+  if (K == 0) return out;
+  double t0 = now_ms();
+  visacd_ctx* ctx = context();
+  std::vector<std::vector<float>> v(K), cv(K);
+  std::vector<std::vector<uint8_t>> mask(K);
+  std::vector<BvhHandle> sb(K), cb(K);
+  std::vector<const float*> pts(K);
+  std::vector<int32_t> n(K);
+  std::vector<const uint8_t*> masks(K, nullptr);
+  std::vector<const visacd_bvh*> sbs(K), cbs(K);
+  for (size_t k = 0; k < K; ++k) {
+    const Mesh& mesh = *parts[k];
+    const Mesh& cage = *cages[k];
+    to_f32(mesh.vertices, v[k]);
+    to_f32(cage.vertices, cv[k]);
+    check(visacd_bvh_build(ctx, v[k].data(), (int32_t)mesh.vertices.size(),
+                           reinterpret_cast<const uint32_t*>(mesh.triangles.data()),
+                           (int32_t)mesh.triangles.size(), 0, &sb[k].h),
+          "visacd_bvh_build(part)");
+    check(visacd_bvh_build(ctx, cv[k].data(), (int32_t)cage.vertices.size(),
+                           reinterpret_cast<const uint32_t*>(cage.triangles.data()),
+                           (int32_t)cage.triangles.size(), 0, &cb[k].h),
+          "visacd_bvh_build(cage)");
+    if (!mesh.is_new.empty()) {
+      mask[k].assign(mesh.vertices.size(), 0);
+      for (size_t i = 0; i < mesh.is_new.size() && i < mask[k].size(); ++i) mask[k][i] = mesh.is_new[i] ? 1 : 0;
+      masks[k] = mask[k].data();
+    }
+    pts[k] = v[k].data();
+    n[k] = (int32_t)mesh.vertices.size();
+    sbs[k] = sb[k].h;
+    cbs[k] = cb[k].h;
+  }
+  std::vector<int64_t> ne(K, 0);
+  visacd_vis_stats st;
+  check(visacd_visibility_batch(ctx, (int32_t)K, pts.data(), n.data(), masks.data(), sbs.data(), cbs.data(),
+                                ne.data(), &st),
+        "visacd_visibility_batch");
+  int64_t total = 0;
+  for (int64_t x : ne) total += x;
+  std::vector<uint32_t> flat(2 * (size_t)total);
+  check(visacd_visibility_edges(ctx, flat.data(), total), "visacd_visibility_edges");
+  int64_t at = 0;
+  for (size_t k = 0; k < K; ++k) {
+    out[k].resize((size_t)ne[k]);
+    for (int64_t e = 0; e < ne[k]; ++e, ++at) out[k][e] = {flat[2 * at], flat[2 * at + 1]};
+  }
+  auto& c = counters();
+  c.vis_calls++;
+  c.vis_pairs += st.pairs_tested;
+  c.vis_edges += total;
+  c.vis_ms += now_ms() - t0;
+  return out;
+}
+
 namespace {
 
 // The edge draws of one candidate-plane generation, taken in advance from a

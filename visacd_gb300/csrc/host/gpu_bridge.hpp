@@ -42,6 +42,13 @@ std::vector<Plane> propose_planes(const Mesh& mesh);
 // pairs with a new endpoint when mesh.is_new is non-empty, else all pairs.
 std::vector<Edge> visibility_edges(const Mesh& mesh, const Mesh& cage);
 
+// visibility_edges of several parts in one GPU call (visacd_visibility_batch:
+// per-part preparation, one persistent visibility launch over all parts, one
+// compaction). Part k is traced against cages[k]; same edges as one
+// visibility_edges call per part.
+std::vector<std::vector<Edge>> visibility_edges_batch(const std::vector<const Mesh*>& parts,
+                                                      const std::vector<const Mesh*>& cages);
+
 // Plane scores (float64, exact crossing classification) and the first argmax.
 std::vector<double> score_planes(const std::vector<Plane>& planes, const std::vector<Vec3>& pts,
                                  const std::vector<Edge>& edges);

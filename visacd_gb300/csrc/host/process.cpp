@@ -219,18 +219,37 @@ bool decompose_iteration(Mesh& mesh, MeshList& parts, Mesh& cage,
     if (map2[a] && map2[b]) halves[1].intersecting_edges.push_back({(unsigned)(map2[a] - 1), (unsigned)(map2[b] - 1)});
   }
   separate_disjoint(halves);
-  for (auto& part : halves) {
-    if (part.vertices.size() < 10) continue;
+  // Every new sub-part gets its cage, then all of them are traced in one
+  // batched visibility call (the reference traces them one by one,
+  // lib/src/process.cpp:165-178; neither step draws random numbers, so the
+  // order does not change results).
+  std::vector<Mesh> cages;
+  std::vector<const Mesh*> todo, todo_cages;
+  std::vector<size_t> which;
+  cages.reserve(halves.size());
+  for (size_t k = 0; k < halves.size(); ++k) {
+    if (halves[k].vertices.size() < 10) continue;
     double c0 = now_ms();
-    cage = part.copy_geometry();
-    manifold_preprocess(cage, 40, 0.02);
-    double c1 = now_ms();
-    g_times.cages += c1 - c0;
-    std::vector<Edge> fresh = gpu::visibility_edges(part, cage);
-    g_times.visibility += now_ms() - c1;
-    part.intersecting_edges.insert(part.intersecting_edges.end(), fresh.begin(), fresh.end());
-    parts.push_back(part);
+    cages.push_back(halves[k].copy_geometry());
+    manifold_preprocess(cages.back(), 40, 0.02);
+    g_times.cages += now_ms() - c0;
+    which.push_back(k);
   }
+  for (size_t k = 0; k < which.size(); ++k) {
+    todo.push_back(&halves[which[k]]);
+    todo_cages.push_back(&cages[k]);
+  }
+  if (!todo.empty()) {
+    double c1 = now_ms();
+    std::vector<std::vector<Edge>> fresh = gpu::visibility_edges_batch(todo, todo_cages);
+    g_times.visibility += now_ms() - c1;
+    for (size_t k = 0; k < which.size(); ++k) {
+      Mesh& part = halves[which[k]];
+      part.intersecting_edges.insert(part.intersecting_edges.end(), fresh[k].begin(), fresh[k].end());
+    }
+    cage = cages.back();
+  }
+  for (size_t k : which) parts.push_back(halves[k]);
   return false;
 }
 
@@ -356,10 +375,14 @@ ProcessResult process(Mesh mesh, double concavity, int num_parts) {
   g_times.preprocess = now_ms() - t_start;
   {
     double t0 = now_ms();
+    std::vector<const Mesh*> ps, cs;
     for (auto& part : parts) {
-      auto e = gpu::visibility_edges(part, cage);
-      part.intersecting_edges.insert(part.intersecting_edges.end(), e.begin(), e.end());
+      ps.push_back(&part);
+      cs.push_back(&cage);
     }
+    std::vector<std::vector<Edge>> e = gpu::visibility_edges_batch(ps, cs);
+    for (size_t k = 0; k < parts.size(); ++k)
+      parts[k].intersecting_edges.insert(parts[k].intersecting_edges.end(), e[k].begin(), e[k].end());
     g_times.visibility += now_ms() - t0;
   }
   HullCache hull_cache;
