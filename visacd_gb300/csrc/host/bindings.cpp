@@ -141,6 +141,23 @@ PYBIND11_MODULE(visacd, m) {
       },
       py::arg("host_clip") = py::none(), py::arg("host_concavity") = py::none(),
       py::arg("host_remesh") = py::none(), py::arg("host_merge") = py::none());
+  // Test hook: record every visibility call of process() (the part with its
+  // is_new mask and the edges found, and its cage); reading clears the record.
+  m.def("_record_visibility", [](bool on) {
+    checker_hooks().record_visibility = on;
+    recorded_visibility().clear();
+  });
+  m.def("_recorded_visibility", []() {
+    py::list out;
+    for (const auto& r : recorded_visibility()) {
+      py::dict d;
+      d["part"] = mesh_dict(r.part);
+      d["cage"] = mesh_dict(r.cage);
+      out.append(d);
+    }
+    recorded_visibility().clear();
+    return out;
+  });
   m.attr("config") = py::cast(&config(), py::return_value_policy::reference);
   // The trained proposer ships next to this module (proposer_weights.bin).
   if (config().proposer_weights.empty()) {

@@ -33,6 +33,11 @@ CheckerHooks& checker_hooks() {
   return h;
 }
 
+std::vector<VisibilityRecord>& recorded_visibility() {
+  static std::vector<VisibilityRecord> r;
+  return r;
+}
+
 void Mt19937::seed(result_type s) {
   x_[0] = s;
   for (int i = 1; i < kN; ++i) x_[i] = 1812433253u * (x_[i - 1] ^ (x_[i - 1] >> 30)) + (uint32_t)i;

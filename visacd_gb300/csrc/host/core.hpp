@@ -114,8 +114,15 @@ struct CheckerHooks {
   bool host_concavity = false;   // host Hausdorff term of the concavity metric
   bool host_remesh = false;      // host SDF remesh (manifold and cages)
   bool host_merge = false;       // host hull-pair distances in hull merging
+  bool record_visibility = false;  // keep every visibility call's part, cage and edges
 };
 CheckerHooks& checker_hooks();
+
+// Visibility calls recorded while checker_hooks().record_visibility is on.
+struct VisibilityRecord {
+  Mesh part, cage;  // part with is_new and the edges found for it
+};
+std::vector<VisibilityRecord>& recorded_visibility();
 
 // The 32-bit Mersenne Twister MT19937 (Matsumoto and Nishimura, 1998) with the
 // parameters and seeding std::mt19937 is defined with, so the same seed gives

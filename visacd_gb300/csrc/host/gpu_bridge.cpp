@@ -139,6 +139,13 @@ std::vector<std::vector<Edge>> visibility_edges_batch(const std::vector<const Me
     out[k].resize((size_t)ne[k]);
     for (int64_t e = 0; e < ne[k]; ++e, ++at) out[k][e] = {flat[2 * at], flat[2 * at + 1]};
   }
+  if (checker_hooks().record_visibility) {
+    for (size_t k = 0; k < K; ++k) {
+      VisibilityRecord r{*parts[k], cages[k]->copy_geometry()};
+      r.part.intersecting_edges = out[k];
+      recorded_visibility().push_back(std::move(r));
+    }
+  }
   auto& c = counters();
   c.vis_calls++;
   c.vis_pairs += st.pairs_tested;
