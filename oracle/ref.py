@@ -41,6 +41,8 @@ def lib() -> C.CDLL:
         L.ref_hull_bt.restype = C.c_int
         L.ref_multimerge.argtypes = [P, P, P, P, C.c_int, C.c_double, C.c_double, C.c_uint]
         L.ref_multimerge.restype = C.c_int
+        L.ref_score_trace.argtypes = [P, C.c_int]
+        L.ref_score_trace.restype = C.c_int
         L.ref_process.argtypes = [P, C.c_int, P, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int,
                                   C.c_int, C.POINTER(C.c_double)]
         _lib = L
@@ -133,6 +135,14 @@ def hull_bt(v):
     if nt < 0:
         raise ValueError("hull buffers too small")
     return ov[: nv.value], ot[:nt]
+
+
+def score_trace():
+    """The reference loop's split searches since the last call: rows of
+    (planes, points, edges, first float maximum, its score)."""
+    out = np.zeros((4096, 5))
+    n = lib().ref_score_trace(_p(out), 4096)
+    return out[:n]
 
 
 def multimerge(meshes, current_concavity, threshold, seed):

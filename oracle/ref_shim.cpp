@@ -20,6 +20,7 @@
 #include <process.hpp>
 #include <support_surface.hpp>
 
+#include <array>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -87,6 +88,8 @@ std::vector<Plane> get_candidate_planes(std::vector<Vec3D>& vertices,
                                         int num_planes);
 }  // namespace neural_acd
 
+static std::vector<std::array<double, 5>> g_score_trace;
+
 extern "C" void classify_and_rate_planes(const float* planes, const float* points,
                                          const unsigned int* edges, float* scores, int numPlanes,
                                          int numPoints, int numEdges) {
@@ -95,6 +98,12 @@ extern "C" void classify_and_rate_planes(const float* planes, const float* point
   int64_t sk = 0;
   oracle_score_planes(planes, numPlanes, points, numPoints, edges, numEdges, nullptr, q.data(), &qexp, &sk);
   for (int p = 0; p < numPlanes; ++p) scores[p] = (float)std::ldexp((double)q[p], qexp);
+  // Trace of the split searches (size and first float maximum), for tests.
+  int best = 0;
+  for (int p = 1; p < numPlanes; ++p)
+    if (scores[p] > scores[best]) best = p;
+  g_score_trace.push_back({(double)numPlanes, (double)numPoints, (double)numEdges, (double)best,
+                           numPlanes > 0 ? (double)scores[best] : 0.0});
 }
 
 // ---- C entry points for the tests -----------------------------------------
@@ -112,6 +121,16 @@ static Mesh make_mesh(const double* v, int nv, const int* t, int nt) {
 extern "C" {
 
 int ref_part_count(void) { return (int)g_parts.size(); }
+
+// The split searches since the last call: rows of (planes, points, edges,
+// first maximum, its float score); returns the count and clears the trace.
+int ref_score_trace(double* out, int cap) {
+  const int n = (int)g_score_trace.size();
+  for (int i = 0; i < n && i < cap; ++i)
+    for (int k = 0; k < 5; ++k) out[5 * i + k] = g_score_trace[i][k];
+  g_score_trace.clear();
+  return n;
+}
 int ref_part_sizes(int i, int* nv, int* nt, int* nedges) {
   if (i < 0 || i >= (int)g_parts.size()) return -1;
   *nv = (int)g_parts[i].vertices.size();

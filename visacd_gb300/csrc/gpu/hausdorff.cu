@@ -16,10 +16,21 @@
 //  * k-NN candidates are ranked in FP32 with a proven rounding margin and the
 //    exact 10 chosen in FP64; triangle distances whose FP32 lower bound cannot
 //    lower the minimum are skipped.
-//  * Point-triangle distance: closest point by Voronoi region (Ericson,
-//    Real-Time Collision Detection 5.1.5) in FP64 with explicit round-to-
-//    nearest intrinsics in the host's operation order, so values equal the
-//    host implementation's.
+//  * Point-triangle distance: the reference's own formula (projection onto the
+//    triangle's plane, barycentric test, else Pythagorean edge and vertex
+//    distances; ref_point_tri_dist) in FP64 with explicit round-to-nearest
+//    intrinsics in its operation order, so values equal the host's and the
+//    reference's. On a degenerate triangle that formula can give NaN (the
+//    triangle then never lowers a minimum) or a value below the true distance,
+//    so every shortcut that relies on the true distance is applied only where
+//    it holds for the formula:
+//      - the FP32 lower-bound skip of a triangle only for regular triangles
+//        (|cross product| >= 1e-6 of the longest edge squared, where the
+//        formula is the true distance up to rounding far inside the margin);
+//      - a query's upper bound is the formula's own value for the triangle of
+//        a sample proven to be among its 10 nearest (the term is at most that,
+//        or the nearest-sample distance when the rule for minima above 10
+//        applies); queries without such a bound are evaluated in full.
 #include <float.h>
 
 #include "common.cuh"
@@ -230,8 +241,11 @@ __device__ double query_term(const HSide& S, int qi, float tmargin) {
     for (int u = 0; u < j; ++u) dup |= seen[u] == tri;
     seen[j] = tri;
     if (dup) continue;
-    if (cmin < DBL_MAX) {
-      const float4 lo = S.tb[3 * (int64_t)tri], hi = S.tb[3 * (int64_t)tri + 1], pl = S.tb[3 * (int64_t)tri + 2];
+    const float4 lo = S.tb[3 * (int64_t)tri];
+    // Irregular triangles (lo.w == 0) are always evaluated: the bound holds
+    // for the true distance, not for the formula there.
+    if (cmin < DBL_MAX && lo.w != 0.f) {
+      const float4 hi = S.tb[3 * (int64_t)tri + 1], pl = S.tb[3 * (int64_t)tri + 2];
       const float gx = fmaxf(fmaxf(lo.x - qfx, qfx - hi.x), 0.f);
       const float gy = fmaxf(fmaxf(lo.y - qfy, qfy - hi.y), 0.f);
       const float gz = fmaxf(fmaxf(lo.z - qfz, qfz - hi.z), 0.f);
@@ -239,7 +253,7 @@ __device__ double query_term(const HSide& S, int qi, float tmargin) {
       if ((double)(lb - tmargin) >= cmin) continue;
     }
     const int* t = S.mt + 3 * (int64_t)tri;
-    const double d = point_tri_dist(q, S.mv + 3 * (int64_t)t[0], S.mv + 3 * (int64_t)t[1], S.mv + 3 * (int64_t)t[2]);
+    const double d = ref_point_tri_dist(q, S.mv + 3 * (int64_t)t[0], S.mv + 3 * (int64_t)t[1], S.mv + 3 * (int64_t)t[2]);
     if (d < cmin) {
       cmin = d;
       if (cmin < 1e-14) break;
@@ -273,12 +287,13 @@ __device__ __forceinline__ float warp_take_min(const float (&fd)[kKnnF], const i
 // has kKnnF smaller ones in that lane alone); a warp tournament takes them in
 // order. Same stop rule, same FP32-to-FP64 selection proof and the same term
 // as query_term; returns false (on all lanes) when the proof fails, and the
-// caller then uses query_term. Returns kTermSkipped (on all lanes) as soon as
-// the nearest sample found bounds the term by a value `prune` accepts (a
-// bound that cannot change the result).
+// caller then uses query_term. (These queries are evaluated in full: the
+// nearest sample's distance does not bound the reference formula's minimum
+// when its triangle is degenerate, so it is not used to skip them.)
 constexpr int kTermOk = 0, kTermUnproven = 1, kTermSkipped = 2;
-// r0: the first ring to walk; the rings inside it are known to hold no sample
-// of G (a query without a bound found none within kBoundRings rings).
+// r0: the first ring to walk (0: every ring; the rings inside r0 must hold no
+// sample of G).
+
 template <class Prune>
 __device__ int query_term_warp(const HSide& S, int qi, int r0, const Prune& prune, double& term) {
   const int lane = threadIdx.x & 31;
@@ -324,14 +339,6 @@ __device__ int query_term_warp(const HSide& S, int qi, int r0, const Prune& prun
     }
     for (int o = 16; o; o >>= 1) seen += __shfl_xor_sync(0xffffffffu, seen, o);
     total += seen;
-    if (seen > 0) {
-      // The term is at most the nearest sample's distance, itself at most the
-      // warp's smallest FP32 distance so far rounded upwards plus the bound.
-      float m = nf > 0 ? fd[0] : 3.4e38f;
-      for (int o = 16; o; o >>= 1) m = fminf(m, __shfl_xor_sync(0xffffffffu, m, o));
-      const double ub = (double)__fadd_ru(__fmul_ru(__fsqrt_ru(m), 1.0f + 1.0f / 1048576.0f), G.eabs);
-      if (__shfl_sync(0xffffffffu, prune(ub) ? 1 : 0, 0)) return kTermSkipped;
-    }
     if (total >= kKnn) {
       int ptr = 0, id;
       float v = 3.4e38f;
@@ -400,7 +407,7 @@ __device__ int query_term_warp(const HSide& S, int qi, int r0, const Prune& prun
   if (which >= 0) {
     const int tj = S.ids[which];
     const int* t = S.mt + 3 * (int64_t)tj;
-    dj = point_tri_dist(q, S.mv + 3 * (int64_t)t[0], S.mv + 3 * (int64_t)t[1], S.mv + 3 * (int64_t)t[2]);
+    dj = ref_point_tri_dist(q, S.mv + 3 * (int64_t)t[0], S.mv + 3 * (int64_t)t[1], S.mv + 3 * (int64_t)t[2]);
   }
   double cmin = DBL_MAX;
   for (int j = 0; j < cnt; ++j) {
@@ -504,13 +511,18 @@ __global__ void hprep_kernel(HBatch H, long long nsamp, long long ntri, int* __r
       double nx = uy * vz - uz * vy, ny = uz * vx - ux * vz, nz = ux * vy - uy * vx;
       const double nl = sqrt(nx * nx + ny * ny + nz * nz);
       float4 pl = make_float4(0.f, 0.f, 0.f, 0.f);
+      // Regular: cross product at least 1e-6 of the longest edge squared.
+      const double wx = c[0] - b[0], wy = c[1] - b[1], wz = c[2] - b[2];
+      const double l2 = fmax(fmax(ux * ux + uy * uy + uz * uz, vx * vx + vy * vy + vz * vz),
+                             wx * wx + wy * wy + wz * wz);
+      const float regular = (nl >= 1e-6 * l2 && l2 > 0.0) ? 1.f : 0.f;
       if (nl > 1e-30) {
         nx /= nl;
         ny /= nl;
         nz /= nl;
         pl = make_float4((float)nx, (float)ny, (float)nz, (float)-(nx * a[0] + ny * a[1] + nz * a[2]));
       }
-      H.tb[3 * j] = make_float4(lo[0], lo[1], lo[2], 0.f);
+      H.tb[3 * j] = make_float4(lo[0], lo[1], lo[2], regular);
       H.tb[3 * j + 1] = make_float4(hi[0], hi[1], hi[2], 0.f);
       H.tb[3 * j + 2] = pl;
     }
@@ -559,13 +571,51 @@ __global__ void hfinish_kernel(HBatch H, long long nsamp, int ncells, const unsi
   }
 }
 
+// Samples of G within ring r of cell (cx, cy, cz) whose FP32 squared distance
+// to qf is at most lim: count and the smallest one (value, local id).
+__device__ __forceinline__ void ring_scan(const HGrid& G, int cx, int cy, int cz, int r, const float (&qf)[3],
+                                          float lim, float& best, int& best_id, int& count) {
+  for (int dz = -r; dz <= r; ++dz) {
+    const int z = cz + dz;
+    if (z < 0 || z >= G.dim[2]) continue;
+    for (int dy = -r; dy <= r; ++dy) {
+      const int y = cy + dy;
+      if (y < 0 || y >= G.dim[1]) continue;
+      const bool face = abs(dz) == r || abs(dy) == r;
+      for (int dx = -r; dx <= r; dx += (face ? 1 : 2 * r > 0 ? 2 * r : 1)) {
+        const int x = cx + dx;
+        if (x >= 0 && x < G.dim[0]) {
+          const int c = (z * G.dim[1] + y) * G.dim[0] + x;
+          for (int k = G.start[c]; k < G.start[c + 1]; ++k) {
+            const float4 sp = G.spts[k];
+            const float ex = sp.x - qf[0], ey = sp.y - qf[1], ez = sp.z - qf[2];
+            const float d2 = ex * ex + ey * ey + ez * ez;
+            if (d2 < best) {
+              best = d2;
+              best_id = __float_as_int(sp.w);
+            }
+            count += d2 <= lim;
+          }
+        }
+        if (dx == r) break;
+      }
+    }
+  }
+}
+
 // Upper bound of every query's term, one thread per query (all sets, each in
-// its own grid's cell order): the distance to the nearest sample within two
-// rings of cells around the query, in FP32 rounded upwards plus the
-// coordinate rounding bound (the term is at most the distance to the nearest
-// sample, itself at most this). A query with no sample that close gets no
-// bound (+inf) and is appended to farlist (*far entries): those are evaluated
-// one warp each. qref[e] = (set, local query index).
+// its own grid's cell order). The nearest sample s within up to
+// kBoundRings + 1 rings (FP32) is proven to be among the exact 10 nearest
+// when at most 10 samples lie within its distance plus twice the rounding
+// bound and that distance lies inside the rings searched. The term is then at
+// most the formula's distance r_s from the query to s's triangle (a minimum
+// over the 10 nearest includes it, or an earlier evaluated value, or a
+// skipped one provably not smaller) or, under the rule for minima above 10,
+// the nearest-sample distance: the bound is the larger of the two, rounded
+// upwards plus the coordinate rounding bound. Queries without a proof, or
+// with r_s NaN or DBL_MAX (a degenerate triangle), get no bound (+inf) and
+// are appended to farlist (*far entries): those are evaluated one warp each.
+// qref[e] = (set, local query index).
 __global__ void __launch_bounds__(128) hbound_kernel(HBatch H, long long nsamp, const int* __restrict__ order,
                                                      float* __restrict__ ubs, int2* __restrict__ qref,
                                                      unsigned* __restrict__ far, long long* __restrict__ farlist) {
@@ -581,44 +631,51 @@ __global__ void __launch_bounds__(128) hbound_kernel(HBatch H, long long nsamp, 
     const int cy = cell_coord(q[1], G.lo[1], G.h, G.dim[1]);
     const int cz = cell_coord(q[2], G.lo[2], G.h, G.dim[2]);
     const float qf[3] = {(float)q[0], (float)q[1], (float)q[2]};
+    const float hf = (float)G.h;
     float best = 3.4e38f;
-    for (int r = 0; r <= kBoundRings; ++r) {
-      for (int dz = -r; dz <= r; ++dz) {
-        const int z = cz + dz;
-        if (z < 0 || z >= G.dim[2]) continue;
-        for (int dy = -r; dy <= r; ++dy) {
-          const int y = cy + dy;
-          if (y < 0 || y >= G.dim[1]) continue;
-          const bool face = abs(dz) == r || abs(dy) == r;
-          for (int dx = -r; dx <= r; dx += (face ? 1 : 2 * r > 0 ? 2 * r : 1)) {
-            const int x = cx + dx;
-            if (x >= 0 && x < G.dim[0]) {
-              const int c = (z * G.dim[1] + y) * G.dim[0] + x;
-              for (int k = G.start[c]; k < G.start[c + 1]; ++k) {
-                const float4 sp = G.spts[k];
-                const float ex = sp.x - qf[0], ey = sp.y - qf[1], ez = sp.z - qf[2];
-                best = fminf(best, ex * ex + ey * ey + ez * ez);
-              }
-            }
-            if (dx == r) break;
-          }
-        }
+    int best_id = -1, unused = 0;
+    int r_end = -1;
+    float dist_up = 0.f, reach = 0.f;
+    for (int r = 0; r <= kBoundRings + 1; ++r) {
+      ring_scan(G, cx, cy, cz, r, qf, -1.f, best, best_id, unused);
+      r_end = r;
+      if (best < 3.4e38f) {
+        dist_up = __fmul_ru(__fsqrt_ru(best), 1.0f + 1.0f / 1048576.0f);
+        reach = __fadd_ru(dist_up, __fmul_ru(2.0f, G.eabs));
+        if (reach <= __fmul_rd((float)r, hf) * (1.0f - 1e-6f)) break;
       }
-      if (r >= 1 && best < 3.4e38f) break;
     }
     float ub = __int_as_float(0x7f800000);  // +inf: no bound
-    if (best < 3.4e38f)
-      ub = __fadd_ru(__fmul_ru(__fsqrt_ru(best), 1.0f + 1.0f / 1048576.0f), G.eabs);
-    else
-      farlist[atomicAdd(far, 1u)] = e;
+    bool proven = best < 3.4e38f && reach <= __fmul_rd((float)r_end, hf) * (1.0f - 1e-6f);
+    if (proven) {
+      // Samples whose exact distance can be at most s's: FP32 distance at
+      // most reach (squared, rounded up).
+      const float lim = __fmul_ru(__fmul_ru(reach, reach), 1.0f + 1.0f / 262144.0f);
+      float b2 = 3.4e38f;
+      int id2 = -1, count = 0;
+      for (int r = 0; r <= r_end; ++r) ring_scan(G, cx, cy, cz, r, qf, lim, b2, id2, count);
+      proven = count <= kKnn;
+    }
+    if (proven) {
+      const int* t = S.mt + 3 * (int64_t)S.ids[best_id];
+      const double rs =
+          ref_point_tri_dist(q, S.mv + 3 * (int64_t)t[0], S.mv + 3 * (int64_t)t[1], S.mv + 3 * (int64_t)t[2]);
+      if (rs < DBL_MAX) {
+        const float rsf = __fadd_ru(__fmul_ru(__double2float_ru(rs), 1.0f + 1.0f / 1048576.0f), G.eabs);
+        ub = fmaxf(__fadd_ru(dist_up, G.eabs), rsf);
+      } else {
+        proven = false;
+      }
+    }
+    if (!proven) farlist[atomicAdd(far, 1u)] = e;
     ubs[e] = ub;
     qref[e] = make_int2(s, qi);
   }
 }
 
-// Terms of the queries without a bound (the farlist), one warp each: they are
-// far from the other surface, walk many rings, and their exact terms raise the
-// maxima that prune the rest.
+// Terms of the queries without a bound (the farlist), one warp each: mostly
+// queries far from the other surface, which walk many rings (and a few near a
+// degenerate triangle); their exact terms raise the maxima that prune the rest.
 __global__ void __launch_bounds__(128) hhead_kernel(HBatch H, const int2* __restrict__ qref,
                                                     const long long* __restrict__ farlist,
                                                     const unsigned* __restrict__ far) {
@@ -630,7 +687,7 @@ __global__ void __launch_bounds__(128) hhead_kernel(HBatch H, const int2* __rest
     const HSide& S = H.sides[r.x];
     double term;
     const int status =
-        query_term_warp(S, r.y, kBoundRings + 1, [&](double ub) { return prunable(H, job, ub); }, term);
+        query_term_warp(S, r.y, 0, [&](double ub) { return prunable(H, job, ub); }, term);
     if (status == kTermSkipped) continue;
     if (status == kTermUnproven) term = query_term(S, r.y, H.tmargin[job]);
     if ((threadIdx.x & 31) == 0 && term < DBL_MAX) publish(H, job, term);

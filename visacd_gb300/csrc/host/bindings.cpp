@@ -146,6 +146,13 @@ PYBIND11_MODULE(visacd, m) {
   m.def("_record_visibility", [](bool on) {
     checker_hooks().record_visibility = on;
     recorded_visibility().clear();
+    recorded_splits().clear();
+  });
+  m.def("_recorded_splits", []() {
+    py::list out;
+    for (const auto& r : recorded_splits()) out.append(py::make_tuple(r[0], r[1], r[2], r[3], r[4]));
+    recorded_splits().clear();
+    return out;
   });
   m.def("_recorded_visibility", []() {
     py::list out;

@@ -38,6 +38,11 @@ std::vector<VisibilityRecord>& recorded_visibility() {
   return r;
 }
 
+std::vector<std::array<double, 5>>& recorded_splits() {
+  static std::vector<std::array<double, 5>> r;
+  return r;
+}
+
 void Mt19937::seed(result_type s) {
   x_[0] = s;
   for (int i = 1; i < kN; ++i) x_[i] = 1812433253u * (x_[i - 1] ^ (x_[i - 1] >> 30)) + (uint32_t)i;

@@ -114,7 +114,7 @@ struct CheckerHooks {
   bool host_concavity = false;   // host Hausdorff term of the concavity metric
   bool host_remesh = false;      // host SDF remesh (manifold and cages)
   bool host_merge = false;       // host hull-pair distances in hull merging
-  bool record_visibility = false;  // keep every visibility call's part, cage and edges
+  bool record_visibility = false;  // keep every visibility call and split search
 };
 CheckerHooks& checker_hooks();
 
@@ -123,6 +123,9 @@ struct VisibilityRecord {
   Mesh part, cage;  // part with is_new and the edges found for it
 };
 std::vector<VisibilityRecord>& recorded_visibility();
+// Split searches recorded alongside: (planes scored, points, edges, index of
+// the chosen plane, its float score).
+std::vector<std::array<double, 5>>& recorded_splits();
 
 // The 32-bit Mersenne Twister MT19937 (Matsumoto and Nishimura, 1998) with the
 // parameters and seeding std::mt19937 is defined with, so the same seed gives

@@ -10,7 +10,7 @@
 // made in bulk with the same values, see extract_point_set). The host
 // nearest-sample search is this
 // project's kd-tree (the reference uses nanoflann); distances to the sampled
-// triangles use the exact closest-point test.
+// triangles are the reference's own formula (ref_point_triangle_distance).
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -231,6 +231,74 @@ class KdTree {
   }
 };
 
+// The reference's point-triangle distance (lib/include/hausdorff.hpp:97-212),
+// restated with its arithmetic in its order: the plane distance when the
+// point's projection passes the barycentric test, else the smallest of the
+// three edge distances (Pythagoras on the projection along the edge; +max
+// double when the projection falls outside the edge) and the three vertex
+// distances, combined by std::min (a NaN operand drops out when it is the
+// second one). On proper triangles this is the exact distance up to rounding;
+// on degenerate ones (zero area, repeated vertices) the NaNs of the plane
+// normal and of 0/0 projections make it differ, and those values decide which
+// part the reference splits next, so they are kept as they are.
+constexpr double kRefInf = std::numeric_limits<double>::max();
+inline double sq(double x) { return x * x; }
+inline double ref_min(double a, double b) { return (b < a) ? b : a; }
+
+double ref_point_point(const Vec3& p, const Vec3& q) {
+  return std::sqrt(sq(p[0] - q[0]) + sq(p[1] - q[1]) + sq(p[2] - q[2]));
+}
+
+double ref_point_segment(const Vec3& p, const Vec3& s0, const Vec3& s1) {
+  const double BA0 = p[0] - s1[0], BA1 = p[1] - s1[1], BA2 = p[2] - s1[2];
+  const double BC0 = s0[0] - s1[0], BC1 = s0[1] - s1[1], BC2 = s0[2] - s1[2];
+  const double proj = (BA0 * BC0 + BA1 * BC1 + BA2 * BC2) / std::sqrt(sq(BC0) + sq(BC1) + sq(BC2));
+  const double ab = std::sqrt(sq(BA0) + sq(BA1) + sq(BA2));
+  const double bc = std::sqrt(sq(BC0) + sq(BC1) + sq(BC2));
+  if (proj < 0 || proj > bc) return kRefInf;
+  return std::sqrt(sq(ab) - sq(proj));
+}
+
+bool ref_in_triangle(const Vec3& p, const Vec3& t0, const Vec3& t1, const Vec3& t2) {
+  const Vec3 v0 = t2 - t0, v1 = t1 - t0, v2 = p - t0;
+  const double d00 = v0[0] * v0[0] + v0[1] * v0[1] + v0[2] * v0[2];
+  const double d01 = v0[0] * v1[0] + v0[1] * v1[1] + v0[2] * v1[2];
+  const double d02 = v0[0] * v2[0] + v0[1] * v2[1] + v0[2] * v2[2];
+  const double d11 = v1[0] * v1[0] + v1[1] * v1[1] + v1[2] * v1[2];
+  const double d12 = v1[0] * v2[0] + v1[1] * v2[1] + v1[2] * v2[2];
+  const double inv = 1.0 / (d00 * d11 - d01 * d01);
+  const double u = (d11 * d02 - d01 * d12) * inv;
+  const double v = (d00 * d12 - d01 * d02) * inv;
+  return (u >= 0) && (v >= 0) && (u + v <= 1);
+}
+
+}  // namespace
+
+double ref_point_triangle_distance(const Vec3& pt, const Vec3& t0, const Vec3& t1, const Vec3& t2) {
+  const double A = (t1[1] - t0[1]) * (t2[2] - t0[2]) - (t1[2] - t0[2]) * (t2[1] - t0[1]);
+  const double B = (t1[2] - t0[2]) * (t2[0] - t0[0]) - (t1[0] - t0[0]) * (t2[2] - t0[2]);
+  const double C = (t1[0] - t0[0]) * (t2[1] - t0[1]) - (t1[1] - t0[1]) * (t2[0] - t0[0]);
+  const double a = A / std::sqrt(sq(A) + sq(B) + sq(C));
+  const double b = B / std::sqrt(sq(A) + sq(B) + sq(C));
+  const double c = C / std::sqrt(sq(A) + sq(B) + sq(C));
+  const double d = 0 - (a * t0[0] + b * t0[1] + c * t0[2]);
+  const double dist = std::fabs(a * pt[0] + b * pt[1] + c * pt[2] + d) / std::sqrt(sq(a) + sq(b) + sq(c));
+  const double r = pt[0] * a + pt[1] * b + pt[2] * c + d;  // Plane::side(pt, 1e-8)
+  Vec3 proj = pt;
+  if (r > 1e-8) {
+    proj = {pt[0] - a * dist, pt[1] - b * dist, pt[2] - c * dist};
+  } else if (r < -1 * 1e-8) {
+    proj = {pt[0] + a * dist, pt[1] + b * dist, pt[2] + c * dist};
+  }
+  if (ref_in_triangle(proj, t0, t1, t2)) return dist;
+  const double ab = ref_point_segment(pt, t0, t1), bc = ref_point_segment(pt, t1, t2),
+               ca = ref_point_segment(pt, t2, t0);
+  const double pa = ref_point_point(pt, t0), pb = ref_point_point(pt, t1), pc = ref_point_point(pt, t2);
+  return ref_min(ref_min(ref_min(ab, bc), ca), ref_min(ref_min(pa, pb), pc));
+}
+
+namespace {
+
 // One direction of the face Hausdorff distance: for each query sample, the
 // smallest distance to the triangles of its 10 nearest samples on the other
 // side (lib/include/hausdorff.hpp:236-263).
@@ -247,8 +315,8 @@ double directed(const std::vector<Vec3>& Q, const KdTree& tree, const Mesh& othe
       double cmin = kInf;
       for (const auto& r : nn) {
         const auto& t = other.triangles[other_ids[r.second]];
-        double d = point_triangle_distance(Q[i], other.vertices[t[0]], other.vertices[t[1]],
-                                           other.vertices[t[2]]);
+        double d = ref_point_triangle_distance(Q[i], other.vertices[t[0]], other.vertices[t[1]],
+                                               other.vertices[t[2]]);
         if (d < cmin) {
           cmin = d;
           if (cmin < 1e-14) break;

@@ -16,6 +16,10 @@ void manifold_preprocess(Mesh& m, double scale, double level);
 void manifold_preprocess_host(Mesh& m, double scale, double level);
 Vec3 closest_point_on_triangle(const Vec3& p, const Vec3& a, const Vec3& b, const Vec3& c);
 double point_triangle_distance(const Vec3& p, const Vec3& a, const Vec3& b, const Vec3& c);
+// The reference's distance of the concavity metric (hausdorff.hpp:156-212):
+// equal to point_triangle_distance up to rounding on proper triangles, not on
+// degenerate ones (see cost.cpp).
+double ref_point_triangle_distance(const Vec3& pt, const Vec3& t0, const Vec3& t1, const Vec3& t2);
 
 // ---- hull.cpp: convex hull (replaces qhull "Qt Pp", lib/src/core.cpp:59-111).
 // As with qhull, the hull mesh keeps every input point as a vertex (interior

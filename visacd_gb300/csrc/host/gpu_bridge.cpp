@@ -250,6 +250,10 @@ bool split_search(const Mesh& mesh, const std::vector<Plane>& flat_planes, doubl
                             &info),
         "visacd_split_search");
   take_draws(plan, info.draws_used);
+  if (checker_hooks().record_visibility)
+    recorded_splits().push_back({(double)(info.n_candidates + (int)flat_planes.size()),
+                                 (double)mesh.vertices.size(), (double)edges.size(),
+                                 (double)info.best_index, info.best_score});
   auto& c = counters();
   c.score_calls++;
   c.plane_edge_pairs += (long long)(info.n_candidates + (int)flat_planes.size()) * (long long)edges.size();
