@@ -839,6 +839,59 @@ def run_batching(args) -> dict:
                          "speedup": t_plain / t_batch}}
 
 
+def run_batch_decompositions(args) -> dict:
+    """Decompositions of the batching workload's meshes (displaced blobs of
+    subdivision 2-5, independent seeds), process(0.02, 64): process_batch over
+    all of them (exhaustive and learned) against the plain sequential loop on
+    the first --c3-plain of them (the loop's rate is per mesh, so a prefix
+    measures it; the prefix's results are checked equal to the batch's)."""
+    from visacd_gb300 import build
+
+    build.build_host()
+    from visacd_gb300 import visacd as V
+
+    V.config.verbose = False
+    parts = batch_parts(args.batch_parts)
+    meshes = V.MeshList()
+    for v, t, _, _, _ in parts:
+        m = V.Mesh()
+        m.vertices = V.VecArray3d(v.astype(np.float64).tolist())
+        m.triangles = V.make_vecarray3i(np.asarray(t, dtype=np.int32))
+        meshes.append(m)
+    seeds = list(range(7000, 7000 + len(meshes)))
+    conc, nparts = 0.02, 64
+    V.set_seed(0)
+    V.process(meshes[0], conc, nparts)  # warm-up
+    out = {"workload": f"{len(meshes)} displaced blobs, subdivision 2-5 (the batching workload's meshes), "
+                       "process(0.02, 64)", "meshes": len(meshes)}
+    try:
+        for mode in ("exhaustive", "learned"):
+            V.config.plane_proposer = mode
+            t0 = time.perf_counter()
+            res = V.process_batch(meshes, conc, nparts, seeds, args.c5_threads)
+            out[f"batched_{mode}_decomps_per_s"] = len(meshes) / (time.perf_counter() - t0)
+            out[f"batched_{mode}_parts_mean"] = float(np.mean([r.num_parts for r in res]))
+            out[f"batched_{mode}_concavity_mean"] = float(np.mean([r.concavity for r in res]))
+            if mode == "exhaustive":
+                batched = res
+        V.config.plane_proposer = "exhaustive"
+        k = min(args.c3_plain, len(meshes))
+        t0 = time.perf_counter()
+        plain = []
+        for i in range(k):
+            V.set_seed(seeds[i])
+            plain.append(V.process(meshes[i], conc, nparts))
+        out["plain_decomps_per_s"] = k / (time.perf_counter() - t0)
+        out["plain_meshes_timed"] = k
+        out["plain_equals_batched"] = all(a.concavity == b.concavity and a.num_parts == b.num_parts
+                                          for a, b in zip(plain, batched[:k]))
+    finally:
+        V.config.plane_proposer = "exhaustive"
+    out["speedup_batched_vs_plain"] = out["batched_exhaustive_decomps_per_s"] / out["plain_decomps_per_s"]
+    out["speedup_batched_learned_vs_plain"] = out["batched_learned_decomps_per_s"] / out["plain_decomps_per_s"]
+    return {"batch_decompositions": out}
+
+
 WORKLOAD_TEXT = ("displaced icosphere s5 blob: 10242 verts, 20480 tris, all 52,444,161 pairs vs "
                  "part + 0.03 offset cage, then 2500 candidate planes scored")
 REF_STRIDE = 4  # the reference arm's step: every 4th pair row (a quarter of the pairs)
@@ -912,6 +965,10 @@ def main():
     ap.add_argument("--sweep", action="store_true", help="scoring precision sweep only")
     ap.add_argument("--batch", action="store_true", help="batching workload only")
     ap.add_argument("--batch-parts", type=int, default=256)
+    ap.add_argument("--c3-decomps", action="store_true",
+                    help="decompositions of the batching workload's meshes: batched vs plain")
+    ap.add_argument("--c3-plain", type=int, default=64, help="meshes the plain loop times in --c3-decomps")
+    ap.add_argument("--no-c3", action="store_true", help="skip the 256-mesh decompositions")
     ap.add_argument("--sweep-sizes", type=int, nargs="+", default=[20, 22, 24, 26])
     ap.add_argument("--segtri", type=int, default=1 << 20, help="segment-triangle tests in the sweep")
     ap.add_argument("--c5", action="store_true", help="batched + learned decompositions only")
@@ -936,6 +993,9 @@ def main():
     if args.batch:
         print(json.dumps(run_batching(args)))
         return
+    if args.c3_decomps:
+        print(json.dumps(run_batch_decompositions(args)))
+        return
     if args.impl == "reference":
         out, rank = run_reference(args)
     else:
@@ -953,6 +1013,8 @@ def main():
             out["process"] = run_decompositions(args)
         if rank == 0 and single and not args.no_c5:
             out["decomps"] = run_learned_batch(args)
+        if rank == 0 and single and not args.no_c3:
+            out["decomps_256"] = run_batch_decompositions(args)["batch_decompositions"]
     if rank == 0 and out is not None:
         print(json.dumps(out))
 

@@ -16,9 +16,10 @@
 //    thread of the CTA reads the same edge (shared-memory broadcast).
 //  * The FP32 plane value carries an a-priori rounding bound B_p (Higham,
 //    3 nested FMAs: |err| <= 3u * (|a|X + |b|Y + |c|Z + |d|)). Per (plane, edge
-//    block) the kernel accumulates the certain crossings (beyond eps + B) and the
-//    possible ones (beyond eps - B); if they differ the block is queued and
-//    score_recheck re-decides only its band pairs in FP64 — the same FP64
+//    block) the kernel accumulates the certain crossings (both sides beyond
+//    eps + B) and flags the block when some pair comes within the band
+//    [eps - B, eps + B] (score_edge_block); a flagged block is queued and
+//    score_recheck re-decides its band pairs in FP64 — the same FP64
 //    evaluation the oracle uses — so classification equals the FP64 oracle's.
 //  * Sums are integers (order independent), so scores are deterministic.
 #include "score_device.cuh"
