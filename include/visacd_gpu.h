@@ -29,6 +29,9 @@
  *                                     lib/src/process.cpp:28-72
  *   visacd_split_search ............. the split search of decompose_iteration,
  *                                     lib/src/process.cpp:96-134
+ *   visacd_learned_split_search ..... the same split search with the learned
+ *                                     proposer (no reference counterpart) in
+ *                                     place of most of the candidate draw
  */
 #ifndef VISACD_GPU_H
 #define VISACD_GPU_H
@@ -387,7 +390,10 @@ int visacd_hull_distances(visacd_ctx* ctx, const double* verts, const int64_t* o
 typedef struct visacd_lp visacd_lp;
 
 int visacd_lp_param_count(void);
-/* params: 87,744 floats, or NULL for a seeded He-uniform initialisation. */
+/* params: 87,744 floats, or NULL for a seeded He-uniform initialisation. The
+   proposer runs on ctx's stream. Destroying ctx first releases the proposer's
+   device memory: later calls on it fail and visacd_lp_destroy only frees its
+   host side. */
 int visacd_lp_create(visacd_ctx* ctx, const float* params, uint32_t seed, visacd_lp** out);
 int visacd_lp_destroy(visacd_lp* lp);
 int visacd_lp_get_params(visacd_lp* lp, float* out);
@@ -414,6 +420,44 @@ int visacd_lp_set_tcgen05(visacd_lp* lp, int enable);
 /* visacd_lp_grads followed by one Adam step (beta 0.9 / 0.999, eps 1e-8). */
 int visacd_lp_train_step(visacd_lp* lp, const float* feats, const float* labels, const float* lw,
                          int32_t B, int32_t L, float lr, float* loss_out);
+
+/* The learned split search of one part in one call, in place of the candidate
+   draw and scoring of lib/src/process.cpp:96-134 when the proposer is on:
+    1. the proposer's 16 planes, as visacd_lp_propose (center, scale);
+    2. refinement: per proposal, the refine_k (0..32) perpendicular-bisector
+       planes of visibility edges (the reference's candidate form,
+       lib/src/process.cpp:45-53; edges shorter than 1e-6 have none) nearest
+       under D = 2 - 2|n_q . n_e| + ((s d_q - d_e) / half)^2 with
+       s = sign(n_q . n_e), ties by edge index; their union in edge order;
+    3. a probe: the candidates visacd_candidate_planes keeps from probe_draws
+       with num_planes = probe_planes;
+    4. the exact scores (visacd_score_planes) of [proposals, refined, probe,
+       flat planes], the flat scores times flat_k;
+    5. the decision: info->fallback = 1 when the best proposal or refined score
+       is below (1 - tolerance) x the best probe score (0 without probe
+       planes): the caller then runs the full search (visacd_split_search)
+       with the draws after info->draws_used. best_plane and best_index are
+       the first maximum of all scores in the order of step 4 either way.
+   Planes and scores are FP64 and equal, bit for bit, to those of the separate
+   calls. verts n x 3 float64, edges E x 2 uint32 (E > 0), probe_draws and
+   flat_planes (n_flat x 4 float64) are host arrays. Synchronizes twice. */
+typedef struct {
+  int32_t best_index;  /* in step 4's order: [0,16) proposals, then refined, probe, flat */
+  int32_t n_refined;
+  int32_t n_probe;     /* probe candidates kept */
+  int32_t draws_used;  /* probe draws consumed */
+  int32_t fallback;
+  int32_t reserved;
+  double best_score;
+  double best_proposal_score; /* over the proposals and the refined planes */
+  double best_probe_score;    /* 0 without probe planes */
+} visacd_learned_split_info;
+int visacd_learned_split_search(visacd_lp* lp, const double* verts, int32_t n, const uint32_t* edges,
+                                int64_t E, const float* center, float scale, double half,
+                                int32_t refine_k, const int32_t* probe_draws, int32_t n_probe_draws,
+                                int32_t probe_planes, const double* flat_planes, int32_t n_flat,
+                                double flat_k, double tolerance, double* best_plane,
+                                visacd_learned_split_info* info);
 
 /* Allocation-free variant of visacd_score_planes. No counterpart in the
    reference: it exists for callers that cannot allocate — code running under a

@@ -33,6 +33,7 @@ EXPORTED = [
     "visacd_sdf_remesh", "visacd_sdf_fetch", "visacd_hull_distances", "visacd_segment_triangle_tests",
     "visacd_set_blocking_sync", "visacd_lp_set_tcgen05", "visacd_ctx_set_blocking_wait",
     "visacd_candidate_planes", "visacd_split_search", "visacd_visibility_batch",
+    "visacd_learned_split_search",
 ]
 
 LP_POINTS = 2048
@@ -69,6 +70,16 @@ class SplitInfo(C.Structure):
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_ if f != "pad"}
+
+
+class LearnedSplitInfo(C.Structure):
+    _fields_ = [("best_index", C.c_int32), ("n_refined", C.c_int32), ("n_probe", C.c_int32),
+                ("draws_used", C.c_int32), ("fallback", C.c_int32), ("reserved", C.c_int32),
+                ("best_score", C.c_double), ("best_proposal_score", C.c_double),
+                ("best_probe_score", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
 
 
 def load() -> C.CDLL:
@@ -111,6 +122,9 @@ def load() -> C.CDLL:
                                             C.POINTER(i32)]
     lib.visacd_split_search.argtypes = [P, P, i32, P, i64, P, i32, i32, P, i32, C.c_double, P,
                                         C.POINTER(SplitInfo)]
+    lib.visacd_learned_split_search.argtypes = [P, P, i32, P, i64, P, C.c_float, C.c_double, i32, P, i32,
+                                                i32, P, i32, C.c_double, C.c_double, P,
+                                                C.POINTER(LearnedSplitInfo)]
     lib.visacd_clip.argtypes = [P, P, i32, P, i32, P, C.POINTER(ClipResult)]
     lib.visacd_measure_fp32_peak.argtypes = [P, C.POINTER(C.c_double)]
     lib.visacd_batch_create.argtypes = [P, i32, C.POINTER(P), P, C.POINTER(P), C.POINTER(P), C.POINTER(P),
@@ -609,6 +623,25 @@ class PlaneProposer:
         _check(lib().visacd_lp_propose(self._h, _ptr(pt), len(pt), _ptr(ed), len(ed), _ptr(c),
                                        float(scale), _ptr(out)), "visacd_lp_propose")
         return out
+
+    def split_search(self, verts, edges, center, scale: float, half: float, refine_k: int, draws,
+                     probe_planes: int, flat_planes=None, flat_k: float = 2.0, tolerance: float = 0.01):
+        """The learned split search of one part in one call
+        (visacd_learned_split_search): (best plane 4 float64, info dict)."""
+        v = np.ascontiguousarray(np.asarray(verts, dtype=np.float64).reshape(-1, 3))
+        ed = _u32(edges, 2)
+        c = np.ascontiguousarray(np.asarray(center, dtype=np.float32).reshape(3))
+        dr = np.ascontiguousarray(np.asarray(draws, dtype=np.int32))
+        fl = None if flat_planes is None or len(flat_planes) == 0 else \
+            np.ascontiguousarray(np.asarray(flat_planes, dtype=np.float64).reshape(-1, 4))
+        best = np.zeros(4, np.float64)
+        info = LearnedSplitInfo()
+        _check(lib().visacd_learned_split_search(self._h, _ptr(v), len(v), _ptr(ed), len(ed), _ptr(c),
+                                                 float(scale), float(half), int(refine_k), _ptr(dr), len(dr),
+                                                 int(probe_planes), _ptr(fl), 0 if fl is None else len(fl),
+                                                 float(flat_k), float(tolerance), _ptr(best),
+                                                 C.byref(info)), "visacd_learned_split_search")
+        return best, info.as_dict()
 
     @staticmethod
     def _batch(feats, labels, weights):

@@ -46,6 +46,27 @@ struct __align__(32) Plane64 {
 };
 enum : uint8_t { kUndecided = 0, kKept = 1, kDropped = 2, kInvalid = 3 };
 
+// The perpendicular-bisector plane of edge idx (lib/src/process.cpp:45-53) in
+// FP64 with the host's operation order; false for edges shorter than 1e-6.
+__device__ __forceinline__ bool edge_bisector(const double* __restrict__ verts,
+                                              const uint32_t* __restrict__ edges, int64_t idx,
+                                              Plane64& pl) {
+  const uint32_t i0 = edges[2 * idx], i1 = edges[2 * idx + 1];
+  const double* p1 = verts + 3 * (int64_t)i0;
+  const double* p2 = verts + 3 * (int64_t)i1;
+  const double nx = __dsub_rn(p2[0], p1[0]), ny = __dsub_rn(p2[1], p1[1]), nz = __dsub_rn(p2[2], p1[2]);
+  const double l =
+      __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(nx, nx), __dmul_rn(ny, ny)), __dmul_rn(nz, nz)));
+  if (l < 1e-6) return false;
+  const double a = __ddiv_rn(nx, l), b = __ddiv_rn(ny, l), c = __ddiv_rn(nz, l);
+  const double mx = __dmul_rn(__dadd_rn(p1[0], p2[0]), 0.5);
+  const double my = __dmul_rn(__dadd_rn(p1[1], p2[1]), 0.5);
+  const double mz = __dmul_rn(__dadd_rn(p1[2], p2[2]), 0.5);
+  const double d = -__dadd_rn(__dadd_rn(__dmul_rn(a, mx), __dmul_rn(b, my)), __dmul_rn(c, mz));
+  pl = Plane64{a, b, c, d};
+  return true;
+}
+
 __global__ void cand_planes_kernel(const double* __restrict__ verts, int32_t n,
                                    const uint32_t* __restrict__ edges, int64_t E,
                                    const int32_t* __restrict__ draws, int32_t D,
@@ -55,25 +76,12 @@ __global__ void cand_planes_kernel(const double* __restrict__ verts, int32_t n,
     const int32_t idx = draws[k];
     uint8_t st = kInvalid;
     Plane64 pl = Plane64{0.0, 0.0, 0.0, 0.0};
-    if (idx >= 0 && (int64_t)idx < E) {
-      const uint32_t i0 = edges[2 * (int64_t)idx], i1 = edges[2 * (int64_t)idx + 1];
-      if (i0 < (uint32_t)n && i1 < (uint32_t)n) {
-        const double* p1 = verts + 3 * (int64_t)i0;
-        const double* p2 = verts + 3 * (int64_t)i1;
-        const double nx = __dsub_rn(p2[0], p1[0]), ny = __dsub_rn(p2[1], p1[1]),
-                     nz = __dsub_rn(p2[2], p1[2]);
-        const double l = __dsqrt_rn(
-            __dadd_rn(__dadd_rn(__dmul_rn(nx, nx), __dmul_rn(ny, ny)), __dmul_rn(nz, nz)));
-        if (!(l < 1e-6)) {
-          const double a = __ddiv_rn(nx, l), b = __ddiv_rn(ny, l), c = __ddiv_rn(nz, l);
-          const double mx = __dmul_rn(__dadd_rn(p1[0], p2[0]), 0.5);
-          const double my = __dmul_rn(__dadd_rn(p1[1], p2[1]), 0.5);
-          const double mz = __dmul_rn(__dadd_rn(p1[2], p2[2]), 0.5);
-          const double d =
-              -__dadd_rn(__dadd_rn(__dmul_rn(a, mx), __dmul_rn(b, my)), __dmul_rn(c, mz));
-          pl = Plane64{a, b, c, d};
-          st = kUndecided;
-        }
+    if (idx >= 0 && (int64_t)idx < E && edges[2 * (int64_t)idx] < (uint32_t)n &&
+        edges[2 * (int64_t)idx + 1] < (uint32_t)n) {
+      if (edge_bisector(verts, edges, idx, pl)) {
+        st = kUndecided;
+      } else {
+        pl = Plane64{0.0, 0.0, 0.0, 0.0};
       }
     }
     planes[k] = pl;
@@ -325,6 +333,282 @@ __global__ void split_argmax_kernel(const double* __restrict__ scores, const Pla
   }
 }
 
+// ---- learned split search --------------------------------------------------
+// Refinement of the proposer's planes: per proposal q, the kRefineK smallest
+// (D, edge) pairs over the edges with a bisector plane b,
+//   D = (2 - 2|c|) + dd^2,  c = n_q . n_b,  dd = (s d_q - d_b) / half,
+//   s = +1 when c >= 0 else -1,
+// in FP64 in this order. Each warp keeps a sorted list of 32 (key, edge)
+// entries, lane l holding the l-th smallest; D maps to an unsigned key with the
+// same order, so (key, edge) compares like (D, edge).
+constexpr int kRefineK = 32;
+constexpr int kRefineTile = 512;  // edges per block step; one warp per proposal
+constexpr int kLearnedProps = 16;
+constexpr int kRefineSlots = kLearnedProps * kRefineK;
+constexpr int kProbeBase = kLearnedProps + kRefineSlots;  // first probe slot
+constexpr unsigned long long kNoKey = ~0ull;
+constexpr int32_t kNoEdge = 0x7fffffff;
+
+struct __align__(16) RefineEntry {
+  unsigned long long key;
+  int32_t edge;
+  int32_t pad;
+};
+
+__device__ __forceinline__ unsigned long long order_key(double v) {
+  if (v != v) return kNoKey - 1;  // NaN after every number
+  if (v == 0.0) v = 0.0;          // -0 with +0
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  return (b >> 63) ? ~b : (b | (1ull << 63));
+}
+
+__device__ __forceinline__ bool entry_less(unsigned long long ka, int32_t ia, unsigned long long kb,
+                                           int32_t ib) {
+  return ka < kb || (ka == kb && ia < ib);
+}
+
+// Offers one candidate per lane to the warp's sorted list (lk, li); all 32
+// lanes call it. A candidate enters when it is below the list's last entry at
+// its turn; the list stays sorted and holds distinct edges.
+__device__ __forceinline__ void warp_offer(unsigned long long& lk, int32_t& li, unsigned long long ck,
+                                           int32_t ci) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const unsigned long long tk = __shfl_sync(full, lk, 31);
+  const int32_t ti = __shfl_sync(full, li, 31);
+  unsigned want = __ballot_sync(full, entry_less(ck, ci, tk, ti));
+  while (want) {
+    const int src = __ffs(want) - 1;
+    want &= want - 1;
+    const unsigned long long xk = __shfl_sync(full, ck, src);
+    const int32_t xi = __shfl_sync(full, ci, src);
+    // Lanes whose entry lies after x: a suffix of the sorted list.
+    const unsigned after = __ballot_sync(full, entry_less(xk, xi, lk, li));
+    if (!after) continue;
+    const int pos = __ffs(after) - 1;
+    const unsigned long long uk = __shfl_up_sync(full, lk, 1);
+    const int32_t ui = __shfl_up_sync(full, li, 1);
+    if (lane == pos) {
+      lk = xk;
+      li = xi;
+    } else if (lane > pos) {
+      lk = uk;
+      li = ui;
+    }
+  }
+}
+
+// Pass 1: block b scans edges [b chunk, (b + 1) chunk); warp q keeps
+// proposal q's 32 nearest bisectors of the chunk and writes them to
+// partial[b][q][0..32). The block computes each bisector once per tile.
+__global__ void __launch_bounds__(kRefineTile) refine_partial_kernel(
+    const double* __restrict__ verts, const uint32_t* __restrict__ edges, int64_t E,
+    const double* __restrict__ props, double half, int64_t chunk, RefineEntry* __restrict__ partial) {
+  __shared__ Plane64 tile[kRefineTile];
+  __shared__ uint8_t valid[kRefineTile];
+  const int q = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const double pa = props[4 * q], pb = props[4 * q + 1], pc = props[4 * q + 2], pd = props[4 * q + 3];
+  unsigned long long lk = kNoKey;
+  int32_t li = kNoEdge;
+  const int64_t begin = (int64_t)blockIdx.x * chunk;
+  const int64_t end = min(E, begin + chunk);
+  for (int64_t base = begin; base < end; base += kRefineTile) {
+    const int64_t i = base + threadIdx.x;
+    Plane64 pl = Plane64{0.0, 0.0, 0.0, 0.0};
+    valid[threadIdx.x] = (i < end) && edge_bisector(verts, edges, i, pl);
+    tile[threadIdx.x] = pl;
+    __syncthreads();
+    for (int j = 0; j < kRefineTile; j += 32) {
+      const int t = j + lane;
+      unsigned long long ck = kNoKey;
+      int32_t ci = kNoEdge;
+      if (valid[t]) {
+        const Plane64 b = tile[t];
+        const double c = __dadd_rn(__dadd_rn(__dmul_rn(pa, b.x), __dmul_rn(pb, b.y)), __dmul_rn(pc, b.z));
+        const double sg = c >= 0 ? 1.0 : -1.0;
+        const double dd = __ddiv_rn(__dsub_rn(__dmul_rn(sg, pd), b.w), half);
+        const double D = __dadd_rn(__dsub_rn(2.0, __dmul_rn(2.0, fabs(c))), __dmul_rn(dd, dd));
+        ck = order_key(D);
+        ci = (int32_t)(base + t);
+      }
+      warp_offer(lk, li, ck, ci);
+    }
+    __syncthreads();
+  }
+  partial[((int64_t)blockIdx.x * kLearnedProps + q) * kRefineK + lane] = RefineEntry{lk, li, 0};
+}
+
+// Pass 2 (one block of 16 warps): merges the blocks' lists per proposal,
+// keeps the first `per` entries of each, and writes the union's bisector
+// planes in edge order to out64/out32 [0, n) (zeros in [n, 512)); n to
+// *n_refined.
+__global__ void __launch_bounds__(kRefineTile) refine_merge_kernel(
+    const RefineEntry* __restrict__ partial, int32_t blocks, int32_t per,
+    const double* __restrict__ verts, const uint32_t* __restrict__ edges, Plane64* __restrict__ out64,
+    float4* __restrict__ out32, int32_t* __restrict__ n_refined) {
+  __shared__ int32_t sel[kRefineSlots];
+  __shared__ int warp_base[kLearnedProps + 1];
+  const int t = threadIdx.x, q = t >> 5, lane = t & 31;
+  unsigned long long lk = kNoKey;
+  int32_t li = kNoEdge;
+  for (int b = 0; b < blocks; ++b) {
+    const RefineEntry e = partial[((int64_t)b * kLearnedProps + q) * kRefineK + lane];
+    warp_offer(lk, li, e.key, e.edge);
+  }
+  sel[t] = (lane < per) ? li : kNoEdge;
+  __syncthreads();
+  // Bitonic sort of the 512 edge indices, ascending.
+  for (int k = 2; k <= kRefineSlots; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      const int x = t ^ j;
+      if (x > t) {
+        const int32_t a = sel[t], b = sel[x];
+        if ((a > b) == ((t & k) == 0)) {
+          sel[t] = b;
+          sel[x] = a;
+        }
+      }
+      __syncthreads();
+    }
+  }
+  const int32_t v = sel[t];
+  const bool keep = v != kNoEdge && (t == 0 || sel[t - 1] != v);
+  const unsigned m = __ballot_sync(0xffffffffu, keep);
+  if (lane == 0) warp_base[q + 1] = __popc(m);
+  __syncthreads();
+  if (t == 0) {
+    warp_base[0] = 0;
+    for (int w = 1; w <= kLearnedProps; ++w) warp_base[w] += warp_base[w - 1];
+    *n_refined = warp_base[kLearnedProps];
+  }
+  __syncthreads();
+  const int n = warp_base[kLearnedProps];
+  if (keep) {
+    const int pos = warp_base[q] + __popc(m & ((1u << lane) - 1u));
+    Plane64 pl = Plane64{0.0, 0.0, 0.0, 0.0};
+    edge_bisector(verts, edges, v, pl);
+    out64[pos] = pl;
+    out32[pos] = make_float4((float)pl.x, (float)pl.y, (float)pl.z, (float)pl.w);
+  }
+  if (t >= n) {
+    out64[t] = Plane64{0.0, 0.0, 0.0, 0.0};
+    out32[t] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+}
+
+// The scored plane list of the learned search: [0, 16) proposals, [16, 528)
+// refined (written by refine_merge_kernel), [528, 528 + probe_slots) the kept
+// probe candidates (zeros after them), then the F flat planes.
+__global__ void learned_assemble_kernel(const double* __restrict__ props, const Plane64* __restrict__ probe,
+                                        const int32_t* __restrict__ cinfo, int32_t probe_slots,
+                                        const double* __restrict__ flat, int32_t F,
+                                        Plane64* __restrict__ out64, float4* __restrict__ out32) {
+  const int n_probe = cinfo[0];
+  const int total = kLearnedProps + probe_slots + F;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+    Plane64 p = Plane64{0.0, 0.0, 0.0, 0.0};
+    int slot;
+    if (i < kLearnedProps) {
+      p = Plane64{props[4 * i], props[4 * i + 1], props[4 * i + 2], props[4 * i + 3]};
+      slot = i;
+    } else if (i < kLearnedProps + probe_slots) {
+      const int r = i - kLearnedProps;
+      if (r < n_probe) p = probe[r];
+      slot = kProbeBase + r;
+    } else {
+      const int r = i - kLearnedProps - probe_slots;
+      p = Plane64{flat[4 * r], flat[4 * r + 1], flat[4 * r + 2], flat[4 * r + 3]};
+      slot = kProbeBase + probe_slots + r;
+    }
+    out64[slot] = p;
+    out32[slot] = make_float4((float)p.x, (float)p.y, (float)p.z, (float)p.w);
+  }
+}
+
+struct LearnedOut {
+  double plane[4];
+  double score, best_prop, best_probe;
+  int32_t index, n_refined, n_probe, draws_used, fallback;
+  uint32_t score_status, recheck_count, pad;
+};
+
+// The decision over [proposals, refined, probe, flat x flat_k] (FP64 scores,
+// as the host compares them): the best proposal or refined score, the best
+// probe score (from 0), fallback when the former is below (1 - tol) x the
+// latter, and the first maximum of all.
+__global__ void learned_decide_kernel(const double* __restrict__ scores, const Plane64* __restrict__ planes,
+                                      const int32_t* __restrict__ n_refined_p,
+                                      const int32_t* __restrict__ cinfo, int32_t probe_slots, int32_t F,
+                                      double flat_k, double tol, const unsigned* __restrict__ score_status,
+                                      const unsigned* __restrict__ recheck_count,
+                                      LearnedOut* __restrict__ out) {
+  const int n_ref = *n_refined_p, n_probe = cinfo[0];
+  const int n_prop = kLearnedProps + n_ref;
+  const int total = n_prop + n_probe + F;
+  double best = -1.0 / 0.0, bprop = -1.0 / 0.0, bprobe = 0.0;
+  int best_r = 0x7fffffff;
+  for (int r = threadIdx.x; r < total; r += blockDim.x) {
+    int slot;
+    double v;
+    if (r < n_prop) {
+      slot = r;
+      v = scores[slot];
+      bprop = fmax(bprop, v);
+    } else if (r < n_prop + n_probe) {
+      slot = kProbeBase + (r - n_prop);
+      v = scores[slot];
+      bprobe = fmax(bprobe, v);
+    } else {
+      slot = kProbeBase + probe_slots + (r - n_prop - n_probe);
+      v = __dmul_rn(scores[slot], flat_k);
+    }
+    if (v > best || (v == best && r < best_r)) {
+      best = v;
+      best_r = r;
+    }
+  }
+  __shared__ double sv[1024], sp[1024], sq[1024];
+  __shared__ int si[1024];
+  sv[threadIdx.x] = best;
+  si[threadIdx.x] = best_r;
+  sp[threadIdx.x] = bprop;
+  sq[threadIdx.x] = bprobe;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o; o >>= 1) {
+    if ((int)threadIdx.x < o) {
+      const int u = threadIdx.x + o;
+      if (sv[u] > sv[threadIdx.x] || (sv[u] == sv[threadIdx.x] && si[u] < si[threadIdx.x])) {
+        sv[threadIdx.x] = sv[u];
+        si[threadIdx.x] = si[u];
+      }
+      sp[threadIdx.x] = fmax(sp[threadIdx.x], sp[u]);
+      sq[threadIdx.x] = fmax(sq[threadIdx.x], sq[u]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const int r = si[0];
+    out->n_refined = n_ref;
+    out->n_probe = n_probe;
+    out->draws_used = cinfo[1];
+    out->best_prop = sp[0];
+    out->best_probe = sq[0];
+    out->fallback = sp[0] < __dmul_rn(__dsub_rn(1.0, tol), sq[0]) ? 1 : 0;
+    out->score_status = score_status ? *score_status : 0u;
+    out->recheck_count = recheck_count ? *recheck_count : 0u;
+    const int slot = r < n_prop ? r
+                     : (r < n_prop + n_probe ? kProbeBase + (r - n_prop)
+                                             : kProbeBase + probe_slots + (r - n_prop - n_probe));
+    const Plane64 p = planes[slot];
+    out->index = r;
+    out->score = sv[0];
+    out->plane[0] = p.x;
+    out->plane[1] = p.y;
+    out->plane[2] = p.z;
+    out->plane[3] = p.w;
+  }
+}
+
 // Scratch of one candidate-plane generation, carved from the context's slot.
 struct CandScratch {
   Plane64* planes;   // D
@@ -557,6 +841,100 @@ extern "C" int visacd_split_search(visacd_ctx* ctx, const double* verts, int32_t
     info->n_candidates = r.n_planes;
     info->draws_used = r.draws_used;
     info->best_score = r.score;
+  }
+  return VISACD_OK;
+}
+
+extern "C" int visacd_learned_split_search(visacd_lp* lp, const double* verts, int32_t n,
+                                           const uint32_t* edges, int64_t E, const float* center,
+                                           float scale, double half, int32_t refine_k,
+                                           const int32_t* probe_draws, int32_t n_probe_draws,
+                                           int32_t probe_planes, const double* flat_planes, int32_t n_flat,
+                                           double flat_k, double tolerance, double* best_plane,
+                                           visacd_learned_split_info* info) {
+  VCHECK(lp, VISACD_ERR_INVALID_ARG, "learned_split_search: null proposer");
+  visacd_ctx* ctx = lp_context(lp);
+  VCHECK(ctx, VISACD_ERR_INVALID_ARG, "learned_split_search: the proposer's context was destroyed");
+  VTRY(check_args(verts, n, edges, E, probe_draws, n_probe_draws, probe_planes));
+  VCHECK(n > 0 && E > 0, VISACD_ERR_INVALID_ARG, "learned_split_search: a part without visibility edges");
+  VCHECK(center && best_plane, VISACD_ERR_INVALID_ARG, "learned_split_search: center or best_plane is NULL");
+  VCHECK(scale > 0.f && half > 0.0, VISACD_ERR_INVALID_ARG,
+         "learned_split_search: scale and half must be positive");
+  VCHECK(refine_k >= 0 && refine_k <= kRefineK, VISACD_ERR_INVALID_ARG,
+         "learned_split_search: refine_k must be in [0, 32]");
+  VCHECK(n_flat >= 0 && (n_flat == 0 || flat_planes), VISACD_ERR_INVALID_ARG,
+         "learned_split_search: flat_planes is NULL");
+  VCUDA(cudaSetDevice(ctx->device));
+  const int32_t probe_slots = std::max(0, std::min(probe_planes, n_probe_draws));
+  CandScratch s;
+  VTRY(generate(ctx, verts, n, edges, E, probe_draws, n_probe_draws, probe_planes, flat_planes, n_flat,
+                std::max(1, probe_slots), s));
+  VTRY(ensure_slot(ctx, kSlotPoints, (size_t)n * 12));
+  float* pts32 = slot<float>(ctx, kSlotPoints);
+  VLAUNCH(ctx, kKCandidates, grid_for(3LL * n, 256, 4LL * ctx->sm_count), 256, 0, f64_to_f32_kernel, s.verts,
+          pts32, 3LL * n);
+
+  // Refinement blocks: up to two per SM, each a whole number of tiles.
+  const int64_t tiles = (E + kRefineTile - 1) / kRefineTile;
+  const int64_t want = std::min<int64_t>(tiles, 2LL * ctx->sm_count);
+  const int64_t chunk = ((tiles + want - 1) / want) * kRefineTile;
+  const int32_t blocks = (int32_t)((E + chunk - 1) / chunk);
+  const int32_t P = kProbeBase + probe_slots + n_flat;
+  const size_t b_props = 256 * 2, b_partial = align256((size_t)blocks * kRefineSlots * sizeof(RefineEntry)),
+               b_o64 = align256((size_t)P * sizeof(Plane64)), b_o32 = align256((size_t)P * sizeof(float4)),
+               b_nref = 256, b_out = align256(sizeof(LearnedOut));
+  VTRY(ensure_slot(ctx, kSlotLearned, b_props + b_partial + b_o64 + b_o32 + b_nref + b_out));
+  char* p = slot<char>(ctx, kSlotLearned);
+  double* props = reinterpret_cast<double*>(p);
+  RefineEntry* partial = reinterpret_cast<RefineEntry*>(p + b_props);
+  Plane64* L64 = reinterpret_cast<Plane64*>(p + b_props + b_partial);
+  float4* L32 = reinterpret_cast<float4*>(p + b_props + b_partial + b_o64);
+  int32_t* nref = reinterpret_cast<int32_t*>(p + b_props + b_partial + b_o64 + b_o32);
+  LearnedOut* dout = reinterpret_cast<LearnedOut*>(p + b_props + b_partial + b_o64 + b_o32 + b_nref);
+
+  VTRY(lp_propose_device(lp, pts32, n, s.edges, E, center, scale, props));
+  VLAUNCH(ctx, kKLpRefine, blocks, kRefineTile, 0, refine_partial_kernel, s.verts, s.edges, E, props, half,
+          chunk, partial);
+  VLAUNCH(ctx, kKLpRefine, 1, kRefineTile, 0, refine_merge_kernel, partial, blocks, refine_k, s.verts,
+          s.edges, L64 + kLearnedProps, L32 + kLearnedProps, nref);
+  VLAUNCH(ctx, kKLpSplit, grid_for(kLearnedProps + probe_slots + n_flat, 256, 64), 256, 0,
+          learned_assemble_kernel, props, s.out64, s.info, probe_slots, s.flat, n_flat, L64, L32);
+
+  VTRY(ensure_slot(ctx, kSlotScores, (size_t)P * 8));
+  double* scores = slot<double>(ctx, kSlotScores);
+  unsigned rcap = score_recheck_capacity(P, E);
+  LearnedOut* h = nullptr;
+  VTRY(pinned(ctx, sizeof(LearnedOut), (void**)&h));
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    const unsigned* st_status = nullptr;
+    const unsigned* st_count = nullptr;
+    VTRY(score_planes_device_async(ctx, reinterpret_cast<const float*>(L32), P, pts32, n, s.edges, E, scores,
+                                   rcap, &st_status, &st_count));
+    VLAUNCH(ctx, kKLpSplit, 1, 1024, 0, learned_decide_kernel, scores, L64, nref, s.info, probe_slots,
+            n_flat, flat_k, tolerance, st_status, st_count, dout);
+    VCUDA(cudaMemcpyAsync(h, dout, sizeof(LearnedOut), cudaMemcpyDeviceToHost, ctx->stream));
+    VCUDA(stream_wait(ctx));
+    VCHECK(!(h->score_status & kStatusMbarrierTimeout), VISACD_ERR_DEVICE,
+           "learned_split_search: a bulk-copy wait of the scoring kernel timed out");
+    if (!(h->score_status & kStatusRecheckOverflow)) break;
+    VCHECK(attempt == 0, VISACD_ERR_DEVICE, "learned_split_search: FP64 queue overflow after a rerun");
+    rcap = h->recheck_count;
+  }
+  // The read-back shares the pinned staging area with the status check: copy
+  // it out first.
+  const LearnedOut r = *h;
+  VTRY(check_status(ctx, "learned_split_search"));
+  for (int c = 0; c < 4; ++c) best_plane[c] = r.plane[c];
+  if (info) {
+    info->best_index = r.index;
+    info->n_refined = r.n_refined;
+    info->n_probe = r.n_probe;
+    info->draws_used = r.draws_used;
+    info->fallback = r.fallback;
+    info->reserved = 0;
+    info->best_score = r.score;
+    info->best_proposal_score = r.best_prop;
+    info->best_probe_score = r.best_probe;
   }
   return VISACD_OK;
 }

@@ -117,6 +117,7 @@ enum CtxSlot {
   kSlotCandidates,
   kSlotCandLinks,
   kSlotVisMulti,
+  kSlotLearned,
   kSlotCount
 };
 
@@ -140,6 +141,7 @@ struct visacd_ctx {
   std::unordered_map<uint32_t, int> vis_tuned;    // shape class -> autotuned variant
   visacd_clip_result clip_out{};                  // last clip result (device-resident)
   std::vector<visacd_bvh*> bvhs;                  // live BVHs built on this context
+  std::vector<visacd_lp*> lps;                    // live proposers made on this context
   int clip_nv = 0;
   int32_t sdf_nv = 0, sdf_nt = 0;                 // last SDF remesh result (device-resident)
   void* clip_ptrs[7] = {nullptr};
@@ -195,6 +197,8 @@ enum KernelId {
   kKHullDist,
   kKSegTri,
   kKCandidates,
+  kKLpRefine,
+  kKLpSplit,
   kKMisc,
   kKCount
 };
@@ -298,6 +302,17 @@ int score_planes_device_async(visacd_ctx* ctx, const float* d_planes, int32_t P,
                               int32_t N, const uint32_t* d_edges, int64_t E, double* d_scores,
                               unsigned rcap, const unsigned** d_status, const unsigned** d_recheck_count);
 unsigned score_recheck_capacity(int32_t P, int64_t E);
+
+// The learned proposer on a part already on the device (learned.cu): f32
+// points, edge pairs, the part's frame (centre, half extent). Writes its 16
+// planes, FP64 in the input frame, to d_planes (16 x 4 doubles) without a
+// host wait.
+visacd_ctx* lp_context(visacd_lp* lp);
+// Releases a proposer's device memory and unbinds it from its context (on
+// context destruction; the host side stays until visacd_lp_destroy).
+void lp_detach(visacd_lp* lp);
+int lp_propose_device(visacd_lp* lp, const float* d_pts, int32_t n, const uint32_t* d_edges, int64_t E,
+                      const float* center, float scale, double* d_planes);
 
 }  // namespace vgpu
 

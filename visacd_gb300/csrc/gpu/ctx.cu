@@ -87,7 +87,7 @@ static const char* kNames[kKCount] = {
     "lp_gemm",       "lp_pool",        "lp_loss",      "lp_adam",
     "lp_misc",       "sdf_remesh",     "sdf_dist",     "sdf_cross",
     "hull_dist",     "seg_tri",        "candidates",
-    "misc"};
+    "lp_refine",     "lp_split",       "misc"};
 
 const char* kernel_name(int id) { return (id >= 0 && id < kKCount) ? kNames[id] : "?"; }
 
@@ -578,6 +578,9 @@ extern "C" int visacd_ctx_destroy(visacd_ctx* ctx) {
   // BVHs still alive lose their device memory with their context.
   for (visacd_bvh* b : ctx->bvhs) bvh_detach(b);
   ctx->bvhs.clear();
+  // So do proposers: destroying one afterwards only frees its host side.
+  for (visacd_lp* lp : ctx->lps) lp_detach(lp);
+  ctx->lps.clear();
   for (int i = 0; i < kSlotCount; ++i) release(ctx->buf[i]);
   cudaStreamSynchronize(ctx->stream);
   if (ctx->d_status) cudaFree(ctx->d_status);

@@ -18,6 +18,7 @@
 // back to the full candidate draw when a probe says the proposals are worse.
 #include <cuda_bf16.h>
 
+#include <cstring>
 #include <random>
 
 #include "common.cuh"
@@ -656,6 +657,23 @@ __global__ void lp_to_bf16_kernel(const float* __restrict__ p, int count, bf16* 
   if (i < count) pb[i] = __float2bfloat16_rn(p[i]);
 }
 
+// The proposals back in the part's input frame. The network sees (x - c) / s,
+// so n . (x - c) / s + d' = 0 gives d = s d' - n . c, in FP64 in this order
+// (explicit round-to-nearest, no contraction): the planes are the same on
+// every path that asks for them.
+__global__ void lp_frame_kernel(const float* __restrict__ pl, float cx, float cy, float cz, float s,
+                                double* __restrict__ out) {
+  const int q = threadIdx.x;
+  if (q >= kPlanes) return;
+  const double nx = pl[4 * q], ny = pl[4 * q + 1], nz = pl[4 * q + 2];
+  const double nc = __dadd_rn(__dadd_rn(__dmul_rn(nx, (double)cx), __dmul_rn(ny, (double)cy)),
+                              __dmul_rn(nz, (double)cz));
+  out[4 * q] = nx;
+  out[4 * q + 1] = ny;
+  out[4 * q + 2] = nz;
+  out[4 * q + 3] = __dsub_rn(__dmul_rn((double)s, (double)pl[4 * q + 3]), nc);
+}
+
 }  // namespace
 
 struct visacd_lp {
@@ -666,7 +684,14 @@ struct visacd_lp {
   DevBuf params, params_bf16, grads, adam_m, adam_v;
   DevBuf x0, a1, a2, a3, poolkey, g, gb, arg, a4, a5, z6;
   DevBuf dz6, dz5, dz4, dg, dz3, dz2, dz1;
-  DevBuf parts, labels, lw, loss, feats, planes, pts, edges;
+  DevBuf parts, labels, lw, loss, feats, planes, pts, edges, frame;
+  template <class F>
+  void each_buf(F f) {
+    for (DevBuf* b : {&params, &params_bf16, &grads, &adam_m, &adam_v, &x0, &a1, &a2, &a3, &poolkey, &g, &gb,
+                      &arg, &a4, &a5, &z6, &dz6, &dz5, &dz4, &dg, &dz3, &dz2, &dz1, &parts, &labels, &lw,
+                      &loss, &feats, &planes, &pts, &edges, &frame})
+      f(*b);
+  }
 };
 
 namespace {
@@ -881,11 +906,8 @@ extern "C" int visacd_lp_create(visacd_ctx* ctx, const float* params, uint32_t s
   VCUDA(cudaSetDevice(ctx->device));
   visacd_lp* lp = new visacd_lp();
   lp->ctx = ctx;
-  for (DevBuf* b : {&lp->params, &lp->params_bf16, &lp->grads, &lp->adam_m, &lp->adam_v, &lp->x0, &lp->a1,
-                    &lp->a2, &lp->a3, &lp->poolkey, &lp->g, &lp->gb, &lp->arg, &lp->a4, &lp->a5, &lp->z6,
-                    &lp->dz6, &lp->dz5, &lp->dz4, &lp->dg, &lp->dz3, &lp->dz2, &lp->dz1, &lp->parts,
-                    &lp->labels, &lp->lw, &lp->loss, &lp->feats, &lp->planes, &lp->pts, &lp->edges})
-    b->stream = ctx->stream;
+  ctx->lps.push_back(lp);
+  lp->each_buf([&](DevBuf& b) { b.stream = ctx->stream; });
   const size_t pb = (size_t)kOff.total * 4;
   int rc = VISACD_OK;
   auto fail = [&](int code) {
@@ -936,18 +958,18 @@ extern "C" int visacd_lp_create(visacd_ctx* ctx, const float* params, uint32_t s
 
 extern "C" int visacd_lp_destroy(visacd_lp* lp) {
   if (!lp) return VISACD_OK;
-  for (DevBuf* b : {&lp->params, &lp->params_bf16, &lp->grads, &lp->adam_m, &lp->adam_v, &lp->x0, &lp->a1,
-                    &lp->a2, &lp->a3, &lp->poolkey, &lp->g, &lp->gb, &lp->arg, &lp->a4, &lp->a5, &lp->z6,
-                    &lp->dz6, &lp->dz5, &lp->dz4, &lp->dg, &lp->dz3, &lp->dz2, &lp->dz1, &lp->parts,
-                    &lp->labels, &lp->lw, &lp->loss, &lp->feats, &lp->planes, &lp->pts, &lp->edges})
-    vgpu::release(*b);
-  cudaStreamSynchronize(lp->ctx->stream);
+  if (lp->ctx) {
+    auto& v = lp->ctx->lps;
+    v.erase(std::remove(v.begin(), v.end(), lp), v.end());
+    vgpu::lp_detach(lp);
+  }
   delete lp;
   return VISACD_OK;
 }
 
 extern "C" int visacd_lp_get_params(visacd_lp* lp, float* out) {
   VCHECK(lp && out, VISACD_ERR_INVALID_ARG, "lp_get_params: null argument");
+  VCHECK(lp->ctx, VISACD_ERR_INVALID_ARG, "lp_get_params: the proposer's context was destroyed");
   VCUDA(cudaMemcpyAsync(out, lp->params.p, (size_t)kOff.total * 4, cudaMemcpyDeviceToHost, lp->ctx->stream));
   VCUDA(vgpu::stream_wait(lp->ctx));
   return VISACD_OK;
@@ -956,6 +978,7 @@ extern "C" int visacd_lp_get_params(visacd_lp* lp, float* out) {
 extern "C" int visacd_lp_features(visacd_lp* lp, const float* points, int32_t n, const uint32_t* edges,
                                   int64_t E, const float* center, float scale, float* feats_out) {
   VCHECK(lp && center && feats_out && scale > 0.f, VISACD_ERR_INVALID_ARG, "lp_features: bad argument");
+  VCHECK(lp->ctx, VISACD_ERR_INVALID_ARG, "lp_features: the proposer's context was destroyed");
   visacd_ctx* ctx = lp->ctx;
   VCUDA(cudaSetDevice(ctx->device));
   VTRY(upload_part(ctx, lp, points, n, edges, E));
@@ -970,6 +993,7 @@ extern "C" int visacd_lp_features(visacd_lp* lp, const float* points, int32_t n,
 
 extern "C" int visacd_lp_forward(visacd_lp* lp, const float* feats, int32_t B, float* planes_out) {
   VCHECK(lp && feats && planes_out && B > 0, VISACD_ERR_INVALID_ARG, "lp_forward: bad argument");
+  VCHECK(lp->ctx, VISACD_ERR_INVALID_ARG, "lp_forward: the proposer's context was destroyed");
   visacd_ctx* ctx = lp->ctx;
   VCUDA(cudaSetDevice(ctx->device));
   VTRY(upload_batch(lp, feats, B, nullptr, nullptr, 0));
@@ -982,35 +1006,58 @@ extern "C" int visacd_lp_forward(visacd_lp* lp, const float* feats, int32_t B, f
   return VISACD_OK;
 }
 
+namespace vgpu {
+
+visacd_ctx* lp_context(visacd_lp* lp) { return lp->ctx; }
+
+void lp_detach(visacd_lp* lp) {
+  cudaSetDevice(lp->ctx->device);
+  lp->each_buf([](DevBuf& b) { release(b); });
+  cudaStreamSynchronize(lp->ctx->stream);
+  lp->ctx = nullptr;
+}
+
+int lp_propose_device(visacd_lp* lp, const float* d_pts, int32_t n, const uint32_t* d_edges, int64_t E,
+                      const float* center, float scale, double* d_planes) {
+  VCHECK(lp && d_pts && d_edges && center && d_planes && n > 0 && E > 0 && scale > 0.f,
+         VISACD_ERR_INVALID_ARG, "lp_propose: bad argument");
+  visacd_ctx* ctx = lp->ctx;
+  VTRY(alloc_batch(lp, 1));
+  VLAUNCH(ctx, kKLpFeatures, kPts / 256, 256, 0, lp_features_kernel, d_pts, d_edges, E, n, center[0],
+          center[1], center[2], 1.f / scale, (float*)nullptr, P<bf16>(lp->x0), ctx->d_status);
+  VTRY(forward(lp, 1));
+  VLAUNCH(ctx, kKLpLoss, 1, 32, 0, lp_planes_kernel, P<float>(lp->z6), 1, P<float>(lp->planes));
+  VLAUNCH(ctx, kKLpMisc, 1, 32, 0, lp_frame_kernel, P<float>(lp->planes), center[0], center[1], center[2],
+          scale, d_planes);
+  return VISACD_OK;
+}
+
+}  // namespace vgpu
+
 extern "C" int visacd_lp_propose(visacd_lp* lp, const float* points, int32_t n, const uint32_t* edges,
                                  int64_t E, const float* center, float scale, double* planes_out) {
   VCHECK(lp && center && planes_out && scale > 0.f, VISACD_ERR_INVALID_ARG, "lp_propose: bad argument");
+  VCHECK(lp->ctx, VISACD_ERR_INVALID_ARG, "lp_propose: the proposer's context was destroyed");
   visacd_ctx* ctx = lp->ctx;
   VCUDA(cudaSetDevice(ctx->device));
   VTRY(upload_part(ctx, lp, points, n, edges, E));
-  VTRY(alloc_batch(lp, 1));
-  VLAUNCH(ctx, vgpu::kKLpFeatures, kPts / 256, 256, 0, lp_features_kernel, P<float>(lp->pts),
-          P<uint32_t>(lp->edges), E, n, center[0], center[1], center[2], 1.f / scale, (float*)nullptr,
-          P<bf16>(lp->x0), ctx->d_status);
-  VTRY(forward(lp, 1));
-  VLAUNCH(ctx, vgpu::kKLpLoss, 1, 32, 0, lp_planes_kernel, P<float>(lp->z6), 1, P<float>(lp->planes));
-  float pl[kPlanes * 4];
-  VCUDA(cudaMemcpyAsync(pl, lp->planes.p, sizeof(pl), cudaMemcpyDeviceToHost, ctx->stream));
-  VTRY(vgpu::check_status(ctx, "lp_propose"));
-  // Back to the input frame: n . (x - c) / s + d' = 0  =>  d = s d' - n . c.
-  for (int q = 0; q < kPlanes; ++q) {
-    const double nx = pl[4 * q], ny = pl[4 * q + 1], nz = pl[4 * q + 2];
-    planes_out[4 * q] = nx;
-    planes_out[4 * q + 1] = ny;
-    planes_out[4 * q + 2] = nz;
-    planes_out[4 * q + 3] = (double)scale * pl[4 * q + 3] - (nx * center[0] + ny * center[1] + nz * center[2]);
-  }
-  return VISACD_OK;
+  VTRY(ensure(lp->frame, (size_t)kPlanes * 32));
+  VTRY(vgpu::lp_propose_device(lp, P<float>(lp->pts), n, P<uint32_t>(lp->edges), E, center, scale,
+                               P<double>(lp->frame)));
+  double* h = nullptr;
+  VTRY(vgpu::pinned(ctx, (size_t)kPlanes * 32, (void**)&h));
+  VCUDA(cudaMemcpyAsync(h, lp->frame.p, (size_t)kPlanes * 32, cudaMemcpyDeviceToHost, ctx->stream));
+  VCUDA(vgpu::stream_wait(ctx));
+  // The read-back shares the pinned staging area with the status check: copy
+  // it out first.
+  std::memcpy(planes_out, h, (size_t)kPlanes * 32);
+  return vgpu::check_status(ctx, "lp_propose");
 }
 
 extern "C" int visacd_lp_grads(visacd_lp* lp, const float* feats, const float* labels, const float* lw,
                                int32_t B, int32_t L, float* grads_out, float* loss_out) {
   VCHECK(lp && feats && labels && lw && B > 0 && L > 0, VISACD_ERR_INVALID_ARG, "lp_grads: bad argument");
+  VCHECK(lp->ctx, VISACD_ERR_INVALID_ARG, "lp_grads: the proposer's context was destroyed");
   visacd_ctx* ctx = lp->ctx;
   VCUDA(cudaSetDevice(ctx->device));
   VTRY(upload_batch(lp, feats, B, labels, lw, L));
@@ -1045,6 +1092,7 @@ extern "C" int visacd_lp_train_step(visacd_lp* lp, const float* feats, const flo
 
 extern "C" int visacd_lp_set_tcgen05(visacd_lp* lp, int enable) {
   VCHECK(lp, VISACD_ERR_INVALID_ARG, "lp_set_tcgen05: null proposer");
+  VCHECK(lp->ctx, VISACD_ERR_INVALID_ARG, "lp_set_tcgen05: the proposer's context was destroyed");
   if (enable) {
     VCUDA(cudaSetDevice(lp->ctx->device));
     VCUDA(cudaFuncSetAttribute(lp_gemm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem));

@@ -99,7 +99,7 @@ struct Config {
   std::string plane_proposer = "exhaustive";
   std::string proposer_weights;  // float32 parameter file of the proposer
   int proposer_probe_planes = 64;
-  int proposer_refine = 32;  // bisector planes kept per proposal in the refinement
+  int proposer_refine = 32;  // bisector planes kept per proposal in the refinement (0..32)
   double proposer_tolerance = 0.01;
 };
 

@@ -481,9 +481,9 @@ std::shared_ptr<const std::vector<float>> proposer_params(const std::string& pat
 }
 }  // namespace
 
-std::vector<Plane> propose_planes(const Mesh& mesh) {
-  double t0 = now_ms();
-  visacd_ctx* ctx = context();
+namespace {
+// This thread's proposer on its context, made from config().proposer_weights.
+visacd_lp* proposer(visacd_ctx* ctx) {
   if (!tl_lp || tl_lp_ctx != ctx || tl_lp_path != config().proposer_weights) {
     if (tl_lp) visacd_lp_destroy(tl_lp);
     tl_lp = nullptr;
@@ -492,12 +492,28 @@ std::vector<Plane> propose_planes(const Mesh& mesh) {
     tl_lp_ctx = ctx;
     tl_lp_path = config().proposer_weights;
   }
-  // The part's frame: bounding-box centre and half of the longest extent.
+  return tl_lp;
+}
+
+// The part's frame for the proposer: bounding-box centre (float) and half of
+// the longest extent (1 for a point).
+void part_frame(const Mesh& mesh, float center[3], double& half) {
   auto b = bbox(mesh);
-  const float center[3] = {(float)(0.5 * (b[0] + b[1])), (float)(0.5 * (b[2] + b[3])),
-                           (float)(0.5 * (b[4] + b[5]))};
-  double half = 0.5 * std::max(b[1] - b[0], std::max(b[3] - b[2], b[5] - b[4]));
+  center[0] = (float)(0.5 * (b[0] + b[1]));
+  center[1] = (float)(0.5 * (b[2] + b[3]));
+  center[2] = (float)(0.5 * (b[4] + b[5]));
+  half = 0.5 * std::max(b[1] - b[0], std::max(b[3] - b[2], b[5] - b[4]));
   if (!(half > 0)) half = 1.0;
+}
+}  // namespace
+
+std::vector<Plane> propose_planes(const Mesh& mesh) {
+  double t0 = now_ms();
+  visacd_ctx* ctx = context();
+  visacd_lp* lp = proposer(ctx);
+  float center[3];
+  double half;
+  part_frame(mesh, center, half);
   std::vector<float> v;
   to_f32(mesh.vertices, v);
   std::vector<uint32_t> e(2 * mesh.intersecting_edges.size());
@@ -506,7 +522,7 @@ std::vector<Plane> propose_planes(const Mesh& mesh) {
     e[2 * k + 1] = mesh.intersecting_edges[k].second;
   }
   double out[VISACD_LP_PLANES * 4];
-  check(visacd_lp_propose(tl_lp, v.data(), (int32_t)mesh.vertices.size(), e.data(),
+  check(visacd_lp_propose(lp, v.data(), (int32_t)mesh.vertices.size(), e.data(),
                           (int64_t)mesh.intersecting_edges.size(), center, (float)half, out),
         "visacd_lp_propose");
   std::vector<Plane> planes;
@@ -516,6 +532,51 @@ std::vector<Plane> propose_planes(const Mesh& mesh) {
   c.lp_calls++;
   c.lp_ms += now_ms() - t0;
   return planes;
+}
+
+bool learned_split_search(const Mesh& mesh, const std::vector<Plane>& flat_planes, double flat_k, Plane& out,
+                          bool& fallback) {
+  const auto& edges = mesh.intersecting_edges;
+  fallback = false;
+  if (edges.empty()) return false;
+  double t0 = now_ms();
+  visacd_ctx* ctx = context();
+  visacd_lp* lp = proposer(ctx);
+  float center[3];
+  double half;
+  part_frame(mesh, center, half);
+  const int probe = config().proposer_probe_planes;
+  const DrawPlan plan = plan_draws(edges.size(), probe);
+  std::vector<double> flat(4 * flat_planes.size());
+  for (size_t i = 0; i < flat_planes.size(); ++i) {
+    flat[4 * i] = flat_planes[i].a;
+    flat[4 * i + 1] = flat_planes[i].b;
+    flat[4 * i + 2] = flat_planes[i].c;
+    flat[4 * i + 3] = flat_planes[i].d;
+  }
+  double best[4];
+  visacd_learned_split_info info{};
+  check(visacd_learned_split_search(lp, reinterpret_cast<const double*>(mesh.vertices.data()),
+                                    (int32_t)mesh.vertices.size(), reinterpret_cast<const uint32_t*>(edges.data()),
+                                    (int64_t)edges.size(), center, (float)half, half, config().proposer_refine,
+                                    plan.draws.data(), (int32_t)plan.draws.size(), probe,
+                                    flat.empty() ? nullptr : flat.data(), (int32_t)flat_planes.size(), flat_k,
+                                    config().proposer_tolerance, best, &info),
+        "visacd_learned_split_search");
+  take_draws(plan, info.draws_used);
+  auto& c = counters();
+  c.lp_calls++;
+  c.score_calls++;
+  c.plane_edge_pairs +=
+      (long long)(VISACD_LP_PLANES + info.n_refined + info.n_probe + (int)flat_planes.size()) * (long long)edges.size();
+  c.lp_ms += now_ms() - t0;
+  if (info.fallback) {
+    fallback = true;
+    return false;
+  }
+  if (info.best_index < 0) return false;
+  out = Plane(best[0], best[1], best[2], best[3]);
+  return true;
 }
 
 }  // namespace gpu

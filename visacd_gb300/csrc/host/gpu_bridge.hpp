@@ -38,6 +38,17 @@ class ThreadContext {
 // frame; parameters from config().proposer_weights).
 std::vector<Plane> propose_planes(const Mesh& mesh);
 
+// The learned split search in one GPU call (visacd_learned_split_search): the
+// proposer's planes, their refinement by nearby bisector planes
+// (config().proposer_refine per proposal), a probe of
+// config().proposer_probe_planes candidates drawn from the process engine, and
+// the flat planes (scores times flat_k), scored together. fallback is set when
+// the proposals score more than config().proposer_tolerance below the probe's
+// best: the caller then runs the full search. Returns true with the first
+// maximum otherwise.
+bool learned_split_search(const Mesh& mesh, const std::vector<Plane>& flat_planes, double flat_k, Plane& out,
+                          bool& fallback);
+
 // compute_intersection_matrix(mesh, cage) of lib/src/intersections.cpp:327-385:
 // pairs with a new endpoint when mesh.is_new is non-empty, else all pairs.
 std::vector<Edge> visibility_edges(const Mesh& mesh, const Mesh& cage);

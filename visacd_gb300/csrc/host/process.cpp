@@ -104,7 +104,9 @@ bool exhaustive_plane(const Mesh& mesh, const std::vector<Plane>& flat_planes, P
 // planes (the reference's candidate form, lib/src/process.cpp:45-53) of the
 // `per` visibility edges whose bisectors are nearest to it, under the distance
 // the proposer is trained with: 2 - 2|n_q . n_e| + ((s d_q - d_e) / half)^2,
-// s = sign(n_q . n_e). Returned in edge order, each edge once.
+// s = sign(n_q . n_e). Returned in edge order, each edge once. The host
+// statement of the GPU refinement (refine_partial_kernel, refine_merge_kernel),
+// for tests.
 std::vector<Plane> refine_proposals(const Mesh& mesh, const std::vector<Plane>& prop, int per) {
   const auto& V = mesh.vertices;
   const auto& E = mesh.intersecting_edges;
@@ -161,32 +163,16 @@ namespace {
 
 // Learned search: the proposer's 16 planes refined by nearby bisector planes,
 // a probe of proposer_probe_planes random candidates (the reference's draw,
-// smaller) and the flat planes, scored together by the exact kernel. If the
-// best learned plane scores more than proposer_tolerance below the probe's
-// best, the proposals are not trusted for this split and the exhaustive search
-// runs instead.
+// smaller) and the flat planes, scored together by the exact kernel, all in
+// one GPU call. If the best learned plane scores more than proposer_tolerance
+// below the probe's best, the proposals are not trusted for this split and the
+// exhaustive search runs instead, with the draws after the probe's.
 bool learned_plane(const Mesh& mesh, const std::vector<Plane>& flat_planes, Plane& out) {
-  if (mesh.intersecting_edges.empty()) return false;
-  std::vector<Plane> planes = gpu::propose_planes(mesh);
-  std::vector<Plane> refined = refine_proposals(mesh, planes, config().proposer_refine);
-  planes.insert(planes.end(), refined.begin(), refined.end());
-  const size_t n_prop = planes.size();
-  std::vector<Plane> probe =
-      gpu::candidate_planes(mesh.vertices, mesh.intersecting_edges, config().proposer_probe_planes);
-  planes.insert(planes.end(), probe.begin(), probe.end());
-  const size_t flat_offset = planes.size();
-  planes.insert(planes.end(), flat_planes.begin(), flat_planes.end());
-  std::vector<double> scores = gpu::score_planes(planes, mesh.vertices, mesh.intersecting_edges);
-  for (size_t i = flat_offset; i < planes.size(); ++i) scores[i] *= config().flat_surface_k;
-  const double best_prop = *std::max_element(scores.begin(), scores.begin() + n_prop);
-  double best_probe = 0;
-  for (size_t i = n_prop; i < flat_offset; ++i) best_probe = std::max(best_probe, scores[i]);
-  if (best_prop < (1.0 - config().proposer_tolerance) * best_probe) {
-    gpu::counters().lp_fallbacks++;
-    return exhaustive_plane(mesh, flat_planes, out);
-  }
-  out = planes[std::max_element(scores.begin(), scores.end()) - scores.begin()];
-  return true;
+  bool fallback = false;
+  if (gpu::learned_split_search(mesh, flat_planes, config().flat_surface_k, out, fallback)) return true;
+  if (!fallback) return false;
+  gpu::counters().lp_fallbacks++;
+  return exhaustive_plane(mesh, flat_planes, out);
 }
 
 }  // namespace
@@ -349,6 +335,8 @@ double compute_final_concavity(const MeshList& parts, const MeshList& hulls) {
 ProcessResult process(Mesh mesh, double concavity, int num_parts) {
   if (config().plane_proposer != "exhaustive" && config().plane_proposer != "learned")
     throw std::runtime_error("config.plane_proposer must be 'exhaustive' or 'learned'");
+  if (config().proposer_refine < 0 || config().proposer_refine > 32)
+    throw std::runtime_error("config.proposer_refine must be in [0, 32]");
   g_times = StageTimes();
   const double t_start = now_ms();
   gpu::context();

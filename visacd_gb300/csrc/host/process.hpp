@@ -23,9 +23,11 @@ std::vector<Plane> get_candidate_planes(const std::vector<Vec3>& vertices,
 bool decompose_iteration(Mesh& mesh, MeshList& parts, Mesh& cage,
                          const std::vector<Plane>& flat_planes);
 
-// The learned search's refinement: for each proposal, the perpendicular-
-// bisector planes of the `per` visibility edges nearest to it under the
-// proposer's training distance, in edge order, each edge once.
+// The learned search's refinement on the host: for each proposal, the
+// perpendicular-bisector planes of the `per` visibility edges nearest to it
+// under the proposer's training distance, in edge order, each edge once. The
+// split search runs it on the GPU (visacd_learned_split_search); this
+// statement is what tests check that against.
 std::vector<Plane> refine_proposals(const Mesh& mesh, const std::vector<Plane>& prop, int per);
 
 double compute_part_score(const Mesh& part);
