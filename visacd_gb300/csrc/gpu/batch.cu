@@ -60,9 +60,7 @@ __global__ void __launch_bounds__(kVisThreads, 6)
                             unsigned long long total_tiles, uint32_t* __restrict__ bitset,
                             BatchCounters* __restrict__ cnt, unsigned* __restrict__ status) {
   constexpr int TC = 32 / TR;
-  __shared__ int stk_all[kStack * (kVisThreads / 32)];
   const int lane = threadIdx.x & 31;
-  int* wstk = stk_all + (threadIdx.x >> 5) * kStack;
   unsigned rechecks = 0, status_bits = 0, visits = 0, tri_tests = 0;
   for (int guard = 0; guard < (1 << 30); ++guard) {
     unsigned long long w = 0;
@@ -100,11 +98,11 @@ __global__ void __launch_bounds__(kVisThreads, 6)
     if (!__ballot_sync(0xffffffffu, active)) continue;
     // The cage first; the self test only for segments that leave it.
     s.exclude = false;
-    const bool cage_hit = packet_any_hit(P.cage_nodes, P.cage_tris, P.cage_nt, s, P.pts, active, wstk,
+    const bool cage_hit = packet_any_hit(P.cage_nodes, P.cage_tris, P.cage_nt, s, P.pts, active,
                                          rechecks, status_bits, visits, tri_tests);
     active = active && cage_hit;
     s.exclude = true;
-    const bool self_hit = packet_any_hit(P.self_nodes, P.self_tris, P.self_nt, s, P.pts, active, wstk,
+    const bool self_hit = packet_any_hit(P.self_nodes, P.self_tris, P.self_nt, s, P.pts, active,
                                          rechecks, status_bits, visits, tri_tests);
     if (active && !self_hit) {
       const int64_t k = row_start(i, P.n) + (int64_t)(j - i - 1);

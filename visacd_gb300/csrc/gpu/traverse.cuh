@@ -209,35 +209,41 @@ __device__ __forceinline__ bool leaf_hit(const float4* __restrict__ tris, int le
 // walks one path through the BVH: a child is visited when any still-active
 // lane's segment overlaps its box (ballot), node records are fetched at a
 // warp-uniform address (one broadcast transaction), and a lane retires at its
-// first hit. The stack is per warp (shared memory, kStack entries).
-// Returns this lane's hit flag. `status_bits` collects stack-overflow /
-// iteration-overrun conditions (the lane is then reported as hit and the call
-// fails on the host).
+// first hit. The stack is per warp and lives in registers: entry k is held by
+// lane k mod 32, in the first register for k < 32 and the second above, so a
+// push is a select and a pop one shuffle (no shared memory, no warp barrier).
+// Lanes retire only at leaf tests, so the warp checks for an early exit only
+// after those. Returns this lane's hit flag; `visits` grows by the node
+// records fetched. `status_bits` collects stack-overflow / iteration-overrun
+// conditions (the lane is then reported as hit and the call fails on the
+// host).
 static __device__ bool packet_any_hit(const float4* __restrict__ nodes, const float4* __restrict__ tris,
-                               int nt, const Seg& s, const float* __restrict__ pts, bool active,
-                               int* __restrict__ wstk,
-                               unsigned& rechecks, unsigned& status_bits, unsigned& visits,
-                               unsigned& tri_tests) {
+                                      int nt, const Seg& s, const float* __restrict__ pts, bool active,
+                                      unsigned& rechecks, unsigned& status_bits, unsigned& visits,
+                                      unsigned& tri_tests) {
+  static_assert(kStack == 64, "two stack registers per lane");
+  const unsigned full = 0xffffffffu;
   bool hit = false;
   if (nt <= 0) return false;
-  unsigned live = __ballot_sync(0xffffffffu, active);
-  if (!live) return false;
+  if (!__ballot_sync(full, active)) return false;
   const int lane = threadIdx.x & 31;
+  int stk0 = 0, stk1 = 0;
   int node = 0, sp = 0;
   const int max_iter = 4 * nt + 64;
   for (int it = 0; it < max_iter; ++it) {
-    ++visits;
     const ulonglong2* nd = reinterpret_cast<const ulonglong2*>(nodes) + 4 * node;
     const ulonglong2 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2);
     const int2 lr = __ldg(reinterpret_cast<const int2*>(nd + 3));
     const int l = lr.x, r = lr.y;
     const bool hl = active && box_hit(s, n0.x, n0.y, n1.x);
     const bool hr = active && box_hit(s, n1.y, n2.x, n2.y);
-    const unsigned bl = __ballot_sync(0xffffffffu, hl);
-    const unsigned br = __ballot_sync(0xffffffffu, hr);
+    const unsigned bl = __ballot_sync(full, hl);
+    const unsigned br = __ballot_sync(full, hr);
     int next = -1;
+    bool leaf = false;
     if (bl) {
       if (l < 0) {
+        leaf = true;
         if (hl) {
           ++tri_tests;
           if (leaf_hit(tris, ~l, s, pts, rechecks)) {
@@ -251,6 +257,7 @@ static __device__ bool packet_any_hit(const float4* __restrict__ nodes, const fl
     }
     if (br) {
       if (r < 0) {
+        leaf = true;
         if (hr && active) {
           ++tri_tests;
           if (leaf_hit(tris, ~r, s, pts, rechecks)) {
@@ -262,24 +269,33 @@ static __device__ bool packet_any_hit(const float4* __restrict__ nodes, const fl
         next = r;
       } else {
         if (sp >= kStack) {
+          visits += it + 1;
           status_bits |= kStatusStackOverflow;
           return true;
         }
-        if (lane == 0) wstk[sp] = r;
+        if (sp < 32) {
+          stk0 = lane == sp ? r : stk0;
+        } else {
+          stk1 = lane == sp - 32 ? r : stk1;
+        }
         ++sp;
       }
     }
-    live = __ballot_sync(0xffffffffu, active);
-    if (!live) return hit;
-    if (next < 0) {
-      if (sp == 0) return hit;
-      --sp;
-      __syncwarp();
-      next = wstk[sp];
+    if (leaf && !__ballot_sync(full, active)) {
+      visits += it + 1;
+      return hit;
     }
-    __syncwarp();
+    if (next < 0) {
+      if (sp == 0) {
+        visits += it + 1;
+        return hit;
+      }
+      --sp;
+      next = __shfl_sync(full, sp < 32 ? stk0 : stk1, sp & 31);
+    }
     node = next;
   }
+  visits += max_iter;
   status_bits |= kStatusTraversalOverrun;
   return true;
 }

@@ -93,7 +93,7 @@ struct VisLaneCounters {
 // edge bits.
 template <int TR>
 __device__ __forceinline__ void vis_tile(const VisParams& P, unsigned long long w, int lane,
-                                         int* __restrict__ wstk, VisLaneCounters& c) {
+                                         VisLaneCounters& c) {
   constexpr int TC = 32 / TR;
   const int64_t n = P.n;
   int64_t tr, tc;
@@ -133,12 +133,12 @@ __device__ __forceinline__ void vis_tile(const VisParams& P, unsigned long long 
   if (!__ballot_sync(0xffffffffu, active)) return;
   // The cage first: few segments leave it, so the self test runs for few.
   s.exclude = false;
-  const bool cage_hit = packet_any_hit(P.cage_nodes, P.cage_tris, P.cage_nt, s, P.pts, active, wstk,
+  const bool cage_hit = packet_any_hit(P.cage_nodes, P.cage_tris, P.cage_nt, s, P.pts, active,
                                        c.rechecks, c.status_bits, c.visits, c.tri_tests);
   if (active && cage_hit) ++c.cage;
   active = active && cage_hit;
   s.exclude = true;
-  const bool self_hit = packet_any_hit(P.self_nodes, P.self_tris, P.self_nt, s, P.pts, active, wstk,
+  const bool self_hit = packet_any_hit(P.self_nodes, P.self_tris, P.self_nt, s, P.pts, active,
                                        c.rechecks, c.status_bits, c.visits, c.tri_tests);
   if (active && self_hit) ++c.self;
   if (active && !self_hit) {
@@ -176,16 +176,14 @@ __device__ __forceinline__ void vis_flush_counters(VisCounters* cnt, unsigned* s
 
 template <int TR, int MINB>
 __global__ void __launch_bounds__(kVisThreads, MINB) visibility_kernel(VisParams P) {
-  __shared__ int stk_all[kStack * (kVisThreads / 32)];
   const int lane = threadIdx.x & 31;
-  int* wstk = stk_all + (threadIdx.x >> 5) * kStack;
   VisLaneCounters c;
   for (int guard = 0; guard < (1 << 30); ++guard) {
     unsigned long long w = 0;
     if (lane == 0) w = atomicAdd(&P.cnt->work, 1ull);
     w = __shfl_sync(0xffffffffu, w, 0);
     if (w >= P.total_tiles) break;
-    vis_tile<TR>(P, w, lane, wstk, c);
+    vis_tile<TR>(P, w, lane, c);
   }
   vis_flush_counters(P.cnt, P.status, lane, c);
 }
@@ -200,9 +198,7 @@ __global__ void __launch_bounds__(kVisThreads, MINB)
                             const unsigned long long* __restrict__ tile_start,
                             unsigned long long total_tiles, VisCounters* __restrict__ cnt,
                             unsigned* __restrict__ status) {
-  __shared__ int stk_all[kStack * (kVisThreads / 32)];
   const int lane = threadIdx.x & 31;
-  int* wstk = stk_all + (threadIdx.x >> 5) * kStack;
   VisLaneCounters c;
   for (int guard = 0; guard < (1 << 30); ++guard) {
     unsigned long long w = 0;
@@ -214,7 +210,7 @@ __global__ void __launch_bounds__(kVisThreads, MINB)
       const int mid = (lo + hi + 1) >> 1;
       if (tile_start[mid] <= w) lo = mid; else hi = mid - 1;
     }
-    vis_tile<TR>(parts[lo], w - tile_start[lo], lane, wstk, c);
+    vis_tile<TR>(parts[lo], w - tile_start[lo], lane, c);
   }
   vis_flush_counters(cnt, status, lane, c);
 }
