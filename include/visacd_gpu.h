@@ -182,6 +182,17 @@ int visacd_autotune_visibility(visacd_ctx* ctx, const float* pts, int32_t n, con
                                const visacd_bvh* cage_bvh, int* best_variant,
                                double* ms_per_variant);
 
+/* Free-space walks (on by default). A visibility call with at least 2^20
+   pairs first walks each segment through a grid over its cage that bounds,
+   per cell, the distance to the cage's triangles (built once per cage BVH,
+   kept with it): a segment whose whole length the walk covers cannot hit the
+   cage and skips the cage BVH; every other segment is traced as before. The
+   edges are the same either way. visacd_ctx_vis_trace_counts reports, for the
+   context's last visacd_visibility call, the segments cleared this way and
+   the grid cells read. */
+int visacd_ctx_set_vis_trace(visacd_ctx* ctx, int enable);
+int visacd_ctx_vis_trace_counts(const visacd_ctx* ctx, int64_t* cleared, int64_t* grid_reads);
+
 /* One call that builds both BVHs, runs visacd_visibility and copies the edges
    out: the C form of compute_intersection_matrix(mesh, cage). If the edge
    count exceeds capacity_edges, *n_edges holds the count and the call returns

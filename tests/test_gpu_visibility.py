@@ -154,7 +154,10 @@ def test_torus_64x32_all_pairs(ctx, orc):
     e, st, ost, nd = _compare(ctx, orc, v, t, cv, ct)
     assert ost["pairs"] == 2096128
     assert nd <= ost["n_grazing"]
-    print(f"torus 64x32: {len(e)} edges, {ost['n_grazing']} grazing pairs, {nd} differ (all grazing)")
+    cleared, reads = ctx.vis_trace_counts()
+    assert cleared > 0  # the free-space walk took part
+    print(f"torus 64x32: {len(e)} edges, {ost['n_grazing']} grazing pairs, {nd} differ (all grazing); "
+          f"{cleared} segments cleared by the free-space walk ({reads} grid reads)")
 
 
 def test_blob_s5_all_pairs(ctx, orc):
@@ -167,7 +170,57 @@ def test_blob_s5_all_pairs(ctx, orc):
     e, st, ost, nd = _compare(ctx, orc, v, t, cv, ct)
     assert ost["pairs"] == 52444161
     assert nd <= ost["n_grazing"]
-    print(f"blob s5: {len(e)} edges, {ost['n_grazing']} grazing pairs, {nd} differ (all grazing)")
+    cleared, reads = ctx.vis_trace_counts()
+    assert cleared > 0
+    print(f"blob s5: {len(e)} edges, {ost['n_grazing']} grazing pairs, {nd} differ (all grazing); "
+          f"{cleared} segments cleared by the free-space walk ({reads} grid reads)")
+
+
+@pytest.mark.parametrize("case", ["blob_s5", "torus_64x32", "blob_s4_masked", "tiny_cage_gap"])
+def test_free_space_walk_changes_nothing(ctx, case):
+    """The cage's free-space walk only skips segments that cannot hit the cage:
+    the edges and the pair, hit and degenerate counts are the same with and
+    without it; only the BVH work (node visits, triangle tests, FP64
+    re-decisions) shrinks."""
+    is_new = None
+    if case == "blob_s5":
+        v, t = mg.displaced_blob(5, seed=2026)
+        cv, ct = mg.offset_cage(v, t, 0.03)
+    elif case == "torus_64x32":
+        v, t = mg.torus(nu=64, nv=32, seed=42)
+        cv, ct = mg.offset_cage(v, t, 0.03)
+    elif case == "blob_s4_masked":  # 1/3 of the vertices new: about 2.4M pairs
+        v, t = mg.displaced_blob(4, seed=7)
+        v = np.concatenate([v, v * 0.999])  # two shells: many pairs graze or cross
+        t = np.concatenate([t, t[:, ::-1] + len(v) // 2])
+        cv, ct = mg.offset_cage(v[: len(v) // 2], t[: len(t) // 2], 0.03)
+        is_new = (np.arange(len(v)) % 3 == 0).astype(np.uint8)
+    else:  # a cage 1e-4 off the part: few segments are cleared
+        v, t = mg.displaced_blob(4, seed=3)
+        cv, ct = mg.offset_cage(v, t, 1e-4)
+    sb, cb = ctx.bvh(v, t), ctx.bvh(cv, ct)
+    try:
+        ctx.set_vis_trace(False)
+        e0, s0 = ctx.visibility(v, sb, cb, is_new=is_new)
+        ctx.set_vis_trace(True)
+        e1, s1 = ctx.visibility(v, sb, cb, is_new=is_new)
+    finally:
+        ctx.set_vis_trace(True)
+    cleared, reads = ctx.vis_trace_counts()
+    np.testing.assert_array_equal(e0, e1)
+    for k in ("pairs_tested", "n_edges", "self_hits", "cage_hits", "degenerate"):
+        assert s0[k] == s1[k], k
+    # Cleared segments skip their cage triangle tests (and those tests' FP64
+    # re-decisions).
+    assert s1["fp64_rechecks"] <= s0["fp64_rechecks"] and s1["tri_tests"] <= s0["tri_tests"]
+    # The share cleared depends on the shape: most chords of the blob stay far
+    # from its cage; the torus's run close to its tube.
+    least = {"blob_s5": 0.9, "torus_64x32": 0.3, "blob_s4_masked": 0.3, "tiny_cage_gap": 0.0}[case]
+    if s1["pairs_tested"] >= 1 << 20 and least > 0:
+        assert cleared > least * s1["pairs_tested"]
+        assert s1["node_visits"] < s0["node_visits"]
+    print(f"{case}: {s1['pairs_tested']} pairs, {cleared} cleared, {reads} grid reads, "
+          f"node visits {s0['node_visits']} -> {s1['node_visits']}")
 
 
 def test_bvh_depth_on_clustered_and_degenerate_meshes(ctx, orc):

@@ -33,7 +33,7 @@ EXPORTED = [
     "visacd_sdf_remesh", "visacd_sdf_fetch", "visacd_hull_distances", "visacd_segment_triangle_tests",
     "visacd_set_blocking_sync", "visacd_lp_set_tcgen05", "visacd_ctx_set_blocking_wait",
     "visacd_candidate_planes", "visacd_split_search", "visacd_visibility_batch",
-    "visacd_learned_split_search",
+    "visacd_learned_split_search", "visacd_ctx_set_vis_trace", "visacd_ctx_vis_trace_counts",
 ]
 
 LP_POINTS = 2048
@@ -122,6 +122,8 @@ def load() -> C.CDLL:
                                             C.POINTER(i32)]
     lib.visacd_split_search.argtypes = [P, P, i32, P, i64, P, i32, i32, P, i32, C.c_double, P,
                                         C.POINTER(SplitInfo)]
+    lib.visacd_ctx_set_vis_trace.argtypes = [P, C.c_int]
+    lib.visacd_ctx_vis_trace_counts.argtypes = [P, C.POINTER(i64), C.POINTER(i64)]
     lib.visacd_learned_split_search.argtypes = [P, P, i32, P, i64, P, C.c_float, C.c_double, i32, P, i32,
                                                 i32, P, i32, C.c_double, C.c_double, P,
                                                 C.POINTER(LearnedSplitInfo)]
@@ -280,6 +282,16 @@ class Context:
             out.append(flat[at:at + ne[k]])
             at += int(ne[k])
         return out, st.as_dict()
+
+    def set_vis_trace(self, on: bool) -> None:
+        """Free-space walks before the cage BVH in large visibility calls."""
+        _check(lib().visacd_ctx_set_vis_trace(self._h, int(bool(on))), "visacd_ctx_set_vis_trace")
+
+    def vis_trace_counts(self) -> tuple[int, int]:
+        """(segments cleared by the walk, grid cells read) of the last visibility call."""
+        a, b = C.c_int64(), C.c_int64()
+        _check(lib().visacd_ctx_vis_trace_counts(self._h, C.byref(a), C.byref(b)), "vis_trace_counts")
+        return a.value, b.value
 
     def set_vis_variant(self, v: int) -> None:
         _check(lib().visacd_ctx_set_vis_variant(self._h, v), "set_vis_variant")

@@ -380,7 +380,9 @@ int bvh_build(visacd_ctx* ctx, const float* verts, int32_t nv, const uint32_t* t
 void bvh_detach(visacd_bvh* b) {
   if (b->nodes) cudaFreeAsync(b->nodes, b->stream);
   if (b->tris) cudaFreeAsync(b->tris, b->stream);
+  if (b->free_lb) cudaFreeAsync(b->free_lb, b->stream);
   b->nodes = b->tris = nullptr;
+  b->free_lb = nullptr;
   b->ctx = nullptr;
   b->stream = nullptr;
 }

@@ -21,6 +21,12 @@ struct visacd_bvh {
   float4* tris = nullptr;
   visacd_ctx* ctx = nullptr;       // owning context (null once it is destroyed)
   cudaStream_t stream = nullptr;   // the owner's stream (stream-ordered allocations)
+  // Free-space grid (freegrid.cu), built on first use for a large visibility
+  // call when this BVH is the cage: lb per cell, x fastest.
+  bool free_built = false;
+  float* free_lb = nullptr;
+  float fg_ox = 0.f, fg_oy = 0.f, fg_oz = 0.f, fg_inv_h = 0.f, fg_margin = 0.f;
+  int32_t fg_nx = 0, fg_ny = 0, fg_nz = 0;
 };
 
 namespace vgpu {
@@ -36,5 +42,10 @@ int bvh_build(visacd_ctx* ctx, const float* verts, int32_t nv, const uint32_t* t
 // Frees a BVH's device memory when its context goes away (the handle itself
 // stays valid until visacd_bvh_destroy, and is rejected by queries).
 void bvh_detach(visacd_bvh* b);
+// Builds the BVH's free-space grid (once; a BVH whose grid would not be
+// usable keeps none). Uses the context's counter slot and pinned staging
+// buffer (waits for the stream first), so it runs before a call takes them.
+// Asynchronous after one small read-back.
+int free_grid_build(visacd_ctx* ctx, visacd_bvh* b);
 
 }  // namespace vgpu

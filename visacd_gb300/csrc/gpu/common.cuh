@@ -118,6 +118,7 @@ enum CtxSlot {
   kSlotCandLinks,
   kSlotVisMulti,
   kSlotLearned,
+  kSlotFreeGrid,
   kSlotCount
 };
 
@@ -142,6 +143,8 @@ struct visacd_ctx {
   visacd_clip_result clip_out{};                  // last clip result (device-resident)
   std::vector<visacd_bvh*> bvhs;                  // live BVHs built on this context
   std::vector<visacd_lp*> lps;                    // live proposers made on this context
+  bool vis_trace = true;                          // free-space walks before the cage BVH
+  int64_t last_vis_certified = 0, last_vis_trace_steps = 0;  // of the last visibility call
   int clip_nv = 0;
   int32_t sdf_nv = 0, sdf_nt = 0;                 // last SDF remesh result (device-resident)
   void* clip_ptrs[7] = {nullptr};
@@ -199,6 +202,9 @@ enum KernelId {
   kKCandidates,
   kKLpRefine,
   kKLpSplit,
+  kKGridNear,
+  kKGridEdt,
+  kKGridFinal,
   kKMisc,
   kKCount
 };

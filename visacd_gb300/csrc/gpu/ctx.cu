@@ -87,7 +87,8 @@ static const char* kNames[kKCount] = {
     "lp_gemm",       "lp_pool",        "lp_loss",      "lp_adam",
     "lp_misc",       "sdf_remesh",     "sdf_dist",     "sdf_cross",
     "hull_dist",     "seg_tri",        "candidates",
-    "lp_refine",     "lp_split",       "misc"};
+    "lp_refine",     "lp_split",       "grid_near",    "grid_edt",
+    "grid_final",    "misc"};
 
 const char* kernel_name(int id) { return (id >= 0 && id < kKCount) ? kNames[id] : "?"; }
 

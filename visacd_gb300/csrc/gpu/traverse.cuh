@@ -21,7 +21,45 @@ struct VisCounters {
   unsigned long long node_visits, tri_tests;  // per-warp node fetches, per-lane triangle tests
   unsigned pmin[3], pmax[3];  // orderable point bounds
   unsigned long long n_rows;  // rows of the tile space (masked mode)
+  unsigned long long certified, trace_steps;  // free-space walks: segments cleared, grid reads
 };
+
+// A cage's free-space grid as the visibility kernel reads it (freegrid.cu).
+struct FreeGridView {
+  const float* lb;  // null: no grid
+  float ox, oy, oz, inv_h, margin;
+  int32_t nx, ny, nz;
+};
+constexpr int kTraceSteps = 48;  // grid reads per segment before it goes to the BVH
+
+// Free-space walk of the segment p -> q (d = q - p rounded, len its FP32
+// length) through a cage's grid. From the point at t the walk may advance by
+// (lb - margin) / |q - p|: lb bounds the distance from every point of the
+// point's cell, grown by the margin, to the cage (the margin covers the FP32
+// rounding of the point and of its cell index), so no cage triangle lies
+// within the margin of the part covered. True when the walk covers [0, 1]:
+// the segment cannot hit the cage. Roundings are directed so that the part
+// covered is never overstated. `steps` counts the grid reads.
+__device__ __forceinline__ bool trace_free(const FreeGridView& g, float px, float py, float pz, float dx,
+                                           float dy, float dz, float len, unsigned long long& steps) {
+  // 1 / |q - p| rounded down; |q - p| <= len (1 + 17u).
+  const float inv_len = __frcp_rd(__fmul_ru(len, 1.000001f));
+  float t = 0.f;
+  for (int k = 0; k < kTraceSteps; ++k) {
+    const float x = fmaf(t, dx, px), y = fmaf(t, dy, py), z = fmaf(t, dz, pz);
+    const int ix = __float2int_rd((x - g.ox) * g.inv_h);
+    const int iy = __float2int_rd((y - g.oy) * g.inv_h);
+    const int iz = __float2int_rd((z - g.oz) * g.inv_h);
+    if ((unsigned)ix >= (unsigned)g.nx || (unsigned)iy >= (unsigned)g.ny || (unsigned)iz >= (unsigned)g.nz)
+      return false;
+    const float lb = __ldg(&g.lb[((int64_t)iz * g.ny + iy) * g.nx + ix]);
+    ++steps;
+    if (!(lb > g.margin)) return false;
+    t = __fadd_rd(t, __fmul_rd(__fsub_rd(lb, g.margin), inv_len));
+    if (t >= 1.f) return true;
+  }
+  return false;
+}
 
 struct Seg {
   unsigned long long ox2, oy2, oz2;  // (o, o) pairs for packed slab tests

@@ -30,6 +30,9 @@
 
 namespace vgpu {
 
+// Pairs from which a call builds and uses the cage's free-space grid.
+constexpr int64_t kFreeGridMinPairs = 1 << 20;
+
 struct VisParams {
   const float* pts;
   int32_t n;
@@ -52,6 +55,7 @@ struct VisParams {
   int64_t ntc;                          // tile columns
   int64_t ntr;                          // tile rows
   const unsigned long long* row_start;  // triangular mode: first tile of each tile row
+  FreeGridView cage_free;               // the cage's free-space grid (lb null: none)
 };
 
 // Work item w -> tile (tr, tc). Rectangle mode: row-major. Triangular mode:
@@ -84,7 +88,7 @@ __global__ void tile_row_counts_kernel(int64_t ntr, int64_t ntc, int TR, int TC,
 
 // Per-lane counters of a visibility launch, reduced over the warp at the end.
 struct VisLaneCounters {
-  unsigned long long pairs = 0, edges = 0, self = 0, cage = 0, deg = 0;
+  unsigned long long pairs = 0, edges = 0, self = 0, cage = 0, deg = 0, certified = 0, trace_steps = 0;
   unsigned rechecks = 0, status_bits = 0, visits = 0, tri_tests = 0;
 };
 
@@ -132,8 +136,16 @@ __device__ __forceinline__ void vis_tile(const VisParams& P, unsigned long long 
   }
   if (!__ballot_sync(0xffffffffu, active)) return;
   // The cage first: few segments leave it, so the self test runs for few.
+  // Segments the free-space walk clears cannot hit the cage; the others go
+  // through the BVH.
   s.exclude = false;
-  const bool cage_hit = packet_any_hit(P.cage_nodes, P.cage_tris, P.cage_nt, s, P.pts, active,
+  bool cage_test = active;
+  if (P.cage_free.lb != nullptr && active &&
+      trace_free(P.cage_free, p.x, p.y, p.z, s.dx, s.dy, s.dz, seg_len(s), c.trace_steps)) {
+    cage_test = false;
+    ++c.certified;
+  }
+  const bool cage_hit = packet_any_hit(P.cage_nodes, P.cage_tris, P.cage_nt, s, P.pts, cage_test,
                                        c.rechecks, c.status_bits, c.visits, c.tri_tests);
   if (active && cage_hit) ++c.cage;
   active = active && cage_hit;
@@ -159,6 +171,8 @@ __device__ __forceinline__ void vis_flush_counters(VisCounters* cnt, unsigned* s
     c.deg += __shfl_xor_sync(0xffffffffu, c.deg, o);
     c.rechecks += __shfl_xor_sync(0xffffffffu, c.rechecks, o);
     c.tri_tests += __shfl_xor_sync(0xffffffffu, c.tri_tests, o);
+    c.certified += __shfl_xor_sync(0xffffffffu, c.certified, o);
+    c.trace_steps += __shfl_xor_sync(0xffffffffu, c.trace_steps, o);
     c.status_bits |= __shfl_xor_sync(0xffffffffu, c.status_bits, o);
   }
   if (lane == 0) {
@@ -170,6 +184,8 @@ __device__ __forceinline__ void vis_flush_counters(VisCounters* cnt, unsigned* s
     atomicAdd(&cnt->rechecks, (unsigned long long)c.rechecks);
     atomicAdd(&cnt->node_visits, (unsigned long long)c.visits);
     atomicAdd(&cnt->tri_tests, (unsigned long long)c.tri_tests);
+    if (c.certified) atomicAdd(&cnt->certified, c.certified);
+    if (c.trace_steps) atomicAdd(&cnt->trace_steps, c.trace_steps);
     if (c.status_bits) atomicOr(status, c.status_bits);
   }
 }
@@ -416,6 +432,11 @@ int vis_morton_order(visacd_ctx* ctx, const float* d_pts, int32_t n, uint32_t* p
 static int vis_device(visacd_ctx* ctx, const float* d_pts, int32_t n, const uint8_t* d_new,
                       const visacd_bvh* self_bvh, const visacd_bvh* cage_bvh, int64_t* n_edges,
                       visacd_vis_stats* stats) {
+  // The cage's free-space grid, for large calls: built once per cage BVH,
+  // before this call's counters take the shared scratch and staging buffers.
+  const bool use_grid = ctx->vis_trace && n >= 2 &&
+                        (int64_t)n * (n - 1) / 2 >= kFreeGridMinPairs && cage_bvh->nt > 0;
+  if (use_grid) VTRY(free_grid_build(ctx, const_cast<visacd_bvh*>(cage_bvh)));
   VTRY(ensure_slot(ctx, kSlotCounters, sizeof(VisCounters)));
   VisCounters* cnt = slot<VisCounters>(ctx, kSlotCounters);
   VisCounters init;
@@ -506,6 +527,22 @@ static int vis_device(visacd_ctx* ctx, const float* d_pts, int32_t n, const uint
   P.cage_nodes = cage_bvh->nodes;
   P.cage_tris = cage_bvh->tris;
   P.cage_nt = cage_bvh->nt;
+  // Large calls first clear what they can with the cage's free-space grid
+  // (built at the top of this call).
+  if (use_grid) {
+    const visacd_bvh* cb = cage_bvh;
+    if (cb->free_lb) {
+      P.cage_free.lb = cb->free_lb;
+      P.cage_free.ox = cb->fg_ox;
+      P.cage_free.oy = cb->fg_oy;
+      P.cage_free.oz = cb->fg_oz;
+      P.cage_free.inv_h = cb->fg_inv_h;
+      P.cage_free.margin = cb->fg_margin;
+      P.cage_free.nx = cb->fg_nx;
+      P.cage_free.ny = cb->fg_ny;
+      P.cage_free.nz = cb->fg_nz;
+    }
+  }
   VTRY(ensure_slot(ctx, kSlotBitset, (size_t)nw * 4));
   P.bitset = slot<uint32_t>(ctx, kSlotBitset);
   VCUDA(cudaMemsetAsync(P.bitset, 0, (size_t)nw * 4, ctx->stream));
@@ -522,8 +559,11 @@ static int vis_device(visacd_ctx* ctx, const float* d_pts, int32_t n, const uint
   VTRY(exclusive_scan_u32_to_u64(ctx, wc, wo, nw));
   VCUDA(cudaMemcpyAsync(h, cnt, sizeof(VisCounters), cudaMemcpyDeviceToHost, ctx->stream));
   VCUDA(stream_wait(ctx));
+  // The read-back shares the pinned staging area with the status check: copy
+  // it out first.
+  const VisCounters hc = *h;
   VTRY(check_status(ctx, "visibility"));
-  const int64_t ne = (int64_t)h->edges;
+  const int64_t ne = (int64_t)hc.edges;
   VTRY(ensure_slot(ctx, kSlotEdgesOut, (size_t)(ne > 0 ? ne : 1) * 8));
   if (ne > 0) {
     VLAUNCH(ctx, kKBitEmit, gw, 256, 0, bit_emit_kernel, P.bitset, nw, wo, (int64_t)n,
@@ -532,15 +572,17 @@ static int vis_device(visacd_ctx* ctx, const float* d_pts, int32_t n, const uint
   ctx->last_n_edges = ne;
   if (n_edges) *n_edges = ne;
   if (stats) {
-    stats->pairs_tested = (int64_t)h->pairs;
+    stats->pairs_tested = (int64_t)hc.pairs;
     stats->n_edges = ne;
-    stats->self_hits = (int64_t)h->self_hits;
-    stats->cage_hits = (int64_t)h->cage_hits;
-    stats->fp64_rechecks = (int64_t)h->rechecks;
-    stats->degenerate = (int64_t)h->degenerate;
-    stats->node_visits = (int64_t)h->node_visits;
-    stats->tri_tests = (int64_t)h->tri_tests;
+    stats->self_hits = (int64_t)hc.self_hits;
+    stats->cage_hits = (int64_t)hc.cage_hits;
+    stats->fp64_rechecks = (int64_t)hc.rechecks;
+    stats->degenerate = (int64_t)hc.degenerate;
+    stats->node_visits = (int64_t)hc.node_visits;
+    stats->tri_tests = (int64_t)hc.tri_tests;
   }
+  ctx->last_vis_certified = (int64_t)hc.certified;
+  ctx->last_vis_trace_steps = (int64_t)hc.trace_steps;
   return VISACD_OK;
 }
 
@@ -944,6 +986,19 @@ extern "C" int visacd_ctx_set_vis_variant(visacd_ctx* ctx, int variant) {
   VCHECK(variant >= -1 && variant < kNumVisVariants, VISACD_ERR_INVALID_ARG,
          "set_vis_variant: variant %d out of range", variant);
   ctx->vis_variant_override = variant;
+  return VISACD_OK;
+}
+
+extern "C" int visacd_ctx_set_vis_trace(visacd_ctx* ctx, int enable) {
+  VCHECK(ctx, VISACD_ERR_INVALID_ARG, "set_vis_trace: null context");
+  ctx->vis_trace = enable != 0;
+  return VISACD_OK;
+}
+
+extern "C" int visacd_ctx_vis_trace_counts(const visacd_ctx* ctx, int64_t* cleared, int64_t* grid_reads) {
+  VCHECK(ctx, VISACD_ERR_INVALID_ARG, "vis_trace_counts: null context");
+  if (cleared) *cleared = ctx->last_vis_certified;
+  if (grid_reads) *grid_reads = ctx->last_vis_trace_steps;
   return VISACD_OK;
 }
 
