@@ -119,6 +119,7 @@ enum CtxSlot {
   kSlotVisMulti,
   kSlotLearned,
   kSlotFreeGrid,
+  kSlotVisCleared,
   kSlotCount
 };
 
@@ -205,6 +206,7 @@ enum KernelId {
   kKGridNear,
   kKGridEdt,
   kKGridFinal,
+  kKVisWalk,
   kKMisc,
   kKCount
 };

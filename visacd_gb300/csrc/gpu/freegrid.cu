@@ -157,71 +157,118 @@ __global__ void fg_near_kernel(const float4* __restrict__ tris, int32_t nt, FgPa
   }
 }
 
-// EDT pass along x: squared distance (cells) to the nearest surface cell of
-// the row (a surface cell: near value <= hd).
+// EDT pass along x, one warp per row: squared distance (cells) to the nearest
+// surface cell of the row (a surface cell: near value <= hd), kFgInf when
+// the row has none. The nearest surface index at or before / at or after
+// each cell comes from warp max / min scans, 32 cells at a time.
 __global__ void fg_edt_x_kernel(const unsigned* __restrict__ near, FgParams g, float hd, int* __restrict__ d2) {
+  constexpr unsigned full = 0xffffffffu;
+  constexpr int kNone = 1 << 20;
+  const int lane = threadIdx.x & 31;
   const int64_t rows = (int64_t)g.ny * g.nz;
-  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows;
-       r += (int64_t)gridDim.x * blockDim.x) {
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int chunks = (g.nx + 31) >> 5;  // <= 8
+  for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < rows; r += nwarps) {
     const int64_t base = r * g.nx;
-    int dist = kFgInf;
-    for (int i = 0; i < g.nx; ++i) {
-      if (__uint_as_float(near[base + i]) <= hd) dist = 0;
-      else if (dist < kFgInf) ++dist;
-      d2[base + i] = dist;
+    unsigned seeds[kFgMaxDim / 32];
+    int last[kFgMaxDim / 32];
+    int carry = -kNone;
+#pragma unroll
+    for (int m = 0; m < kFgMaxDim / 32; ++m) {
+      if (m < chunks) {
+        const int i = 32 * m + lane;
+        const bool seed = i < g.nx && __uint_as_float(near[base + i]) <= hd;
+        seeds[m] = __ballot_sync(full, seed);
+        int x = seed ? i : -kNone;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(full, x, o);
+          if (lane >= o) x = max(x, y);
+        }
+        x = max(x, carry);
+        last[m] = x;
+        carry = __shfl_sync(full, x, 31);
+      }
     }
-    dist = kFgInf;
-    for (int i = g.nx - 1; i >= 0; --i) {
-      if (d2[base + i] == 0) dist = 0;
-      else if (dist < kFgInf) ++dist;
-      const int m = min(dist, d2[base + i]);
-      d2[base + i] = m >= kFgInf ? kFgInf : m * m;
+    carry = 2 * kNone;
+#pragma unroll
+    for (int m = kFgMaxDim / 32 - 1; m >= 0; --m) {
+      if (m < chunks) {
+        const int i = 32 * m + lane;
+        int x = ((seeds[m] >> lane) & 1u) ? i : 2 * kNone;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_down_sync(full, x, o);
+          if (lane + o < 32) x = min(x, y);
+        }
+        x = min(x, carry);
+        carry = __shfl_sync(full, x, 0);
+        if (i < g.nx) {
+          const int d = min(i - last[m], x - i);
+          d2[base + i] = d >= kNone ? kFgInf : d * d;
+        }
+      }
     }
   }
 }
 
-// EDT pass along y (axis 1) or z (axis 2): lower envelope of parabolas
-// (Felzenszwalb and Huttenlocher, 2012) over each line, integer inputs.
+// EDT pass along y (AXIS 1) or z (AXIS 2): lower envelope of the parabolas
+// (q - p)^2 + f(p) over each line (Felzenszwalb and Huttenlocher, 2012), one
+// line per thread. The envelope's parabolas live in shared memory, one column
+// per thread, packed as (f << 8) | p (f < 2^24, p < 256); breakpoints are
+// compared exactly by cross-multiplying their integer numerators and
+// denominators.
+constexpr int kEdtThreads = 64;
 template <int AXIS>
-__global__ void fg_edt_yz_kernel(FgParams g, int* __restrict__ d2) {
+__global__ void __launch_bounds__(kEdtThreads) fg_edt_yz_kernel(FgParams g, int* __restrict__ d2) {
+  extern __shared__ uint32_t env[];  // [kFgMaxDim][kEdtThreads]
+  const int tid = threadIdx.x;
   const int n = AXIS == 1 ? g.ny : g.nz;
   const int64_t lines = AXIS == 1 ? (int64_t)g.nx * g.nz : (int64_t)g.nx * g.ny;
   const int64_t stride = AXIS == 1 ? g.nx : (int64_t)g.nx * g.ny;
-  // Breakpoints in FP64: they are ratios of integers below 2^18 over
-  // denominators below 2^10, so FP64 orders them exactly (ties included).
-  int f[kFgMaxDim], v[kFgMaxDim];
-  double zb[kFgMaxDim + 1];
-  for (int64_t l = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; l < lines;
-       l += (int64_t)gridDim.x * blockDim.x) {
-    int64_t base;
-    if (AXIS == 1) {
-      base = (l / g.nx) * g.nx * g.ny + (l % g.nx);  // (x, z) -> x + z nx ny
-    } else {
-      base = l;  // (x, y) -> x + y nx
-    }
-    for (int q = 0; q < n; ++q) f[q] = d2[base + q * stride];
+  for (int64_t l = (int64_t)blockIdx.x * blockDim.x + tid; l < lines; l += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t base = AXIS == 1 ? (l / g.nx) * g.nx * g.ny + (l % g.nx) : l;
     int k = -1;
+    // The line's values are read 8 at a time (independent loads in flight).
+    int buf[8];
     for (int q = 0; q < n; ++q) {
-      if (f[q] >= kFgInf) continue;
-      double s = 0.0;
-      while (k >= 0) {
-        const int p = v[k];
-        s = (double)((long long)f[q] + (long long)q * q - (long long)f[p] - (long long)p * p) /
-            (double)(2 * (q - p));
-        if (s <= zb[k]) --k;
+      if ((q & 7) == 0) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) buf[u] = q + u < n ? d2[base + (int64_t)(q + u) * stride] : kFgInf;
+      }
+      int fq = buf[0];
+#pragma unroll
+      for (int u = 1; u < 8; ++u)
+        if ((q & 7) == u) fq = buf[u];
+      if (fq >= kFgInf) continue;
+      const long long hq = (long long)fq + (long long)q * q;
+      while (k >= 1) {
+        const uint32_t e0 = env[(k - 1) * kEdtThreads + tid], e1 = env[k * kEdtThreads + tid];
+        const int v0 = (int)(e0 & 255u), v1 = (int)(e1 & 255u);
+        const long long h0 = (long long)(e0 >> 8) + (long long)v0 * v0;
+        const long long h1 = (long long)(e1 >> 8) + (long long)v1 * v1;
+        // Drop v1 when the new parabola's breakpoint with it lies at or
+        // before v1's own breakpoint with v0.
+        if ((hq - h1) * (long long)(v1 - v0) <= (h1 - h0) * (long long)(q - v1)) --k;
         else break;
       }
       ++k;
-      v[k] = q;
-      zb[k] = k == 0 ? -1e300 : s;
-      zb[k + 1] = 1e300;
+      env[k * kEdtThreads + tid] = ((uint32_t)fq << 8) | (uint32_t)q;
     }
     if (k < 0) continue;  // no surface cell on this line: stays infinite
     int j = 0;
     for (int q = 0; q < n; ++q) {
-      while (zb[j + 1] < (double)q) ++j;
-      const long long dq = (long long)(q - v[j]);
-      const long long val = dq * dq + (long long)f[v[j]];
+      while (j < k) {
+        const uint32_t e0 = env[j * kEdtThreads + tid], e1 = env[(j + 1) * kEdtThreads + tid];
+        const int v0 = (int)(e0 & 255u), v1 = (int)(e1 & 255u);
+        const long long h0 = (long long)(e0 >> 8) + (long long)v0 * v0;
+        const long long h1 = (long long)(e1 >> 8) + (long long)v1 * v1;
+        if (h1 - h0 < 2LL * q * (v1 - v0)) ++j;
+        else break;
+      }
+      const uint32_t e = env[j * kEdtThreads + tid];
+      const long long dq = (long long)(q - (int)(e & 255u));
+      const long long val = dq * dq + (long long)(e >> 8);
       d2[base + q * stride] = val >= kFgInf ? kFgInf : (int)val;
     }
   }
@@ -312,12 +359,19 @@ int free_grid_build(visacd_ctx* ctx, visacd_bvh* b) {
   VCUDA(cudaMemsetAsync(near, 0x7f, (size_t)cells * 4, ctx->stream));
   VLAUNCH(ctx, kKGridNear, grid_for((int64_t)b->nt * 32, 256, 16LL * ctx->sm_count), 256, 0, fg_near_kernel,
           b->tris, b->nt, g, near);
-  VLAUNCH(ctx, kKGridEdt, grid_for((int64_t)g.ny * g.nz, 128, 4LL * ctx->sm_count), 128, 0, fg_edt_x_kernel,
-          near, g, hd, d2);
-  VLAUNCH(ctx, kKGridEdt, grid_for((int64_t)g.nx * g.nz, 64, 8LL * ctx->sm_count), 64, 0, fg_edt_yz_kernel<1>, g,
-          d2);
-  VLAUNCH(ctx, kKGridEdt, grid_for((int64_t)g.nx * g.ny, 64, 8LL * ctx->sm_count), 64, 0, fg_edt_yz_kernel<2>, g,
-          d2);
+  VLAUNCH(ctx, kKGridEdt, grid_for((int64_t)g.ny * g.nz * 32, 256, 16LL * ctx->sm_count), 256, 0,
+          fg_edt_x_kernel, near, g, hd, d2);
+  const int edt_smem = kFgMaxDim * kEdtThreads * 4;
+  static bool edt_configured = false;
+  if (!edt_configured) {
+    VCUDA(cudaFuncSetAttribute(fg_edt_yz_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, edt_smem));
+    VCUDA(cudaFuncSetAttribute(fg_edt_yz_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, edt_smem));
+    edt_configured = true;
+  }
+  VLAUNCH(ctx, kKGridEdt, grid_for((int64_t)g.nx * g.nz, kEdtThreads, 8LL * ctx->sm_count), kEdtThreads,
+          edt_smem, fg_edt_yz_kernel<1>, g, d2);
+  VLAUNCH(ctx, kKGridEdt, grid_for((int64_t)g.nx * g.ny, kEdtThreads, 8LL * ctx->sm_count), kEdtThreads,
+          edt_smem, fg_edt_yz_kernel<2>, g, d2);
   VLAUNCH(ctx, kKGridFinal, grid_for(cells, 256, 8LL * ctx->sm_count), 256, 0, fg_final_kernel, near, d2, cells,
           g.R, g.h, hd, lb);
   b->free_lb = lb;

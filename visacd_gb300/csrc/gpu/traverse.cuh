@@ -22,6 +22,8 @@ struct VisCounters {
   unsigned pmin[3], pmax[3];  // orderable point bounds
   unsigned long long n_rows;  // rows of the tile space (masked mode)
   unsigned long long certified, trace_steps;  // free-space walks: segments cleared, grid reads
+  unsigned long long walk_work;               // tile counter of the walk kernel
+  unsigned long long pending;                 // tiles the walk left to the traversal
 };
 
 // A cage's free-space grid as the visibility kernel reads it (freegrid.cu).
@@ -30,33 +32,39 @@ struct FreeGridView {
   float ox, oy, oz, inv_h, margin;
   int32_t nx, ny, nz;
 };
-constexpr int kTraceSteps = 48;  // grid reads per segment before it goes to the BVH
+constexpr int kTraceSteps = 32;  // rounds (two grid reads each) before a segment goes to the BVH
 
 // Free-space walk of the segment p -> q (d = q - p rounded, len its FP32
-// length) through a cage's grid. From the point at t the walk may advance by
-// (lb - margin) / |q - p|: lb bounds the distance from every point of the
-// point's cell, grown by the margin, to the cage (the margin covers the FP32
-// rounding of the point and of its cell index), so no cage triangle lies
-// within the margin of the part covered. True when the walk covers [0, 1]:
-// the segment cannot hit the cage. Roundings are directed so that the part
-// covered is never overstated. `steps` counts the grid reads.
+// length) through a cage's grid, from both ends at once (two independent
+// chains of dependent reads). From the point at t the walk may advance by
+// (lb - margin) / |q - p| in either direction: lb bounds the distance from
+// every point of the point's cell, grown by the margin, to the cage (the
+// margin covers the FP32 rounding of the point and of its cell index), so no
+// cage triangle lies within the margin of the part covered. True when the two
+// covered parts [0, t] and [s, 1] meet: the segment cannot hit the cage.
+// Roundings are directed so that the parts covered are never overstated.
+// `steps` counts the grid reads.
 __device__ __forceinline__ bool trace_free(const FreeGridView& g, float px, float py, float pz, float dx,
                                            float dy, float dz, float len, unsigned long long& steps) {
   // 1 / |q - p| rounded down; |q - p| <= len (1 + 17u).
   const float inv_len = __frcp_rd(__fmul_ru(len, 1.000001f));
-  float t = 0.f;
+  float t = 0.f, s = 1.f;
   for (int k = 0; k < kTraceSteps; ++k) {
-    const float x = fmaf(t, dx, px), y = fmaf(t, dy, py), z = fmaf(t, dz, pz);
-    const int ix = __float2int_rd((x - g.ox) * g.inv_h);
-    const int iy = __float2int_rd((y - g.oy) * g.inv_h);
-    const int iz = __float2int_rd((z - g.oz) * g.inv_h);
-    if ((unsigned)ix >= (unsigned)g.nx || (unsigned)iy >= (unsigned)g.ny || (unsigned)iz >= (unsigned)g.nz)
+    const float x0 = fmaf(t, dx, px), y0 = fmaf(t, dy, py), z0 = fmaf(t, dz, pz);
+    const float x1 = fmaf(s, dx, px), y1 = fmaf(s, dy, py), z1 = fmaf(s, dz, pz);
+    const int ix0 = __float2int_rd((x0 - g.ox) * g.inv_h), ix1 = __float2int_rd((x1 - g.ox) * g.inv_h);
+    const int iy0 = __float2int_rd((y0 - g.oy) * g.inv_h), iy1 = __float2int_rd((y1 - g.oy) * g.inv_h);
+    const int iz0 = __float2int_rd((z0 - g.oz) * g.inv_h), iz1 = __float2int_rd((z1 - g.oz) * g.inv_h);
+    if ((unsigned)ix0 >= (unsigned)g.nx || (unsigned)iy0 >= (unsigned)g.ny || (unsigned)iz0 >= (unsigned)g.nz ||
+        (unsigned)ix1 >= (unsigned)g.nx || (unsigned)iy1 >= (unsigned)g.ny || (unsigned)iz1 >= (unsigned)g.nz)
       return false;
-    const float lb = __ldg(&g.lb[((int64_t)iz * g.ny + iy) * g.nx + ix]);
-    ++steps;
-    if (!(lb > g.margin)) return false;
-    t = __fadd_rd(t, __fmul_rd(__fsub_rd(lb, g.margin), inv_len));
-    if (t >= 1.f) return true;
+    const float lb0 = __ldg(&g.lb[((int64_t)iz0 * g.ny + iy0) * g.nx + ix0]);
+    const float lb1 = __ldg(&g.lb[((int64_t)iz1 * g.ny + iy1) * g.nx + ix1]);
+    steps += 2;
+    if (!(lb0 > g.margin) || !(lb1 > g.margin)) return false;
+    t = __fadd_rd(t, __fmul_rd(__fsub_rd(lb0, g.margin), inv_len));
+    s = __fsub_ru(s, __fmul_rd(__fsub_rd(lb1, g.margin), inv_len));
+    if (t >= s) return true;
   }
   return false;
 }

@@ -56,6 +56,10 @@ struct VisParams {
   int64_t ntr;                          // tile rows
   const unsigned long long* row_start;  // triangular mode: first tile of each tile row
   FreeGridView cage_free;               // the cage's free-space grid (lb null: none)
+  // After a walk: the tiles with lanes left for the traversal, and per such
+  // tile the lanes that are done (no pair, degenerate, or cleared).
+  unsigned long long* pend_tiles;       // null: no walk, every tile is traversed
+  uint32_t* pend_done;
 };
 
 // Work item w -> tile (tr, tc). Rectangle mode: row-major. Triangular mode:
@@ -66,6 +70,23 @@ __device__ __forceinline__ void tile_of(const VisParams& P, unsigned long long w
   if (!P.triangular) {
     tr = (int64_t)(w / (unsigned long long)P.ntc);
     tc = (int64_t)(w % (unsigned long long)P.ntc);
+    return;
+  }
+  if (TR >= TC) {
+    // r = TR / TC is an integer and row t holds ntc - r t tiles (never
+    // negative: r (ntr - 1) <= ntc), so row t starts at
+    // S(t) = t ntc - r t (t - 1) / 2. Solve S(t) <= w < S(t + 1) in FP64 and
+    // settle the rounding with the exact integers.
+    const int64_t r = TR / TC, ntc = P.ntc;
+    auto S = [&](int64_t t) { return t * ntc - r * t * (t - 1) / 2; };
+    const double b = (double)ntc + 0.5 * (double)r;
+    const double disc = b * b - 2.0 * (double)r * (double)w;
+    int64_t t = (int64_t)((b - sqrt(disc > 0.0 ? disc : 0.0)) / (double)r);
+    t = t < 0 ? 0 : (t > P.ntr - 1 ? P.ntr - 1 : t);
+    while (t > 0 && (unsigned long long)S(t) > w) --t;
+    while (t < P.ntr - 1 && (unsigned long long)S(t + 1) <= w) ++t;
+    tr = t;
+    tc = t * r + (int64_t)(w - (unsigned long long)S(t));
     return;
   }
   int64_t lo = 0, hi = P.ntr - 1;
@@ -88,18 +109,17 @@ __global__ void tile_row_counts_kernel(int64_t ntr, int64_t ntc, int TR, int TC,
 
 // Per-lane counters of a visibility launch, reduced over the warp at the end.
 struct VisLaneCounters {
-  unsigned long long pairs = 0, edges = 0, self = 0, cage = 0, deg = 0, certified = 0, trace_steps = 0;
+  unsigned long long pairs = 0, edges = 0, self = 0, cage = 0, deg = 0;
   unsigned rechecks = 0, status_bits = 0, visits = 0, tri_tests = 0;
 };
 
-// One tile (work item w of P's tile space) for the calling warp: the cage
-// test, then the self test for lanes whose segment leaves the cage, and the
-// edge bits.
+// The pair of `lane` in tile w of P's tile space (original vertex ids i < j),
+// or valid = false. The walk and the traversal kernels share it, so a tile's
+// lane means the same pair in both.
 template <int TR>
-__device__ __forceinline__ void vis_tile(const VisParams& P, unsigned long long w, int lane,
-                                         VisLaneCounters& c) {
+__device__ __forceinline__ bool lane_pair(const VisParams& P, unsigned long long w, int lane, uint32_t& i,
+                                          uint32_t& j) {
   constexpr int TC = 32 / TR;
-  const int64_t n = P.n;
   int64_t tr, tc;
   tile_of(P, w, tr, tc, TR, TC);
   const int64_t a = tr * TR + lane / TC;
@@ -120,11 +140,27 @@ __device__ __forceinline__ void vis_tile(const VisParams& P, unsigned long long 
       valid = oi != oj && (!P.is_new[oj] || P.newrank[oj] > a);
     }
   }
-  const uint32_t i = min(oi, oj), j = max(oi, oj);
+  i = min(oi, oj);
+  j = max(oi, oj);
+  return valid;
+}
+
+// One tile (work item w of P's tile space) for the calling warp: the cage
+// test, then the self test for lanes whose segment leaves the cage, and the
+// edge bits. After a free-space walk (walked) the walk has taken the tile's
+// pair and degenerate counts, and `done` marks the lanes it settled: they
+// take no part.
+template <int TR>
+__device__ __forceinline__ void vis_tile(const VisParams& P, unsigned long long w, int lane,
+                                         VisLaneCounters& c, bool walked, uint32_t done) {
+  const int64_t n = P.n;
+  uint32_t i, j;
+  const bool mine = !((done >> lane) & 1u);
+  const bool valid = lane_pair<TR>(P, w, lane, i, j) && mine;
   Seg s;
   float3 p = make_float3(0.f, 0.f, 0.f), q = make_float3(0.f, 0.f, 0.f);
   if (valid) {
-    ++c.pairs;
+    if (!walked) ++c.pairs;
     p = make_float3(P.pts[3 * (int64_t)i], P.pts[3 * (int64_t)i + 1], P.pts[3 * (int64_t)i + 2]);
     q = make_float3(P.pts[3 * (int64_t)j], P.pts[3 * (int64_t)j + 1], P.pts[3 * (int64_t)j + 2]);
   }
@@ -136,16 +172,8 @@ __device__ __forceinline__ void vis_tile(const VisParams& P, unsigned long long 
   }
   if (!__ballot_sync(0xffffffffu, active)) return;
   // The cage first: few segments leave it, so the self test runs for few.
-  // Segments the free-space walk clears cannot hit the cage; the others go
-  // through the BVH.
   s.exclude = false;
-  bool cage_test = active;
-  if (P.cage_free.lb != nullptr && active &&
-      trace_free(P.cage_free, p.x, p.y, p.z, s.dx, s.dy, s.dz, seg_len(s), c.trace_steps)) {
-    cage_test = false;
-    ++c.certified;
-  }
-  const bool cage_hit = packet_any_hit(P.cage_nodes, P.cage_tris, P.cage_nt, s, P.pts, cage_test,
+  const bool cage_hit = packet_any_hit(P.cage_nodes, P.cage_tris, P.cage_nt, s, P.pts, active,
                                        c.rechecks, c.status_bits, c.visits, c.tri_tests);
   if (active && cage_hit) ++c.cage;
   active = active && cage_hit;
@@ -171,8 +199,6 @@ __device__ __forceinline__ void vis_flush_counters(VisCounters* cnt, unsigned* s
     c.deg += __shfl_xor_sync(0xffffffffu, c.deg, o);
     c.rechecks += __shfl_xor_sync(0xffffffffu, c.rechecks, o);
     c.tri_tests += __shfl_xor_sync(0xffffffffu, c.tri_tests, o);
-    c.certified += __shfl_xor_sync(0xffffffffu, c.certified, o);
-    c.trace_steps += __shfl_xor_sync(0xffffffffu, c.trace_steps, o);
     c.status_bits |= __shfl_xor_sync(0xffffffffu, c.status_bits, o);
   }
   if (lane == 0) {
@@ -184,8 +210,6 @@ __device__ __forceinline__ void vis_flush_counters(VisCounters* cnt, unsigned* s
     atomicAdd(&cnt->rechecks, (unsigned long long)c.rechecks);
     atomicAdd(&cnt->node_visits, (unsigned long long)c.visits);
     atomicAdd(&cnt->tri_tests, (unsigned long long)c.tri_tests);
-    if (c.certified) atomicAdd(&cnt->certified, c.certified);
-    if (c.trace_steps) atomicAdd(&cnt->trace_steps, c.trace_steps);
     if (c.status_bits) atomicOr(status, c.status_bits);
   }
 }
@@ -194,14 +218,74 @@ template <int TR, int MINB>
 __global__ void __launch_bounds__(kVisThreads, MINB) visibility_kernel(VisParams P) {
   const int lane = threadIdx.x & 31;
   VisLaneCounters c;
+  // After a walk only the tiles it left are traversed (their count is on the
+  // device, written by the walk kernel before this launch).
+  const unsigned long long items = P.pend_tiles ? P.cnt->pending : P.total_tiles;
   for (int guard = 0; guard < (1 << 30); ++guard) {
     unsigned long long w = 0;
     if (lane == 0) w = atomicAdd(&P.cnt->work, 1ull);
     w = __shfl_sync(0xffffffffu, w, 0);
-    if (w >= P.total_tiles) break;
-    vis_tile<TR>(P, w, lane, c);
+    if (w >= items) break;
+    if (P.pend_tiles)
+      vis_tile<TR>(P, P.pend_tiles[w], lane, c, true, P.pend_done[w]);
+    else
+      vis_tile<TR>(P, w, lane, c, false, 0u);
   }
   vis_flush_counters(P.cnt, P.status, lane, c);
+}
+
+// The free-space walk over P's tile space, before the traversal kernel. It
+// takes the pair and degenerate counts of every tile, and lists the tiles
+// that keep a lane for the traversal (P.pend_tiles) with the lanes that are
+// done (no pair, degenerate, or cleared: the segment cannot hit the cage;
+// traverse.cuh, trace_free). Few registers, so many warps per SM hide the
+// latency of the walk's dependent grid reads.
+template <int TR>
+__global__ void __launch_bounds__(kVisThreads, 16) visibility_walk_kernel(VisParams P) {
+  const int lane = threadIdx.x & 31;
+  unsigned long long pairs = 0, deg = 0, cleared = 0, steps = 0;
+  for (int guard = 0; guard < (1 << 30); ++guard) {
+    unsigned long long w = 0;
+    if (lane == 0) w = atomicAdd(&P.cnt->walk_work, 1ull);
+    w = __shfl_sync(0xffffffffu, w, 0);
+    if (w >= P.total_tiles) break;
+    uint32_t i, j;
+    bool done = true;
+    if (lane_pair<TR>(P, w, lane, i, j)) {
+      ++pairs;
+      const float px = P.pts[3 * (int64_t)i], py = P.pts[3 * (int64_t)i + 1], pz = P.pts[3 * (int64_t)i + 2];
+      const float dx = __fsub_rn(P.pts[3 * (int64_t)j], px), dy = __fsub_rn(P.pts[3 * (int64_t)j + 1], py),
+                  dz = __fsub_rn(P.pts[3 * (int64_t)j + 2], pz);
+      const float len =
+          __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
+      if (!(len > 0.f)) {  // coincident endpoints (or NaN): never an edge (as in vis_tile)
+        ++deg;
+      } else if (trace_free(P.cage_free, px, py, pz, dx, dy, dz, len, steps)) {
+        ++cleared;
+      } else {
+        done = false;
+      }
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, done);
+    if (lane == 0 && m != 0xffffffffu) {
+      const unsigned long long k = atomicAdd(&P.cnt->pending, 1ull);
+      P.pend_tiles[k] = w;
+      P.pend_done[k] = m;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    pairs += __shfl_xor_sync(0xffffffffu, pairs, o);
+    deg += __shfl_xor_sync(0xffffffffu, deg, o);
+    cleared += __shfl_xor_sync(0xffffffffu, cleared, o);
+    steps += __shfl_xor_sync(0xffffffffu, steps, o);
+  }
+  if (lane == 0) {
+    if (pairs) atomicAdd(&P.cnt->pairs, pairs);
+    if (deg) atomicAdd(&P.cnt->degenerate, deg);
+    if (cleared) atomicAdd(&P.cnt->certified, cleared);
+    if (steps) atomicAdd(&P.cnt->trace_steps, steps);
+  }
 }
 
 // Many parts in one persistent launch: the work items of all parts are
@@ -226,7 +310,7 @@ __global__ void __launch_bounds__(kVisThreads, MINB)
       const int mid = (lo + hi + 1) >> 1;
       if (tile_start[mid] <= w) lo = mid; else hi = mid - 1;
     }
-    vis_tile<TR>(parts[lo], w - tile_start[lo], lane, c);
+    vis_tile<TR>(parts[lo], w - tile_start[lo], lane, c, false, 0u);
   }
   vis_flush_counters(cnt, status, lane, c);
 }
@@ -374,6 +458,17 @@ constexpr int kDefaultVisVariant = 1;
 
 static int launch_vis_variant(visacd_ctx* ctx, int v, const VisParams& P) {
   const unsigned grid = (unsigned)(ctx->sm_count * kVisVariants[v].minb);
+  if (P.pend_tiles != nullptr) {
+    const unsigned wg = (unsigned)(ctx->sm_count * 16);
+    switch (kVisVariants[v].tr) {
+      case 8: VLAUNCH(ctx, kKVisWalk, wg, kVisThreads, 0, visibility_walk_kernel<8>, P); break;
+      case 4: VLAUNCH(ctx, kKVisWalk, wg, kVisThreads, 0, visibility_walk_kernel<4>, P); break;
+      case 16: VLAUNCH(ctx, kKVisWalk, wg, kVisThreads, 0, visibility_walk_kernel<16>, P); break;
+      case 2: VLAUNCH(ctx, kKVisWalk, wg, kVisThreads, 0, visibility_walk_kernel<2>, P); break;
+      case 1: VLAUNCH(ctx, kKVisWalk, wg, kVisThreads, 0, visibility_walk_kernel<1>, P); break;
+      default: VLAUNCH(ctx, kKVisWalk, wg, kVisThreads, 0, visibility_walk_kernel<32>, P); break;
+    }
+  }
   switch (v) {
     case 0: VLAUNCH(ctx, kKVisibility, grid, kVisThreads, 0, (visibility_kernel<8, 6>), P); break;
     case 1: VLAUNCH(ctx, kKVisibility, grid, kVisThreads, 0, (visibility_kernel<8, 8>), P); break;
@@ -528,10 +623,15 @@ static int vis_device(visacd_ctx* ctx, const float* d_pts, int32_t n, const uint
   P.cage_tris = cage_bvh->tris;
   P.cage_nt = cage_bvh->nt;
   // Large calls first clear what they can with the cage's free-space grid
-  // (built at the top of this call).
-  if (use_grid) {
+  // (built at the top of this call): a walk kernel, then the traversal.
+  if (use_grid && cage_bvh->free_lb && P.total_tiles > 0) {
+    VTRY(ensure_slot(ctx, kSlotVisCleared, (size_t)P.total_tiles * 12 + 256));
+    P.pend_tiles = slot<unsigned long long>(ctx, kSlotVisCleared);
+    P.pend_done = reinterpret_cast<uint32_t*>(P.pend_tiles + P.total_tiles);
+  }
+  if (P.pend_tiles != nullptr) {
     const visacd_bvh* cb = cage_bvh;
-    if (cb->free_lb) {
+    {
       P.cage_free.lb = cb->free_lb;
       P.cage_free.ox = cb->fg_ox;
       P.cage_free.oy = cb->fg_oy;
@@ -1029,7 +1129,8 @@ extern "C" int visacd_autotune_visibility(visacd_ctx* ctx, const float* pts, int
       if (rc == VISACD_OK) rc = visacd_ctx_kernel_times(ctx, names, t, cnt, 64, &nk);
       ms = 0.0;
       for (int k = 0; k < nk && k < 64; ++k)
-        if (strcmp(names[k], kernel_name(kKVisibility)) == 0) ms = t[k];
+        if (strcmp(names[k], kernel_name(kKVisibility)) == 0 || strcmp(names[k], kernel_name(kKVisWalk)) == 0)
+          ms += t[k];
     }
     if (ms_per_variant) ms_per_variant[v] = ms;
     if (ms < best_ms) {
