@@ -151,6 +151,12 @@ __global__ void fg_near_kernel(const float4* __restrict__ tris, int32_t nt, FgPa
       const float x = g.ox + ((float)ix + 0.5f) * g.h;
       const float y = g.oy + ((float)iy + 0.5f) * g.h;
       const float z = g.oz + ((float)iz + 0.5f) * g.h;
+      // Cells whose centre lies farther than R from the triangle's box keep
+      // their value: the cap at R already bounds them.
+      const float gx = fmaxf(0.f, fmaxf(lo[0] + g.R - x, x - (hi[0] - g.R)));
+      const float gy = fmaxf(0.f, fmaxf(lo[1] + g.R - y, y - (hi[1] - g.R)));
+      const float gz = fmaxf(0.f, fmaxf(lo[2] + g.R - z, z - (hi[2] - g.R)));
+      if (gx * gx + gy * gy + gz * gz > 1.0001f * g.R * g.R) continue;
       const float lb = fg_tri_lb(x, y, z, A, B, C);
       atomicMin(&near[((int64_t)iz * g.ny + iy) * g.nx + ix], __float_as_uint(lb));
     }
