@@ -381,6 +381,13 @@ void bvh_detach(visacd_bvh* b) {
   if (b->nodes) cudaFreeAsync(b->nodes, b->stream);
   if (b->tris) cudaFreeAsync(b->tris, b->stream);
   if (b->free_lb) cudaFreeAsync(b->free_lb, b->stream);
+  if (b->free_tex) cudaDestroyTextureObject(b->free_tex);
+  if (b->free_arr) {
+    cudaStreamSynchronize(b->stream);  // a queued walk may still read it
+    cudaFreeArray(b->free_arr);
+  }
+  b->free_tex = 0;
+  b->free_arr = nullptr;
   b->nodes = b->tris = nullptr;
   b->free_lb = nullptr;
   b->ctx = nullptr;

@@ -380,6 +380,41 @@ int free_grid_build(visacd_ctx* ctx, visacd_bvh* b) {
           edt_smem, fg_edt_yz_kernel<2>, g, d2);
   VLAUNCH(ctx, kKGridFinal, grid_for(cells, 256, 8LL * ctx->sm_count), 256, 0, fg_final_kernel, near, d2, cells,
           g.R, g.h, hd, lb);
+  // The bounds as a 3D texture: point sampling at cell coordinate u reads
+  // cell floor(u), and the texture's block-linear layout keeps nearby cells
+  // (in 3D) in the same cache lines; reads outside the grid return 0 (the
+  // border), which stops a walk.
+  {
+    cudaChannelFormatDesc fd = cudaCreateChannelDesc<float>();
+    cudaArray_t arr = nullptr;
+    VCUDA(cudaMalloc3DArray(&arr, &fd, make_cudaExtent(g.nx, g.ny, g.nz)));
+    cudaMemcpy3DParms cp = {};
+    cp.srcPtr = make_cudaPitchedPtr(lb, (size_t)g.nx * sizeof(float), g.nx, g.ny);
+    cp.dstArray = arr;
+    cp.extent = make_cudaExtent(g.nx, g.ny, g.nz);
+    cp.kind = cudaMemcpyDeviceToDevice;
+    cudaError_t e = cudaMemcpy3DAsync(&cp, ctx->stream);
+    cudaTextureObject_t tex = 0;
+    if (e == cudaSuccess) {
+      cudaResourceDesc rd = {};
+      rd.resType = cudaResourceTypeArray;
+      rd.res.array.array = arr;
+      cudaTextureDesc td = {};
+      td.addressMode[0] = td.addressMode[1] = td.addressMode[2] = cudaAddressModeBorder;
+      td.borderColor[0] = td.borderColor[1] = td.borderColor[2] = td.borderColor[3] = 0.f;
+      td.filterMode = cudaFilterModePoint;
+      td.readMode = cudaReadModeElementType;
+      td.normalizedCoords = 0;
+      e = cudaCreateTextureObject(&tex, &rd, &td, nullptr);
+    }
+    if (e != cudaSuccess) {
+      cudaFreeArray(arr);
+      set_error("free_grid_build: %s", cudaGetErrorString(e));
+      return VISACD_ERR_CUDA;
+    }
+    b->free_arr = arr;
+    b->free_tex = tex;
+  }
   b->free_lb = lb;
   lb = nullptr;  // owned by the BVH now
   b->fg_ox = g.ox;

@@ -28,7 +28,8 @@ struct VisCounters {
 
 // A cage's free-space grid as the visibility kernel reads it (freegrid.cu).
 struct FreeGridView {
-  const float* lb;  // null: no grid
+  const float* lb;          // null: no grid
+  cudaTextureObject_t tex;  // the same bounds as a 3D texture (border 0)
   float ox, oy, oz, inv_h, margin;
   int32_t nx, ny, nz;
 };
@@ -52,14 +53,9 @@ __device__ __forceinline__ bool trace_free(const FreeGridView& g, float px, floa
   for (int k = 0; k < kTraceSteps; ++k) {
     const float x0 = fmaf(t, dx, px), y0 = fmaf(t, dy, py), z0 = fmaf(t, dz, pz);
     const float x1 = fmaf(s, dx, px), y1 = fmaf(s, dy, py), z1 = fmaf(s, dz, pz);
-    const int ix0 = __float2int_rd((x0 - g.ox) * g.inv_h), ix1 = __float2int_rd((x1 - g.ox) * g.inv_h);
-    const int iy0 = __float2int_rd((y0 - g.oy) * g.inv_h), iy1 = __float2int_rd((y1 - g.oy) * g.inv_h);
-    const int iz0 = __float2int_rd((z0 - g.oz) * g.inv_h), iz1 = __float2int_rd((z1 - g.oz) * g.inv_h);
-    if ((unsigned)ix0 >= (unsigned)g.nx || (unsigned)iy0 >= (unsigned)g.ny || (unsigned)iz0 >= (unsigned)g.nz ||
-        (unsigned)ix1 >= (unsigned)g.nx || (unsigned)iy1 >= (unsigned)g.ny || (unsigned)iz1 >= (unsigned)g.nz)
-      return false;
-    const float lb0 = __ldg(&g.lb[((int64_t)iz0 * g.ny + iy0) * g.nx + ix0]);
-    const float lb1 = __ldg(&g.lb[((int64_t)iz1 * g.ny + iy1) * g.nx + ix1]);
+    // Cell coordinates; point sampling reads cell floor(u), the border 0.
+    const float lb0 = tex3D<float>(g.tex, (x0 - g.ox) * g.inv_h, (y0 - g.oy) * g.inv_h, (z0 - g.oz) * g.inv_h);
+    const float lb1 = tex3D<float>(g.tex, (x1 - g.ox) * g.inv_h, (y1 - g.oy) * g.inv_h, (z1 - g.oz) * g.inv_h);
     steps += 2;
     if (!(lb0 > g.margin) || !(lb1 > g.margin)) return false;
     t = __fadd_rd(t, __fmul_rd(__fsub_rd(lb0, g.margin), inv_len));

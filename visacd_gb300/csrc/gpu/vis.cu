@@ -633,6 +633,7 @@ static int vis_device(visacd_ctx* ctx, const float* d_pts, int32_t n, const uint
     const visacd_bvh* cb = cage_bvh;
     {
       P.cage_free.lb = cb->free_lb;
+      P.cage_free.tex = cb->free_tex;
       P.cage_free.ox = cb->fg_ox;
       P.cage_free.oy = cb->fg_oy;
       P.cage_free.oz = cb->fg_oz;
