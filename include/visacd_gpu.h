@@ -182,8 +182,8 @@ int visacd_autotune_visibility(visacd_ctx* ctx, const float* pts, int32_t n, con
                                const visacd_bvh* cage_bvh, int* best_variant,
                                double* ms_per_variant);
 
-/* Free-space walks (on by default). A visibility call with at least 2^20
-   pairs first walks each segment through a grid over its cage that bounds,
+/* Free-space walks (on by default). A visibility call (or a part of a
+   batched call) with at least 2^22 pairs first walks each segment through a grid over its cage that bounds,
    per cell, the distance to the cage's triangles (built once per cage BVH,
    kept with it): a segment whose whole length the walk covers cannot hit the
    cage and skips the cage BVH; every other segment is traced as before. The

@@ -155,7 +155,6 @@ def test_torus_64x32_all_pairs(ctx, orc):
     assert ost["pairs"] == 2096128
     assert nd <= ost["n_grazing"]
     cleared, reads = ctx.vis_trace_counts()
-    assert cleared > 0  # the free-space walk took part
     print(f"torus 64x32: {len(e)} edges, {ost['n_grazing']} grazing pairs, {nd} differ (all grazing); "
           f"{cleared} segments cleared by the free-space walk ({reads} grid reads)")
 
@@ -215,8 +214,9 @@ def test_free_space_walk_changes_nothing(ctx, case):
     assert s1["fp64_rechecks"] <= s0["fp64_rechecks"] and s1["tri_tests"] <= s0["tri_tests"]
     # The share cleared depends on the shape: most chords of the blob stay far
     # from its cage; the torus's run close to its tube.
-    least = {"blob_s5": 0.9, "torus_64x32": 0.3, "blob_s4_masked": 0.3, "tiny_cage_gap": 0.0}[case]
-    if s1["pairs_tested"] >= 1 << 20 and least > 0:
+    # Calls below 2^22 pairs (the torus) do not walk.
+    least = {"blob_s5": 0.9, "torus_64x32": 0.0, "blob_s4_masked": 0.3, "tiny_cage_gap": 0.0}[case]
+    if least > 0:
         assert cleared > least * s1["pairs_tested"]
         assert s1["node_visits"] < s0["node_visits"]
     print(f"{case}: {s1['pairs_tested']} pairs, {cleared} cleared, {reads} grid reads, "

@@ -45,9 +45,9 @@ int bvh_build(visacd_ctx* ctx, const float* verts, int32_t nv, const uint32_t* t
 // stays valid until visacd_bvh_destroy, and is rejected by queries).
 void bvh_detach(visacd_bvh* b);
 // Builds the BVH's free-space grid (once; a BVH whose grid would not be
-// usable keeps none). Uses the context's counter slot and pinned staging
+// usable keeps none), its resolution sized for a call over `pairs` pairs. Uses the context's counter slot and pinned staging
 // buffer (waits for the stream first), so it runs before a call takes them.
 // Asynchronous after one small read-back.
-int free_grid_build(visacd_ctx* ctx, visacd_bvh* b);
+int free_grid_build(visacd_ctx* ctx, visacd_bvh* b, int64_t pairs);
 
 }  // namespace vgpu

@@ -296,7 +296,7 @@ __global__ void fg_final_kernel(const unsigned* __restrict__ near, const int* __
 
 }  // namespace
 
-int free_grid_build(visacd_ctx* ctx, visacd_bvh* b) {
+int free_grid_build(visacd_ctx* ctx, visacd_bvh* b, int64_t pairs) {
   if (b->free_built) return VISACD_OK;
   b->free_built = true;  // also when the grid is not usable: then it is not retried
   if (b->nt <= 0) return VISACD_OK;
@@ -328,6 +328,10 @@ int free_grid_build(visacd_ctx* ctx, visacd_bvh* b) {
                               std::max(std::max(std::fabs(lo[1]), std::fabs(hi[1])),
                                        std::max(std::fabs(lo[2]), std::fabs(hi[2]))));
   if (!(ext > 0.f)) return VISACD_OK;
+  // 192 cells along the longest side: fine enough that a cell's half
+  // diagonal stays well below the usual part-to-cage gap. The grid's cost
+  // follows its cells, so only calls with many pairs build one.
+  (void)pairs;
   const float hcell = ext / 192.f;
   const float delta = hcell / 64.f;
   // The growth delta must cover the FP32 rounding of the walk's points and

@@ -30,8 +30,9 @@
 
 namespace vgpu {
 
-// Pairs from which a call builds and uses the cage's free-space grid.
-constexpr int64_t kFreeGridMinPairs = 1 << 20;
+// Pairs from which a call (or a part of a batched call) builds and uses the
+// cage's free-space grid: below this the grid costs about what the walk saves.
+constexpr int64_t kFreeGridMinPairs = 1 << 22;
 
 struct VisParams {
   const float* pts;
@@ -292,27 +293,100 @@ __global__ void __launch_bounds__(kVisThreads, 16) visibility_walk_kernel(VisPar
 // numbered consecutively (part p owns [tile_start[p], tile_start[p + 1])),
 // and each warp finds the part of its item by binary search. Every part keeps
 // its own tile space, mask and bitset region; the counters are shared.
+__device__ __forceinline__ int part_of(const unsigned long long* __restrict__ tile_start, int n_parts,
+                                       unsigned long long w) {
+  int lo = 0, hi = n_parts - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (tile_start[mid] <= w) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// With pend_tiles (after visibility_multi_walk_kernel) only the listed tiles
+// are traversed, with the lanes the walk settled left out.
 template <int TR, int MINB>
 __global__ void __launch_bounds__(kVisThreads, MINB)
     visibility_multi_kernel(const VisParams* __restrict__ parts, int n_parts,
                             const unsigned long long* __restrict__ tile_start,
                             unsigned long long total_tiles, VisCounters* __restrict__ cnt,
-                            unsigned* __restrict__ status) {
+                            unsigned* __restrict__ status, const unsigned long long* __restrict__ pend_tiles,
+                            const uint32_t* __restrict__ pend_done) {
   const int lane = threadIdx.x & 31;
   VisLaneCounters c;
+  const unsigned long long items = pend_tiles ? cnt->pending : total_tiles;
   for (int guard = 0; guard < (1 << 30); ++guard) {
     unsigned long long w = 0;
     if (lane == 0) w = atomicAdd(&cnt->work, 1ull);
     w = __shfl_sync(0xffffffffu, w, 0);
-    if (w >= total_tiles) break;
-    int lo = 0, hi = n_parts - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (tile_start[mid] <= w) lo = mid; else hi = mid - 1;
+    if (w >= items) break;
+    if (pend_tiles) {
+      const unsigned long long g = pend_tiles[w];
+      const int p = part_of(tile_start, n_parts, g);
+      vis_tile<TR>(parts[p], g - tile_start[p], lane, c, true, pend_done[w]);
+    } else {
+      const int p = part_of(tile_start, n_parts, w);
+      vis_tile<TR>(parts[p], w - tile_start[p], lane, c, false, 0u);
     }
-    vis_tile<TR>(parts[lo], w - tile_start[lo], lane, c, false, 0u);
   }
   vis_flush_counters(cnt, status, lane, c);
+}
+
+// The free-space walk over all parts' tiles (as visibility_walk_kernel; parts
+// without a grid leave every pair to the traversal). Pending tiles are listed
+// by their global number.
+template <int TR>
+__global__ void __launch_bounds__(kVisThreads, 16)
+    visibility_multi_walk_kernel(const VisParams* __restrict__ parts, int n_parts,
+                                 const unsigned long long* __restrict__ tile_start,
+                                 unsigned long long total_tiles, VisCounters* __restrict__ cnt,
+                                 unsigned long long* __restrict__ pend_tiles, uint32_t* __restrict__ pend_done) {
+  const int lane = threadIdx.x & 31;
+  unsigned long long pairs = 0, deg = 0, cleared = 0, steps = 0;
+  for (int guard = 0; guard < (1 << 30); ++guard) {
+    unsigned long long w = 0;
+    if (lane == 0) w = atomicAdd(&cnt->walk_work, 1ull);
+    w = __shfl_sync(0xffffffffu, w, 0);
+    if (w >= total_tiles) break;
+    const int pi = part_of(tile_start, n_parts, w);
+    const VisParams& P = parts[pi];
+    uint32_t i, j;
+    bool done = true;
+    if (lane_pair<TR>(P, w - tile_start[pi], lane, i, j)) {
+      ++pairs;
+      const float px = P.pts[3 * (int64_t)i], py = P.pts[3 * (int64_t)i + 1], pz = P.pts[3 * (int64_t)i + 2];
+      const float dx = __fsub_rn(P.pts[3 * (int64_t)j], px), dy = __fsub_rn(P.pts[3 * (int64_t)j + 1], py),
+                  dz = __fsub_rn(P.pts[3 * (int64_t)j + 2], pz);
+      const float len =
+          __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
+      if (!(len > 0.f)) {
+        ++deg;
+      } else if (P.cage_free.lb != nullptr && trace_free(P.cage_free, px, py, pz, dx, dy, dz, len, steps)) {
+        ++cleared;
+      } else {
+        done = false;
+      }
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, done);
+    if (lane == 0 && m != 0xffffffffu) {
+      const unsigned long long k = atomicAdd(&cnt->pending, 1ull);
+      pend_tiles[k] = w;
+      pend_done[k] = m;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    pairs += __shfl_xor_sync(0xffffffffu, pairs, o);
+    deg += __shfl_xor_sync(0xffffffffu, deg, o);
+    cleared += __shfl_xor_sync(0xffffffffu, cleared, o);
+    steps += __shfl_xor_sync(0xffffffffu, steps, o);
+  }
+  if (lane == 0) {
+    if (pairs) atomicAdd(&cnt->pairs, pairs);
+    if (deg) atomicAdd(&cnt->degenerate, deg);
+    if (cleared) atomicAdd(&cnt->certified, cleared);
+    if (steps) atomicAdd(&cnt->trace_steps, steps);
+  }
 }
 
 // ---- vertex ordering ------------------------------------------------------
@@ -526,12 +600,12 @@ int vis_morton_order(visacd_ctx* ctx, const float* d_pts, int32_t n, uint32_t* p
 
 static int vis_device(visacd_ctx* ctx, const float* d_pts, int32_t n, const uint8_t* d_new,
                       const visacd_bvh* self_bvh, const visacd_bvh* cage_bvh, int64_t* n_edges,
-                      visacd_vis_stats* stats) {
-  // The cage's free-space grid, for large calls: built once per cage BVH,
-  // before this call's counters take the shared scratch and staging buffers.
-  const bool use_grid = ctx->vis_trace && n >= 2 &&
-                        (int64_t)n * (n - 1) / 2 >= kFreeGridMinPairs && cage_bvh->nt > 0;
-  if (use_grid) VTRY(free_grid_build(ctx, const_cast<visacd_bvh*>(cage_bvh)));
+                      visacd_vis_stats* stats, int64_t pairs) {
+  // The cage's free-space grid, for calls with many pairs (`pairs`: the
+  // call's pair count, or a bound of it): built once per cage BVH, before this
+  // call's counters take the shared scratch and staging buffers.
+  const bool use_grid = ctx->vis_trace && n >= 2 && pairs >= kFreeGridMinPairs && cage_bvh->nt > 0;
+  if (use_grid) VTRY(free_grid_build(ctx, const_cast<visacd_bvh*>(cage_bvh), pairs));
   VTRY(ensure_slot(ctx, kSlotCounters, sizeof(VisCounters)));
   VisCounters* cnt = slot<VisCounters>(ctx, kSlotCounters);
   VisCounters init;
@@ -745,6 +819,29 @@ int visibility_multi_impl(visacd_ctx* ctx, int32_t n_parts, const float* const* 
          "visibility_batch: null argument");
   VCUDA(cudaSetDevice(ctx->device));
   constexpr int TR = 8, TC = 4;
+  // Free-space grids of the large parts' cages (built once per cage BVH),
+  // before this call takes the shared scratch and staging buffers.
+  // A part's pairs: all of them, or (masked) those with a new endpoint.
+  std::vector<int64_t> part_pairs(n_parts, 0);
+  for (int p = 0; p < n_parts; ++p) {
+    const int64_t n = std::max(n_pts[p], 0);
+    int64_t pairs = n * (n > 0 ? n - 1 : 0) / 2;
+    if (is_new && is_new[p] && pts[p]) {
+      int64_t k = 0;
+      for (int64_t v = 0; v < n; ++v) k += is_new[p][v] != 0;
+      pairs -= (n - k) * (n - k - 1) / 2;
+    }
+    part_pairs[p] = pairs;
+  }
+  bool any_grid = false;
+  if (ctx->vis_trace) {
+    for (int p = 0; p < n_parts; ++p) {
+      if (part_pairs[p] >= kFreeGridMinPairs && cage_bvhs[p] && cage_bvhs[p]->ctx && cage_bvhs[p]->nt > 0) {
+        VTRY(free_grid_build(ctx, const_cast<visacd_bvh*>(cage_bvhs[p]), part_pairs[p]));
+        any_grid = any_grid || cage_bvhs[p]->free_lb != nullptr;
+      }
+    }
+  }
   // Layout of the per-part arrays in one buffer (256-byte aligned pieces).
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   std::vector<size_t> o_pts(n_parts), o_mask(n_parts), o_perm(n_parts), o_rows(n_parts),
@@ -902,6 +999,19 @@ int visibility_multi_impl(visacd_ctx* ctx, int32_t n_parts, const float* const* 
     P.cage_nodes = cage_bvhs[p]->nodes;
     P.cage_tris = cage_bvhs[p]->tris;
     P.cage_nt = cage_bvhs[p]->nt;
+    const visacd_bvh* cb = cage_bvhs[p];
+    if (any_grid && cb->free_lb && part_pairs[p] >= kFreeGridMinPairs) {
+      P.cage_free.lb = cb->free_lb;
+      P.cage_free.tex = cb->free_tex;
+      P.cage_free.ox = cb->fg_ox;
+      P.cage_free.oy = cb->fg_oy;
+      P.cage_free.oz = cb->fg_oz;
+      P.cage_free.inv_h = cb->fg_inv_h;
+      P.cage_free.margin = cb->fg_margin;
+      P.cage_free.nx = cb->fg_nx;
+      P.cage_free.ny = cb->fg_ny;
+      P.cage_free.nz = cb->fg_nz;
+    }
     P.bitset = bits + word_start[p];
     P.cnt = cnt;
     P.status = ctx->d_status;
@@ -923,8 +1033,17 @@ int visibility_multi_impl(visacd_ctx* ctx, int32_t n_parts, const float* const* 
   const unsigned long long* d_tiles = reinterpret_cast<const unsigned long long*>(base + o_tiles);
   const unsigned long long* d_words = reinterpret_cast<const unsigned long long*>(base + o_words);
   if (tiles) {
+    unsigned long long* pend = nullptr;
+    uint32_t* pend_done = nullptr;
+    if (any_grid) {
+      VTRY(ensure_slot(ctx, kSlotVisCleared, (size_t)tiles * 12 + 256));
+      pend = slot<unsigned long long>(ctx, kSlotVisCleared);
+      pend_done = reinterpret_cast<uint32_t*>(pend + tiles);
+      VLAUNCH(ctx, kKVisWalk, (unsigned)(ctx->sm_count * 16), kVisThreads, 0, visibility_multi_walk_kernel<8>,
+              d_desc, n_parts, d_tiles, tiles, cnt, pend, pend_done);
+    }
     VLAUNCH(ctx, kKVisibility, (unsigned)(ctx->sm_count * 8), kVisThreads, 0, (visibility_multi_kernel<8, 8>),
-            d_desc, n_parts, d_tiles, tiles, cnt, ctx->d_status);
+            d_desc, n_parts, d_tiles, tiles, cnt, ctx->d_status, pend, pend_done);
   }
   // Compaction over the concatenated bitset.
   const int64_t nw = (int64_t)words;
@@ -993,6 +1112,12 @@ int visibility_impl(visacd_ctx* ctx, const float* pts, int32_t n, const uint8_t*
   VCUDA(cudaSetDevice(ctx->device));
   const float* d_pts = pts;
   const uint8_t* d_new = is_new;
+  int64_t pairs = (int64_t)n * (n > 0 ? n - 1 : 0) / 2;
+  if (is_new && !device_ptrs) {
+    int64_t k = 0;
+    for (int32_t v = 0; v < n; ++v) k += is_new[v] != 0;
+    pairs -= ((int64_t)n - k) * ((int64_t)n - k - 1) / 2;
+  }
   if (!device_ptrs && n > 0) {
     VTRY(ensure_slot(ctx, kSlotPoints, (size_t)n * 12));
     if (is_new) VTRY(ensure_slot(ctx, kSlotMask, (size_t)n));
@@ -1005,7 +1130,7 @@ int visibility_impl(visacd_ctx* ctx, const float* pts, int32_t n, const uint8_t*
       d_new = slot<uint8_t>(ctx, kSlotMask);
     }
   }
-  return vis_device(ctx, d_pts, n, d_new, self_bvh, cage_bvh, n_edges, stats);
+  return vis_device(ctx, d_pts, n, d_new, self_bvh, cage_bvh, n_edges, stats, pairs);
 }
 
 }  // namespace vgpu
