@@ -57,7 +57,7 @@ def measured_throughput(workload_name: str, kernel: str) -> dict:
             return {"l1_pct": float(f[2]), "l2_pct": float(f[3]), "issue_active_pct": float(f[4]),
                     "achieved_occupancy_pct": float(f[5]),
                     "survey_roofline_max_l1_l2_pct": max(float(f[2]), float(f[3])),
-                    "source": "ncu --set full of this launch (profiles/visibility_kernel_blob_s5_full.md)"}
+                    "source": f"ncu --set full of this launch (profiles/{kernel}_blob_s5_full.md)"}
     return {}
 
 
@@ -198,6 +198,7 @@ def run_ours(args) -> dict:
     # Setup: one pass to get edges for the candidate planes.
     sb, cb = ctx.bvh(v, t), ctx.bvh(cv, ct)
     edges0, st0 = ctx.visibility(v, sb, cb)
+    walk_cleared, walk_reads = ctx.vis_trace_counts()
     bvh_depth = (sb.info()[1], cb.info()[1])
     # Autotune the visibility launch shape for this shape class (setup, untimed).
     tuned_variant, tuned_ms = ctx.autotune_visibility(v, sb, cb)
@@ -291,9 +292,17 @@ def run_ours(args) -> dict:
     e2e = {"value": world * n_pairs / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(bytes_in + ne_e * 8),
            "d2h_bytes_per_step": int(ne_e * 8 + N_PLANES * 8), "ms_per_step": e2e_s * 1e3}
 
-    # Rooflines. Both hot kernels are FP32-issue bound (the BVHs and edge
-    # records are L2-resident), so the denominator is this GPU's measured
-    # FP32 FMA rate (MEASURED_PEAKS.json lists HBM copy and bf16 GEMM only).
+    # Rooflines. The hot kernels work out of L1/L2 (the grid, the BVHs and
+    # the edge records are L2-resident), so the denominator of their work
+    # models is this GPU's measured FP32 FMA rate (MEASURED_PEAKS.json lists
+    # HBM copy and bf16 GEMM only); ncu's L1 / L2 throughput and issue
+    # activity of each (profiles/) say what binds them.
+    walk_ms, walk_n = ktimes.get("vis_walk", (0.0, 0))
+    walk_launch_s = walk_ms / max(walk_n, 1) / 1e3
+    # Free-space walk per launch: each grid read takes the point (3 FMA), its
+    # cell coordinates (3 sub + 3 mul) and the step (sub, mul, add): 15 FLOP.
+    walk_flop = 15.0 * walk_reads
+    walk_achieved = walk_flop / walk_launch_s / 1e12 if walk_ms else None
     vis_ms, vis_n = ktimes.get("visibility", (0.0, 0))
     sc_ms, sc_n = ktimes.get("score_planes", (0.0, 0))
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
@@ -321,16 +330,25 @@ def run_ours(args) -> dict:
         "gpu_launches": int(launches),
         "kernels_ms_per_step": {k: v[0] / args.steps for k, v in sorted(ktimes.items(), key=lambda kv: -kv[1][0])},
         "kernel_launches": {k: v[1] for k, v in ktimes.items()},
-        "roofline": {"kernel": "visibility_kernel", "bound": "fp32-issue",
-                     "achieved": vis_achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                     "frac": vis_achieved / fp32_peak if vis_achieved else None,
-                     "traffic": measured_traffic(args.workload, "visibility_kernel"),
-                     "ncu": measured_throughput(args.workload, "visibility_kernel"),
-                     "ms_per_launch": vis_ms / max(vis_n, 1),
-                     "pairs_per_s": n_pairs / vis_launch_s if vis_ms else None,
-                     "work_model": "packet node visits x 32 lanes x 2 boxes x 12 FLOP + triangle tests x 60 FLOP",
+        "roofline": {"kernel": "visibility_walk_kernel", "bound": "l1-latency",
+                     "achieved": walk_achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": walk_achieved / fp32_peak if walk_achieved else None,
+                     "traffic": measured_traffic(args.workload, "visibility_walk_kernel"),
+                     "ncu": measured_throughput(args.workload, "visibility_walk_kernel"),
+                     "ms_per_launch": walk_ms / max(walk_n, 1),
+                     "segments_cleared": int(walk_cleared), "grid_reads": int(walk_reads),
+                     "work_model": "grid reads x 15 FLOP (point, cell coordinates, step)",
                      "peak_source": "measured in-process (fma.rn.f32x2 loop); HBM peak of measured "
-                                    f"{peaks.get('hbm_gbs')} GB/s not binding (L2-resident BVHs)"},
+                                    f"{peaks.get('hbm_gbs')} GB/s not binding (L2-resident grid)"},
+        "roofline_traversal": {"kernel": "visibility_kernel", "bound": "fp32-issue",
+                               "achieved": vis_achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                               "frac": vis_achieved / fp32_peak if vis_achieved else None,
+                               "traffic": measured_traffic(args.workload, "visibility_kernel"),
+                               "ncu": measured_throughput(args.workload, "visibility_kernel"),
+                               "ms_per_launch": vis_ms / max(vis_n, 1),
+                               "pairs_per_s": n_pairs / (vis_launch_s + walk_launch_s) if vis_ms else None,
+                               "work_model": "packet node visits x 32 lanes x 2 boxes x 12 FLOP + "
+                                             "triangle tests x 60 FLOP (the pairs the walk left)"},
         "roofline_scoring": {"kernel": "score_planes_kernel", "bound": "fp32-issue",
                              "achieved": sc_achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                              "frac": sc_achieved / fp32_peak if sc_achieved else None,

@@ -27,7 +27,7 @@ struct visacd_bvh {
   float* free_lb = nullptr;
   cudaArray_t free_arr = nullptr;            // the same values as a 3D texture
   cudaTextureObject_t free_tex = 0;          // (point sampling, border 0)
-  float fg_ox = 0.f, fg_oy = 0.f, fg_oz = 0.f, fg_inv_h = 0.f, fg_margin = 0.f;
+  float fg_ox = 0.f, fg_oy = 0.f, fg_oz = 0.f, fg_h = 0.f, fg_inv_h = 0.f, fg_margin = 0.f;
   int32_t fg_nx = 0, fg_ny = 0, fg_nz = 0;
 };
 

@@ -1,24 +1,22 @@
 // Free-space grid of a cage: for every cell of a uniform grid over the cage's
-// bounding box, a lower bound lb of the distance from any point of the cell
-// (grown by delta on every side) to the cage's triangles. The visibility
-// kernel walks a segment through it (traverse.cuh, trace_free): from the
-// point at parameter t it may advance by (lb - margin) / |q - p|, because no
-// cage triangle lies within lb of that point; a segment whose whole length is
-// covered this way cannot hit the cage, which is the answer the exact test
-// gives for it. Segments it cannot cover (they cross the cage, or pass within
-// a few cells of it) go through the BVH as before, so results do not change.
+// bounding box, a lower bound B of the distance from the cell's centre to the
+// cage's triangles. The visibility kernel walks a segment through it
+// (traverse.cuh, trace_free): from a point x it may advance by
+// B - |x - centre| - margin, because no cage triangle lies within
+// B - |x - centre| of x; a segment whose whole length is covered this way
+// cannot hit the cage, which is the answer the exact test gives for it.
+// Segments it cannot cover (they cross the cage, or pass within a few cells
+// of it) go through the BVH as before, so results do not change.
 //
-// The bound of a cell is the larger of two rigorous lower bounds:
+// The bound of a centre is the larger of two rigorous lower bounds:
 //  * near: the smallest lower bound, over the triangles whose bounding box
-//    lies within R of the cell centre, of the distance from the centre to the
+//    lies within R of the centre, of the distance from the centre to the
 //    triangle (plane distance and in-plane edge half-planes, minus a rounding
 //    allowance; or the distance to the triangle's bounding box), capped at R
-//    (triangles farther than R from the centre were not visited), minus the
-//    cell's half diagonal;
+//    (triangles farther than R from the centre were not visited);
 //  * far: h x the exact Euclidean distance, in cells, from the cell to the
 //    nearest "surface" cell (one whose centre lies within a half diagonal of
-//    a triangle: every cage point is in such a cell), minus two half
-//    diagonals.
+//    a triangle: every cage point is in such a cell), minus a half diagonal.
 // All roundings that matter are directed (down for bounds).
 #include <cmath>
 
@@ -148,9 +146,10 @@ __global__ void fg_near_kernel(const float4* __restrict__ tris, int32_t nt, FgPa
     const int total = sx * sy * sz;
     for (int k = lane; k < total; k += 32) {
       const int ix = c0[0] + k % sx, iy = c0[1] + (k / sx) % sy, iz = c0[2] + k / (sx * sy);
-      const float x = g.ox + ((float)ix + 0.5f) * g.h;
-      const float y = g.oy + ((float)iy + 0.5f) * g.h;
-      const float z = g.oz + ((float)iz + 0.5f) * g.h;
+      // The centre exactly as the walk computes it.
+      const float x = __fadd_rn(g.ox, __fmul_rn((float)ix + 0.5f, g.h));
+      const float y = __fadd_rn(g.oy, __fmul_rn((float)iy + 0.5f, g.h));
+      const float z = __fadd_rn(g.oz, __fmul_rn((float)iz + 0.5f, g.h));
       // Cells whose centre lies farther than R from the triangle's box keep
       // their value: the cap at R already bounds them.
       const float gx = fmaxf(0.f, fmaxf(lo[0] + g.R - x, x - (hi[0] - g.R)));
@@ -280,16 +279,16 @@ __global__ void __launch_bounds__(kEdtThreads) fg_edt_yz_kernel(FgParams g, int*
   }
 }
 
-// lb = max(min(near, R) - hd, h sqrt(d2) - 2 hd), rounded down; hd is the
-// half diagonal of a cell grown by delta, rounded up.
+// The bound of a cell's centre: B = max(min(near, R), h sqrt(d2) - hd),
+// rounded down (hd: the half diagonal of a cell grown by delta, rounded up).
+// A walk at point x in the cell takes B - |x - centre| (traverse.cuh).
 __global__ void fg_final_kernel(const unsigned* __restrict__ near, const int* __restrict__ d2, int64_t cells,
                                 float R, float h, float hd, float* __restrict__ lb) {
   for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < cells;
        c += (int64_t)gridDim.x * blockDim.x) {
-    const float nv = fminf(__uint_as_float(near[c]), R);
-    const float a = __fsub_rd(nv, hd);
+    const float a = fminf(__uint_as_float(near[c]), R);
     const int e = d2[c];
-    const float b = e >= kFgInf ? 3.0e38f : __fsub_rd(__fmul_rd(__fsqrt_rd((float)e), h), 2.f * hd);
+    const float b = e >= kFgInf ? 3.0e38f : __fsub_rd(__fmul_rd(__fsqrt_rd((float)e), h), hd);
     lb[c] = fmaxf(a, b);
   }
 }
@@ -424,6 +423,7 @@ int free_grid_build(visacd_ctx* ctx, visacd_bvh* b, int64_t pairs) {
   b->fg_ox = g.ox;
   b->fg_oy = g.oy;
   b->fg_oz = g.oz;
+  b->fg_h = g.h;
   b->fg_inv_h = 1.f / g.h;
   b->fg_margin = delta;
   b->fg_nx = g.nx;

@@ -30,19 +30,37 @@ struct VisCounters {
 struct FreeGridView {
   const float* lb;          // null: no grid
   cudaTextureObject_t tex;  // the same bounds as a 3D texture (border 0)
-  float ox, oy, oz, inv_h, margin;
+  float ox, oy, oz, h, inv_h, margin;
   int32_t nx, ny, nz;
 };
+
+// Lower bound of the distance from (x, y, z) to the cage: the bound B of the
+// centre of the cell the point falls in, less the point's distance to that
+// centre (the centre as the grid build computed it). Outside the grid the
+// texture's border gives B = 0, so the result is negative.
+__device__ __forceinline__ float free_bound(const FreeGridView& g, float x, float y, float z) {
+  const float u = (x - g.ox) * g.inv_h, v = (y - g.oy) * g.inv_h, w = (z - g.oz) * g.inv_h;
+  const float B = tex3D<float>(g.tex, u, v, w);
+  const float cx = __fadd_rn(g.ox, __fmul_rn(floorf(u) + 0.5f, g.h));
+  const float cy = __fadd_rn(g.oy, __fmul_rn(floorf(v) + 0.5f, g.h));
+  const float cz = __fadd_rn(g.oz, __fmul_rn(floorf(w) + 0.5f, g.h));
+  const float dx = x - cx, dy = y - cy, dz = z - cz;
+  // |x - centre| from the hardware reciprocal square root (2 ulp) rounded
+  // up by a relative 1e-6.
+  const float q = dx * dx + dy * dy + dz * dz;
+  return B - q * rsqrtf(q + 1e-30f) * 1.000001f;
+}
 constexpr int kTraceSteps = 32;  // rounds (two grid reads each) before a segment goes to the BVH
 
 // Free-space walk of the segment p -> q (d = q - p rounded, len its FP32
 // length) through a cage's grid, from both ends at once (two independent
-// chains of dependent reads). From the point at t the walk may advance by
-// (lb - margin) / |q - p| in either direction: lb bounds the distance from
-// every point of the point's cell, grown by the margin, to the cage (the
-// margin covers the FP32 rounding of the point and of its cell index), so no
-// cage triangle lies within the margin of the part covered. True when the two
-// covered parts [0, t] and [s, 1] meet: the segment cannot hit the cage.
+// chains of dependent reads). From a point x on the segment the walk may
+// advance by (lb - margin) / |q - p| in either direction, lb = free_bound(x):
+// no cage triangle lies within lb of x. The margin covers the FP32 rounding of
+// x against the true point of the segment, of the cell centre and of the
+// distance to it, a cell read on either side of a face the point lies on, and
+// leaves every covered point at least that far from the cage. True when the
+// two covered parts [0, t] and [s, 1] meet: the segment cannot hit the cage.
 // Roundings are directed so that the parts covered are never overstated.
 // `steps` counts the grid reads.
 __device__ __forceinline__ bool trace_free(const FreeGridView& g, float px, float py, float pz, float dx,
@@ -51,11 +69,8 @@ __device__ __forceinline__ bool trace_free(const FreeGridView& g, float px, floa
   const float inv_len = __frcp_rd(__fmul_ru(len, 1.000001f));
   float t = 0.f, s = 1.f;
   for (int k = 0; k < kTraceSteps; ++k) {
-    const float x0 = fmaf(t, dx, px), y0 = fmaf(t, dy, py), z0 = fmaf(t, dz, pz);
-    const float x1 = fmaf(s, dx, px), y1 = fmaf(s, dy, py), z1 = fmaf(s, dz, pz);
-    // Cell coordinates; point sampling reads cell floor(u), the border 0.
-    const float lb0 = tex3D<float>(g.tex, (x0 - g.ox) * g.inv_h, (y0 - g.oy) * g.inv_h, (z0 - g.oz) * g.inv_h);
-    const float lb1 = tex3D<float>(g.tex, (x1 - g.ox) * g.inv_h, (y1 - g.oy) * g.inv_h, (z1 - g.oz) * g.inv_h);
+    const float lb0 = free_bound(g, fmaf(t, dx, px), fmaf(t, dy, py), fmaf(t, dz, pz));
+    const float lb1 = free_bound(g, fmaf(s, dx, px), fmaf(s, dy, py), fmaf(s, dz, pz));
     steps += 2;
     if (!(lb0 > g.margin) || !(lb1 > g.margin)) return false;
     t = __fadd_rd(t, __fmul_rd(__fsub_rd(lb0, g.margin), inv_len));
