@@ -30,47 +30,49 @@ struct VisCounters {
 struct FreeGridView {
   const float* lb;          // null: no grid
   cudaTextureObject_t tex;  // the same bounds as a 3D texture (border 0)
-  float ox, oy, oz, h, inv_h, margin;
+  float ox, oy, oz, h_up, inv_h, margin;  // h_up: the cell size times (1 + 1e-6)
   int32_t nx, ny, nz;
 };
 
-// Lower bound of the distance from (x, y, z) to the cage: the bound B of the
-// centre of the cell the point falls in, less the point's distance to that
-// centre (the centre as the grid build computed it). Outside the grid the
-// texture's border gives B = 0, so the result is negative.
-__device__ __forceinline__ float free_bound(const FreeGridView& g, float x, float y, float z) {
-  const float u = (x - g.ox) * g.inv_h, v = (y - g.oy) * g.inv_h, w = (z - g.oz) * g.inv_h;
+// Lower bound of the distance to the cage from the point at cell coordinates
+// (u, v, w) (x = o + u h): the bound B of the centre of the cell the point
+// falls in, less h x the point's distance to that centre in cells. Outside
+// the grid the texture's border gives B = 0, so the result is negative.
+__device__ __forceinline__ float free_bound(const FreeGridView& g, float u, float v, float w) {
   const float B = tex3D<float>(g.tex, u, v, w);
-  const float cx = __fadd_rn(g.ox, __fmul_rn(floorf(u) + 0.5f, g.h));
-  const float cy = __fadd_rn(g.oy, __fmul_rn(floorf(v) + 0.5f, g.h));
-  const float cz = __fadd_rn(g.oz, __fmul_rn(floorf(w) + 0.5f, g.h));
-  const float dx = x - cx, dy = y - cy, dz = z - cz;
-  // |x - centre| from the hardware reciprocal square root (2 ulp) rounded
-  // up by a relative 1e-6.
-  const float q = dx * dx + dy * dy + dz * dz;
-  return B - q * rsqrtf(q + 1e-30f) * 1.000001f;
+  // u - floor(u) is exact; so is subtracting 0.5 from it.
+  const float rx = (u - floorf(u)) - 0.5f, ry = (v - floorf(v)) - 0.5f, rz = (w - floorf(w)) - 0.5f;
+  // |r| from the hardware reciprocal square root (2 ulp), rounded up through
+  // the factor folded into h_up = h (1 + 1e-6).
+  const float q = rx * rx + ry * ry + rz * rz;
+  return B - q * rsqrtf(q + 1e-30f) * g.h_up;
 }
+
 constexpr int kTraceSteps = 32;  // rounds (two grid reads each) before a segment goes to the BVH
 
 // Free-space walk of the segment p -> q (d = q - p rounded, len its FP32
 // length) through a cage's grid, from both ends at once (two independent
-// chains of dependent reads). From a point x on the segment the walk may
-// advance by (lb - margin) / |q - p| in either direction, lb = free_bound(x):
-// no cage triangle lies within lb of x. The margin covers the FP32 rounding of
-// x against the true point of the segment, of the cell centre and of the
-// distance to it, a cell read on either side of a face the point lies on, and
-// leaves every covered point at least that far from the cage. True when the
-// two covered parts [0, t] and [s, 1] meet: the segment cannot hit the cage.
-// Roundings are directed so that the parts covered are never overstated.
-// `steps` counts the grid reads.
+// chains of dependent reads). The point at t has cell coordinates
+// u0 + t du with u0 = (p - o) / h and du = d / h; from it the walk may
+// advance by (lb - margin) / |q - p| in either direction, lb = free_bound:
+// no cage triangle lies within lb of the point. The margin covers the FP32
+// rounding of those coordinates against the true point of the segment (below
+// 2e-4 cells for grids of at most 256 cells a side), of the cell centres, a
+// cell read on either side of a face the point lies on, and leaves every
+// covered point at least that far from the cage. True when the two covered
+// parts [0, t] and [s, 1] meet: the segment cannot hit the cage. Roundings
+// are directed so that the parts covered are never overstated. `steps`
+// counts the grid reads.
 __device__ __forceinline__ bool trace_free(const FreeGridView& g, float px, float py, float pz, float dx,
                                            float dy, float dz, float len, unsigned long long& steps) {
   // 1 / |q - p| rounded down; |q - p| <= len (1 + 17u).
   const float inv_len = __frcp_rd(__fmul_ru(len, 1.000001f));
+  const float u0 = (px - g.ox) * g.inv_h, v0 = (py - g.oy) * g.inv_h, w0 = (pz - g.oz) * g.inv_h;
+  const float du = dx * g.inv_h, dv = dy * g.inv_h, dw = dz * g.inv_h;
   float t = 0.f, s = 1.f;
   for (int k = 0; k < kTraceSteps; ++k) {
-    const float lb0 = free_bound(g, fmaf(t, dx, px), fmaf(t, dy, py), fmaf(t, dz, pz));
-    const float lb1 = free_bound(g, fmaf(s, dx, px), fmaf(s, dy, py), fmaf(s, dz, pz));
+    const float lb0 = free_bound(g, fmaf(t, du, u0), fmaf(t, dv, v0), fmaf(t, dw, w0));
+    const float lb1 = free_bound(g, fmaf(s, du, u0), fmaf(s, dv, v0), fmaf(s, dw, w0));
     steps += 2;
     if (!(lb0 > g.margin) || !(lb1 > g.margin)) return false;
     t = __fadd_rd(t, __fmul_rd(__fsub_rd(lb0, g.margin), inv_len));

@@ -711,7 +711,7 @@ static int vis_device(visacd_ctx* ctx, const float* d_pts, int32_t n, const uint
       P.cage_free.ox = cb->fg_ox;
       P.cage_free.oy = cb->fg_oy;
       P.cage_free.oz = cb->fg_oz;
-      P.cage_free.h = cb->fg_h;
+      P.cage_free.h_up = cb->fg_h * 1.000001f;
       P.cage_free.inv_h = cb->fg_inv_h;
       P.cage_free.margin = cb->fg_margin;
       P.cage_free.nx = cb->fg_nx;
@@ -1007,7 +1007,7 @@ int visibility_multi_impl(visacd_ctx* ctx, int32_t n_parts, const float* const* 
       P.cage_free.ox = cb->fg_ox;
       P.cage_free.oy = cb->fg_oy;
       P.cage_free.oz = cb->fg_oz;
-      P.cage_free.h = cb->fg_h;
+      P.cage_free.h_up = cb->fg_h * 1.000001f;
       P.cage_free.inv_h = cb->fg_inv_h;
       P.cage_free.margin = cb->fg_margin;
       P.cage_free.nx = cb->fg_nx;
