@@ -205,6 +205,8 @@ def run_ours(args) -> dict:
     sb.close()
     cb.close()
     planes = bisector_planes(v, edges0, N_PLANES, seed=1)
+    # Autotune the scoring kernel's planes per thread for this shape class.
+    score_k, score_k_ms = ctx.autotune_scoring(planes, v, edges0)
     d_planes = torch.from_numpy(planes).to(dev)
     d_scores = torch.empty(N_PLANES, dtype=torch.float64, device=dev)
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
@@ -324,6 +326,8 @@ def run_ours(args) -> dict:
                    "name": args.workload, "bvh_depth": bvh_depth,
                    "visibility_counters": st0,
                    "vis_variant": tuned_variant, "vis_variant_ms": [round(x, 3) for x in tuned_ms],
+                   "score_planes_per_thread": score_k,
+                   "score_k_ms": {str(k): round(x, 4) for k, x in zip((1, 2, 4, 8), score_k_ms)},
                    "l2": "flushed before each timed step (256 MB write)",
                    "parallelism": f"replicas x{world}"},
         "e2e": e2e,

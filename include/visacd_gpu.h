@@ -222,6 +222,17 @@ int visacd_compute_intersection_matrix(visacd_ctx* ctx, const float* verts, int3
 int visacd_score_planes(visacd_ctx* ctx, const float* planes, int32_t P, const float* points,
                         int32_t N, const uint32_t* edges, int64_t E, int device_ptrs,
                         double* scores, visacd_score_stats* stats);
+/* Planes per scoring thread (1, 2, 4 or 8; the scores do not depend on it):
+   visacd_ctx_set_score_k forces one (0: the autotuned choice of the call's
+   shape class if one was measured, else a rule on P). visacd_autotune_scoring
+   times each on this exact call (twice, CUDA events on the context stream),
+   caches the fastest for the call's shape class (log2 buckets of P and E) in
+   the context and reports it; ms_per_k (optional) gets 4 entries. Resets the
+   context's kernel timers. */
+int visacd_ctx_set_score_k(visacd_ctx* ctx, int k);
+int visacd_autotune_scoring(visacd_ctx* ctx, const float* planes, int32_t P, const float* points,
+                            int32_t N, const uint32_t* edges, int64_t E, int device_ptrs, int* best_k,
+                            double* ms_per_k);
 
 /* ---- candidate planes and the split search -------------------------------- */
 /* Candidate split planes from drawn visibility edges. Replaces the plane

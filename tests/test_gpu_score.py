@@ -132,3 +132,30 @@ def test_precision_sweep_sizes(ctx, orc, E):
     q_gpu = np.round(np.ldexp(s_gpu[sub], -qexp)).astype(np.uint64)
     np.testing.assert_array_equal(q_gpu, q)
     assert np.max(np.abs(s_gpu[sub] - s64) / s64) <= REL_TOL
+
+
+def test_planes_per_thread_change_no_score(ctx):
+    """Scores and the argmax are the same whatever planes each thread takes
+    (forced 1, 2, 4, 8), and the autotuner picks one of them."""
+    rng = np.random.default_rng(21)
+    pts = rng.normal(size=(3000, 3)).astype(np.float32)
+    e = rng.integers(0, 3000, size=(20000, 2)).astype(np.uint32)
+    nrm = rng.normal(size=(1500, 3))
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    planes = np.concatenate([nrm, rng.uniform(-0.5, 0.5, (1500, 1))], 1).astype(np.float32)
+    planes[:20, 3] = -(planes[:20, :3] @ pts[e[:20, 0]].T).diagonal()  # planes through edge endpoints
+    ref = None
+    try:
+        for k in (1, 2, 4, 8):
+            ctx.set_score_k(k)
+            s, st = ctx.score_planes(planes, pts, e)
+            if ref is None:
+                ref = (s, st["argmax"])
+            np.testing.assert_array_equal(s, ref[0])
+            assert st["argmax"] == ref[1]
+    finally:
+        ctx.set_score_k(0)
+    best, ms = ctx.autotune_scoring(planes, pts, e)
+    assert best in (1, 2, 4, 8) and len(ms) == 4 and all(m > 0 for m in ms)
+    s, _ = ctx.score_planes(planes, pts, e)
+    np.testing.assert_array_equal(s, ref[0])

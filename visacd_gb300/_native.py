@@ -34,6 +34,7 @@ EXPORTED = [
     "visacd_set_blocking_sync", "visacd_lp_set_tcgen05", "visacd_ctx_set_blocking_wait",
     "visacd_candidate_planes", "visacd_split_search", "visacd_visibility_batch",
     "visacd_learned_split_search", "visacd_ctx_set_vis_trace", "visacd_ctx_vis_trace_counts",
+    "visacd_ctx_set_score_k", "visacd_autotune_scoring",
 ]
 
 LP_POINTS = 2048
@@ -122,6 +123,9 @@ def load() -> C.CDLL:
                                             C.POINTER(i32)]
     lib.visacd_split_search.argtypes = [P, P, i32, P, i64, P, i32, i32, P, i32, C.c_double, P,
                                         C.POINTER(SplitInfo)]
+    lib.visacd_ctx_set_score_k.argtypes = [P, C.c_int]
+    lib.visacd_autotune_scoring.argtypes = [P, P, i32, P, i32, P, i64, C.c_int, C.POINTER(C.c_int),
+                                            C.POINTER(C.c_double)]
     lib.visacd_ctx_set_vis_trace.argtypes = [P, C.c_int]
     lib.visacd_ctx_vis_trace_counts.argtypes = [P, C.POINTER(i64), C.POINTER(i64)]
     lib.visacd_learned_split_search.argtypes = [P, P, i32, P, i64, P, C.c_float, C.c_double, i32, P, i32,
@@ -282,6 +286,22 @@ class Context:
             out.append(flat[at:at + ne[k]])
             at += int(ne[k])
         return out, st.as_dict()
+
+    def set_score_k(self, k: int) -> None:
+        """Force planes per scoring thread (1, 2, 4, 8; 0 = tuned / default)."""
+        _check(lib().visacd_ctx_set_score_k(self._h, int(k)), "visacd_ctx_set_score_k")
+
+    def autotune_scoring(self, planes, points, edges):
+        """Time 1, 2, 4 and 8 planes per thread on this call, cache the fastest
+        for its shape class: (best, ms per choice)."""
+        pl = _f32(planes, 4)
+        pt = _f32(points, 3)
+        ed = _u32(edges, 2)
+        best = C.c_int()
+        ms = (C.c_double * 4)()
+        _check(lib().visacd_autotune_scoring(self._h, _ptr(pl), len(pl), _ptr(pt), len(pt), _ptr(ed), len(ed),
+                                             0, C.byref(best), ms), "visacd_autotune_scoring")
+        return best.value, list(ms)
 
     def set_vis_trace(self, on: bool) -> None:
         """Free-space walks before the cage BVH in large visibility calls."""

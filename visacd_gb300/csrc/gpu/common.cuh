@@ -141,6 +141,8 @@ struct visacd_ctx {
   bool timing = false;
   int vis_variant_override = -1;                  // forced launch shape, -1 = tuned/default
   std::unordered_map<uint32_t, int> vis_tuned;    // shape class -> autotuned variant
+  int score_k_override = 0;                       // forced planes per scoring thread, 0 = tuned/default
+  std::unordered_map<uint32_t, int> score_tuned;  // scoring shape class -> autotuned planes per thread
   visacd_clip_result clip_out{};                  // last clip result (device-resident)
   std::vector<visacd_bvh*> bvhs;                  // live BVHs built on this context
   std::vector<visacd_lp*> lps;                    // live proposers made on this context

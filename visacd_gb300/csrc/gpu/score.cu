@@ -22,6 +22,9 @@
 //    score_recheck re-decides its band pairs in FP64 — the same FP64
 //    evaluation the oracle uses — so classification equals the FP64 oracle's.
 //  * Sums are integers (order independent), so scores are deterministic.
+#include <cstring>
+#include <vector>
+
 #include "score_device.cuh"
 
 namespace vgpu {
@@ -225,6 +228,23 @@ struct ScoreCounters {
   int argmax[2];                     // argmax, qexp
 };
 
+// Shape class of a scoring call: log2 buckets of P and E.
+static uint32_t score_shape_class(int32_t P, int64_t E) {
+  auto lg = [](int64_t x) { int r = 0; while (x > 1) { x >>= 1; ++r; } return r; };
+  return (uint32_t)lg(P) | ((uint32_t)lg(E) << 8);
+}
+
+static int planes_per_thread(int32_t P);
+
+// Planes per thread of a call: forced, autotuned for its shape class, or the
+// default rule.
+static int choose_score_k(visacd_ctx* ctx, int32_t P, int64_t E) {
+  if (ctx->score_k_override) return ctx->score_k_override;
+  auto it = ctx->score_tuned.find(score_shape_class(P, E));
+  if (it != ctx->score_tuned.end()) return it->second;
+  return planes_per_thread(P);
+}
+
 static int planes_per_thread(int32_t P) {
   if (P > 4 * kScoreThreads * 152 / 2) return 8;
   if (P > 2 * kScoreThreads * 4) return 4;
@@ -284,7 +304,7 @@ static int score_device(visacd_ctx* ctx, const float* d_planes, int32_t P, const
     VTRY(ensure_slot(ctx, kSlotRecheck, (size_t)rcap * sizeof(uint2)));
     uint2* rq = slot<uint2>(ctx, kSlotRecheck);
     const float4* pl = reinterpret_cast<const float4*>(d_planes);
-    int K = planes_per_thread(P);
+    int K = choose_score_k(ctx, P, E);
     switch (K) {
       case 8: VTRY(launch_score<8>(ctx, pl, P, recs, E, cnt->stats, sq, rq, &cnt->recheck_count, rcap, &cnt->status)); break;
       case 4: VTRY(launch_score<4>(ctx, pl, P, recs, E, cnt->stats, sq, rq, &cnt->recheck_count, rcap, &cnt->status)); break;
@@ -400,6 +420,65 @@ extern "C" int visacd_score_planes(visacd_ctx* ctx, const float* planes, int32_t
                                    visacd_score_stats* stats) {
   return score_planes_impl(ctx, planes, P, points, N, edges, E, device_ptrs, scores, nullptr,
                            stats);
+}
+
+extern "C" int visacd_ctx_set_score_k(visacd_ctx* ctx, int k) {
+  VCHECK(ctx, VISACD_ERR_INVALID_ARG, "set_score_k: null context");
+  VCHECK(k == 0 || k == 1 || k == 2 || k == 4 || k == 8, VISACD_ERR_INVALID_ARG,
+         "set_score_k: %d is not 0, 1, 2, 4 or 8", k);
+  ctx->score_k_override = k;
+  return VISACD_OK;
+}
+
+extern "C" int visacd_autotune_scoring(visacd_ctx* ctx, const float* planes, int32_t P, const float* points,
+                                       int32_t N, const uint32_t* edges, int64_t E, int device_ptrs,
+                                       int* best_k, double* ms_per_k) {
+  VCHECK(ctx, VISACD_ERR_INVALID_ARG, "autotune_scoring: null context");
+  const int saved_override = ctx->score_k_override;
+  const bool saved_timing = ctx->timing;
+  static const int kKs[4] = {1, 2, 4, 8};
+  int best = 0;
+  double best_ms = 1e300;
+  int rc = VISACD_OK;
+  std::vector<double> scores((size_t)(P > 0 ? P : 1));
+  for (int v = 0; v < 4 && rc == VISACD_OK; ++v) {
+    ctx->score_k_override = kKs[v];
+    double ms = 0.0;
+    for (int rep = 0; rep < 2 && rc == VISACD_OK; ++rep) {
+      ctx->timing = true;
+      rc = visacd_ctx_reset_times(ctx);
+      // Device pointers get a device score buffer (the context's), host
+      // pointers a host one.
+      double* out = scores.data();
+      if (rc == VISACD_OK && device_ptrs) {
+        rc = ensure_slot(ctx, kSlotScores, (size_t)(P > 0 ? P : 1) * 8);
+        out = slot<double>(ctx, kSlotScores);
+      }
+      if (rc == VISACD_OK)
+        rc = score_planes_impl(ctx, planes, P, points, N, edges, E, device_ptrs, out, nullptr, nullptr);
+      const char* names[64];
+      double t[64];
+      int64_t cnt[64];
+      int nk = 0;
+      if (rc == VISACD_OK) rc = visacd_ctx_kernel_times(ctx, names, t, cnt, 64, &nk);
+      ms = 0.0;
+      for (int k = 0; k < nk && k < 64; ++k)
+        if (strcmp(names[k], kernel_name(kKScore)) == 0 || strcmp(names[k], kernel_name(kKScoreRecheck)) == 0)
+          ms += t[k];
+    }
+    if (ms_per_k) ms_per_k[v] = ms;
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = kKs[v];
+    }
+  }
+  ctx->score_k_override = saved_override;
+  ctx->timing = saved_timing;
+  visacd_ctx_reset_times(ctx);
+  if (rc != VISACD_OK) return rc;
+  ctx->score_tuned[score_shape_class(P, E)] = best;
+  if (best_k) *best_k = best;
+  return VISACD_OK;
 }
 
 // ---------------------------------------------------------------------------
