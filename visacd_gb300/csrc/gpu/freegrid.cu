@@ -18,6 +18,7 @@
 //    nearest "surface" cell (one whose centre lies within a half diagonal of
 //    a triangle: every cage point is in such a cell), minus a half diagonal.
 // All roundings that matter are directed (down for bounds).
+#include <atomic>
 #include <cmath>
 
 #include "bvh.cuh"
@@ -371,11 +372,13 @@ int free_grid_build(visacd_ctx* ctx, visacd_bvh* b, int64_t pairs) {
   VLAUNCH(ctx, kKGridEdt, grid_for((int64_t)g.ny * g.nz * 32, 256, 16LL * ctx->sm_count), 256, 0,
           fg_edt_x_kernel, near, g, hd, d2);
   const int edt_smem = kFgMaxDim * kEdtThreads * 4;
-  static bool edt_configured = false;
-  if (!edt_configured) {
+  // The shared-memory opt-in is per device.
+  static std::atomic<bool> edt_configured[64];
+  const bool known = ctx->device >= 0 && ctx->device < 64;
+  if (!known || !edt_configured[ctx->device].load()) {
     VCUDA(cudaFuncSetAttribute(fg_edt_yz_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, edt_smem));
     VCUDA(cudaFuncSetAttribute(fg_edt_yz_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, edt_smem));
-    edt_configured = true;
+    if (known) edt_configured[ctx->device].store(true);
   }
   VLAUNCH(ctx, kKGridEdt, grid_for((int64_t)g.nx * g.nz, kEdtThreads, 8LL * ctx->sm_count), kEdtThreads,
           edt_smem, fg_edt_yz_kernel<1>, g, d2);
