@@ -287,3 +287,45 @@ def test_visibility_batch_equals_per_part_calls(ctx, orc):
     gb = np.zeros(len(bits), bool)
     gb[k] = True
     assert not np.any((gb != (bits & 1).astype(bool)) & ~(bits & 2).astype(bool))
+
+
+@pytest.mark.parametrize("case", ["far_translated", "cage_inside_part", "degenerate_cage", "single_far_triangle"])
+def test_free_space_walk_edge_cases(ctx, case):
+    """Cages the free-space grid cannot serve, or serves oddly, still give the
+    same edges as the traversal alone: coordinates far from the origin (the
+    grid is refused: its margin would not cover the rounding), a cage smaller
+    than the part (walks start outside the grid), degenerate cage triangles
+    (their distance bound falls back to the triangle's box), and a cage of one
+    far triangle (a tiny grid the segments never enter)."""
+    v, t = mg.displaced_blob(4, seed=9)
+    v = np.concatenate([v, v * 0.98])  # 5124 vertices: 13.1M pairs, above the walk's 2^22
+    t = np.concatenate([t, t[:, ::-1] + len(v) // 2])
+    cv, ct = mg.offset_cage(v[: len(v) // 2], t[: len(t) // 2], 0.03)
+    if case == "far_translated":
+        v = v + 1.0e5
+        cv = cv + 1.0e5
+    elif case == "cage_inside_part":
+        cv = cv * 0.5
+    elif case == "degenerate_cage":
+        ct = ct.copy()
+        ct[::3, 1] = ct[::3, 0]  # every third triangle collapsed to an edge
+    else:
+        cv = np.array([[10.0, 10.0, 10.0], [10.1, 10.0, 10.0], [10.0, 10.1, 10.0]])
+        ct = np.array([[0, 1, 2]])
+    sb, cb = ctx.bvh(v, t), ctx.bvh(cv, ct)
+    try:
+        ctx.set_vis_trace(False)
+        e0, s0 = ctx.visibility(v, sb, cb)
+        ctx.set_vis_trace(True)
+        e1, s1 = ctx.visibility(v, sb, cb)
+    finally:
+        ctx.set_vis_trace(True)
+    cleared, reads = ctx.vis_trace_counts()
+    np.testing.assert_array_equal(e0, e1)
+    for k in ("pairs_tested", "n_edges", "self_hits", "cage_hits", "degenerate"):
+        assert s0[k] == s1[k], k
+    if case == "far_translated":
+        assert cleared == 0 and reads == 0  # no grid
+    if case == "degenerate_cage":
+        assert cleared > 0.5 * s1["pairs_tested"]
+    print(f"{case}: {s1['pairs_tested']} pairs, {len(e1)} edges, {cleared} cleared, {reads} grid reads")
