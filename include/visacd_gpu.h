@@ -32,6 +32,11 @@
  *   visacd_learned_split_search ..... the same split search with the learned
  *                                     proposer (no reference counterpart) in
  *                                     place of most of the candidate draw
+ *   visacd_convex_hulls ............. Mesh::compute_ch for a batch of parts,
+ *                                     lib/src/core.cpp:59-111 (qhull replaced
+ *                                     by this project's QuickHull)
+ *   visacd_hull_distances ........... mesh_dist of multimerge_ch,
+ *                                     lib/src/cost.cpp:125-159
  */
 #ifndef VISACD_GPU_H
 #define VISACD_GPU_H
@@ -381,6 +386,23 @@ int visacd_sdf_remesh(visacd_ctx* ctx, const double* verts, int32_t nv, const in
                       int32_t nt, double scale, double level, int32_t* out_nv, int32_t* out_nt);
 /* Copies the last remesh result: verts out_nv x 3 float64, tris out_nt x 3 int32. */
 int visacd_sdf_fetch(visacd_ctx* ctx, double* verts, int32_t* tris);
+
+/* ---- convex hulls ---------------------------------------------------------- */
+/* Convex hulls of many point sets in one launch: Mesh::compute_ch
+   (lib/src/core.cpp:59-111) for every part of a batch, this project's
+   QuickHull standing in for qhull "Qt Pp". Part k owns the points
+   [offsets[k], offsets[k+1]) of points (float64 xyz, host, finite, at most
+   2^22 a part). Its hull triangles (indices into its own points, every input
+   point stays a vertex as with qhull) go to tris + 6 * offsets[k] (host; tris
+   holds 6 * offsets[nparts] int32, room for 2 triangles a point) and their
+   number to counts[k]; with fix_normals every triangle faces away from the
+   point centroid (lib/src/core.cpp:33-57). The triangles, and their order,
+   equal the host QuickHull's; coplanar input gives the two-sided fan of its 2D
+   hull, and fewer than 3 points or collinear input no triangle. One warp per
+   part; a part that outgrows its working room (a multiple of its point count)
+   runs again with four times the room. Synchronizes. */
+int visacd_convex_hulls(visacd_ctx* ctx, const double* points, const int64_t* offsets, int32_t nparts,
+                        int32_t fix_normals, int32_t* tris, int32_t* counts);
 
 /* ---- hull merging ---------------------------------------------------------- */
 /* Exact minimum vertex-to-vertex distance between pairs of hulls: the

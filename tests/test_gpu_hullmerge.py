@@ -46,7 +46,13 @@ def test_hull_distances_equal_host(V, ctx):
             assert dc == d or dc == np.finfo(np.float64).max
 
 
-def test_merging_same_with_gpu_distances(V):
+@pytest.mark.parametrize("hooks", [{"host_merge": True, "host_hull": True},  # merge distances and union hulls on host
+                                   {"host_merge": True, "host_hull": False},  # union hulls on the GPU
+                                   {"host_merge": False, "host_hull": True}])  # distances on the GPU
+def test_merging_same_with_gpu_distances_and_hulls(V, hooks):
+    """process() with hull merging: the GPU hull-pair distances and the GPU
+    union hulls (visacd_convex_hulls, batched per cost pass) give the same
+    merges, parts and concavity as the host ones."""
     from visacd_gb300 import meshgen as mg
     v, t = mg.torus(nu=48, nv=24, seed=3)
     m = V.Mesh()
@@ -55,14 +61,15 @@ def test_merging_same_with_gpu_distances(V):
     V.config.use_merging = True
     out = []
     try:
-        for gm in (False, True):
-            V._checker_hooks(host_merge=not gm)
+        for h in (hooks, {"host_merge": False, "host_hull": False}):
+            V._checker_hooks(**h)
             V.set_seed(11)
             out.append(V.process(m, 0.05, 12))
     finally:
         V.config.use_merging = False
-        V._checker_hooks(host_merge=False)
+        V._checker_hooks(host_merge=False, host_hull=False)
     a, b = out
     assert a.num_parts == b.num_parts and a.concavity == b.concavity
     for pa, pb in zip(a.parts, b.parts):
         np.testing.assert_array_equal(np.array(pa.vertices), np.array(pb.vertices))
+        np.testing.assert_array_equal(np.array(pa.triangles), np.array(pb.triangles))

@@ -14,8 +14,8 @@ from visacd_gb300 import build, meshgen as mg
 def V():
     build.build_host()
     from visacd_gb300 import visacd
-    # host Hausdorff and remesh (test hooks): these tests run without a GPU
-    visacd._checker_hooks(host_concavity=True, host_remesh=True)
+    # host Hausdorff, remesh and merge hulls (test hooks): these tests run without a GPU
+    visacd._checker_hooks(host_concavity=True, host_remesh=True, host_hull=True)
     return visacd
 
 

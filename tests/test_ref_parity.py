@@ -17,7 +17,7 @@ def V():
     build.build_host()
     from visacd_gb300 import visacd
     # host Hausdorff and remesh (test hooks): these tests run without a GPU
-    visacd._checker_hooks(host_concavity=True, host_remesh=True)
+    visacd._checker_hooks(host_concavity=True, host_remesh=True, host_hull=True)
     return visacd
 
 

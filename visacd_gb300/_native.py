@@ -34,7 +34,7 @@ EXPORTED = [
     "visacd_set_blocking_sync", "visacd_lp_set_tcgen05", "visacd_ctx_set_blocking_wait",
     "visacd_candidate_planes", "visacd_split_search", "visacd_visibility_batch",
     "visacd_learned_split_search", "visacd_ctx_set_vis_trace", "visacd_ctx_vis_trace_counts",
-    "visacd_ctx_set_score_k", "visacd_autotune_scoring",
+    "visacd_ctx_set_score_k", "visacd_autotune_scoring", "visacd_convex_hulls",
 ]
 
 LP_POINTS = 2048
@@ -150,6 +150,7 @@ def load() -> C.CDLL:
     lib.visacd_sdf_remesh.argtypes = [P, P, i32, P, i32, C.c_double, C.c_double, C.POINTER(i32), C.POINTER(i32)]
     lib.visacd_sdf_fetch.argtypes = [P, P, P]
     lib.visacd_hull_distances.argtypes = [P, P, P, i32, P, i64, C.c_double, P]
+    lib.visacd_convex_hulls.argtypes = [P, P, P, i32, i32, P, P]
     lib.visacd_segment_triangle_tests.argtypes = [P, P, P, i64, P, C.POINTER(i64)]
     lib.visacd_set_blocking_sync.argtypes = [C.c_int, C.c_int]
     lib.visacd_lp_param_count.argtypes = []
@@ -440,6 +441,20 @@ class Context:
         _check(lib().visacd_segment_triangle_tests(self._h, _ptr(sg), _ptr(tr), len(sg), _ptr(out), C.byref(n64)),
                "visacd_segment_triangle_tests")
         return out.astype(bool), n64.value
+
+    # ---- convex hulls ------------------------------------------------------
+    def convex_hulls(self, point_sets, fix_normals: bool = True):
+        """Hull triangles (k x 3 int32, indices into its own points) of every
+        point array in point_sets, in one launch."""
+        vs = [np.ascontiguousarray(np.asarray(p, dtype=np.float64)).reshape(-1, 3) for p in point_sets]
+        off = np.zeros(len(vs) + 1, dtype=np.int64)
+        off[1:] = np.cumsum([len(v) for v in vs])
+        allv = np.ascontiguousarray(np.concatenate(vs) if vs else np.zeros((0, 3)))
+        tris = np.empty(6 * int(off[-1]), dtype=np.int32)
+        counts = np.zeros(len(vs), dtype=np.int32)
+        _check(lib().visacd_convex_hulls(self._h, _ptr(allv), _ptr(off), len(vs), int(bool(fix_normals)),
+                                         _ptr(tris), _ptr(counts)), "visacd_convex_hulls")
+        return [tris[6 * off[k]:6 * off[k] + 3 * counts[k]].reshape(-1, 3).copy() for k in range(len(vs))]
 
     # ---- hull merging ------------------------------------------------------
     def hull_distances(self, hulls, pairs, cutoff: float = np.finfo(np.float64).max):

@@ -120,6 +120,7 @@ enum CtxSlot {
   kSlotLearned,
   kSlotFreeGrid,
   kSlotVisCleared,
+  kSlotConvexHull,
   kSlotCount
 };
 
@@ -209,6 +210,7 @@ enum KernelId {
   kKGridEdt,
   kKGridFinal,
   kKVisWalk,
+  kKConvexHull,
   kKMisc,
   kKCount
 };

@@ -88,7 +88,8 @@ static const char* kNames[kKCount] = {
     "lp_misc",       "sdf_remesh",     "sdf_dist",     "sdf_cross",
     "hull_dist",     "seg_tri",        "candidates",
     "lp_refine",     "lp_split",       "grid_near",    "grid_edt",
-    "grid_final",    "vis_walk",       "misc"};
+    "grid_final",    "vis_walk",       "convex_hull",
+    "misc"};
 
 const char* kernel_name(int id) { return (id >= 0 && id < kKCount) ? kNames[id] : "?"; }
 

@@ -126,21 +126,24 @@ PYBIND11_MODULE(visacd, m) {
   // None keep their setting; returns the settings after the call.
   m.def(
       "_checker_hooks",
-      [](py::object clip, py::object concavity, py::object remesh, py::object merge) {
+      [](py::object clip, py::object concavity, py::object remesh, py::object merge, py::object hull) {
         CheckerHooks& h = checker_hooks();
         if (!clip.is_none()) h.host_clip = clip.cast<bool>();
         if (!concavity.is_none()) h.host_concavity = concavity.cast<bool>();
         if (!remesh.is_none()) h.host_remesh = remesh.cast<bool>();
         if (!merge.is_none()) h.host_merge = merge.cast<bool>();
+        if (!hull.is_none()) h.host_hull = hull.cast<bool>();
         py::dict d;
         d["host_clip"] = h.host_clip;
         d["host_concavity"] = h.host_concavity;
         d["host_remesh"] = h.host_remesh;
         d["host_merge"] = h.host_merge;
+        d["host_hull"] = h.host_hull;
         return d;
       },
       py::arg("host_clip") = py::none(), py::arg("host_concavity") = py::none(),
-      py::arg("host_remesh") = py::none(), py::arg("host_merge") = py::none());
+      py::arg("host_remesh") = py::none(), py::arg("host_merge") = py::none(),
+      py::arg("host_hull") = py::none());
   // Test hook: record every visibility call of process() (the part with its
   // is_new mask and the edges found, and its cage); reading clears the record.
   m.def("_record_visibility", [](bool on) {
@@ -248,10 +251,13 @@ PYBIND11_MODULE(visacd, m) {
     gpu::sdf_remesh(mm, scale, level);
     return mesh_dict(mm);
   });
-  m.def("_convex_hull", [](py::array_t<double> v) {
-    Mesh tmp = np_to_mesh(v, py::array_t<int>(std::vector<py::ssize_t>{0, 3}));
-    return mesh_dict(convex_hull(tmp.vertices, true));
-  });
+  m.def(
+      "_convex_hull",
+      [](py::array_t<double> v, bool fix_normals) {
+        Mesh tmp = np_to_mesh(v, py::array_t<int>(std::vector<py::ssize_t>{0, 3}));
+        return mesh_dict(convex_hull(tmp.vertices, fix_normals));
+      },
+      py::arg("v"), py::arg("fix_normals") = true);
   m.def("_clip", [](py::array_t<double> v, py::array_t<int> t, std::array<double, 4> pl) {
     Mesh mm = np_to_mesh(v, t);
     std::vector<int> m1, m2;

@@ -114,6 +114,7 @@ struct CheckerHooks {
   bool host_concavity = false;   // host Hausdorff term of the concavity metric
   bool host_remesh = false;      // host SDF remesh (manifold and cages)
   bool host_merge = false;       // host hull-pair distances in hull merging
+  bool host_hull = false;        // host QuickHull instead of visacd_convex_hulls
   bool record_visibility = false;  // keep every visibility call and split search
 };
 CheckerHooks& checker_hooks();

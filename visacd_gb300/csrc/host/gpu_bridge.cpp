@@ -432,6 +432,29 @@ void sdf_remesh(Mesh& m, double scale, double level) {
   m.triangles = std::move(ot);
 }
 
+MeshList convex_hulls(const std::vector<const std::vector<Vec3>*>& sets, bool fix_normals) {
+  MeshList out(sets.size());
+  if (sets.empty()) return out;
+  visacd_ctx* ctx = context();
+  std::vector<int64_t> off(sets.size() + 1, 0);
+  for (size_t k = 0; k < sets.size(); ++k) off[k + 1] = off[k] + (int64_t)sets[k]->size();
+  std::vector<double> v;
+  v.reserve(3 * (size_t)off.back());
+  for (const auto* s : sets)
+    for (const auto& p : *s) v.insert(v.end(), p.begin(), p.end());
+  std::vector<int32_t> tris(6 * (size_t)off.back()), counts(sets.size());
+  check(visacd_convex_hulls(ctx, v.data(), off.data(), (int32_t)sets.size(), fix_normals ? 1 : 0, tris.data(),
+                            counts.data()),
+        "visacd_convex_hulls");
+  for (size_t k = 0; k < sets.size(); ++k) {
+    out[k].vertices = *sets[k];
+    const int32_t* t = tris.data() + 6 * off[k];
+    out[k].triangles.resize(counts[k]);
+    for (int32_t i = 0; i < counts[k]; ++i) out[k].triangles[i] = {t[3 * i], t[3 * i + 1], t[3 * i + 2]};
+  }
+  return out;
+}
+
 std::vector<double> hull_distances(const MeshList& hulls, const std::vector<std::pair<int, int>>& pairs,
                                    double cutoff) {
   std::vector<double> out(pairs.size());

@@ -87,6 +87,10 @@ MeshList clip(const Mesh& mesh, const Plane& plane, std::vector<int>& pos_map,
 // manifold_preprocess_host.
 void sdf_remesh(Mesh& m, double scale, double level);
 
+// Convex hulls of many point sets in one launch (visacd_convex_hulls): the
+// same meshes as convex_hull(*sets[k], fix_normals), every input point a vertex.
+MeshList convex_hulls(const std::vector<const std::vector<Vec3>*>& sets, bool fix_normals);
+
 // mesh_dist of hull pairs on the GPU (visacd_hull_distances); DBL_MAX where the
 // bounding boxes are farther apart than cutoff.
 std::vector<double> hull_distances(const MeshList& hulls, const std::vector<std::pair<int, int>>& pairs,

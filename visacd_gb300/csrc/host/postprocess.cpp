@@ -132,10 +132,35 @@ std::vector<double> pair_distances(const MeshList& cvxs, const std::vector<std::
   return d;
 }
 
-Mesh merged_hull(const Mesh& a, const Mesh& b) {
-  std::vector<Vec3> pts = a.vertices;
-  pts.insert(pts.end(), b.vertices.begin(), b.vertices.end());
-  return convex_hull(pts, true);
+// Hulls of the unions of hull pairs (the reference's merge_ch,
+// lib/src/postprocess.cpp:30-43: the hull of both vertex lists, the pair's
+// first hull first), many in one launch of visacd_convex_hulls (the host
+// QuickHull under the test hook host_hull; both give the same meshes). Hulls
+// draw no random numbers, so building the ones a cost pass needs before that
+// pass changes nothing.
+MeshList union_hulls(const MeshList& cvxs, const std::vector<std::pair<int, int>>& pairs) {
+  std::vector<std::vector<Vec3>> pts(pairs.size());
+  std::vector<const std::vector<Vec3>*> sets(pairs.size());
+  for (size_t k = 0; k < pairs.size(); ++k) {
+    const Mesh &a = cvxs[pairs[k].first], &b = cvxs[pairs[k].second];
+    pts[k] = a.vertices;
+    pts[k].insert(pts[k].end(), b.vertices.begin(), b.vertices.end());
+    sets[k] = &pts[k];
+  }
+  if (!checker_hooks().host_hull) return gpu::convex_hulls(sets, true);
+  MeshList h(pairs.size());
+#pragma omp parallel for schedule(dynamic, 1) if (pairs.size() > 1)
+  for (long k = 0; k < (long)pairs.size(); ++k) h[k] = convex_hull(pts[k], true);
+  return h;
+}
+
+// The pairs of `pairs` closer than threshold, with their union hulls.
+MeshList close_union_hulls(const MeshList& cvxs, const std::vector<std::pair<int, int>>& pairs,
+                           const std::vector<double>& dist, double threshold) {
+  std::vector<std::pair<int, int>> close;
+  for (size_t k = 0; k < pairs.size(); ++k)
+    if (dist[k] < threshold) close.push_back(pairs[k]);
+  return union_hulls(cvxs, close);
 }
 
 }  // namespace
@@ -160,11 +185,13 @@ void multimerge_ch(MeshList& meshes, MeshList& cvxs, double current_concavity, d
     all_pairs[idx] = {(int)(p1 + 1), (int)(idx - sum)};
   }
   const std::vector<double> all_dist = pair_distances(cvxs, all_pairs, threshold);
+  const MeshList all_ch = close_union_hulls(cvxs, all_pairs, all_dist, threshold);
+  size_t next_ch = 0;
   for (size_t idx = 0; idx < bound; ++idx) {
     const size_t p1 = (size_t)all_pairs[idx].first, p2 = (size_t)all_pairs[idx].second;
     double dist = all_dist[idx];
     if (dist < threshold) {
-      Mesh ch = merged_hull(cvxs[p1], cvxs[p2]);
+      const Mesh& ch = all_ch[next_ch++];
       cost[idx] = compute_h3(cvxs[p1], cvxs[p2], ch, 0.3, 10000);
       precost[idx] = std::max(compute_h(meshes[p1], cvxs[p1], 0.3, 10000),
                               compute_h(meshes[p2], cvxs[p2], 0.3, 10000));
@@ -194,8 +221,8 @@ void multimerge_ch(MeshList& meshes, MeshList& cvxs, double current_concavity, d
     const size_t addrI = ((size_t)(int)std::sqrt(1 + (8.0 * addr)) - 1) >> 1;
     const size_t p1 = addrI + 1;
     const size_t p2 = addr - ((addrI * (addrI + 1)) >> 1);
-    Mesh cch = merged_hull(cvxs[p1], cvxs[p2]);
-    cvxs[p2] = cch;
+    MeshList cch = union_hulls(cvxs, {{(int)p1, (int)p2}});
+    cvxs[p2] = std::move(cch[0]);
     std::swap(cvxs[p1], cvxs[cvxs.size() - 1]);
     cvxs.pop_back();
     cost_size -= 1;
@@ -204,11 +231,13 @@ void multimerge_ch(MeshList& meshes, MeshList& cvxs, double current_concavity, d
     for (size_t i = 0; i < cost_size; ++i)
       if (i != p2) row_pairs.push_back({(int)p2, (int)i});
     const std::vector<double> row_dist = pair_distances(cvxs, row_pairs, threshold);
+    const MeshList row_ch = close_union_hulls(cvxs, row_pairs, row_dist, threshold);
+    next_ch = 0;
     size_t row = ((p2 - 1) * p2) >> 1;
     for (size_t i = 0; i < p2; ++i) {
       double dist = row_dist[i];
       if (dist < threshold) {
-        Mesh ch = merged_hull(cvxs[p2], cvxs[i]);
+        const Mesh& ch = row_ch[next_ch++];
         cost[row] = compute_h3(cvxs[p2], cvxs[i], ch, 0.3, 10000);
         precost[row++] = std::max(pre(p2) + best, pre(i));
       } else {
@@ -219,7 +248,7 @@ void multimerge_ch(MeshList& meshes, MeshList& cvxs, double current_concavity, d
     for (size_t i = p2 + 1; i < cost_size; ++i) {
       double dist = row_dist[i - 1];
       if (dist < threshold) {
-        Mesh ch = merged_hull(cvxs[p2], cvxs[i]);
+        const Mesh& ch = row_ch[next_ch++];
         cost[row] = compute_h3(cvxs[p2], cvxs[i], ch, 0.3, 10000);
         precost[row] = std::max(pre(p2) + best, pre(i));
       } else {
