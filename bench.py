@@ -301,14 +301,19 @@ def run_ours(args) -> dict:
     # activity of each (profiles/) say what binds them.
     walk_ms, walk_n = ktimes.get("vis_walk", (0.0, 0))
     walk_launch_s = walk_ms / max(walk_n, 1) / 1e3
-    # Free-space walk per launch: each grid read takes the point (3 FMA), its
-    # cell coordinates (3 sub + 3 mul) and the step (sub, mul, add): 15 FLOP.
+    # Free-space walk per launch: one point-sampled texture fetch of the bound
+    # grid per step (grid reads, counted by the kernel), and around it the
+    # point (3 FMA), its cell coordinates (3 sub + 3 mul) and the step (sub,
+    # mul, add): 15 FLOP. The texture fetch rate binds it (ncu: L1/TEX is its
+    # busiest unit); the FP32 figure is kept beside it.
+    walk_fetch = walk_reads / walk_launch_s / 1e9 if walk_ms else None
     walk_flop = 15.0 * walk_reads
     walk_achieved = walk_flop / walk_launch_s / 1e12 if walk_ms else None
     vis_ms, vis_n = ktimes.get("visibility", (0.0, 0))
     sc_ms, sc_n = ktimes.get("score_planes", (0.0, 0))
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     fp32_peak = ctx.fp32_peak_tflops()
+    tex_coherent, tex_divergent = ctx.tex_peak_gfetch()
     vis_launch_s = vis_ms / max(vis_n, 1) / 1e3
     # Traversal arithmetic per launch: each packet node visit runs 2 packed
     # slab tests (12 FLOP each) on 32 lanes; each triangle test ~60 FLOP.
@@ -334,15 +339,22 @@ def run_ours(args) -> dict:
         "gpu_launches": int(launches),
         "kernels_ms_per_step": {k: v[0] / args.steps for k, v in sorted(ktimes.items(), key=lambda kv: -kv[1][0])},
         "kernel_launches": {k: v[1] for k, v in ktimes.items()},
-        "roofline": {"kernel": "visibility_walk_kernel", "bound": "l1-latency",
-                     "achieved": walk_achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                     "frac": walk_achieved / fp32_peak if walk_achieved else None,
+        "roofline": {"kernel": "visibility_walk_kernel", "bound": "texture-fetch",
+                     "achieved": walk_fetch, "peak": tex_coherent, "unit": "Gfetch/s",
+                     "frac": walk_fetch / tex_coherent if walk_fetch else None,
+                     "frac_of_divergent_fetch_rate": walk_fetch / tex_divergent if walk_fetch else None,
+                     "peak_divergent": tex_divergent,
+                     "fp32_model": {"achieved": walk_achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                                    "frac": walk_achieved / fp32_peak if walk_achieved else None,
+                                    "work_model": "grid reads x 15 FLOP (point, cell coordinates, step)"},
                      "traffic": measured_traffic(args.workload, "visibility_walk_kernel"),
                      "ncu": measured_throughput(args.workload, "visibility_walk_kernel"),
                      "ms_per_launch": walk_ms / max(walk_n, 1),
                      "segments_cleared": int(walk_cleared), "grid_reads": int(walk_reads),
-                     "work_model": "grid reads x 15 FLOP (point, cell coordinates, step)",
-                     "peak_source": "measured in-process (fma.rn.f32x2 loop); HBM peak of measured "
+                     "work_model": "grid reads (one point-sampled tex3D<float> fetch each) per launch",
+                     "peak_source": "measured in-process: tex3D<float> point fetches from a cache-resident "
+                                    "32^3 texture, coherent 8x4 texel blocks per warp (peak) and one line per "
+                                    "lane (peak_divergent); HBM peak of measured "
                                     f"{peaks.get('hbm_gbs')} GB/s not binding (L2-resident grid)"},
         "roofline_traversal": {"kernel": "visibility_kernel", "bound": "fp32-issue",
                                "achieved": vis_achieved, "peak": fp32_peak, "unit": "TFLOP/s",

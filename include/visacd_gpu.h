@@ -125,6 +125,12 @@ int visacd_set_blocking_sync(int device, int blocking);
 /* FP32 FMA throughput of this GPU in TFLOP/s (packed f32x2 FMA loop, best of
    3 timed launches): the denominator of the FP32-bound rooflines. */
 int visacd_measure_fp32_peak(visacd_ctx* ctx, double* tflops);
+/* Texture fetch rate of this GPU (G fetches/s, point-sampled tex3D<float> from
+   a cache-resident texture), the denominator of the free-space walk's
+   roofline: coherent = a warp reads an 8 x 4 block of neighbouring texels (the
+   best case), divergent = every lane walks its own line through the texture.
+   Synchronizes. */
+int visacd_measure_tex_peak(visacd_ctx* ctx, double* coherent_gfetch, double* divergent_gfetch);
 
 /* ---- BVH ---------------------------------------------------------------- */
 /* Linear BVH over a triangle mesh: 63-bit Morton codes of triangle centroids,

@@ -23,7 +23,7 @@ EXPORTED = [
     "visacd_compute_intersection_matrix",
     "visacd_vis_variant_count", "visacd_ctx_set_vis_variant", "visacd_autotune_visibility",
     "visacd_score_planes", "visacd_score_planes_noalloc", "classify_and_rate_planes",
-    "visacd_clip", "visacd_clip_fetch", "visacd_measure_fp32_peak", "visacd_face_hausdorff",
+    "visacd_clip", "visacd_clip_fetch", "visacd_measure_fp32_peak", "visacd_measure_tex_peak", "visacd_face_hausdorff",
     "visacd_face_hausdorff_floor", "visacd_face_hausdorff_batch",
     "visacd_batch_create", "visacd_batch_run", "visacd_batch_results", "visacd_batch_info",
     "visacd_batch_destroy",
@@ -133,6 +133,7 @@ def load() -> C.CDLL:
                                                 C.POINTER(LearnedSplitInfo)]
     lib.visacd_clip.argtypes = [P, P, i32, P, i32, P, C.POINTER(ClipResult)]
     lib.visacd_measure_fp32_peak.argtypes = [P, C.POINTER(C.c_double)]
+    lib.visacd_measure_tex_peak.argtypes = [P, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     lib.visacd_batch_create.argtypes = [P, i32, C.POINTER(P), P, C.POINTER(P), C.POINTER(P), C.POINTER(P),
                                         P, i64, C.POINTER(P)]
     lib.visacd_batch_run.argtypes = [P, P, C.c_int]
@@ -348,6 +349,12 @@ class Context:
         t = C.c_double()
         _check(lib().visacd_measure_fp32_peak(self._h, C.byref(t)), "measure_fp32_peak")
         return t.value
+
+    def tex_peak_gfetch(self) -> tuple[float, float]:
+        """Texture fetch rate (G fetches/s): (coherent, divergent)."""
+        c, d = C.c_double(), C.c_double()
+        _check(lib().visacd_measure_tex_peak(self._h, C.byref(c), C.byref(d)), "measure_tex_peak")
+        return c.value, d.value
 
     # ---- clipping ----------------------------------------------------------
     def clip(self, verts, tris, plane):
