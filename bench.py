@@ -407,6 +407,56 @@ def grazing_check(v, bits, edges_gpu) -> dict:
             "differing_outside_grazing_band": int((diff & ~graze).sum())}
 
 
+def run_hulls(args) -> dict:
+    """Convex hulls of a batch of clipped parts (64 displaced blobs, s3 and
+    s4, each cut by two seeded planes with the host clip: planar caps, as the
+    decomposition's parts have): visacd_convex_hulls in one call against the
+    host QuickHull on one core, wall clock with host buffers, and whether
+    every GPU hull equals the host's triangle for triangle."""
+    from visacd_gb300 import _native as N, build, meshgen
+
+    build.build_host()
+    from visacd_gb300 import visacd as V
+
+    rng = np.random.default_rng(23)
+    parts = []
+
+    def plane():
+        nrm = rng.normal(size=3)
+        return [*(nrm / np.linalg.norm(nrm)), rng.uniform(-0.3, 0.3)]
+
+    for s in range(64):
+        v, t = meshgen.displaced_blob(3 + (s % 2), seed=40 + s)
+        halves, _, _ = V._clip(v, t, plane())
+        for h in halves:
+            quarters, _, _ = V._clip(np.asarray(h["vertices"]), np.asarray(h["triangles"]), plane())
+            parts += [np.asarray(q["vertices"]) for q in quarters]
+    ctx = N.Context(0)
+    try:
+        ctx.convex_hulls(parts[:4])
+
+        def med(f, r):
+            ts = []
+            for _ in range(r):
+                t0 = time.perf_counter()
+                f()
+                ts.append(time.perf_counter() - t0)
+            return 1e3 * float(np.median(ts))
+
+        gpu = ctx.convex_hulls(parts)
+        equal = all(np.array_equal(g, np.asarray(V._convex_hull(p)["triangles"], np.int32).reshape(-1, 3))
+                    for p, g in zip(parts, gpu))
+        out = {"parts": len(parts), "points": int(sum(len(p) for p in parts)),
+               "gpu_ms_one_call": med(lambda: ctx.convex_hulls(parts), 3),
+               "host_ms_one_core": med(lambda: [V._convex_hull(p) for p in parts], 3),
+               "gpu_ms_two_parts": med(lambda: ctx.convex_hulls(parts[:2]), 5),
+               "host_ms_two_parts_one_core": med(lambda: [V._convex_hull(p) for p in parts[:2]], 5),
+               "equal_to_host": bool(equal)}
+    finally:
+        ctx.close()
+    return out
+
+
 def run_decompositions(args) -> dict:
     """End-to-end visacd.process() on the torus (64 x 32, concavity 0.04, 32
     parts) and the s5 blob (concavity 0.02, 64 parts): decompositions/s."""
@@ -1016,6 +1066,7 @@ def main():
                     help="decompositions of the batching workload's meshes: batched vs plain")
     ap.add_argument("--c3-plain", type=int, default=64, help="meshes the plain loop times in --c3-decomps")
     ap.add_argument("--no-c3", action="store_true", help="skip the 256-mesh decompositions")
+    ap.add_argument("--no-hulls", action="store_true", help="skip the batched convex hull timing")
     ap.add_argument("--sweep-sizes", type=int, nargs="+", default=[20, 22, 24, 26])
     ap.add_argument("--segtri", type=int, default=1 << 20, help="segment-triangle tests in the sweep")
     ap.add_argument("--c5", action="store_true", help="batched + learned decompositions only")
@@ -1062,6 +1113,8 @@ def main():
             out["decomps"] = run_learned_batch(args)
         if rank == 0 and single and not args.no_c3:
             out["decomps_256"] = run_batch_decompositions(args)["batch_decompositions"]
+        if rank == 0 and single and not args.no_hulls:
+            out["hulls"] = run_hulls(args)
     if rank == 0 and out is not None:
         print(json.dumps(out))
 

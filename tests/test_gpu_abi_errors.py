@@ -83,3 +83,11 @@ def test_clip_bad_triangle_index(native, ctx):
     v = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], float)
     with pytest.raises(native.VisacdError):
         ctx.clip(v, np.array([[0, 1, -1]], np.int32), [1.0, 0.0, 0.0, -0.5])
+
+
+def test_throughput_probes(ctx):
+    """The in-process roofline denominators: the FP32 FMA rate and the texture
+    fetch rates (coherent blocks faster than one line per lane)."""
+    assert ctx.fp32_peak_tflops() > 1.0
+    coherent, divergent = ctx.tex_peak_gfetch()
+    assert coherent > divergent > 1.0
