@@ -33,7 +33,14 @@ struct BuildCounters {
   unsigned bad_index;
   int depth;
   int pad;
+  unsigned tb[6];    // orderable bounds of the triangles' vertices: min xyz, max xyz
 };
+
+// Order-preserving map of a float to unsigned (for atomic min / max).
+__device__ __forceinline__ unsigned ord_f32(float f) {
+  const unsigned b = __float_as_uint(f);
+  return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
 
 __global__ void vert_absmax_kernel(const float* __restrict__ v, int32_t nv,
                                    BuildCounters* __restrict__ c) {
@@ -171,10 +178,15 @@ __global__ void karras_kernel(const uint64_t* __restrict__ keys, int32_t n,
 __global__ void leaf_kernel(const float* __restrict__ v, int32_t nv,
                             const uint32_t* __restrict__ t,
                             const uint32_t* __restrict__ order, int32_t n,
-                            const BuildCounters* __restrict__ c, float4* __restrict__ tris,
+                            BuildCounters* __restrict__ c, float4* __restrict__ tris,
                             float* __restrict__ leafbox) {
   float pad = __uint_as_float(c->amax) * 1.9073486e-6f + 1e-30f;  // 2^-19 * max|coord|
+  // Bounds of all triangles' vertices (exact min / max; the free-space grid
+  // of a cage is laid over them).
+  float blo[3] = {INFINITY, INFINITY, INFINITY}, bhi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  bool any = false;
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+    any = true;
     uint32_t tri = order[s];
     uint32_t id[3] = {t[3 * (int64_t)tri], t[3 * (int64_t)tri + 1], t[3 * (int64_t)tri + 2]};
     float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
@@ -193,6 +205,22 @@ __global__ void leaf_kernel(const float* __restrict__ v, int32_t nv,
     for (int a = 0; a < 3; ++a) {
       leafbox[6 * (int64_t)s + a] = lo[a] - pad;
       leafbox[6 * (int64_t)s + 3 + a] = hi[a] + pad;
+      blo[a] = fminf(blo[a], lo[a]);
+      bhi[a] = fmaxf(bhi[a], hi[a]);
+    }
+  }
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      blo[a] = fminf(blo[a], __shfl_xor_sync(0xffffffffu, blo[a], o));
+      bhi[a] = fmaxf(bhi[a], __shfl_xor_sync(0xffffffffu, bhi[a], o));
+    }
+  }
+  if (__any_sync(0xffffffffu, any) && (threadIdx.x & 31) == 0) {
+    for (int a = 0; a < 3; ++a) {
+      atomicMin(&c->tb[a], ord_f32(blo[a]));
+      atomicMax(&c->tb[3 + a], ord_f32(bhi[a]));
     }
   }
 }
@@ -324,6 +352,10 @@ int bvh_build(visacd_ctx* ctx, const float* verts, int32_t nv, const uint32_t* t
   init.bad_index = 0;
   init.depth = 0;
   init.pad = 0;
+  for (int a = 0; a < 3; ++a) {
+    init.tb[a] = 0xffffffffu;
+    init.tb[3 + a] = 0u;
+  }
   BuildCounters* hcnt = nullptr;
   VTRY(pinned(ctx, sizeof(BuildCounters), (void**)&hcnt));
   *hcnt = init;
@@ -371,6 +403,7 @@ int bvh_build(visacd_ctx* ctx, const float* verts, int32_t nv, const uint32_t* t
   }
   b->depth = nt == 1 ? 1 : hcnt->depth;
   b->amax = __uint_as_float_host(hcnt->amax);
+  for (int a = 0; a < 6; ++a) b->tri_bounds[a] = hcnt->tb[a];
   b->ctx = ctx;
   ctx->bvhs.push_back(b);
   *out = b;

@@ -17,6 +17,9 @@ struct visacd_bvh {
   int32_t nv = 0;
   int32_t depth = 0;
   float amax = 0.f;  // largest |vertex coordinate|
+  // Bounds of the triangles' vertices as order-preserving unsigned values
+  // (min xyz, max xyz), read back with the build's counters.
+  unsigned tri_bounds[6] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u};
   float4* nodes = nullptr;
   float4* tris = nullptr;
   visacd_ctx* ctx = nullptr;       // owning context (null once it is destroyed)

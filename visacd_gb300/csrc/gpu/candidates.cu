@@ -815,7 +815,9 @@ extern "C" int visacd_split_search(visacd_ctx* ctx, const double* verts, int32_t
   // every queued block.
   unsigned rcap = score_recheck_capacity(P, E);
   SplitOut* h = nullptr;
-  VTRY(pinned(ctx, sizeof(SplitOut), (void**)&h));
+  const size_t o_st = (sizeof(SplitOut) + 15) & ~size_t(15);
+  VTRY(pinned(ctx, o_st + 16, (void**)&h));
+  uint32_t* hst = reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(h) + o_st);
   for (int attempt = 0; attempt < 2; ++attempt) {
     const unsigned* st_status = nullptr;
     const unsigned* st_count = nullptr;
@@ -824,6 +826,7 @@ extern "C" int visacd_split_search(visacd_ctx* ctx, const double* verts, int32_t
     VLAUNCH(ctx, kKCandidates, 1, 1024, 0, split_argmax_kernel, scores, s.out64, s.info, cand_slots,
             n_flat, flat_k, st_status, st_count, s.split);
     VCUDA(cudaMemcpyAsync(h, s.split, sizeof(SplitOut), cudaMemcpyDeviceToHost, ctx->stream));
+    VCUDA(cudaMemcpyAsync(hst, ctx->d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
     VCUDA(stream_wait(ctx));
     VCHECK(!(h->score_status & kStatusMbarrierTimeout), VISACD_ERR_DEVICE,
            "split_search: a bulk-copy wait of the scoring kernel timed out");
@@ -831,10 +834,8 @@ extern "C" int visacd_split_search(visacd_ctx* ctx, const double* verts, int32_t
     VCHECK(attempt == 0, VISACD_ERR_DEVICE, "split_search: FP64 queue overflow after a rerun");
     rcap = h->recheck_count;
   }
-  // The read-back shares the pinned staging area with the status check: copy
-  // it out first.
   const SplitOut r = *h;
-  VTRY(check_status(ctx, "split_search"));
+  VTRY(status_result(ctx, *hst, "split_search"));
   for (int c = 0; c < 4; ++c) best_plane[c] = r.plane[c];
   if (info) {
     info->best_index = r.index;
@@ -904,7 +905,9 @@ extern "C" int visacd_learned_split_search(visacd_lp* lp, const double* verts, i
   double* scores = slot<double>(ctx, kSlotScores);
   unsigned rcap = score_recheck_capacity(P, E);
   LearnedOut* h = nullptr;
-  VTRY(pinned(ctx, sizeof(LearnedOut), (void**)&h));
+  const size_t o_st = (sizeof(LearnedOut) + 15) & ~size_t(15);
+  VTRY(pinned(ctx, o_st + 16, (void**)&h));
+  uint32_t* hst = reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(h) + o_st);
   for (int attempt = 0; attempt < 2; ++attempt) {
     const unsigned* st_status = nullptr;
     const unsigned* st_count = nullptr;
@@ -913,6 +916,7 @@ extern "C" int visacd_learned_split_search(visacd_lp* lp, const double* verts, i
     VLAUNCH(ctx, kKLpSplit, 1, 1024, 0, learned_decide_kernel, scores, L64, nref, s.info, probe_slots,
             n_flat, flat_k, tolerance, st_status, st_count, dout);
     VCUDA(cudaMemcpyAsync(h, dout, sizeof(LearnedOut), cudaMemcpyDeviceToHost, ctx->stream));
+    VCUDA(cudaMemcpyAsync(hst, ctx->d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
     VCUDA(stream_wait(ctx));
     VCHECK(!(h->score_status & kStatusMbarrierTimeout), VISACD_ERR_DEVICE,
            "learned_split_search: a bulk-copy wait of the scoring kernel timed out");
@@ -920,10 +924,8 @@ extern "C" int visacd_learned_split_search(visacd_lp* lp, const double* verts, i
     VCHECK(attempt == 0, VISACD_ERR_DEVICE, "learned_split_search: FP64 queue overflow after a rerun");
     rcap = h->recheck_count;
   }
-  // The read-back shares the pinned staging area with the status check: copy
-  // it out first.
   const LearnedOut r = *h;
-  VTRY(check_status(ctx, "learned_split_search"));
+  VTRY(status_result(ctx, *hst, "learned_split_search"));
   for (int c = 0; c < 4; ++c) best_plane[c] = r.plane[c];
   if (info) {
     info->best_index = r.index;

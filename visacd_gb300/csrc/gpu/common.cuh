@@ -226,6 +226,9 @@ int after_launch(visacd_ctx* ctx, const char* what);
 // Read back and clear the device status word; returns VISACD_ERR_DEVICE with a
 // message when any bit is set. Synchronizes the context stream.
 int check_status(visacd_ctx* ctx, const char* what);
+// The same for a status word the caller already read back (with its own
+// results, in one wait): clears the device word when it is set.
+int status_result(visacd_ctx* ctx, uint32_t status, const char* what);
 
 // Pinned host staging of at least `bytes`.
 int pinned(visacd_ctx* ctx, size_t bytes, void** out);

@@ -194,7 +194,10 @@ int check_status(visacd_ctx* ctx, const char* what) {
   VTRY(pinned(ctx, 64, (void**)&h));
   VCUDA(cudaMemcpyAsync(h, ctx->d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
   VCUDA(stream_wait(ctx));
-  uint32_t s = h[0];
+  return status_result(ctx, h[0], what);
+}
+
+int status_result(visacd_ctx* ctx, uint32_t s, const char* what) {
   if (s) {
     VCUDA(cudaMemsetAsync(ctx->d_status, 0, sizeof(uint32_t), ctx->stream));
     set_error("%s: device status 0x%x (traversal overrun=%d, stack overflow=%d, recheck "

@@ -31,39 +31,6 @@ constexpr int kFgMaxDim = 256;          // cells per axis at most (EDT row buffe
 constexpr int kFgInf = 0x3fffffff;      // "no surface cell" squared distance
 constexpr float kU32 = 5.9604645e-8f;   // 2^-24
 
-__device__ __forceinline__ unsigned fg_ord(float f) {
-  const unsigned b = __float_as_uint(f);
-  return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
-}
-
-// Bounding box of the triangles (orderable bits, atomics).
-__global__ void fg_bounds_kernel(const float4* __restrict__ tris, int32_t nt, unsigned* __restrict__ bb) {
-  float mn[3] = {3.4e38f, 3.4e38f, 3.4e38f}, mx[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < 3LL * nt;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const float4 v = tris[i];
-    mn[0] = fminf(mn[0], v.x);
-    mn[1] = fminf(mn[1], v.y);
-    mn[2] = fminf(mn[2], v.z);
-    mx[0] = fmaxf(mx[0], v.x);
-    mx[1] = fmaxf(mx[1], v.y);
-    mx[2] = fmaxf(mx[2], v.z);
-  }
-  for (int a = 0; a < 3; ++a) {
-#pragma unroll
-    for (int o = 16; o; o >>= 1) {
-      mn[a] = fminf(mn[a], __shfl_xor_sync(0xffffffffu, mn[a], o));
-      mx[a] = fmaxf(mx[a], __shfl_xor_sync(0xffffffffu, mx[a], o));
-    }
-  }
-  if ((threadIdx.x & 31) == 0) {
-    for (int a = 0; a < 3; ++a) {
-      atomicMin(&bb[a], fg_ord(mn[a]));
-      atomicMax(&bb[3 + a], fg_ord(mx[a]));
-    }
-  }
-}
-
 __device__ __forceinline__ float fg_dot(float ax, float ay, float az, float bx, float by, float bz) {
   return ax * bx + ay * by + az * bz;
 }
@@ -300,20 +267,9 @@ int free_grid_build(visacd_ctx* ctx, visacd_bvh* b, int64_t pairs) {
   if (b->free_built) return VISACD_OK;
   b->free_built = true;  // also when the grid is not usable: then it is not retried
   if (b->nt <= 0) return VISACD_OK;
-  // Bounding box of the triangles. The caller's pinned staging buffer and
-  // counters are not in use yet; earlier work on the stream is waited for.
-  VCUDA(stream_wait(ctx));
-  VTRY(ensure_slot(ctx, kSlotCounters, 64));
-  unsigned* bb = slot<unsigned>(ctx, kSlotCounters);
-  unsigned init[6] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u};
-  unsigned* h = nullptr;
-  VTRY(pinned(ctx, 64, (void**)&h));
-  memcpy(h, init, sizeof(init));
-  VCUDA(cudaMemcpyAsync(bb, h, sizeof(init), cudaMemcpyHostToDevice, ctx->stream));
-  VLAUNCH(ctx, kKVisPrep, grid_for(3LL * b->nt, 256, 4LL * ctx->sm_count), 256, 0, fg_bounds_kernel, b->tris,
-          b->nt, bb);
-  VCUDA(cudaMemcpyAsync(h, bb, sizeof(init), cudaMemcpyDeviceToHost, ctx->stream));
-  VCUDA(stream_wait(ctx));
+  // Bounding box of the triangles, read back with the BVH build's counters
+  // (order-preserving unsigned values).
+  const unsigned* h = b->tri_bounds;
   float lo[3], hi[3];
   for (int a = 0; a < 3; ++a) {
     const unsigned ol = h[a], oh = h[3 + a];

@@ -379,27 +379,32 @@ int score_planes_impl(visacd_ctx* ctx, const float* planes, int32_t P, const flo
   ScoreCounters* cnt = nullptr;
   VTRY(score_device(ctx, d_planes, P, d_pts, N, d_edges, E, d_scores, d_scores_f32, &cnt, rcap));
   if (!device_ptrs || stats) {
+    // Counters, the context's status word and (host mode) the scores in one wait.
     ScoreCounters* h = nullptr;
-    VTRY(pinned(ctx, sizeof(ScoreCounters), (void**)&h));
-    VCUDA(cudaMemcpyAsync(h, cnt, sizeof(ScoreCounters), cudaMemcpyDeviceToHost, ctx->stream));
-    VCUDA(stream_wait(ctx));
+    const size_t o_st = (sizeof(ScoreCounters) + 15) & ~size_t(15);
+    VTRY(pinned(ctx, o_st + 16, (void**)&h));
+    uint32_t* hst = reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(h) + o_st);
+    auto read_back = [&]() -> int {
+      VCUDA(cudaMemcpyAsync(h, cnt, sizeof(ScoreCounters), cudaMemcpyDeviceToHost, ctx->stream));
+      VCUDA(cudaMemcpyAsync(hst, ctx->d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+      if (!device_ptrs && P)
+        VCUDA(cudaMemcpyAsync(scores, d_scores, (size_t)P * 8, cudaMemcpyDeviceToHost, ctx->stream));
+      VCUDA(stream_wait(ctx));
+      return VISACD_OK;
+    };
+    VTRY(read_back());
     ScoreCounters hc = *h;
     if (hc.recheck_count > rcap && !(hc.status & kStatusMbarrierTimeout)) {
       // The FP64 queue overflowed: rerun with room for every queued block.
       rcap = hc.recheck_count;
       VTRY(score_device(ctx, d_planes, P, d_pts, N, d_edges, E, d_scores, d_scores_f32, &cnt, rcap));
-      VCUDA(cudaMemcpyAsync(h, cnt, sizeof(ScoreCounters), cudaMemcpyDeviceToHost, ctx->stream));
-      VCUDA(stream_wait(ctx));
+      VTRY(read_back());
       hc = *h;
     }
     VCHECK(!(hc.status & (kStatusMbarrierTimeout | kStatusRecheckOverflow)), VISACD_ERR_DEVICE,
            "score_planes: device status 0x%x (bulk-copy wait timed out or FP64 queue full)",
            hc.status);
-    VTRY(check_status(ctx, "score_planes"));
-    if (!device_ptrs && P) {
-      VCUDA(cudaMemcpyAsync(scores, d_scores, (size_t)P * 8, cudaMemcpyDeviceToHost, ctx->stream));
-      VCUDA(stream_wait(ctx));
-    }
+    VTRY(status_result(ctx, *hst, "score_planes"));
     if (stats) {
       stats->quantum_exp = hc.argmax[1];
       stats->argmax = hc.argmax[0];
@@ -554,7 +559,6 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 static unsigned char* noalloc_scratch_ptr(int device, int* rc) {
   static std::mutex mu;
   static unsigned char* ptrs[64] = {nullptr};
-  static int sms[64] = {0};
   std::lock_guard<std::mutex> lock(mu);
   if (device < 0 || device >= 64) {
     set_error("score_planes_noalloc: device %d out of range", device);

@@ -683,12 +683,14 @@ static int vis_device(visacd_ctx* ctx, const float* d_pts, int32_t n, const uint
     VLAUNCH(ctx, kKVisPrep, grid_for(P.ntr, 256, 4LL * ctx->sm_count), 256, 0,
             tile_row_counts_kernel, P.ntr, P.ntc, TR, TC, rc);
     VTRY(exclusive_scan_u32_to_u64(ctx, rc, rs, P.ntr));
-    uint64_t* ht = nullptr;
-    VTRY(pinned(ctx, 8, (void**)&ht));
-    VCUDA(cudaMemcpyAsync(ht, rs + P.ntr, 8, cudaMemcpyDeviceToHost, ctx->stream));
-    VCUDA(stream_wait(ctx));
     P.row_start = reinterpret_cast<const unsigned long long*>(rs);
-    P.total_tiles = (unsigned long long)*ht;
+    // The same total as the device scan, counted here (no read-back).
+    unsigned long long total = 0;
+    for (int64_t r = 0; r < P.ntr; ++r) {
+      const int64_t c = P.ntc - (r * TR) / TC;
+      total += (unsigned long long)(c > 0 ? c : 0);
+    }
+    P.total_tiles = total;
   }
   P.self_nodes = self_bvh->nodes;
   P.self_tris = self_bvh->tris;
@@ -733,12 +735,15 @@ static int vis_device(visacd_ctx* ctx, const float* d_pts, int32_t n, const uint
   const unsigned gw = grid_for(nw, 256, 16LL * ctx->sm_count);
   VLAUNCH(ctx, kKBitPopc, gw, 256, 0, bit_popc_kernel, P.bitset, nw, wc);
   VTRY(exclusive_scan_u32_to_u64(ctx, wc, wo, nw));
+  // Counters and the status word in one wait.
+  uint32_t* hs = nullptr;
+  VTRY(pinned(ctx, sizeof(VisCounters) + 64, (void**)&h));
+  hs = reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(h) + ((sizeof(VisCounters) + 15) & ~size_t(15)));
   VCUDA(cudaMemcpyAsync(h, cnt, sizeof(VisCounters), cudaMemcpyDeviceToHost, ctx->stream));
+  VCUDA(cudaMemcpyAsync(hs, ctx->d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
   VCUDA(stream_wait(ctx));
-  // The read-back shares the pinned staging area with the status check: copy
-  // it out first.
   const VisCounters hc = *h;
-  VTRY(check_status(ctx, "visibility"));
+  VTRY(status_result(ctx, *hs, "visibility"));
   const int64_t ne = (int64_t)hc.edges;
   VTRY(ensure_slot(ctx, kSlotEdgesOut, (size_t)(ne > 0 ? ne : 1) * 8));
   if (ne > 0) {
@@ -1062,19 +1067,22 @@ int visibility_multi_impl(visacd_ctx* ctx, int32_t n_parts, const float* const* 
   }
   uint64_t* d_poff = reinterpret_cast<uint64_t*>(base + o_poff);
   VLAUNCH(ctx, kKVisPrep, 1, 256, 0, multi_part_offsets_kernel, d_words, n_parts, wo, d_poff);
+  // Counters, part offsets and the status word in one wait.
   char* hb = nullptr;
-  VTRY(pinned(ctx, sizeof(VisCounters) + 8 * (size_t)(n_parts + 1), (void**)&hb));
+  const size_t o_st = (sizeof(VisCounters) + 8 * (size_t)(n_parts + 1) + 15) & ~size_t(15);
+  VTRY(pinned(ctx, o_st + 16, (void**)&hb));
   VCUDA(cudaMemcpyAsync(hb, cnt, sizeof(VisCounters), cudaMemcpyDeviceToHost, ctx->stream));
   VCUDA(cudaMemcpyAsync(hb + sizeof(VisCounters), d_poff, 8 * (size_t)(n_parts + 1), cudaMemcpyDeviceToHost,
                         ctx->stream));
+  VCUDA(cudaMemcpyAsync(hb + o_st, ctx->d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
   VCUDA(stream_wait(ctx));
-  // Copy the read-back out of the pinned staging area before the status
-  // check reuses it.
   VisCounters hc;
   memcpy(&hc, hb, sizeof(hc));
   std::vector<uint64_t> poff(n_parts + 1);
   memcpy(poff.data(), hb + sizeof(VisCounters), 8 * (size_t)(n_parts + 1));
-  VTRY(check_status(ctx, "visibility_batch"));
+  uint32_t dev_status = 0;
+  memcpy(&dev_status, hb + o_st, sizeof(uint32_t));
+  VTRY(status_result(ctx, dev_status, "visibility_batch"));
   for (int p = 0; p < n_parts; ++p) n_edges[p] = (int64_t)(poff[p + 1] - poff[p]);
   const int64_t ne = (int64_t)poff[n_parts];
   VTRY(ensure_slot(ctx, kSlotEdgesOut, (size_t)(ne > 0 ? ne : 1) * 8));
