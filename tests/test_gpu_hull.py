@@ -116,3 +116,16 @@ def test_gpu_hull_rejects_bad_arguments(native, ctx):
     with pytest.raises(native.VisacdError):
         ctx.convex_hulls([bad])
     assert [len(t) for t in ctx.convex_hulls([])] == []
+
+
+def test_gpu_hull_batch_over_several_launches(V, ctx):
+    """A batch whose work regions pass 1 GiB runs as several launches (each
+    part's result lands at its own offset): 132 s5-blob point sets of 10,242
+    points, four distinct orders of the same points cycled."""
+    v = mg.displaced_blob(5, seed=8)[0]
+    rng = np.random.default_rng(5)
+    sets = [v] + [v[rng.permutation(len(v))] for _ in range(3)]
+    want = [_host(V, p) for p in sets]
+    got = ctx.convex_hulls([sets[k % 4] for k in range(132)])
+    for k, g in enumerate(got):
+        assert np.array_equal(g, want[k % 4]), k

@@ -27,7 +27,8 @@
 // rounded, so every distance, plane and decision equals the host's.
 // Capacities (faces, pool, lists) are multiples of the part's point count;
 // a part that outgrows them stops with a status code and the entry point runs
-// it again with four times the room.
+// it again with four times the room. Launches keep their work regions under
+// 1 GiB, so large batches run as several launches.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -706,20 +707,36 @@ extern "C" int visacd_convex_hulls(visacd_ctx* ctx, const double* points, const 
                oCnt = oTri + hull_align256((size_t)N * 24), oSt = oCnt + hull_align256((size_t)nparts * 4),
                oIds = oSt + hull_align256((size_t)nparts * 4), oRoff = oIds + hull_align256((size_t)nparts * 4),
                oArena = oRoff + hull_align256((size_t)(nparts + 1) * 8);
-  std::vector<int32_t> ids(nparts);
-  for (int32_t k = 0; k < nparts; ++k) ids[k] = k;
+  // Pending parts with their room multiplier, run in launches whose work
+  // regions stay under kHullArenaCap (a part larger than that runs alone).
+  constexpr int64_t kHullArenaCap = 1LL << 30;
+  std::vector<std::pair<int32_t, int>> queue(nparts);
+  for (int32_t k = 0; k < nparts; ++k) queue[k] = {k, 1};
+  std::vector<int32_t> ids;
   std::vector<int64_t> roff;
   std::vector<int32_t> cnt_now(nparts), st_now(nparts);
-  int mult = 1;
-  while (!ids.empty()) {
-    roff.assign(ids.size() + 1, 0);
-    for (size_t j = 0; j < ids.size(); ++j)
-      roff[j + 1] = roff[j] + hull_region_bytes(offsets[ids[j] + 1] - offsets[ids[j]], mult);
+  char* sent_to = nullptr;  // slot base the inputs were last uploaded to
+  size_t head = 0;
+  while (head < queue.size()) {
+    // The next launch: parts of one multiplier, in queue order, under the cap.
+    const int mult = queue[head].second;
+    ids.clear();
+    roff.assign(1, 0);
+    while (head < queue.size() && queue[head].second == mult) {
+      const int32_t k = queue[head].first;
+      const int64_t r = hull_region_bytes(offsets[k + 1] - offsets[k], mult);
+      if (!ids.empty() && roff.back() + r > kHullArenaCap) break;
+      ids.push_back(k);
+      roff.push_back(roff.back() + r);
+      ++head;
+    }
     VTRY(ensure_slot(ctx, kSlotConvexHull, oArena + (size_t)roff.back()));
     char* base = slot<char>(ctx, kSlotConvexHull);
-    // Inputs are sent on every launch: a slot that grew does not keep its contents.
-    if (N) VCUDA(cudaMemcpyAsync(base + oPts, points, (size_t)N * 24, cudaMemcpyHostToDevice, st));
-    VCUDA(cudaMemcpyAsync(base + oOff, offsets, (size_t)(nparts + 1) * 8, cudaMemcpyHostToDevice, st));
+    if (base != sent_to) {  // a slot that grew does not keep its contents
+      if (N) VCUDA(cudaMemcpyAsync(base + oPts, points, (size_t)N * 24, cudaMemcpyHostToDevice, st));
+      VCUDA(cudaMemcpyAsync(base + oOff, offsets, (size_t)(nparts + 1) * 8, cudaMemcpyHostToDevice, st));
+      sent_to = base;
+    }
     VCUDA(cudaMemcpyAsync(base + oIds, ids.data(), ids.size() * 4, cudaMemcpyHostToDevice, st));
     VCUDA(cudaMemcpyAsync(base + oRoff, roff.data(), roff.size() * 8, cudaMemcpyHostToDevice, st));
     const unsigned blocks =
@@ -735,7 +752,6 @@ extern "C" int visacd_convex_hulls(visacd_ctx* ctx, const double* points, const 
     // part ran in this launch, one per part otherwise.
     if (all && N) VCUDA(cudaMemcpyAsync(tris, base + oTri, (size_t)N * 24, cudaMemcpyDeviceToHost, st));
     VCUDA(stream_wait(ctx));
-    std::vector<int32_t> again;
     for (int32_t k : ids) {
       const int s = st_now[k];
       if (s == kHullOk) {
@@ -745,7 +761,9 @@ extern "C" int visacd_convex_hulls(visacd_ctx* ctx, const double* points, const 
           VCUDA(cudaMemcpyAsync(tris + 6 * o, base + oTri + (size_t)o * 24, (size_t)cnt_now[k] * 12,
                                 cudaMemcpyDeviceToHost, st));
       } else if (s == kHullFaceCap || s == kHullPoolCap || s == kHullListCap) {
-        again.push_back(k);
+        VCHECK(mult * 4 <= kMaxHullMult, VISACD_ERR_DEVICE,
+               "convex_hulls: part %d outgrows %d times the default room", (int)k, mult);
+        queue.push_back({k, mult * 4});
       } else {
         VCUDA(stream_wait(ctx));
         set_error("convex_hulls: part %d: %s", (int)k,
@@ -756,12 +774,6 @@ extern "C" int visacd_convex_hulls(visacd_ctx* ctx, const double* points, const 
       }
     }
     VCUDA(stream_wait(ctx));
-    if (!again.empty()) {
-      VCHECK(mult * 4 <= kMaxHullMult, VISACD_ERR_DEVICE,
-             "convex_hulls: a part outgrows %d times the default capacity", mult);
-      mult *= 4;
-    }
-    ids.swap(again);
   }
   return VISACD_OK;
 }
