@@ -194,7 +194,7 @@ __global__ void fg_edt_x_kernel(const unsigned* __restrict__ near, FgParams g, f
 constexpr int kEdtThreads = 64;
 template <int AXIS>
 __global__ void __launch_bounds__(kEdtThreads) fg_edt_yz_kernel(FgParams g, int* __restrict__ d2) {
-  extern __shared__ uint32_t env[];  // [kFgMaxDim][kEdtThreads]
+  extern __shared__ uint32_t env[];  // [line length][kEdtThreads]
   const int tid = threadIdx.x;
   const int n = AXIS == 1 ? g.ny : g.nz;
   const int64_t lines = AXIS == 1 ? (int64_t)g.nx * g.nz : (int64_t)g.nx * g.ny;
@@ -336,10 +336,13 @@ int free_grid_build(visacd_ctx* ctx, visacd_bvh* b, int64_t pairs) {
     VCUDA(cudaFuncSetAttribute(fg_edt_yz_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, edt_smem));
     if (known) edt_configured[ctx->device].store(true);
   }
+  // Each pass takes the shared memory its line length needs (an envelope
+  // holds at most one parabola per cell of the line), so more blocks fit on
+  // an SM than with the 256-cell maximum.
   VLAUNCH(ctx, kKGridEdt, grid_for((int64_t)g.nx * g.nz, kEdtThreads, 8LL * ctx->sm_count), kEdtThreads,
-          edt_smem, fg_edt_yz_kernel<1>, g, d2);
+          g.ny * kEdtThreads * 4, fg_edt_yz_kernel<1>, g, d2);
   VLAUNCH(ctx, kKGridEdt, grid_for((int64_t)g.nx * g.ny, kEdtThreads, 8LL * ctx->sm_count), kEdtThreads,
-          edt_smem, fg_edt_yz_kernel<2>, g, d2);
+          g.nz * kEdtThreads * 4, fg_edt_yz_kernel<2>, g, d2);
   VLAUNCH(ctx, kKGridFinal, grid_for(cells, 256, 8LL * ctx->sm_count), 256, 0, fg_final_kernel, near, d2, cells,
           g.R, g.h, hd, lb);
   // The bounds as a 3D texture: point sampling at cell coordinate u reads
