@@ -34,7 +34,7 @@ EXPORTED = [
     "visacd_set_blocking_sync", "visacd_lp_set_tcgen05", "visacd_ctx_set_blocking_wait",
     "visacd_candidate_planes", "visacd_split_search", "visacd_visibility_batch",
     "visacd_learned_split_search", "visacd_ctx_set_vis_trace", "visacd_ctx_vis_trace_counts",
-    "visacd_ctx_set_score_k", "visacd_autotune_scoring", "visacd_convex_hulls",
+    "visacd_ctx_set_score_k", "visacd_autotune_scoring", "visacd_convex_hulls", "visacd_radix_sort_pairs",
 ]
 
 LP_POINTS = 2048
@@ -152,6 +152,7 @@ def load() -> C.CDLL:
     lib.visacd_sdf_fetch.argtypes = [P, P, P]
     lib.visacd_hull_distances.argtypes = [P, P, P, i32, P, i64, C.c_double, P]
     lib.visacd_convex_hulls.argtypes = [P, P, P, i32, i32, P, P]
+    lib.visacd_radix_sort_pairs.argtypes = [P, P, P, i32, C.c_int]
     lib.visacd_segment_triangle_tests.argtypes = [P, P, P, i64, P, C.POINTER(i64)]
     lib.visacd_set_blocking_sync.argtypes = [C.c_int, C.c_int]
     lib.visacd_lp_param_count.argtypes = []
@@ -448,6 +449,15 @@ class Context:
         _check(lib().visacd_segment_triangle_tests(self._h, _ptr(sg), _ptr(tr), len(sg), _ptr(out), C.byref(n64)),
                "visacd_segment_triangle_tests")
         return out.astype(bool), n64.value
+
+    # ---- device sort -------------------------------------------------------
+    def radix_sort_pairs(self, keys, vals, key_bits: int):
+        """Stable sort of (keys, vals) by key on the device; returns sorted copies."""
+        k = np.ascontiguousarray(np.asarray(keys, dtype=np.uint64)).copy()
+        v = np.ascontiguousarray(np.asarray(vals, dtype=np.uint32)).copy()
+        _check(lib().visacd_radix_sort_pairs(self._h, _ptr(k), _ptr(v), len(k), int(key_bits)),
+               "visacd_radix_sort_pairs")
+        return k, v
 
     # ---- convex hulls ------------------------------------------------------
     def convex_hulls(self, point_sets, fix_normals: bool = True):

@@ -469,6 +469,103 @@ __global__ void __launch_bounds__(1024) small_sort_kernel(uint64_t* __restrict__
   }
 }
 
+// Mid-size inputs (kSmallSort < n <= kMidSort) in one CTA: the same stable
+// LSD passes over 8-bit digits as below, all in one launch (instead of three
+// launches per pass). Warp w owns the contiguous run [w C, (w + 1) C) of the
+// input; per pass, per-warp digit counts give every (digit, warp) its output
+// offset (digit-major, warp-minor), and each warp scatters its run in order,
+// 32 keys at a time with match-any ranks, so the order is stable. Keys and
+// values ping-pong between the two buffer pairs in global memory (L2), plain
+// loads only (the data changes between passes within the launch).
+constexpr int kMidSort = 32768;
+
+__global__ void __launch_bounds__(1024) mid_sort_kernel(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt,
+                                                        uint32_t* vals_alt, int n, int passes) {
+  __shared__ uint32_t cnt[32][256];
+  __shared__ uint32_t dbase[256];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int chunk = (n + 31) / 32;
+  const int b0 = min(n, warp * chunk), b1 = min(n, b0 + chunk);
+  const unsigned lt = (1u << lane) - 1u;
+  uint64_t* ks = keys;
+  uint32_t* vs = vals;
+  uint64_t* kd = keys_alt;
+  uint32_t* vd = vals_alt;
+  for (int p = 0; p < passes; ++p) {
+    const int shift = 8 * p;
+    for (int d = lane; d < 256; d += 32) cnt[warp][d] = 0;
+    __syncwarp();
+    for (int i = b0 + lane; i < b1; i += 32) atomicAdd(&cnt[warp][(uint32_t)(ks[i] >> shift) & 0xffu], 1u);
+    __syncthreads();
+    if (threadIdx.x < 256) {
+      uint32_t t = 0;
+      for (int w = 0; w < 32; ++w) t += cnt[w][threadIdx.x];
+      dbase[threadIdx.x] = t;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      // Exclusive scan of the 256 digit totals: 8 consecutive digits a lane.
+      uint32_t v[8], sum = 0;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        v[k] = dbase[8 * lane + k];
+        sum += v[k];
+      }
+      uint32_t incl = sum;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+      }
+      uint32_t run = incl - sum;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        dbase[8 * lane + k] = run;
+        run += v[k];
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x < 256) {
+      uint32_t run = dbase[threadIdx.x];
+      for (int w = 0; w < 32; ++w) {
+        const uint32_t c = cnt[w][threadIdx.x];
+        cnt[w][threadIdx.x] = run;
+        run += c;
+      }
+    }
+    __syncthreads();
+    for (int base = b0; base < b1; base += 32) {
+      const int i = base + lane;
+      const bool valid = i < b1;
+      const uint64_t k = valid ? ks[i] : 0ull;
+      const uint32_t v = valid ? vs[i] : 0u;
+      const uint32_t digit = valid ? ((uint32_t)(k >> shift) & 0xffu) : 0xffffffffu;
+      const unsigned peers = __match_any_sync(0xffffffffu, digit);
+      if (valid) {
+        const uint32_t pos = cnt[warp][digit] + __popc(peers & lt);
+        kd[pos] = k;
+        vd[pos] = v;
+      }
+      __syncwarp();
+      if (valid && (peers & lt) == 0) cnt[warp][digit] += __popc(peers);
+      __syncwarp();
+    }
+    __syncthreads();
+    uint64_t* kt = ks;
+    ks = kd;
+    kd = kt;
+    uint32_t* vt = vs;
+    vs = vd;
+    vd = vt;
+  }
+  if (ks != keys) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      keys[i] = ks[i];
+      vals[i] = vs[i];
+    }
+  }
+}
+
 int radix_sort_u64(visacd_ctx* ctx, uint64_t* keys, uint32_t* vals, uint64_t* keys_alt,
                    uint32_t* vals_alt, int32_t n, int key_bits) {
   if (n <= 1) return VISACD_OK;
@@ -481,6 +578,11 @@ int radix_sort_u64(visacd_ctx* ctx, uint64_t* keys, uint32_t* vals, uint64_t* ke
     }
     const uint64_t mask = key_bits >= 64 ? ~0ull : ((1ull << key_bits) - 1);
     VLAUNCH(ctx, kKSortScatter, 1, 1024, kSmallSortSmem, small_sort_kernel, keys, vals, n, mask);
+    return VISACD_OK;
+  }
+  if (n <= kMidSort) {
+    VLAUNCH(ctx, kKSortScatter, 1, 1024, 0, mid_sort_kernel, keys, vals, keys_alt, vals_alt, n,
+            (key_bits + 7) / 8);
     return VISACD_OK;
   }
   int nblocks = (int)((n + kSortTile - 1) / kSortTile);
@@ -665,6 +767,36 @@ extern "C" int visacd_ctx_kernel_times(visacd_ctx* ctx, const char** names, doub
 
 extern "C" int64_t visacd_ctx_launch_count(const visacd_ctx* ctx) { return ctx ? ctx->launches : 0; }
 extern "C" int visacd_ctx_sm_count(const visacd_ctx* ctx) { return ctx ? ctx->sm_count : 0; }
+
+extern "C" int visacd_radix_sort_pairs(visacd_ctx* ctx, uint64_t* keys, uint32_t* vals, int32_t n, int key_bits) {
+  VCHECK(ctx && (n == 0 || (keys && vals)), VISACD_ERR_INVALID_ARG, "radix_sort_pairs: null argument");
+  VCHECK(n >= 0 && key_bits >= 1 && key_bits <= 64, VISACD_ERR_INVALID_ARG, "radix_sort_pairs: bad size");
+  if (key_bits < 64)
+    for (int32_t i = 0; i < n; ++i)
+      VCHECK(!(keys[i] >> key_bits), VISACD_ERR_INVALID_ARG, "radix_sort_pairs: key %d has bits above key_bits",
+             (int)i);
+  if (n <= 1) return VISACD_OK;
+  VCUDA(cudaSetDevice(ctx->device));
+  uint64_t* d = nullptr;
+  VCUDA(cudaMallocAsync((void**)&d, (size_t)n * 24, ctx->stream));
+  uint64_t *k0 = d, *k1 = d + n;
+  uint32_t *v0 = reinterpret_cast<uint32_t*>(d + 2 * (size_t)n), *v1 = v0 + n;
+  cudaError_t e = cudaMemcpyAsync(k0, keys, (size_t)n * 8, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(v0, vals, (size_t)n * 4, cudaMemcpyHostToDevice, ctx->stream);
+  int rc = e == cudaSuccess ? radix_sort_u64(ctx, k0, v0, k1, v1, n, key_bits) : VISACD_ERR_CUDA;
+  if (rc == VISACD_OK) {
+    e = cudaMemcpyAsync(keys, k0, (size_t)n * 8, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(vals, v0, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e != cudaSuccess) rc = VISACD_ERR_CUDA;
+  }
+  cudaFreeAsync(d, ctx->stream);
+  const cudaError_t w = cudaStreamSynchronize(ctx->stream);
+  if (rc == VISACD_OK && (e != cudaSuccess || w != cudaSuccess)) {
+    set_error("radix_sort_pairs: %s", cudaGetErrorString(e != cudaSuccess ? e : w));
+    rc = VISACD_ERR_CUDA;
+  }
+  return rc;
+}
 
 extern "C" int visacd_set_blocking_sync(int device, int blocking) {
   VCUDA(cudaSetDevice(device));
