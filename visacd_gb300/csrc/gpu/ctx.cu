@@ -472,21 +472,17 @@ __global__ void __launch_bounds__(1024) small_sort_kernel(uint64_t* __restrict__
 // Mid-size inputs (kSmallSort < n <= kMidSort) in one CTA: the same stable
 // LSD passes over 8-bit digits as below, all in one launch (instead of three
 // launches per pass). Warp w owns the contiguous run [w C, (w + 1) C) of the
-// input; per pass the run's keys are staged in shared memory (one coalesced
-// load), per-warp digit counts give every (digit, warp) its output offset
-// (digit-major, warp-minor), and each warp scatters its run in order, 32 keys
-// at a time with match-any ranks, so the order is stable. Keys and values
-// ping-pong between the two buffer pairs in global memory (L2), plain loads
-// only (the data changes between passes within the launch).
-constexpr int kMidSort = 24576;
-constexpr size_t kMidSortSmem = (size_t)kMidSort * 8 + 32 * 256 * 4 + 256 * 4;
+// input; per pass, per-warp digit counts give every (digit, warp) its output
+// offset (digit-major, warp-minor), and each warp scatters its run in order,
+// 32 keys at a time with match-any ranks, so the order is stable. Keys and
+// values ping-pong between the two buffer pairs in global memory (L2), plain
+// loads only (the data changes between passes within the launch).
+constexpr int kMidSort = 32768;
 
 __global__ void __launch_bounds__(1024) mid_sort_kernel(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt,
                                                         uint32_t* vals_alt, int n, int passes) {
-  extern __shared__ __align__(16) unsigned char ms_raw[];
-  uint64_t* sk = reinterpret_cast<uint64_t*>(ms_raw);                              // [kMidSort]
-  uint32_t (*cnt)[256] = reinterpret_cast<uint32_t (*)[256]>(ms_raw + (size_t)kMidSort * 8);  // [32][256]
-  uint32_t* dbase = reinterpret_cast<uint32_t*>(ms_raw + (size_t)kMidSort * 8 + 32 * 256 * 4);
+  __shared__ uint32_t cnt[32][256];
+  __shared__ uint32_t dbase[256];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int chunk = (n + 31) / 32;
   const int b0 = min(n, warp * chunk), b1 = min(n, b0 + chunk);
@@ -498,9 +494,8 @@ __global__ void __launch_bounds__(1024) mid_sort_kernel(uint64_t* keys, uint32_t
   for (int p = 0; p < passes; ++p) {
     const int shift = 8 * p;
     for (int d = lane; d < 256; d += 32) cnt[warp][d] = 0;
-    for (int i = b0 + lane; i < b1; i += 32) sk[i] = ks[i];
     __syncwarp();
-    for (int i = b0 + lane; i < b1; i += 32) atomicAdd(&cnt[warp][(uint32_t)(sk[i] >> shift) & 0xffu], 1u);
+    for (int i = b0 + lane; i < b1; i += 32) atomicAdd(&cnt[warp][(uint32_t)(ks[i] >> shift) & 0xffu], 1u);
     __syncthreads();
     if (threadIdx.x < 256) {
       uint32_t t = 0;
@@ -542,7 +537,7 @@ __global__ void __launch_bounds__(1024) mid_sort_kernel(uint64_t* keys, uint32_t
     for (int base = b0; base < b1; base += 32) {
       const int i = base + lane;
       const bool valid = i < b1;
-      const uint64_t k = valid ? sk[i] : 0ull;
+      const uint64_t k = valid ? ks[i] : 0ull;
       const uint32_t v = valid ? vs[i] : 0u;
       const uint32_t digit = valid ? ((uint32_t)(k >> shift) & 0xffu) : 0xffffffffu;
       const unsigned peers = __match_any_sync(0xffffffffu, digit);
@@ -586,13 +581,7 @@ int radix_sort_u64(visacd_ctx* ctx, uint64_t* keys, uint32_t* vals, uint64_t* ke
     return VISACD_OK;
   }
   if (n <= kMidSort) {
-    static std::atomic<bool> mid_attr_set[64];
-    if (ctx->device < 0 || ctx->device >= 64 || !mid_attr_set[ctx->device].load()) {
-      VCUDA(cudaFuncSetAttribute(mid_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)kMidSortSmem));
-      if (ctx->device >= 0 && ctx->device < 64) mid_attr_set[ctx->device].store(true);
-    }
-    VLAUNCH(ctx, kKSortScatter, 1, 1024, kMidSortSmem, mid_sort_kernel, keys, vals, keys_alt, vals_alt, n,
+    VLAUNCH(ctx, kKSortScatter, 1, 1024, 0, mid_sort_kernel, keys, vals, keys_alt, vals_alt, n,
             (key_bits + 7) / 8);
     return VISACD_OK;
   }
