@@ -414,10 +414,20 @@ void bvh_detach(visacd_bvh* b) {
   if (b->nodes) cudaFreeAsync(b->nodes, b->stream);
   if (b->tris) cudaFreeAsync(b->tris, b->stream);
   if (b->free_lb) cudaFreeAsync(b->free_lb, b->stream);
-  if (b->free_tex) cudaDestroyTextureObject(b->free_tex);
-  if (b->free_arr) {
-    cudaStreamSynchronize(b->stream);  // a queued walk may still read it
-    cudaFreeArray(b->free_arr);
+  if (b->free_arr && b->ctx && !b->ctx->grid_arr) {
+    // Kept on the context for the next grid of this size: work queued on the
+    // context's stream reads it before any later copy into it.
+    b->ctx->grid_arr = b->free_arr;
+    b->ctx->grid_tex = b->free_tex;
+    b->ctx->grid_dims[0] = b->fg_nx;
+    b->ctx->grid_dims[1] = b->fg_ny;
+    b->ctx->grid_dims[2] = b->fg_nz;
+  } else {
+    if (b->free_tex) cudaDestroyTextureObject(b->free_tex);
+    if (b->free_arr) {
+      cudaStreamSynchronize(b->stream);  // a queued walk may still read it
+      cudaFreeArray(b->free_arr);
+    }
   }
   b->free_tex = 0;
   b->free_arr = nullptr;

@@ -147,6 +147,12 @@ struct visacd_ctx {
   visacd_clip_result clip_out{};                  // last clip result (device-resident)
   std::vector<visacd_bvh*> bvhs;                  // live BVHs built on this context
   std::vector<visacd_lp*> lps;                    // live proposers made on this context
+  // The last free-space grid's 3D array and texture, kept when its BVH goes
+  // so that the next grid of the same size reuses them (no allocation and no
+  // wait for the walks still queued on this context's stream).
+  cudaArray_t grid_arr = nullptr;
+  cudaTextureObject_t grid_tex = 0;
+  int grid_dims[3] = {0, 0, 0};
   bool vis_trace = true;                          // free-space walks before the cage BVH
   int64_t last_vis_certified = 0, last_vis_trace_steps = 0;  // of the last visibility call
   int clip_nv = 0;

@@ -685,6 +685,10 @@ extern "C" int visacd_ctx_destroy(visacd_ctx* ctx) {
   // BVHs still alive lose their device memory with their context.
   for (visacd_bvh* b : ctx->bvhs) bvh_detach(b);
   ctx->bvhs.clear();
+  if (ctx->grid_tex) cudaDestroyTextureObject(ctx->grid_tex);
+  if (ctx->grid_arr) cudaFreeArray(ctx->grid_arr);
+  ctx->grid_tex = 0;
+  ctx->grid_arr = nullptr;
   // So do proposers: destroying one afterwards only frees its host side.
   for (visacd_lp* lp : ctx->lps) lp_detach(lp);
   ctx->lps.clear();

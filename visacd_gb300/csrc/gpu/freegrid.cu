@@ -350,17 +350,31 @@ int free_grid_build(visacd_ctx* ctx, visacd_bvh* b, int64_t pairs) {
   // (in 3D) in the same cache lines; reads outside the grid return 0 (the
   // border), which stops a walk.
   {
-    cudaChannelFormatDesc fd = cudaCreateChannelDesc<float>();
+    // The context's kept array and texture when the size matches; a kept one
+    // of another size goes (after the work that may still read it).
     cudaArray_t arr = nullptr;
-    VCUDA(cudaMalloc3DArray(&arr, &fd, make_cudaExtent(g.nx, g.ny, g.nz)));
+    cudaTextureObject_t tex = 0;
+    if (ctx->grid_arr && ctx->grid_dims[0] == g.nx && ctx->grid_dims[1] == g.ny && ctx->grid_dims[2] == g.nz) {
+      arr = ctx->grid_arr;
+      tex = ctx->grid_tex;
+    } else if (ctx->grid_arr) {
+      cudaDestroyTextureObject(ctx->grid_tex);
+      VCUDA(stream_wait(ctx));
+      cudaFreeArray(ctx->grid_arr);
+    }
+    ctx->grid_arr = nullptr;
+    ctx->grid_tex = 0;
+    if (!arr) {
+      cudaChannelFormatDesc fd = cudaCreateChannelDesc<float>();
+      VCUDA(cudaMalloc3DArray(&arr, &fd, make_cudaExtent(g.nx, g.ny, g.nz)));
+    }
     cudaMemcpy3DParms cp = {};
     cp.srcPtr = make_cudaPitchedPtr(lb, (size_t)g.nx * sizeof(float), g.nx, g.ny);
     cp.dstArray = arr;
     cp.extent = make_cudaExtent(g.nx, g.ny, g.nz);
     cp.kind = cudaMemcpyDeviceToDevice;
     cudaError_t e = cudaMemcpy3DAsync(&cp, ctx->stream);
-    cudaTextureObject_t tex = 0;
-    if (e == cudaSuccess) {
+    if (e == cudaSuccess && !tex) {
       cudaResourceDesc rd = {};
       rd.resType = cudaResourceTypeArray;
       rd.res.array.array = arr;
@@ -373,6 +387,8 @@ int free_grid_build(visacd_ctx* ctx, visacd_bvh* b, int64_t pairs) {
       e = cudaCreateTextureObject(&tex, &rd, &td, nullptr);
     }
     if (e != cudaSuccess) {
+      if (tex) cudaDestroyTextureObject(tex);
+      cudaStreamSynchronize(ctx->stream);
       cudaFreeArray(arr);
       set_error("free_grid_build: %s", cudaGetErrorString(e));
       return VISACD_ERR_CUDA;
