@@ -329,3 +329,27 @@ def test_free_space_walk_edge_cases(ctx, case):
     if case == "degenerate_cage":
         assert cleared > 0.5 * s1["pairs_tested"]
     print(f"{case}: {s1['pairs_tested']} pairs, {len(e1)} edges, {cleared} cleared, {reads} grid reads")
+
+
+def test_free_space_grid_reused_for_the_next_cage(ctx):
+    """A context keeps the last grid's 3D array for the next grid of the same
+    size: a cage moved by a small offset (same extent, same grid size, other
+    bounds) built after the first cage's BVH is gone must walk on its own
+    bounds, so its edges equal those with the walk off."""
+    v, t = mg.displaced_blob(5, seed=2026)
+    cv, ct = mg.offset_cage(v, t, 0.03)
+    sb = ctx.bvh(v, t)
+    out = []
+    for shift in (0.0, 0.02):
+        cb = ctx.bvh(cv + np.array([shift, -shift, 0.5 * shift]), ct)
+        ctx.set_vis_trace(True)
+        e1, s1 = ctx.visibility(v, sb, cb)
+        cleared, _ = ctx.vis_trace_counts()
+        ctx.set_vis_trace(False)
+        e0, s0 = ctx.visibility(v, sb, cb)
+        ctx.set_vis_trace(True)
+        np.testing.assert_array_equal(e0, e1)
+        assert s0["n_edges"] == s1["n_edges"] and cleared > 0
+        out.append(len(e1))
+        cb.close()
+    assert out[0] != out[1]  # the moved cage gives other edges
