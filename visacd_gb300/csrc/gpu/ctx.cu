@@ -469,20 +469,27 @@ __global__ void __launch_bounds__(1024) small_sort_kernel(uint64_t* __restrict__
   }
 }
 
-// Mid-size inputs (kSmallSort < n <= kMidSort) in one CTA: the same stable
-// LSD passes over 8-bit digits as below, all in one launch (instead of three
-// launches per pass). Warp w owns the contiguous run [w C, (w + 1) C) of the
-// input; per pass, per-warp digit counts give every (digit, warp) its output
-// offset (digit-major, warp-minor), and each warp scatters its run in order,
-// 32 keys at a time with match-any ranks, so the order is stable. Keys and
-// values ping-pong between the two buffer pairs in global memory (L2), plain
-// loads only (the data changes between passes within the launch).
+// Mid-size inputs (kSmallSort < n <= kMidSort) in one CTA: stable LSD passes
+// over 10-bit digits (a stable sort on the same key bits, so the same order
+// as the multi-launch path), all in one launch instead of three launches per
+// pass. Warp w owns the contiguous run [w C, (w + 1) C) of the input; per
+// pass, per-warp digit counts give every (digit, warp) its output offset
+// (digit-major, warp-minor), and each warp scatters its run in order, 32 keys
+// at a time with match-any ranks (the next 32 loaded while one group is
+// placed), so the order is stable. Keys and values ping-pong between the two
+// buffer pairs in global memory (L2), plain loads only (the data changes
+// between passes within the launch).
 constexpr int kMidSort = 32768;
+constexpr int kMidDigitBits = 10;
+constexpr int kMidDigits = 1 << kMidDigitBits;
+constexpr size_t kMidSortSmem = (size_t)32 * kMidDigits * 4 + (size_t)kMidDigits * 4 + 32 * 4;
 
 __global__ void __launch_bounds__(1024) mid_sort_kernel(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt,
                                                         uint32_t* vals_alt, int n, int passes) {
-  __shared__ uint32_t cnt[32][256];
-  __shared__ uint32_t dbase[256];
+  extern __shared__ __align__(16) uint32_t ms_smem[];
+  uint32_t* cnt = ms_smem;                          // [32][kMidDigits]
+  uint32_t* dbase = ms_smem + 32 * kMidDigits;      // [kMidDigits]
+  uint32_t* wsum = dbase + kMidDigits;              // [32]
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int chunk = (n + 31) / 32;
   const int b0 = min(n, warp * chunk), b1 = min(n, b0 + chunk);
@@ -491,63 +498,70 @@ __global__ void __launch_bounds__(1024) mid_sort_kernel(uint64_t* keys, uint32_t
   uint32_t* vs = vals;
   uint64_t* kd = keys_alt;
   uint32_t* vd = vals_alt;
+  uint32_t* my = cnt + warp * kMidDigits;
   for (int p = 0; p < passes; ++p) {
-    const int shift = 8 * p;
-    for (int d = lane; d < 256; d += 32) cnt[warp][d] = 0;
+    const int shift = kMidDigitBits * p;
+    for (int d = lane; d < kMidDigits; d += 32) my[d] = 0;
     __syncwarp();
-    for (int i = b0 + lane; i < b1; i += 32) atomicAdd(&cnt[warp][(uint32_t)(ks[i] >> shift) & 0xffu], 1u);
+    for (int i = b0 + lane; i < b1; i += 32)
+      atomicAdd(&my[(uint32_t)(ks[i] >> shift) & (kMidDigits - 1)], 1u);
     __syncthreads();
-    if (threadIdx.x < 256) {
-      uint32_t t = 0;
-      for (int w = 0; w < 32; ++w) t += cnt[w][threadIdx.x];
-      dbase[threadIdx.x] = t;
-    }
-    __syncthreads();
-    if (threadIdx.x < 32) {
-      // Exclusive scan of the 256 digit totals: 8 consecutive digits a lane.
-      uint32_t v[8], sum = 0;
+    // Digit totals, then their exclusive scan (thread d holds digit d).
+    const int d = threadIdx.x;
+    uint32_t tot = 0;
+    for (int w = 0; w < 32; ++w) tot += cnt[w * kMidDigits + d];
+    uint32_t incl = tot;
 #pragma unroll
-      for (int k = 0; k < 8; ++k) {
-        v[k] = dbase[8 * lane + k];
-        sum += v[k];
-      }
-      uint32_t incl = sum;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    if (lane == 31) wsum[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+      const uint32_t x = wsum[lane];
+      uint32_t xi = x;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += y;
+        const uint32_t y = __shfl_up_sync(0xffffffffu, xi, o);
+        if (lane >= o) xi += y;
       }
-      uint32_t run = incl - sum;
-#pragma unroll
-      for (int k = 0; k < 8; ++k) {
-        dbase[8 * lane + k] = run;
-        run += v[k];
-      }
+      wsum[lane] = xi - x;
     }
     __syncthreads();
-    if (threadIdx.x < 256) {
-      uint32_t run = dbase[threadIdx.x];
+    {
+      uint32_t run = wsum[warp] + incl - tot;
       for (int w = 0; w < 32; ++w) {
-        const uint32_t c = cnt[w][threadIdx.x];
-        cnt[w][threadIdx.x] = run;
+        const uint32_t c = cnt[w * kMidDigits + d];
+        cnt[w * kMidDigits + d] = run;
         run += c;
       }
     }
     __syncthreads();
+    uint64_t kn = 0;
+    uint32_t vn = 0;
+    if (b0 + lane < b1) {
+      kn = ks[b0 + lane];
+      vn = vs[b0 + lane];
+    }
     for (int base = b0; base < b1; base += 32) {
       const int i = base + lane;
       const bool valid = i < b1;
-      const uint64_t k = valid ? ks[i] : 0ull;
-      const uint32_t v = valid ? vs[i] : 0u;
-      const uint32_t digit = valid ? ((uint32_t)(k >> shift) & 0xffu) : 0xffffffffu;
+      const uint64_t k = kn;
+      const uint32_t v = vn;
+      if (i + 32 < b1) {
+        kn = ks[i + 32];
+        vn = vs[i + 32];
+      }
+      const uint32_t digit = valid ? ((uint32_t)(k >> shift) & (kMidDigits - 1)) : 0xffffffffu;
       const unsigned peers = __match_any_sync(0xffffffffu, digit);
       if (valid) {
-        const uint32_t pos = cnt[warp][digit] + __popc(peers & lt);
+        const uint32_t pos = my[digit] + __popc(peers & lt);
         kd[pos] = k;
         vd[pos] = v;
       }
       __syncwarp();
-      if (valid && (peers & lt) == 0) cnt[warp][digit] += __popc(peers);
+      if (valid && (peers & lt) == 0) my[digit] += __popc(peers);
       __syncwarp();
     }
     __syncthreads();
@@ -581,8 +595,14 @@ int radix_sort_u64(visacd_ctx* ctx, uint64_t* keys, uint32_t* vals, uint64_t* ke
     return VISACD_OK;
   }
   if (n <= kMidSort) {
-    VLAUNCH(ctx, kKSortScatter, 1, 1024, 0, mid_sort_kernel, keys, vals, keys_alt, vals_alt, n,
-            (key_bits + 7) / 8);
+    static std::atomic<bool> mid_attr_set[64];
+    if (ctx->device < 0 || ctx->device >= 64 || !mid_attr_set[ctx->device].load()) {
+      VCUDA(cudaFuncSetAttribute(mid_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kMidSortSmem));
+      if (ctx->device >= 0 && ctx->device < 64) mid_attr_set[ctx->device].store(true);
+    }
+    VLAUNCH(ctx, kKSortScatter, 1, 1024, kMidSortSmem, mid_sort_kernel, keys, vals, keys_alt, vals_alt, n,
+            (key_bits + kMidDigitBits - 1) / kMidDigitBits);
     return VISACD_OK;
   }
   int nblocks = (int)((n + kSortTile - 1) / kSortTile);
