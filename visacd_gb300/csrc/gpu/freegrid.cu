@@ -190,7 +190,9 @@ __global__ void fg_edt_x_kernel(const unsigned* __restrict__ near, FgParams g, f
 // line per thread. The envelope's parabolas live in shared memory, one column
 // per thread, packed as (f << 8) | p (f < 2^24, p < 256); breakpoints are
 // compared exactly by cross-multiplying their integer numerators and
-// denominators.
+// denominators. 32-bit arithmetic is exact here: finite values are squared
+// cell distances of at most 3 x 255^2 < 2^18, so h = f + p^2 < 2^19 and every
+// cross product stays below 2^27.
 constexpr int kEdtThreads = 64;
 template <int AXIS>
 __global__ void __launch_bounds__(kEdtThreads) fg_edt_yz_kernel(FgParams g, int* __restrict__ d2) {
@@ -214,15 +216,15 @@ __global__ void __launch_bounds__(kEdtThreads) fg_edt_yz_kernel(FgParams g, int*
       for (int u = 1; u < 8; ++u)
         if ((q & 7) == u) fq = buf[u];
       if (fq >= kFgInf) continue;
-      const long long hq = (long long)fq + (long long)q * q;
+      const int hq = fq + q * q;
       while (k >= 1) {
         const uint32_t e0 = env[(k - 1) * kEdtThreads + tid], e1 = env[k * kEdtThreads + tid];
         const int v0 = (int)(e0 & 255u), v1 = (int)(e1 & 255u);
-        const long long h0 = (long long)(e0 >> 8) + (long long)v0 * v0;
-        const long long h1 = (long long)(e1 >> 8) + (long long)v1 * v1;
+        const int h0 = (int)(e0 >> 8) + v0 * v0;
+        const int h1 = (int)(e1 >> 8) + v1 * v1;
         // Drop v1 when the new parabola's breakpoint with it lies at or
         // before v1's own breakpoint with v0.
-        if ((hq - h1) * (long long)(v1 - v0) <= (h1 - h0) * (long long)(q - v1)) --k;
+        if ((hq - h1) * (v1 - v0) <= (h1 - h0) * (q - v1)) --k;
         else break;
       }
       ++k;
@@ -234,15 +236,15 @@ __global__ void __launch_bounds__(kEdtThreads) fg_edt_yz_kernel(FgParams g, int*
       while (j < k) {
         const uint32_t e0 = env[j * kEdtThreads + tid], e1 = env[(j + 1) * kEdtThreads + tid];
         const int v0 = (int)(e0 & 255u), v1 = (int)(e1 & 255u);
-        const long long h0 = (long long)(e0 >> 8) + (long long)v0 * v0;
-        const long long h1 = (long long)(e1 >> 8) + (long long)v1 * v1;
-        if (h1 - h0 < 2LL * q * (v1 - v0)) ++j;
+        const int h0 = (int)(e0 >> 8) + v0 * v0;
+        const int h1 = (int)(e1 >> 8) + v1 * v1;
+        if (h1 - h0 < 2 * q * (v1 - v0)) ++j;
         else break;
       }
       const uint32_t e = env[j * kEdtThreads + tid];
-      const long long dq = (long long)(q - (int)(e & 255u));
-      const long long val = dq * dq + (long long)(e >> 8);
-      d2[base + q * stride] = val >= kFgInf ? kFgInf : (int)val;
+      const int dq = q - (int)(e & 255u);
+      const int val = dq * dq + (int)(e >> 8);
+      d2[base + q * stride] = val >= kFgInf ? kFgInf : val;
     }
   }
 }
