@@ -469,10 +469,9 @@ __global__ void __launch_bounds__(1024) small_sort_kernel(uint64_t* __restrict__
   }
 }
 
-// Mid-size inputs (kSmallSort < n <= kMidSort) in one CTA: stable LSD passes
-// over 10-bit digits (a stable sort on the same key bits, so the same order
-// as the multi-launch path), all in one launch instead of three launches per
-// pass. Warp w owns the contiguous run [w C, (w + 1) C) of the input; per
+// Mid-size inputs (kSmallSort < n <= kMidSort) in one CTA: the same stable
+// LSD passes over 8-bit digits as below, all in one launch instead of three
+// launches per pass. Warp w owns the contiguous run [w C, (w + 1) C) of the input; per
 // pass, per-warp digit counts give every (digit, warp) its output offset
 // (digit-major, warp-minor), and each warp scatters its run in order, 32 keys
 // at a time with match-any ranks (the next 32 loaded while one group is
@@ -480,16 +479,15 @@ __global__ void __launch_bounds__(1024) small_sort_kernel(uint64_t* __restrict__
 // buffer pairs in global memory (L2), plain loads only (the data changes
 // between passes within the launch).
 constexpr int kMidSort = 32768;
-constexpr int kMidDigitBits = 10;
+constexpr int kMidDigitBits = 8;  // 10-bit digits measured slower (per-pass fixed cost)
 constexpr int kMidDigits = 1 << kMidDigitBits;
-constexpr size_t kMidSortSmem = (size_t)32 * kMidDigits * 4 + (size_t)kMidDigits * 4 + 32 * 4;
+constexpr size_t kMidSortSmem = (size_t)32 * kMidDigits * 4 + 32 * 4;
 
 __global__ void __launch_bounds__(1024) mid_sort_kernel(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt,
                                                         uint32_t* vals_alt, int n, int passes) {
   extern __shared__ __align__(16) uint32_t ms_smem[];
   uint32_t* cnt = ms_smem;                          // [32][kMidDigits]
-  uint32_t* dbase = ms_smem + 32 * kMidDigits;      // [kMidDigits]
-  uint32_t* wsum = dbase + kMidDigits;              // [32]
+  uint32_t* wsum = ms_smem + 32 * kMidDigits;       // [32]
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int chunk = (n + 31) / 32;
   const int b0 = min(n, warp * chunk), b1 = min(n, b0 + chunk);
@@ -507,29 +505,32 @@ __global__ void __launch_bounds__(1024) mid_sort_kernel(uint64_t* keys, uint32_t
       atomicAdd(&my[(uint32_t)(ks[i] >> shift) & (kMidDigits - 1)], 1u);
     __syncthreads();
     // Digit totals, then their exclusive scan (thread d holds digit d).
+    constexpr int kDigitWarps = kMidDigits / 32;
     const int d = threadIdx.x;
-    uint32_t tot = 0;
-    for (int w = 0; w < 32; ++w) tot += cnt[w * kMidDigits + d];
-    uint32_t incl = tot;
+    uint32_t tot = 0, incl = 0;
+    if (warp < kDigitWarps) {
+      for (int w = 0; w < 32; ++w) tot += cnt[w * kMidDigits + d];
+      incl = tot;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += y;
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+      }
+      if (lane == 31) wsum[warp] = incl;
     }
-    if (lane == 31) wsum[warp] = incl;
     __syncthreads();
     if (warp == 0) {
-      const uint32_t x = wsum[lane];
+      const uint32_t x = lane < kDigitWarps ? wsum[lane] : 0u;
       uint32_t xi = x;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
         const uint32_t y = __shfl_up_sync(0xffffffffu, xi, o);
         if (lane >= o) xi += y;
       }
-      wsum[lane] = xi - x;
+      if (lane < kDigitWarps) wsum[lane] = xi - x;
     }
     __syncthreads();
-    {
+    if (warp < kDigitWarps) {
       uint32_t run = wsum[warp] + incl - tot;
       for (int w = 0; w < 32; ++w) {
         const uint32_t c = cnt[w * kMidDigits + d];
