@@ -117,7 +117,7 @@ int64_t visacd_ctx_launch_count(const visacd_ctx* ctx);
 int visacd_ctx_sm_count(const visacd_ctx* ctx);
 /* The device sort the BVH build and the visibility ordering use: a stable
    sort of (keys[i], vals[i]) by key (keys below 2^key_bits), host arrays
-   sorted in place. Up to 4096 pairs: a bitonic sort in one CTA's shared
+   sorted in place. Up to 512 pairs: a bitonic sort in one CTA's shared
    memory; up to 32768: one CTA running every 8-bit LSD pass; beyond: three
    launches per pass. Synchronizes. */
 int visacd_radix_sort_pairs(visacd_ctx* ctx, uint64_t* keys, uint32_t* vals, int32_t n, int key_bits);

@@ -1,4 +1,4 @@
-"""The device sort (visacd_radix_sort_pairs: bitonic in one CTA up to 4096
+"""The device sort (visacd_radix_sort_pairs: bitonic in one CTA up to 512
 pairs, one CTA running every LSD pass up to 32768, three launches per pass
 beyond) against numpy's stable sort, across the size boundaries, with many
 equal keys (stability) and keys of every width the Morton orders use."""
@@ -8,7 +8,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("n", [2, 3, 100, 4095, 4096, 4097, 10242, 20480, 32767, 32768, 32769, 100003])
+@pytest.mark.parametrize("n", [2, 3, 100, 511, 512, 513, 2000, 4096, 10242, 20480, 32767, 32768, 32769, 100003])
 @pytest.mark.parametrize("key_bits", [30, 63])
 def test_radix_sort_pairs_is_a_stable_sort(ctx, n, key_bits):
     rng = np.random.default_rng(n + key_bits)
