@@ -12,6 +12,8 @@
 //  6. node_layout: traversal records of 64 bytes (both child boxes with each
 //     axis stored as a (lo, hi) pair for packed f32x2 slab tests, + child ids)
 //     and leaf triangles of 48 bytes (3 vertices, vertex ids in .w).
+#include <atomic>
+
 #include "bvh.cuh"
 
 namespace vgpu {
@@ -256,6 +258,57 @@ __global__ void fit_kernel(const int2* __restrict__ child, const int* __restrict
   }
 }
 
+// The same fit for trees of up to kFitSmallMax leaves in one CTA: the
+// topology (children, parents), the internal boxes, heights and arrival
+// counters live in shared memory, so a level costs shared-memory latency
+// instead of L2 round trips; the boxes go to global memory at the end. Boxes
+// are minima and maxima of the children's, so they equal fit_kernel's.
+constexpr int kFitSmallMax = 4096;
+constexpr size_t kFitSmallBytesPerNode = 6 * 4 + 4 + 4 + 8 + 4;
+
+__global__ void __launch_bounds__(1024) fit_small_kernel(const int2* __restrict__ child,
+                                                         const int* __restrict__ parent_int,
+                                                         const int* __restrict__ parent_leaf,
+                                                         const float* __restrict__ leafbox,
+                                                         float* __restrict__ nodebox, int32_t n,
+                                                         BuildCounters* __restrict__ c) {
+  extern __shared__ __align__(16) unsigned char fit_smem[];
+  const int ni = n - 1;
+  int2* ch_s = reinterpret_cast<int2*>(fit_smem);
+  float* nb = reinterpret_cast<float*>(ch_s + ni);
+  unsigned* vis = reinterpret_cast<unsigned*>(nb + 6 * ni);
+  int* hgt = reinterpret_cast<int*>(vis + ni);
+  int* par = hgt + ni;
+  for (int i = threadIdx.x; i < ni; i += blockDim.x) {
+    ch_s[i] = child[i];
+    par[i] = parent_int[i];
+    vis[i] = 0u;
+  }
+  __syncthreads();
+  for (int s = threadIdx.x; s < n; s += blockDim.x) {
+    int node = parent_leaf[s];
+    for (int guard = 0; node >= 0 && guard < n + 1; ++guard) {
+      __threadfence_block();
+      if (atomicAdd(&vis[node], 1u) == 0u) break;
+      __threadfence_block();
+      const int2 ch = ch_s[node];
+      const int h = 1 + max(ch.x < 0 ? 0 : hgt[ch.x], ch.y < 0 ? 0 : hgt[ch.y]);
+      hgt[node] = h;
+      if (node == 0) atomicMax(&c->depth, h);
+      const float* lb = ch.x < 0 ? &leafbox[6 * (int64_t)(~ch.x)] : &nb[6 * ch.x];
+      const float* rb = ch.y < 0 ? &leafbox[6 * (int64_t)(~ch.y)] : &nb[6 * ch.y];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        nb[6 * node + a] = fminf(lb[a], rb[a]);
+        nb[6 * node + 3 + a] = fmaxf(lb[3 + a], rb[3 + a]);
+      }
+      node = par[node];
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < 6 * ni; i += blockDim.x) nodebox[i] = nb[i];
+}
+
 __global__ void node_layout_kernel(const int2* __restrict__ child,
                                    const float* __restrict__ leafbox,
                                    const float* __restrict__ nodebox, int32_t n_internal,
@@ -387,8 +440,19 @@ int bvh_build(visacd_ctx* ctx, const float* verts, int32_t nv, const uint32_t* t
   } else {
     const unsigned gi = grid_for(n_int, 256, 8LL * ctx->sm_count);
     VLAUNCH(ctx, kKKarras, gi, 256, 0, karras_kernel, keys, nt, child, pint, pleaf);
-    VLAUNCH(ctx, kKFit, g, 256, 0, fit_kernel, child, pint, pleaf, leafbox, nodebox, visits, height, nt,
+    if (nt <= kFitSmallMax) {
+      const size_t fit_smem = (size_t)n_int * kFitSmallBytesPerNode;
+      static std::atomic<bool> fit_attr_set[64];
+      if (ctx->device < 0 || ctx->device >= 64 || !fit_attr_set[ctx->device].load()) {
+        VCUDA(cudaFuncSetAttribute(fit_small_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)(kFitSmallMax * kFitSmallBytesPerNode)));
+        if (ctx->device >= 0 && ctx->device < 64) fit_attr_set[ctx->device].store(true);
+      }
+      VLAUNCH(ctx, kKFit, 1, 1024, fit_smem, fit_small_kernel, child, pint, pleaf, leafbox, nodebox, nt, cnt);
+    } else {
+      VLAUNCH(ctx, kKFit, g, 256, 0, fit_kernel, child, pint, pleaf, leafbox, nodebox, visits, height, nt,
             cnt);
+    }
     VLAUNCH(ctx, kKNodeLayout, gi, 256, 0, node_layout_kernel, child, leafbox, nodebox, n_int,
             b->nodes);
   }
