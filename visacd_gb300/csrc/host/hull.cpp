@@ -15,12 +15,14 @@ namespace visacd {
 
 namespace {
 
+// A face; its outside set is the segment [out, out + nout) of the hull's
+// append-only pool (each face's set is written once, when the face is made).
 struct Face {
   int v[3];
   int nb[3];  // neighbour across edge (v[e], v[(e+1)%3])
   Vec3 n;
   double off;
-  std::vector<int> outside;
+  int out = 0, nout = 0;
   bool alive = true;
   int visit = -1;
 };
@@ -28,6 +30,7 @@ struct Face {
 struct Hull {
   const std::vector<Vec3>& P;
   std::vector<Face> F;
+  std::vector<int> pool;
   double eps;
   explicit Hull(const std::vector<Vec3>& p) : P(p) {}
 
@@ -41,10 +44,42 @@ struct Hull {
     double l = norm(n);
     f.n = l > 0 ? n / l : Vec3{0, 0, 0};
     f.off = dot(f.n, P[a]);
-    F.push_back(std::move(f));
+    F.push_back(f);
     return (int)F.size() - 1;
   }
   double dist(int f, int p) const { return dot(F[f].n, P[p]) - F[f].off; }
+  // Each of pts goes to the first of the faces f0..f0+L-1 with the largest
+  // distance above eps (or nowhere); every face's set is then appended to the
+  // pool in point order. best is scratch.
+  void assign(const int* pts, int m, int f0, int L, std::vector<int>& best) {
+    best.resize(m);
+    for (int q = 0; q < L; ++q) F[f0 + q].nout = 0;
+    for (int k = 0; k < m; ++k) {
+      int bf = -1;
+      double bd = eps;
+      for (int q = 0; q < L; ++q) {
+        const double d = dist(f0 + q, pts[k]);
+        if (d > bd) {
+          bd = d;
+          bf = q;
+        }
+      }
+      best[k] = bf;
+      if (bf >= 0) ++F[f0 + bf].nout;
+    }
+    int top = (int)pool.size();
+    for (int q = 0; q < L; ++q) {
+      F[f0 + q].out = top;
+      top += F[f0 + q].nout;
+      F[f0 + q].nout = 0;
+    }
+    pool.resize(top);
+    for (int k = 0; k < m; ++k)
+      if (best[k] >= 0) {
+        Face& f = F[f0 + best[k]];
+        pool[f.out + f.nout++] = pts[k];
+      }
+  }
 };
 
 void link(std::vector<Face>& F, int f, int a, int b, int g) {
@@ -135,29 +170,27 @@ Mesh convex_hull(const std::vector<Vec3>& pts, bool fix_normals) {
   (void)f1;
   (void)f2;
   (void)f3;
-  for (int i = 0; i < n; ++i) {
-    if (i == i0 || i == i1 || i == i2 || i == i3) continue;
-    int bf = -1;
-    double bd = eps;
-    for (int f = 0; f < 4; ++f) {
-      double d = H.dist(f, i);
-      if (d > bd) {
-        bd = d;
-        bf = f;
-      }
-    }
-    if (bf >= 0) F[bf].outside.push_back(i);
+  H.F.reserve((size_t)8 * n + 64);
+  H.pool.reserve((size_t)4 * n + 64);
+  std::vector<int> choice, orphans, stack, visible, nf;
+  {
+    std::vector<int> rest;
+    rest.reserve(n);
+    for (int i = 0; i < n; ++i)
+      if (i != i0 && i != i1 && i != i2 && i != i3) rest.push_back(i);
+    H.assign(rest.data(), (int)rest.size(), 0, 4, choice);
   }
-  std::vector<int> stack, visible;
-  std::vector<std::pair<int, int>> horizon;  // (face, edge) on the visible side
+  std::vector<std::pair<int, int>> horizon, loop;  // (face, edge) on the visible side
+  std::vector<char> used;
   int iter = 0;
   for (size_t cur = 0; cur < F.size(); ++cur) {
-    if (!F[cur].alive || F[cur].outside.empty()) continue;
+    if (!F[cur].alive || F[cur].nout == 0) continue;
     if (++iter > 4 * n + 64) break;
     // Farthest outside point of this face.
     int apex = -1;
     double bd = -1;
-    for (int p : F[cur].outside) {
+    for (int k = 0; k < F[cur].nout; ++k) {
+      const int p = H.pool[F[cur].out + k];
       double d = H.dist((int)cur, p);
       if (d > bd) {
         bd = d;
@@ -185,10 +218,9 @@ Mesh convex_hull(const std::vector<Vec3>& pts, bool fix_normals) {
       }
     }
     // Order the horizon as a loop: edge (u, w) of face f seen from outside.
-    std::vector<std::pair<int, int>> loop;
-    loop.reserve(horizon.size());
+    loop.clear();
     {
-      std::vector<char> used(horizon.size(), 0);
+      used.assign(horizon.size(), 0);
       loop.push_back(horizon[0]);
       used[0] = 1;
       for (size_t k = 1; k < horizon.size(); ++k) {
@@ -206,21 +238,23 @@ Mesh convex_hull(const std::vector<Vec3>& pts, bool fix_normals) {
         if (!found) break;
       }
       if (loop.size() != horizon.size()) {  // numerically inconsistent horizon
-        F[cur].outside.clear();
+        F[cur].nout = 0;
         continue;
       }
     }
     // Collect orphaned outside points.
-    std::vector<int> orphans;
+    orphans.clear();
     for (int f : visible) {
       F[f].alive = false;
-      for (int p : F[f].outside)
+      for (int k = 0; k < F[f].nout; ++k) {
+        const int p = H.pool[F[f].out + k];
         if (p != apex) orphans.push_back(p);
-      F[f].outside.clear();
-      F[f].outside.shrink_to_fit();
+      }
+      F[f].nout = 0;
     }
     // New faces (u, w, apex) for each horizon edge.
-    std::vector<int> nf(loop.size());
+    nf.resize(loop.size());
+    const int first = (int)F.size();
     for (size_t k = 0; k < loop.size(); ++k) {
       int f = loop[k].first, e = loop[k].second;
       int u = F[f].v[e], w = F[f].v[(e + 1) % 3];
@@ -235,18 +269,7 @@ Mesh convex_hull(const std::vector<Vec3>& pts, bool fix_normals) {
       F[a].nb[1] = b;  // edge (w, apex) shared with the next face's (apex, u')
       F[b].nb[2] = a;
     }
-    for (int p : orphans) {
-      int bf = -1;
-      double bdist = eps;
-      for (int f : nf) {
-        double d = H.dist(f, p);
-        if (d > bdist) {
-          bdist = d;
-          bf = f;
-        }
-      }
-      if (bf >= 0) F[bf].outside.push_back(p);
-    }
+    H.assign(orphans.data(), (int)orphans.size(), first, (int)loop.size(), choice);
   }
   for (const auto& f : F)
     if (f.alive) out.triangles.push_back({f.v[0], f.v[1], f.v[2]});
